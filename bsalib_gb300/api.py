@@ -1,0 +1,237 @@
+"""Python binding of libbsagpu (ctypes over include/bsa_gpu.h).
+
+`BsaSession` mirrors the standalone driver's use of BsaLib (app/bsa.F90:107-117 and its
+`setup`, :525-606): it calls bsa_Init, the setters with the Problem's arrays (which the
+library borrows -- the session keeps them alive), bsa_setTotDamping and bsa_Run.
+
+The library is the only compute path: there is no CPU fallback.  If libbsagpu.so is
+missing, `load()` raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import re
+from typing import Dict, Optional
+
+import numpy as np
+
+from .problem import Problem
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libbsagpu.so")
+HEADER = os.path.join(HERE, "..", "include", "bsa_gpu.h")
+
+BSA_OK = 0
+PREC_FP64 = 0
+PREC_BF16X3 = 1
+
+_lib = None
+
+
+class BsaError(RuntimeError):
+    pass
+
+
+class Stats(C.Structure):
+    _fields_ = [("ms_total", C.c_double), ("ms_contraction", C.c_double), ("points", C.c_double),
+                ("kernels", C.c_int), ("precision", C.c_int)]
+
+
+def header_symbols():
+    """Every function name declared in include/bsa_gpu.h."""
+    with open(HEADER) as fh:
+        txt = fh.read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b((?:bsa|bsacl)\w*)\s*\(", txt)))
+
+
+def load(path: Optional[str] = None):
+    """Load libbsagpu.so (build it first with `python -m bsalib_gb300.build`)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise BsaError(f"{p} is missing: build it with `python -m bsalib_gb300.build`")
+    lib = C.CDLL(p)
+    vp, i, d = C.c_void_p, C.c_int, C.c_double
+    sig = {
+        "bsa_Init": [], "bsa_Finalise": [], "bsa_lastError": None,
+        "bsa_setAnalysisType": [i], "bsa_setVersion": [i], "bsa_setScalingConv": [i],
+        "bsa_setSpectraComputation": [i, i], "bsa_setSpectraExtension": [i], "bsa_setSpatialSymmetry": [i],
+        "bsa_setSpectraSymmetries": [i], "bsa_setTestMode": [i], "bsa_setupClassic": [i, d],
+        "bsa_setClassicMode": [i], "bsa_setupMesher": [i, i, d, d, d, i, i],
+        "bsa_setWindDirections": [vp, i], "bsa_setWindTurbComps": [vp, i], "bsa_setTotalNOfNodes": [i],
+        "bsa_setNumOfNodalDOFs": [i], "bsa_setTotalNumOfDOFs": [i], "bsa_setLoadedNodes": [vp, i],
+        "bsa_setLoadedNodalDOFs": [vp, i], "bsa_setNodalCoords": [i, vp], "bsa_setModalInfo": [i, i, vp, vp],
+        "bsa_setModalMatrices": [i, vp, vp, vp], "bsa_setTotDamping": [vp, i], "bsa_setPSDType": [i],
+        "bsa_setWindVertProf": [i], "bsa_setWindAltDir": [i], "bsa_setAirDensity": [d],
+        "bsa_setWZMeanWindVel": [vp, i], "bsa_setWZRefAlt": [vp, i], "bsa_setTurbWindScales": [vp, i],
+        "bsa_setTurbWindSDT": [vp, i], "bsa_setNodalVel": [vp, i], "bsa_setNodalWindZones": [vp, i],
+        "bsa_setNodalWindAltitudes": [vp, i], "bsa_setSpatialNodalCorr": [vp, C.c_int64],
+        "bsa_setWindFCoeffs": [vp, i, i, i], "bsa_getNModesEff": [vp],
+        "bsa_Run": [vp] * 7, "bsa_computeSkewness": [i, vp, vp, vp],
+        "bsa_gpu_setPrecision": [i], "bsa_gpu_setClassicTruncation": [i],
+        "bsa_gpu_clsBispectra": [vp, i, vp, vp, vp], "bsa_gpu_mshBispectra": [vp, vp, i, vp, vp],
+        "bsa_gpu_mshMoments": [vp, vp, vp, i, vp, vp], "bsa_gpu_getStats": [vp],
+    }
+    for name, args in sig.items():
+        fn = getattr(lib, name)
+        if name == "bsa_lastError":
+            fn.restype = C.c_char_p
+            fn.argtypes = []
+        else:
+            fn.restype = C.c_int
+            fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def check(rc: int, what: str = ""):
+    if rc != BSA_OK:
+        msg = load().bsa_lastError().decode(errors="replace")
+        raise BsaError(f"{what} failed ({rc}): {msg}")
+
+
+class BsaSession:
+    """One BsaLib run over a Problem (borrowed arrays are kept alive here)."""
+
+    def __init__(self, prob: Problem, precision: int = PREC_FP64, classic_truncation: bool = True):
+        self.lib = load()
+        self.prob = prob
+        self._keep = {}
+        self.precision = precision
+        self.classic_truncation = classic_truncation
+        self._setup()
+
+    def _arr(self, name, a, dt):
+        a = np.asfortranarray(np.asarray(a, dtype=dt))
+        self._keep[name] = a
+        return _p(a)
+
+    def _setup(self):
+        L, p, s = self.lib, self.prob, self.prob.settings
+        check(L.bsa_Init(), "bsa_Init")
+        # settings (app/bsa.F90:560-575)
+        if s.suban:
+            check(L.bsa_setAnalysisType(s.suban), "bsa_setAnalysisType")
+        if s.vers:
+            check(L.bsa_setVersion(s.vers), "bsa_setVersion")
+        if s.defsc:
+            check(L.bsa_setScalingConv(s.defsc), "bsa_setScalingConv")
+        check(L.bsa_setSpectraComputation(s.ipsd, s.ibisp), "bsa_setSpectraComputation")
+        check(L.bsa_setSpectraExtension(s.onlyd), "bsa_setSpectraExtension")
+        check(L.bsa_setSpatialSymmetry(s.bispsym), "bsa_setSpatialSymmetry")
+        check(L.bsa_setSpectraSymmetries(s.sym3d), "bsa_setSpectraSymmetries")
+        check(L.bsa_setTestMode(s.test), "bsa_setTestMode")
+        check(L.bsa_setupClassic(s.nfreqs, float(s.df)), "bsa_setupClassic")
+        check(L.bsa_setClassicMode(s.scalar), "bsa_setClassicMode")
+        check(L.bsa_setupMesher(s.svd, s.bkgrfmt, s.bkgaext, s.genpaext, s.maxaext, s.fcov, s.dumpmod),
+              "bsa_setupMesher")
+        check(L.bsa_setWindDirections(self._arr("dirs", s.dirs, np.int32), len(s.dirs)), "dirs")
+        check(L.bsa_setWindTurbComps(self._arr("tc", s.tc, np.int32), len(s.tc)), "tc")
+        # nodal
+        check(L.bsa_setTotalNOfNodes(p.nn), "nn")
+        check(L.bsa_setNumOfNodalDOFs(p.nlibs), "nlibs")
+        check(L.bsa_setLoadedNodes(self._arr("nl", p.n_load, np.int32), p.nnl), "loaded nodes")
+        check(L.bsa_setLoadedNodalDOFs(self._arr("ll", p.libs_load, np.int32), p.nlibsl), "loaded DOFs")
+        check(L.bsa_setNodalCoords(p.nn, self._arr("coords", p.coords, np.float64)), "coords")
+        # wind
+        check(L.bsa_setWindVertProf(p.i_varu), "wind profile")
+        check(L.bsa_setPSDType(p.psd_type), "psd type")
+        check(L.bsa_setWindAltDir(p.i_vert), "vert dir")
+        check(L.bsa_setAirDensity(p.air_dens), "air density")
+        check(L.bsa_setWZMeanWindVel(self._arr("ubref", p.UBref, np.float64), p.nz), "UBref")
+        check(L.bsa_setWZRefAlt(self._arr("zref", p.Zref, np.float64), p.nz), "Zref")
+        check(L.bsa_setTurbWindScales(self._arr("L", p.L, np.float64), p.nz), "L")
+        check(L.bsa_setTurbWindSDT(self._arr("sigma", p.sigma, np.float64), p.nz), "sigma")
+        check(L.bsa_setNodalVel(self._arr("unod", p.u_node, np.float64), p.nn), "u_node")
+        check(L.bsa_setNodalWindZones(self._arr("wz", p.wz_node, np.int32), p.nn), "wz")
+        check(L.bsa_setNodalWindAltitudes(self._arr("walt", p.wAlt_node, np.float64), p.nn), "walt")
+        check(L.bsa_setSpatialNodalCorr(self._arr("corr", p.nod_corr, np.float64), p.nod_corr.shape[0]), "corr")
+        w = p.wfc
+        check(L.bsa_setWindFCoeffs(self._arr("wfc", w, np.float64), w.shape[0], w.shape[1], w.shape[2]), "wfc")
+        # modal
+        check(L.bsa_setModalInfo(p.ndofs, p.nm, self._arr("phi", p.phi, np.float64),
+                                 self._arr("natf", p.natf, np.float64)), "modal info")
+        check(L.bsa_setModalMatrices(p.nm, self._arr("Mg", p.Mg, np.float64), self._arr("Kg", p.Kg, np.float64),
+                                     self._arr("Cg", p.Cg, np.float64)), "modal matrices")
+        check(L.bsa_setTotDamping(self._arr("xsi", p.xsi, np.float64), p.nm), "damping")
+        check(L.bsa_gpu_setPrecision(self.precision), "precision")
+        check(L.bsa_gpu_setClassicTruncation(1 if self.classic_truncation else 0), "truncation")
+
+    def set_precision(self, prec: int):
+        self.precision = prec
+        check(self.lib.bsa_gpu_setPrecision(prec), "bsa_gpu_setPrecision")
+
+    def nmodes(self) -> int:
+        n = np.zeros(1, dtype=np.int32)
+        check(self.lib.bsa_getNModesEff(_p(n)), "bsa_getNModesEff")
+        return int(n[0])
+
+    def run(self) -> Dict[str, np.ndarray]:
+        """bsa_Run: returns m2mf_cls, m2mr_cls, m2o2mr_cls, m3mf_msh, m3mr_msh, m3mf_cls, m3mr_cls."""
+        nm = self.nmodes()
+        out = {k: np.zeros(nm * nm) for k in ("m2mf_cls", "m2mr_cls", "m2o2mr_cls")}
+        out.update({k: np.zeros(nm ** 3) for k in ("m3mf_msh", "m3mr_msh", "m3mf_cls", "m3mr_cls")})
+        check(self.lib.bsa_Run(_p(out["m2mf_cls"]), _p(out["m2mr_cls"]), _p(out["m2o2mr_cls"]),
+                               _p(out["m3mf_msh"]), _p(out["m3mr_msh"]), _p(out["m3mf_cls"]),
+                               _p(out["m3mr_cls"])), "bsa_Run")
+        return out
+
+    def classic_bispectra(self):
+        """Materialised force / response bispectra on the classic grid (f1 fastest)."""
+        nm = self.nmodes()
+        nf_cap = self.prob.classic_nf() + 8
+        nf = np.zeros(1, dtype=np.int32)
+        f = np.zeros(nf_cap)
+        # query the size first
+        s = self.prob.settings
+        nfx = self.prob.classic_nf() if s.test else nf_cap * 4
+        bf = np.zeros(nfx * nfx * nm ** 3)
+        br = np.zeros(nfx * nfx * nm ** 3)
+        check(self.lib.bsa_gpu_clsBispectra(_p(f), nf_cap, _p(nf), _p(bf), _p(br)), "bsa_gpu_clsBispectra")
+        n = int(nf[0])
+        # library layout: (nm^3, nf*nf) column-major, point p = i1 + nf*i2
+        bf = bf[: n * n * nm ** 3].reshape(n, n, nm ** 3).transpose(1, 0, 2)
+        br = br[: n * n * nm ** 3].reshape(n, n, nm ** 3).transpose(1, 0, 2)
+        return f[:n].copy(), bf, br
+
+    def msh_bispectra(self, fi, fj):
+        fi = np.ascontiguousarray(fi, dtype=np.float64)
+        fj = np.ascontiguousarray(fj, dtype=np.float64)
+        nm = self.nmodes()
+        bfm = np.zeros((fi.size, nm ** 3))
+        brm = np.zeros((fi.size, nm ** 3))
+        check(self.lib.bsa_gpu_mshBispectra(_p(fi), _p(fj), fi.size, _p(bfm), _p(brm)), "bsa_gpu_mshBispectra")
+        return bfm, brm
+
+    def msh_moments(self, fi, fj, w):
+        fi = np.ascontiguousarray(fi, dtype=np.float64)
+        fj = np.ascontiguousarray(fj, dtype=np.float64)
+        w = np.ascontiguousarray(w, dtype=np.float64)
+        nm = self.nmodes()
+        mf, mr = np.zeros(nm ** 3), np.zeros(nm ** 3)
+        check(self.lib.bsa_gpu_mshMoments(_p(fi), _p(fj), _p(w), fi.size, _p(mf), _p(mr)), "bsa_gpu_mshMoments")
+        return mf, mr
+
+    def stats(self) -> Stats:
+        st = Stats()
+        check(self.lib.bsa_gpu_getStats(C.byref(st)), "bsa_gpu_getStats")
+        return st
+
+    def skewness(self, m2, m3):
+        nm = self.nmodes()
+        sk = np.zeros(nm ** 3)
+        check(self.lib.bsa_computeSkewness(nm, _p(np.ascontiguousarray(m2)), _p(np.ascontiguousarray(m3)),
+                                           _p(sk)), "bsa_computeSkewness")
+        return sk
+
+    def close(self):
+        self.lib.bsa_Finalise()
+        self._keep.clear()

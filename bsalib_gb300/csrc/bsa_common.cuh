@@ -1,0 +1,71 @@
+// bsa_common.cuh -- device-side data layout shared by the BFM kernels of libbsagpu.
+//
+// Layout in HBM (all FP64 unless stated):
+//   k index           k = itc * nnl + i   (turbulent component major, loaded node minor)
+//   L[k][m], Q[k][m]  modal projections of the linear / quadratic force coefficients,
+//                     L = PHItimesC(:, :, tc), Q = PHItimesC(:, :, tc+3)
+//                     (setPhitimesCLocalInstance_, src/bsa/BsaLibImpl.F90:611-671)
+//   logc[itc][i][j]   log of the nodal coherence base c_ij for component tc
+//   S[f][itc][i]      nodal turbulence PSD (evalPSD_, src/wind/WindPSDImpl.F90:123-144)
+//   A[f][k][m]        A(f) = S(f) L with S_ij(f) = c_ij^|f| sqrt(S_i S_j): the per-frequency
+//                     factor of the BFM contraction (every term of functionsImpl.F90:1494-1538
+//                     is a product of two such factors and one row of Q)
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace bsa {
+
+constexpr double kPi = 3.14159265358979323846264338327950288;
+constexpr double kPi2 = 2.0 * kPi;
+constexpr double kPi4 = 4.0 * kPi;
+
+// Per (component, loaded node) parameters of the nodal PSD models.
+struct PsdNode {
+    double U;      // nodal mean wind speed u_node(n)
+    double sigma;  // sigmaUVW_wz_(tc, wz)
+    double Ls;     // turbulence length scale used by the model
+    double Uref;   // u_mean_ref_wz_(wz) (Davenport-Greisch)
+};
+
+// How the contraction kernel enumerates its (f1, f2) points.
+enum PointMode : int {
+    kPointsGrid = 0,   // classic grid: p -> (i1 = p % nf, i2 = p / nf)
+    kPointsList = 1,   // explicit lists of A-table rows and weights
+};
+
+enum WeightMode : int {
+    kWeightClassicVect = 0,  // intgSpectraVect_ edge weights (BsaClassicImpl.F90:596-632)
+    kWeightUniform = 1,      // one weight for every point (scalar classic, BsaCL)
+    kWeightList = 2,         // per point
+};
+
+struct PointSrc {
+    int mode;
+    int nf;                 // grid size (kPointsGrid)
+    int n_pad;              // (nf - 1) / 2, centre offset of the padded S(f1+f2) copy
+    int trunc;              // 1: S(f1+f2) beyond the grid reads zero
+    int sum_base;           // A-table row of the analytic sum table (s = i1 + i2)
+    int wmode;
+    double wval;            // uniform weight, or d^2 for the classic edge weights
+    const double *fgrid;    // grid frequencies (kPointsGrid)
+    const int *ix, *iy, *iz; // A rows of f1, f2, f1+f2 (kPointsList; iz < 0: zero)
+    const double *w;        // weights (kWeightList)
+    const double *f1, *f2;  // point frequencies (kPointsList)
+};
+
+struct FrfPar {
+    const double *M, *K, *C;  // kept modes: generalised mass, stiffness, damping C(m,m)
+};
+
+__host__ __device__ inline void frf_eval(double M, double K, double C, double w, double &hr,
+                                         double &hi) {
+    // H(w) = 1 / (K - w^2 M + i w C)  (functionsImpl.F90:1031-1115)
+    const double r = -(w * w * M) + K;
+    const double ip = C * w;
+    const double h = r * r + ip * ip;
+    hr = r / h;
+    hi = -ip / h;
+}
+
+}  // namespace bsa

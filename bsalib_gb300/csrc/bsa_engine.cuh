@@ -1,0 +1,104 @@
+// bsa_engine.cuh -- the library's single state object (BsaLib keeps the same state in
+// module globals: settings, wd, struct_data; src/bsa/data/BsaLibData.F90).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "bsa_common.cuh"
+
+namespace bsa {
+
+// Device buffer that only grows (kept across runs; freed by bsa_Finalise).
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+    cudaError_t reserve(size_t nbytes);
+    void release();
+    template <class T>
+    T *as() const { return (T *)p; }
+};
+
+// Borrowed caller arrays (Fortran layouts), as the reference keeps pointers to them.
+struct Inputs {
+    int nn = 0, nlibs = 0, ndofs = 0, phi_ndofs = 0, nnl = 0, nlibsl = 0;
+    const int *n_load = nullptr, *libs_load = nullptr;
+    const double *coords = nullptr;
+    int nm = 0;
+    const double *phi = nullptr, *natf = nullptr, *Mg = nullptr, *Kg = nullptr, *Cg = nullptr, *xsi = nullptr;
+    int psd_type = 5;  // WindData_t default i_psd_type_ (src/wind/WindType.F90:76)
+    int nz = 0;
+    const double *ubref = nullptr, *zref = nullptr, *L = nullptr, *sigma = nullptr;
+    const double *unod = nullptr, *walt = nullptr;
+    const int *wz = nullptr;
+    const double *corr = nullptr;
+    long long ncorr = 0;
+    const double *wfc = nullptr;
+    int wfc_nl = 0, wfc_nd = 0, wfc_nn = 0;
+    int wprof = 2, vert = 3;
+    double air_dens = 1.22;
+    // Projected coefficients supplied directly (BsaCL's bsaclAcquirePhiTimesCMat): then the
+    // mode list and PHItimesC are taken as given instead of derived from Phi and wfc.
+    const double *ext_phitc = nullptr;
+    const int *ext_modes = nullptr;
+    int ext_nme = 0, ext_nnl = 0, ext_nd = 0;
+};
+
+// settings_t defaults (src/settings/Settings.F90:25-116).
+struct Settings {
+    int suban = 2, vers = 2, defsc = 1, ipsd = 1, ibisp = 1, onlyd = 0, bispsym = 0, spctrsym = 0, test = 0;
+    int nfreqs = 0, scalar = 0;
+    double df = 0.0;
+    int svd = 1, bkgrfmt = 20, fcov = 1, dumpmod = 0;
+    double bkgaext = 2.0, genpaext = 2.0, maxaext = 2.0;
+    std::vector<int> dirs{1};
+    std::vector<int> tc{1};
+};
+
+struct Engine {
+    Inputs in;
+    Settings set;
+    bool inited = false, halted = false, derived_ok = false, dev_uploaded = false;
+    std::string last_error;
+    int precision = 0;          // BSA_PREC_FP64
+    bool classic_trunc = true;  // S(f1+f2) beyond the classic grid reads zero
+
+    // derived (validate)
+    std::vector<int> modes;
+    int nme = 0, K = 0;
+    std::vector<double> phitc, hL, hQ, hLogc, hM, hK, hC;
+    std::vector<PsdNode> hPsd;
+
+    // device
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr;
+    DevBuf dL, dQ, dLogc, dPsdPar, dFrfM, dFrfK, dFrfC, dFreq, dS, dA, dPartF, dPartR, dOut, dPsdF, dWf, dPts,
+        dPtsD, dBF, dBR, dMixA, dMixB, dMixH, dMixPart;
+
+    // stats
+    double last_ms = 0, last_ms_contraction = 0, last_points = 0;
+    int kernels = 0;
+
+    int fail(int code, const char *fmt, ...);
+    int cuda_fail(cudaError_t e, const char *what);
+    void reset_inputs();
+    void free_device();
+    int ensure_stream();
+    int validate();
+    int upload_problem();
+    FrfPar frf() const;
+    int build_atable(const std::vector<double> &freqs);
+    int classic_grid(std::vector<double> &f);
+    int run_classic(double *m2mf, double *m2mr, double *m2o2mr, double *m3mf, double *m3mr, double *bf_host,
+                    double *br_host, std::vector<double> *grid_out);
+    int contract(const PointSrc &ps, long long npts, double *m3mf, double *m3mr, double *bf_host, double *br_host);
+    int contract_mixed(const PointSrc &ps, long long npts, double *m3mf, double *m3mr);
+    int run_points(const double *fi, const double *fj, const double *w, double wuniform, long long npts,
+                   double *m3mf, double *m3mr, double *bfm, double *brm);
+    int run_mesher(double *m3mf, double *m3mr);
+};
+
+Engine &eng();
+
+}  // namespace bsa

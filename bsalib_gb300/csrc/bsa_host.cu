@@ -1,0 +1,766 @@
+// bsa_host.cu -- host side of libbsagpu: the BsaLib API state (borrowed inputs, settings),
+// validation and projection, the Classic / point-set drivers, and the BsaCL-compatible
+// entry points.  All exported symbols are declared in include/bsa_gpu.h.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/bsa_gpu.h"
+#include "bsa_common.cuh"
+#include "bsa_engine.cuh"
+#include "bsa_kernels.cuh"
+
+namespace bsa {
+
+Engine &eng() {
+    static Engine e;
+    return e;
+}
+
+int Engine::fail(int code, const char *fmt, ...) {
+    if (!halted) {
+        char buf[512];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, sizeof buf, fmt, ap);
+        va_end(ap);
+        last_error = buf;
+        halted = true;
+    }
+    return code;
+}
+
+int Engine::cuda_fail(cudaError_t e, const char *what) {
+    return fail(e == cudaErrorMemoryAllocation ? BSA_ERR_NOMEM : BSA_ERR_CUDA, "%s: %s", what,
+                cudaGetErrorString(e));
+}
+
+void DevBuf::release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+}
+
+cudaError_t DevBuf::reserve(size_t nbytes) {
+    if (nbytes <= bytes && p) return cudaSuccess;
+    release();
+    if (nbytes == 0) return cudaSuccess;
+    cudaError_t e = cudaMalloc(&p, nbytes);
+    if (e == cudaSuccess) bytes = nbytes;
+    else p = nullptr;
+    return e;
+}
+
+void Engine::reset_inputs() {
+    in = Inputs();
+    set = Settings();
+    derived_ok = false;
+}
+
+void Engine::free_device() {
+    for (DevBuf *b : {&dL, &dQ, &dLogc, &dPsdPar, &dFrfM, &dFrfK, &dFrfC, &dFreq, &dS, &dA, &dPartF, &dPartR,
+                      &dOut, &dPsdF, &dWf, &dPts, &dPtsD, &dBF, &dBR, &dMixA, &dMixB, &dMixH, &dMixPart})
+        b->release();
+    if (stream) cudaStreamDestroy(stream);
+    stream = nullptr;
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+    if (ev2) cudaEventDestroy(ev2);
+    ev0 = ev1 = ev2 = nullptr;
+    dev_uploaded = false;
+}
+
+int Engine::ensure_stream() {
+    if (stream) return BSA_OK;
+    cudaError_t e = cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamCreate");
+    if ((e = cudaEventCreate(&ev0)) != cudaSuccess) return cuda_fail(e, "cudaEventCreate");
+    if ((e = cudaEventCreate(&ev1)) != cudaSuccess) return cuda_fail(e, "cudaEventCreate");
+    if ((e = cudaEventCreate(&ev2)) != cudaSuccess) return cuda_fail(e, "cudaEventCreate");
+    return BSA_OK;
+}
+
+static long corr_index(int ni, int nj, int tot) {
+    // util_getCorrVectIndex, src/utils/utility.F90:60-71 (1-based)
+    if (nj >= ni) return (long)(ni - 1) * tot + nj - ((long)ni * ni - ni) / 2;
+    return (long)(nj - 1) * tot + ni - ((long)nj * nj - nj) / 2;
+}
+
+// validateAll_ (src/bsa/BsaLibImpl.F90:469-535) restricted to what the BFM path reads:
+// sizes, mode validation (validateModalInfo_, :545-599), the projection PHItimesC
+// (setPhitimesCLocalInstance_, :611-671) and the device-side parameter tables.
+int Engine::validate() {
+    if (halted) return BSA_ERR_STATE;
+    if (derived_ok) return BSA_OK;
+    const Inputs &I = in;
+    const bool ext = I.ext_phitc != nullptr;
+    if (I.nn <= 0) return fail(BSA_ERR_STATE, "total number of nodes not set");
+    if (!I.n_load || I.nnl <= 0) return fail(BSA_ERR_STATE, "loaded nodes not set");
+    if (!I.Mg || !I.Kg || !I.Cg) return fail(BSA_ERR_STATE, "modal matrices not set");
+    if (!I.corr) return fail(BSA_ERR_STATE, "nodal coherence not set");
+    if (!I.unod || !I.wz || !I.sigma || !I.L) return fail(BSA_ERR_STATE, "wind field data not set");
+    if (I.psd_type == 3 && !I.ubref) return fail(BSA_ERR_STATE, "zone mean wind speeds not set");
+    if (I.ncorr != ((long)I.nn * I.nn + I.nn) / 2)
+        return fail(BSA_ERR_ARG, "nodal coherence has %lld rows, expected (nn^2+nn)/2", (long long)I.ncorr);
+    if (set.onlyd != 0) return fail(BSA_ERR_UNSUPPORTED, "diagonal-only spectra are not on this path");
+    if (set.tc.empty() || set.tc.size() > 3) return fail(BSA_ERR_ARG, "1 to 3 turbulent components");
+    for (int tc : set.tc)
+        if (tc < 1 || tc > 3) return fail(BSA_ERR_ARG, "turbulent component id out of range");
+    if (!(I.psd_type == 1 || I.psd_type == 2 || I.psd_type == 3 || I.psd_type == 5))
+        return fail(BSA_ERR_UNSUPPORTED, "PSD type %d has no model function", I.psd_type);
+    for (int i = 0; i < I.nnl; ++i)
+        if (I.n_load[i] < 1 || I.n_load[i] > I.nn) return fail(BSA_ERR_ARG, "loaded node id out of range");
+    const int tcmax = *std::max_element(set.tc.begin(), set.tc.end());
+    const int nnl = I.nnl;
+    int nd = 0;
+    if (ext) {
+        if (I.ext_nnl != nnl) return fail(BSA_ERR_ARG, "N. of loaded nodes does not match");
+        if (I.ext_nd < 3 + tcmax) return fail(BSA_ERR_ARG, "projected coefficients have too few columns");
+        if (!I.ext_modes || I.ext_nme <= 0) return fail(BSA_ERR_STATE, "kept-mode list not set");
+        modes.assign(I.ext_modes, I.ext_modes + I.ext_nme);
+        for (int m : modes)
+            if (m < 1 || m > I.nm) return fail(BSA_ERR_ARG, "kept mode id out of range");
+        nme = I.ext_nme;
+        nd = I.ext_nd;
+        phitc.assign(I.ext_phitc, I.ext_phitc + (size_t)nme * nnl * nd);
+    } else {
+        if (I.nlibs <= 0) return fail(BSA_ERR_STATE, "number of nodal DOFs not set");
+        if (!I.libs_load || I.nlibsl <= 0) return fail(BSA_ERR_STATE, "loaded nodal DOFs not set");
+        if (!I.phi || I.nm <= 0) return fail(BSA_ERR_STATE, "modal matrix not set");
+        if (!I.wfc) return fail(BSA_ERR_STATE, "wind force coefficients were not acquired");
+        const int ndofs = I.ndofs ? I.ndofs : I.nn * I.nlibs;
+        if (I.phi_ndofs != ndofs) return fail(BSA_ERR_ARG, "NDOFs does not match modal matrix size");
+        if (ndofs != I.nn * I.nlibs) return fail(BSA_ERR_ARG, "incorrect value for ndofs");
+        if (I.wfc_nn != I.nnl) return fail(BSA_ERR_ARG, "N. of loaded nodes does not match");
+        if (I.wfc_nl != I.nlibsl) return fail(BSA_ERR_ARG, "N. of loaded libs does not match");
+        if (I.wfc_nd < 3 + tcmax) return fail(BSA_ERR_ARG, "wind force coefficients have too few columns");
+        for (int l = 0; l < I.nlibsl; ++l)
+            if (I.libs_load[l] < 1 || I.libs_load[l] > I.nlibs) return fail(BSA_ERR_ARG, "loaded DOF id out of range");
+        // validateModalInfo_: keep modes with max|Phi| == 1 exactly.
+        modes.clear();
+        for (int m = 0; m < I.nm; ++m) {
+            double mx = 0.0;
+            for (int d = 0; d < ndofs; ++d) mx = std::max(mx, std::fabs(I.phi[(size_t)d + (size_t)ndofs * m]));
+            if (mx == 1.0) modes.push_back(m + 1);
+        }
+        nme = (int)modes.size();
+        if (nme == 0) return fail(BSA_ERR_ARG, "effective number of modes to be kept is 0");
+        if (nme > 64) return fail(BSA_ERR_UNSUPPORTED, "more than 64 kept modes");
+        // PHItimesC(im, in, id) = sum_l wfc(l, id, in) Phi((n-1)*nlibs + libs_load(l), modes(im))
+        nd = I.wfc_nd;
+        const int nl = I.nlibsl;
+        phitc.assign((size_t)nme * nnl * nd, 0.0);
+        for (int i = 0; i < nnl; ++i) {
+            const int skip = (I.n_load[i] - 1) * I.nlibs;
+            for (int id = 0; id < nd; ++id)
+                for (int im = 0; im < nme; ++im) {
+                    double s = 0.0;
+                    for (int l = 0; l < nl; ++l)
+                        s += I.wfc[(size_t)l + (size_t)nl * ((size_t)id + (size_t)nd * i)] *
+                             I.phi[(size_t)(skip + I.libs_load[l] - 1) + (size_t)ndofs * (modes[im] - 1)];
+                    phitc[(size_t)im + (size_t)nme * ((size_t)i + (size_t)nnl * id)] += s;
+                }
+        }
+    }
+    if (nme > 64) return fail(BSA_ERR_UNSUPPORTED, "more than 64 kept modes");
+    // Device layouts: k = itc * nnl + i.
+    const int ntc = (int)set.tc.size();
+    K = ntc * nnl;
+    hL.assign((size_t)K * nme, 0.0);
+    hQ.assign((size_t)K * nme, 0.0);
+    for (int itc = 0; itc < ntc; ++itc) {
+        const int tc = set.tc[itc];
+        for (int i = 0; i < nnl; ++i)
+            for (int m = 0; m < nme; ++m) {
+                hL[((size_t)itc * nnl + i) * nme + m] = phitc[(size_t)m + (size_t)nme * ((size_t)i + (size_t)nnl * (tc - 1))];
+                hQ[((size_t)itc * nnl + i) * nme + m] = phitc[(size_t)m + (size_t)nme * ((size_t)i + (size_t)nnl * (tc + 2))];
+            }
+    }
+    const long ncorr = (long)I.ncorr;
+    hLogc.assign((size_t)ntc * nnl * nnl, 0.0);
+    for (int itc = 0; itc < ntc; ++itc)
+        for (int i = 0; i < nnl; ++i)
+            for (int j = 0; j < nnl; ++j) {
+                const long id = corr_index(I.n_load[i], I.n_load[j], I.nn);
+                const double c = I.corr[(size_t)(id - 1) + (size_t)ncorr * (set.tc[itc] - 1)];
+                hLogc[((size_t)itc * nnl + i) * nnl + j] = std::log(c);
+            }
+    const int idir = set.dirs.empty() ? 1 : set.dirs[0];
+    hPsd.assign((size_t)ntc * nnl, PsdNode{});
+    for (int itc = 0; itc < ntc; ++itc) {
+        const int tc = set.tc[itc];
+        for (int i = 0; i < nnl; ++i) {
+            const int n = I.n_load[i];
+            const int wz = I.wz[n - 1];
+            if (wz < 1 || wz > I.nz) return fail(BSA_ERR_ARG, "wind zone of node %d out of range", n);
+            PsdNode p;
+            p.U = I.unod[n - 1];
+            p.sigma = I.sigma[(size_t)(tc - 1) + 3 * (size_t)(wz - 1)];
+            const int lrow = (I.psd_type == 1 && tc == 1) ? 1 : tc;  // vonKarmanPSD_ u form reads L(1, idir, wz)
+            p.Ls = I.L[(size_t)(lrow - 1) + 3 * ((size_t)(idir - 1) + 3 * (size_t)(wz - 1))];
+            p.Uref = I.ubref ? I.ubref[wz - 1] : 0.0;
+            hPsd[(size_t)itc * nnl + i] = p;
+        }
+    }
+    hM.resize(nme); hK.resize(nme); hC.resize(nme);
+    for (int im = 0; im < nme; ++im) {
+        const int m = modes[im] - 1;
+        hM[im] = I.Mg[m];
+        hK[im] = I.Kg[m];
+        hC[im] = I.Cg[(size_t)m + (size_t)I.nm * m];
+    }
+    derived_ok = true;
+    dev_uploaded = false;
+    return BSA_OK;
+}
+
+template <class T>
+static cudaError_t upload(DevBuf &b, const std::vector<T> &v, cudaStream_t st) {
+    cudaError_t e = b.reserve(sizeof(T) * v.size());
+    if (e != cudaSuccess || v.empty()) return e;
+    return cudaMemcpyAsync(b.p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, st);
+}
+
+int Engine::upload_problem() {
+    int rc = validate();
+    if (rc) return rc;
+    if ((rc = ensure_stream())) return rc;
+    if (dev_uploaded) return BSA_OK;
+    cudaError_t e;
+    if ((e = upload(dL, hL, stream)) || (e = upload(dQ, hQ, stream)) || (e = upload(dLogc, hLogc, stream)) ||
+        (e = upload(dPsdPar, hPsd, stream)) || (e = upload(dFrfM, hM, stream)) || (e = upload(dFrfK, hK, stream)) ||
+        (e = upload(dFrfC, hC, stream)))
+        return cuda_fail(e, "uploading problem data");
+    dev_uploaded = true;
+    return BSA_OK;
+}
+
+FrfPar Engine::frf() const { return FrfPar{dFrfM.as<double>(), dFrfK.as<double>(), dFrfC.as<double>()}; }
+
+// Nodal PSD + A(f) for a host list of frequencies, into dA rows [row0, row0 + nf).
+int Engine::build_atable(const std::vector<double> &freqs) {
+    const int nf = (int)freqs.size();
+    const int ntc = (int)set.tc.size();
+    cudaError_t e;
+    if ((e = upload(dFreq, freqs, stream))) return cuda_fail(e, "uploading frequencies");
+    if ((e = dS.reserve(sizeof(double) * (size_t)nf * ntc * in.nnl))) return cuda_fail(e, "allocating S");
+    if ((e = dA.reserve(sizeof(double) * (size_t)nf * K * nme))) return cuda_fail(e, "allocating A");
+    if ((e = launch_nodal_psd(stream, nf, dFreq.as<double>(), ntc, set.tc.data(), in.nnl, dPsdPar.as<PsdNode>(),
+                              in.psd_type, set.defsc, dS.as<double>())))
+        return cuda_fail(e, "nodal PSD kernel");
+    if ((e = launch_atable(stream, nf, dFreq.as<double>(), ntc, in.nnl, nme, dLogc.as<double>(), dS.as<double>(),
+                           dL.as<double>(), dA.as<double>())))
+        return cuda_fail(e, "A-table kernel");
+    kernels += 2;
+    return BSA_OK;
+}
+
+// computeFreqsVect_ (BsaClassicImpl.F90:443-560).
+int Engine::classic_grid(std::vector<double> &f) {
+    if (set.nfreqs == 0 || set.df == 0.0) return fail(BSA_ERR_ARG, "either NFREQs or DF are == 0");
+    if (!in.natf) return fail(BSA_ERR_STATE, "natural frequencies not set");
+    double df = set.df;
+    double df_ref = INFINITY, max_ref = -INFINITY;
+    for (int m = 0; m < in.nm; ++m) {
+        if (!in.xsi) return fail(BSA_ERR_STATE, "damping (bsa_setTotDamping) not set");
+        df_ref = std::min(df_ref, in.xsi[m] * in.natf[m]);
+        max_ref = std::max(max_ref, in.natf[m]);
+    }
+    df_ref /= 5.0;
+    const bool big = df > df_ref;
+    int nf1 = set.nfreqs - 1;
+    if (set.test == 0) {
+        double mxf = df * nf1;
+        if (mxf < max_ref) {
+            if (big) {
+                mxf = df_ref * nf1;
+                if (mxf < max_ref) nf1 = (int)std::ceil(max_ref / df_ref);
+                df = df_ref;
+            } else {
+                nf1 = (int)std::ceil(max_ref / df);
+            }
+        }
+    }
+    int nf, n0;
+    if (set.defsc == 1) {
+        nf = nf1 * 2 + 1;
+        n0 = -nf1;
+    } else {
+        if (nf1 % 2 != 0) nf1 += 1;
+        nf = nf1 + 1;
+        n0 = 0;
+    }
+    f.resize(nf);
+    for (int i = n0; i <= nf1; ++i) f[i - n0] = (double)i * df;
+    return BSA_OK;
+}
+
+// Classic analysis on the GPU (mainClassic_, BsaClassicImpl.F90:39-376): every grid point,
+// moments reduced in the kernel epilogue.  Optional materialised bispectra (nf, nf, nm^3).
+int Engine::run_classic(double *m2mf, double *m2mr, double *m2o2mr, double *m3mf, double *m3mr, double *bf_host,
+                        double *br_host, std::vector<double> *grid_out) {
+    int rc = upload_problem();
+    if (rc) return rc;
+    std::vector<double> f;
+    if ((rc = classic_grid(f))) return rc;
+    if (grid_out) *grid_out = f;
+    const int nf = (int)f.size();
+    if (nf < 2) return fail(BSA_ERR_ARG, "classic grid needs at least 2 frequencies");
+    // Vectorised / scalar branch (checkMaxAllocation_, BsaClassicImpl.F90:384-434): only the
+    // integration weights differ here, the spectra are never stored.
+    bool scalar = set.scalar != 0;
+    const long long nm3 = (long long)nme * nme * nme;
+    if (set.test == 0 && !scalar && set.ibisp && (long long)nf * nf * nm3 > 1000000000LL) scalar = true;
+    double delta = f[1] - f[0];
+    if (set.defsc == 1) delta *= kPi2;
+    const bool analytic = !classic_trunc;
+    std::vector<double> ftab = f;
+    if (analytic) {
+        // s-table: f1 + f2 = 2 f[0] + s df, s = i1 + i2.
+        const double d = f[1] - f[0];
+        for (int s = 0; s < 2 * nf - 1; ++s) ftab.push_back(2.0 * f[0] + s * d);
+    }
+    kernels = 0;
+    cudaError_t e;
+    if ((e = cudaEventRecord(ev0, stream))) return cuda_fail(e, "event");
+    if ((rc = build_atable(ftab))) return rc;
+    const int nm2 = nme * nme;
+    if (set.ipsd && (m2mf || m2mr || m2o2mr)) {
+        std::vector<double> wf(nf, scalar ? delta : delta);
+        if (!scalar) { wf[0] = delta / 2; wf[nf - 1] = delta / 2; }
+        if ((e = upload(dWf, wf, stream))) return cuda_fail(e, "weights");
+        if ((e = dPsdF.reserve(sizeof(double) * (size_t)nf * nm2))) return cuda_fail(e, "psd");
+        if ((e = dOut.reserve(sizeof(double) * (3 * (size_t)nm2 + 2 * (size_t)nm3))))
+            return cuda_fail(e, "out");
+        if ((e = launch_force_psd(stream, nf, (int)set.tc.size(), in.nnl, nme, dL.as<double>(), dA.as<double>(),
+                                  dPsdF.as<double>())))
+            return cuda_fail(e, "force PSD kernel");
+        double *o = dOut.as<double>();
+        if ((e = launch_m2(stream, nf, nme, dFreq.as<double>(), dWf.as<double>(), dPsdF.as<double>(), frf(), o,
+                           o + nm2, o + 2 * nm2)))
+            return cuda_fail(e, "m2 kernel");
+        kernels += 2;
+        std::vector<double> h(3 * (size_t)nm2);
+        if ((e = cudaMemcpyAsync(h.data(), o, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, stream)) ||
+            (e = cudaStreamSynchronize(stream)))
+            return cuda_fail(e, "m2 copy");
+        if (m2mf) std::memcpy(m2mf, h.data(), sizeof(double) * nm2);
+        if (m2mr) std::memcpy(m2mr, h.data() + nm2, sizeof(double) * nm2);
+        if (m2o2mr) std::memcpy(m2o2mr, h.data() + 2 * nm2, sizeof(double) * nm2);
+    }
+    last_points = 0;
+    if (set.ibisp && (m3mf || m3mr || bf_host || br_host)) {
+        PointSrc ps{};
+        ps.mode = kPointsGrid;
+        ps.nf = nf;
+        ps.n_pad = (nf - 1) / 2;
+        ps.trunc = analytic ? 0 : 1;
+        ps.sum_base = nf;
+        ps.wmode = scalar ? kWeightUniform : kWeightClassicVect;
+        ps.wval = delta * delta;
+        ps.fgrid = dFreq.as<double>();
+        const long long npts = (long long)nf * nf;
+        rc = contract(ps, npts, m3mf, m3mr, bf_host, br_host);
+        if (rc) return rc;
+        last_points = (double)npts;
+    }
+    if ((e = cudaEventRecord(ev1, stream)) || (e = cudaEventSynchronize(ev1))) return cuda_fail(e, "event");
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ev0, ev1);
+    last_ms = ms;
+    return BSA_OK;
+}
+
+// Contraction + FRF + reduction over a point source; dA must hold every row it names.
+int Engine::contract(const PointSrc &ps, long long npts, double *m3mf, double *m3mr, double *bf_host,
+                     double *br_host) {
+    const long long nm3 = (long long)nme * nme * nme;
+    cudaError_t e;
+    if (precision == BSA_PREC_BF16X3 && ps.mode == kPointsGrid && !bf_host && !br_host)
+        return contract_mixed(ps, npts, m3mf, m3mr);
+    const int G = bfm_fp64_groups(npts, nme);
+    if ((e = dPartF.reserve(sizeof(double) * (size_t)G * nm3)) || (e = dPartR.reserve(sizeof(double) * (size_t)G * nm3)))
+        return cuda_fail(e, "allocating partial sums");
+    if ((e = dOut.reserve(sizeof(double) * (3 * (size_t)nme * nme + 2 * (size_t)nm3)))) return cuda_fail(e, "out");
+    double *bfd = nullptr, *brd = nullptr;
+    if (bf_host || br_host) {
+        if ((e = dBF.reserve(sizeof(double) * (size_t)npts * nm3)) || (e = dBR.reserve(sizeof(double) * (size_t)npts * nm3)))
+            return cuda_fail(e, "allocating bispectra");
+        bfd = dBF.as<double>();
+        brd = dBR.as<double>();
+    }
+    if ((e = cudaEventRecord(ev2, stream))) return cuda_fail(e, "event");
+    if ((e = launch_bfm_fp64(stream, dA.as<double>(), dQ.as<double>(), K, nme, ps, npts, frf(), G, dPartF.as<double>(),
+                             dPartR.as<double>(), bfd, brd)))
+        return cuda_fail(e, "FP64 contraction kernel");
+    double *o = dOut.as<double>() + 3 * (size_t)nme * nme;
+    if ((e = launch_reduce_groups(stream, G, nm3, dPartF.as<double>(), o, dPartR.as<double>(), o + nm3)))
+        return cuda_fail(e, "reduction kernel");
+    kernels += 2;
+    std::vector<double> h(2 * (size_t)nm3);
+    if ((e = cudaMemcpyAsync(h.data(), o, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, stream)))
+        return cuda_fail(e, "moment copy");
+    if (bf_host && (e = cudaMemcpyAsync(bf_host, bfd, sizeof(double) * (size_t)npts * nm3, cudaMemcpyDeviceToHost, stream)))
+        return cuda_fail(e, "bispectrum copy");
+    if (br_host && (e = cudaMemcpyAsync(br_host, brd, sizeof(double) * (size_t)npts * nm3, cudaMemcpyDeviceToHost, stream)))
+        return cuda_fail(e, "bispectrum copy");
+    if ((e = cudaEventRecord(ev1, stream)) || (e = cudaStreamSynchronize(stream))) return cuda_fail(e, "sync");
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ev2, ev1);
+    last_ms_contraction = ms;
+    if (m3mf) std::memcpy(m3mf, h.data(), sizeof(double) * nm3);
+    if (m3mr) std::memcpy(m3mr, h.data() + nm3, sizeof(double) * nm3);
+    return BSA_OK;
+}
+
+// Point-set evaluation with analytic f1+f2 (Mesher functions and BsaCL semantics).
+int Engine::run_points(const double *fi, const double *fj, const double *w, double wuniform, long long npts,
+                       double *m3mf, double *m3mr, double *bfm, double *brm) {
+    int rc = upload_problem();
+    if (rc) return rc;
+    if (npts <= 0) return fail(BSA_ERR_ARG, "empty point set");
+    // Distinct frequencies: f1, f2 and f1+f2 of every point share one A table.
+    std::vector<double> ftab;
+    ftab.reserve(3 * (size_t)npts);
+    std::vector<int> ix(npts), iy(npts), iz(npts);
+    {
+        std::vector<std::pair<double, int>> key;
+        key.reserve(3 * (size_t)npts);
+        for (long long p = 0; p < npts; ++p) {
+            key.push_back({fi[p], (int)(3 * p)});
+            key.push_back({fj[p], (int)(3 * p + 1)});
+            key.push_back({fi[p] + fj[p], (int)(3 * p + 2)});
+        }
+        std::sort(key.begin(), key.end());
+        int row = -1;
+        double last = NAN;
+        for (auto &kv : key) {
+            if (!(kv.first == last)) {
+                ftab.push_back(kv.first);
+                last = kv.first;
+                ++row;
+            }
+            const int p = kv.second / 3, which = kv.second % 3;
+            (which == 0 ? ix : which == 1 ? iy : iz)[p] = row;
+        }
+    }
+    kernels = 0;
+    cudaError_t e;
+    if ((e = cudaEventRecord(ev0, stream))) return cuda_fail(e, "event");
+    if ((rc = build_atable(ftab))) return rc;
+    std::vector<double> f1(fi, fi + npts), f2(fj, fj + npts);
+    const size_t n = (size_t)npts;
+    if ((e = dPts.reserve(n * 3 * sizeof(int))) || (e = dPtsD.reserve(n * 3 * sizeof(double))))
+        return cuda_fail(e, "points");
+    int *dix = dPts.as<int>(), *diy = dix + n, *diz = diy + n;
+    double *df1 = dPtsD.as<double>(), *df2 = df1 + n, *dw = df2 + n;
+    if ((e = cudaMemcpyAsync(dix, ix.data(), n * sizeof(int), cudaMemcpyHostToDevice, stream)) ||
+        (e = cudaMemcpyAsync(diy, iy.data(), n * sizeof(int), cudaMemcpyHostToDevice, stream)) ||
+        (e = cudaMemcpyAsync(diz, iz.data(), n * sizeof(int), cudaMemcpyHostToDevice, stream)) ||
+        (e = cudaMemcpyAsync(df1, f1.data(), n * sizeof(double), cudaMemcpyHostToDevice, stream)) ||
+        (e = cudaMemcpyAsync(df2, f2.data(), n * sizeof(double), cudaMemcpyHostToDevice, stream)) ||
+        (w && (e = cudaMemcpyAsync(dw, w, n * sizeof(double), cudaMemcpyHostToDevice, stream))))
+        return cuda_fail(e, "point upload");
+    PointSrc ps{};
+    ps.mode = kPointsList;
+    ps.wmode = w ? kWeightList : kWeightUniform;
+    ps.wval = wuniform;
+    ps.ix = dix; ps.iy = diy; ps.iz = diz;
+    ps.f1 = df1; ps.f2 = df2; ps.w = w ? dw : nullptr;
+    rc = contract(ps, npts, m3mf, m3mr, bfm, brm);
+    if (rc) return rc;
+    last_points = (double)npts;
+    if ((e = cudaEventRecord(ev1, stream)) || (e = cudaEventSynchronize(ev1))) return cuda_fail(e, "event");
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ev0, ev1);
+    last_ms = ms;
+    return BSA_OK;
+}
+
+}  // namespace bsa
+
+using bsa::eng;
+
+#define GUARD()                                                        \
+    do {                                                               \
+        if (eng().halted) return BSA_ERR_STATE;                        \
+    } while (0)
+#define SETTER_BODY(stmt) \
+    GUARD();              \
+    stmt;                 \
+    eng().derived_ok = false; \
+    return BSA_OK
+
+extern "C" {
+
+int bsa_Init(void) {
+    bsa::Engine &E = eng();
+    E.free_device();
+    E.reset_inputs();
+    E.halted = false;
+    E.last_error.clear();
+    E.inited = true;
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0)
+        return E.fail(BSA_ERR_CUDA, "no CUDA device: %s", e == cudaSuccess ? "0 devices" : cudaGetErrorString(e));
+    return BSA_OK;
+}
+
+int bsa_setAnalysisType(int v) {
+    GUARD();
+    if (v < 0 || v > 3) return eng().fail(BSA_ERR_ARG, "invalid sub-analysis value");
+    eng().set.suban = v;
+    return BSA_OK;
+}
+int bsa_setVersion(int v) {
+    GUARD();
+    if (v < 0 || v > 2) return eng().fail(BSA_ERR_ARG, "invalid version value");
+    eng().set.vers = v;
+    return BSA_OK;
+}
+int bsa_setScalingConv(int v) {
+    GUARD();
+    if (v < 0 || v > 2) return eng().fail(BSA_ERR_ARG, "invalid scaling convention");
+    if (v != 0) eng().set.defsc = v;
+    eng().derived_ok = false;
+    return BSA_OK;
+}
+int bsa_setSpectraComputation(int ipsd, int ibisp) {
+    GUARD();
+    eng().set.ipsd = (ipsd < 0 || ipsd > 1) ? 1 : ipsd;
+    eng().set.ibisp = (ibisp < 0 || ibisp > 1) ? 1 : ibisp;
+    return BSA_OK;
+}
+int bsa_setSpectraExtension(int v) {
+    GUARD();
+    if (v < 0 || v > 1) return eng().fail(BSA_ERR_ARG, "invalid only-diagonal value");
+    eng().set.onlyd = v;
+    return BSA_OK;
+}
+int bsa_setSpatialSymmetry(int v) {
+    GUARD();
+    eng().set.bispsym = (v == 0 || v == 4) ? v : 2;
+    return BSA_OK;
+}
+int bsa_setSpectraSymmetries(int v) {
+    GUARD();
+    eng().set.spctrsym = (v == 0 || v == 1) ? v : 0;
+    return BSA_OK;
+}
+int bsa_setTestMode(int v) {
+    GUARD();
+    if (v < 0 || v > 1) return eng().fail(BSA_ERR_ARG, "invalid test-mode value");
+    eng().set.test = v;
+    return BSA_OK;
+}
+int bsa_setupClassic(int nfreqs, double df) {
+    GUARD();
+    eng().set.nfreqs = nfreqs;
+    eng().set.df = df;
+    return BSA_OK;
+}
+int bsa_setClassicMode(int v) {
+    GUARD();
+    eng().set.scalar = (v == 0 || v == 1) ? v : 0;
+    return BSA_OK;
+}
+int bsa_setupMesher(int isvd, int bkgrfmt, double bkgaext, double genpaext, double maxaext, int ifcov, int idumpmod) {
+    GUARD();
+    bsa::Settings &s = eng().set;
+    s.svd = isvd; s.bkgrfmt = bkgrfmt; s.bkgaext = bkgaext; s.genpaext = genpaext; s.maxaext = maxaext;
+    s.fcov = ifcov; s.dumpmod = idumpmod;
+    return BSA_OK;
+}
+int bsa_setWindDirections(const int *dirs, int ndirs) {
+    GUARD();
+    if (!dirs || ndirs < 1 || ndirs > 3) return eng().fail(BSA_ERR_ARG, "size mismatch in setting spatial directions");
+    SETTER_BODY(eng().set.dirs.assign(dirs, dirs + ndirs));
+}
+int bsa_setWindTurbComps(const int *tc, int ntc) {
+    GUARD();
+    if (!tc || ntc < 1 || ntc > 3) return eng().fail(BSA_ERR_ARG, "size mismatch in setting turbulent components");
+    SETTER_BODY(eng().set.tc.assign(tc, tc + ntc));
+}
+int bsa_setTotalNOfNodes(int nn) { SETTER_BODY(eng().in.nn = nn); }
+int bsa_setNumOfNodalDOFs(int nlibs) { SETTER_BODY(eng().in.nlibs = nlibs); }
+int bsa_setTotalNumOfDOFs(int ndofs) { SETTER_BODY(eng().in.ndofs = ndofs); }
+int bsa_setLoadedNodes(const int *nodes, int nnl) {
+    GUARD();
+    if (!nodes || nnl <= 0) return eng().fail(BSA_ERR_ARG, "empty loaded-node list");
+    SETTER_BODY((eng().in.n_load = nodes, eng().in.nnl = nnl));
+}
+int bsa_setLoadedNodalDOFs(const int *libs, int nlibsl) {
+    GUARD();
+    if (!libs || nlibsl <= 0) return eng().fail(BSA_ERR_ARG, "empty loaded-DOF list");
+    SETTER_BODY((eng().in.libs_load = libs, eng().in.nlibsl = nlibsl));
+}
+int bsa_setNodalCoords(int nn, const double *coords) {
+    GUARD();
+    bsa::Inputs &I = eng().in;
+    if (I.nn != 0 && I.nn != nn) return eng().fail(BSA_ERR_ARG, "nodal info does not match in setting nodal coordinates");
+    SETTER_BODY((I.nn = nn, I.coords = coords));
+}
+int bsa_setModalInfo(int ndofs, int nm, const double *phi, const double *natf) {
+    GUARD();
+    bsa::Inputs &I = eng().in;
+    SETTER_BODY((I.ndofs = ndofs, I.phi_ndofs = ndofs, I.nm = nm, I.phi = phi, I.natf = natf));
+}
+int bsa_setModalMatrices(int nm, const double *M, const double *Kg, const double *Cg) {
+    GUARD();
+    bsa::Inputs &I = eng().in;
+    if (I.nm != 0 && I.nm != nm) return eng().fail(BSA_ERR_ARG, "nm differs from previously set");
+    SETTER_BODY((I.nm = nm, I.Mg = M, I.Kg = Kg, I.Cg = Cg));
+}
+int bsa_setTotDamping(const double *xsi, int nm) {
+    GUARD();
+    if (eng().in.nm == 0) return eng().fail(BSA_ERR_STATE, "NM == 0 when setting damping info");
+    if (nm != eng().in.nm) return eng().fail(BSA_ERR_ARG, "damping size does not match nm");
+    SETTER_BODY(eng().in.xsi = xsi);
+}
+int bsa_setPSDType(int ipsd) {
+    GUARD();
+    SETTER_BODY(eng().in.psd_type = (ipsd < 1 || ipsd > 5) ? 5 : ipsd);
+}
+int bsa_setWindVertProf(int v) {
+    GUARD();
+    if (v == 5) v = 1;
+    if (v < 1 || v > 3) return eng().fail(BSA_ERR_ARG, "invalid iwprof value");
+    eng().in.wprof = v;
+    return BSA_OK;
+}
+int bsa_setWindAltDir(int v) {
+    GUARD();
+    if (v < 1 || v > 3) return eng().fail(BSA_ERR_ARG, "invalid ivert value");
+    eng().in.vert = v;
+    return BSA_OK;
+}
+int bsa_setAirDensity(double a) {
+    GUARD();
+    if (a < 0.0) return eng().fail(BSA_ERR_ARG, "air density has a negative value");
+    eng().in.air_dens = a;
+    return BSA_OK;
+}
+int bsa_setWZMeanWindVel(const double *u, int nz) { SETTER_BODY((eng().in.ubref = u, eng().in.nz = std::max(eng().in.nz, nz))); }
+int bsa_setWZRefAlt(const double *z, int nz) { SETTER_BODY((eng().in.zref = z, eng().in.nz = std::max(eng().in.nz, nz))); }
+int bsa_setTurbWindScales(const double *L, int nz) { SETTER_BODY((eng().in.L = L, eng().in.nz = std::max(eng().in.nz, nz))); }
+int bsa_setTurbWindSDT(const double *s, int nz) { SETTER_BODY((eng().in.sigma = s, eng().in.nz = std::max(eng().in.nz, nz))); }
+int bsa_setNodalVel(const double *u, int nn) { (void)nn; SETTER_BODY(eng().in.unod = u); }
+int bsa_setNodalWindZones(const int *wz, int nn) { (void)nn; SETTER_BODY(eng().in.wz = wz); }
+int bsa_setNodalWindAltitudes(const double *a, int nn) { (void)nn; SETTER_BODY(eng().in.walt = a); }
+int bsa_setSpatialNodalCorr(const double *c, int64_t ncorr) { SETTER_BODY((eng().in.corr = c, eng().in.ncorr = ncorr)); }
+int bsa_setWindFCoeffs(const double *wfc, int nl, int nd, int nn) {
+    GUARD();
+    bsa::Inputs &I = eng().in;
+    SETTER_BODY((I.wfc = wfc, I.wfc_nl = nl, I.wfc_nd = nd, I.wfc_nn = nn));
+}
+
+int bsa_getNModesEff(int *nm_eff) {
+    GUARD();
+    int rc = eng().validate();
+    if (rc) return rc;
+    if (nm_eff) *nm_eff = eng().nme;
+    return BSA_OK;
+}
+
+int bsa_Run(double *m2mf_cls, double *m2mr_cls, double *m2o2mr_cls, double *m3mf_msh, double *m3mr_msh,
+            double *m3mf_cls, double *m3mr_cls) {
+    GUARD();
+    bsa::Engine &E = eng();
+    if (!E.inited) return E.fail(BSA_ERR_STATE, "bsa_Init was not called");
+    if (E.set.ipsd == 0 && E.set.ibisp == 0) return BSA_OK;  // both disabled: nothing to do
+    int rc = E.validate();
+    if (rc) return rc;
+    const int su = E.set.suban;
+    if (su == 2 || su == 3) {
+        rc = E.run_mesher(m3mf_msh, m3mr_msh);
+        if (rc) return rc;
+    }
+    if (su == 1 || su == 3 || su == 0) {
+        rc = E.run_classic(m2mf_cls, m2mr_cls, m2o2mr_cls, m3mf_cls, m3mr_cls, nullptr, nullptr, nullptr);
+        if (rc) return rc;
+    }
+    return BSA_OK;
+}
+
+int bsa_Finalise(void) {
+    bsa::Engine &E = eng();
+    E.free_device();
+    E.reset_inputs();
+    E.halted = false;
+    E.inited = false;
+    return BSA_OK;
+}
+
+int bsa_computeSkewness(int nm, const double *m2, const double *m3, double *sk) {
+    if (nm <= 0 || !m2 || !m3 || !sk) return BSA_ERR_ARG;
+    size_t pm3 = 0;
+    for (int k = 0; k < nm; ++k)
+        for (int j = 0; j < nm; ++j)
+            for (int i = 0; i < nm; ++i, ++pm3)
+                sk[pm3] = m3[pm3] / (std::sqrt(m2[k * nm + k]) * std::sqrt(m2[j * nm + j]) * std::sqrt(m2[i * nm + i]));
+    return BSA_OK;
+}
+
+const char *bsa_lastError(void) { return eng().last_error.c_str(); }
+
+int bsa_gpu_setPrecision(int prec) {
+    GUARD();
+    if (prec != BSA_PREC_FP64 && prec != BSA_PREC_BF16X3) return eng().fail(BSA_ERR_ARG, "unknown precision");
+    eng().precision = prec;
+    return BSA_OK;
+}
+
+int bsa_gpu_setClassicTruncation(int on) {
+    GUARD();
+    eng().classic_trunc = on != 0;
+    return BSA_OK;
+}
+
+int bsa_gpu_clsBispectra(double *f_out, int nf_cap, int *nf, double *bisp_f, double *bisp_r) {
+    GUARD();
+    bsa::Engine &E = eng();
+    int rc = E.validate();
+    if (rc) return rc;
+    std::vector<double> grid;
+    if ((rc = E.classic_grid(grid))) return rc;
+    if (nf) *nf = (int)grid.size();
+    if ((int)grid.size() > nf_cap) return E.fail(BSA_ERR_ARG, "grid has %zu points, capacity %d", grid.size(), nf_cap);
+    const int prec = E.precision;
+    E.precision = BSA_PREC_FP64;
+    rc = E.run_classic(nullptr, nullptr, nullptr, nullptr, nullptr, bisp_f, bisp_r, &grid);
+    E.precision = prec;
+    if (rc) return rc;
+    if (f_out) std::memcpy(f_out, grid.data(), sizeof(double) * grid.size());
+    return BSA_OK;
+}
+
+int bsa_gpu_mshBispectra(const double *fi, const double *fj, int npts, double *bfm, double *brm) {
+    GUARD();
+    if (!fi || !fj || npts <= 0) return eng().fail(BSA_ERR_ARG, "empty point set");
+    return eng().run_points(fi, fj, nullptr, 0.0, npts, nullptr, nullptr, bfm, brm);
+}
+
+int bsa_gpu_mshMoments(const double *fi, const double *fj, const double *w, int npts, double *m3mf, double *m3mr) {
+    GUARD();
+    if (!fi || !fj || !w || npts <= 0) return eng().fail(BSA_ERR_ARG, "empty point set");
+    return eng().run_points(fi, fj, w, 0.0, npts, m3mf, m3mr, nullptr, nullptr);
+}
+
+int bsa_gpu_getStats(bsa_gpu_stats *st) {
+    if (!st) return BSA_ERR_ARG;
+    st->ms_total = eng().last_ms;
+    st->ms_contraction = eng().last_ms_contraction;
+    st->points = eng().last_points;
+    st->kernels = eng().kernels;
+    st->precision = eng().precision;
+    return BSA_OK;
+}
+
+}  // extern "C"

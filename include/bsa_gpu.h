@@ -1,0 +1,187 @@
+/*
+ * bsa_gpu.h -- C-ABI of libbsagpu, a GB300 (sm_103a) implementation of BsaLib's
+ * bispectral-force-model (BFM) hot path.
+ *
+ * Three groups of entry points, all plain C (pointers and sizes; arrays in the Fortran
+ * column-major layouts the reference uses; ids 1-based as in the reference):
+ *
+ *  1. The BsaLib public API for the path (module BsaLib, src/BsaLib.F90): bsa_Init, the
+ *     setters the standalone driver calls (app/bsa.F90:525-606), bsa_Run, bsa_Finalise.
+ *     Setters BORROW the caller's arrays, exactly like the reference (which keeps Fortran
+ *     pointers to them): they must stay alive until bsa_Finalise.  bsa_Run writes into
+ *     caller-owned buffers (the reference allocates them; here the caller sizes them with
+ *     bsa_getNModesEff: nm^2 for m2*, nm^3 for m3*).
+ *
+ *  2. The reference's device offload ABI, BsaCL (BsaCL/include/bsacl.h:28-55), with the
+ *     same names and argument meaning, so a Fortran host built with BSA_USE_GPU can link
+ *     this library in place of BsaCL.
+ *
+ *  3. Plugin-level batched entries standing in for the procedure pointers the hot path
+ *     sits behind (getBFMClsVect / getBRMClsVect / getMshBFM / getMshBRM,
+ *     src/bsa/data/BsaLibData.F90:166-185, 295-309), plus precision control.
+ *
+ * Error convention: every int-returning function returns BSA_OK (0) or a negative code
+ * and never exits the process (the reference's bsa_Abort ends in `error stop`).  After a
+ * failure the library is halted (sticky, as BsaCL's has_halted__) until bsa_Finalise;
+ * bsa_lastError() describes the first failure.  Not re-entrant: one host thread.
+ */
+#ifndef BSA_GPU_H_
+#define BSA_GPU_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BSA_OK 0
+#define BSA_ERR_ARG -1        /* invalid argument or size mismatch                  */
+#define BSA_ERR_STATE -2      /* call out of order, missing input, or halted        */
+#define BSA_ERR_CUDA -3       /* CUDA runtime error (message in bsa_lastError)      */
+#define BSA_ERR_UNSUPPORTED -4 /* valid in the reference but not on this path       */
+#define BSA_ERR_TIMEOUT -5    /* a device-side wait ran out of its iteration budget */
+#define BSA_ERR_NOMEM -6      /* device allocation failed                           */
+
+#define BSA_PREC_FP64 0       /* plain FP64 contraction (parity path)               */
+#define BSA_PREC_BF16X3 1     /* split BF16x3 tensor-core contraction, FP32 accum.   */
+
+/* ---------------------------------------------------------------------------------- */
+/* 1. BsaLib API (src/BsaLib.F90, src/bsa/BsaLibImpl.F90)                              */
+/* ---------------------------------------------------------------------------------- */
+
+/* bsa_Init, src/BsaLib.F90:294 (BsaLibImpl.F90:61-85): reset state, select the device. */
+int bsa_Init(void);
+
+/* Settings (src/bsa/BsaLibImpl.F90:750-980, src/settings/SettingsImpl.F90). */
+int bsa_setAnalysisType(int isuban);           /* BsaLibImpl.F90:909, 1 classic 2 mesher 3 both */
+int bsa_setVersion(int ivers);                 /* BsaLibImpl.F90:923                          */
+int bsa_setScalingConv(int iconv);             /* BsaLibImpl.F90:930, 1 circular 2 frequency  */
+int bsa_setSpectraComputation(int ipsd, int ibisp); /* BsaLibImpl.F90:937                     */
+int bsa_setSpectraExtension(int ionlydiag);    /* BsaLibImpl.F90:945 (only 0 = full is on the path) */
+int bsa_setSpatialSymmetry(int isym);          /* BsaLibImpl.F90:750                          */
+int bsa_setSpectraSymmetries(int isym);        /* BsaLibImpl.F90:771                          */
+int bsa_setTestMode(int itest);                /* BsaLibImpl.F90:951                          */
+int bsa_setupClassic(int nfreqs, double df);   /* BsaLibImpl.F90:959                          */
+int bsa_setClassicMode(int imode);             /* BsaLibImpl.F90:916, 0 vectorised 1 scalar   */
+int bsa_setupMesher(int isvd, int bkgrfmt, double bkgaext, double genpaext, double maxaext,
+                    int ifcov, int idumpmod);  /* BsaLibImpl.F90:966                          */
+int bsa_setWindDirections(const int *dirs, int ndirs);  /* BsaLibImpl.F90:983                 */
+int bsa_setWindTurbComps(const int *tc, int ntc);       /* BsaLibImpl.F90:991                 */
+
+/* Structure (src/structure/StructureImpl.F90). */
+int bsa_setTotalNOfNodes(int nn);                       /* BsaLibImpl.F90:1180           */
+int bsa_setNumOfNodalDOFs(int nlibs);                   /* BsaLibImpl.F90:1172           */
+int bsa_setTotalNumOfDOFs(int ndofs);                   /* BsaLibImpl.F90:1163           */
+int bsa_setLoadedNodes(const int *nodes_l, int nn_l);   /* BsaLibImpl.F90:1208           */
+int bsa_setLoadedNodalDOFs(const int *libs_l, int nlibs_l); /* BsaLibImpl.F90:1188       */
+int bsa_setNodalCoords(int nn, const double *coords);   /* BsaLibImpl.F90:1154, (3, nn)  */
+int bsa_setModalInfo(int ndofs, int nm, const double *phi, const double *natf); /* BsaLibImpl.F90:1238 */
+int bsa_setModalMatrices(int nm, const double *Mgen, const double *Kgen, const double *Cgen); /* BsaLibImpl.F90:1247, C (nm,nm) */
+int bsa_setTotDamping(const double *xsi, int nm);       /* BsaLibImpl.F90:1264           */
+
+/* Wind (src/wind/WindSetImpl.F90). */
+int bsa_setPSDType(int ipsd);                           /* BsaLibImpl.F90:1006, ids 1,2,3,5 */
+int bsa_setWindVertProf(int iwprof);                    /* BsaLibImpl.F90:1000 (stored)  */
+int bsa_setWindAltDir(int ivert);                       /* BsaLibImpl.F90:1013 (stored)  */
+int bsa_setAirDensity(double aird);                     /* BsaLibImpl.F90:1033 (stored)  */
+int bsa_setWZMeanWindVel(const double *ubref, int nz);  /* BsaLibImpl.F90:1047           */
+int bsa_setWZRefAlt(const double *zref, int nz);        /* BsaLibImpl.F90:1054 (stored)  */
+int bsa_setTurbWindScales(const double *L, int nz);     /* BsaLibImpl.F90:1061, (3,3,nz) */
+int bsa_setTurbWindSDT(const double *sigma, int nz);    /* BsaLibImpl.F90:1068, (3,nz)   */
+int bsa_setNodalVel(const double *unod, int nn);        /* BsaLibImpl.F90:1104           */
+int bsa_setNodalWindZones(const int *wz, int nn);       /* BsaLibImpl.F90:1111           */
+int bsa_setNodalWindAltitudes(const double *walt, int nn); /* BsaLibImpl.F90:1118 (stored) */
+int bsa_setSpatialNodalCorr(const double *corr, int64_t ncorr); /* BsaLibImpl.F90:1125, (ncorr,3) */
+int bsa_setWindFCoeffs(const double *wfc, int nlibs_l, int ndegw3, int nn_l); /* BsaLibImpl.F90:1133, (nlibs_l,ndegw+3,nn_l) */
+
+/* Validates the inputs (validateAll_, BsaLibImpl.F90:469-535: mode validation
+ * validateModalInfo_ :545-599, projection setPhitimesCLocalInstance_ :611-671) and returns
+ * the number of kept modes, which sizes bsa_Run's outputs. */
+int bsa_getNModesEff(int *nm_eff);
+
+/* bsa_Run, src/BsaLib.F90:372-399 (BsaLibImpl.F90:153-462).  Classic outputs m2mf_cls,
+ * m2mr_cls, m2o2mr_cls (nm^2), m3mf_cls, m3mr_cls (nm^3); Mesher outputs m3mf_msh,
+ * m3mr_msh (nm^3).  Any pointer may be NULL when not wanted. */
+int bsa_Run(double *m2mf_cls, double *m2mr_cls, double *m2o2mr_cls, double *m3mf_msh,
+            double *m3mr_msh, double *m3mf_cls, double *m3mr_cls);
+
+/* bsa_Finalise, src/BsaLib.F90:401 (cleanBSAData_): drop borrowed pointers, free device memory. */
+int bsa_Finalise(void);
+
+/* computeSkewness_ (BsaLibImpl.F90:1630-1707): sk = m3_mno / (sig_m sig_n sig_o). */
+int bsa_computeSkewness(int nm, const double *m2, const double *m3, double *sk);
+
+const char *bsa_lastError(void);
+
+/* ---------------------------------------------------------------------------------- */
+/* 2. BsaCL device ABI (BsaCL/include/bsacl.h:28-55; bodies in BsaCL/src/bsacl.c)       */
+/*    bsaclRun computes the response third moments m3mr (nm^3) over the outer product  */
+/*    of the acquired fi x fj lists with the uniform influence dfi*dfj*4*pi^2, as      */
+/*    bsacl.c:1544-1572 does; S(fi+fj) is analytic (bsacl.cl).                         */
+/* ---------------------------------------------------------------------------------- */
+int bsaclInit(unsigned n_threads);                                        /* bsacl.c:1032 */
+int bsaclInitDeviceMemory(void);                                          /* bsacl.c:1099 */
+int bsaclRun(unsigned i_thread, size_t dim, double *h_res);               /* bsacl.c:1307 */
+int bsaclSetKernelID(unsigned kid);                                       /* bsacl.c:1597 */
+void bsaclAcquirePSDId(uint32_t psdid);                                   /* bsacl.c:1614 */
+void bsaclAcquireStructModMat(double *modmat, double *natf, uint32_t ndofs, uint32_t nmodes); /* bsacl.c:1633 */
+void bsaclAcquireModalMatrices(double *Mg, double *Cg, double *Kg);       /* bsacl.c:1653 */
+void bsaclAcquireLoadedNodesList(int *nodes_load, uint32_t nnodes_l);     /* bsacl.c:1672 */
+void bsaclAcquireTotalNOfNodes(uint32_t nnodes_tot);                      /* bsacl.c:1687 */
+void bsaclAcquireUsedModesList(int *modes, uint32_t nmodes_eff);          /* bsacl.c:1702 */
+void bsaclAcquireWindCoeffs(double *wfc, uint32_t nnodes_l, uint32_t nlibs, uint32_t ndegw); /* bsacl.c:1724 */
+void bsaclAcquireTurbComponentsList(int *tc, uint32_t ntc);               /* bsacl.c:1747 */
+void bsaclAcquirePhiTimesCMat(double *phi_T_c, uint32_t nmodes_eff, uint32_t nnodes_l, uint32_t ndegw); /* bsacl.c:1763 */
+void bsaclAcquireNodalCorrelation(double *nod_corr, uint32_t nnod_corr);  /* bsacl.c:1782 */
+void bsaclAcquireWindNodalVelocities(double *nod_vel);                    /* bsacl.c:1791 */
+void bsaclAcquireWindNodalWindZones(int *nod_wz);                         /* bsacl.c:1797 */
+void bsaclAcquireWindTurbScales(double *wt_scl, uint32_t nwz);            /* bsacl.c:1803 */
+void bsaclAcquireWindTurbStd(double *wt_std, uint32_t nwz);               /* bsacl.c:1810 */
+void bsaclAcquireComputationFreqs(unsigned i_thread, uint32_t nfi, double *fi, uint32_t nfj, double *fj); /* bsacl.c:1870 */
+void bsaclAcquireBaseWindTurbPSD(double *S_uvw);                          /* bsacl.c:1895 */
+void bsaclSetDeviceType(uint32_t itype);                                  /* bsacl.c:1914 */
+void bsaclVerifyMaxAllocCondition(size_t idim, unsigned int *ican);       /* bsacl.c:1946 */
+void bsaclAbort(int ierr);                                                /* bsacl.c:1965 */
+void bsaclFinalise(void);                                                 /* bsacl.c:1975 */
+
+/* ---------------------------------------------------------------------------------- */
+/* 3. Plugin-level entries and controls                                                */
+/* ---------------------------------------------------------------------------------- */
+
+/* Contraction precision for the Classic grid (BSA_PREC_FP64 default, or BSA_PREC_BF16X3). */
+int bsa_gpu_setPrecision(int prec);
+
+/* Classic S(f1+f2) beyond the grid: 1 (default) reads zero, as the reference's padded
+ * copy (functionsImpl.F90:1358-1363, 1409-1413); 0 evaluates it analytically. */
+int bsa_gpu_setClassicTruncation(int on);
+
+/* getBFMClsVect + getBRMClsVect materialised (functionsImpl.F90:1312-1738): force and
+ * response bispectra on the classic grid, (nf, nf, nm^3) with f1 fastest, and the grid.
+ * Runs validation and the grid set-up of bsa_Run; for small grids (tests). */
+int bsa_gpu_clsBispectra(double *f_out, int nf_cap, int *nf, double *bisp_f, double *bisp_r);
+
+/* getMshBFM / getMshBRM batched over npts arbitrary points (getFM_full_tnm_scalar_msh_,
+ * functionsImpl.F90:247-465; getRM_full_scalar_msh_, :1031-1115, point-wise): bfm and brm
+ * are (nm^3, npts); either may be NULL. */
+int bsa_gpu_mshBispectra(const double *fi, const double *fj, int npts, double *bfm, double *brm);
+
+/* Weighted moments over an arbitrary point set (the Mesher's zone integration,
+ * _shared_poly2d.fi:2091-2119): m3mf += sum_p w_p B_F(p), m3mr += sum_p w_p B_R(p). */
+int bsa_gpu_mshMoments(const double *fi, const double *fj, const double *w, int npts,
+                       double *m3mf, double *m3mr);
+
+/* Timing and counters of the last run. */
+typedef struct {
+    double ms_total;          /* device time of the last run (CUDA events)           */
+    double ms_contraction;    /* device time of the contraction kernels               */
+    double points;            /* (f1,f2) points at which B_R was produced             */
+    int kernels;              /* kernels launched by the last run                     */
+    int precision;            /* BSA_PREC_* used                                      */
+} bsa_gpu_stats;
+int bsa_gpu_getStats(bsa_gpu_stats *st);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BSA_GPU_H_ */
