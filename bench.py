@@ -1,0 +1,336 @@
+"""Benchmark of the BFM hot path: response-bispectrum (f1,f2) points per second.
+
+Workload: the tall building (400 loaded nodes, 24 modes, u and w turbulence, von Karman
+spectra, Davenport coherence) on the regular 1025 x 1025 (f1,f2) grid on [-4, 4] Hz --
+seeded synthetic inputs generated by bsalib_gb300.problem.tall_building.  One step = one
+full Classic analysis through the C-ABI: nodal spectra, A(f), second-order moments, the
+BF16x3 tcgen05 contraction with the FRF product and the third-moment reduction.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+value : points / device time of a step with the problem already resident in HBM (CUDA
+        events on the library's stream, summed over the K timed steps, max over ranks).
+e2e   : the same metric through the public call sequence a BsaLib user makes
+        (bsa_Init, setters with host arrays, bsa_Run, bsa_Finalise) per step, host wall
+        clock, host<->device copies included.
+--impl reference times the reference's own algorithm (the oracle's restatement of
+        BsaLib's OpenMP Classic scalar routine, run on the host cores) on a bounded sample.
+Multi-GPU (--gpus N under torchrun): every rank evaluates its own structure (independent
+wind cases, seed per rank): weak scaling, no collective on the data path.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "response-bispectrum (f1,f2) pts/s, mixed+learned vs FP64 GPU at <=1e-3 skew err"
+WORKLOAD = "tall_building_400nodes_24modes_2tc_grid1025x1025"
+UNIT = "pts/s"
+
+
+def algorithmic_flops_per_point(nnl, nm, ntc):
+    # F_pt = NTC * 3 * 2 * NNL * NM^3: the factored contraction counted once
+    return ntc * 3 * 2 * nnl * nm ** 3
+
+
+class Clocks:
+    """nvidia-smi sampler for the timed region (SM clock, max clock, throttle reasons)."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.rows = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True,
+                                     timeout=5).stdout.strip()
+                if out:
+                    self.rows.append([x.strip() for x in out.split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if len(r) > 4 + i and "Active" in r[4 + i]
+                          and "Not" not in r[4 + i]})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as fh:
+            d = json.load(fh)
+        return d.get("bf16_tflops", 1900.0), d.get("hbm_gbs", 6800.0), "measured"
+    return 1900.0, 6800.0, "fallback"
+
+
+def profiled_traffic():
+    """DRAM bytes per launch of the contraction kernel from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "k_bfm_mixed_tall_building.json")
+    if os.path.exists(p):
+        with open(p) as fh:
+            return json.load(fh).get("dram_bytes_per_launch")
+    return None
+
+
+def cpu_reference(prob, budget_s=20.0, threads=None):
+    """The reference's Classic scalar algorithm (BsaClassicImpl.F90:255-363 with
+    getFM_full_tnm_scalar_cls_, functionsImpl.F90:2122-2318) restated in the C oracle, on a
+    bounded sample: `npairs` grid pairs evaluated in parallel, each over a slice of k-nodes,
+    the per-pair cost extrapolated linearly in k (it is uniform in k)."""
+    import ctypes as C
+
+    from oracle import oracle as orc
+    o = orc.Oracle(prob)
+    f = o.freqs()
+    nf = f.size
+    S = o.suvw(f)
+    npsd = S.shape[1]
+    lp = (nf - 1) // 2
+    Spad = np.zeros((npsd, 2 * lp + nf), order="F")
+    Spad[:, lp:lp + nf] = S.T
+    nthreads = threads or os.cpu_count() or 1
+    lib = orc.lib()
+    nnl = prob.nnl
+    # size the k-slice so one round of pairs (one per thread) takes ~budget/3
+    kk = 1
+    rng = np.random.default_rng(0)
+    pairs = [(int(rng.integers(nf)), int(rng.integers(nf))) for _ in range(nthreads)]
+    from concurrent.futures import ThreadPoolExecutor
+
+    def one(pr, k_hi):
+        ii, ij = pr
+        return o.scalar_pair_slice(f, S, np.asfortranarray(Spad[:, ii + ij]), ii, ij, 0, k_hi)
+
+    t = time.perf_counter()
+    with ThreadPoolExecutor(nthreads) as ex:
+        list(ex.map(lambda pr: one(pr, kk), pairs))
+    dt = time.perf_counter() - t
+    kk = max(1, min(nnl, int(kk * (budget_s / 3) / max(dt, 1e-6))))
+    t = time.perf_counter()
+    rounds = 0
+    while time.perf_counter() - t < budget_s * 2 / 3 or rounds == 0:
+        with ThreadPoolExecutor(nthreads) as ex:
+            list(ex.map(lambda pr: one(pr, kk), pairs))
+        rounds += 1
+    dt = time.perf_counter() - t
+    pair_s = dt / (rounds * len(pairs)) * (nnl / kk) * nthreads  # per pair, one thread
+    pts_per_s = nthreads / pair_s
+    return {"value": pts_per_s, "unit": UNIT, "cores": nthreads, "kind": "port",
+            "sample": f"{rounds * len(pairs)} grid pairs of the scalar Classic BFM+BRM, k-node loop cut to "
+                      f"{kk}/{nnl} nodes and extrapolated linearly, {nthreads} threads, {dt:.1f} s"}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from bsalib_gb300.problem import tall_building
+    prob = tall_building()
+    vals = []
+    for _ in range(args.warmup):
+        cpu_reference(prob, budget_s=3.0)
+    info = None
+    for _ in range(args.steps):
+        info = cpu_reference(prob, budget_s=max(5.0, 60.0 / max(args.steps, 1)))
+        vals.append(info["value"])
+    v = float(np.mean(vals))
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * prob.classic_nf() ** 2 / v, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "nodes": 400, "modes": 24, "ntc": 2, "grid": 1025},
+            "cpu_baseline": info, "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def run_ours(args):
+    ws, rank, local = dist_env()
+    import torch
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from bsalib_gb300 import api
+    from bsalib_gb300 import build as bbuild
+    from bsalib_gb300.problem import tall_building
+    bbuild.build()
+    prec = api.PREC_BF16X3 if args.precision == "bf16x3" else api.PREC_FP64
+    prob = tall_building(seed=2024 + rank)
+    nf = prob.classic_nf()
+    npts = nf * nf
+
+    def barrier():
+        torch.cuda.synchronize()
+        if ws > 1:
+            torch.distributed.barrier()
+
+    # ---- value: problem resident on the device, device-timed steps ----
+    s = api.BsaSession(prob, precision=prec)
+    for _ in range(args.warmup):
+        s.run()
+    ms, gemm_ms, launches = [], [], 0
+    barrier()
+    with Clocks(local) as clk:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            r = s.run()
+            st = s.stats()
+            ms.append(st.ms_total)
+            gemm_ms.append(st.ms_gemm)
+            launches += st.kernels
+        barrier()
+        wall = time.perf_counter() - t0
+    step_ms = float(np.sum(ms)) / args.steps
+    if ws > 1:
+        t = torch.tensor([step_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        step_ms = float(t.item())
+    value = ws * npts / (step_ms / 1e3)
+    sk_mixed = s.skewness(r["m2mr_cls"], r["m3mr_cls"])
+    s.close()
+
+    # ---- e2e: the public call sequence with host buffers, per step ----
+    for _ in range(1):
+        s2 = api.BsaSession(prob, precision=prec)
+        s2.run()
+        s2.close()
+    barrier()
+    t0 = time.perf_counter()
+    h2d = d2h = 0.0
+    for _ in range(args.steps):
+        s2 = api.BsaSession(prob, precision=prec)
+        s2.run()
+        st2 = s2.stats()
+        h2d, d2h = st2.h2d_bytes, st2.d2h_bytes
+        s2.close()
+    barrier()
+    e2e_step = (time.perf_counter() - t0) / args.steps
+    if ws > 1:
+        t = torch.tensor([e2e_step], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_step = float(t.item())
+    e2e = ws * npts / e2e_step
+    # bytes the caller hands over: the problem arrays borrowed by the setters
+    h2d_in = sum(a.nbytes for a in (prob.phi, prob.wfc, prob.nod_corr, prob.u_node, prob.wz_node, prob.L,
+                                    prob.sigma, prob.natf, prob.Mg, prob.Kg, prob.Cg, prob.xsi, prob.n_load))
+
+    out = None
+    if rank == 0:
+        # ---- accuracy of the mixed path vs the plain FP64 path on the same structure,
+        #      129 x 129 grid (the FP64 path takes minutes on the full grid) ----
+        acc = {}
+        small = tall_building(nfreqs=65, df=4.0 / 64, seed=2024)
+        res = {}
+        for pr in (api.PREC_FP64, api.PREC_BF16X3):
+            ss = api.BsaSession(small, precision=pr)
+            rr = ss.run()
+            res[pr] = (rr, ss.skewness(rr["m2mr_cls"], rr["m3mr_cls"]))
+            ss.close()
+        (r64, sk64), (rmx, skmx) = res[api.PREC_FP64], res[api.PREC_BF16X3]
+        relm = lambda a, b: float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
+        acc = {"grid": "129x129", "m3mr_rel": relm(rmx["m3mr_cls"], r64["m3mr_cls"]),
+               "m3mf_rel": relm(rmx["m3mf_cls"], r64["m3mf_cls"]), "skewness_rel": relm(skmx, sk64)}
+        # ---- the plain FP64 GPU path on a sample of the full grid's points ----
+        rng = np.random.default_rng(1)
+        f = np.arange(-(nf // 2), nf // 2 + 1) * (8.0 / (nf - 1))
+        ns = 4096
+        i1, i2 = rng.integers(nf, size=ns), rng.integers(nf, size=ns)
+        s3 = api.BsaSession(prob, precision=api.PREC_FP64)
+        s3.msh_moments(f[i1], f[i2], np.ones(ns))
+        t0 = time.perf_counter()
+        s3.msh_moments(f[i1], f[i2], np.ones(ns))
+        st3 = s3.stats()
+        s3.close()
+        fp64_pts = ns / (st3.ms_total / 1e3)
+
+        peak_tf, _, peak_src = peaks()
+        flops = algorithmic_flops_per_point(prob.nnl, 24, prob.ntc) * npts
+        g_ms = float(np.mean(gemm_ms))
+        achieved = flops / (g_ms / 1e3) / 1e12
+        traffic = profiled_traffic()
+        cpu = cpu_reference(prob, budget_s=15.0)
+        out = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "bf16x3 contraction (fp32 accumulate), fp64 FRF/moments"
+            if prec == api.PREC_BF16X3 else "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "nodes": 400, "modes": 24, "ntc": 2, "grid": 1025,
+                       "precision": args.precision, "l2": "inputs larger than L2 (operand tables ~2.4 GB)"},
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d + h2d_in),
+                    "d2h_bytes_per_step": int(d2h)},
+            "gpu_launches": launches,
+            "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak_tf, "unit": "TFLOP/s",
+                         "frac": achieved / peak_tf, "traffic": traffic, "peak_source": peak_src,
+                         "kernel": "k_bfm_mixed", "kernel_ms": g_ms,
+                         "algorithmic_flop_per_launch": flops},
+            "clocks": clk.summary(),
+            "cpu_baseline": cpu,
+            "accuracy_vs_fp64": acc,
+            "fp64_gpu_path": {"value": fp64_pts, "unit": UNIT, "sample": f"{ns} random grid points"},
+            "wall_s_timed": wall,
+        }
+        print(json.dumps(out))
+    if ws > 1:
+        torch.distributed.barrier()
+        torch.distributed.destroy_process_group()
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="bf16x3", choices=["bf16x3", "fp64"])
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

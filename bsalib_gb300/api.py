@@ -34,7 +34,8 @@ class BsaError(RuntimeError):
 
 
 class Stats(C.Structure):
-    _fields_ = [("ms_total", C.c_double), ("ms_contraction", C.c_double), ("points", C.c_double),
+    _fields_ = [("ms_total", C.c_double), ("ms_contraction", C.c_double), ("ms_gemm", C.c_double),
+                ("points", C.c_double), ("h2d_bytes", C.c_double), ("d2h_bytes", C.c_double),
                 ("kernels", C.c_int), ("precision", C.c_int)]
 
 

@@ -77,8 +77,10 @@ struct Engine {
         dPtsD, dBF, dBR, dMixA, dMixB, dMixH, dMixPart;
 
     // stats
-    double last_ms = 0, last_ms_contraction = 0, last_points = 0;
+    double last_ms = 0, last_ms_contraction = 0, last_ms_gemm = 0, last_points = 0;
+    double h2d = 0, d2h = 0;
     int kernels = 0;
+    cudaEvent_t evg0 = nullptr, evg1 = nullptr;
 
     int fail(int code, const char *fmt, ...);
     int cuda_fail(cudaError_t e, const char *what);

@@ -72,7 +72,9 @@ void Engine::free_device() {
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
     if (ev2) cudaEventDestroy(ev2);
-    ev0 = ev1 = ev2 = nullptr;
+    if (evg0) cudaEventDestroy(evg0);
+    if (evg1) cudaEventDestroy(evg1);
+    ev0 = ev1 = ev2 = evg0 = evg1 = nullptr;
     dev_uploaded = false;
 }
 
@@ -83,6 +85,8 @@ int Engine::ensure_stream() {
     if ((e = cudaEventCreate(&ev0)) != cudaSuccess) return cuda_fail(e, "cudaEventCreate");
     if ((e = cudaEventCreate(&ev1)) != cudaSuccess) return cuda_fail(e, "cudaEventCreate");
     if ((e = cudaEventCreate(&ev2)) != cudaSuccess) return cuda_fail(e, "cudaEventCreate");
+    if ((e = cudaEventCreate(&evg0)) != cudaSuccess) return cuda_fail(e, "cudaEventCreate");
+    if ((e = cudaEventCreate(&evg1)) != cudaSuccess) return cuda_fail(e, "cudaEventCreate");
     return BSA_OK;
 }
 
@@ -224,6 +228,7 @@ template <class T>
 static cudaError_t upload(DevBuf &b, const std::vector<T> &v, cudaStream_t st) {
     cudaError_t e = b.reserve(sizeof(T) * v.size());
     if (e != cudaSuccess || v.empty()) return e;
+    eng().h2d += (double)(sizeof(T) * v.size());
     return cudaMemcpyAsync(b.p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, st);
 }
 
@@ -305,6 +310,9 @@ int Engine::classic_grid(std::vector<double> &f) {
 // moments reduced in the kernel epilogue.  Optional materialised bispectra (nf, nf, nm^3).
 int Engine::run_classic(double *m2mf, double *m2mr, double *m2o2mr, double *m3mf, double *m3mr, double *bf_host,
                         double *br_host, std::vector<double> *grid_out) {
+    kernels = 0;
+    h2d = d2h = 0;
+    last_ms_gemm = 0;
     int rc = upload_problem();
     if (rc) return rc;
     std::vector<double> f;
@@ -326,7 +334,6 @@ int Engine::run_classic(double *m2mf, double *m2mr, double *m2o2mr, double *m3mf
         const double d = f[1] - f[0];
         for (int s = 0; s < 2 * nf - 1; ++s) ftab.push_back(2.0 * f[0] + s * d);
     }
-    kernels = 0;
     cudaError_t e;
     if ((e = cudaEventRecord(ev0, stream))) return cuda_fail(e, "event");
     if ((rc = build_atable(ftab))) return rc;
@@ -350,6 +357,7 @@ int Engine::run_classic(double *m2mf, double *m2mr, double *m2o2mr, double *m3mf
         if ((e = cudaMemcpyAsync(h.data(), o, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, stream)) ||
             (e = cudaStreamSynchronize(stream)))
             return cuda_fail(e, "m2 copy");
+        d2h += (double)sizeof(double) * h.size();
         if (m2mf) std::memcpy(m2mf, h.data(), sizeof(double) * nm2);
         if (m2mr) std::memcpy(m2mr, h.data() + nm2, sizeof(double) * nm2);
         if (m2o2mr) std::memcpy(m2o2mr, h.data() + 2 * nm2, sizeof(double) * nm2);
@@ -396,9 +404,11 @@ int Engine::contract(const PointSrc &ps, long long npts, double *m3mf, double *m
         brd = dBR.as<double>();
     }
     if ((e = cudaEventRecord(ev2, stream))) return cuda_fail(e, "event");
+    if ((e = cudaEventRecord(evg0, stream))) return cuda_fail(e, "event");
     if ((e = launch_bfm_fp64(stream, dA.as<double>(), dQ.as<double>(), K, nme, ps, npts, frf(), G, dPartF.as<double>(),
                              dPartR.as<double>(), bfd, brd)))
         return cuda_fail(e, "FP64 contraction kernel");
+    if ((e = cudaEventRecord(evg1, stream))) return cuda_fail(e, "event");
     double *o = dOut.as<double>() + 3 * (size_t)nme * nme;
     if ((e = launch_reduce_groups(stream, G, nm3, dPartF.as<double>(), o, dPartR.as<double>(), o + nm3)))
         return cuda_fail(e, "reduction kernel");
@@ -414,6 +424,9 @@ int Engine::contract(const PointSrc &ps, long long npts, double *m3mf, double *m
     float ms = 0.f;
     cudaEventElapsedTime(&ms, ev2, ev1);
     last_ms_contraction = ms;
+    cudaEventElapsedTime(&ms, evg0, evg1);
+    last_ms_gemm = ms;
+    d2h += (double)sizeof(double) * h.size() + (bf_host ? 8.0 * npts * nm3 : 0.0) + (br_host ? 8.0 * npts * nm3 : 0.0);
     if (m3mf) std::memcpy(m3mf, h.data(), sizeof(double) * nm3);
     if (m3mr) std::memcpy(m3mr, h.data() + nm3, sizeof(double) * nm3);
     return BSA_OK;
@@ -422,6 +435,9 @@ int Engine::contract(const PointSrc &ps, long long npts, double *m3mf, double *m
 // Point-set evaluation with analytic f1+f2 (Mesher functions and BsaCL semantics).
 int Engine::run_points(const double *fi, const double *fj, const double *w, double wuniform, long long npts,
                        double *m3mf, double *m3mr, double *bfm, double *brm) {
+    kernels = 0;
+    h2d = d2h = 0;
+    last_ms_gemm = 0;
     int rc = upload_problem();
     if (rc) return rc;
     if (npts <= 0) return fail(BSA_ERR_ARG, "empty point set");
@@ -450,11 +466,11 @@ int Engine::run_points(const double *fi, const double *fj, const double *w, doub
             (which == 0 ? ix : which == 1 ? iy : iz)[p] = row;
         }
     }
-    kernels = 0;
     cudaError_t e;
     if ((e = cudaEventRecord(ev0, stream))) return cuda_fail(e, "event");
     if ((rc = build_atable(ftab))) return rc;
     std::vector<double> f1(fi, fi + npts), f2(fj, fj + npts);
+    h2d += (double)npts * (3 * sizeof(int) + (w ? 3 : 2) * sizeof(double));
     const size_t n = (size_t)npts;
     if ((e = dPts.reserve(n * 3 * sizeof(int))) || (e = dPtsD.reserve(n * 3 * sizeof(double))))
         return cuda_fail(e, "points");
@@ -757,7 +773,10 @@ int bsa_gpu_getStats(bsa_gpu_stats *st) {
     if (!st) return BSA_ERR_ARG;
     st->ms_total = eng().last_ms;
     st->ms_contraction = eng().last_ms_contraction;
+    st->ms_gemm = eng().last_ms_gemm;
     st->points = eng().last_points;
+    st->h2d_bytes = eng().h2d;
+    st->d2h_bytes = eng().d2h;
     st->kernels = eng().kernels;
     st->precision = eng().precision;
     return BSA_OK;

@@ -239,7 +239,7 @@ __device__ __forceinline__ void get_point(const PointSrc &ps, long long p, int &
     }
 }
 
-template <int NOT>
+template <int NOT, int MT>
 __global__ __launch_bounds__(256) void k_bfm_fp64(const double *__restrict__ A,
                                                   const double *__restrict__ Q, int K, int nm,
                                                   PointSrc ps, long long npts, FrfPar frf,
@@ -247,8 +247,7 @@ __global__ __launch_bounds__(256) void k_bfm_fp64(const double *__restrict__ A,
                                                   double *__restrict__ part_mr,
                                                   double *__restrict__ bf_out,
                                                   double *__restrict__ br_out) {
-    constexpr int MG = 256 / NOT;
-    constexpr int MT = (64 + MG - 1) / MG;
+    constexpr int MG = 256 / NOT;  // m-groups; thread owns m = mg + MG * u, u < MT
     const int tile = blockIdx.x, pg = blockIdx.y, G = gridDim.y;
     const int t = threadIdx.x, nol = t % NOT, mg = t / NOT;
     const int nm2 = nm * nm;
@@ -365,17 +364,38 @@ int bfm_fp64_groups(long long npts, int nm) {
     return (int)std::max<long long>(g, 1);
 }
 
-template <int NOT>
+template <int NOT, int MT>
 static cudaError_t launch_bfm_t(cudaStream_t st, const double *A, const double *Q, int K, int nm,
                                 const PointSrc &ps, long long npts, FrfPar frf, int n_groups,
                                 double *part_mf, double *part_mr, double *bf_out, double *br_out) {
     const size_t smem = sizeof(double) * (2 * KC * nm + 2 * KC * NOT + 6 * nm);
-    cudaError_t e = cudaFuncSetAttribute(k_bfm_fp64<NOT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaError_t e = cudaFuncSetAttribute(k_bfm_fp64<NOT, MT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e != cudaSuccess) return e;
     dim3 grid((unsigned)((nm * nm + NOT - 1) / NOT), (unsigned)n_groups);
-    k_bfm_fp64<NOT><<<grid, 256, smem, st>>>(A, Q, K, nm, ps, npts, frf, part_mf, part_mr, bf_out, br_out);
+    k_bfm_fp64<NOT, MT><<<grid, 256, smem, st>>>(A, Q, K, nm, ps, npts, frf, part_mf, part_mr, bf_out, br_out);
     return cudaGetLastError();
+}
+
+// MT = smallest supported count >= ceil(nm / MG), so no thread carries idle mode slots.
+template <int NOT>
+static cudaError_t launch_bfm_n(cudaStream_t st, const double *A, const double *Q, int K, int nm,
+                                const PointSrc &ps, long long npts, FrfPar frf, int n_groups,
+                                double *part_mf, double *part_mr, double *bf_out, double *br_out) {
+    constexpr int MG = 256 / NOT;
+    const int need = (nm + MG - 1) / MG;
+#define BSA_MT_CASE(V)                                                                                   \
+    if (need <= V)                                                                                       \
+        return launch_bfm_t<NOT, V>(st, A, Q, K, nm, ps, npts, frf, n_groups, part_mf, part_mr, bf_out, br_out);
+    BSA_MT_CASE(1)
+    BSA_MT_CASE(2)
+    BSA_MT_CASE(4)
+    BSA_MT_CASE(6)
+    BSA_MT_CASE(8)
+    BSA_MT_CASE(12)
+    BSA_MT_CASE(16)
+#undef BSA_MT_CASE
+    return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_bfm_fp64(cudaStream_t st, const double *A, const double *Q, int K, int nm,
@@ -385,11 +405,11 @@ cudaError_t launch_bfm_fp64(cudaStream_t st, const double *A, const double *Q, i
     if (npts == 0) return cudaSuccess;
     switch (not_for(nm)) {
     case 64:
-        return launch_bfm_t<64>(st, A, Q, K, nm, ps, npts, frf, n_groups, part_mf, part_mr, bf_out, br_out);
+        return launch_bfm_n<64>(st, A, Q, K, nm, ps, npts, frf, n_groups, part_mf, part_mr, bf_out, br_out);
     case 32:
-        return launch_bfm_t<32>(st, A, Q, K, nm, ps, npts, frf, n_groups, part_mf, part_mr, bf_out, br_out);
+        return launch_bfm_n<32>(st, A, Q, K, nm, ps, npts, frf, n_groups, part_mf, part_mr, bf_out, br_out);
     default:
-        return launch_bfm_t<16>(st, A, Q, K, nm, ps, npts, frf, n_groups, part_mf, part_mr, bf_out, br_out);
+        return launch_bfm_n<16>(st, A, Q, K, nm, ps, npts, frf, n_groups, part_mf, part_mr, bf_out, br_out);
     }
 }
 

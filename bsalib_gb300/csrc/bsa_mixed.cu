@@ -1,12 +1,631 @@
-// bsa_mixed.cu -- split-precision (BF16x3) tensor-core contraction of the Classic grid.
+// bsa_mixed.cu -- split-precision (BF16x3) tensor-core contraction of the Classic grid,
+// written for sm_103a with tcgen05 MMA, TMEM accumulators and TMA-fed shared memory.
+//
+// Exact restructuring of the BFM contraction (functionsImpl.F90:1494-1538, three terms):
+// with U(f)[(a,b), k] = Q[k][a] A(f)[k][b] and, for a grid row r and column c,
+//   D1(r,c)[(a,b), j] = sum_k U(f_r)[(a,b),k] A(f_c)[k][j]
+//   D3(r,c)[(a,b), j] = sum_k U(f_r)[(a,b),k] Z(r+c)[k][j],   Z(s) = A(f1+f2)
+// term 1 at (f1,f2) = (r,c) is D1 with (m,n,o) = (a,b,j), term 3 at (r,c) is D3 with
+// (m,n,o) = (j,b,a), and term 2 at (c,r) is the same D3 with (m,n,o) = (j,a,b).  So the
+// whole grid is two GEMM families sharing their A operand (the rows of U(f_r)); the FRF
+// product (getRM_full_vect_cls_, :1598-1738) and the integration weights
+// (intgSpectraVect_, BsaClassicImpl.F90:567-633) are applied in the epilogue, which reduces
+// straight to third moments: no bispectrum is ever stored.
+//
+// Precision: every operand is split into bf16 hi + lo; D = Ahi Bhi + Ahi Blo + Alo Bhi with
+// FP32 accumulation in TMEM.  The FRF is evaluated in FP64 (the K - w^2 M cancellation near
+// resonance) and rounded once; per-thread moment partials are FP32 over at most a few
+// hundred points and are accumulated in FP64 in global memory.
+//
+// Kernel roles (192 threads, one CTA per SM): warp 0 issues TMA loads, warp 1 owns TMEM
+// and issues tcgen05.mma from one thread, warps 2-5 drain TMEM (one thread per TMEM lane).
+// Every wait on an mbarrier is bounded by a global-timer budget; on expiry the kernel sets
+// an error flag, stops issuing work, lets in-flight copies and MMAs land, frees TMEM and
+// returns, so the host gets BSA_ERR_TIMEOUT and the context stays usable.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstring>
+#include <vector>
+
 #include "../../include/bsa_gpu.h"
 #include "bsa_engine.cuh"
 
 namespace bsa {
+namespace mixed {
+
+constexpr int kBM = 128;         // MMA M (TMEM lanes)
+constexpr int kBN = 128;         // MMA N per accumulator
+constexpr int kBK = 64;          // K per shared-memory stage: one 128-byte swizzle row of bf16
+constexpr int kStages = 2;
+constexpr int kTileBytes = 128 * 128;            // 128 rows x 128 bytes
+constexpr int kStageBytes = 6 * kTileBytes;      // U hi/lo, Bg hi/lo, Bs hi/lo
+constexpr int kKinds = 5;                        // mr1, mr3, mr2, mf1, mf23
+constexpr int kFlushTiles = 16;                  // FP32 -> FP64 flush period (N tiles)
+constexpr unsigned long long kWaitNs = 2000000000ull;  // 2 s budget per wait
+
+struct Params {
+    int nf;          // grid size
+    int nm;          // kept modes
+    int Mp;          // rows per frequency in U (nm^2 rounded up to 128)
+    int MT;          // Mp / 128
+    int nk;          // K chunks (Kp / 64)
+    int n_ntiles;    // ceil(nf / NC)
+    int wmode;       // kWeightClassicVect or kWeightUniform
+    double wval;
+    const float2 *Hg;  // [nf][NMT]  H_j(w_c)
+    const float2 *Hs;  // [2nf-1][NMT]  H_j(w_r + w_c), s = r + c
+    double *part;      // [grid][kKinds][NMT][128]
+    int *err;
+};
+
+__device__ __forceinline__ uint32_t su32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ uint64_t gtime() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *b, uint32_t n) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(su32(b)), "r"(n) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *b, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(su32(b)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t *b) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(su32(b)) : "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint64_t *b, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(su32(b)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Bounded wait.  Returns false if the budget ran out or another role already failed.
+__device__ __forceinline__ bool mbar_wait(uint64_t *b, uint32_t parity, int *err, int code) {
+    if (mbar_try(b, parity)) return true;
+    const uint64_t t0 = gtime();
+    for (uint32_t it = 1;; ++it) {
+        if (mbar_try(b, parity)) return true;
+        if ((it & 255u) == 0) {
+            if (*(volatile int *)err) return false;
+            if (gtime() - t0 > kWaitNs) {
+                atomicCAS(err, 0, code);
+                return false;
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ void tma_2d(void *dst, const CUtensorMap *tm, uint64_t *bar, int x, int y) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];" ::
+            "r"(su32(dst)),
+        "l"((uint64_t)tm), "r"(su32(bar)), "r"(x), "r"(y)
+        : "memory");
+}
+
+__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// Shared-memory matrix descriptor, K-major operand in the 128-byte swizzle layout written
+// by TMA: 8-row groups 1024 bytes apart (SBO), leading offset unused, descriptor version 1.
+__device__ __forceinline__ uint64_t sdesc(uint32_t saddr) {
+    return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)(1024u >> 4) << 32) | (1ull << 46) | (2ull << 61);
+}
+
+// Instruction descriptor: kind::f16, A = B = bf16, D = f32, both K-major, M = 128, N = 128.
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kBN >> 3) << 17) | ((uint32_t)(kBM >> 4) << 24);
+
+__device__ __forceinline__ void mma(uint32_t d, uint64_t a, uint64_t b, uint32_t acc) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
+        "l"(a), "l"(b), "r"(kIdesc), "r"(acc)
+        : "memory");
+}
+__device__ __forceinline__ void mma_commit(uint64_t *b) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(su32(b)) : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t *v) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+        "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]), "=r"(v[8]),
+          "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]), "=r"(v[16]),
+          "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]),
+          "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+        : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+__device__ __forceinline__ float2 conjf2(float2 a) { return make_float2(a.x, -a.y); }
+
+__device__ __forceinline__ float point_weight(const Params &p, int r, int c) {
+    if (p.wmode == kWeightClassicVect) {
+        const bool b1 = (r == 0 || r == p.nf - 1), b2 = (c == 0 || c == p.nf - 1);
+        return (float)(p.wval * ((b1 && b2) ? -0.5 : ((b1 || b2) ? 0.5 : 1.0)));
+    }
+    return (float)p.wval;
+}
+
+template <int NMT>
+__global__ void __launch_bounds__(192, 1)
+    k_bfm_mixed(const __grid_constant__ CUtensorMap tmUh, const __grid_constant__ CUtensorMap tmUl,
+                const __grid_constant__ CUtensorMap tmGh, const __grid_constant__ CUtensorMap tmGl,
+                const __grid_constant__ CUtensorMap tmSh, const __grid_constant__ CUtensorMap tmSl, const Params p) {
+    constexpr int NC = kBN / NMT;         // grid columns per N tile
+    constexpr int BROWS = NC * NMT;       // B rows loaded by TMA per tile
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint64_t *bars = (uint64_t *)(smem + kStages * kStageBytes);
+    uint64_t *full = bars, *empty = bars + kStages, *tfull = bars + 2 * kStages, *tempty = bars + 2 * kStages + 2;
+    uint64_t *done = bars + 2 * kStages + 4;
+    uint32_t *tmem_slot = (uint32_t *)(bars + 2 * kStages + 5);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int *err = p.err;
+
+    // Rows of the B tiles that TMA never writes (BROWS..127) are zero for the whole run.
+    for (int s = 0; s < kStages; ++s)
+        for (int t = 2; t < 6; ++t) {
+            uint8_t *tile = smem + s * kStageBytes + t * kTileBytes;
+            for (int x = threadIdx.x; x < (128 - BROWS) * 128 / 16; x += blockDim.x)
+                ((uint4 *)(tile + BROWS * 128))[x] = make_uint4(0, 0, 0, 0);
+        }
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kStages; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(&tfull[b], 1);
+            mbar_init(&tempty[b], 128);
+        }
+        mbar_init(done, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(su32(tmem_slot)) : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    const int mt = blockIdx.x % p.MT;
+    const int rstep = gridDim.x / p.MT;
+    const int r0 = blockIdx.x / p.MT;
+    const uint32_t tx_bytes = 2u * kTileBytes + 4u * (uint32_t)(BROWS * 128);
+
+    if (warp == 0) {
+        // ---------------- TMA producer ----------------
+        if (lane == 0) {
+            uint32_t it = 0;
+            bool ok = true;
+            for (int r = r0; r < p.nf && ok; r += rstep)
+                for (int nt = 0; nt < p.n_ntiles && ok; ++nt)
+                    for (int kc = 0; kc < p.nk && ok; ++kc, ++it) {
+                        const int s = it % kStages;
+                        const uint32_t ph = (it / kStages) & 1u;
+                        if (!mbar_wait(&empty[s], ph ^ 1u, err, 1)) { ok = false; break; }
+                        uint8_t *st = smem + s * kStageBytes;
+                        mbar_expect_tx(&full[s], tx_bytes);
+                        const int x = kc * kBK;
+                        const int yu = r * p.Mp + mt * kBM;
+                        tma_2d(st + 0 * kTileBytes, &tmUh, &full[s], x, yu);
+                        tma_2d(st + 1 * kTileBytes, &tmUl, &full[s], x, yu);
+                        const int yg = nt * BROWS;
+                        tma_2d(st + 2 * kTileBytes, &tmGh, &full[s], x, yg);
+                        tma_2d(st + 3 * kTileBytes, &tmGl, &full[s], x, yg);
+                        const int ys = (r + nt * NC) * NMT;
+                        tma_2d(st + 4 * kTileBytes, &tmSh, &full[s], x, ys);
+                        tma_2d(st + 5 * kTileBytes, &tmSl, &full[s], x, ys);
+                    }
+            // Let the copies already issued land before the CTA can leave (bounded).
+            const uint32_t last = it;
+            for (uint32_t q = (last > (uint32_t)kStages ? last - kStages : 0); q < last; ++q) {
+                const int s = q % kStages;
+                const uint32_t ph = (q / kStages) & 1u;
+                const uint64_t t0 = gtime();
+                while (!mbar_try(&full[s], ph) && gtime() - t0 < kWaitNs) {
+                }
+            }
+        }
+        __syncwarp();
+    } else if (warp == 1) {
+        // ---------------- MMA issuer ----------------
+        if (lane == 0) {
+            uint32_t it = 0, tile = 0;
+            bool ok = true;
+            for (int r = r0; r < p.nf && ok; r += rstep)
+                for (int nt = 0; nt < p.n_ntiles && ok; ++nt, ++tile) {
+                    const int buf = tile & 1;
+                    const uint32_t tph = (tile >> 1) & 1u;
+                    if (!mbar_wait(&tempty[buf], tph ^ 1u, err, 2)) { ok = false; break; }
+                    fence_after();
+                    const uint32_t d1 = tmem + buf * 256, d3 = d1 + 128;
+                    for (int kc = 0; kc < p.nk; ++kc, ++it) {
+                        const int s = it % kStages;
+                        const uint32_t ph = (it / kStages) & 1u;
+                        if (!mbar_wait(&full[s], ph, err, 3)) { ok = false; break; }
+                        fence_after();
+                        const uint32_t base = su32(smem + s * kStageBytes);
+#pragma unroll
+                        for (int ks = 0; ks < kBK / 16; ++ks) {
+                            const uint32_t off = ks * 32;
+                            const uint64_t uh = sdesc(base + 0 * kTileBytes + off), ul = sdesc(base + 1 * kTileBytes + off);
+                            const uint64_t gh = sdesc(base + 2 * kTileBytes + off), gl = sdesc(base + 3 * kTileBytes + off);
+                            const uint64_t sh = sdesc(base + 4 * kTileBytes + off), sl = sdesc(base + 5 * kTileBytes + off);
+                            const uint32_t acc = (kc > 0 || ks > 0) ? 1u : 0u;
+                            mma(d1, uh, gh, acc);
+                            mma(d1, uh, gl, 1u);
+                            mma(d1, ul, gh, 1u);
+                            mma(d3, uh, sh, acc);
+                            mma(d3, uh, sl, 1u);
+                            mma(d3, ul, sh, 1u);
+                        }
+                        mma_commit(&empty[s]);  // stage free once these MMAs have read it
+                    }
+                    if (!ok) break;
+                    mma_commit(&tfull[buf]);  // accumulators ready for the epilogue
+                }
+            // Every MMA issued so far completes before TMEM is released.
+            mma_commit(done);
+            const uint64_t t0 = gtime();
+            while (!mbar_try(done, 0) && gtime() - t0 < kWaitNs) {
+            }
+        }
+        __syncwarp();
+    } else {
+        // ---------------- epilogue: FRF x weight, reduce to moments ----------------
+        const int quarter = warp & 3;
+        const int row = quarter * 32 + lane;          // TMEM lane = row of the M tile
+        const int grow = mt * kBM + row;               // row of U(f_r): a * nm + b
+        const bool vrow = grow < p.nm * p.nm;
+        const int a = vrow ? grow / p.nm : 0, b = vrow ? grow % p.nm : 0;
+        const uint32_t lane_base = tmem + ((uint32_t)(quarter * 32) << 16);
+        double *part = p.part + (size_t)blockIdx.x * kKinds * NMT * 128 + row;
+        for (int k = 0; k < kKinds * NMT; ++k) part[(size_t)k * 128] = 0.0;
+        float acc[kKinds][NMT];
+#pragma unroll
+        for (int k = 0; k < kKinds; ++k)
+#pragma unroll
+            for (int j = 0; j < NMT; ++j) acc[k][j] = 0.f;
+        auto flush = [&]() {
+#pragma unroll
+            for (int k = 0; k < kKinds; ++k)
+#pragma unroll
+                for (int j = 0; j < NMT; ++j) {
+                    part[(size_t)(k * NMT + j) * 128] += (double)acc[k][j];
+                    acc[k][j] = 0.f;
+                }
+        };
+        uint32_t tile = 0;
+        bool ok = true;
+        for (int r = r0; r < p.nf && ok; r += rstep) {
+            const float2 hra = p.Hg[r * NMT + a];
+            for (int nt = 0; nt < p.n_ntiles; ++nt, ++tile) {
+                const int buf = tile & 1;
+                const uint32_t tph = (tile >> 1) & 1u;
+                // warp-uniform outcome: tcgen05.ld below is .sync.aligned
+                const bool got = __all_sync(0xffffffffu, mbar_wait(&tfull[buf], tph, err, 4));
+                if (!got) { ok = false; break; }
+                fence_after();
+                const int c0 = nt * NC;
+                // Two passes per 32-column chunk (D1, then D3) keep one chunk of TMEM values
+                // live at a time.  Per grid column c the row-dependent FRF factors are formed
+                // once (j == 0) from FP32 copies of FP64-evaluated FRF tables.
+#pragma unroll
+                for (int q = 0; q < kBN / 32; ++q) {
+#pragma unroll
+                    for (int pass = 0; pass < 2; ++pass) {
+                        uint32_t v[32];
+                        tmem_ld32(lane_base + buf * 256 + pass * 128 + q * 32, v);
+                        tmem_wait_ld();
+                        float2 PA = make_float2(0.f, 0.f), PB = PA;
+                        float wc = 0.f;
+                        bool cval = false;
+                        int cg = 0, sidx = 0;
+#pragma unroll
+                        for (int e = 0; e < 32; ++e) {
+                            const int col = q * 32 + e;
+                            const int c = col / NMT, j = col % NMT;
+                            if (c >= NC) continue;
+                            if (j == 0 || e == 0) {
+                                cg = c0 + c;
+                                cval = cg < p.nf;
+                                if (cval) {
+                                    sidx = r + cg;
+                                    wc = point_weight(p, r, cg);
+                                    const float2 hcb = p.Hg[cg * NMT + b];
+                                    if (pass == 0) {
+                                        const float2 t1 = cmul(hra, hcb);          // term 1 at (r, c)
+                                        PA = make_float2(wc * t1.x, wc * t1.y);
+                                    } else {
+                                        const float2 hsa = p.Hs[sidx * NMT + a];
+                                        const float2 hsb = p.Hs[sidx * NMT + b];
+                                        const float2 t3 = cmul(hcb, conjf2(hsa));  // term 3 at (r, c)
+                                        PA = make_float2(wc * t3.x, wc * t3.y);
+                                        const float2 t2 = cmul(hra, conjf2(hsb));  // term 2 at (c, r)
+                                        PB = make_float2(wc * t2.x, wc * t2.y);
+                                    }
+                                }
+                            }
+                            if (cval && j < p.nm) {
+                                const float x = __uint_as_float(v[e]);
+                                if (pass == 0) {
+                                    const float2 hs = p.Hs[sidx * NMT + j];
+                                    const float F1 = PA.x * hs.x + PA.y * hs.y;    // Re[P1 conj(H_j(s))]
+                                    acc[0][j] = fmaf(F1, x, acc[0][j]);
+                                    acc[3][j] = fmaf(wc, x, acc[3][j]);
+                                } else {
+                                    const float2 hr = p.Hg[r * NMT + j];
+                                    const float2 hc = p.Hg[cg * NMT + j];
+                                    const float F3 = hr.x * PA.x - hr.y * PA.y;    // Re[H_j(w_r) P3]
+                                    const float F2 = hc.x * PB.x - hc.y * PB.y;    // Re[H_j(w_c) P2]
+                                    acc[1][j] = fmaf(F3, x, acc[1][j]);
+                                    acc[2][j] = fmaf(F2, x, acc[2][j]);
+                                    acc[4][j] = fmaf(wc, x, acc[4][j]);
+                                }
+                            }
+                        }
+                    }
+                }
+                fence_before();
+                mbar_arrive(&tempty[buf]);
+                if ((nt + 1) % kFlushTiles == 0) flush();
+            }
+            flush();
+        }
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem) : "memory");
+}
+
+// ------------------------------------------------------------------------------------
+// Operand preparation (FP64 -> bf16 hi/lo).
+// ------------------------------------------------------------------------------------
+__device__ __forceinline__ void split_bf16(double u, __nv_bfloat16 &hi, __nv_bfloat16 &lo) {
+    hi = __double2bfloat16(u);
+    lo = __double2bfloat16(u - (double)__bfloat162float(hi));
+}
+
+// U[(r*Mp + a*nm + b)][k] = Q[k][a] * A(f_r)[k][b]   (rows >= nm^2 and k >= K are zero)
+__global__ void k_prep_u(int nm, int K, int Kp, int Mp, const double *__restrict__ A, const double *__restrict__ Q,
+                         __nv_bfloat16 *__restrict__ Uh, __nv_bfloat16 *__restrict__ Ul) {
+    const int r = blockIdx.x, k0 = blockIdx.y * 64;
+    __shared__ double As[64][33], Qs[64][33];
+    const double *Ar = A + (size_t)r * K * nm;
+    for (int e = threadIdx.x; e < 64 * nm; e += blockDim.x) {
+        const int kk = e / nm, m = e % nm, k = k0 + kk;
+        As[kk][m] = k < K ? Ar[(size_t)k * nm + m] : 0.0;
+        Qs[kk][m] = k < K ? Q[(size_t)k * nm + m] : 0.0;
+    }
+    __syncthreads();
+    const int nm2 = nm * nm;
+    for (int e = threadIdx.x; e < Mp * 64; e += blockDim.x) {
+        const int row = e / 64, kk = e % 64;
+        double u = 0.0;
+        if (row < nm2) u = Qs[kk][row / nm] * As[kk][row % nm];
+        __nv_bfloat16 hi, lo;
+        split_bf16(u, hi, lo);
+        const size_t o = ((size_t)r * Mp + row) * Kp + k0 + kk;
+        Uh[o] = hi;
+        Ul[o] = lo;
+    }
+}
+
+// T[(t*NMT + j)][k] = A(src(t))[k][j]; src(t) < 0 gives a zero row (j >= nm too).
+__global__ void k_prep_b(int nm, int NMT, int K, int Kp, int nrows, int nf, int n_pad, int trunc, int sum_base,
+                         int is_sum, const double *__restrict__ A, __nv_bfloat16 *__restrict__ Th,
+                         __nv_bfloat16 *__restrict__ Tl) {
+    const int t = blockIdx.x, k0 = blockIdx.y * 64;
+    int src = t;
+    if (is_sum) {
+        if (trunc) {
+            const int c = t - n_pad;
+            src = (c >= 0 && c < nf) ? c : -1;
+        } else {
+            src = sum_base + t;
+        }
+    }
+    __shared__ double As[64][33];
+    for (int e = threadIdx.x; e < 64 * nm; e += blockDim.x) {
+        const int kk = e / nm, m = e % nm, k = k0 + kk;
+        As[kk][m] = (src >= 0 && k < K) ? A[((size_t)src * K + k) * nm + m] : 0.0;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < NMT * 64; e += blockDim.x) {
+        const int j = e / 64, kk = e % 64;
+        const double u = j < nm ? As[kk][j] : 0.0;
+        __nv_bfloat16 hi, lo;
+        split_bf16(u, hi, lo);
+        const size_t o = ((size_t)t * NMT + j) * Kp + k0 + kk;
+        Th[o] = hi;
+        Tl[o] = lo;
+    }
+    (void)nrows;
+}
+
+// FRF tables in FP64, rounded once to FP32: Hg[c][j] = H_j(w_c), Hs[s][j] = H_j(w_r + w_c).
+__global__ void k_prep_h(int nf, int nm, int NMT, const double *__restrict__ f, FrfPar frf, float2 *__restrict__ Hg,
+                         float2 *__restrict__ Hs) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int ng = nf * NMT, ns = (2 * nf - 1) * NMT;
+    if (t < ng) {
+        const int c = t / NMT, j = t % NMT;
+        double hr = 0, hi = 0;
+        if (j < nm) frf_eval(frf.M[j], frf.K[j], frf.C[j], f[c] * kPi2, hr, hi);
+        Hg[t] = make_float2((float)hr, (float)hi);
+    } else if (t < ng + ns) {
+        const int u = t - ng, s = u / NMT, j = u % NMT;
+        const int r = s / 2, c = s - r;
+        double hr = 0, hi = 0;
+        if (j < nm) frf_eval(frf.M[j], frf.K[j], frf.C[j], f[r] * kPi2 + f[c] * kPi2, hr, hi);
+        Hs[u] = make_float2((float)hr, (float)hi);
+    }
+}
+
+// m3[m + nm n + nm^2 o] from the per-CTA FP64 partials: three term contributions each.
+__global__ void k_mixed_reduce(int nm, int NMT, int MT, int grid, const double *__restrict__ part,
+                               double *__restrict__ m3mf, double *__restrict__ m3mr) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nm3 = nm * nm * nm;
+    if (x >= nm3) return;
+    const int m = x % nm, n = (x / nm) % nm, o = x / (nm * nm);
+    auto sum = [&](int kind, int a, int b, int j) {
+        const int R = a * nm + b, mtile = R / 128, lane = R % 128;
+        double s = 0.0;
+        for (int g = mtile; g < grid; g += MT) s += part[(((size_t)g * kKinds + kind) * NMT + j) * 128 + lane];
+        return s;
+    };
+    const double mr = sum(0, m, n, o) + sum(1, o, n, m) + sum(2, n, o, m);
+    const double mf = sum(3, m, n, o) + sum(4, o, n, m) + sum(4, n, o, m);
+    m3mr[x] = 2.0 * mr;  // B_F = 2 * (term1 + term2 + term3)
+    m3mf[x] = 2.0 * mf;
+}
+
+typedef CUresult (*EncodeTiled)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiled encoder() {
+    static EncodeTiled fn = nullptr;
+    if (!fn) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (EncodeTiled)p;
+    }
+    return fn;
+}
+
+// 2-D bf16 tensor [rows][Kp], box 64 x box_rows, 128-byte swizzle, zero fill out of range.
+static bool make_map(CUtensorMap *m, void *base, uint64_t Kp, uint64_t rows, uint32_t box_rows) {
+    EncodeTiled enc = encoder();
+    if (!enc) return false;
+    cuuint64_t dims[2] = {Kp, rows};
+    cuuint64_t strides[1] = {Kp * 2};
+    cuuint32_t box[2] = {(cuuint32_t)kBK, box_rows};
+    cuuint32_t es[2] = {1, 1};
+    return enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+               CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) ==
+           CUDA_SUCCESS;
+}
+
+template <int NMT>
+static cudaError_t launch_gemm(cudaStream_t st, const CUtensorMap *maps, const Params &p, int grid) {
+    const size_t smem = (size_t)kStages * kStageBytes + 1024 + 256;
+    cudaError_t e = cudaFuncSetAttribute(k_bfm_mixed<NMT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k_bfm_mixed<NMT><<<grid, 192, smem, st>>>(maps[0], maps[1], maps[2], maps[3], maps[4], maps[5], p);
+    return cudaGetLastError();
+}
+
+}  // namespace mixed
 
 int Engine::contract_mixed(const PointSrc &ps, long long npts, double *m3mf, double *m3mr) {
-    (void)ps; (void)npts; (void)m3mf; (void)m3mr;
-    return fail(BSA_ERR_UNSUPPORTED, "BF16x3 contraction not available in this build");
+    using namespace mixed;
+    (void)npts;
+    const int nf = ps.nf, nm = nme;
+    if (nm > 32) return fail(BSA_ERR_UNSUPPORTED, "BF16x3 contraction supports at most 32 kept modes");
+    const int NMT = nm <= 8 ? 8 : nm <= 16 ? 16 : nm <= 24 ? 24 : 32;
+    const int NC = kBN / NMT;
+    const int Kp = ((K + kBK - 1) / kBK) * kBK;
+    const int Mp = ((nm * nm + kBM - 1) / kBM) * kBM;
+    const int MT = Mp / kBM;
+    const int ns = 2 * nf - 1;
+    int dev = 0, nsm = 0;
+    cudaError_t e;
+    if ((e = cudaGetDevice(&dev)) || (e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev)))
+        return cuda_fail(e, "device query");
+    int grid = (nsm / MT) * MT;
+    if (grid < MT) grid = MT;
+    const size_t uel = (size_t)nf * Mp * Kp, gel = (size_t)nf * NMT * Kp, sel = (size_t)ns * NMT * Kp;
+    const size_t bytesA = 2 * uel * 2, bytesB = 2 * (gel + sel) * 2;
+    const size_t bytesH = sizeof(float2) * (size_t)(nf + ns) * NMT;
+    const size_t bytesP = sizeof(double) * (size_t)grid * kKinds * NMT * 128;
+    if ((e = dMixA.reserve(bytesA)) || (e = dMixB.reserve(bytesB)) || (e = dMixH.reserve(bytesH + 256)) ||
+        (e = dMixPart.reserve(bytesP + 256)))
+        return cuda_fail(e, "allocating BF16x3 operands");
+    __nv_bfloat16 *Uh = dMixA.as<__nv_bfloat16>(), *Ul = Uh + uel;
+    __nv_bfloat16 *Gh = dMixB.as<__nv_bfloat16>(), *Gl = Gh + gel, *Sh = Gl + gel, *Sl = Sh + sel;
+    float2 *Hg = dMixH.as<float2>(), *Hs = Hg + (size_t)nf * NMT;
+    int *derr = (int *)((char *)dMixPart.p + bytesP);
+    if ((e = cudaEventRecord(ev2, stream))) return cuda_fail(e, "event");
+    if ((e = cudaMemsetAsync(derr, 0, sizeof(int), stream))) return cuda_fail(e, "memset");
+    {
+        dim3 gu(nf, Kp / 64);
+        k_prep_u<<<gu, 256, 0, stream>>>(nm, K, Kp, Mp, dA.as<double>(), dQ.as<double>(), Uh, Ul);
+        dim3 gg(nf, Kp / 64), gs(ns, Kp / 64);
+        k_prep_b<<<gg, 256, 0, stream>>>(nm, NMT, K, Kp, nf, nf, ps.n_pad, ps.trunc, ps.sum_base, 0, dA.as<double>(), Gh, Gl);
+        k_prep_b<<<gs, 256, 0, stream>>>(nm, NMT, K, Kp, ns, nf, ps.n_pad, ps.trunc, ps.sum_base, 1, dA.as<double>(), Sh, Sl);
+        const int nh = (nf + ns) * NMT;
+        k_prep_h<<<(nh + 255) / 256, 256, 0, stream>>>(nf, nm, NMT, ps.fgrid, frf(), Hg, Hs);
+        if ((e = cudaGetLastError())) return cuda_fail(e, "BF16x3 operand preparation");
+        kernels += 4;
+    }
+    CUtensorMap maps[6];
+    if (!make_map(&maps[0], Uh, Kp, (uint64_t)nf * Mp, kBM) || !make_map(&maps[1], Ul, Kp, (uint64_t)nf * Mp, kBM) ||
+        !make_map(&maps[2], Gh, Kp, (uint64_t)nf * NMT, NC * NMT) || !make_map(&maps[3], Gl, Kp, (uint64_t)nf * NMT, NC * NMT) ||
+        !make_map(&maps[4], Sh, Kp, (uint64_t)ns * NMT, NC * NMT) || !make_map(&maps[5], Sl, Kp, (uint64_t)ns * NMT, NC * NMT))
+        return fail(BSA_ERR_CUDA, "cuTensorMapEncodeTiled failed");
+    Params prm{};
+    prm.nf = nf;
+    prm.nm = nm;
+    prm.Mp = Mp;
+    prm.MT = MT;
+    prm.nk = Kp / kBK;
+    prm.n_ntiles = (nf + NC - 1) / NC;
+    prm.wmode = ps.wmode;
+    prm.wval = ps.wval;
+    prm.Hg = Hg;
+    prm.Hs = Hs;
+    prm.part = dMixPart.as<double>();
+    prm.err = derr;
+    if ((e = cudaEventRecord(evg0, stream))) return cuda_fail(e, "event");
+    switch (NMT) {
+    case 8: e = launch_gemm<8>(stream, maps, prm, grid); break;
+    case 16: e = launch_gemm<16>(stream, maps, prm, grid); break;
+    case 24: e = launch_gemm<24>(stream, maps, prm, grid); break;
+    default: e = launch_gemm<32>(stream, maps, prm, grid); break;
+    }
+    if (e) return cuda_fail(e, "BF16x3 tcgen05 contraction kernel");
+    if ((e = cudaEventRecord(evg1, stream))) return cuda_fail(e, "event");
+    const long long nm3 = (long long)nm * nm * nm;
+    if ((e = dOut.reserve(sizeof(double) * (3 * (size_t)nm * nm + 2 * (size_t)nm3)))) return cuda_fail(e, "out");
+    double *o = dOut.as<double>() + 3 * (size_t)nm * nm;
+    k_mixed_reduce<<<(unsigned)((nm3 + 127) / 128), 128, 0, stream>>>(nm, NMT, MT, grid, prm.part, o, o + nm3);
+    if ((e = cudaGetLastError())) return cuda_fail(e, "BF16x3 reduction");
+    kernels += 2;
+    std::vector<double> h(2 * (size_t)nm3);
+    int herr = 0;
+    if ((e = cudaMemcpyAsync(h.data(), o, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, stream)) ||
+        (e = cudaMemcpyAsync(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost, stream)) ||
+        (e = cudaEventRecord(ev1, stream)) || (e = cudaStreamSynchronize(stream)))
+        return cuda_fail(e, "BF16x3 contraction");
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ev2, ev1);
+    last_ms_contraction = ms;
+    cudaEventElapsedTime(&ms, evg0, evg1);
+    last_ms_gemm = ms;
+    d2h += (double)sizeof(double) * h.size() + sizeof(int);
+    if (herr) return fail(BSA_ERR_TIMEOUT, "BF16x3 kernel: a pipeline wait ran out of its budget (role %d)", herr);
+    if (m3mf) std::memcpy(m3mf, h.data(), sizeof(double) * nm3);
+    if (m3mr) std::memcpy(m3mr, h.data() + nm3, sizeof(double) * nm3);
+    return BSA_OK;
 }
 
 int Engine::run_mesher(double *m3mf, double *m3mr) {

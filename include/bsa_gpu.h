@@ -175,7 +175,10 @@ int bsa_gpu_mshMoments(const double *fi, const double *fj, const double *w, int 
 typedef struct {
     double ms_total;          /* device time of the last run (CUDA events)           */
     double ms_contraction;    /* device time of the contraction kernels               */
+    double ms_gemm;           /* device time of the dominant contraction kernel alone  */
     double points;            /* (f1,f2) points at which B_R was produced             */
+    double h2d_bytes;         /* host-to-device bytes copied by the last run          */
+    double d2h_bytes;         /* device-to-host bytes copied by the last run          */
     int kernels;              /* kernels launched by the last run                     */
     int precision;            /* BSA_PREC_* used                                      */
 } bsa_gpu_stats;

@@ -1,0 +1,86 @@
+"""The split-precision (BF16x3, FP32 accumulation) tcgen05 contraction against the plain
+FP64 GPU path on the same inputs.
+
+Tolerances (the mixed-precision bar of the BFM path): third moments within 1e-4 relative
+(max-norm over the tensor) and response skewness within 1e-3 relative.
+"""
+import numpy as np
+import pytest
+
+from bsalib_gb300 import api
+from bsalib_gb300.problem import cantilever_tower, tall_building
+
+pytestmark = pytest.mark.gpu
+TOL_M3 = 1e-4
+TOL_SK = 1e-3
+
+
+def rel(a, b):
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+def both(prob, truncation=True):
+    out = {}
+    for prec in (api.PREC_FP64, api.PREC_BF16X3):
+        s = api.BsaSession(prob, precision=prec, classic_truncation=truncation)
+        try:
+            r = s.run()
+            r["sk"] = s.skewness(r["m2mr_cls"], r["m3mr_cls"])
+            r["stats"] = s.stats()
+        finally:
+            s.close()
+        out[prec] = r
+    return out[api.PREC_FP64], out[api.PREC_BF16X3]
+
+
+CASES = [
+    ("tower_nm4", cantilever_tower(nfreqs=17, df=0.25, nodes=30)),
+    ("bldg_nm6_2tc", tall_building(nodes=40, modes=6, nfreqs=11, df=0.4, seed=11)),
+    ("bldg_nm12", tall_building(nodes=64, modes=12, nfreqs=21, df=0.2, seed=3)),
+    ("bldg_nm24", tall_building(nodes=100, modes=24, nfreqs=25, df=0.16, seed=5)),
+    ("bldg_nm30", tall_building(nodes=50, modes=30, nfreqs=9, df=0.5, seed=8)),
+]
+
+
+@pytest.mark.parametrize("name,prob", CASES, ids=[c[0] for c in CASES])
+def test_mixed_matches_fp64(name, prob):
+    ref, mix = both(prob)
+    assert mix["stats"].precision == api.PREC_BF16X3
+    assert rel(mix["m3mf_cls"], ref["m3mf_cls"]) < TOL_M3
+    assert rel(mix["m3mr_cls"], ref["m3mr_cls"]) < TOL_M3
+    assert rel(mix["sk"], ref["sk"]) < TOL_SK
+    # the second-order path is FP64 in both
+    assert np.array_equal(mix["m2mr_cls"], ref["m2mr_cls"])
+
+
+def test_mixed_analytic_sum_frequency():
+    prob = tall_building(nodes=48, modes=8, nfreqs=13, df=0.3, seed=21)
+    ref, mix = both(prob, truncation=False)
+    assert rel(mix["m3mr_cls"], ref["m3mr_cls"]) < TOL_M3
+
+
+def test_mixed_uniform_weights():
+    prob = tall_building(nodes=32, modes=10, nfreqs=9, df=0.3, seed=22)
+    prob.settings.scalar = 1
+    ref, mix = both(prob)
+    assert rel(mix["m3mr_cls"], ref["m3mr_cls"]) < TOL_M3
+    assert rel(mix["m3mf_cls"], ref["m3mf_cls"]) < TOL_M3
+
+
+def test_mixed_building_129_grid():
+    """The 400-node, 24-mode, two-component building on a 129 x 129 grid."""
+    prob = tall_building(nfreqs=65, df=4.0 / 64)
+    ref, mix = both(prob)
+    assert rel(mix["m3mr_cls"], ref["m3mr_cls"]) < TOL_M3
+    assert rel(mix["sk"], ref["sk"]) < TOL_SK
+
+
+def test_mixed_is_deterministic():
+    prob = tall_building(nodes=40, modes=16, nfreqs=17, df=0.25, seed=30)
+    s = api.BsaSession(prob, precision=api.PREC_BF16X3)
+    try:
+        a = s.run()["m3mr_cls"]
+        b = s.run()["m3mr_cls"]
+    finally:
+        s.close()
+    assert np.array_equal(a, b)
