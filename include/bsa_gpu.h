@@ -171,6 +171,27 @@ int bsa_gpu_mshBispectra(const double *fi, const double *fj, int npts, double *b
 int bsa_gpu_mshMoments(const double *fi, const double *fj, const double *w, int npts,
                        double *m3mf, double *m3mr);
 
+/* No counterpart in the reference.  For callers that cannot allocate device memory (a host
+ * that passes buffers from its own pool or arena and forbids allocation behind its back):
+ * the weighted third moments of bsa_gpu_mshMoments over a point set, with every argument a
+ * caller-owned DEVICE pointer and no cudaMalloc / cudaFree or other allocating call inside.
+ *   A   [rows][K][nm]  per-frequency factors A(f) = S(f) L  (k = itc*nnl + loaded node)
+ *   Q   [K][nm]        projected quadratic coefficients
+ *   ix, iy, iz [npts]  rows of A at f1, f2, f1+f2 (iz < 0: S(f1+f2) taken as zero)
+ *   f1, f2, w [npts]   point frequencies [Hz] and integration weights
+ *   Mm, Km, Cm [nm]    generalised mass, stiffness, damping of the kept modes
+ *   m3mf, m3mr [nm^3]  outputs (m fastest); stream: a cudaStream_t (NULL = legacy stream).
+ * Its scratch (per-group partial sums) is a fixed 4 MiB device array held by every GPU
+ * that loads the library until the process exits; nm is limited to 64, where 2*nm^3
+ * doubles fill it.  The first call on each device resolves the array's device address
+ * (cudaGetSymbolAddress) and should be made before any stream capture.  All calls share
+ * the array: calls that overlap on the GPU race and must be serialised by the caller.
+ * Returns BSA_OK or BSA_ERR_ARG / BSA_ERR_CUDA (message in bsa_lastError). */
+int bsa_gpu_pointMomentsNoAlloc(const double *A, int K, int nm, const double *Q, const int *ix,
+                                const int *iy, const int *iz, const double *f1, const double *f2,
+                                const double *w, int npts, const double *Mm, const double *Km,
+                                const double *Cm, double *m3mf, double *m3mr, void *stream);
+
 /* Timing and counters of the last run. */
 typedef struct {
     double ms_total;          /* device time of the last run (CUDA events)           */
