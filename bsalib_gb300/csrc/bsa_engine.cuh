@@ -74,7 +74,7 @@ struct Engine {
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr;
     DevBuf dL, dQ, dLogc, dPsdPar, dFrfM, dFrfK, dFrfC, dFreq, dS, dA, dPartF, dPartR, dOut, dPsdF, dWf, dPts,
-        dPtsD, dBF, dBR, dMixA, dMixB, dMixH, dMixPart;
+        dPtsD, dBF, dBR, dMixA, dMixB, dMixH, dMixPart, dA32;
 
     // stats
     double last_ms = 0, last_ms_contraction = 0, last_ms_gemm = 0, last_points = 0;
@@ -90,7 +90,7 @@ struct Engine {
     int validate();
     int upload_problem();
     FrfPar frf() const;
-    int build_atable(const std::vector<double> &freqs);
+    int build_atable(const std::vector<double> &freqs, bool fp32 = false);
     int classic_grid(std::vector<double> &f);
     int run_classic(double *m2mf, double *m2mr, double *m2o2mr, double *m3mf, double *m3mr, double *bf_host,
                     double *br_host, std::vector<double> *grid_out);

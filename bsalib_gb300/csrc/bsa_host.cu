@@ -65,7 +65,7 @@ void Engine::reset_inputs() {
 
 void Engine::free_device() {
     for (DevBuf *b : {&dL, &dQ, &dLogc, &dPsdPar, &dFrfM, &dFrfK, &dFrfC, &dFreq, &dS, &dA, &dPartF, &dPartR,
-                      &dOut, &dPsdF, &dWf, &dPts, &dPtsD, &dBF, &dBR, &dMixA, &dMixB, &dMixH, &dMixPart})
+                      &dOut, &dPsdF, &dWf, &dPts, &dPtsD, &dBF, &dBR, &dMixA, &dMixB, &dMixH, &dMixPart, &dA32})
         b->release();
     if (stream) cudaStreamDestroy(stream);
     stream = nullptr;
@@ -248,20 +248,26 @@ int Engine::upload_problem() {
 
 FrfPar Engine::frf() const { return FrfPar{dFrfM.as<double>(), dFrfK.as<double>(), dFrfC.as<double>()}; }
 
-// Nodal PSD + A(f) for a host list of frequencies, into dA rows [row0, row0 + nf).
-int Engine::build_atable(const std::vector<double> &freqs) {
+// Nodal PSD + A(f) for a host list of frequencies, into dA (FP64) or dA32 (FP32) rows.
+int Engine::build_atable(const std::vector<double> &freqs, bool fp32) {
     const int nf = (int)freqs.size();
     const int ntc = (int)set.tc.size();
     cudaError_t e;
     if ((e = upload(dFreq, freqs, stream))) return cuda_fail(e, "uploading frequencies");
     if ((e = dS.reserve(sizeof(double) * (size_t)nf * ntc * in.nnl))) return cuda_fail(e, "allocating S");
-    if ((e = dA.reserve(sizeof(double) * (size_t)nf * K * nme))) return cuda_fail(e, "allocating A");
     if ((e = launch_nodal_psd(stream, nf, dFreq.as<double>(), ntc, set.tc.data(), in.nnl, dPsdPar.as<PsdNode>(),
                               in.psd_type, set.defsc, dS.as<double>())))
         return cuda_fail(e, "nodal PSD kernel");
-    if ((e = launch_atable(stream, nf, dFreq.as<double>(), ntc, in.nnl, nme, dLogc.as<double>(), dS.as<double>(),
-                           dL.as<double>(), dA.as<double>())))
-        return cuda_fail(e, "A-table kernel");
+    if (fp32) {
+        if ((e = dA32.reserve(sizeof(float) * (size_t)nf * K * nme))) return cuda_fail(e, "allocating A");
+        e = launch_atable32(stream, nf, dFreq.as<double>(), ntc, in.nnl, nme, dLogc.as<double>(), dS.as<double>(),
+                            dL.as<double>(), dA32.as<float>());
+    } else {
+        if ((e = dA.reserve(sizeof(double) * (size_t)nf * K * nme))) return cuda_fail(e, "allocating A");
+        e = launch_atable(stream, nf, dFreq.as<double>(), ntc, in.nnl, nme, dLogc.as<double>(), dS.as<double>(),
+                          dL.as<double>(), dA.as<double>());
+    }
+    if (e) return cuda_fail(e, "A-table kernel");
     kernels += 2;
     return BSA_OK;
 }
@@ -334,9 +340,12 @@ int Engine::run_classic(double *m2mf, double *m2mr, double *m2o2mr, double *m3mf
         const double d = f[1] - f[0];
         for (int s = 0; s < 2 * nf - 1; ++s) ftab.push_back(2.0 * f[0] + s * d);
     }
+    // The split-precision contraction reduces to moments only; it reads an FP32 A table.
+    const bool mixed = precision == BSA_PREC_BF16X3 && !bf_host && !br_host;
+    if (mixed && nme > 32) return fail(BSA_ERR_UNSUPPORTED, "BF16x3 contraction supports at most 32 kept modes");
     cudaError_t e;
     if ((e = cudaEventRecord(ev0, stream))) return cuda_fail(e, "event");
-    if ((rc = build_atable(ftab))) return rc;
+    if ((rc = build_atable(ftab, mixed))) return rc;
     const int nm2 = nme * nme;
     if (set.ipsd && (m2mf || m2mr || m2o2mr)) {
         std::vector<double> wf(nf, scalar ? delta : delta);
@@ -345,9 +354,11 @@ int Engine::run_classic(double *m2mf, double *m2mr, double *m2o2mr, double *m3mf
         if ((e = dPsdF.reserve(sizeof(double) * (size_t)nf * nm2))) return cuda_fail(e, "psd");
         if ((e = dOut.reserve(sizeof(double) * (3 * (size_t)nm2 + 2 * (size_t)nm3))))
             return cuda_fail(e, "out");
-        if ((e = launch_force_psd(stream, nf, (int)set.tc.size(), in.nnl, nme, dL.as<double>(), dA.as<double>(),
-                                  dPsdF.as<double>())))
-            return cuda_fail(e, "force PSD kernel");
+        e = mixed ? launch_force_psd32(stream, nf, (int)set.tc.size(), in.nnl, nme, dL.as<double>(),
+                                       dA32.as<float>(), dPsdF.as<double>())
+                  : launch_force_psd(stream, nf, (int)set.tc.size(), in.nnl, nme, dL.as<double>(), dA.as<double>(),
+                                     dPsdF.as<double>());
+        if (e) return cuda_fail(e, "force PSD kernel");
         double *o = dOut.as<double>();
         if ((e = launch_m2(stream, nf, nme, dFreq.as<double>(), dWf.as<double>(), dPsdF.as<double>(), frf(), o,
                            o + nm2, o + 2 * nm2)))
@@ -374,7 +385,7 @@ int Engine::run_classic(double *m2mf, double *m2mr, double *m2o2mr, double *m3mf
         ps.wval = delta * delta;
         ps.fgrid = dFreq.as<double>();
         const long long npts = (long long)nf * nf;
-        rc = contract(ps, npts, m3mf, m3mr, bf_host, br_host);
+        rc = mixed ? contract_mixed(ps, npts, m3mf, m3mr) : contract(ps, npts, m3mf, m3mr, bf_host, br_host);
         if (rc) return rc;
         last_points = (double)npts;
     }
@@ -390,8 +401,6 @@ int Engine::contract(const PointSrc &ps, long long npts, double *m3mf, double *m
                      double *br_host) {
     const long long nm3 = (long long)nme * nme * nme;
     cudaError_t e;
-    if (precision == BSA_PREC_BF16X3 && ps.mode == kPointsGrid && !bf_host && !br_host)
-        return contract_mixed(ps, npts, m3mf, m3mr);
     const int G = bfm_fp64_groups(npts, nme);
     if ((e = dPartF.reserve(sizeof(double) * (size_t)G * nm3)) || (e = dPartR.reserve(sizeof(double) * (size_t)G * nm3)))
         return cuda_fail(e, "allocating partial sums");

@@ -147,19 +147,85 @@ cudaError_t launch_atable(cudaStream_t st, int nf, const double *f, int ntc, int
     return cudaGetLastError();
 }
 
+// Same factor in FP32 (operand source of the BF16x3 contraction, whose operands are
+// rounded to bf16 hi + lo anyway): FP32 exp and FMAs instead of the slow FP64 pipe.
+__global__ __launch_bounds__(256) void k_atable32(int nf, const double *__restrict__ f, int ntc, int nnl,
+                                                  int nm, const double *__restrict__ logc,
+                                                  const double *__restrict__ S,
+                                                  const double *__restrict__ L, float *__restrict__ A) {
+    const int fi = blockIdx.x / ntc, itc = blockIdx.x % ntc;
+    const int i0 = blockIdx.y * 32;
+    __shared__ float Gs[32][33];
+    __shared__ float Ls[32][65];
+    const float af = (float)fabs(f[fi]);
+    const double *Sf = S + ((size_t)fi * ntc + itc) * nnl;
+    const double *lc = logc + (size_t)itc * nnl * nnl;
+    const double *Lt = L + (size_t)itc * nnl * nm;
+    const int t = threadIdx.x, il = t >> 3, mg = t & 7;
+    float acc[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) acc[u] = 0.f;
+    for (int j0 = 0; j0 < nnl; j0 += 32) {
+        for (int e = t; e < 32 * 32; e += 256) {
+            const int ii = e >> 5, jj = e & 31, gi = i0 + ii, gj = j0 + jj;
+            float g = 0.f;
+            if (gi < nnl && gj < nnl) {
+                const float l = (float)lc[(size_t)gi * nnl + gj];
+                g = (af == 0.f) ? 1.f : expf(af * l);
+            }
+            Gs[ii][jj] = g;
+        }
+        for (int e = t; e < 32 * nm; e += 256) {
+            const int jj = e / nm, m = e % nm, gj = j0 + jj;
+            Ls[jj][m] = gj < nnl ? (float)(sqrt(Sf[gj]) * Lt[(size_t)gj * nm + m]) : 0.f;
+        }
+        __syncthreads();
+#pragma unroll 8
+        for (int jj = 0; jj < 32; ++jj) {
+            const float g = Gs[il][jj];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const int m = mg + 8 * u;
+                if (m < nm) acc[u] = fmaf(g, Ls[jj][m], acc[u]);
+            }
+        }
+        __syncthreads();
+    }
+    const int gi = i0 + il;
+    if (gi < nnl) {
+        const float si = (float)sqrt(Sf[gi]);
+        float *out = A + (((size_t)fi * ntc + itc) * nnl + gi) * nm;
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const int m = mg + 8 * u;
+            if (m < nm) out[m] = si * acc[u];
+        }
+    }
+}
+
+cudaError_t launch_atable32(cudaStream_t st, int nf, const double *f, int ntc, int nnl, int nm,
+                            const double *logc, const double *S, const double *L, float *A) {
+    if (nf == 0) return cudaSuccess;
+    if (nm > 64) return cudaErrorInvalidValue;
+    dim3 grid((unsigned)nf * ntc, (unsigned)((nnl + 31) / 32));
+    k_atable32<<<grid, 256, 0, st>>>(nf, f, ntc, nnl, nm, logc, S, L, A);
+    return cudaGetLastError();
+}
+
 // ------------------------------------------------------------------------------------
 // Second-order path: force PSD and m2 moments (functionsImpl.F90:1548-1560, 1653-1676;
 // BsaClassicImpl.F90:149-154, 197-210).
 // ------------------------------------------------------------------------------------
-__global__ void k_force_psd(int ntc, int nnl, int nm, const double *__restrict__ L,
-                            const double *__restrict__ A, double *__restrict__ psd) {
+template <class TA>
+__global__ void k_force_psd(int ntc, int nnl, int nm, const double *__restrict__ L, const TA *__restrict__ A,
+                            double *__restrict__ psd) {
     const int fi = blockIdx.x;
     const int nm2 = nm * nm, K = ntc * nnl;
-    const double *Af = A + (size_t)fi * K * nm;
+    const TA *Af = A + (size_t)fi * K * nm;
     for (int pr = threadIdx.x; pr < nm2; pr += blockDim.x) {
         const int n = pr % nm, o = pr / nm;
         double s = 0.0;
-        for (int k = 0; k < K; ++k) s = fma(L[(size_t)k * nm + o], Af[(size_t)k * nm + n], s);
+        for (int k = 0; k < K; ++k) s = fma(L[(size_t)k * nm + o], (double)Af[(size_t)k * nm + n], s);
         psd[(size_t)fi * nm2 + pr] = s;
     }
 }
@@ -167,19 +233,26 @@ __global__ void k_force_psd(int ntc, int nnl, int nm, const double *__restrict__
 cudaError_t launch_force_psd(cudaStream_t st, int nf, int ntc, int nnl, int nm, const double *L,
                              const double *A, double *psd) {
     if (nf == 0) return cudaSuccess;
-    k_force_psd<<<nf, 256, 0, st>>>(ntc, nnl, nm, L, A, psd);
+    k_force_psd<double><<<nf, 256, 0, st>>>(ntc, nnl, nm, L, A, psd);
     return cudaGetLastError();
 }
 
+cudaError_t launch_force_psd32(cudaStream_t st, int nf, int ntc, int nnl, int nm, const double *L,
+                               const float *A, double *psd) {
+    if (nf == 0) return cudaSuccess;
+    k_force_psd<float><<<nf, 256, 0, st>>>(ntc, nnl, nm, L, A, psd);
+    return cudaGetLastError();
+}
+
+// One block per (n, o) pair; threads stride over frequencies, fixed-order tree reduction.
 __global__ void k_m2(int nf, int nm, const double *__restrict__ f, const double *__restrict__ wf,
                      const double *__restrict__ psd, FrfPar frf, double *m2mf, double *m2mr,
                      double *m2o2mr) {
     const int nm2 = nm * nm;
-    const int pr = blockIdx.x * blockDim.x + threadIdx.x;
-    if (pr >= nm2) return;
+    const int pr = blockIdx.x;
     const int n = pr % nm, o = pr / nm;
     double sf = 0.0, sr = 0.0, so = 0.0;
-    for (int k = 0; k < nf; ++k) {
+    for (int k = threadIdx.x; k < nf; k += blockDim.x) {
         const double w = f[k] * kPi2;
         double hnr, hni, hor, hoi;
         frf_eval(frf.M[n], frf.K[n], frf.C[n], w, hnr, hni);
@@ -190,15 +263,26 @@ __global__ void k_m2(int nf, int nm, const double *__restrict__ f, const double 
         sr += wf[k] * pr_;
         so += wf[k] * (pr_ * w * w);
     }
-    if (m2mf) m2mf[pr] = sf;
-    if (m2mr) m2mr[pr] = sr;
-    if (m2o2mr) m2o2mr[pr] = so;
+    __shared__ double red[3][256];
+    red[0][threadIdx.x] = sf;
+    red[1][threadIdx.x] = sr;
+    red[2][threadIdx.x] = so;
+    __syncthreads();
+    for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+        if ((int)threadIdx.x < h)
+            for (int q = 0; q < 3; ++q) red[q][threadIdx.x] += red[q][threadIdx.x + h];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        if (m2mf) m2mf[pr] = red[0][0];
+        if (m2mr) m2mr[pr] = red[1][0];
+        if (m2o2mr) m2o2mr[pr] = red[2][0];
+    }
 }
 
 cudaError_t launch_m2(cudaStream_t st, int nf, int nm, const double *f, const double *wf,
                       const double *psd, FrfPar frf, double *m2mf, double *m2mr, double *m2o2mr) {
-    const int nm2 = nm * nm;
-    k_m2<<<(nm2 + 127) / 128, 128, 0, st>>>(nf, nm, f, wf, psd, frf, m2mf, m2mr, m2o2mr);
+    k_m2<<<nm * nm, 256, 0, st>>>(nf, nm, f, wf, psd, frf, m2mf, m2mr, m2o2mr);
     return cudaGetLastError();
 }
 

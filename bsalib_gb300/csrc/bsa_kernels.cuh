@@ -13,11 +13,17 @@ cudaError_t launch_nodal_psd(cudaStream_t st, int nf, const double *f, int ntc, 
 cudaError_t launch_atable(cudaStream_t st, int nf, const double *f, int ntc, int nnl, int nm,
                           const double *logc, const double *S, const double *L, double *A);
 
+// The same factor in FP32 (source of the split-precision contraction's operands).
+cudaError_t launch_atable32(cudaStream_t st, int nf, const double *f, int ntc, int nnl, int nm,
+                            const double *logc, const double *S, const double *L, float *A);
+
 // Force PSD on the grid psd[f][n + nm*o] = sum_k L[k][o] A[f][k][n]
 // (functionsImpl.F90:1548-1560), then the second-order moments
 // m2mf, m2mr (x Re[H_o conj H_n]), m2o2mr (x w^2) with per-frequency weights wf.
 cudaError_t launch_force_psd(cudaStream_t st, int nf, int ntc, int nnl, int nm, const double *L,
                              const double *A, double *psd);
+cudaError_t launch_force_psd32(cudaStream_t st, int nf, int ntc, int nnl, int nm, const double *L,
+                               const float *A, double *psd);
 cudaError_t launch_m2(cudaStream_t st, int nf, int nm, const double *f, const double *wf,
                       const double *psd, FrfPar frf, double *m2mf, double *m2mr, double *m2o2mr);
 

@@ -401,35 +401,37 @@ __device__ __forceinline__ void split_bf16(double u, __nv_bfloat16 &hi, __nv_bfl
     lo = __double2bfloat16(u - (double)__bfloat162float(hi));
 }
 
-// U[(r*Mp + a*nm + b)][k] = Q[k][a] * A(f_r)[k][b]   (rows >= nm^2 and k >= K are zero)
-__global__ void k_prep_u(int nm, int K, int Kp, int Mp, const double *__restrict__ A, const double *__restrict__ Q,
+// U[(r*Mp + a*nm + b)][k] = Q[k][a] * A(f_r)[k][b]   (rows >= nm^2 and k >= K are zero).
+// Each thread writes 8 consecutive k of one row as one 16-byte store per hi / lo table.
+__global__ void k_prep_u(int nm, int K, int Kp, int Mp, const float *__restrict__ A, const double *__restrict__ Q,
                          __nv_bfloat16 *__restrict__ Uh, __nv_bfloat16 *__restrict__ Ul) {
     const int r = blockIdx.x, k0 = blockIdx.y * 64;
     __shared__ double As[64][33], Qs[64][33];
-    const double *Ar = A + (size_t)r * K * nm;
+    const float *Ar = A + (size_t)r * K * nm;
     for (int e = threadIdx.x; e < 64 * nm; e += blockDim.x) {
         const int kk = e / nm, m = e % nm, k = k0 + kk;
-        As[kk][m] = k < K ? Ar[(size_t)k * nm + m] : 0.0;
+        As[kk][m] = k < K ? (double)Ar[(size_t)k * nm + m] : 0.0;
         Qs[kk][m] = k < K ? Q[(size_t)k * nm + m] : 0.0;
     }
     __syncthreads();
     const int nm2 = nm * nm;
-    for (int e = threadIdx.x; e < Mp * 64; e += blockDim.x) {
-        const int row = e / 64, kk = e % 64;
-        double u = 0.0;
-        if (row < nm2) u = Qs[kk][row / nm] * As[kk][row % nm];
-        __nv_bfloat16 hi, lo;
-        split_bf16(u, hi, lo);
-        const size_t o = ((size_t)r * Mp + row) * Kp + k0 + kk;
-        Uh[o] = hi;
-        Ul[o] = lo;
+    for (int e = threadIdx.x; e < Mp * 8; e += blockDim.x) {
+        const int row = e >> 3, kv = (e & 7) * 8;
+        __align__(16) __nv_bfloat16 hi[8], lo[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const double u = row < nm2 ? Qs[kv + q][row / nm] * As[kv + q][row % nm] : 0.0;
+            split_bf16(u, hi[q], lo[q]);
+        }
+        const size_t o = ((size_t)r * Mp + row) * Kp + k0 + kv;
+        *(uint4 *)(Uh + o) = *(const uint4 *)hi;
+        *(uint4 *)(Ul + o) = *(const uint4 *)lo;
     }
 }
 
 // T[(t*NMT + j)][k] = A(src(t))[k][j]; src(t) < 0 gives a zero row (j >= nm too).
-__global__ void k_prep_b(int nm, int NMT, int K, int Kp, int nrows, int nf, int n_pad, int trunc, int sum_base,
-                         int is_sum, const double *__restrict__ A, __nv_bfloat16 *__restrict__ Th,
-                         __nv_bfloat16 *__restrict__ Tl) {
+__global__ void k_prep_b(int nm, int NMT, int K, int Kp, int nf, int n_pad, int trunc, int sum_base, int is_sum,
+                         const float *__restrict__ A, __nv_bfloat16 *__restrict__ Th, __nv_bfloat16 *__restrict__ Tl) {
     const int t = blockIdx.x, k0 = blockIdx.y * 64;
     int src = t;
     if (is_sum) {
@@ -440,22 +442,21 @@ __global__ void k_prep_b(int nm, int NMT, int K, int Kp, int nrows, int nf, int 
             src = sum_base + t;
         }
     }
-    __shared__ double As[64][33];
+    __shared__ float As[64][33];
     for (int e = threadIdx.x; e < 64 * nm; e += blockDim.x) {
         const int kk = e / nm, m = e % nm, k = k0 + kk;
-        As[kk][m] = (src >= 0 && k < K) ? A[((size_t)src * K + k) * nm + m] : 0.0;
+        As[kk][m] = (src >= 0 && k < K) ? A[((size_t)src * K + k) * nm + m] : 0.f;
     }
     __syncthreads();
-    for (int e = threadIdx.x; e < NMT * 64; e += blockDim.x) {
-        const int j = e / 64, kk = e % 64;
-        const double u = j < nm ? As[kk][j] : 0.0;
-        __nv_bfloat16 hi, lo;
-        split_bf16(u, hi, lo);
-        const size_t o = ((size_t)t * NMT + j) * Kp + k0 + kk;
-        Th[o] = hi;
-        Tl[o] = lo;
+    for (int e = threadIdx.x; e < NMT * 8; e += blockDim.x) {
+        const int j = e >> 3, kv = (e & 7) * 8;
+        __align__(16) __nv_bfloat16 hi[8], lo[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) split_bf16(j < nm ? (double)As[kv + q][j] : 0.0, hi[q], lo[q]);
+        const size_t o = ((size_t)t * NMT + j) * Kp + k0 + kv;
+        *(uint4 *)(Th + o) = *(const uint4 *)hi;
+        *(uint4 *)(Tl + o) = *(const uint4 *)lo;
     }
-    (void)nrows;
 }
 
 // FRF tables in FP64, rounded once to FP32: Hg[c][j] = H_j(w_c), Hs[s][j] = H_j(w_r + w_c).
@@ -568,10 +569,10 @@ int Engine::contract_mixed(const PointSrc &ps, long long npts, double *m3mf, dou
     if ((e = cudaMemsetAsync(derr, 0, sizeof(int), stream))) return cuda_fail(e, "memset");
     {
         dim3 gu(nf, Kp / 64);
-        k_prep_u<<<gu, 256, 0, stream>>>(nm, K, Kp, Mp, dA.as<double>(), dQ.as<double>(), Uh, Ul);
+        k_prep_u<<<gu, 256, 0, stream>>>(nm, K, Kp, Mp, dA32.as<float>(), dQ.as<double>(), Uh, Ul);
         dim3 gg(nf, Kp / 64), gs(ns, Kp / 64);
-        k_prep_b<<<gg, 256, 0, stream>>>(nm, NMT, K, Kp, nf, nf, ps.n_pad, ps.trunc, ps.sum_base, 0, dA.as<double>(), Gh, Gl);
-        k_prep_b<<<gs, 256, 0, stream>>>(nm, NMT, K, Kp, ns, nf, ps.n_pad, ps.trunc, ps.sum_base, 1, dA.as<double>(), Sh, Sl);
+        k_prep_b<<<gg, 256, 0, stream>>>(nm, NMT, K, Kp, nf, ps.n_pad, ps.trunc, ps.sum_base, 0, dA32.as<float>(), Gh, Gl);
+        k_prep_b<<<gs, 256, 0, stream>>>(nm, NMT, K, Kp, nf, ps.n_pad, ps.trunc, ps.sum_base, 1, dA32.as<float>(), Sh, Sl);
         const int nh = (nf + ns) * NMT;
         k_prep_h<<<(nh + 255) / 256, 256, 0, stream>>>(nf, nm, NMT, ps.fgrid, frf(), Hg, Hs);
         if ((e = cudaGetLastError())) return cuda_fail(e, "BF16x3 operand preparation");

@@ -49,8 +49,9 @@ def test_mixed_matches_fp64(name, prob):
     assert rel(mix["m3mf_cls"], ref["m3mf_cls"]) < TOL_M3
     assert rel(mix["m3mr_cls"], ref["m3mr_cls"]) < TOL_M3
     assert rel(mix["sk"], ref["sk"]) < TOL_SK
-    # the second-order path is FP64 in both
-    assert np.array_equal(mix["m2mr_cls"], ref["m2mr_cls"])
+    # second-order moments: FP64 sums of the FP32 factor table in the mixed run
+    assert rel(mix["m2mr_cls"], ref["m2mr_cls"]) < 1e-6
+    assert rel(mix["m2mf_cls"], ref["m2mf_cls"]) < 1e-6
 
 
 def test_mixed_analytic_sum_frequency():
