@@ -33,6 +33,13 @@ class BsaError(RuntimeError):
     pass
 
 
+class Zone(C.Structure):
+    """bsa_zone: a rectangular Mesher zone (include/bsa_gpu.h)."""
+    _fields_ = [("fi0", C.c_double), ("fj0", C.c_double), ("dIi", C.c_double), ("dIj", C.c_double),
+                ("dJi", C.c_double), ("dJj", C.c_double), ("ni", C.c_int), ("nj", C.c_int),
+                ("Fi", C.c_int), ("Fj", C.c_int), ("sym", C.c_double), ("policy", C.c_int)]
+
+
 class Stats(C.Structure):
     _fields_ = [("ms_total", C.c_double), ("ms_contraction", C.c_double), ("ms_gemm", C.c_double),
                 ("points", C.c_double), ("h2d_bytes", C.c_double), ("d2h_bytes", C.c_double),
@@ -77,6 +84,7 @@ def load(path: Optional[str] = None):
         "bsa_gpu_clsBispectra": [vp, i, vp, vp, vp], "bsa_gpu_mshBispectra": [vp, vp, i, vp, vp],
         "bsa_gpu_mshMoments": [vp, vp, vp, i, vp, vp], "bsa_gpu_getStats": [vp],
         "bsa_gpu_pointMomentsNoAlloc": [vp, i, i, vp, vp, vp, vp, vp, vp, vp, i, vp, vp, vp, vp, vp, vp],
+        "bsa_gpu_mshZones": [vp, i, vp, vp, vp], "bsa_gpu_mshGenerateZones": [vp, i, vp],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)
@@ -221,6 +229,25 @@ class BsaSession:
         mf, mr = np.zeros(nm ** 3), np.zeros(nm ** 3)
         check(self.lib.bsa_gpu_mshMoments(_p(fi), _p(fj), _p(w), fi.size, _p(mf), _p(mr)), "bsa_gpu_mshMoments")
         return mf, mr
+
+    def msh_zones(self, zones):
+        """Third moments (m3mf, m3mr) over a list of Zone structures, and the BFM / BRM
+        lattice point counts."""
+        arr = (Zone * len(zones))(*zones)
+        nm = self.nmodes()
+        mf, mr, cnt = np.zeros(nm ** 3), np.zeros(nm ** 3), np.zeros(2)
+        check(self.lib.bsa_gpu_mshZones(C.cast(arr, C.c_void_p), len(zones), _p(mf), _p(mr), _p(cnt)),
+              "bsa_gpu_mshZones")
+        return mf, mr, cnt
+
+    def generate_zones(self):
+        """The zone layout of the Mesher analysis."""
+        n = C.c_int(0)
+        check(self.lib.bsa_gpu_mshGenerateZones(None, 0, C.byref(n)), "bsa_gpu_mshGenerateZones")
+        arr = (Zone * n.value)()
+        check(self.lib.bsa_gpu_mshGenerateZones(C.cast(arr, C.c_void_p), n.value, C.byref(n)),
+              "bsa_gpu_mshGenerateZones")
+        return list(arr)
 
     def stats(self) -> Stats:
         st = Stats()

@@ -34,6 +34,19 @@ enum PointMode : int {
     kPointsList = 1,   // explicit lists of A-table rows and weights
 };
 
+// A rectangular Mesher zone on the device: BFM lattice point (i, j), 0 <= i < ni,
+// 0 <= j < nj, sits at (f1, f2) = (fi0, fj0) + i (dIi, dIj) + j (dJi, dJj).  The response
+// bispectrum is integrated on the BRM lattice refined by (Fi, Fj), with the force
+// bispectrum interpolated bilinearly between BFM points and the trapezoid weights of the
+// zone integration (_shared_poly2d.fi:470-2166): vertex 1/4, border 1/2, centre 1, times
+// the lattice cell area (wI / Fi) (wJ / Fj), times the spatial-symmetry factor sym.
+struct ZoneDev {
+    double fi0, fj0, dIi, dIj, dJi, dJj;
+    double wI, wJ;   // BFM lattice steps in rad/s (|dI| 2 pi, |dJ| 2 pi)
+    double sym;
+    int ni, nj, Fi, Fj;
+};
+
 enum WeightMode : int {
     kWeightClassicVect = 0,  // intgSpectraVect_ edge weights (BsaClassicImpl.F90:596-632)
     kWeightUniform = 1,      // one weight for every point (scalar classic, BsaCL)
@@ -52,6 +65,8 @@ struct PointSrc {
     const int *ix, *iy, *iz; // A rows of f1, f2, f1+f2 (kPointsList; iz < 0: zero)
     const double *w;        // weights (kWeightList)
     const double *f1, *f2;  // point frequencies (kPointsList)
+    const ZoneDev *zones;   // optional (kPointsList): BRM neighbourhood of each point
+    const int *zid, *zi, *zj; // zone and lattice coordinates of each point
 };
 
 struct FrfPar {

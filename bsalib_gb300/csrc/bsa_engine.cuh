@@ -74,7 +74,7 @@ struct Engine {
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr;
     DevBuf dL, dQ, dLogc, dPsdPar, dFrfM, dFrfK, dFrfC, dFreq, dS, dA, dPartF, dPartR, dOut, dPsdF, dWf, dPts,
-        dPtsD, dBF, dBR, dMixA, dMixB, dMixH, dMixPart, dA32;
+        dPtsD, dBF, dBR, dMixA, dMixB, dMixH, dMixPart, dA32, dZones, dZidx;
 
     // stats
     double last_ms = 0, last_ms_contraction = 0, last_ms_gemm = 0, last_points = 0;
@@ -97,7 +97,11 @@ struct Engine {
     int contract(const PointSrc &ps, long long npts, double *m3mf, double *m3mr, double *bf_host, double *br_host);
     int contract_mixed(const PointSrc &ps, long long npts, double *m3mf, double *m3mr);
     int run_points(const double *fi, const double *fj, const double *w, double wuniform, long long npts,
-                   double *m3mf, double *m3mr, double *bfm, double *brm);
+                   double *m3mf, double *m3mr, double *bfm, double *brm,
+                   const std::vector<ZoneDev> *zones = nullptr, const int *zid = nullptr, const int *zi = nullptr,
+                   const int *zj = nullptr);
+    int run_zones(const std::vector<ZoneDev> &zones, double *m3mf, double *m3mr, double *npts);
+    int mesher_zones(std::vector<ZoneDev> &zones, std::vector<int> &policy);
     int run_mesher(double *m3mf, double *m3mr);
 };
 

@@ -65,7 +65,8 @@ void Engine::reset_inputs() {
 
 void Engine::free_device() {
     for (DevBuf *b : {&dL, &dQ, &dLogc, &dPsdPar, &dFrfM, &dFrfK, &dFrfC, &dFreq, &dS, &dA, &dPartF, &dPartR,
-                      &dOut, &dPsdF, &dWf, &dPts, &dPtsD, &dBF, &dBR, &dMixA, &dMixB, &dMixH, &dMixPart, &dA32})
+                      &dOut, &dPsdF, &dWf, &dPts, &dPtsD, &dBF, &dBR, &dMixA, &dMixB, &dMixH, &dMixPart, &dA32,
+                      &dZones, &dZidx})
         b->release();
     if (stream) cudaStreamDestroy(stream);
     stream = nullptr;
@@ -443,7 +444,8 @@ int Engine::contract(const PointSrc &ps, long long npts, double *m3mf, double *m
 
 // Point-set evaluation with analytic f1+f2 (Mesher functions and BsaCL semantics).
 int Engine::run_points(const double *fi, const double *fj, const double *w, double wuniform, long long npts,
-                       double *m3mf, double *m3mr, double *bfm, double *brm) {
+                       double *m3mf, double *m3mr, double *bfm, double *brm, const std::vector<ZoneDev> *zones,
+                       const int *zid, const int *zi, const int *zj) {
     kernels = 0;
     h2d = d2h = 0;
     last_ms_gemm = 0;
@@ -498,6 +500,20 @@ int Engine::run_points(const double *fi, const double *fj, const double *w, doub
     ps.wval = wuniform;
     ps.ix = dix; ps.iy = diy; ps.iz = diz;
     ps.f1 = df1; ps.f2 = df2; ps.w = w ? dw : nullptr;
+    if (zones) {
+        if ((e = upload(dZones, *zones, stream)) || (e = dZidx.reserve(n * 3 * sizeof(int))))
+            return cuda_fail(e, "zone upload");
+        int *dzid = dZidx.as<int>(), *dzi = dzid + n, *dzj = dzi + n;
+        if ((e = cudaMemcpyAsync(dzid, zid, n * sizeof(int), cudaMemcpyHostToDevice, stream)) ||
+            (e = cudaMemcpyAsync(dzi, zi, n * sizeof(int), cudaMemcpyHostToDevice, stream)) ||
+            (e = cudaMemcpyAsync(dzj, zj, n * sizeof(int), cudaMemcpyHostToDevice, stream)))
+            return cuda_fail(e, "zone upload");
+        h2d += (double)n * 3 * sizeof(int);
+        ps.zones = dZones.as<ZoneDev>();
+        ps.zid = dzid;
+        ps.zi = dzi;
+        ps.zj = dzj;
+    }
     rc = contract(ps, npts, m3mf, m3mr, bfm, brm);
     if (rc) return rc;
     last_points = (double)npts;

@@ -392,6 +392,60 @@ __global__ __launch_bounds__(256) void k_bfm_fp64(const double *__restrict__ A,
             }
             __syncthreads();
         }
+        if (ps.zones) {
+            // Mesher zone point: the force bispectrum of this BFM lattice point enters every
+            // BRM lattice point of its bilinear support with weight lambda; accumulate
+            // G = sum_q lambda_q w_q Re[H_m(w1_q) H_n(w2_q) conj H_o(w1_q + w2_q)].
+            const ZoneDev z = ps.zones[ps.zid[p]];
+            const int li = ps.zi[p], lj = ps.zj[p];
+            const int NI = (z.ni - 1) * z.Fi, NJ = (z.nj - 1) * z.Fj;  // last BRM index
+            double g[MT];
+#pragma unroll
+            for (int u = 0; u < MT; ++u) g[u] = 0.0;
+            for (int di = 1 - z.Fi; di < z.Fi; ++di) {
+                const int qi = li * z.Fi + di;
+                if (qi < 0 || qi > NI) continue;
+                for (int dj = 1 - z.Fj; dj < z.Fj; ++dj) {
+                    const int qj = lj * z.Fj + dj;
+                    if (qj < 0 || qj > NJ) continue;
+                    const double lam = (1.0 - (double)abs(di) / z.Fi) * (1.0 - (double)abs(dj) / z.Fj);
+                    const double ti = (qi == 0 || qi == NI) ? 0.5 : 1.0, tj = (qj == 0 || qj == NJ) ? 0.5 : 1.0;
+                    const double wq = z.sym * (z.wI / z.Fi) * (z.wJ / z.Fj) * ti * tj * lam;
+                    const double a = (double)qi / z.Fi, bq = (double)qj / z.Fj;
+                    const double q1 = z.fi0 + a * z.dIi + bq * z.dJi, q2 = z.fj0 + a * z.dIj + bq * z.dJj;
+                    const double v1 = q1 * kPi2, v2 = q2 * kPi2;
+                    if (t < nm) {
+                        frf_eval(frf.M[t], frf.K[t], frf.C[t], v1, Hs[2 * t], Hs[2 * t + 1]);
+                        frf_eval(frf.M[t], frf.K[t], frf.C[t], v2, Hs[2 * nm + 2 * t], Hs[2 * nm + 2 * t + 1]);
+                        frf_eval(frf.M[t], frf.K[t], frf.C[t], v1 + v2, Hs[4 * nm + 2 * t], Hs[4 * nm + 2 * t + 1]);
+                    }
+                    __syncthreads();
+                    if (ok) {
+                        const double h2r = Hs[2 * nm + 2 * n], h2i = Hs[2 * nm + 2 * n + 1];
+                        const double h3r = Hs[4 * nm + 2 * o], h3i = Hs[4 * nm + 2 * o + 1];
+                        const double cr = h2r * h3r + h2i * h3i, ci = h2i * h3r - h2r * h3i;
+#pragma unroll
+                        for (int u = 0; u < MT; ++u) {
+                            const int m = mg + MG * u;
+                            if (m < nm) g[u] = fma(wq, Hs[2 * m] * cr - Hs[2 * m + 1] * ci, g[u]);
+                        }
+                    }
+                    __syncthreads();
+                }
+            }
+            if (ok) {
+#pragma unroll
+                for (int u = 0; u < MT; ++u) {
+                    const int m = mg + MG * u;
+                    if (m < nm) {
+                        const double bfv = 2.0 * acc[u];
+                        smf[u] = fma(w, bfv, smf[u]);
+                        smr[u] = fma(g[u], bfv, smr[u]);
+                    }
+                }
+            }
+            continue;
+        }
         const double w1 = f1 * kPi2, w2 = f2 * kPi2;
         if (t < nm) {
             frf_eval(frf.M[t], frf.K[t], frf.C[t], w1, Hs[2 * t], Hs[2 * t + 1]);

@@ -629,9 +629,4 @@ int Engine::contract_mixed(const PointSrc &ps, long long npts, double *m3mf, dou
     return BSA_OK;
 }
 
-int Engine::run_mesher(double *m3mf, double *m3mr) {
-    (void)m3mf; (void)m3mr;
-    return fail(BSA_ERR_UNSUPPORTED, "Mesher zone generation not available in this build");
-}
-
 }  // namespace bsa

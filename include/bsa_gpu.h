@@ -192,6 +192,34 @@ int bsa_gpu_pointMomentsNoAlloc(const double *A, int K, int nm, const double *Q,
                                 const double *w, int npts, const double *Mm, const double *Km,
                                 const double *Cm, double *m3mf, double *m3mr, void *stream);
 
+/* A rectangular Mesher zone (MRectZone_t, src/bsa/meshing/zones/MRectZoneImpl.F90): BFM
+ * lattice point (i, j), 0 <= i < ni, 0 <= j < nj, at (f1, f2) = (fi0, fj0) + i (dIi, dIj)
+ * + j (dJi, dJj) [Hz]; the response bispectrum is integrated on the BRM lattice refined by
+ * (Fi, Fj) with the force bispectrum interpolated bilinearly (interpolateRZ_HTPC_v3,
+ * _shared_poly2d.fi:470-2166) and trapezoid weights; sym multiplies the zone's integrals
+ * (settings i_bisp_sym_, 1 for the full plane). */
+typedef struct {
+    double fi0, fj0;
+    double dIi, dIj;
+    double dJi, dJj;
+    int ni, nj;
+    int Fi, Fj;
+    double sym;
+    int policy;   /* MPolicy id of the zone (src/bsa/meshing/policy/MPolicy.F90:34-43) */
+} bsa_zone;
+
+/* Third moments over a list of zones in one batched device pass (the post-mesh zone loop,
+ * Mesh / interpolate, BsaMesherImpl.F90:1416-1553, _shared_poly2d.fi:2091-2119):
+ * m3mf = sum over zones of the BFM-lattice integral, m3mr = of the BRM-lattice integral.
+ * npts (optional, 2 doubles): BFM and BRM lattice point counts. */
+int bsa_gpu_mshZones(const bsa_zone *zones, int nz, double *m3mf, double *m3mr, double *npts);
+
+/* The zone layout the Mesher analysis (bsa_Run with analysis type 2) evaluates: restates
+ * prefetchZoneLimits_ (BsaMesherImpl.F90:1638-1859) and the background peak zone of
+ * PreMesh (:266-420), and lays rectangular zones over those limits on both axes.  Writes
+ * at most cap zones, *nz receives the full count. */
+int bsa_gpu_mshGenerateZones(bsa_zone *zones, int cap, int *nz);
+
 /* Timing and counters of the last run. */
 typedef struct {
     double ms_total;          /* device time of the last run (CUDA events)           */

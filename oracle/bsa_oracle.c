@@ -811,3 +811,58 @@ int orc_num_threads(void)
     return 1;
 #endif
 }
+
+/*
+ * One rectangular Mesher zone, post-mesh (compute_rz_ and interpolateRZ_HTPC_v3,
+ * src/bsa/meshing/zones/_shared_poly2d.fi:40-454 and 470-2166, with the BFM multi-level
+ * refinement off): the direct BFM (getFM_full_tnm_scalar_msh_) on the ni x nj lattice
+ * (f1, f2) = (fi0, fj0) + i (dIi, dIj) + j (dJi, dJj); the BFM integral with the lattice's
+ * trapezoid weights (vertex dwI dwJ / 4, border / 2, centre 1); the BRM lattice refined by
+ * (Fi, Fj), the BFM interpolated linearly along J then along I between lattice points, the
+ * BRM (getRM_full_scalar_msh_) at every BRM point and its trapezoid weights with
+ * (dwI / Fi)(dwJ / Fj).  Both integrals times sym are added to m3mf / m3mr (nm^3).
+ */
+int orc_rect_zone(const orc_problem *P, double fi0, double fj0, double dIi, double dIj, double dJi, double dJj,
+                  int ni, int nj, int Fi, int Fj, double sym, double *m3mf, double *m3mr)
+{
+    const int nme = P->nm_eff;
+    const size_t nm3 = (size_t)nme * nme * nme;
+    if (ni < 2 || nj < 2 || Fi < 1 || Fj < 1 || nme > 256) return -1;
+    double *bfm = malloc(sizeof(double) * nm3 * (size_t)ni * nj);
+    double *tmp = malloc(sizeof(double) * nm3), *brm = malloc(sizeof(double) * nm3);
+    if (!bfm || !tmp || !brm) { free(bfm); free(tmp); free(brm); return -3; }
+    for (int i = 0; i < ni; ++i)
+        for (int j = 0; j < nj; ++j) {
+            const double f1 = fi0 + i * dIi + j * dJi, f2 = fj0 + i * dIj + j * dJj;
+            int rc = orc_msh_bfm_direct(P, f1, f2, bfm + nm3 * ((size_t)i * nj + j));
+            if (rc) { free(bfm); free(tmp); free(brm); return rc; }
+        }
+    const double dwI = sqrt(dIi * dIi + dIj * dIj) * PIt2, dwJ = sqrt(dJi * dJi + dJj * dJj) * PIt2;
+    for (int i = 0; i < ni; ++i)
+        for (int j = 0; j < nj; ++j) {
+            const double w = sym * dwI * dwJ * ((i == 0 || i == ni - 1) ? 0.5 : 1.0) * ((j == 0 || j == nj - 1) ? 0.5 : 1.0);
+            const double *b = bfm + nm3 * ((size_t)i * nj + j);
+            for (size_t x = 0; x < nm3; ++x) m3mf[x] += w * b[x];
+        }
+    const int NI = (ni - 1) * Fi, NJ = (nj - 1) * Fj;
+    for (int qi = 0; qi <= NI; ++qi)
+        for (int qj = 0; qj <= NJ; ++qj) {
+            const int i0 = qi / Fi < ni - 1 ? qi / Fi : ni - 2, j0 = qj / Fj < nj - 1 ? qj / Fj : nj - 2;
+            const double ti = (double)(qi - i0 * Fi) / Fi, tj = (double)(qj - j0 * Fj) / Fj;
+            const double *b00 = bfm + nm3 * ((size_t)i0 * nj + j0), *b01 = bfm + nm3 * ((size_t)i0 * nj + j0 + 1);
+            const double *b10 = bfm + nm3 * ((size_t)(i0 + 1) * nj + j0), *b11 = bfm + nm3 * ((size_t)(i0 + 1) * nj + j0 + 1);
+            for (size_t x = 0; x < nm3; ++x) {
+                const double left = b00[x] * (1.0 - tj) + b01[x] * tj;     /* along J, column i0   */
+                const double right = b10[x] * (1.0 - tj) + b11[x] * tj;    /* along J, column i0+1 */
+                tmp[x] = left * (1.0 - ti) + right * ti;                    /* along I              */
+            }
+            const double a = (double)qi / Fi, bq = (double)qj / Fj;
+            const double f1 = fi0 + a * dIi + bq * dJi, f2 = fj0 + a * dIj + bq * dJj;
+            orc_msh_brm(P, 1, &f1, 1, &f2, tmp, brm);
+            const double w = sym * (dwI / Fi) * (dwJ / Fj) * ((qi == 0 || qi == NI) ? 0.5 : 1.0) *
+                             ((qj == 0 || qj == NJ) ? 0.5 : 1.0);
+            for (size_t x = 0; x < nm3; ++x) m3mr[x] += w * brm[x];
+        }
+    free(bfm); free(tmp); free(brm);
+    return 0;
+}

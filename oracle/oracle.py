@@ -63,6 +63,7 @@ def lib():
         _lib.orc_msh_brm.argtypes = [vp, C.c_int, vp, C.c_int, vp, vp, vp]
         _lib.orc_skewness.argtypes = [C.c_int, vp, vp, vp]
         _lib.orc_modal_recomb.argtypes = [C.c_int, C.c_int, vp, vp, vp, vp, vp, vp]
+        _lib.orc_rect_zone.argtypes = [vp] + [C.c_double] * 6 + [C.c_int] * 4 + [C.c_double, vp, vp]
     return _lib
 
 
@@ -215,6 +216,16 @@ class Oracle:
         out = np.zeros_like(bfm)
         lib().orc_msh_brm(C.byref(self.st), fi.size, _p(fi), fj.size, _p(fj), _p(bfm), _p(out))
         return out
+
+    # -- a12 ------------------------------------------------------------------------------
+    def rect_zone(self, fi0, fj0, dIi, dIj, dJi, dJj, ni, nj, Fi, Fj, sym=1.0):
+        """(m3mf, m3mr) contributions of one rectangular zone."""
+        mf, mr = np.zeros(self.nme ** 3), np.zeros(self.nme ** 3)
+        rc = lib().orc_rect_zone(C.byref(self.st), fi0, fj0, dIi, dIj, dJi, dJj, int(ni), int(nj), int(Fi),
+                                 int(Fj), float(sym), _p(mf), _p(mr))
+        if rc:
+            raise RuntimeError(f"orc_rect_zone failed ({rc})")
+        return mf, mr
 
     # -- a15 ------------------------------------------------------------------------------
     def skewness(self, m2, m3):

@@ -1,0 +1,113 @@
+"""The Mesher path: rectangular zones (BFM lattice, bilinear BRM interpolation, trapezoid
+zone weights) evaluated on the GPU in one batched pass, against the oracle's restatement of
+the zone integration; the zone layout; and bsa_Run with the Mesher analysis.
+FP64 path: 1e-10 relative (max-norm)."""
+import numpy as np
+import pytest
+
+from bsalib_gb300 import api
+from bsalib_gb300.problem import cantilever_tower, tall_building
+from oracle.oracle import Oracle
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-10
+
+
+def rel(a, b):
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+def zone(fi0, fj0, dIi, dIj, dJi, dJj, ni, nj, Fi, Fj, sym=1.0):
+    return api.Zone(fi0, fj0, dIi, dIj, dJi, dJj, ni, nj, Fi, Fj, sym, 0)
+
+
+ZONES = [
+    zone(-0.4, -0.4, 0.1, 0.0, 0.0, 0.1, 9, 9, 4, 4),              # background-like square
+    zone(0.4, -0.4, 0.05, 0.0, 0.0, 0.2, 5, 5, 4, 2),              # crest-like strip
+    zone(1.2, 0.6, 0.0, 0.15, -0.12, 0.0, 4, 6, 2, 3),             # swapped axes (rot 90)
+    zone(-1.0, 1.0, 0.07, 0.07, 0.07, -0.07, 3, 4, 1, 2, 2.0),     # 45-degree lattice, sym 2
+]
+
+
+def test_zones_vs_oracle(bsalib):
+    prob = tall_building(nodes=12, modes=4, nfreqs=5, df=0.3, seed=31)
+    o = Oracle(prob)
+    ref_f = np.zeros(o.nme ** 3)
+    ref_r = np.zeros(o.nme ** 3)
+    for z in ZONES:
+        mf, mr = o.rect_zone(z.fi0, z.fj0, z.dIi, z.dIj, z.dJi, z.dJj, z.ni, z.nj, z.Fi, z.Fj, z.sym)
+        ref_f += mf
+        ref_r += mr
+    s = api.BsaSession(prob)
+    try:
+        mf, mr, cnt = s.msh_zones(ZONES)
+        st = s.stats()
+    finally:
+        s.close()
+    assert rel(mf, ref_f) < TOL
+    assert rel(mr, ref_r) < TOL
+    nbfm = sum(z.ni * z.nj for z in ZONES)
+    nbrm = sum(((z.ni - 1) * z.Fi + 1) * ((z.nj - 1) * z.Fj + 1) for z in ZONES)
+    assert cnt[0] == nbfm and cnt[1] == nbrm and st.points == nbrm
+
+
+def test_zone_with_unit_factors_is_plain_trapezoid(bsalib):
+    """Fi = Fj = 1: the BRM lattice is the BFM lattice, so m3mr is the trapezoid sum of B_R."""
+    prob = cantilever_tower(nfreqs=5, df=0.5, nodes=6)
+    z = zone(-0.3, 0.2, 0.1, 0.0, 0.0, 0.15, 4, 3, 1, 1)
+    s = api.BsaSession(prob)
+    try:
+        _, mr, _ = s.msh_zones([z])
+        fi = np.array([z.fi0 + i * z.dIi for i in range(4) for j in range(3)])
+        fj = np.array([z.fj0 + j * z.dJj for i in range(4) for j in range(3)])
+        ti = np.array([0.5 if i in (0, 3) else 1.0 for i in range(4) for j in range(3)])
+        tj = np.array([0.5 if j in (0, 2) else 1.0 for i in range(4) for j in range(3)])
+        w = ti * tj * (0.1 * 2 * np.pi) * (0.15 * 2 * np.pi)
+        _, mr2 = s.msh_moments(fi, fj, w)
+    finally:
+        s.close()
+    assert rel(mr, mr2) < 1e-12
+
+
+def test_mesher_layout_covers_the_plane(bsalib):
+    prob = cantilever_tower(nodes=8)
+    prob.settings.suban = 2
+    s = api.BsaSession(prob)
+    try:
+        zs = s.generate_zones()
+    finally:
+        s.close()
+    assert len(zs) > 9
+    area = sum(((z.ni - 1) * z.dIi) * ((z.nj - 1) * z.dJj) for z in zs)
+    X = max(z.fi0 + (z.ni - 1) * z.dIi for z in zs)
+    assert np.isclose(area, (2 * X) ** 2, rtol=1e-12)
+    assert np.isclose(X, prob.natf.max() * prob.settings.maxaext)
+    # resonant peak bands are zone frontiers: f_n +- xsi f_n * peak_area_ext
+    edges = {round(z.fi0, 12) for z in zs}
+    for f, x in zip(prob.natf, prob.xsi):
+        ext = x * f * prob.settings.genpaext
+        assert any(abs(e - (f - ext)) < 1e-9 or abs(e - (f + ext)) < 1e-9 for e in edges) or f - ext < 0.4
+
+
+def test_mesher_run_vs_oracle_on_its_zones(bsalib):
+    """bsa_Run with the Mesher analysis equals the oracle's zone integration over the same
+    layout."""
+    prob = cantilever_tower(nodes=5)
+    prob.settings.suban = 2
+    prob.settings.bkgrfmt = 6
+    s = api.BsaSession(prob)
+    try:
+        out = s.run()
+        zs = s.generate_zones()
+    finally:
+        s.close()
+    o = Oracle(prob)
+    ref_f = np.zeros(o.nme ** 3)
+    ref_r = np.zeros(o.nme ** 3)
+    for z in zs:
+        mf, mr = o.rect_zone(z.fi0, z.fj0, z.dIi, z.dIj, z.dJi, z.dJj, z.ni, z.nj, z.Fi, z.Fj, z.sym)
+        ref_f += mf
+        ref_r += mr
+    assert rel(out["m3mf_msh"], ref_f) < TOL
+    assert rel(out["m3mr_msh"], ref_r) < TOL
+    assert np.all(out["m3mr_cls"] == 0.0)  # analysis type 2 runs the Mesher only
