@@ -80,7 +80,7 @@ def load(path: Optional[str] = None):
         "bsa_setNodalWindAltitudes": [vp, i], "bsa_setSpatialNodalCorr": [vp, C.c_int64],
         "bsa_setWindFCoeffs": [vp, i, i, i], "bsa_getNModesEff": [vp],
         "bsa_Run": [vp] * 7, "bsa_computeSkewness": [i, vp, vp, vp],
-        "bsa_gpu_setPrecision": [i], "bsa_gpu_setClassicTruncation": [i],
+        "bsa_gpu_setPrecision": [i], "bsa_gpu_setClassicTruncation": [i], "bsa_gpu_setClassicRows": [i, i],
         "bsa_gpu_clsBispectra": [vp, i, vp, vp, vp], "bsa_gpu_mshBispectra": [vp, vp, i, vp, vp],
         "bsa_gpu_mshMoments": [vp, vp, vp, i, vp, vp], "bsa_gpu_getStats": [vp],
         "bsa_gpu_pointMomentsNoAlloc": [vp, i, i, vp, vp, vp, vp, vp, vp, vp, i, vp, vp, vp, vp, vp, vp],
@@ -178,6 +178,10 @@ class BsaSession:
     def set_precision(self, prec: int):
         self.precision = prec
         check(self.lib.bsa_gpu_setPrecision(prec), "bsa_gpu_setPrecision")
+
+    def set_rows(self, r_begin: int, r_end: int = -1):
+        """Evaluate only Classic grid rows [r_begin, r_end) (f1 index)."""
+        check(self.lib.bsa_gpu_setClassicRows(int(r_begin), int(r_end)), "bsa_gpu_setClassicRows")
 
     def nmodes(self) -> int:
         n = np.zeros(1, dtype=np.int32)

@@ -59,6 +59,7 @@ struct PointSrc {
     int n_pad;              // (nf - 1) / 2, centre offset of the padded S(f1+f2) copy
     int trunc;              // 1: S(f1+f2) beyond the grid reads zero
     int sum_base;           // A-table row of the analytic sum table (s = i1 + i2)
+    int r0, nr;             // grid rows (f1 index) of this run: i1 in [r0, r0 + nr)
     int wmode;
     double wval;            // uniform weight, or d^2 for the classic edge weights
     const double *fgrid;    // grid frequencies (kPointsGrid)

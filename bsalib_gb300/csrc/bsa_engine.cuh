@@ -63,6 +63,7 @@ struct Engine {
     std::string last_error;
     int precision = 0;          // BSA_PREC_FP64
     bool classic_trunc = true;  // S(f1+f2) beyond the classic grid reads zero
+    int shard_r0 = 0, shard_r1 = -1;  // classic grid rows evaluated (-1: to the end)
 
     // derived (validate)
     std::vector<int> modes;

@@ -327,6 +327,12 @@ int Engine::run_classic(double *m2mf, double *m2mr, double *m2o2mr, double *m3mf
     if (grid_out) *grid_out = f;
     const int nf = (int)f.size();
     if (nf < 2) return fail(BSA_ERR_ARG, "classic grid needs at least 2 frequencies");
+    // Row shard (f1 index): the moments of all shards sum to the full grid's.
+    const int r0 = std::min(std::max(shard_r0, 0), nf);
+    const int r1 = shard_r1 < 0 ? nf : std::min(shard_r1, nf);
+    if (r1 <= r0) return fail(BSA_ERR_ARG, "empty classic row shard [%d, %d)", r0, r1);
+    if ((bf_host || br_host) && (r0 != 0 || r1 != nf))
+        return fail(BSA_ERR_ARG, "materialised bispectra need the full grid");
     // Vectorised / scalar branch (checkMaxAllocation_, BsaClassicImpl.F90:384-434): only the
     // integration weights differ here, the spectra are never stored.
     bool scalar = set.scalar != 0;
@@ -361,7 +367,7 @@ int Engine::run_classic(double *m2mf, double *m2mr, double *m2o2mr, double *m3mf
                                      dPsdF.as<double>());
         if (e) return cuda_fail(e, "force PSD kernel");
         double *o = dOut.as<double>();
-        if ((e = launch_m2(stream, nf, nme, dFreq.as<double>(), dWf.as<double>(), dPsdF.as<double>(), frf(), o,
+        if ((e = launch_m2(stream, r0, r1, nme, dFreq.as<double>(), dWf.as<double>(), dPsdF.as<double>(), frf(), o,
                            o + nm2, o + 2 * nm2)))
             return cuda_fail(e, "m2 kernel");
         kernels += 2;
@@ -385,7 +391,9 @@ int Engine::run_classic(double *m2mf, double *m2mr, double *m2o2mr, double *m3mf
         ps.wmode = scalar ? kWeightUniform : kWeightClassicVect;
         ps.wval = delta * delta;
         ps.fgrid = dFreq.as<double>();
-        const long long npts = (long long)nf * nf;
+        ps.r0 = r0;
+        ps.nr = r1 - r0;
+        const long long npts = (long long)(r1 - r0) * nf;
         rc = mixed ? contract_mixed(ps, npts, m3mf, m3mr) : contract(ps, npts, m3mf, m3mr, bf_host, br_host);
         if (rc) return rc;
         last_points = (double)npts;
@@ -755,6 +763,14 @@ int bsa_gpu_setPrecision(int prec) {
     GUARD();
     if (prec != BSA_PREC_FP64 && prec != BSA_PREC_BF16X3) return eng().fail(BSA_ERR_ARG, "unknown precision");
     eng().precision = prec;
+    return BSA_OK;
+}
+
+int bsa_gpu_setClassicRows(int r_begin, int r_end) {
+    GUARD();
+    if (r_begin < 0 || (r_end >= 0 && r_end <= r_begin)) return eng().fail(BSA_ERR_ARG, "invalid classic row range");
+    eng().shard_r0 = r_begin;
+    eng().shard_r1 = r_end;
     return BSA_OK;
 }
 

@@ -245,14 +245,14 @@ cudaError_t launch_force_psd32(cudaStream_t st, int nf, int ntc, int nnl, int nm
 }
 
 // One block per (n, o) pair; threads stride over frequencies, fixed-order tree reduction.
-__global__ void k_m2(int nf, int nm, const double *__restrict__ f, const double *__restrict__ wf,
+__global__ void k_m2(int k0, int k1, int nm, const double *__restrict__ f, const double *__restrict__ wf,
                      const double *__restrict__ psd, FrfPar frf, double *m2mf, double *m2mr,
                      double *m2o2mr) {
     const int nm2 = nm * nm;
     const int pr = blockIdx.x;
     const int n = pr % nm, o = pr / nm;
     double sf = 0.0, sr = 0.0, so = 0.0;
-    for (int k = threadIdx.x; k < nf; k += blockDim.x) {
+    for (int k = k0 + threadIdx.x; k < k1; k += blockDim.x) {
         const double w = f[k] * kPi2;
         double hnr, hni, hor, hoi;
         frf_eval(frf.M[n], frf.K[n], frf.C[n], w, hnr, hni);
@@ -280,9 +280,9 @@ __global__ void k_m2(int nf, int nm, const double *__restrict__ f, const double 
     }
 }
 
-cudaError_t launch_m2(cudaStream_t st, int nf, int nm, const double *f, const double *wf,
+cudaError_t launch_m2(cudaStream_t st, int k0, int k1, int nm, const double *f, const double *wf,
                       const double *psd, FrfPar frf, double *m2mf, double *m2mr, double *m2o2mr) {
-    k_m2<<<nm * nm, 256, 0, st>>>(nf, nm, f, wf, psd, frf, m2mf, m2mr, m2o2mr);
+    k_m2<<<nm * nm, 256, 0, st>>>(k0, k1, nm, f, wf, psd, frf, m2mf, m2mr, m2o2mr);
     return cudaGetLastError();
 }
 
@@ -295,7 +295,7 @@ __device__ __forceinline__ void get_point(const PointSrc &ps, long long p, int &
                                           double &w, double &f1, double &f2) {
     if (ps.mode == kPointsGrid) {
         const int nf = ps.nf;
-        const int i1 = (int)(p % nf), i2 = (int)(p / nf);
+        const int i1 = ps.r0 + (int)(p % ps.nr), i2 = (int)(p / ps.nr);
         ix = i1;
         iy = i2;
         const int s = i1 + i2;

@@ -24,7 +24,8 @@ cudaError_t launch_force_psd(cudaStream_t st, int nf, int ntc, int nnl, int nm, 
                              const double *A, double *psd);
 cudaError_t launch_force_psd32(cudaStream_t st, int nf, int ntc, int nnl, int nm, const double *L,
                                const float *A, double *psd);
-cudaError_t launch_m2(cudaStream_t st, int nf, int nm, const double *f, const double *wf,
+// Second-order moments over the grid frequencies k in [k0, k1).
+cudaError_t launch_m2(cudaStream_t st, int k0, int k1, int nm, const double *f, const double *wf,
                       const double *psd, FrfPar frf, double *m2mf, double *m2mr, double *m2o2mr);
 
 // FP64 BFM contraction + FRF + weighted reduction over a point set.

@@ -48,6 +48,7 @@ constexpr unsigned long long kWaitNs = 2000000000ull;  // 2 s budget per wait
 
 struct Params {
     int nf;          // grid size
+    int rb, re;      // grid rows r in [rb, re) evaluated by this launch
     int nm;          // kept modes
     int Mp;          // rows per frequency in U (nm^2 rounded up to 128)
     int MT;          // Mp / 128
@@ -211,7 +212,7 @@ __global__ void __launch_bounds__(192, 1)
         if (lane == 0) {
             uint32_t it = 0;
             bool ok = true;
-            for (int r = r0; r < p.nf && ok; r += rstep)
+            for (int r = p.rb + r0; r < p.re && ok; r += rstep)
                 for (int nt = 0; nt < p.n_ntiles && ok; ++nt)
                     for (int kc = 0; kc < p.nk && ok; ++kc, ++it) {
                         const int s = it % kStages;
@@ -246,7 +247,7 @@ __global__ void __launch_bounds__(192, 1)
         if (lane == 0) {
             uint32_t it = 0, tile = 0;
             bool ok = true;
-            for (int r = r0; r < p.nf && ok; r += rstep)
+            for (int r = p.rb + r0; r < p.re && ok; r += rstep)
                 for (int nt = 0; nt < p.n_ntiles && ok; ++nt, ++tile) {
                     const int buf = tile & 1;
                     const uint32_t tph = (tile >> 1) & 1u;
@@ -311,7 +312,7 @@ __global__ void __launch_bounds__(192, 1)
         };
         uint32_t tile = 0;
         bool ok = true;
-        for (int r = r0; r < p.nf && ok; r += rstep) {
+        for (int r = p.rb + r0; r < p.re && ok; r += rstep) {
             const float2 hra = p.Hg[r * NMT + a];
             for (int nt = 0; nt < p.n_ntiles; ++nt, ++tile) {
                 const int buf = tile & 1;
@@ -585,6 +586,8 @@ int Engine::contract_mixed(const PointSrc &ps, long long npts, double *m3mf, dou
         return fail(BSA_ERR_CUDA, "cuTensorMapEncodeTiled failed");
     Params prm{};
     prm.nf = nf;
+    prm.rb = ps.r0;
+    prm.re = ps.r0 + ps.nr;
     prm.nm = nm;
     prm.Mp = Mp;
     prm.MT = MT;

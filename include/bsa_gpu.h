@@ -156,6 +156,11 @@ int bsa_gpu_setPrecision(int prec);
  * copy (functionsImpl.F90:1358-1363, 1409-1413); 0 evaluates it analytically. */
 int bsa_gpu_setClassicTruncation(int on);
 
+/* Restrict the Classic analysis to grid rows (f1 index, 0-based) in [r_begin, r_end);
+ * r_end = -1 runs to the last row.  The moments returned by the shards of a partition of
+ * the rows sum to the full grid's (multi-GPU / multi-process sharding, one host sum). */
+int bsa_gpu_setClassicRows(int r_begin, int r_end);
+
 /* getBFMClsVect + getBRMClsVect materialised (functionsImpl.F90:1312-1738): force and
  * response bispectra on the classic grid, (nf, nf, nm^3) with f1 fastest, and the grid.
  * Runs validation and the grid set-up of bsa_Run; for small grids (tests). */

@@ -214,3 +214,23 @@ def test_bsacl_abi_matches_oracle(bsalib):
         for b in fj:
             ref += infl * o.msh_bfm(a, b) * o.brm_factor(a, b)
     assert rel(res, ref) < TOL
+
+
+@pytest.mark.parametrize("prec,tol", [(api.PREC_FP64, 1e-12), (api.PREC_BF16X3, 1e-6)])
+def test_row_shards_sum_to_full_grid(prec, tol):
+    """Contiguous row shards (the multi-GPU split) add up to the full Classic analysis."""
+    from bsalib_gb300.dist import MOMENT_KEYS, shard_rows
+    prob = tall_building(nodes=30, modes=6, nfreqs=9, df=0.3, seed=12)
+    s = api.BsaSession(prob, precision=prec)
+    try:
+        full = s.run()
+        acc = {k: np.zeros_like(full[k]) for k in MOMENT_KEYS}
+        for r in range(3):
+            s.set_rows(*shard_rows(prob.classic_nf(), r, 3))
+            part = s.run()
+            for k in MOMENT_KEYS:
+                acc[k] += part[k]
+    finally:
+        s.close()
+    for k in MOMENT_KEYS:
+        assert rel(acc[k], full[k]) < tol, k
