@@ -61,6 +61,11 @@ void Engine::reset_inputs() {
     in = Inputs();
     set = Settings();
     derived_ok = false;
+    // controls of the GPU path return to their defaults with the inputs
+    precision = BSA_PREC_FP64;
+    classic_trunc = true;
+    shard_r0 = 0;
+    shard_r1 = -1;
 }
 
 void Engine::free_device() {

@@ -43,7 +43,7 @@ constexpr int kStages = 2;
 constexpr int kTileBytes = 128 * 128;            // 128 rows x 128 bytes
 constexpr int kStageBytes = 6 * kTileBytes;      // U hi/lo, Bg hi/lo, Bs hi/lo
 constexpr int kKinds = 5;                        // mr1, mr3, mr2, mf1, mf23
-constexpr int kFlushTiles = 16;                  // FP32 -> FP64 flush period (N tiles)
+constexpr int kFlushTiles = 64;                  // FP32 -> FP64 flush period (N tiles)
 constexpr unsigned long long kWaitNs = 2000000000ull;  // 2 s budget per wait
 
 struct Params {

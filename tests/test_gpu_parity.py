@@ -234,3 +234,20 @@ def test_row_shards_sum_to_full_grid(prec, tol):
         s.close()
     for k in MOMENT_KEYS:
         assert rel(acc[k], full[k]) < tol, k
+
+
+def test_controls_reset_by_finalise(bsalib):
+    """A new session does not inherit the previous one's row shard or precision."""
+    prob = tall_building(nodes=16, modes=4, nfreqs=7, df=0.3, seed=2)
+    s = api.BsaSession(prob)
+    full = s.run()
+    s.set_rows(5, -1)
+    s.set_precision(api.PREC_BF16X3)
+    s.close()
+    s2 = api.BsaSession(prob)
+    try:
+        again = s2.run()
+        assert s2.stats().precision == api.PREC_FP64
+    finally:
+        s2.close()
+    assert np.array_equal(again["m3mr_cls"], full["m3mr_cls"])
