@@ -78,7 +78,7 @@ def load(path: Optional[str] = None):
         "bsa_setWZMeanWindVel": [vp, i], "bsa_setWZRefAlt": [vp, i], "bsa_setTurbWindScales": [vp, i],
         "bsa_setTurbWindSDT": [vp, i], "bsa_setNodalVel": [vp, i], "bsa_setNodalWindZones": [vp, i],
         "bsa_setNodalWindAltitudes": [vp, i], "bsa_setSpatialNodalCorr": [vp, C.c_int64],
-        "bsa_setWindFCoeffs": [vp, i, i, i], "bsa_getNModesEff": [vp],
+        "bsa_setWindFCoeffs": [vp, i, i, i], "bsa_getNModesEff": [vp], "bsa_getSpectraDims": [vp, vp],
         "bsa_Run": [vp] * 7, "bsa_computeSkewness": [i, vp, vp, vp],
         "bsa_gpu_setPrecision": [i], "bsa_gpu_setClassicTruncation": [i], "bsa_gpu_setClassicRows": [i, i],
         "bsa_gpu_clsBispectra": [vp, i, vp, vp, vp], "bsa_gpu_mshBispectra": [vp, vp, i, vp, vp],
@@ -188,11 +188,17 @@ class BsaSession:
         check(self.lib.bsa_getNModesEff(_p(n)), "bsa_getNModesEff")
         return int(n[0])
 
+    def dims(self):
+        """(dim_psd, dim_bisp): nm^2 / nm^3, or nm / nm with the diagonal-only spectra."""
+        d = np.zeros(2, dtype=np.int32)
+        check(self.lib.bsa_getSpectraDims(_p(d[:1]), _p(d[1:])), "bsa_getSpectraDims")
+        return int(d[0]), int(d[1])
+
     def run(self) -> Dict[str, np.ndarray]:
         """bsa_Run: returns m2mf_cls, m2mr_cls, m2o2mr_cls, m3mf_msh, m3mr_msh, m3mf_cls, m3mr_cls."""
-        nm = self.nmodes()
-        out = {k: np.zeros(nm * nm) for k in ("m2mf_cls", "m2mr_cls", "m2o2mr_cls")}
-        out.update({k: np.zeros(nm ** 3) for k in ("m3mf_msh", "m3mr_msh", "m3mf_cls", "m3mr_cls")})
+        d2, d3 = self.dims()
+        out = {k: np.zeros(d2) for k in ("m2mf_cls", "m2mr_cls", "m2o2mr_cls")}
+        out.update({k: np.zeros(d3) for k in ("m3mf_msh", "m3mr_msh", "m3mf_cls", "m3mr_cls")})
         check(self.lib.bsa_Run(_p(out["m2mf_cls"]), _p(out["m2mr_cls"]), _p(out["m2o2mr_cls"]),
                                _p(out["m3mf_msh"]), _p(out["m3mr_msh"]), _p(out["m3mf_cls"]),
                                _p(out["m3mr_cls"])), "bsa_Run")
@@ -200,28 +206,28 @@ class BsaSession:
 
     def classic_bispectra(self):
         """Materialised force / response bispectra on the classic grid (f1 fastest)."""
-        nm = self.nmodes()
+        nm3 = self.dims()[1]
         nf_cap = self.prob.classic_nf() + 8
         nf = np.zeros(1, dtype=np.int32)
         f = np.zeros(nf_cap)
         # query the size first
         s = self.prob.settings
         nfx = self.prob.classic_nf() if s.test else nf_cap * 4
-        bf = np.zeros(nfx * nfx * nm ** 3)
-        br = np.zeros(nfx * nfx * nm ** 3)
+        bf = np.zeros(nfx * nfx * nm3)
+        br = np.zeros(nfx * nfx * nm3)
         check(self.lib.bsa_gpu_clsBispectra(_p(f), nf_cap, _p(nf), _p(bf), _p(br)), "bsa_gpu_clsBispectra")
         n = int(nf[0])
-        # library layout: (nm^3, nf*nf) column-major, point p = i1 + nf*i2
-        bf = bf[: n * n * nm ** 3].reshape(n, n, nm ** 3).transpose(1, 0, 2)
-        br = br[: n * n * nm ** 3].reshape(n, n, nm ** 3).transpose(1, 0, 2)
+        # library layout: (dim_bisp, nf*nf) column-major, point p = i1 + nf*i2
+        bf = bf[: n * n * nm3].reshape(n, n, nm3).transpose(1, 0, 2)
+        br = br[: n * n * nm3].reshape(n, n, nm3).transpose(1, 0, 2)
         return f[:n].copy(), bf, br
 
     def msh_bispectra(self, fi, fj):
         fi = np.ascontiguousarray(fi, dtype=np.float64)
         fj = np.ascontiguousarray(fj, dtype=np.float64)
-        nm = self.nmodes()
-        bfm = np.zeros((fi.size, nm ** 3))
-        brm = np.zeros((fi.size, nm ** 3))
+        nm3 = self.dims()[1]
+        bfm = np.zeros((fi.size, nm3))
+        brm = np.zeros((fi.size, nm3))
         check(self.lib.bsa_gpu_mshBispectra(_p(fi), _p(fj), fi.size, _p(bfm), _p(brm)), "bsa_gpu_mshBispectra")
         return bfm, brm
 
@@ -229,8 +235,8 @@ class BsaSession:
         fi = np.ascontiguousarray(fi, dtype=np.float64)
         fj = np.ascontiguousarray(fj, dtype=np.float64)
         w = np.ascontiguousarray(w, dtype=np.float64)
-        nm = self.nmodes()
-        mf, mr = np.zeros(nm ** 3), np.zeros(nm ** 3)
+        nm3 = self.dims()[1]
+        mf, mr = np.zeros(nm3), np.zeros(nm3)
         check(self.lib.bsa_gpu_mshMoments(_p(fi), _p(fj), _p(w), fi.size, _p(mf), _p(mr)), "bsa_gpu_mshMoments")
         return mf, mr
 
@@ -238,8 +244,8 @@ class BsaSession:
         """Third moments (m3mf, m3mr) over a list of Zone structures, and the BFM / BRM
         lattice point counts."""
         arr = (Zone * len(zones))(*zones)
-        nm = self.nmodes()
-        mf, mr, cnt = np.zeros(nm ** 3), np.zeros(nm ** 3), np.zeros(2)
+        nm3 = self.dims()[1]
+        mf, mr, cnt = np.zeros(nm3), np.zeros(nm3), np.zeros(2)
         check(self.lib.bsa_gpu_mshZones(C.cast(arr, C.c_void_p), len(zones), _p(mf), _p(mr), _p(cnt)),
               "bsa_gpu_mshZones")
         return mf, mr, cnt
@@ -260,7 +266,7 @@ class BsaSession:
 
     def skewness(self, m2, m3):
         nm = self.nmodes()
-        sk = np.zeros(nm ** 3)
+        sk = np.zeros(self.dims()[1])
         check(self.lib.bsa_computeSkewness(nm, _p(np.ascontiguousarray(m2)), _p(np.ascontiguousarray(m3)),
                                            _p(sk)), "bsa_computeSkewness")
         return sk

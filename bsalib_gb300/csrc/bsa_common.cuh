@@ -84,4 +84,38 @@ __host__ __device__ inline void frf_eval(double M, double K, double C, double w,
     hi = -ip / h;
 }
 
+// Point p of a point source: A/S-table rows of f1, f2, f1+f2 (iz < 0: the sum reads zero),
+// integration weight and the two frequencies.
+__device__ __forceinline__ void get_point(const PointSrc &ps, long long p, int &ix, int &iy, int &iz,
+                                          double &w, double &f1, double &f2) {
+    if (ps.mode == kPointsGrid) {
+        const int nf = ps.nf;
+        const int i1 = ps.r0 + (int)(p % ps.nr), i2 = (int)(p / ps.nr);
+        ix = i1;
+        iy = i2;
+        const int s = i1 + i2;
+        if (ps.trunc) {
+            const int c = s - ps.n_pad;
+            iz = (c >= 0 && c < nf) ? c : -1;
+        } else {
+            iz = ps.sum_base + s;
+        }
+        f1 = ps.fgrid[i1];
+        f2 = ps.fgrid[i2];
+        if (ps.wmode == kWeightClassicVect) {
+            const bool b1 = (i1 == 0 || i1 == nf - 1), b2 = (i2 == 0 || i2 == nf - 1);
+            w = ps.wval * ((b1 && b2) ? -0.5 : ((b1 || b2) ? 0.5 : 1.0));
+        } else {
+            w = ps.wval;
+        }
+    } else {
+        ix = ps.ix[p];
+        iy = ps.iy[p];
+        iz = ps.iz[p];
+        f1 = ps.f1[p];
+        f2 = ps.f2[p];
+        w = (ps.wmode == kWeightList) ? ps.w[p] : ps.wval;
+    }
+}
+
 }  // namespace bsa

@@ -69,13 +69,14 @@ struct Engine {
     std::vector<int> modes;
     int nme = 0, K = 0;
     std::vector<double> phitc, hL, hQ, hLogc, hM, hK, hC;
+    std::vector<double> hWd3, hWd2;  // diagonal-only weights Q L^2 and L^2, [k][m]
     std::vector<PsdNode> hPsd;
 
     // device
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr;
     DevBuf dL, dQ, dLogc, dPsdPar, dFrfM, dFrfK, dFrfC, dFreq, dS, dA, dPartF, dPartR, dOut, dPsdF, dWf, dPts,
-        dPtsD, dBF, dBR, dMixA, dMixB, dMixH, dMixPart, dA32, dZones, dZidx;
+        dPtsD, dBF, dBR, dMixA, dMixB, dMixH, dMixPart, dA32, dZones, dZidx, dWd3, dWd2;
 
     // stats
     double last_ms = 0, last_ms_contraction = 0, last_ms_gemm = 0, last_points = 0;
@@ -92,11 +93,18 @@ struct Engine {
     int upload_problem();
     FrfPar frf() const;
     int build_atable(const std::vector<double> &freqs, bool fp32 = false);
+    int build_psd(const std::vector<double> &freqs);
+    // dimM_psd_ / dimM_bisp_ (src/bsa/BsaLibImpl.F90:313-355): nm / nm for the diagonal-only
+    // spectra, nm^2 / nm^3 otherwise.
+    long long dim_psd() const { return set.onlyd ? nme : (long long)nme * nme; }
+    long long dim_bisp() const { return set.onlyd ? nme : (long long)nme * nme * nme; }
     int classic_grid(std::vector<double> &f);
     int run_classic(double *m2mf, double *m2mr, double *m2o2mr, double *m3mf, double *m3mr, double *bf_host,
                     double *br_host, std::vector<double> *grid_out);
     int contract(const PointSrc &ps, long long npts, double *m3mf, double *m3mr, double *bf_host, double *br_host);
     int contract_mixed(const PointSrc &ps, long long npts, double *m3mf, double *m3mr);
+    int contract_diag(const PointSrc &ps, long long npts, int msh_form, double *m3mf, double *m3mr,
+                      double *bf_host, double *br_host);
     int run_points(const double *fi, const double *fj, const double *w, double wuniform, long long npts,
                    double *m3mf, double *m3mr, double *bfm, double *brm,
                    const std::vector<ZoneDev> *zones = nullptr, const int *zid = nullptr, const int *zi = nullptr,

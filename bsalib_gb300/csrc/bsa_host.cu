@@ -71,7 +71,7 @@ void Engine::reset_inputs() {
 void Engine::free_device() {
     for (DevBuf *b : {&dL, &dQ, &dLogc, &dPsdPar, &dFrfM, &dFrfK, &dFrfC, &dFreq, &dS, &dA, &dPartF, &dPartR,
                       &dOut, &dPsdF, &dWf, &dPts, &dPtsD, &dBF, &dBR, &dMixA, &dMixB, &dMixH, &dMixPart, &dA32,
-                      &dZones, &dZidx})
+                      &dZones, &dZidx, &dWd3, &dWd2})
         b->release();
     if (stream) cudaStreamDestroy(stream);
     stream = nullptr;
@@ -118,7 +118,6 @@ int Engine::validate() {
     if (I.psd_type == 3 && !I.ubref) return fail(BSA_ERR_STATE, "zone mean wind speeds not set");
     if (I.ncorr != ((long)I.nn * I.nn + I.nn) / 2)
         return fail(BSA_ERR_ARG, "nodal coherence has %lld rows, expected (nn^2+nn)/2", (long long)I.ncorr);
-    if (set.onlyd != 0) return fail(BSA_ERR_UNSUPPORTED, "diagonal-only spectra are not on this path");
     if (set.tc.empty() || set.tc.size() > 3) return fail(BSA_ERR_ARG, "1 to 3 turbulent components");
     for (int tc : set.tc)
         if (tc < 1 || tc > 3) return fail(BSA_ERR_ARG, "turbulent component id out of range");
@@ -192,6 +191,13 @@ int Engine::validate() {
                 hQ[((size_t)itc * nnl + i) * nme + m] = phitc[(size_t)m + (size_t)nme * ((size_t)i + (size_t)nnl * (tc + 2))];
             }
     }
+    // Diagonal-only spectra: the three per-node projected sums of one mode multiply.
+    hWd3.assign((size_t)K * nme, 0.0);
+    hWd2.assign((size_t)K * nme, 0.0);
+    for (size_t x = 0; x < hWd3.size(); ++x) {
+        hWd3[x] = hQ[x] * hL[x] * hL[x];
+        hWd2[x] = hL[x] * hL[x];
+    }
     const long ncorr = (long)I.ncorr;
     hLogc.assign((size_t)ntc * nnl * nnl, 0.0);
     for (int itc = 0; itc < ntc; ++itc)
@@ -246,7 +252,7 @@ int Engine::upload_problem() {
     cudaError_t e;
     if ((e = upload(dL, hL, stream)) || (e = upload(dQ, hQ, stream)) || (e = upload(dLogc, hLogc, stream)) ||
         (e = upload(dPsdPar, hPsd, stream)) || (e = upload(dFrfM, hM, stream)) || (e = upload(dFrfK, hK, stream)) ||
-        (e = upload(dFrfC, hC, stream)))
+        (e = upload(dFrfC, hC, stream)) || (e = upload(dWd3, hWd3, stream)) || (e = upload(dWd2, hWd2, stream)))
         return cuda_fail(e, "uploading problem data");
     dev_uploaded = true;
     return BSA_OK;
@@ -254,8 +260,8 @@ int Engine::upload_problem() {
 
 FrfPar Engine::frf() const { return FrfPar{dFrfM.as<double>(), dFrfK.as<double>(), dFrfC.as<double>()}; }
 
-// Nodal PSD + A(f) for a host list of frequencies, into dA (FP64) or dA32 (FP32) rows.
-int Engine::build_atable(const std::vector<double> &freqs, bool fp32) {
+// Nodal PSD table S[f][k] for a host list of frequencies (into dFreq, dS).
+int Engine::build_psd(const std::vector<double> &freqs) {
     const int nf = (int)freqs.size();
     const int ntc = (int)set.tc.size();
     cudaError_t e;
@@ -264,6 +270,17 @@ int Engine::build_atable(const std::vector<double> &freqs, bool fp32) {
     if ((e = launch_nodal_psd(stream, nf, dFreq.as<double>(), ntc, set.tc.data(), in.nnl, dPsdPar.as<PsdNode>(),
                               in.psd_type, set.defsc, dS.as<double>())))
         return cuda_fail(e, "nodal PSD kernel");
+    kernels += 1;
+    return BSA_OK;
+}
+
+// Nodal PSD + A(f) for a host list of frequencies, into dA (FP64) or dA32 (FP32) rows.
+int Engine::build_atable(const std::vector<double> &freqs, bool fp32) {
+    const int nf = (int)freqs.size();
+    const int ntc = (int)set.tc.size();
+    cudaError_t e;
+    int rc = build_psd(freqs);
+    if (rc) return rc;
     if (fp32) {
         if ((e = dA32.reserve(sizeof(float) * (size_t)nf * K * nme))) return cuda_fail(e, "allocating A");
         e = launch_atable32(stream, nf, dFreq.as<double>(), ntc, in.nnl, nme, dLogc.as<double>(), dS.as<double>(),
@@ -274,7 +291,7 @@ int Engine::build_atable(const std::vector<double> &freqs, bool fp32) {
                           dL.as<double>(), dA.as<double>());
     }
     if (e) return cuda_fail(e, "A-table kernel");
-    kernels += 2;
+    kernels += 1;
     return BSA_OK;
 }
 
@@ -341,8 +358,7 @@ int Engine::run_classic(double *m2mf, double *m2mr, double *m2o2mr, double *m3mf
     // Vectorised / scalar branch (checkMaxAllocation_, BsaClassicImpl.F90:384-434): only the
     // integration weights differ here, the spectra are never stored.
     bool scalar = set.scalar != 0;
-    const long long nm3 = (long long)nme * nme * nme;
-    if (set.test == 0 && !scalar && set.ibisp && (long long)nf * nf * nm3 > 1000000000LL) scalar = true;
+    if (set.test == 0 && !scalar && set.ibisp && (long long)nf * nf * dim_bisp() > 1000000000LL) scalar = true;
     double delta = f[1] - f[0];
     if (set.defsc == 1) delta *= kPi2;
     const bool analytic = !classic_trunc;
@@ -352,28 +368,31 @@ int Engine::run_classic(double *m2mf, double *m2mr, double *m2o2mr, double *m3mf
         const double d = f[1] - f[0];
         for (int s = 0; s < 2 * nf - 1; ++s) ftab.push_back(2.0 * f[0] + s * d);
     }
+    // Diagonal-only spectra read the nodal PSD table alone and stay FP64 (O(K nm) per point).
+    const bool diagonal = set.onlyd != 0;
     // The split-precision contraction reduces to moments only; it reads an FP32 A table.
-    const bool mixed = precision == BSA_PREC_BF16X3 && !bf_host && !br_host;
+    const bool mixed = !diagonal && precision == BSA_PREC_BF16X3 && !bf_host && !br_host;
     if (mixed && nme > 32) return fail(BSA_ERR_UNSUPPORTED, "BF16x3 contraction supports at most 32 kept modes");
     cudaError_t e;
     if ((e = cudaEventRecord(ev0, stream))) return cuda_fail(e, "event");
-    if ((rc = build_atable(ftab, mixed))) return rc;
-    const int nm2 = nme * nme;
+    if ((rc = diagonal ? build_psd(ftab) : build_atable(ftab, mixed))) return rc;
+    const long long nm2 = dim_psd();
     if (set.ipsd && (m2mf || m2mr || m2o2mr)) {
         std::vector<double> wf(nf, scalar ? delta : delta);
         if (!scalar) { wf[0] = delta / 2; wf[nf - 1] = delta / 2; }
         if ((e = upload(dWf, wf, stream))) return cuda_fail(e, "weights");
         if ((e = dPsdF.reserve(sizeof(double) * (size_t)nf * nm2))) return cuda_fail(e, "psd");
-        if ((e = dOut.reserve(sizeof(double) * (3 * (size_t)nm2 + 2 * (size_t)nm3))))
+        if ((e = dOut.reserve(sizeof(double) * (3 * (size_t)nm2 + 2 * (size_t)dim_bisp()))))
             return cuda_fail(e, "out");
-        e = mixed ? launch_force_psd32(stream, nf, (int)set.tc.size(), in.nnl, nme, dL.as<double>(),
-                                       dA32.as<float>(), dPsdF.as<double>())
-                  : launch_force_psd(stream, nf, (int)set.tc.size(), in.nnl, nme, dL.as<double>(), dA.as<double>(),
-                                     dPsdF.as<double>());
+        e = diagonal ? launch_force_psd_diag(stream, nf, K, nme, dS.as<double>(), dWd2.as<double>(), dPsdF.as<double>())
+            : mixed  ? launch_force_psd32(stream, nf, (int)set.tc.size(), in.nnl, nme, dL.as<double>(),
+                                          dA32.as<float>(), dPsdF.as<double>())
+                     : launch_force_psd(stream, nf, (int)set.tc.size(), in.nnl, nme, dL.as<double>(), dA.as<double>(),
+                                        dPsdF.as<double>());
         if (e) return cuda_fail(e, "force PSD kernel");
         double *o = dOut.as<double>();
-        if ((e = launch_m2(stream, r0, r1, nme, dFreq.as<double>(), dWf.as<double>(), dPsdF.as<double>(), frf(), o,
-                           o + nm2, o + 2 * nm2)))
+        if ((e = launch_m2(stream, r0, r1, nme, diagonal ? 1 : 0, dFreq.as<double>(), dWf.as<double>(),
+                           dPsdF.as<double>(), frf(), o, o + nm2, o + 2 * nm2)))
             return cuda_fail(e, "m2 kernel");
         kernels += 2;
         std::vector<double> h(3 * (size_t)nm2);
@@ -399,7 +418,9 @@ int Engine::run_classic(double *m2mf, double *m2mr, double *m2o2mr, double *m3mf
         ps.r0 = r0;
         ps.nr = r1 - r0;
         const long long npts = (long long)(r1 - r0) * nf;
-        rc = mixed ? contract_mixed(ps, npts, m3mf, m3mr) : contract(ps, npts, m3mf, m3mr, bf_host, br_host);
+        rc = diagonal ? contract_diag(ps, npts, 0, m3mf, m3mr, bf_host, br_host)
+             : mixed  ? contract_mixed(ps, npts, m3mf, m3mr)
+                      : contract(ps, npts, m3mf, m3mr, bf_host, br_host);
         if (rc) return rc;
         last_points = (double)npts;
     }
@@ -492,7 +513,7 @@ int Engine::run_points(const double *fi, const double *fj, const double *w, doub
     }
     cudaError_t e;
     if ((e = cudaEventRecord(ev0, stream))) return cuda_fail(e, "event");
-    if ((rc = build_atable(ftab))) return rc;
+    if ((rc = set.onlyd ? build_psd(ftab) : build_atable(ftab))) return rc;
     std::vector<double> f1(fi, fi + npts), f2(fj, fj + npts);
     h2d += (double)npts * (3 * sizeof(int) + (w ? 3 : 2) * sizeof(double));
     const size_t n = (size_t)npts;
@@ -527,7 +548,8 @@ int Engine::run_points(const double *fi, const double *fj, const double *w, doub
         ps.zi = dzi;
         ps.zj = dzj;
     }
-    rc = contract(ps, npts, m3mf, m3mr, bfm, brm);
+    // Mesher functions: the diagonal-only form is getFM_diag_tnm_scalar_msh_'s.
+    rc = set.onlyd ? contract_diag(ps, npts, 1, m3mf, m3mr, bfm, brm) : contract(ps, npts, m3mf, m3mr, bfm, brm);
     if (rc) return rc;
     last_points = (double)npts;
     if ((e = cudaEventRecord(ev1, stream)) || (e = cudaEventSynchronize(ev1))) return cuda_fail(e, "event");
@@ -754,6 +776,11 @@ int bsa_Finalise(void) {
 
 int bsa_computeSkewness(int nm, const double *m2, const double *m3, double *sk) {
     if (nm <= 0 || !m2 || !m3 || !sk) return BSA_ERR_ARG;
+    if (eng().set.onlyd) {
+        // computeSkewness_ diagonal branch (BsaLibImpl.F90:1641-1644): sk = m3 / m2^(3/2).
+        for (int i = 0; i < nm; ++i) sk[i] = m3[i] / std::pow(m2[i], 1.5);
+        return BSA_OK;
+    }
     size_t pm3 = 0;
     for (int k = 0; k < nm; ++k)
         for (int j = 0; j < nm; ++j)
@@ -763,6 +790,16 @@ int bsa_computeSkewness(int nm, const double *m2, const double *m3, double *sk) 
 }
 
 const char *bsa_lastError(void) { return eng().last_error.c_str(); }
+
+int bsa_getSpectraDims(int *dim_psd, int *dim_bisp) {
+    GUARD();
+    bsa::Engine &E = eng();
+    int rc = E.validate();
+    if (rc) return rc;
+    if (dim_psd) *dim_psd = (int)E.dim_psd();
+    if (dim_bisp) *dim_bisp = (int)E.dim_bisp();
+    return BSA_OK;
+}
 
 int bsa_gpu_setPrecision(int prec) {
     GUARD();

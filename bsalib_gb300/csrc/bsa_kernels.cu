@@ -245,12 +245,13 @@ cudaError_t launch_force_psd32(cudaStream_t st, int nf, int ntc, int nnl, int nm
 }
 
 // One block per (n, o) pair; threads stride over frequencies, fixed-order tree reduction.
-__global__ void k_m2(int k0, int k1, int nm, const double *__restrict__ f, const double *__restrict__ wf,
+// diag != 0: psd[f][m] holds the same-mode spectra (length nm), pair (n, o) = (m, m).
+__global__ void k_m2(int k0, int k1, int nm, int diag, const double *__restrict__ f, const double *__restrict__ wf,
                      const double *__restrict__ psd, FrfPar frf, double *m2mf, double *m2mr,
                      double *m2o2mr) {
-    const int nm2 = nm * nm;
+    const int nm2 = diag ? nm : nm * nm;
     const int pr = blockIdx.x;
-    const int n = pr % nm, o = pr / nm;
+    const int n = diag ? pr : pr % nm, o = diag ? pr : pr / nm;
     double sf = 0.0, sr = 0.0, so = 0.0;
     for (int k = k0 + threadIdx.x; k < k1; k += blockDim.x) {
         const double w = f[k] * kPi2;
@@ -280,9 +281,9 @@ __global__ void k_m2(int k0, int k1, int nm, const double *__restrict__ f, const
     }
 }
 
-cudaError_t launch_m2(cudaStream_t st, int k0, int k1, int nm, const double *f, const double *wf,
+cudaError_t launch_m2(cudaStream_t st, int k0, int k1, int nm, int diag, const double *f, const double *wf,
                       const double *psd, FrfPar frf, double *m2mf, double *m2mr, double *m2o2mr) {
-    k_m2<<<nm * nm, 256, 0, st>>>(k0, k1, nm, f, wf, psd, frf, m2mf, m2mr, m2o2mr);
+    k_m2<<<diag ? nm : nm * nm, 256, 0, st>>>(k0, k1, nm, diag, f, wf, psd, frf, m2mf, m2mr, m2o2mr);
     return cudaGetLastError();
 }
 
@@ -290,38 +291,6 @@ cudaError_t launch_m2(cudaStream_t st, int k0, int k1, int nm, const double *f, 
 // Stages (b)+(c) in FP64, one block per (point group, tile of NOT (n,o) pairs).
 // ------------------------------------------------------------------------------------
 constexpr int KC = 32;
-
-__device__ __forceinline__ void get_point(const PointSrc &ps, long long p, int &ix, int &iy, int &iz,
-                                          double &w, double &f1, double &f2) {
-    if (ps.mode == kPointsGrid) {
-        const int nf = ps.nf;
-        const int i1 = ps.r0 + (int)(p % ps.nr), i2 = (int)(p / ps.nr);
-        ix = i1;
-        iy = i2;
-        const int s = i1 + i2;
-        if (ps.trunc) {
-            const int c = s - ps.n_pad;
-            iz = (c >= 0 && c < nf) ? c : -1;
-        } else {
-            iz = ps.sum_base + s;
-        }
-        f1 = ps.fgrid[i1];
-        f2 = ps.fgrid[i2];
-        if (ps.wmode == kWeightClassicVect) {
-            const bool b1 = (i1 == 0 || i1 == nf - 1), b2 = (i2 == 0 || i2 == nf - 1);
-            w = ps.wval * ((b1 && b2) ? -0.5 : ((b1 || b2) ? 0.5 : 1.0));
-        } else {
-            w = ps.wval;
-        }
-    } else {
-        ix = ps.ix[p];
-        iy = ps.iy[p];
-        iz = ps.iz[p];
-        f1 = ps.f1[p];
-        f2 = ps.f2[p];
-        w = (ps.wmode == kWeightList) ? ps.w[p] : ps.wval;
-    }
-}
 
 template <int NOT, int MT>
 __global__ __launch_bounds__(256) void k_bfm_fp64(const double *__restrict__ A,

@@ -24,9 +24,14 @@ cudaError_t launch_force_psd(cudaStream_t st, int nf, int ntc, int nnl, int nm, 
                              const double *A, double *psd);
 cudaError_t launch_force_psd32(cudaStream_t st, int nf, int ntc, int nnl, int nm, const double *L,
                                const float *A, double *psd);
-// Second-order moments over the grid frequencies k in [k0, k1).
-cudaError_t launch_m2(cudaStream_t st, int k0, int k1, int nm, const double *f, const double *wf,
+// Second-order moments over the grid frequencies k in [k0, k1); diag != 0 for the
+// same-mode spectra psd[f][m].
+cudaError_t launch_m2(cudaStream_t st, int k0, int k1, int nm, int diag, const double *f, const double *wf,
                       const double *psd, FrfPar frf, double *m2mf, double *m2mr, double *m2o2mr);
+
+// Diagonal-only force PSD psd[f][m] = sum_k W2[k][m] S[f][k], W2 = L^2 (functionsImpl.F90:1924-1947).
+cudaError_t launch_force_psd_diag(cudaStream_t st, int nf, int K, int nm, const double *S, const double *W2,
+                                  double *psd);
 
 // FP64 BFM contraction + FRF + weighted reduction over a point set.
 //   B_F[m,n,o](p) = 2 sum_k ( Q_km X_kn Y_ko + Z_km (Q_kn Y_ko + X_kn Q_ko) ),

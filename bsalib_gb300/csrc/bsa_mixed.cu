@@ -53,6 +53,7 @@ struct Params {
     int Mp;          // rows per frequency in U (nm^2 rounded up to 128)
     int MT;          // Mp / 128
     int nk;          // K chunks (Kp / 64)
+    int ks_last;     // 16-wide K steps of the last chunk that hold data (the rest is zero padding)
     int n_ntiles;    // ceil(nf / NC)
     int wmode;       // kWeightClassicVect or kWeightUniform
     double wval;
@@ -260,8 +261,11 @@ __global__ void __launch_bounds__(192, 1)
                         if (!mbar_wait(&full[s], ph, err, 3)) { ok = false; break; }
                         fence_after();
                         const uint32_t base = su32(smem + s * kStageBytes);
+                        // K steps past the data in the last chunk multiply zero padding: skip them
+                        const int nks = kc == p.nk - 1 ? p.ks_last : kBK / 16;
 #pragma unroll
                         for (int ks = 0; ks < kBK / 16; ++ks) {
+                            if (ks >= nks) break;
                             const uint32_t off = ks * 32;
                             const uint64_t uh = sdesc(base + 0 * kTileBytes + off), ul = sdesc(base + 1 * kTileBytes + off);
                             const uint64_t gh = sdesc(base + 2 * kTileBytes + off), gl = sdesc(base + 3 * kTileBytes + off);
@@ -592,6 +596,7 @@ int Engine::contract_mixed(const PointSrc &ps, long long npts, double *m3mf, dou
     prm.Mp = Mp;
     prm.MT = MT;
     prm.nk = Kp / kBK;
+    prm.ks_last = (K - (prm.nk - 1) * kBK + 15) / 16;
     prm.n_ntiles = (nf + NC - 1) / NC;
     prm.wmode = ps.wmode;
     prm.wval = ps.wval;

@@ -10,7 +10,7 @@
  *     Setters BORROW the caller's arrays, exactly like the reference (which keeps Fortran
  *     pointers to them): they must stay alive until bsa_Finalise.  bsa_Run writes into
  *     caller-owned buffers (the reference allocates them; here the caller sizes them with
- *     bsa_getNModesEff: nm^2 for m2*, nm^3 for m3*).
+ *     bsa_getSpectraDims: nm^2 for m2*, nm^3 for m3*, nm for both with diagonal-only spectra).
  *
  *  2. The reference's device offload ABI, BsaCL (BsaCL/include/bsacl.h:28-55), with the
  *     same names and argument meaning, so a Fortran host built with BSA_USE_GPU can link
@@ -58,7 +58,7 @@ int bsa_setAnalysisType(int isuban);           /* BsaLibImpl.F90:909, 1 classic 
 int bsa_setVersion(int ivers);                 /* BsaLibImpl.F90:923                          */
 int bsa_setScalingConv(int iconv);             /* BsaLibImpl.F90:930, 1 circular 2 frequency  */
 int bsa_setSpectraComputation(int ipsd, int ibisp); /* BsaLibImpl.F90:937                     */
-int bsa_setSpectraExtension(int ionlydiag);    /* BsaLibImpl.F90:945 (only 0 = full is on the path) */
+int bsa_setSpectraExtension(int ionlydiag);    /* BsaLibImpl.F90:945, 1 = diagonal-only spectra */
 int bsa_setSpatialSymmetry(int isym);          /* BsaLibImpl.F90:750                          */
 int bsa_setSpectraSymmetries(int isym);        /* BsaLibImpl.F90:771                          */
 int bsa_setTestMode(int itest);                /* BsaLibImpl.F90:951                          */
@@ -100,16 +100,25 @@ int bsa_setWindFCoeffs(const double *wfc, int nlibs_l, int ndegw3, int nn_l); /*
  * the number of kept modes, which sizes bsa_Run's outputs. */
 int bsa_getNModesEff(int *nm_eff);
 
+/* Lengths of one PSD and one bispectrum tensor, dimM_psd_ / dimM_bisp_
+ * (src/bsa/data/BsaLibData.F90:60-64, set at BsaLibImpl.F90:313-355): nm^2 / nm^3, or nm / nm
+ * with the diagonal-only spectra (bsa_setSpectraExtension(1)).  These size bsa_Run's
+ * outputs and every per-point tensor below. */
+int bsa_getSpectraDims(int *dim_psd, int *dim_bisp);
+
 /* bsa_Run, src/BsaLib.F90:372-399 (BsaLibImpl.F90:153-462).  Classic outputs m2mf_cls,
- * m2mr_cls, m2o2mr_cls (nm^2), m3mf_cls, m3mr_cls (nm^3); Mesher outputs m3mf_msh,
- * m3mr_msh (nm^3).  Any pointer may be NULL when not wanted. */
+ * m2mr_cls, m2o2mr_cls (dim_psd), m3mf_cls, m3mr_cls (dim_bisp); Mesher outputs m3mf_msh,
+ * m3mr_msh (dim_bisp).  Any pointer may be NULL when not wanted.  The diagonal-only
+ * spectra always run in FP64, whatever bsa_gpu_setPrecision says. */
 int bsa_Run(double *m2mf_cls, double *m2mr_cls, double *m2o2mr_cls, double *m3mf_msh,
             double *m3mr_msh, double *m3mf_cls, double *m3mr_cls);
 
 /* bsa_Finalise, src/BsaLib.F90:401 (cleanBSAData_): drop borrowed pointers, free device memory. */
 int bsa_Finalise(void);
 
-/* computeSkewness_ (BsaLibImpl.F90:1630-1707): sk = m3_mno / (sig_m sig_n sig_o). */
+/* computeSkewness_ (BsaLibImpl.F90:1630-1707): sk = m3_mno / (sig_m sig_n sig_o); with the
+ * diagonal-only spectra selected (bsa_setSpectraExtension(1)) m2, m3 and sk have length nm
+ * and sk = m3 / m2^(3/2), as the reference's module state selects. */
 int bsa_computeSkewness(int nm, const double *m2, const double *m3, double *sk);
 
 const char *bsa_lastError(void);
@@ -162,13 +171,15 @@ int bsa_gpu_setClassicTruncation(int on);
 int bsa_gpu_setClassicRows(int r_begin, int r_end);
 
 /* getBFMClsVect + getBRMClsVect materialised (functionsImpl.F90:1312-1738): force and
- * response bispectra on the classic grid, (nf, nf, nm^3) with f1 fastest, and the grid.
+ * response bispectra on the classic grid, (nf, nf, dim_bisp) with f1 fastest, and the grid.
  * Runs validation and the grid set-up of bsa_Run; for small grids (tests). */
 int bsa_gpu_clsBispectra(double *f_out, int nf_cap, int *nf, double *bisp_f, double *bisp_r);
 
 /* getMshBFM / getMshBRM batched over npts arbitrary points (getFM_full_tnm_scalar_msh_,
  * functionsImpl.F90:247-465; getRM_full_scalar_msh_, :1031-1115, point-wise): bfm and brm
- * are (nm^3, npts); either may be NULL. */
+ * are (dim_bisp, npts); either may be NULL.  With the diagonal-only spectra these are the
+ * Mesher's diagonal functions (getFM_diag_tnm_scalar_msh_, :1123-1210, whose products read
+ * S(fi) S(fj) where the Classic form reads S(fi+fj); kept as written). */
 int bsa_gpu_mshBispectra(const double *fi, const double *fj, int npts, double *bfm, double *brm);
 
 /* Weighted moments over an arbitrary point set (the Mesher's zone integration,

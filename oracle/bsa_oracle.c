@@ -822,11 +822,17 @@ int orc_num_threads(void)
  * BRM (getRM_full_scalar_msh_) at every BRM point and its trapezoid weights with
  * (dwI / Fi)(dwJ / Fj).  Both integrals times sym are added to m3mf / m3mr (nm^3).
  */
-int orc_rect_zone(const orc_problem *P, double fi0, double fj0, double dIi, double dIj, double dJi, double dJj,
-                  int ni, int nj, int Fi, int Fj, double sym, double *m3mf, double *m3mr)
+int orc_msh_bfm_diag(const orc_problem *P, double fi, double fj, double *bfm);
+void orc_msh_brm_diag(const orc_problem *P, int nfi, const double *fi, int nfj, const double *fj,
+                      const double *bfm, double *brm);
+
+static int rect_zone_impl(const orc_problem *P, double fi0, double fj0, double dIi, double dIj, double dJi,
+                          double dJj, int ni, int nj, int Fi, int Fj, double sym, int diag, double *m3mf,
+                          double *m3mr)
 {
     const int nme = P->nm_eff;
-    const size_t nm3 = (size_t)nme * nme * nme;
+    /* per-point tensor length: nm^3, or nm for the diagonal-only spectra */
+    const size_t nm3 = diag ? (size_t)nme : (size_t)nme * nme * nme;
     if (ni < 2 || nj < 2 || Fi < 1 || Fj < 1 || nme > 256) return -1;
     double *bfm = malloc(sizeof(double) * nm3 * (size_t)ni * nj);
     double *tmp = malloc(sizeof(double) * nm3), *brm = malloc(sizeof(double) * nm3);
@@ -834,7 +840,8 @@ int orc_rect_zone(const orc_problem *P, double fi0, double fj0, double dIi, doub
     for (int i = 0; i < ni; ++i)
         for (int j = 0; j < nj; ++j) {
             const double f1 = fi0 + i * dIi + j * dJi, f2 = fj0 + i * dIj + j * dJj;
-            int rc = orc_msh_bfm_direct(P, f1, f2, bfm + nm3 * ((size_t)i * nj + j));
+            int rc = diag ? orc_msh_bfm_diag(P, f1, f2, bfm + nm3 * ((size_t)i * nj + j))
+                          : orc_msh_bfm_direct(P, f1, f2, bfm + nm3 * ((size_t)i * nj + j));
             if (rc) { free(bfm); free(tmp); free(brm); return rc; }
         }
     const double dwI = sqrt(dIi * dIi + dIj * dIj) * PIt2, dwJ = sqrt(dJi * dJi + dJj * dJj) * PIt2;
@@ -858,7 +865,10 @@ int orc_rect_zone(const orc_problem *P, double fi0, double fj0, double dIi, doub
             }
             const double a = (double)qi / Fi, bq = (double)qj / Fj;
             const double f1 = fi0 + a * dIi + bq * dJi, f2 = fj0 + a * dIj + bq * dJj;
-            orc_msh_brm(P, 1, &f1, 1, &f2, tmp, brm);
+            if (diag)
+                orc_msh_brm_diag(P, 1, &f1, 1, &f2, tmp, brm);
+            else
+                orc_msh_brm(P, 1, &f1, 1, &f2, tmp, brm);
             const double w = sym * (dwI / Fi) * (dwJ / Fj) * ((qi == 0 || qi == NI) ? 0.5 : 1.0) *
                              ((qj == 0 || qj == NJ) ? 0.5 : 1.0);
             for (size_t x = 0; x < nm3; ++x) m3mr[x] += w * brm[x];
@@ -866,3 +876,338 @@ int orc_rect_zone(const orc_problem *P, double fi0, double fj0, double dIi, doub
     free(bfm); free(tmp); free(brm);
     return 0;
 }
+
+int orc_rect_zone(const orc_problem *P, double fi0, double fj0, double dIi, double dIj, double dJi, double dJj,
+                  int ni, int nj, int Fi, int Fj, double sym, double *m3mf, double *m3mr)
+{
+    return rect_zone_impl(P, fi0, fj0, dIi, dIj, dJi, dJj, ni, nj, Fi, Fj, sym, 0, m3mf, m3mr);
+}
+
+/* The same zone with the diagonal-only Mesher functions (m3mf / m3mr of length nm). */
+int orc_rect_zone_diag(const orc_problem *P, double fi0, double fj0, double dIi, double dIj, double dJi,
+                       double dJj, int ni, int nj, int Fi, int Fj, double sym, double *m3mf, double *m3mr)
+{
+    return rect_zone_impl(P, fi0, fj0, dIi, dIj, dJi, dJj, ni, nj, Fi, Fj, sym, 1, m3mf, m3mr);
+}
+
+/* ======================================================================================
+ * Diagonal-only spectra (settings i_only_diag_ = 1, bound at src/bsa/BsaLibImpl.F90:313-336):
+ * same-node, same-mode tensors, dimM_psd_ = dimM_bisp_ = nm.  These follow the reference's
+ * loops over the loaded-DOF triple with the raw force coefficients and modal matrix.
+ * ====================================================================================== */
+#define WFCR(l, c, in) P->wfc[I3(P->libs_load[l] - 1, (c), (in), P->nlibsl, P->ndegw3)]
+#define PHIR(row, m) P->phi[I2((row)-1, (m)-1, P->ndofs)]
+
+/*
+ * getFM_diag_tnlm_vect_cls_ (functionsImpl.F90:1747-1968).  Per (tc, node): the padded
+ * S(f1+f2) (zero beyond the grid), tmp1 = S(f1+f2) S(f2), tmp2 = S(f1+f2) S(f1),
+ * tmp3 = S(f1) S(f2); BF = 2 (q_i l_j l_k tmp3 + l_i q_j l_k tmp1 + l_i l_j q_k tmp2) over
+ * the DOF triple (k, j, i), times phi_k phi_j phi_i of each kept mode.
+ * psd(nf, nm) += phi_j phi_k l_j l_k S(f); bisp(nf, nf, nm) with f1 fastest.
+ */
+int orc_cls_vect_bfm_diag(const orc_problem *P, int nf, const double *f, const double *Suvw, int compute_bisp,
+                          double *psd, double *bisp)
+{
+    const int nnl = P->nnl, nme = P->nm_eff, nl = P->nlibsl;
+    const int n_pad = (nf - 1) / 2, pad_len = (nf - 1) + nf;
+    (void)f;
+    double *Spad = calloc((size_t)pad_len, sizeof(double));
+    double *t1 = malloc(sizeof(double) * (size_t)nf * nf), *t2 = malloc(sizeof(double) * (size_t)nf * nf);
+    double *t3 = malloc(sizeof(double) * (size_t)nf * nf);
+    if (!Spad || !t1 || !t2 || !t3) { free(Spad); free(t1); free(t2); free(t3); return -3; }
+    for (size_t x = 0; x < (size_t)nf * nme; ++x) psd[x] = 0.0;
+    if (compute_bisp)
+        for (size_t x = 0; x < (size_t)nf * nf * nme; ++x) bisp[x] = 0.0;
+    for (int itc = 0; itc < P->ntc; ++itc) {
+        const int tc = P->tc[itc], tcl = tc - 1, tcq = tc + 2;
+        for (int in = 0; in < nnl; ++in) {
+            const int posN = (P->n_load[in] - 1) * P->nlibs;
+            const double *S = Suvw + (size_t)nf * ((size_t)itc * nnl + in);
+            if (compute_bisp) {
+                for (int k = 0; k < nf; ++k) Spad[n_pad + k] = S[k];
+                for (int j = 0; j < nf; ++j)
+                    for (int i = 0; i < nf; ++i) {
+                        const double s12 = Spad[i + j];
+                        t1[I2(i, j, nf)] = s12 * S[j];
+                        t2[I2(i, j, nf)] = s12 * S[i];
+                        t3[I2(i, j, nf)] = S[i] * S[j];
+                    }
+                for (int lk = 0; lk < nl; ++lk) {
+                    const int posk = posN + P->libs_load[lk];
+                    const double akU = WFCR(lk, tcl, in), ak = WFCR(lk, tcq, in);
+                    for (int lj = 0; lj < nl; ++lj) {
+                        const int posj = posN + P->libs_load[lj];
+                        const double ajU = WFCR(lj, tcl, in), aj = WFCR(lj, tcq, in);
+                        for (int li = 0; li < nl; ++li) {
+                            const int posi = posN + P->libs_load[li];
+                            const double aiU = WFCR(li, tcl, in), ai = WFCR(li, tcq, in);
+                            const double c3 = ai * ajU * akU, c1 = aiU * aj * akU, c2 = aiU * ajU * ak;
+                            for (int im = 0; im < nme; ++im) {
+                                const int m = P->modes[im];
+                                const double ph = PHIR(posk, m) * PHIR(posj, m) * PHIR(posi, m);
+                                double *b = bisp + (size_t)nf * nf * im;
+                                for (size_t x = 0; x < (size_t)nf * nf; ++x) {
+                                    const double bf = 2.0 * ((c3 * t3[x]) + (c1 * t1[x]) + (c2 * t2[x]));
+                                    b[x] = b[x] + ph * bf;
+                                }
+                            }
+                        }
+                    }
+                }
+            }
+            for (int lk = 0; lk < nl; ++lk) {
+                const int posk = posN + P->libs_load[lk];
+                const double akU = WFCR(lk, tcl, in);
+                for (int lj = 0; lj < nl; ++lj) {
+                    const int posj = posN + P->libs_load[lj];
+                    const double ajU = WFCR(lj, tcl, in);
+                    for (int im = 0; im < nme; ++im) {
+                        const int m = P->modes[im];
+                        const double ph = PHIR(posj, m) * PHIR(posk, m);
+                        double *p = psd + (size_t)nf * im;
+                        for (int k = 0; k < nf; ++k) p[k] = p[k] + ph * (ajU * akU * S[k]);
+                    }
+                }
+            }
+        }
+    }
+    free(Spad); free(t1); free(t2); free(t3);
+    return 0;
+}
+
+/*
+ * getRM_diag_vect_cls_ (functionsImpl.F90:1974-2101), in place: psd(:, m) *= |H_m|^2,
+ * bisp(:, :, m) *= Re[H_m(w1) H_m(w2) conj H_m(w1 + w2)].
+ */
+void orc_cls_vect_brm_diag(const orc_problem *P, int nf, const double *f, int compute_bisp, double *psd,
+                           double *bisp)
+{
+    const int nme = P->nm_eff;
+    double *Hr = malloc(sizeof(double) * nf), *Hi = malloc(sizeof(double) * nf);
+    for (int im = 0; im < nme; ++im) {
+        for (int k = 0; k < nf; ++k) frf(P, im, f[k] * PIt2, &Hr[k], &Hi[k]);
+        double *p = psd + (size_t)nf * im;
+        for (int k = 0; k < nf; ++k) p[k] = p[k] * (Hr[k] * Hr[k] + Hi[k] * Hi[k]);
+        if (!compute_bisp) continue;
+        double *b = bisp + (size_t)nf * nf * im;
+        for (int j = 0; j < nf; ++j)
+            for (int i = 0; i < nf; ++i) {
+                double h12r, h12i;
+                frf(P, im, f[i] * PIt2 + f[j] * PIt2, &h12r, &h12i);
+                b[I2(i, j, nf)] = b[I2(i, j, nf)] * (Hr[i] * Hr[j] * h12r + Hr[i] * Hi[j] * h12i +
+                                                     Hi[i] * Hr[j] * h12i - Hi[i] * Hi[j] * h12r);
+            }
+    }
+    free(Hr); free(Hi);
+}
+
+/* Classic driver, vectorised branch, diagonal-only (m2* and m3* of length nm). */
+int orc_classic_vect_diag(const orc_problem *P, int nf, const double *f, double *m2mf, double *m2mr,
+                          double *m2o2mr, double *m3mf, double *m3mr, double *bf, double *br)
+{
+    const int nnl = P->nnl, nme = P->nm_eff;
+    double *S = malloc(sizeof(double) * (size_t)nf * nnl * P->ntc);
+    double *psd = malloc(sizeof(double) * (size_t)nf * nme);
+    double *bisp = malloc(sizeof(double) * (size_t)nf * nf * nme);
+    if (!S || !psd || !bisp) { free(S); free(psd); free(bisp); return -3; }
+    for (int itc = 0; itc < P->ntc; ++itc)
+        if (orc_eval_psd(P, nf, f, P->tc[itc], S + (size_t)nf * nnl * itc)) { free(S); free(psd); free(bisp); return -1; }
+    int rc = orc_cls_vect_bfm_diag(P, nf, f, S, 1, psd, bisp);
+    if (rc) { free(S); free(psd); free(bisp); return rc; }
+    orc_intg_vect(nf, f, P->scaling, nme, m2mf ? psd : NULL, m2mf, nme, m3mf ? bisp : NULL, m3mf);
+    if (bf) memcpy(bf, bisp, sizeof(double) * (size_t)nf * nf * nme);
+    orc_cls_vect_brm_diag(P, nf, f, 1, psd, bisp);
+    orc_intg_vect(nf, f, P->scaling, nme, m2mr ? psd : NULL, m2mr, nme, m3mr ? bisp : NULL, m3mr);
+    if (br) memcpy(br, bisp, sizeof(double) * (size_t)nf * nf * nme);
+    if (m2o2mr) {
+        for (int c = 0; c < nme; ++c)
+            for (int k = 0; k < nf; ++k) {
+                const double w = f[k] * PIt2;
+                psd[k + (size_t)nf * c] = psd[k + (size_t)nf * c] * w * w;
+            }
+        orc_intg_vect(nf, f, P->scaling, nme, psd, m2o2mr, 0, NULL, NULL);
+    }
+    free(S); free(psd); free(bisp);
+    return 0;
+}
+
+/*
+ * getFM_diag_tnlm_scalar_cls_ (functionsImpl.F90:2460-2560) at one grid pair (ii, ij),
+ * 0-based: psd(nm) only when ij == 0; Suvw_pad(nnl*ntc) is S at f1+f2 (zero beyond the grid).
+ */
+void orc_cls_scalar_pair_diag(const orc_problem *P, int nf, int ii, int ij, const double *Suvw,
+                              const double *Suvw_pad, int compute_bisp, double *psd, double *bisp)
+{
+    const int nnl = P->nnl, nme = P->nm_eff, nl = P->nlibsl;
+    for (int m = 0; m < nme; ++m) { psd[m] = 0.0; bisp[m] = 0.0; }
+    int iposN = 0;
+    for (int itc = 0; itc < P->ntc; ++itc) {
+        const int tc = P->tc[itc], tcl = tc - 1, tcq = tc + 2;
+        for (int in = 0; in < nnl; ++in, ++iposN) {
+            const int posNi = (P->n_load[in] - 1) * P->nlibs;
+            const double Si = Suvw[I2(ii, iposN, nf)];
+            if (ij == 0) {
+                for (int im = 0; im < nme; ++im) {
+                    const int m = P->modes[im];
+                    double s = 0.0;
+                    for (int l2 = 0; l2 < nl; ++l2)
+                        for (int l1 = 0; l1 < nl; ++l1) {
+                            const double phij = PHIR(posNi + P->libs_load[l1], m) * PHIR(posNi + P->libs_load[l2], m);
+                            s += phij * ((WFCR(l1, tcl, in) * WFCR(l2, tcl, in)) * Si);
+                        }
+                    psd[im] = psd[im] + s;
+                }
+            }
+            if (!compute_bisp) continue;
+            const double Sj = Suvw[I2(ij, iposN, nf)], Sij = Suvw_pad[iposN];
+            for (int lk = 0; lk < nl; ++lk) {
+                const double akU = WFCR(lk, tcl, in), ak = WFCR(lk, tcq, in);
+                for (int im = 0; im < nme; ++im) {
+                    const int m = P->modes[im];
+                    const double phik = PHIR(posNi + P->libs_load[lk], m);
+                    double s = 0.0;
+                    for (int l2 = 0; l2 < nl; ++l2)
+                        for (int l1 = 0; l1 < nl; ++l1) {
+                            const double tmp1 = (WFCR(l1, tcq, in) * WFCR(l2, tcl, in)) * (Si * Sj);
+                            const double tmp2 = (WFCR(l1, tcl, in) * WFCR(l2, tcq, in)) * (Sij * Sj);
+                            const double tmp3 = (WFCR(l1, tcl, in) * WFCR(l2, tcl, in)) * (Sij * Si);
+                            const double bf = 2.0 * ((tmp1 * akU) + (tmp2 * akU) + (tmp3 * ak));
+                            const double phij = PHIR(posNi + P->libs_load[l1], m) * PHIR(posNi + P->libs_load[l2], m);
+                            s += (phij * bf) * phik;
+                        }
+                    bisp[im] = bisp[im] + s;
+                }
+            }
+        }
+    }
+}
+
+/* getRM_diag_scalar_cls_ (functionsImpl.F90:2562-2637). */
+void orc_cls_scalar_brm_diag(const orc_problem *P, int ij, double fi, double fj, const double *psdin,
+                             double *psdout, const double *bispin, double *bispout)
+{
+    const int nme = P->nm_eff;
+    const double wi = fi * PIt2, wj = fj * PIt2;
+    for (int m = 0; m < nme; ++m) {
+        double h1r, h1i, h2r, h2i, h3r, h3i;
+        frf(P, m, wi, &h1r, &h1i);
+        frf(P, m, wj, &h2r, &h2i);
+        frf(P, m, wi + wj, &h3r, &h3i);
+        if (ij == 0) psdout[m] = psdin[m] * (h1r * h1r + h1i * h1i);
+        bispout[m] = bispin[m] * (h1r * h2r * h3r + h1r * h2i * h3i + h1i * h2r * h3i - h1i * h2i * h3r);
+    }
+}
+
+/* Classic driver, scalar branch, diagonal-only (uniform dw^2 weights, rectangle m2). */
+int orc_classic_scalar_diag(const orc_problem *P, int nf, const double *f, double *m2mf, double *m2mr,
+                            double *m2o2mr, double *m3mf, double *m3mr)
+{
+    const int nnl = P->nnl, nme = P->nm_eff, npsd = nnl * P->ntc;
+    double *S = malloc(sizeof(double) * (size_t)nf * npsd);
+    for (int itc = 0; itc < P->ntc; ++itc)
+        if (orc_eval_psd(P, nf, f, P->tc[itc], S + (size_t)nf * nnl * itc)) { free(S); return -1; }
+    const int lp = (nf - 1) / 2, lpad = 2 * lp + nf;
+    double *Spad = calloc((size_t)npsd * lpad, sizeof(double));
+    for (int c = 0; c < npsd; ++c)
+        for (int k = 0; k < nf; ++k) Spad[I2(c, lp + k, npsd)] = S[I2(k, c, nf)];
+    const double dw = (f[1] - f[0]) * PIt2, dw2 = dw * dw;
+    double *bf = malloc(sizeof(double) * nme), *br = malloc(sizeof(double) * nme);
+    double *pf = malloc(sizeof(double) * nme), *pr = malloc(sizeof(double) * nme);
+    double *psdfm = calloc(nme, sizeof(double)), *psdrm = calloc(nme, sizeof(double));
+    for (int m = 0; m < nme; ++m) { m2mf[m] = 0; m2mr[m] = 0; m2o2mr[m] = 0; m3mf[m] = 0; m3mr[m] = 0; }
+    for (int ifr = 0; ifr < nf; ++ifr) {
+        const double fi = f[ifr], omg = fi * PIt2;
+        for (int jfr = 0; jfr < nf; ++jfr) {
+            orc_cls_scalar_pair_diag(P, nf, ifr, jfr, S, Spad + (size_t)npsd * (ifr + jfr), 1, pf, bf);
+            orc_cls_scalar_brm_diag(P, jfr, fi, f[jfr], pf, pr, bf, br);
+            for (int m = 0; m < nme; ++m) {
+                m3mf[m] = m3mf[m] + bf[m] * dw2;
+                m3mr[m] = m3mr[m] + br[m] * dw2;
+            }
+            if (jfr == 0) { memcpy(psdfm, pf, sizeof(double) * nme); memcpy(psdrm, pr, sizeof(double) * nme); }
+        }
+        for (int m = 0; m < nme; ++m) {
+            m2mf[m] = m2mf[m] + psdfm[m] * dw;
+            const double r = psdrm[m] * dw;
+            m2mr[m] = m2mr[m] + r;
+            m2o2mr[m] = m2o2mr[m] + r * omg * omg;
+        }
+    }
+    free(S); free(Spad); free(bf); free(br); free(pf); free(pr); free(psdfm); free(psdrm);
+    return 0;
+}
+
+/*
+ * getFM_diag_tnm_scalar_msh_ (functionsImpl.F90:1123-1210): diagonal-only Mesher BFM at
+ * one point.  The reference evaluates S(fi+fj) but never reads it: its products are
+ * S_IJ = S(fi) S(fj), S_IJJ = S_IJ S(fj), S_IJI = S_IJ S(fi), with
+ * BF = 2 (q_i l_j S_IJ l_k + l_i q_j S_IJJ l_k + l_i l_j S_IJI q_k).  Kept as written.
+ */
+int orc_msh_bfm_diag(const orc_problem *P, double fi, double fj, double *bfm)
+{
+    const int nnl = P->nnl, nme = P->nm_eff, nl = P->nlibsl;
+    for (int l = 0; l < nl; ++l)
+        if (P->libs_load[l] > nl) return -1;
+    for (int m = 0; m < nme; ++m) bfm[m] = 0.0;
+    double *Sfi = malloc(sizeof(double) * nnl), *Sfj = malloc(sizeof(double) * nnl);
+    for (int itc = 0; itc < P->ntc; ++itc) {
+        const int tc = P->tc[itc], tcl = tc - 1, tcq = tc + 2;
+        orc_eval_psd(P, 1, &fi, tc, Sfi);
+        orc_eval_psd(P, 1, &fj, tc, Sfj);
+        for (int in = 0; in < nnl; ++in) {
+            const int posi = (P->n_load[in] - 1) * P->nlibs;
+            const double sij = Sfi[in] * Sfj[in];
+            const double sijj = sij * Sfj[in], siji = sij * Sfi[in];
+            for (int lk = 0; lk < nl; ++lk) {
+                const double akU = WFCR(lk, tcl, in), ak = WFCR(lk, tcq, in);
+                for (int im = 0; im < nme; ++im) {
+                    const int m = P->modes[im];
+                    const double phik = PHIR(posi + P->libs_load[lk], m);
+                    double s = 0.0;
+                    for (int l2 = 0; l2 < nl; ++l2)
+                        for (int l1 = 0; l1 < nl; ++l1) {
+                            const double tmp1 = sij * (WFCR(l1, tcq, in) * WFCR(l2, tcl, in));
+                            const double tmp2 = sijj * (WFCR(l1, tcl, in) * WFCR(l2, tcq, in));
+                            const double tmp3 = siji * (WFCR(l1, tcl, in) * WFCR(l2, tcl, in));
+                            const double bf = 2.0 * ((tmp1 * akU) + (tmp2 * akU) + (tmp3 * ak));
+                            const double ph = (PHIR(posi + P->libs_load[l1], m) * PHIR(posi + P->libs_load[l2], m)) * phik;
+                            s += bf * ph;
+                        }
+                    bfm[im] = bfm[im] + s;
+                }
+            }
+        }
+    }
+    free(Sfi); free(Sfj);
+    return 0;
+}
+
+/* getRM_diag_scalar_msh_ (functionsImpl.F90:1212-1286): bfm/brm are (nm, nfi*nfj), fj fastest. */
+void orc_msh_brm_diag(const orc_problem *P, int nfi, const double *fi, int nfj, const double *fj,
+                      const double *bfm, double *brm)
+{
+    const int nme = P->nm_eff;
+    size_t posf = 0;
+    for (int i = 0; i < nfi; ++i) {
+        const double wi = fi[i] * PIt2;
+        for (int j = 0; j < nfj; ++j, ++posf) {
+            const double wj = fj[j] * PIt2;
+            for (int m = 0; m < nme; ++m) {
+                double h1r, h1i, h2r, h2i, h3r, h3i;
+                frf(P, m, wi, &h1r, &h1i);
+                frf(P, m, wj, &h2r, &h2i);
+                frf(P, m, wi + wj, &h3r, &h3i);
+                brm[m + nme * posf] = bfm[m + nme * posf] *
+                                      (h1r * h2r * h3r + h1r * h2i * h3i + h1i * h2r * h3i - h1i * h2i * h3r);
+            }
+        }
+    }
+}
+
+/* computeSkewness_ (BsaLibImpl.F90:1641-1644), diagonal branch: sk = m3 / m2^(3/2). */
+void orc_skewness_diag(int dim, const double *m2, const double *m3, double *sk)
+{
+    for (int i = 0; i < dim; ++i) sk[i] = m3[i] / pow(m2[i], 1.5);
+}
+#undef WFCR
+#undef PHIR

@@ -64,6 +64,12 @@ def lib():
         _lib.orc_skewness.argtypes = [C.c_int, vp, vp, vp]
         _lib.orc_modal_recomb.argtypes = [C.c_int, C.c_int, vp, vp, vp, vp, vp, vp]
         _lib.orc_rect_zone.argtypes = [vp] + [C.c_double] * 6 + [C.c_int] * 4 + [C.c_double, vp, vp]
+        _lib.orc_rect_zone_diag.argtypes = _lib.orc_rect_zone.argtypes
+        _lib.orc_classic_vect_diag.argtypes = [vp, C.c_int, vp] + [vp] * 7
+        _lib.orc_classic_scalar_diag.argtypes = [vp, C.c_int, vp] + [vp] * 5
+        _lib.orc_msh_bfm_diag.argtypes = [vp, C.c_double, C.c_double, vp]
+        _lib.orc_msh_brm_diag.argtypes = [vp, C.c_int, vp, C.c_int, vp, vp, vp]
+        _lib.orc_skewness_diag.argtypes = [C.c_int, vp, vp, vp]
     return _lib
 
 
@@ -226,6 +232,60 @@ class Oracle:
         if rc:
             raise RuntimeError(f"orc_rect_zone failed ({rc})")
         return mf, mr
+
+    # -- a16: diagonal-only spectra (length-nm tensors) -------------------------------------
+    def classic_vect_diag(self, f=None, keep_bisp=True):
+        f = self.freqs() if f is None else np.ascontiguousarray(f, dtype=np.float64)
+        nf, nm = f.size, self.nme
+        out = {k: np.zeros(nm) for k in ("m2mf", "m2mr", "m2o2mr", "m3mf", "m3mr")}
+        bf = np.zeros((nf, nf, nm), order="F") if keep_bisp else None
+        br = np.zeros((nf, nf, nm), order="F") if keep_bisp else None
+        rc = lib().orc_classic_vect_diag(C.byref(self.st), nf, _p(f), _p(out["m2mf"]), _p(out["m2mr"]),
+                                         _p(out["m2o2mr"]), _p(out["m3mf"]), _p(out["m3mr"]),
+                                         _p(bf) if keep_bisp else None, _p(br) if keep_bisp else None)
+        if rc:
+            raise RuntimeError(f"orc_classic_vect_diag failed ({rc})")
+        out["f"] = f
+        if keep_bisp:
+            out["bf"], out["br"] = bf, br
+        return out
+
+    def classic_scalar_diag(self, f=None):
+        f = self.freqs() if f is None else np.ascontiguousarray(f, dtype=np.float64)
+        out = {k: np.zeros(self.nme) for k in ("m2mf", "m2mr", "m2o2mr", "m3mf", "m3mr")}
+        rc = lib().orc_classic_scalar_diag(C.byref(self.st), f.size, _p(f), _p(out["m2mf"]), _p(out["m2mr"]),
+                                           _p(out["m2o2mr"]), _p(out["m3mf"]), _p(out["m3mr"]))
+        if rc:
+            raise RuntimeError(f"orc_classic_scalar_diag failed ({rc})")
+        return out
+
+    def msh_bfm_diag(self, fi, fj):
+        out = np.zeros(self.nme)
+        rc = lib().orc_msh_bfm_diag(C.byref(self.st), float(fi), float(fj), _p(out))
+        if rc:
+            raise RuntimeError(f"orc_msh_bfm_diag failed ({rc})")
+        return out
+
+    def msh_brm_diag(self, fi, fj, bfm):
+        fi = np.ascontiguousarray(np.atleast_1d(fi), dtype=np.float64)
+        fj = np.ascontiguousarray(np.atleast_1d(fj), dtype=np.float64)
+        bfm = np.asfortranarray(bfm.reshape(self.nme, fi.size * fj.size, order="F"))
+        out = np.zeros_like(bfm)
+        lib().orc_msh_brm_diag(C.byref(self.st), fi.size, _p(fi), fj.size, _p(fj), _p(bfm), _p(out))
+        return out
+
+    def rect_zone_diag(self, fi0, fj0, dIi, dIj, dJi, dJj, ni, nj, Fi, Fj, sym=1.0):
+        mf, mr = np.zeros(self.nme), np.zeros(self.nme)
+        rc = lib().orc_rect_zone_diag(C.byref(self.st), fi0, fj0, dIi, dIj, dJi, dJj, int(ni), int(nj), int(Fi),
+                                      int(Fj), float(sym), _p(mf), _p(mr))
+        if rc:
+            raise RuntimeError(f"orc_rect_zone_diag failed ({rc})")
+        return mf, mr
+
+    def skewness_diag(self, m2, m3):
+        sk = np.zeros(self.nme)
+        lib().orc_skewness_diag(self.nme, _p(np.ascontiguousarray(m2)), _p(np.ascontiguousarray(m3)), _p(sk))
+        return sk
 
     # -- a15 ------------------------------------------------------------------------------
     def skewness(self, m2, m3):
