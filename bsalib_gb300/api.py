@@ -85,6 +85,7 @@ def load(path: Optional[str] = None):
         "bsa_gpu_mshMoments": [vp, vp, vp, i, vp, vp], "bsa_gpu_getStats": [vp],
         "bsa_gpu_pointMomentsNoAlloc": [vp, i, i, vp, vp, vp, vp, vp, vp, vp, i, vp, vp, vp, vp, vp, vp],
         "bsa_gpu_mshZones": [vp, i, vp, vp, vp], "bsa_gpu_mshGenerateZones": [vp, i, vp],
+        "bsa_computeBRdecomp": [vp, vp, vp], "bsa_computePeakFactors": [i, vp, vp, d, vp, vp, vp, vp],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)
@@ -270,6 +271,27 @@ class BsaSession:
         check(self.lib.bsa_computeSkewness(nm, _p(np.ascontiguousarray(m2)), _p(np.ascontiguousarray(m3)),
                                            _p(sk)), "bsa_computeSkewness")
         return sk
+
+    def br_decomp(self, m2mf):
+        """bsa_computeBRdecomp: (background, resonant) parts of each kept mode's variance."""
+        nm = self.nmodes()
+        bkg, res = np.zeros(nm), np.zeros(nm)
+        check(self.lib.bsa_computeBRdecomp(_p(np.ascontiguousarray(m2mf, dtype=np.float64)), _p(bkg), _p(res)),
+              "bsa_computeBRdecomp")
+        return bkg, res
+
+    def peak_factors(self, m2, m2o2, obs_time, sk=None):
+        """bsa_computePeakFactors: (status, peak_g, peak_ng_pos, peak_ng_neg); status is
+        BSA_OK or BSA_SKIPPED (1) where the reference warns and returns."""
+        m2 = np.ascontiguousarray(m2, dtype=np.float64)
+        g, pos, neg = np.zeros(m2.size), np.zeros(m2.size), np.zeros(m2.size)
+        skp = _p(np.ascontiguousarray(sk, dtype=np.float64)) if sk is not None else None
+        rc = self.lib.bsa_computePeakFactors(m2.size, _p(m2), _p(np.ascontiguousarray(m2o2, dtype=np.float64)),
+                                             float(obs_time), _p(g), skp, _p(pos) if sk is not None else None,
+                                             _p(neg) if sk is not None else None)
+        if rc < 0:
+            check(rc, "bsa_computePeakFactors")
+        return rc, g, pos, neg
 
     def close(self):
         self.lib.bsa_Finalise()

@@ -112,8 +112,18 @@ struct Engine {
     int run_zones(const std::vector<ZoneDev> &zones, double *m3mf, double *m3mr, double *npts);
     int mesher_zones(std::vector<ZoneDev> &zones, std::vector<int> &policy);
     int run_mesher(double *m3mf, double *m3mr);
+    int br_decomp(const double *m2mf, double *bkg, double *res);
 };
 
 Engine &eng();
+
+// Host vector -> device buffer on the engine's stream (counted in the H2D statistics).
+template <class T>
+inline cudaError_t upload(DevBuf &b, const std::vector<T> &v, cudaStream_t st) {
+    cudaError_t e = b.reserve(sizeof(T) * v.size());
+    if (e != cudaSuccess || v.empty()) return e;
+    eng().h2d += (double)(sizeof(T) * v.size());
+    return cudaMemcpyAsync(b.p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, st);
+}
 
 }  // namespace bsa

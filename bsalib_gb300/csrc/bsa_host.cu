@@ -236,13 +236,6 @@ int Engine::validate() {
     return BSA_OK;
 }
 
-template <class T>
-static cudaError_t upload(DevBuf &b, const std::vector<T> &v, cudaStream_t st) {
-    cudaError_t e = b.reserve(sizeof(T) * v.size());
-    if (e != cudaSuccess || v.empty()) return e;
-    eng().h2d += (double)(sizeof(T) * v.size());
-    return cudaMemcpyAsync(b.p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, st);
-}
 
 int Engine::upload_problem() {
     int rc = validate();

@@ -42,6 +42,7 @@ extern "C" {
 #define BSA_ERR_UNSUPPORTED -4 /* valid in the reference but not on this path       */
 #define BSA_ERR_TIMEOUT -5    /* a device-side wait ran out of its iteration budget */
 #define BSA_ERR_NOMEM -6      /* device allocation failed                           */
+#define BSA_SKIPPED 1         /* the reference warns and returns: outputs untouched, not sticky */
 
 #define BSA_PREC_FP64 0       /* plain FP64 contraction (parity path)               */
 #define BSA_PREC_BF16X3 1     /* split BF16x3 tensor-core contraction, FP32 accum.   */
@@ -122,6 +123,21 @@ int bsa_Finalise(void);
 int bsa_computeSkewness(int nm, const double *m2, const double *m3, double *sk);
 
 const char *bsa_lastError(void);
+
+/* bsa_computeBRdecomp (src/bsa/BsaLibImpl.F90:1292-1420): background part
+ * bkg[m] = m2mf(m,m) / K_m^2 and resonant part res[m] = pi 2pi f_m S_Fm(f_m) / (2 xsi_m K_m^2)
+ * of each kept mode's response variance, S_Fm(f_m) the modal force PSD at the mode's own
+ * natural frequency (getBR_SFm_val_, functionsImpl.F90:2650-2745, evaluated on the GPU).
+ * m2mf is bsa_Run's m2mf_cls (dim_psd); bkg, res have nm entries. */
+int bsa_computeBRdecomp(const double *m2mf, double *bkg, double *res);
+
+/* bsa_computePeakFactors (BsaLibImpl.F90:1428-1517): Gaussian peak factor
+ * g = gamma / beta + beta, beta = sqrt(2 ln(sqrt(m2o2 / m2) / 2pi * T)), and, when sk is
+ * given, the non-Gaussian (Hermite model) positive / negative peak factors.  n entries.
+ * Returns BSA_SKIPPED (outputs untouched) where the reference warns and returns: m2o2 all
+ * zero, or an observation time T too short (beta < 1).  peak_ng_neg may be NULL. */
+int bsa_computePeakFactors(int n, const double *m2, const double *m2o2, double obs_time, double *peak_g,
+                           const double *sk, double *peak_ng_pos, double *peak_ng_neg);
 
 /* ---------------------------------------------------------------------------------- */
 /* 2. BsaCL device ABI (BsaCL/include/bsacl.h:28-55; bodies in BsaCL/src/bsacl.c)       */

@@ -1211,3 +1211,117 @@ void orc_skewness_diag(int dim, const double *m2, const double *m3, double *sk)
 }
 #undef WFCR
 #undef PHIR
+
+/* ======================================================================================
+ * Second-order post-processing.
+ * ====================================================================================== */
+
+/*
+ * getBR_SFm_val_ (functionsImpl.F90:2650-2745): force PSD of kept mode im (mode id m) at the
+ * frequency fnat; Suvw(nm, nnl*ntc) holds the nodal PSDs at every kept mode's frequency.
+ * The DOF index of node j's mode shape pairs with node k's coefficient, as written.
+ */
+static double br_sfm(const orc_problem *P, int nme, const double *Suvw, double fnat, int im, int m)
+{
+    const int nnl = P->nnl, nl = P->nlibsl, nd = P->ndegw3;
+    const double fiabs = fabs(fnat);
+    double psd = 0.0;
+    for (int itc = 0; itc < P->ntc; ++itc) {
+        const int tc = P->tc[itc], posN = itc * nnl;
+        for (int ink = 0; ink < nnl; ++ink) {
+            const int nk = P->n_load[ink], pos_nk = (nk - 1) * P->nlibs;
+            const double Sk = Suvw[I2(im, posN + ink, nme)];
+            for (int inj = 0; inj < nnl; ++inj) {
+                const int nj = P->n_load[inj], pos_nj = (nj - 1) * P->nlibs;
+                const double corrJK = corr_of(P, nj, nk, tc);
+                const double Sj = Suvw[I2(im, posN + inj, nme)];
+                const double SJK = pow(corrJK, fiabs) * sqrt(Sj * Sk);
+                double s = 0.0;
+                for (int l2 = 0; l2 < nl; ++l2)
+                    for (int l1 = 0; l1 < nl; ++l1) {
+                        const double akU = P->wfc[I3(P->libs_load[l1] - 1, tc - 1, ink, nl, nd)];
+                        const double ajU = P->wfc[I3(P->libs_load[l2] - 1, tc - 1, inj, nl, nd)];
+                        const double phj = P->phi[I2(pos_nj + P->libs_load[l1] - 1, m - 1, P->ndofs)];
+                        const double phk = P->phi[I2(pos_nk + P->libs_load[l2] - 1, m - 1, P->ndofs)];
+                        s += (phj * phk) * ((akU * ajU) * SJK);
+                    }
+                psd = psd + s;
+            }
+        }
+    }
+    return psd;
+}
+
+/*
+ * bsa_computeBRdecomp (src/bsa/BsaLibImpl.F90:1292-1420): bkg(m) = m2mf(m,m) / K_m^2,
+ * res(m) = pi * 2pi * f_m * S_Fm(f_m) / (2 xsi_m K_m^2).  natf, xsi indexed by mode id;
+ * m2mf of length nm (diag != 0) or nm^2.
+ */
+int orc_br_decomp(const orc_problem *P, const double *natf, const double *xsi, int diag, const double *m2mf,
+                  double *bkg, double *res)
+{
+    const int nme = P->nm_eff, nnl = P->nnl;
+    double *fm = malloc(sizeof(double) * nme), *col = malloc(sizeof(double) * nme * nnl);
+    double *Suvw = malloc(sizeof(double) * (size_t)nme * nnl * P->ntc);
+    for (int im = 0; im < nme; ++im) fm[im] = natf[P->modes[im] - 1];
+    for (int itc = 0; itc < P->ntc; ++itc) {
+        if (orc_eval_psd(P, nme, fm, P->tc[itc], col)) { free(fm); free(col); free(Suvw); return -1; }
+        memcpy(Suvw + (size_t)nme * nnl * itc, col, sizeof(double) * nme * nnl);
+    }
+    for (int im = 0; im < nme; ++im) {
+        const int m = P->modes[im];
+        double km2 = P->Km[m - 1];
+        km2 = km2 * km2;
+        bkg[im] = m2mf[diag ? im : im * nme + im] / km2;
+        const double sfm = br_sfm(P, nme, Suvw, fm[im], im, m);
+        res[im] = PI_ * PIt2 * fm[im] * sfm / (2 * xsi[m - 1] * km2);
+    }
+    free(fm); free(col); free(Suvw);
+    return 0;
+}
+
+/*
+ * bsa_computePeakFactors (BsaLibImpl.F90:1428-1517).  Returns 1 (m2o2 all zero) or 2
+ * (observation time too short) where the reference warns and returns.  sk may be NULL.
+ */
+int orc_peak_factors(int n, const double *m2, const double *m2o2, double obs_time, const double *sk,
+                     double *peak_g, double *pos, double *neg)
+{
+    const double gamma_ = 0.5772, PI2 = PI_ * PI_;
+    int any = 0;
+    for (int i = 0; i < n; ++i) any |= (m2o2[i] != 0.0);
+    if (!any) return 1;
+    double *beta = malloc(sizeof(double) * n);
+    for (int i = 0; i < n; ++i) {
+        beta[i] = sqrt(m2o2[i] / m2[i]) / PIt2 * obs_time;
+        if (beta[i] < 1.0) { free(beta); return 2; }
+    }
+    for (int i = 0; i < n; ++i) {
+        beta[i] = sqrt(2 * log(beta[i]));
+        peak_g[i] = gamma_ / beta[i];
+        peak_g[i] = peak_g[i] + beta[i];
+    }
+    if (sk) {
+        for (int i = 0; i < n; ++i) {
+            const double rtmp = sk[i] * sk[i], g4 = 1.5 * rtmp;
+            const double h40 = sqrt(1.0 + 1.5 * g4);
+            const double h3 = sk[i] / (4.0 + 2.0 * h40);
+            const double h4 = (h40 - 1.0) / 18.0;
+            const double k = 1.0 / (sqrt(1 + 2.0 * h3 * h3 + 6.0 * h4 * h4));
+            const double b = beta[i], b2 = b * b, b3 = b2 * b;
+            double p = 5.44 / b3;
+            p = p + (3.0 / b * (PI2 / 6.0 - gamma_ + (gamma_ * gamma_)));
+            p = p + (b3 + 3 * b * (gamma_ - 1));
+            p = p * h4;
+            double q = p;
+            const double r = h3 * (b2 + 2.0 * gamma_ - 1. + 1.98 / b2);
+            p = p + r;
+            q = q - r;
+            p = p + peak_g[i];
+            pos[i] = p * k;
+            if (neg) neg[i] = (q + peak_g[i]) * k;
+        }
+    }
+    free(beta);
+    return 0;
+}

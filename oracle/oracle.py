@@ -70,6 +70,8 @@ def lib():
         _lib.orc_msh_bfm_diag.argtypes = [vp, C.c_double, C.c_double, vp]
         _lib.orc_msh_brm_diag.argtypes = [vp, C.c_int, vp, C.c_int, vp, vp, vp]
         _lib.orc_skewness_diag.argtypes = [C.c_int, vp, vp, vp]
+        _lib.orc_br_decomp.argtypes = [vp, vp, vp, C.c_int, vp, vp, vp]
+        _lib.orc_peak_factors.argtypes = [C.c_int, vp, vp, C.c_double, vp, vp, vp, vp]
     return _lib
 
 
@@ -286,6 +288,27 @@ class Oracle:
         sk = np.zeros(self.nme)
         lib().orc_skewness_diag(self.nme, _p(np.ascontiguousarray(m2)), _p(np.ascontiguousarray(m3)), _p(sk))
         return sk
+
+    # -- second-order post-processing -----------------------------------------------------
+    def br_decomp(self, m2mf):
+        bkg, res = np.zeros(self.nme), np.zeros(self.nme)
+        diag = int(self.prob.settings.onlyd)
+        rc = lib().orc_br_decomp(C.byref(self.st), _p(np.ascontiguousarray(self.prob.natf, dtype=np.float64)),
+                                 _p(np.ascontiguousarray(self.prob.xsi, dtype=np.float64)), diag,
+                                 _p(np.ascontiguousarray(m2mf, dtype=np.float64)), _p(bkg), _p(res))
+        if rc:
+            raise RuntimeError(f"orc_br_decomp failed ({rc})")
+        return bkg, res
+
+    def peak_factors(self, m2, m2o2, obs_time, sk=None):
+        """(status, peak_g, peak_ng_pos, peak_ng_neg); status 1 / 2 where the reference skips."""
+        m2 = np.ascontiguousarray(m2, dtype=np.float64)
+        n = m2.size
+        g, pos, neg = np.zeros(n), np.zeros(n), np.zeros(n)
+        skp = _p(np.ascontiguousarray(sk, dtype=np.float64)) if sk is not None else None
+        rc = lib().orc_peak_factors(n, _p(m2), _p(np.ascontiguousarray(m2o2, dtype=np.float64)), float(obs_time),
+                                    skp, _p(g), _p(pos), _p(neg))
+        return rc, g, pos, neg
 
     # -- a15 ------------------------------------------------------------------------------
     def skewness(self, m2, m3):
