@@ -85,6 +85,7 @@ def load(path: Optional[str] = None):
         "bsa_gpu_mshMoments": [vp, vp, vp, i, vp, vp], "bsa_gpu_getStats": [vp],
         "bsa_gpu_pointMomentsNoAlloc": [vp, i, i, vp, vp, vp, vp, vp, vp, vp, i, vp, vp, vp, vp, vp, vp],
         "bsa_gpu_mshZones": [vp, i, vp, vp, vp], "bsa_gpu_mshGenerateZones": [vp, i, vp],
+        "bsa_setPODTruncationThreshold": [d], "bsa_setPODNOfModesKept": [i],
         "bsa_computeBRdecomp": [vp, vp, vp], "bsa_computePeakFactors": [i, vp, vp, d, vp, vp, vp, vp],
     }
     for name, args in sig.items():

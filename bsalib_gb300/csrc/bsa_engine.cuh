@@ -64,6 +64,15 @@ struct Engine {
     int precision = 0;          // BSA_PREC_FP64
     bool classic_trunc = true;  // S(f1+f2) beyond the classic grid reads zero
     int shard_r0 = 0, shard_r1 = -1;  // classic grid rows evaluated (-1: to the end)
+    // POD truncation requests (bsa_setPODTruncationThreshold / bsa_setPODNOfModesKept)
+    double pod_trunc_lim = 0.0;
+    int pod_nmodes = 0;
+    // The Mesher's POD form truncates only when one of the two was set to a value that
+    // drops modes (BsaLibImpl.F90:97-115, 480); the default keeps every POD mode.
+    bool pod_truncates() const {
+        if (set.svd != 1 || set.onlyd != 0) return false;
+        return (pod_trunc_lim > 0.0 && pod_trunc_lim != 1.0) || (pod_nmodes > 0 && pod_nmodes < in.nnl);
+    }
 
     // derived (validate)
     std::vector<int> modes;

@@ -66,6 +66,8 @@ void Engine::reset_inputs() {
     classic_trunc = true;
     shard_r0 = 0;
     shard_r1 = -1;
+    pod_trunc_lim = 0.0;
+    pod_nmodes = 0;
 }
 
 void Engine::free_device() {
@@ -479,6 +481,8 @@ int Engine::run_points(const double *fi, const double *fj, const double *w, doub
     int rc = upload_problem();
     if (rc) return rc;
     if (npts <= 0) return fail(BSA_ERR_ARG, "empty point set");
+    if (pod_truncates())
+        return fail(BSA_ERR_UNSUPPORTED, "truncated POD (getFM_full_tm_scalar_msh_POD_ with dropped modes) is not on this path");
     // Distinct frequencies: f1, f2 and f1+f2 of every point share one A table.
     std::vector<double> ftab;
     ftab.reserve(3 * (size_t)npts);
@@ -645,6 +649,16 @@ int bsa_setupMesher(int isvd, int bkgrfmt, double bkgaext, double genpaext, doub
     bsa::Settings &s = eng().set;
     s.svd = isvd; s.bkgrfmt = bkgrfmt; s.bkgaext = bkgaext; s.genpaext = genpaext; s.maxaext = maxaext;
     s.fcov = ifcov; s.dumpmod = idumpmod;
+    return BSA_OK;
+}
+int bsa_setPODTruncationThreshold(double rval) {
+    GUARD();
+    if (rval > 0.0) eng().pod_trunc_lim = rval / 100.0;
+    return BSA_OK;
+}
+int bsa_setPODNOfModesKept(int nmodes) {
+    GUARD();
+    eng().pod_nmodes = nmodes;
     return BSA_OK;
 }
 int bsa_setWindDirections(const int *dirs, int ndirs) {

@@ -67,6 +67,11 @@ int bsa_setupClassic(int nfreqs, double df);   /* BsaLibImpl.F90:959            
 int bsa_setClassicMode(int imode);             /* BsaLibImpl.F90:916, 0 vectorised 1 scalar   */
 int bsa_setupMesher(int isvd, int bkgrfmt, double bkgaext, double genpaext, double maxaext,
                     int ifcov, int idumpmod);  /* BsaLibImpl.F90:966                          */
+/* POD truncation of the Mesher's POD form (BsaLibImpl.F90:97-115).  The default keeps every
+ * POD mode, where the POD form equals the direct form evaluated here; a request that drops
+ * modes makes the Mesher functions return BSA_ERR_UNSUPPORTED. */
+int bsa_setPODTruncationThreshold(double rval);  /* percent of the largest eigenvalue */
+int bsa_setPODNOfModesKept(int nmodes);
 int bsa_setWindDirections(const int *dirs, int ndirs);  /* BsaLibImpl.F90:983                 */
 int bsa_setWindTurbComps(const int *tc, int ntc);       /* BsaLibImpl.F90:991                 */
 

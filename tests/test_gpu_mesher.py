@@ -111,3 +111,20 @@ def test_mesher_run_vs_oracle_on_its_zones(bsalib):
     assert rel(out["m3mf_msh"], ref_f) < TOL
     assert rel(out["m3mr_msh"], ref_r) < TOL
     assert np.all(out["m3mr_cls"] == 0.0)  # analysis type 2 runs the Mesher only
+
+
+def test_pod_truncation_requests(bsalib):
+    """The default POD form keeps every mode (== the direct form evaluated here); a request
+    that drops POD modes is refused with BSA_ERR_UNSUPPORTED instead of being ignored."""
+    prob = cantilever_tower(nfreqs=5, df=0.5, nodes=6)
+    s = api.BsaSession(prob)
+    try:
+        L = s.lib
+        assert L.bsa_setPODTruncationThreshold(100.0) == 0    # 100 % keeps every mode
+        assert L.bsa_setPODNOfModesKept(prob.nnl) == 0
+        s.msh_bispectra(np.array([0.3]), np.array([0.4]))
+        assert L.bsa_setPODTruncationThreshold(5.0) == 0
+        with pytest.raises(api.BsaError, match="-4"):
+            s.msh_bispectra(np.array([0.3]), np.array([0.4]))
+    finally:
+        s.close()
