@@ -85,7 +85,7 @@ struct Engine {
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr;
     DevBuf dL, dQ, dLogc, dPsdPar, dFrfM, dFrfK, dFrfC, dFreq, dS, dA, dPartF, dPartR, dOut, dPsdF, dWf, dPts,
-        dPtsD, dBF, dBR, dMixA, dMixB, dMixH, dMixPart, dA32, dZones, dZidx, dWd3, dWd2;
+        dPtsD, dBF, dBR, dMixA, dMixB, dMixH, dMixPart, dA32, dZones, dZidx, dWd3, dWd2, dMshT, dMshIdx;
 
     // stats
     double last_ms = 0, last_ms_contraction = 0, last_ms_gemm = 0, last_points = 0;
@@ -119,6 +119,10 @@ struct Engine {
                    const std::vector<ZoneDev> *zones = nullptr, const int *zid = nullptr, const int *zi = nullptr,
                    const int *zj = nullptr);
     int run_zones(const std::vector<ZoneDev> &zones, double *m3mf, double *m3mr, double *npts);
+    int run_zones_fp64(const std::vector<ZoneDev> &zones, double *m3mf, double *m3mr, double *npts);
+    int run_zones_mixed(const std::vector<ZoneDev> &zones, double *m3mf, double *m3mr, double *npts);
+    int msh_mixed_batch(const std::vector<ZoneDev> &zones, std::vector<double> &accF, std::vector<double> &accR,
+                        float &ms_gemm, float &ms_all);
     int mesher_zones(std::vector<ZoneDev> &zones, std::vector<int> &policy);
     int run_mesher(double *m3mf, double *m3mr);
     int br_decomp(const double *m2mf, double *bkg, double *res);

@@ -73,7 +73,7 @@ void Engine::reset_inputs() {
 void Engine::free_device() {
     for (DevBuf *b : {&dL, &dQ, &dLogc, &dPsdPar, &dFrfM, &dFrfK, &dFrfC, &dFreq, &dS, &dA, &dPartF, &dPartR,
                       &dOut, &dPsdF, &dWf, &dPts, &dPtsD, &dBF, &dBR, &dMixA, &dMixB, &dMixH, &dMixPart, &dA32,
-                      &dZones, &dZidx, &dWd3, &dWd2})
+                      &dZones, &dZidx, &dWd3, &dWd2, &dMshT, &dMshIdx})
         b->release();
     if (stream) cudaStreamDestroy(stream);
     stream = nullptr;

@@ -169,9 +169,17 @@ int Engine::mesher_zones(std::vector<ZoneDev> &zones, std::vector<int> &policy) 
     return BSA_OK;
 }
 
+// Zone integration in the precision selected by bsa_gpu_setPrecision: the split-precision
+// path evaluates the axis-aligned zones on the tensor cores (bsa_msh_mixed.cu); the
+// diagonal-only spectra and the FP64 setting use the FP64 point kernel.
+int Engine::run_zones(const std::vector<ZoneDev> &zones, double *m3mf, double *m3mr, double *npts) {
+    if (precision == BSA_PREC_BF16X3 && !set.onlyd) return run_zones_mixed(zones, m3mf, m3mr, npts);
+    return run_zones_fp64(zones, m3mf, m3mr, npts);
+}
+
 // Every zone's BFM lattice points in one point list; m3mf weights are the trapezoid
 // weights of the BFM lattice, the BRM lattice is handled in the kernel epilogue.
-int Engine::run_zones(const std::vector<ZoneDev> &zones, double *m3mf, double *m3mr, double *npts) {
+int Engine::run_zones_fp64(const std::vector<ZoneDev> &zones, double *m3mf, double *m3mr, double *npts) {
     size_t n = 0;
     double nbrm = 0.0;
     for (const ZoneDev &z : zones) {

@@ -1,0 +1,708 @@
+// bsa_msh_mixed.cu -- split-precision (BF16x3) tensor-core evaluation of Mesher zones.
+//
+// A rectangular zone whose lattice is aligned with the frequency axes has its BFM points at
+// (f1, f2) = (r_i, c_j): every point of lattice line i shares f1 = r_i, every point of
+// column j shares f2 = c_j.  With U(f)[(a,b), k] = Q_ka A_kb(f) and Z = A(f1+f2) per point,
+// the three terms of the factored BFM (functionsImpl.F90:247-465, direct form) at (i, j) are
+//   T1 = U(r_i) A(c_j)      (m,n,o) = (a, b, j')     one GEMM per line i, B = the zone's columns
+//   T3 = U(r_i) Z(i,j)      (m,n,o) = (j', b, a)     same line, B = the line's sum rows
+//   T2 = U(c_j) Z(i,j)      (m,n,o) = (j', a, b)     one GEMM per column j, B = the column's sums
+// and B_F = 2 (T1 + T2 + T3).  Unlike the Classic grid, (c_j, r_i) is not a point of the zone,
+// so T2 needs its own GEMM family (tasks of kind 1).
+//
+// k_msh_mixed runs those GEMMs as tcgen05 MMAs fed by TMA, with the k_bfm_mixed pipeline
+// (one TMA warp, one MMA-issuing warp, four TMEM-draining warps, double-buffered TMEM,
+// bounded mbarrier waits) and stores the three term tensors in FP32.  k_msh_moments then
+// integrates them: the BFM lattice trapezoid for m3mf, and for m3mr the bilinear
+// interpolation onto the BRM lattice refined by (Fi, Fj) times the FRF product
+// Re[H_m(w1) H_n(w2) conj H_o(w1+w2)] (getRM_full_scalar_msh_, :1031-1115) with the
+// trapezoid weights of the refined lattice (_shared_poly2d.fi:470-2166), the FRF evaluated
+// in FP64 and rounded once.  Zones whose lattice is rotated against the axes go to the FP64
+// point kernel.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <vector>
+
+#include "../../include/bsa_gpu.h"
+#include "bsa_engine.cuh"
+#include "bsa_kernels.cuh"
+#include "bsa_tc.cuh"
+
+namespace bsa {
+namespace mshmix {
+
+using namespace tc;
+
+constexpr int kStages = 2;
+constexpr int kStageBytes = 6 * kTileBytes;  // U hi/lo, G hi/lo, S hi/lo
+
+// One task: a lattice line of a zone, i.e. one U(f) row block against the points of the line.
+struct Task {
+    int u_row;    // first U-table row of the line's U(f) (a multiple of Mp)
+    int g_row;    // first column-table row of the zone (D1 operand), -1 for kind 1
+    int s_row;    // first sum-table row of the line's points (NMT rows per point)
+    int ncols;    // points on the line
+    int p0;       // output index of the line's first point
+    int pstride;  // output index step between consecutive points of the line
+    int kind;     // 0: D1 -> T1 and D3 -> T3;  1: D3 -> T2
+};
+
+struct MParams {
+    int nm, NMT, NC, BROWS, Mp, MT, nk, ks_last;
+    int ntasks;
+    const Task *tasks;
+    float *T1, *T3, *T2;  // [point][j'][a*nm + b]
+    int *err;
+};
+
+// Work item w = (task w / MT, row tile w % MT), CTAs stride over work items; all three
+// roles walk the same (item, N tile, K chunk) sequence.
+__global__ void __launch_bounds__(192, 1)
+    k_msh_mixed(const __grid_constant__ CUtensorMap tmUh, const __grid_constant__ CUtensorMap tmUl,
+                const __grid_constant__ CUtensorMap tmGh, const __grid_constant__ CUtensorMap tmGl,
+                const __grid_constant__ CUtensorMap tmSh, const __grid_constant__ CUtensorMap tmSl, const MParams p) {
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint64_t *bars = (uint64_t *)(smem + kStages * kStageBytes);
+    uint64_t *full = bars, *empty = bars + kStages, *tfull = bars + 2 * kStages, *tempty = bars + 2 * kStages + 2;
+    uint64_t *done = bars + 2 * kStages + 4;
+    uint32_t *tmem_slot = (uint32_t *)(bars + 2 * kStages + 5);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int *err = p.err;
+    const int nwork = p.ntasks * p.MT;
+
+    // B-tile rows that TMA never writes (BROWS..127) stay zero for the whole run.
+    for (int s = 0; s < kStages; ++s)
+        for (int t = 2; t < 6; ++t) {
+            uint8_t *tile = smem + s * kStageBytes + t * kTileBytes;
+            for (int x = threadIdx.x; x < (128 - p.BROWS) * 128 / 16; x += blockDim.x)
+                ((uint4 *)(tile + p.BROWS * 128))[x] = make_uint4(0, 0, 0, 0);
+        }
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kStages; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(&tfull[b], 1);
+            mbar_init(&tempty[b], 128);
+        }
+        mbar_init(done, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(su32(tmem_slot)) : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == 0) {
+        // ---------------- TMA producer ----------------
+        if (lane == 0) {
+            uint32_t it = 0;
+            bool ok = true;
+            for (int w = blockIdx.x; w < nwork && ok; w += gridDim.x) {
+                const Task tk = p.tasks[w / p.MT];
+                const int mt = w % p.MT;
+                const int ntiles = (tk.ncols + p.NC - 1) / p.NC;
+                const bool hg = tk.kind == 0;
+                const uint32_t tx = 2u * kTileBytes + (hg ? 4u : 2u) * (uint32_t)(p.BROWS * 128);
+                for (int nt = 0; nt < ntiles && ok; ++nt)
+                    for (int kc = 0; kc < p.nk && ok; ++kc, ++it) {
+                        const int s = it % kStages;
+                        const uint32_t ph = (it / kStages) & 1u;
+                        if (!mbar_wait(&empty[s], ph ^ 1u, err, 1)) { ok = false; break; }
+                        uint8_t *st = smem + s * kStageBytes;
+                        mbar_expect_tx(&full[s], tx);
+                        const int x = kc * kBK;
+                        const int yu = tk.u_row + mt * kBM;
+                        tma_2d(st + 0 * kTileBytes, &tmUh, &full[s], x, yu);
+                        tma_2d(st + 1 * kTileBytes, &tmUl, &full[s], x, yu);
+                        if (hg) {
+                            const int yg = tk.g_row + nt * p.BROWS;
+                            tma_2d(st + 2 * kTileBytes, &tmGh, &full[s], x, yg);
+                            tma_2d(st + 3 * kTileBytes, &tmGl, &full[s], x, yg);
+                        }
+                        const int ys = tk.s_row + nt * p.BROWS;
+                        tma_2d(st + 4 * kTileBytes, &tmSh, &full[s], x, ys);
+                        tma_2d(st + 5 * kTileBytes, &tmSl, &full[s], x, ys);
+                    }
+            }
+            // Let the copies already issued land before the CTA can leave (bounded).
+            const uint32_t last = it;
+            for (uint32_t q = (last > (uint32_t)kStages ? last - kStages : 0); q < last; ++q) {
+                const int s = q % kStages;
+                const uint32_t ph = (q / kStages) & 1u;
+                const uint64_t t0 = gtime();
+                while (!mbar_try(&full[s], ph) && gtime() - t0 < kWaitNs) {
+                }
+            }
+        }
+        __syncwarp();
+    } else if (warp == 1) {
+        // ---------------- MMA issuer ----------------
+        if (lane == 0) {
+            uint32_t it = 0, tile = 0;
+            bool ok = true;
+            for (int w = blockIdx.x; w < nwork && ok; w += gridDim.x) {
+                const Task tk = p.tasks[w / p.MT];
+                const int ntiles = (tk.ncols + p.NC - 1) / p.NC;
+                const bool hg = tk.kind == 0;
+                for (int nt = 0; nt < ntiles && ok; ++nt, ++tile) {
+                    const int buf = tile & 1;
+                    const uint32_t tph = (tile >> 1) & 1u;
+                    if (!mbar_wait(&tempty[buf], tph ^ 1u, err, 2)) { ok = false; break; }
+                    fence_after();
+                    const uint32_t d1 = tmem + buf * 256, d3 = d1 + 128;
+                    for (int kc = 0; kc < p.nk; ++kc, ++it) {
+                        const int s = it % kStages;
+                        const uint32_t ph = (it / kStages) & 1u;
+                        if (!mbar_wait(&full[s], ph, err, 3)) { ok = false; break; }
+                        fence_after();
+                        const uint32_t base = su32(smem + s * kStageBytes);
+                        // K steps past the data in the last chunk multiply zero padding: skip them
+                        const int nks = kc == p.nk - 1 ? p.ks_last : kBK / 16;
+                        for (int ks = 0; ks < nks; ++ks) {
+                            const uint32_t off = ks * 32;
+                            const uint64_t uh = sdesc(base + 0 * kTileBytes + off), ul = sdesc(base + 1 * kTileBytes + off);
+                            const uint64_t sh = sdesc(base + 4 * kTileBytes + off), sl = sdesc(base + 5 * kTileBytes + off);
+                            const uint32_t acc = (kc > 0 || ks > 0) ? 1u : 0u;
+                            if (hg) {
+                                const uint64_t gh = sdesc(base + 2 * kTileBytes + off), gl = sdesc(base + 3 * kTileBytes + off);
+                                mma(d1, uh, gh, acc);
+                                mma(d1, uh, gl, 1u);
+                                mma(d1, ul, gh, 1u);
+                            }
+                            mma(d3, uh, sh, acc);
+                            mma(d3, uh, sl, 1u);
+                            mma(d3, ul, sh, 1u);
+                        }
+                        mma_commit(&empty[s]);  // stage free once these MMAs have read it
+                    }
+                    if (!ok) break;
+                    mma_commit(&tfull[buf]);  // accumulators ready for the epilogue
+                }
+            }
+            // Every MMA issued so far completes before TMEM is released.
+            mma_commit(done);
+            const uint64_t t0 = gtime();
+            while (!mbar_try(done, 0) && gtime() - t0 < kWaitNs) {
+            }
+        }
+        __syncwarp();
+    } else {
+        // ---------------- epilogue: TMEM -> FP32 term tensors ----------------
+        const int quarter = warp & 3;
+        const int row = quarter * 32 + lane;  // TMEM lane = row of the M tile
+        const uint32_t lane_base = tmem + ((uint32_t)(quarter * 32) << 16);
+        const int nm = p.nm, nm2 = nm * nm;
+        uint32_t tile = 0;
+        bool ok = true;
+        for (int w = blockIdx.x; w < nwork && ok; w += gridDim.x) {
+            const Task tk = p.tasks[w / p.MT];
+            const int mt = w % p.MT;
+            const int grow = mt * kBM + row;  // row of U: a * nm + b
+            const bool vrow = grow < nm2;
+            const int ntiles = (tk.ncols + p.NC - 1) / p.NC;
+            float *const outA = tk.kind == 0 ? p.T1 : nullptr;
+            float *const outB = tk.kind == 0 ? p.T3 : p.T2;
+            for (int nt = 0; nt < ntiles; ++nt, ++tile) {
+                const int buf = tile & 1;
+                const uint32_t tph = (tile >> 1) & 1u;
+                // warp-uniform outcome: tcgen05.ld below is .sync.aligned
+                const bool got = __all_sync(0xffffffffu, mbar_wait(&tfull[buf], tph, err, 4));
+                if (!got) { ok = false; break; }
+                fence_after();
+                const int c0 = nt * p.NC;
+                for (int acc = (tk.kind == 0 ? 0 : 1); acc < 2; ++acc) {
+                    float *const out = acc == 0 ? outA : outB;
+                    for (int q = 0; q < kBN / 32; ++q) {
+                        uint32_t v[32];
+                        tmem_ld32(lane_base + buf * 256 + acc * 128 + q * 32, v);
+                        tmem_wait_ld();
+#pragma unroll
+                        for (int e = 0; e < 32; ++e) {
+                            const int col = q * 32 + e;
+                            const int c = col / p.NMT, j = col - c * p.NMT;
+                            if (!vrow || c >= p.NC || j >= nm || c0 + c >= tk.ncols) continue;
+                            const size_t pt = (size_t)tk.p0 + (size_t)(c0 + c) * tk.pstride;
+                            out[(pt * nm + j) * nm2 + grow] = __uint_as_float(v[e]);
+                        }
+                    }
+                }
+                fence_before();
+                mbar_arrive(&tempty[buf]);
+            }
+        }
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem) : "memory");
+}
+
+// ------------------------------------------------------------------------------------
+// Operand preparation from the FP32 A(f) table (rows named by an index list).
+// ------------------------------------------------------------------------------------
+// U[(r*Mp + a*nm + b)][k] = Q[k][a] A(src[r])[k][b]   (rows >= nm^2 and k >= K are zero)
+// One block per (row block r, 32 k); nm <= 64.
+__global__ void k_prep_u_rows(int nm, int K, int Kp, int Mp, const int *__restrict__ src, const float *__restrict__ A,
+                              const double *__restrict__ Q, __nv_bfloat16 *__restrict__ Uh,
+                              __nv_bfloat16 *__restrict__ Ul) {
+    const int r = blockIdx.x, k0 = blockIdx.y * 32;
+    __shared__ double As[32][65], Qs[32][65];
+    const float *Ar = A + (size_t)src[r] * K * nm;
+    for (int e = threadIdx.x; e < 32 * nm; e += blockDim.x) {
+        const int kk = e / nm, m = e % nm, k = k0 + kk;
+        As[kk][m] = k < K ? (double)Ar[(size_t)k * nm + m] : 0.0;
+        Qs[kk][m] = k < K ? Q[(size_t)k * nm + m] : 0.0;
+    }
+    __syncthreads();
+    const int nm2 = nm * nm;
+    for (int e = threadIdx.x; e < Mp * 4; e += blockDim.x) {
+        const int row = e >> 2, kv = (e & 3) * 8;
+        __align__(16) __nv_bfloat16 hi[8], lo[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const double u = row < nm2 ? Qs[kv + q][row / nm] * As[kv + q][row % nm] : 0.0;
+            split_bf16(u, hi[q], lo[q]);
+        }
+        const size_t o = ((size_t)r * Mp + row) * Kp + k0 + kv;
+        *(uint4 *)(Uh + o) = *(const uint4 *)hi;
+        *(uint4 *)(Ul + o) = *(const uint4 *)lo;
+    }
+}
+
+// T[(t*NMT + j)][k] = A(src[t])[k][j]   (j >= nm and k >= K are zero)
+__global__ void k_prep_b_rows(int nm, int NMT, int K, int Kp, const int *__restrict__ src, const float *__restrict__ A,
+                              __nv_bfloat16 *__restrict__ Th, __nv_bfloat16 *__restrict__ Tl) {
+    const int t = blockIdx.x, k0 = blockIdx.y * 64;
+    __shared__ float As[64][65];
+    const float *Ar = A + (size_t)src[t] * K * nm;
+    for (int e = threadIdx.x; e < 64 * nm; e += blockDim.x) {
+        const int kk = e / nm, m = e % nm, k = k0 + kk;
+        As[kk][m] = k < K ? Ar[(size_t)k * nm + m] : 0.f;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < NMT * 8; e += blockDim.x) {
+        const int j = e >> 3, kv = (e & 7) * 8;
+        __align__(16) __nv_bfloat16 hi[8], lo[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) split_bf16(j < nm ? (double)As[kv + q][j] : 0.0, hi[q], lo[q]);
+        const size_t o = ((size_t)t * NMT + j) * Kp + k0 + kv;
+        *(uint4 *)(Th + o) = *(const uint4 *)hi;
+        *(uint4 *)(Tl + o) = *(const uint4 *)lo;
+    }
+}
+
+// ------------------------------------------------------------------------------------
+// Zone integration of the term tensors.
+// ------------------------------------------------------------------------------------
+// An axis-aligned zone of the batch: BFM point (i, j) at (fi0 + i dI, fj0 + j dJ), term
+// tensors at point pbase + i*nj + j, cells (i0, j0), 0 <= i0 < ni-1, 0 <= j0 < nj-1,
+// numbered from cbase.
+struct ZoneM {
+    double fi0, fj0, dI, dJ, wI, wJ, sym;
+    int ni, nj, Fi, Fj;
+    int pbase, cbase;
+};
+
+constexpr int kQB = 24;  // BRM points per FRF staging round
+
+// Block (g, chunk): elements e = chunk*256 + t of the term tensors (e = j'*nm^2 + a*nm + b),
+// cells g, g + G, ...  Each BRM point belongs to the cell (min(qi/Fi, ni-2), min(qj/Fj, nj-2))
+// and each BFM point to the cell (min(i, ni-2), min(j, nj-2)), so every lattice point is
+// counted once.  part[g][6][nm^3]: m3mf of T1, T3, T2, then m3mr of T1, T3, T2.
+__global__ __launch_bounds__(256) void k_msh_moments(int nm, int nz, const ZoneM *__restrict__ zones, int ncells,
+                                                     const float *__restrict__ T1, const float *__restrict__ T3,
+                                                     const float *__restrict__ T2, FrfPar frf,
+                                                     double *__restrict__ part) {
+    __shared__ float2 H[kQB][3][64];
+    __shared__ float wq[kQB], tiq[kQB], tjq[kQB];
+    __shared__ int zsel, ci0, cj0;
+    const int nm2 = nm * nm, nm3 = nm2 * nm;
+    const int e = blockIdx.y * 256 + threadIdx.x;
+    const bool ve = e < nm3;
+    const int ab = ve ? e % nm2 : 0, jj = ve ? e / nm2 : 0, a = ab / nm, b = ab % nm;
+    double mf[3] = {0.0, 0.0, 0.0}, mr[3] = {0.0, 0.0, 0.0};
+    for (int cid = blockIdx.x; cid < ncells; cid += gridDim.x) {
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int lo = 0, hi = nz - 1;  // last zone with cbase <= cid
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) / 2;
+                if (zones[mid].cbase <= cid) lo = mid; else hi = mid - 1;
+            }
+            const int loc = cid - zones[lo].cbase, njc = zones[lo].nj - 1;
+            zsel = lo;
+            ci0 = loc / njc;
+            cj0 = loc % njc;
+        }
+        __syncthreads();
+        const ZoneM z = zones[zsel];
+        const int i0 = ci0, j0 = cj0;
+        const int NI = (z.ni - 1) * z.Fi, NJ = (z.nj - 1) * z.Fj;
+        const int qi0 = i0 * z.Fi, qi1 = (i0 == z.ni - 2) ? NI : (i0 + 1) * z.Fi - 1;
+        const int qj0 = j0 * z.Fj, qj1 = (j0 == z.nj - 2) ? NJ : (j0 + 1) * z.Fj - 1;
+        const int nqj = qj1 - qj0 + 1, nq = (qi1 - qi0 + 1) * nqj;
+        const size_t P00 = (size_t)z.pbase + (size_t)i0 * z.nj + j0, P01 = P00 + 1, P10 = P00 + z.nj, P11 = P10 + 1;
+        float c[3][4];
+        if (ve) {
+            const float *Ts[3] = {T1, T3, T2};
+#pragma unroll
+            for (int t = 0; t < 3; ++t) {
+                c[t][0] = Ts[t][P00 * nm3 + e];
+                c[t][1] = Ts[t][P01 * nm3 + e];
+                c[t][2] = Ts[t][P10 * nm3 + e];
+                c[t][3] = Ts[t][P11 * nm3 + e];
+            }
+            // BFM lattice trapezoid (m3mf): the BFM points this cell owns
+            const double wb = z.sym * z.wI * z.wJ;
+            const int corner_i[4] = {i0, i0, i0 + 1, i0 + 1}, corner_j[4] = {j0, j0 + 1, j0, j0 + 1};
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const int ii = corner_i[k], jc = corner_j[k];
+                const bool own = (ii == i0 || i0 == z.ni - 2) && (jc == j0 || j0 == z.nj - 2);
+                if (!own) continue;
+                const double ti = (ii == 0 || ii == z.ni - 1) ? 0.5 : 1.0, tj = (jc == 0 || jc == z.nj - 1) ? 0.5 : 1.0;
+                const double wp = wb * ti * tj;
+#pragma unroll
+                for (int t = 0; t < 3; ++t) mf[t] += wp * (double)c[t][k];
+            }
+        }
+        float sr[3] = {0.f, 0.f, 0.f};
+        for (int q0 = 0; q0 < nq; q0 += kQB) {
+            const int nb = min(kQB, nq - q0);
+            __syncthreads();
+            for (int x = threadIdx.x; x < nb * 3 * nm; x += blockDim.x) {
+                const int ql = x / (3 * nm), r = x % (3 * nm), which = r / nm, m = r % nm;
+                const int qq = q0 + ql, qi = qi0 + qq / nqj, qj = qj0 + qq % nqj;
+                const double v1 = (z.fi0 + ((double)qi / z.Fi) * z.dI) * kPi2;
+                const double v2 = (z.fj0 + ((double)qj / z.Fj) * z.dJ) * kPi2;
+                const double w = which == 0 ? v1 : which == 1 ? v2 : v1 + v2;
+                double hr, hi;
+                frf_eval(frf.M[m], frf.K[m], frf.C[m], w, hr, hi);
+                H[ql][which][m] = make_float2((float)hr, (float)hi);
+            }
+            for (int ql = threadIdx.x; ql < nb; ql += blockDim.x) {
+                const int qq = q0 + ql, qi = qi0 + qq / nqj, qj = qj0 + qq % nqj;
+                const double ti = (qi == 0 || qi == NI) ? 0.5 : 1.0, tj = (qj == 0 || qj == NJ) ? 0.5 : 1.0;
+                wq[ql] = (float)(z.sym * (z.wI / z.Fi) * (z.wJ / z.Fj) * ti * tj);
+                tiq[ql] = (float)((double)(qi - i0 * z.Fi) / z.Fi);
+                tjq[ql] = (float)((double)(qj - j0 * z.Fj) / z.Fj);
+            }
+            __syncthreads();
+            if (!ve) continue;
+            for (int ql = 0; ql < nb; ++ql) {
+                const float ti = tiq[ql], tj = tjq[ql], w = wq[ql];
+                const float2 h1a = H[ql][0][a], h1j = H[ql][0][jj];
+                const float2 h2a = H[ql][1][a], h2b = H[ql][1][b];
+                const float2 h3a = H[ql][2][a], h3b = H[ql][2][b], h3j = H[ql][2][jj];
+                // Re[x y conj(z)] = (x.re y.re - x.im y.im) z.re + (x.re y.im + x.im y.re) z.im
+                const float f1 = (h1a.x * h2b.x - h1a.y * h2b.y) * h3j.x + (h1a.x * h2b.y + h1a.y * h2b.x) * h3j.y;
+                const float f3 = (h1j.x * h2b.x - h1j.y * h2b.y) * h3a.x + (h1j.x * h2b.y + h1j.y * h2b.x) * h3a.y;
+                const float f2 = (h1j.x * h2a.x - h1j.y * h2a.y) * h3b.x + (h1j.x * h2a.y + h1j.y * h2a.x) * h3b.y;
+                const float fs[3] = {f1, f3, f2};
+#pragma unroll
+                for (int t = 0; t < 3; ++t) {
+                    const float left = c[t][0] * (1.f - tj) + c[t][1] * tj;
+                    const float right = c[t][2] * (1.f - tj) + c[t][3] * tj;
+                    const float v = left * (1.f - ti) + right * ti;
+                    sr[t] = fmaf(w * fs[t], v, sr[t]);
+                }
+            }
+        }
+#pragma unroll
+        for (int t = 0; t < 3; ++t) mr[t] += (double)sr[t];
+    }
+    if (!ve) return;
+    double *pg = part + (size_t)blockIdx.x * 6 * nm3;
+#pragma unroll
+    for (int t = 0; t < 3; ++t) {
+        pg[(size_t)t * nm3 + e] = mf[t];
+        pg[(size_t)(3 + t) * nm3 + e] = mr[t];
+    }
+}
+
+// m3[m + nm n + nm^2 o] = 2 sum_g (T1 at (a,b,j') = (m,n,o) + T3 at (o,n,m) + T2 at (n,o,m)).
+__global__ void k_msh_reduce(int nm, int G, const double *__restrict__ part, double *__restrict__ m3mf,
+                             double *__restrict__ m3mr) {
+    const int nm2 = nm * nm, nm3 = nm2 * nm;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= nm3) return;
+    const int m = x % nm, n = (x / nm) % nm, o = x / nm2;
+    const int e1 = o * nm2 + m * nm + n, e3 = m * nm2 + o * nm + n, e2 = m * nm2 + n * nm + o;
+    double sf = 0.0, sr = 0.0;
+    for (int g = 0; g < G; ++g) {
+        const double *pg = part + (size_t)g * 6 * nm3;
+        sf += pg[e1] + pg[(size_t)nm3 + e3] + pg[(size_t)2 * nm3 + e2];
+        sr += pg[(size_t)3 * nm3 + e1] + pg[(size_t)4 * nm3 + e3] + pg[(size_t)5 * nm3 + e2];
+    }
+    m3mf[x] = 2.0 * sf;
+    m3mr[x] = 2.0 * sr;
+}
+
+}  // namespace mshmix
+
+// ------------------------------------------------------------------------------------
+// Host side: zone batches -> operand tables -> tasks -> contraction -> zone integration.
+// ------------------------------------------------------------------------------------
+namespace {
+
+// The lattice of z aligned with the axes, as (f1 index axis, f2 index axis); false if rotated.
+bool axis_aligned(const ZoneDev &z, ZoneDev &out) {
+    if (z.dIj == 0.0 && z.dJi == 0.0) {
+        out = z;
+        return true;
+    }
+    if (z.dIi == 0.0 && z.dJj == 0.0) {  // f1 runs along J, f2 along I: relabel the axes
+        out = z;
+        out.dIi = z.dJi; out.dIj = 0.0; out.dJi = 0.0; out.dJj = z.dIj;
+        out.wI = z.wJ; out.wJ = z.wI;
+        out.ni = z.nj; out.nj = z.ni;
+        out.Fi = z.Fj; out.Fj = z.Fi;
+        return true;
+    }
+    return false;
+}
+
+struct FreqIndex {
+    std::vector<double> v;
+    void add(double f) { v.push_back(f); }
+    void seal() {
+        std::sort(v.begin(), v.end());
+        v.erase(std::unique(v.begin(), v.end()), v.end());
+    }
+    int at(double f) const { return (int)(std::lower_bound(v.begin(), v.end(), f) - v.begin()); }
+};
+
+}  // namespace
+
+int Engine::msh_mixed_batch(const std::vector<ZoneDev> &zs, std::vector<double> &accF, std::vector<double> &accR,
+                            float &ms_gemm, float &ms_all) {
+    using namespace mshmix;
+    const int nm = nme, nm2 = nm * nm, nm3 = nm2 * nm;
+    const int NMT = ((nm + 7) / 8) * 8, NC = kBN / NMT, BROWS = NC * NMT;
+    const int Kp = ((K + kBK - 1) / kBK) * kBK, Mp = ((nm2 + kBM - 1) / kBM) * kBM, MT = Mp / kBM;
+    // frequencies of lines, columns and points
+    FreqIndex F, UF;
+    long long npts = 0, ncells = 0, ncol = 0;
+    for (const ZoneDev &z : zs) {
+        for (int i = 0; i < z.ni; ++i) {
+            const double r = z.fi0 + i * z.dIi;
+            F.add(r);
+            UF.add(r);
+            for (int j = 0; j < z.nj; ++j) F.add(r + (z.fj0 + j * z.dJj));
+        }
+        for (int j = 0; j < z.nj; ++j) {
+            F.add(z.fj0 + j * z.dJj);
+            UF.add(z.fj0 + j * z.dJj);
+        }
+        npts += (long long)z.ni * z.nj;
+        ncells += (long long)(z.ni - 1) * (z.nj - 1);
+        ncol += z.nj;
+    }
+    F.seal();
+    UF.seal();
+    const int nU = (int)UF.v.size();
+    std::vector<int> usrc(nU), gsrc((size_t)ncol), ssrc(2 * (size_t)npts);
+    for (int u = 0; u < nU; ++u) usrc[u] = F.at(UF.v[u]);
+    std::vector<Task> tasks;
+    std::vector<ZoneM> zm;
+    {
+        long long pb = 0, cb = 0, gb = 0;
+        for (const ZoneDev &z : zs) {
+            ZoneM m{z.fi0, z.fj0, z.dIi, z.dJj, z.wI, z.wJ, z.sym, z.ni, z.nj, z.Fi, z.Fj, (int)pb, (int)cb};
+            zm.push_back(m);
+            for (int j = 0; j < z.nj; ++j) gsrc[gb + j] = F.at(z.fj0 + j * z.dJj);
+            for (int i = 0; i < z.ni; ++i) {
+                const double r = z.fi0 + i * z.dIi;
+                for (int j = 0; j < z.nj; ++j) {
+                    const int row = F.at(r + (z.fj0 + j * z.dJj));
+                    ssrc[pb + (size_t)i * z.nj + j] = row;                  // line order (kind 0)
+                    ssrc[npts + pb + (size_t)j * z.ni + i] = row;           // column order (kind 1)
+                }
+                tasks.push_back(Task{UF.at(r) * Mp, (int)gb * NMT, (int)(pb + (long long)i * z.nj) * NMT, z.nj,
+                                     (int)(pb + (long long)i * z.nj), 1, 0});
+            }
+            for (int j = 0; j < z.nj; ++j)
+                tasks.push_back(Task{UF.at(z.fj0 + j * z.dJj) * Mp, -1, (int)(npts + pb + (long long)j * z.ni) * NMT,
+                                     z.ni, (int)(pb + j), z.nj, 1});
+            pb += (long long)z.ni * z.nj;
+            cb += (long long)(z.ni - 1) * (z.nj - 1);
+            gb += z.nj;
+        }
+    }
+    cudaError_t e;
+    int rc;
+    if ((e = cudaEventRecord(ev2, stream))) return cuda_fail(e, "event");
+    if ((rc = build_atable(F.v, true))) return rc;
+    const size_t uel = (size_t)nU * Mp * Kp, gel = (size_t)ncol * NMT * Kp, sel = 2 * (size_t)npts * NMT * Kp;
+    const size_t tel = (size_t)npts * nm3;
+    const size_t nidx = (size_t)nU + ncol + 2 * (size_t)npts;
+    int dev = 0, nsm = 0;
+    if ((e = cudaGetDevice(&dev)) || (e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev)))
+        return cuda_fail(e, "device query");
+    const int nchunks = (nm3 + 255) / 256;
+    const int G = (int)std::max(1LL, std::min((long long)(4 * nsm + nchunks - 1) / nchunks, ncells));
+    if ((e = dMixA.reserve(2 * uel * 2)) || (e = dMixB.reserve(2 * (gel + sel) * 2)) ||
+        (e = dMshT.reserve(3 * tel * sizeof(float))) ||
+        (e = dMshIdx.reserve(nidx * sizeof(int) + tasks.size() * sizeof(Task) + zm.size() * sizeof(ZoneM) + 64)) ||
+        (e = dMixPart.reserve((size_t)G * 6 * nm3 * sizeof(double) + 2 * (size_t)nm3 * sizeof(double) + 256)))
+        return cuda_fail(e, "allocating Mesher BF16x3 operands");
+    __nv_bfloat16 *Uh = dMixA.as<__nv_bfloat16>(), *Ul = Uh + uel;
+    __nv_bfloat16 *Gh = dMixB.as<__nv_bfloat16>(), *Gl = Gh + gel, *Sh = Gl + gel, *Sl = Sh + sel;
+    float *T1 = dMshT.as<float>(), *T3 = T1 + tel, *T2 = T3 + tel;
+    char *ib = (char *)dMshIdx.p;
+    int *d_usrc = (int *)ib, *d_gsrc = d_usrc + nU, *d_ssrc = d_gsrc + ncol;
+    Task *d_tasks = (Task *)(((uintptr_t)(d_ssrc + 2 * npts) + 15) & ~(uintptr_t)15);
+    ZoneM *d_zones = (ZoneM *)(((uintptr_t)(d_tasks + tasks.size()) + 15) & ~(uintptr_t)15);
+    double *part = dMixPart.as<double>(), *red = part + (size_t)G * 6 * nm3;
+    int *derr = (int *)(red + 2 * (size_t)nm3);
+    if ((e = cudaMemcpyAsync(d_usrc, usrc.data(), nU * sizeof(int), cudaMemcpyHostToDevice, stream)) ||
+        (e = cudaMemcpyAsync(d_gsrc, gsrc.data(), ncol * sizeof(int), cudaMemcpyHostToDevice, stream)) ||
+        (e = cudaMemcpyAsync(d_ssrc, ssrc.data(), 2 * npts * sizeof(int), cudaMemcpyHostToDevice, stream)) ||
+        (e = cudaMemcpyAsync(d_tasks, tasks.data(), tasks.size() * sizeof(Task), cudaMemcpyHostToDevice, stream)) ||
+        (e = cudaMemcpyAsync(d_zones, zm.data(), zm.size() * sizeof(ZoneM), cudaMemcpyHostToDevice, stream)) ||
+        (e = cudaMemsetAsync(derr, 0, sizeof(int), stream)))
+        return cuda_fail(e, "Mesher task upload");
+    h2d += (double)(nidx * sizeof(int) + tasks.size() * sizeof(Task) + zm.size() * sizeof(ZoneM));
+    k_prep_u_rows<<<dim3(nU, Kp / 32), 256, 0, stream>>>(nm, K, Kp, Mp, d_usrc, dA32.as<float>(), dQ.as<double>(), Uh, Ul);
+    k_prep_b_rows<<<dim3((unsigned)ncol, Kp / 64), 256, 0, stream>>>(nm, NMT, K, Kp, d_gsrc, dA32.as<float>(), Gh, Gl);
+    k_prep_b_rows<<<dim3((unsigned)(2 * npts), Kp / 64), 256, 0, stream>>>(nm, NMT, K, Kp, d_ssrc, dA32.as<float>(), Sh, Sl);
+    if ((e = cudaGetLastError())) return cuda_fail(e, "Mesher operand preparation");
+    kernels += 3;
+    CUtensorMap maps[6];
+    if (!make_map(&maps[0], Uh, Kp, (uint64_t)nU * Mp, kBM) || !make_map(&maps[1], Ul, Kp, (uint64_t)nU * Mp, kBM) ||
+        !make_map(&maps[2], Gh, Kp, (uint64_t)ncol * NMT, BROWS) || !make_map(&maps[3], Gl, Kp, (uint64_t)ncol * NMT, BROWS) ||
+        !make_map(&maps[4], Sh, Kp, 2 * (uint64_t)npts * NMT, BROWS) ||
+        !make_map(&maps[5], Sl, Kp, 2 * (uint64_t)npts * NMT, BROWS))
+        return fail(BSA_ERR_CUDA, "cuTensorMapEncodeTiled failed");
+    MParams prm{};
+    prm.nm = nm; prm.NMT = NMT; prm.NC = NC; prm.BROWS = BROWS; prm.Mp = Mp; prm.MT = MT;
+    prm.nk = Kp / kBK;
+    prm.ks_last = (K - (prm.nk - 1) * kBK + 15) / 16;
+    prm.ntasks = (int)tasks.size();
+    prm.tasks = d_tasks;
+    prm.T1 = T1; prm.T3 = T3; prm.T2 = T2;
+    prm.err = derr;
+    const long long nwork = (long long)tasks.size() * MT;
+    const int grid = (int)std::min<long long>(nwork, nsm);
+    const size_t smem = (size_t)kStages * kStageBytes + 1024 + 256;
+    if ((e = cudaFuncSetAttribute(k_msh_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)))
+        return cuda_fail(e, "kernel attribute");
+    if ((e = cudaEventRecord(evg0, stream))) return cuda_fail(e, "event");
+    k_msh_mixed<<<grid, 192, smem, stream>>>(maps[0], maps[1], maps[2], maps[3], maps[4], maps[5], prm);
+    if ((e = cudaGetLastError())) return cuda_fail(e, "Mesher BF16x3 contraction kernel");
+    if ((e = cudaEventRecord(evg1, stream))) return cuda_fail(e, "event");
+    k_msh_moments<<<dim3(G, nchunks), 256, 0, stream>>>(nm, (int)zm.size(), d_zones, (int)ncells, T1, T3, T2, frf(),
+                                                         part);
+    k_msh_reduce<<<(nm3 + 127) / 128, 128, 0, stream>>>(nm, G, part, red, red + nm3);
+    if ((e = cudaGetLastError())) return cuda_fail(e, "Mesher zone integration");
+    kernels += 3;
+    std::vector<double> h(2 * (size_t)nm3);
+    int herr = 0;
+    if ((e = cudaMemcpyAsync(h.data(), red, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, stream)) ||
+        (e = cudaMemcpyAsync(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost, stream)) ||
+        (e = cudaEventRecord(ev1, stream)) || (e = cudaStreamSynchronize(stream)))
+        return cuda_fail(e, "Mesher BF16x3 evaluation");
+    d2h += (double)sizeof(double) * h.size() + sizeof(int);
+    if (herr) return fail(BSA_ERR_TIMEOUT, "Mesher BF16x3 kernel: a pipeline wait ran out of its budget (role %d)", herr);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, evg0, evg1);
+    ms_gemm += ms;
+    cudaEventElapsedTime(&ms, ev2, ev1);
+    ms_all += ms;
+    for (int x = 0; x < nm3; ++x) {
+        accF[x] += h[x];
+        accR[x] += h[nm3 + x];
+    }
+    return BSA_OK;
+}
+
+// Zones in the split precision: axis-aligned zones in batches through the tensor cores,
+// rotated ones through the FP64 point kernel.
+int Engine::run_zones_mixed(const std::vector<ZoneDev> &zones, double *m3mf, double *m3mr, double *npts) {
+    int rc = upload_problem();
+    if (rc) return rc;
+    const int nm = nme;
+    const long long nm3 = (long long)nm * nm * nm;
+    if (nm > 64) return fail(BSA_ERR_UNSUPPORTED, "at most 64 kept modes");
+    std::vector<ZoneDev> axis, rot;
+    double nbfm = 0.0, nbrm = 0.0;
+    for (const ZoneDev &z : zones) {
+        if (z.ni < 2 || z.nj < 2 || z.Fi < 1 || z.Fj < 1)
+            return fail(BSA_ERR_ARG, "zone lattice needs ni, nj >= 2 and Fi, Fj >= 1");
+        ZoneDev a;
+        if (axis_aligned(z, a)) axis.push_back(a); else rot.push_back(z);
+        nbfm += (double)z.ni * z.nj;
+        nbrm += (double)((z.ni - 1) * z.Fi + 1) * ((z.nj - 1) * z.Fj + 1);
+    }
+    std::vector<double> accF(nm3, 0.0), accR(nm3, 0.0);
+    float ms_gemm = 0.f, ms_all = 0.f;
+    int nk = 0;
+    double hb = 0.0, db = 0.0;
+    if (!rot.empty()) {
+        std::vector<double> f(nm3), r(nm3);
+        int rc = run_zones_fp64(rot, f.data(), r.data(), nullptr);
+        if (rc) return rc;
+        ms_gemm += (float)last_ms_gemm;
+        ms_all += (float)last_ms;
+        nk = kernels;
+        hb = h2d;
+        db = d2h;
+        for (long long x = 0; x < nm3; ++x) { accF[x] += f[x]; accR[x] += r[x]; }
+    }
+    kernels = 0;
+    h2d = d2h = 0;
+    if (!axis.empty()) {
+        // batch by device bytes: operand tables, term tensors and U blocks
+        const int NMT = ((nm + 7) / 8) * 8;
+        const double Kp = (double)(((K + 63) / 64) * 64), Mp = (double)(((nm * nm + 127) / 128) * 128);
+        const double per_pt = 2.0 * NMT * Kp * 4.0 + 3.0 * nm3 * 4.0, per_line = Mp * Kp * 4.0 + NMT * Kp * 4.0;
+        const double budget = 12e9;
+        size_t b0 = 0;
+        while (b0 < axis.size()) {
+            double bytes = 0.0;
+            size_t b1 = b0;
+            long long pts = 0;
+            while (b1 < axis.size()) {
+                const ZoneDev &z = axis[b1];
+                const double add = per_pt * z.ni * z.nj + per_line * (z.ni + z.nj);
+                if (b1 > b0 && (bytes + add > budget || pts + (long long)z.ni * z.nj > 4000000)) break;
+                bytes += add;
+                pts += (long long)z.ni * z.nj;
+                ++b1;
+            }
+            std::vector<ZoneDev> batch(axis.begin() + b0, axis.begin() + b1);
+            if ((rc = msh_mixed_batch(batch, accF, accR, ms_gemm, ms_all))) return rc;
+            b0 = b1;
+        }
+    }
+    if (m3mf) std::memcpy(m3mf, accF.data(), sizeof(double) * nm3);
+    if (m3mr) std::memcpy(m3mr, accR.data(), sizeof(double) * nm3);
+    kernels += nk;
+    h2d += hb;
+    d2h += db;
+    last_ms_gemm = ms_gemm;
+    last_ms_contraction = ms_all;
+    last_ms = ms_all;
+    last_points = nbrm;
+    if (npts) {
+        npts[0] = nbfm;
+        npts[1] = nbrm;
+    }
+    return BSA_OK;
+}
+
+}  // namespace bsa

@@ -117,6 +117,7 @@ def test_pod_truncation_requests(bsalib):
     """The default POD form keeps every mode (== the direct form evaluated here); a request
     that drops POD modes is refused with BSA_ERR_UNSUPPORTED instead of being ignored."""
     prob = cantilever_tower(nfreqs=5, df=0.5, nodes=6)
+    prob.settings.svd = 1  # the POD form (the reference's default Mesher function)
     s = api.BsaSession(prob)
     try:
         L = s.lib
