@@ -79,13 +79,14 @@ struct Engine {
     int nme = 0, K = 0;
     std::vector<double> phitc, hL, hQ, hLogc, hM, hK, hC;
     std::vector<double> hWd3, hWd2;  // diagonal-only weights Q L^2 and L^2, [k][m]
+    std::vector<float> hLogc32, hL32;  // FP32 copies for the split-precision A(f) table
     std::vector<PsdNode> hPsd;
 
     // device
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr;
     DevBuf dL, dQ, dLogc, dPsdPar, dFrfM, dFrfK, dFrfC, dFreq, dS, dA, dPartF, dPartR, dOut, dPsdF, dWf, dPts,
-        dPtsD, dBF, dBR, dMixA, dMixB, dMixH, dMixPart, dA32, dZones, dZidx, dWd3, dWd2, dMshT, dMshIdx;
+        dPtsD, dBF, dBR, dMixA, dMixB, dMixH, dMixPart, dA32, dZones, dZidx, dWd3, dWd2, dMshT, dMshIdx, dLogc32, dL32;
 
     // stats
     double last_ms = 0, last_ms_contraction = 0, last_ms_gemm = 0, last_points = 0;

@@ -73,7 +73,7 @@ void Engine::reset_inputs() {
 void Engine::free_device() {
     for (DevBuf *b : {&dL, &dQ, &dLogc, &dPsdPar, &dFrfM, &dFrfK, &dFrfC, &dFreq, &dS, &dA, &dPartF, &dPartR,
                       &dOut, &dPsdF, &dWf, &dPts, &dPtsD, &dBF, &dBR, &dMixA, &dMixB, &dMixH, &dMixPart, &dA32,
-                      &dZones, &dZidx, &dWd3, &dWd2, &dMshT, &dMshIdx})
+                      &dZones, &dZidx, &dWd3, &dWd2, &dMshT, &dMshIdx, &dLogc32, &dL32})
         b->release();
     if (stream) cudaStreamDestroy(stream);
     stream = nullptr;
@@ -209,6 +209,8 @@ int Engine::validate() {
                 const double c = I.corr[(size_t)(id - 1) + (size_t)ncorr * (set.tc[itc] - 1)];
                 hLogc[((size_t)itc * nnl + i) * nnl + j] = std::log(c);
             }
+    hLogc32.assign(hLogc.begin(), hLogc.end());
+    hL32.assign(hL.begin(), hL.end());
     const int idir = set.dirs.empty() ? 1 : set.dirs[0];
     hPsd.assign((size_t)ntc * nnl, PsdNode{});
     for (int itc = 0; itc < ntc; ++itc) {
@@ -247,7 +249,8 @@ int Engine::upload_problem() {
     cudaError_t e;
     if ((e = upload(dL, hL, stream)) || (e = upload(dQ, hQ, stream)) || (e = upload(dLogc, hLogc, stream)) ||
         (e = upload(dPsdPar, hPsd, stream)) || (e = upload(dFrfM, hM, stream)) || (e = upload(dFrfK, hK, stream)) ||
-        (e = upload(dFrfC, hC, stream)) || (e = upload(dWd3, hWd3, stream)) || (e = upload(dWd2, hWd2, stream)))
+        (e = upload(dFrfC, hC, stream)) || (e = upload(dWd3, hWd3, stream)) || (e = upload(dWd2, hWd2, stream)) ||
+        (e = upload(dLogc32, hLogc32, stream)) || (e = upload(dL32, hL32, stream)))
         return cuda_fail(e, "uploading problem data");
     dev_uploaded = true;
     return BSA_OK;
@@ -278,8 +281,8 @@ int Engine::build_atable(const std::vector<double> &freqs, bool fp32) {
     if (rc) return rc;
     if (fp32) {
         if ((e = dA32.reserve(sizeof(float) * (size_t)nf * K * nme))) return cuda_fail(e, "allocating A");
-        e = launch_atable32(stream, nf, dFreq.as<double>(), ntc, in.nnl, nme, dLogc.as<double>(), dS.as<double>(),
-                            dL.as<double>(), dA32.as<float>());
+        e = launch_atable32(stream, nf, dFreq.as<double>(), ntc, in.nnl, nme, dLogc32.as<float>(), dS.as<double>(),
+                            dL32.as<float>(), dA32.as<float>());
     } else {
         if ((e = dA.reserve(sizeof(double) * (size_t)nf * K * nme))) return cuda_fail(e, "allocating A");
         e = launch_atable(stream, nf, dFreq.as<double>(), ntc, in.nnl, nme, dLogc.as<double>(), dS.as<double>(),

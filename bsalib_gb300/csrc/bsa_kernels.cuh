@@ -13,9 +13,10 @@ cudaError_t launch_nodal_psd(cudaStream_t st, int nf, const double *f, int ntc, 
 cudaError_t launch_atable(cudaStream_t st, int nf, const double *f, int ntc, int nnl, int nm,
                           const double *logc, const double *S, const double *L, double *A);
 
-// The same factor in FP32 (source of the split-precision contraction's operands).
+// The same factor in FP32 (source of the split-precision contractions' operands), from FP32
+// copies of log c and L.
 cudaError_t launch_atable32(cudaStream_t st, int nf, const double *f, int ntc, int nnl, int nm,
-                            const double *logc, const double *S, const double *L, float *A);
+                            const float *logc, const double *S, const float *L, float *A);
 
 // Force PSD on the grid psd[f][n + nm*o] = sum_k L[k][o] A[f][k][n]
 // (functionsImpl.F90:1548-1560), then the second-order moments

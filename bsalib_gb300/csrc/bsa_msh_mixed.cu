@@ -310,14 +310,47 @@ __global__ void k_prep_b_rows(int nm, int NMT, int K, int Kp, const int *__restr
 // ------------------------------------------------------------------------------------
 // An axis-aligned zone of the batch: BFM point (i, j) at (fi0 + i dI, fj0 + j dJ), term
 // tensors at point pbase + i*nj + j, cells (i0, j0), 0 <= i0 < ni-1, 0 <= j0 < nj-1,
-// numbered from cbase.
+// numbered from cbase; BRM point (qi, qj), 0 <= qi <= (ni-1) Fi, 0 <= qj <= (nj-1) Fj, at
+// qbase + qi * ((nj-1) Fj + 1) + qj in the FRF table.
 struct ZoneM {
     double fi0, fj0, dI, dJ, wI, wJ, sym;
     int ni, nj, Fi, Fj;
-    int pbase, cbase;
+    int pbase, cbase, qbase;
 };
 
-constexpr int kQB = 24;  // BRM points per FRF staging round
+__device__ __forceinline__ int zone_of(const ZoneM *__restrict__ zones, int nz, int idx, int which) {
+    int lo = 0, hi = nz - 1;  // last zone whose base (cells: which 0, BRM points: which 1) <= idx
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) / 2;
+        const int base = which == 0 ? zones[mid].cbase : zones[mid].qbase;
+        if (base <= idx) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Per BRM point q: H_m(w1), H_m(w2), H_m(w1 + w2) evaluated in FP64 and rounded once
+// (Hq[q][3][nm]), and its integration weight sym (wI/Fi)(wJ/Fj) t_i t_j (Wq[q]).
+__global__ void k_msh_frf(int nm, int nz, const ZoneM *__restrict__ zones, int nq, FrfPar frf,
+                          float2 *__restrict__ Hq, float *__restrict__ Wq) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)nq * 3 * nm) return;
+    const int q = (int)(t / (3 * nm)), r = (int)(t % (3 * nm)), which = r / nm, m = r % nm;
+    const ZoneM z = zones[zone_of(zones, nz, q, 1)];
+    const int NI = (z.ni - 1) * z.Fi, NJ = (z.nj - 1) * z.Fj;
+    const int loc = q - z.qbase, qi = loc / (NJ + 1), qj = loc % (NJ + 1);
+    const double v1 = (z.fi0 + ((double)qi / z.Fi) * z.dI) * kPi2;
+    const double v2 = (z.fj0 + ((double)qj / z.Fj) * z.dJ) * kPi2;
+    const double w = which == 0 ? v1 : which == 1 ? v2 : v1 + v2;
+    double hr, hi;
+    frf_eval(frf.M[m], frf.K[m], frf.C[m], w, hr, hi);
+    Hq[t] = make_float2((float)hr, (float)hi);
+    if (r == 0) {
+        const double ti = (qi == 0 || qi == NI) ? 0.5 : 1.0, tj = (qj == 0 || qj == NJ) ? 0.5 : 1.0;
+        Wq[q] = (float)(z.sym * (z.wI / z.Fi) * (z.wJ / z.Fj) * ti * tj);
+    }
+}
+
+constexpr int kQB = 24;  // BRM points per shared-memory round
 
 // Block (g, chunk): elements e = chunk*256 + t of the term tensors (e = j'*nm^2 + a*nm + b),
 // cells g, g + G, ...  Each BRM point belongs to the cell (min(qi/Fi, ni-2), min(qj/Fj, nj-2))
@@ -325,11 +358,11 @@ constexpr int kQB = 24;  // BRM points per FRF staging round
 // counted once.  part[g][6][nm^3]: m3mf of T1, T3, T2, then m3mr of T1, T3, T2.
 __global__ __launch_bounds__(256) void k_msh_moments(int nm, int nz, const ZoneM *__restrict__ zones, int ncells,
                                                      const float *__restrict__ T1, const float *__restrict__ T3,
-                                                     const float *__restrict__ T2, FrfPar frf,
-                                                     double *__restrict__ part) {
+                                                     const float *__restrict__ T2, const float2 *__restrict__ Hq,
+                                                     const float *__restrict__ Wq, double *__restrict__ part) {
     __shared__ float2 H[kQB][3][64];
     __shared__ float wq[kQB], tiq[kQB], tjq[kQB];
-    __shared__ int zsel, ci0, cj0;
+    __shared__ int zsel;
     const int nm2 = nm * nm, nm3 = nm2 * nm;
     const int e = blockIdx.y * 256 + threadIdx.x;
     const bool ve = e < nm3;
@@ -337,24 +370,15 @@ __global__ __launch_bounds__(256) void k_msh_moments(int nm, int nz, const ZoneM
     double mf[3] = {0.0, 0.0, 0.0}, mr[3] = {0.0, 0.0, 0.0};
     for (int cid = blockIdx.x; cid < ncells; cid += gridDim.x) {
         __syncthreads();
-        if (threadIdx.x == 0) {
-            int lo = 0, hi = nz - 1;  // last zone with cbase <= cid
-            while (lo < hi) {
-                const int mid = (lo + hi + 1) / 2;
-                if (zones[mid].cbase <= cid) lo = mid; else hi = mid - 1;
-            }
-            const int loc = cid - zones[lo].cbase, njc = zones[lo].nj - 1;
-            zsel = lo;
-            ci0 = loc / njc;
-            cj0 = loc % njc;
-        }
+        if (threadIdx.x == 0) zsel = zone_of(zones, nz, cid, 0);
         __syncthreads();
         const ZoneM z = zones[zsel];
-        const int i0 = ci0, j0 = cj0;
+        const int loc = cid - z.cbase, i0 = loc / (z.nj - 1), j0 = loc % (z.nj - 1);
         const int NI = (z.ni - 1) * z.Fi, NJ = (z.nj - 1) * z.Fj;
         const int qi0 = i0 * z.Fi, qi1 = (i0 == z.ni - 2) ? NI : (i0 + 1) * z.Fi - 1;
         const int qj0 = j0 * z.Fj, qj1 = (j0 == z.nj - 2) ? NJ : (j0 + 1) * z.Fj - 1;
         const int nqj = qj1 - qj0 + 1, nq = (qi1 - qi0 + 1) * nqj;
+        const float rFi = 1.f / (float)z.Fi, rFj = 1.f / (float)z.Fj;
         const size_t P00 = (size_t)z.pbase + (size_t)i0 * z.nj + j0, P01 = P00 + 1, P10 = P00 + z.nj, P11 = P10 + 1;
         float c[3][4];
         if (ve) {
@@ -385,21 +409,16 @@ __global__ __launch_bounds__(256) void k_msh_moments(int nm, int nz, const ZoneM
             const int nb = min(kQB, nq - q0);
             __syncthreads();
             for (int x = threadIdx.x; x < nb * 3 * nm; x += blockDim.x) {
-                const int ql = x / (3 * nm), r = x % (3 * nm), which = r / nm, m = r % nm;
-                const int qq = q0 + ql, qi = qi0 + qq / nqj, qj = qj0 + qq % nqj;
-                const double v1 = (z.fi0 + ((double)qi / z.Fi) * z.dI) * kPi2;
-                const double v2 = (z.fj0 + ((double)qj / z.Fj) * z.dJ) * kPi2;
-                const double w = which == 0 ? v1 : which == 1 ? v2 : v1 + v2;
-                double hr, hi;
-                frf_eval(frf.M[m], frf.K[m], frf.C[m], w, hr, hi);
-                H[ql][which][m] = make_float2((float)hr, (float)hi);
+                const int ql = x / (3 * nm), r = x % (3 * nm), qq = q0 + ql;
+                const int qi = qi0 + qq / nqj, qj = qj0 + qq % nqj;
+                const size_t gq = (size_t)z.qbase + (size_t)qi * (NJ + 1) + qj;
+                H[ql][r / nm][r % nm] = Hq[gq * 3 * nm + r];
             }
             for (int ql = threadIdx.x; ql < nb; ql += blockDim.x) {
                 const int qq = q0 + ql, qi = qi0 + qq / nqj, qj = qj0 + qq % nqj;
-                const double ti = (qi == 0 || qi == NI) ? 0.5 : 1.0, tj = (qj == 0 || qj == NJ) ? 0.5 : 1.0;
-                wq[ql] = (float)(z.sym * (z.wI / z.Fi) * (z.wJ / z.Fj) * ti * tj);
-                tiq[ql] = (float)((double)(qi - i0 * z.Fi) / z.Fi);
-                tjq[ql] = (float)((double)(qj - j0 * z.Fj) / z.Fj);
+                wq[ql] = Wq[(size_t)z.qbase + (size_t)qi * (NJ + 1) + qj];
+                tiq[ql] = (float)(qi - i0 * z.Fi) * rFi;
+                tjq[ql] = (float)(qj - j0 * z.Fj) * rFj;
             }
             __syncthreads();
             if (!ve) continue;
@@ -496,7 +515,7 @@ int Engine::msh_mixed_batch(const std::vector<ZoneDev> &zs, std::vector<double> 
     const int Kp = ((K + kBK - 1) / kBK) * kBK, Mp = ((nm2 + kBM - 1) / kBM) * kBM, MT = Mp / kBM;
     // frequencies of lines, columns and points
     FreqIndex F, UF;
-    long long npts = 0, ncells = 0, ncol = 0;
+    long long npts = 0, ncells = 0, ncol = 0, nbrm = 0;
     for (const ZoneDev &z : zs) {
         for (int i = 0; i < z.ni; ++i) {
             const double r = z.fi0 + i * z.dIi;
@@ -511,6 +530,7 @@ int Engine::msh_mixed_batch(const std::vector<ZoneDev> &zs, std::vector<double> 
         npts += (long long)z.ni * z.nj;
         ncells += (long long)(z.ni - 1) * (z.nj - 1);
         ncol += z.nj;
+        nbrm += (long long)((z.ni - 1) * z.Fi + 1) * ((z.nj - 1) * z.Fj + 1);
     }
     F.seal();
     UF.seal();
@@ -520,9 +540,10 @@ int Engine::msh_mixed_batch(const std::vector<ZoneDev> &zs, std::vector<double> 
     std::vector<Task> tasks;
     std::vector<ZoneM> zm;
     {
-        long long pb = 0, cb = 0, gb = 0;
+        long long pb = 0, cb = 0, gb = 0, qb = 0;
         for (const ZoneDev &z : zs) {
-            ZoneM m{z.fi0, z.fj0, z.dIi, z.dJj, z.wI, z.wJ, z.sym, z.ni, z.nj, z.Fi, z.Fj, (int)pb, (int)cb};
+            ZoneM m{z.fi0, z.fj0, z.dIi, z.dJj, z.wI, z.wJ, z.sym, z.ni, z.nj, z.Fi, z.Fj, (int)pb, (int)cb, (int)qb};
+            qb += (long long)((z.ni - 1) * z.Fi + 1) * ((z.nj - 1) * z.Fj + 1);
             zm.push_back(m);
             for (int j = 0; j < z.nj; ++j) gsrc[gb + j] = F.at(z.fj0 + j * z.dJj);
             for (int i = 0; i < z.ni; ++i) {
@@ -558,7 +579,8 @@ int Engine::msh_mixed_batch(const std::vector<ZoneDev> &zs, std::vector<double> 
     if ((e = dMixA.reserve(2 * uel * 2)) || (e = dMixB.reserve(2 * (gel + sel) * 2)) ||
         (e = dMshT.reserve(3 * tel * sizeof(float))) ||
         (e = dMshIdx.reserve(nidx * sizeof(int) + tasks.size() * sizeof(Task) + zm.size() * sizeof(ZoneM) + 64)) ||
-        (e = dMixPart.reserve((size_t)G * 6 * nm3 * sizeof(double) + 2 * (size_t)nm3 * sizeof(double) + 256)))
+        (e = dMixPart.reserve((size_t)G * 6 * nm3 * sizeof(double) + 2 * (size_t)nm3 * sizeof(double) + 256)) ||
+        (e = dMixH.reserve((size_t)nbrm * 3 * nm * sizeof(float2) + (size_t)nbrm * sizeof(float) + 256)))
         return cuda_fail(e, "allocating Mesher BF16x3 operands");
     __nv_bfloat16 *Uh = dMixA.as<__nv_bfloat16>(), *Ul = Uh + uel;
     __nv_bfloat16 *Gh = dMixB.as<__nv_bfloat16>(), *Gl = Gh + gel, *Sh = Gl + gel, *Sl = Sh + sel;
@@ -605,11 +627,17 @@ int Engine::msh_mixed_batch(const std::vector<ZoneDev> &zs, std::vector<double> 
     k_msh_mixed<<<grid, 192, smem, stream>>>(maps[0], maps[1], maps[2], maps[3], maps[4], maps[5], prm);
     if ((e = cudaGetLastError())) return cuda_fail(e, "Mesher BF16x3 contraction kernel");
     if ((e = cudaEventRecord(evg1, stream))) return cuda_fail(e, "event");
-    k_msh_moments<<<dim3(G, nchunks), 256, 0, stream>>>(nm, (int)zm.size(), d_zones, (int)ncells, T1, T3, T2, frf(),
+    float2 *Hq = dMixH.as<float2>();
+    float *Wq = (float *)(Hq + (size_t)nbrm * 3 * nm);
+    {
+        const long long nt = nbrm * 3 * nm;
+        k_msh_frf<<<(unsigned)((nt + 255) / 256), 256, 0, stream>>>(nm, (int)zm.size(), d_zones, (int)nbrm, frf(), Hq, Wq);
+    }
+    k_msh_moments<<<dim3(G, nchunks), 256, 0, stream>>>(nm, (int)zm.size(), d_zones, (int)ncells, T1, T3, T2, Hq, Wq,
                                                          part);
     k_msh_reduce<<<(nm3 + 127) / 128, 128, 0, stream>>>(nm, G, part, red, red + nm3);
     if ((e = cudaGetLastError())) return cuda_fail(e, "Mesher zone integration");
-    kernels += 3;
+    kernels += 4;
     std::vector<double> h(2 * (size_t)nm3);
     int herr = 0;
     if ((e = cudaMemcpyAsync(h.data(), red, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, stream)) ||
@@ -666,22 +694,35 @@ int Engine::run_zones_mixed(const std::vector<ZoneDev> &zones, double *m3mf, dou
     kernels = 0;
     h2d = d2h = 0;
     if (!axis.empty()) {
-        // batch by device bytes: operand tables, term tensors and U blocks
+        // batches by device bytes: U blocks of the distinct line / column frequencies, column
+        // and sum tables, term tensors and BRM-point FRF tables
         const int NMT = ((nm + 7) / 8) * 8;
         const double Kp = (double)(((K + 63) / 64) * 64), Mp = (double)(((nm * nm + 127) / 128) * 128);
-        const double per_pt = 2.0 * NMT * Kp * 4.0 + 3.0 * nm3 * 4.0, per_line = Mp * Kp * 4.0 + NMT * Kp * 4.0;
+        const double per_u = Mp * Kp * 4.0, per_col = NMT * Kp * 4.0;
+        const double per_pt = 2.0 * NMT * Kp * 4.0 + 3.0 * nm3 * 4.0, per_q = 3.0 * nm * 8.0 + 4.0;
         const double budget = 12e9;
         size_t b0 = 0;
         while (b0 < axis.size()) {
+            std::vector<double> uf;
             double bytes = 0.0;
             size_t b1 = b0;
             long long pts = 0;
             while (b1 < axis.size()) {
                 const ZoneDev &z = axis[b1];
-                const double add = per_pt * z.ni * z.nj + per_line * (z.ni + z.nj);
+                size_t nu_new = 0;
+                std::vector<double> cand;
+                for (int i = 0; i < z.ni; ++i) cand.push_back(z.fi0 + i * z.dIi);
+                for (int j = 0; j < z.nj; ++j) cand.push_back(z.fj0 + j * z.dJj);
+                for (double f : cand)
+                    if (!std::binary_search(uf.begin(), uf.end(), f)) ++nu_new;
+                const double nq = (double)((z.ni - 1) * z.Fi + 1) * ((z.nj - 1) * z.Fj + 1);
+                const double add = per_u * nu_new + per_col * z.nj + per_pt * z.ni * z.nj + per_q * nq;
                 if (b1 > b0 && (bytes + add > budget || pts + (long long)z.ni * z.nj > 4000000)) break;
                 bytes += add;
                 pts += (long long)z.ni * z.nj;
+                uf.insert(uf.end(), cand.begin(), cand.end());
+                std::sort(uf.begin(), uf.end());
+                uf.erase(std::unique(uf.begin(), uf.end()), uf.end());
                 ++b1;
             }
             std::vector<ZoneDev> batch(axis.begin() + b0, axis.begin() + b1);

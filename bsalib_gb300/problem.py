@@ -379,6 +379,29 @@ def tall_building(nodes: int = 400, modes: int = 24, nfreqs: int = 513, df: floa
                      quad, (10.0, 10.0, 10.0), 1, s, rho=rho)
 
 
+def bridge_deck(nodes: int = 1200, modes: int = 60, seed: int = 77, span: float = 1200.0) -> Problem:
+    """Long-span bridge deck: `nodes` loaded nodes along `span` m, u and w turbulence
+    (I_u 0.10, I_w 0.05, L_u 100 m, L_w 40 m), uniform U = 40 m/s, `modes` modes closely
+    spaced over 0.08-1.5 Hz (log spacing with a seeded +-2 % jitter), 0.5 % damping, shapes
+    sin(n pi x / span + phase) with seeded integer wave numbers, von Karman spectra,
+    Davenport coherence C = 8 on the separation along the deck (stored as the nodes' third
+    coordinate; only separations enter).  Mesher analysis (analysis type 2)."""
+    rng = np.random.default_rng(seed)
+    x = np.arange(1, nodes + 1) * (span / nodes)
+    U = np.full(nodes, 40.0)
+    natf = np.sort(np.geomspace(0.08, 1.5, modes) * (1.0 + rng.uniform(-0.02, 0.02, modes)))
+    xsi = np.full(modes, 0.005)
+    nwave = rng.integers(1, 16, modes)
+    phase = rng.uniform(0.0, 0.5 * np.pi, modes)
+    phi = _unit_max(np.sin(nwave[None, :] * np.pi * x[:, None] / span + phase[None, :]))
+    rho, CdA = 1.22, 4.0
+    lin = np.zeros((3, nodes)); lin[0] = rho * CdA * U; lin[2] = 0.5 * rho * CdA * U
+    quad = np.zeros((3, nodes)); quad[0] = 0.5 * rho * CdA; quad[2] = 0.125 * rho * CdA
+    s = Settings(suban=2, nfreqs=65, df=1.5 / 32, tc=(1, 3), test=1)
+    return _assemble(x, U, 0.10 * U, 0.07 * U, 0.05 * U, 100.0, 60.0, 40.0, phi, natf, xsi, lin,
+                     quad, (8.0, 8.0, 8.0), 1, s, rho=rho)
+
+
 def random_structure(seed: int, nodes=(30, 600), modes=(4, 40), nfreq_grid=(129, 513),
                      U_mean: Optional[float] = None) -> Problem:
     """A seeded random cantilever (parametric sweeps): nodes uniform in `nodes`, modes

@@ -1,0 +1,57 @@
+"""Run the Mesher analysis (zone layout + zone integration) of a structure a few times.
+
+  python -m bsalib_gb300.profile_mesher [--structure bridge|building|tower] [--nodes N]
+                                        [--modes M] [--precision bf16x3|fp64] [--steps 2]
+
+Prints the zone and lattice-point counts and, per run, the library statistics and the
+response-bispectrum (BRM lattice) points per second.
+"""
+import argparse
+
+from . import api, build
+from .problem import bridge_deck, cantilever_tower, tall_building
+
+
+def make(a):
+    if a.structure == "bridge":
+        return bridge_deck(nodes=a.nodes or 1200, modes=a.modes or 60)
+    if a.structure == "building":
+        p = tall_building(nodes=a.nodes or 400, modes=a.modes or 24, nfreqs=65, df=0.0625)
+    else:
+        p = cantilever_tower(nodes=a.nodes or 30)
+    p.settings.suban = 2
+    return p
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--structure", default="bridge", choices=["bridge", "building", "tower"])
+    ap.add_argument("--nodes", type=int, default=0)
+    ap.add_argument("--modes", type=int, default=0)
+    ap.add_argument("--precision", default="bf16x3", choices=["bf16x3", "fp64"])
+    ap.add_argument("--steps", type=int, default=2)
+    ap.add_argument("--zones-only", action="store_true")
+    a = ap.parse_args()
+    build.build()
+    prob = make(a)
+    prec = api.PREC_BF16X3 if a.precision == "bf16x3" else api.PREC_FP64
+    s = api.BsaSession(prob, precision=prec)
+    try:
+        zs = s.generate_zones()
+        nbfm = sum(z.ni * z.nj for z in zs)
+        nbrm = sum(((z.ni - 1) * z.Fi + 1) * ((z.nj - 1) * z.Fj + 1) for z in zs)
+        print(f"{a.structure}: {prob.nnl} nodes, {s.nmodes()} modes, {len(zs)} zones, "
+              f"{nbfm} BFM points, {nbrm} BRM points", flush=True)
+        if a.zones_only:
+            return
+        for _ in range(a.steps):
+            s.run()
+            st = s.stats()
+            print(f"  {st.ms_total:.1f} ms total, {st.ms_gemm:.1f} ms contraction kernel, {st.kernels} kernels, "
+                  f"{st.points / (st.ms_total * 1e-3):.4g} BRM pts/s", flush=True)
+    finally:
+        s.close()
+
+
+if __name__ == "__main__":
+    main()
