@@ -311,7 +311,7 @@ __global__ void __launch_bounds__(192, 1)
 }
 
 // ------------------------------------------------------------------------------------
-// Operand preparation (FP64 -> bf16 hi/lo).
+// Operand preparation (FP32 -> bf16 hi/lo; the U products Q A formed in FP32).
 // ------------------------------------------------------------------------------------
 
 // U[(r*Mp + a*nm + b)][k] = Q[k][a] * A(f_r)[k][b]   (rows >= nm^2 and k >= K are zero).
@@ -319,12 +319,12 @@ __global__ void __launch_bounds__(192, 1)
 __global__ void k_prep_u(int nm, int K, int Kp, int Mp, const float *__restrict__ A, const double *__restrict__ Q,
                          __nv_bfloat16 *__restrict__ Uh, __nv_bfloat16 *__restrict__ Ul) {
     const int r = blockIdx.x, k0 = blockIdx.y * 64;
-    __shared__ double As[64][33], Qs[64][33];
+    __shared__ float As[64][33], Qs[64][33];
     const float *Ar = A + (size_t)r * K * nm;
     for (int e = threadIdx.x; e < 64 * nm; e += blockDim.x) {
         const int kk = e / nm, m = e % nm, k = k0 + kk;
-        As[kk][m] = k < K ? (double)Ar[(size_t)k * nm + m] : 0.0;
-        Qs[kk][m] = k < K ? Q[(size_t)k * nm + m] : 0.0;
+        As[kk][m] = k < K ? Ar[(size_t)k * nm + m] : 0.f;
+        Qs[kk][m] = k < K ? (float)Q[(size_t)k * nm + m] : 0.f;
     }
     __syncthreads();
     const int nm2 = nm * nm;
@@ -333,8 +333,8 @@ __global__ void k_prep_u(int nm, int K, int Kp, int Mp, const float *__restrict_
         __align__(16) __nv_bfloat16 hi[8], lo[8];
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
-            const double u = row < nm2 ? Qs[kv + q][row / nm] * As[kv + q][row % nm] : 0.0;
-            split_bf16(u, hi[q], lo[q]);
+            const float u = row < nm2 ? Qs[kv + q][row / nm] * As[kv + q][row % nm] : 0.f;
+            split_bf16f(u, hi[q], lo[q]);
         }
         const size_t o = ((size_t)r * Mp + row) * Kp + k0 + kv;
         *(uint4 *)(Uh + o) = *(const uint4 *)hi;
@@ -365,7 +365,7 @@ __global__ void k_prep_b(int nm, int NMT, int K, int Kp, int nf, int n_pad, int 
         const int j = e >> 3, kv = (e & 7) * 8;
         __align__(16) __nv_bfloat16 hi[8], lo[8];
 #pragma unroll
-        for (int q = 0; q < 8; ++q) split_bf16(j < nm ? (double)As[kv + q][j] : 0.0, hi[q], lo[q]);
+        for (int q = 0; q < 8; ++q) split_bf16f(j < nm ? As[kv + q][j] : 0.f, hi[q], lo[q]);
         const size_t o = ((size_t)t * NMT + j) * Kp + k0 + kv;
         *(uint4 *)(Th + o) = *(const uint4 *)hi;
         *(uint4 *)(Tl + o) = *(const uint4 *)lo;

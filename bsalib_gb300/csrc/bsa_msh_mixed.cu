@@ -260,12 +260,12 @@ __global__ void k_prep_u_rows(int nm, int K, int Kp, int Mp, const int *__restri
                               const double *__restrict__ Q, __nv_bfloat16 *__restrict__ Uh,
                               __nv_bfloat16 *__restrict__ Ul) {
     const int r = blockIdx.x, k0 = blockIdx.y * 32;
-    __shared__ double As[32][65], Qs[32][65];
+    __shared__ float As[32][65], Qs[32][65];
     const float *Ar = A + (size_t)src[r] * K * nm;
     for (int e = threadIdx.x; e < 32 * nm; e += blockDim.x) {
         const int kk = e / nm, m = e % nm, k = k0 + kk;
-        As[kk][m] = k < K ? (double)Ar[(size_t)k * nm + m] : 0.0;
-        Qs[kk][m] = k < K ? Q[(size_t)k * nm + m] : 0.0;
+        As[kk][m] = k < K ? Ar[(size_t)k * nm + m] : 0.f;
+        Qs[kk][m] = k < K ? (float)Q[(size_t)k * nm + m] : 0.f;
     }
     __syncthreads();
     const int nm2 = nm * nm;
@@ -274,8 +274,8 @@ __global__ void k_prep_u_rows(int nm, int K, int Kp, int Mp, const int *__restri
         __align__(16) __nv_bfloat16 hi[8], lo[8];
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
-            const double u = row < nm2 ? Qs[kv + q][row / nm] * As[kv + q][row % nm] : 0.0;
-            split_bf16(u, hi[q], lo[q]);
+            const float u = row < nm2 ? Qs[kv + q][row / nm] * As[kv + q][row % nm] : 0.f;
+            split_bf16f(u, hi[q], lo[q]);
         }
         const size_t o = ((size_t)r * Mp + row) * Kp + k0 + kv;
         *(uint4 *)(Uh + o) = *(const uint4 *)hi;
@@ -298,7 +298,7 @@ __global__ void k_prep_b_rows(int nm, int NMT, int K, int Kp, const int *__restr
         const int j = e >> 3, kv = (e & 7) * 8;
         __align__(16) __nv_bfloat16 hi[8], lo[8];
 #pragma unroll
-        for (int q = 0; q < 8; ++q) split_bf16(j < nm ? (double)As[kv + q][j] : 0.0, hi[q], lo[q]);
+        for (int q = 0; q < 8; ++q) split_bf16f(j < nm ? As[kv + q][j] : 0.f, hi[q], lo[q]);
         const size_t o = ((size_t)t * NMT + j) * Kp + k0 + kv;
         *(uint4 *)(Th + o) = *(const uint4 *)hi;
         *(uint4 *)(Tl + o) = *(const uint4 *)lo;
@@ -356,23 +356,20 @@ constexpr int kQB = 24;  // BRM points per shared-memory round
 // cells g, g + G, ...  Each BRM point belongs to the cell (min(qi/Fi, ni-2), min(qj/Fj, nj-2))
 // and each BFM point to the cell (min(i, ni-2), min(j, nj-2)), so every lattice point is
 // counted once.  part[g][6][nm^3]: m3mf of T1, T3, T2, then m3mr of T1, T3, T2.
-__global__ __launch_bounds__(256) void k_msh_moments(int nm, int nz, const ZoneM *__restrict__ zones, int ncells,
+__global__ __launch_bounds__(256) void k_msh_moments(int nm, const ZoneM *__restrict__ zones,
+                                                     const int *__restrict__ cell_zone, int ncells,
                                                      const float *__restrict__ T1, const float *__restrict__ T3,
                                                      const float *__restrict__ T2, const float2 *__restrict__ Hq,
                                                      const float *__restrict__ Wq, double *__restrict__ part) {
     __shared__ float2 H[kQB][3][64];
     __shared__ float wq[kQB], tiq[kQB], tjq[kQB];
-    __shared__ int zsel;
     const int nm2 = nm * nm, nm3 = nm2 * nm;
     const int e = blockIdx.y * 256 + threadIdx.x;
     const bool ve = e < nm3;
     const int ab = ve ? e % nm2 : 0, jj = ve ? e / nm2 : 0, a = ab / nm, b = ab % nm;
     double mf[3] = {0.0, 0.0, 0.0}, mr[3] = {0.0, 0.0, 0.0};
     for (int cid = blockIdx.x; cid < ncells; cid += gridDim.x) {
-        __syncthreads();
-        if (threadIdx.x == 0) zsel = zone_of(zones, nz, cid, 0);
-        __syncthreads();
-        const ZoneM z = zones[zsel];
+        const ZoneM z = zones[cell_zone[cid]];
         const int loc = cid - z.cbase, i0 = loc / (z.nj - 1), j0 = loc % (z.nj - 1);
         const int NI = (z.ni - 1) * z.Fi, NJ = (z.nj - 1) * z.Fj;
         const int qi0 = i0 * z.Fi, qi1 = (i0 == z.ni - 2) ? NI : (i0 + 1) * z.Fi - 1;
@@ -539,12 +536,15 @@ int Engine::msh_mixed_batch(const std::vector<ZoneDev> &zs, std::vector<double> 
     for (int u = 0; u < nU; ++u) usrc[u] = F.at(UF.v[u]);
     std::vector<Task> tasks;
     std::vector<ZoneM> zm;
+    std::vector<int> cellz;
+    cellz.reserve((size_t)ncells);
     {
         long long pb = 0, cb = 0, gb = 0, qb = 0;
         for (const ZoneDev &z : zs) {
             ZoneM m{z.fi0, z.fj0, z.dIi, z.dJj, z.wI, z.wJ, z.sym, z.ni, z.nj, z.Fi, z.Fj, (int)pb, (int)cb, (int)qb};
             qb += (long long)((z.ni - 1) * z.Fi + 1) * ((z.nj - 1) * z.Fj + 1);
             zm.push_back(m);
+            cellz.insert(cellz.end(), (size_t)(z.ni - 1) * (z.nj - 1), (int)zm.size() - 1);
             for (int j = 0; j < z.nj; ++j) gsrc[gb + j] = F.at(z.fj0 + j * z.dJj);
             for (int i = 0; i < z.ni; ++i) {
                 const double r = z.fi0 + i * z.dIi;
@@ -570,7 +570,7 @@ int Engine::msh_mixed_batch(const std::vector<ZoneDev> &zs, std::vector<double> 
     if ((rc = build_atable(F.v, true))) return rc;
     const size_t uel = (size_t)nU * Mp * Kp, gel = (size_t)ncol * NMT * Kp, sel = 2 * (size_t)npts * NMT * Kp;
     const size_t tel = (size_t)npts * nm3;
-    const size_t nidx = (size_t)nU + ncol + 2 * (size_t)npts;
+    const size_t nidx = (size_t)nU + ncol + 2 * (size_t)npts + ncells;
     int dev = 0, nsm = 0;
     if ((e = cudaGetDevice(&dev)) || (e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev)))
         return cuda_fail(e, "device query");
@@ -586,14 +586,15 @@ int Engine::msh_mixed_batch(const std::vector<ZoneDev> &zs, std::vector<double> 
     __nv_bfloat16 *Gh = dMixB.as<__nv_bfloat16>(), *Gl = Gh + gel, *Sh = Gl + gel, *Sl = Sh + sel;
     float *T1 = dMshT.as<float>(), *T3 = T1 + tel, *T2 = T3 + tel;
     char *ib = (char *)dMshIdx.p;
-    int *d_usrc = (int *)ib, *d_gsrc = d_usrc + nU, *d_ssrc = d_gsrc + ncol;
-    Task *d_tasks = (Task *)(((uintptr_t)(d_ssrc + 2 * npts) + 15) & ~(uintptr_t)15);
+    int *d_usrc = (int *)ib, *d_gsrc = d_usrc + nU, *d_ssrc = d_gsrc + ncol, *d_cellz = d_ssrc + 2 * npts;
+    Task *d_tasks = (Task *)(((uintptr_t)(d_cellz + ncells) + 15) & ~(uintptr_t)15);
     ZoneM *d_zones = (ZoneM *)(((uintptr_t)(d_tasks + tasks.size()) + 15) & ~(uintptr_t)15);
     double *part = dMixPart.as<double>(), *red = part + (size_t)G * 6 * nm3;
     int *derr = (int *)(red + 2 * (size_t)nm3);
     if ((e = cudaMemcpyAsync(d_usrc, usrc.data(), nU * sizeof(int), cudaMemcpyHostToDevice, stream)) ||
         (e = cudaMemcpyAsync(d_gsrc, gsrc.data(), ncol * sizeof(int), cudaMemcpyHostToDevice, stream)) ||
         (e = cudaMemcpyAsync(d_ssrc, ssrc.data(), 2 * npts * sizeof(int), cudaMemcpyHostToDevice, stream)) ||
+        (e = cudaMemcpyAsync(d_cellz, cellz.data(), ncells * sizeof(int), cudaMemcpyHostToDevice, stream)) ||
         (e = cudaMemcpyAsync(d_tasks, tasks.data(), tasks.size() * sizeof(Task), cudaMemcpyHostToDevice, stream)) ||
         (e = cudaMemcpyAsync(d_zones, zm.data(), zm.size() * sizeof(ZoneM), cudaMemcpyHostToDevice, stream)) ||
         (e = cudaMemsetAsync(derr, 0, sizeof(int), stream)))
@@ -633,8 +634,7 @@ int Engine::msh_mixed_batch(const std::vector<ZoneDev> &zs, std::vector<double> 
         const long long nt = nbrm * 3 * nm;
         k_msh_frf<<<(unsigned)((nt + 255) / 256), 256, 0, stream>>>(nm, (int)zm.size(), d_zones, (int)nbrm, frf(), Hq, Wq);
     }
-    k_msh_moments<<<dim3(G, nchunks), 256, 0, stream>>>(nm, (int)zm.size(), d_zones, (int)ncells, T1, T3, T2, Hq, Wq,
-                                                         part);
+    k_msh_moments<<<dim3(G, nchunks), 256, 0, stream>>>(nm, d_zones, d_cellz, (int)ncells, T1, T3, T2, Hq, Wq, part);
     k_msh_reduce<<<(nm3 + 127) / 128, 128, 0, stream>>>(nm, G, part, red, red + nm3);
     if ((e = cudaGetLastError())) return cuda_fail(e, "Mesher zone integration");
     kernels += 4;

@@ -112,6 +112,11 @@ __device__ __forceinline__ void split_bf16(double u, __nv_bfloat16 &hi, __nv_bfl
     hi = __double2bfloat16(u);
     lo = __double2bfloat16(u - (double)__bfloat162float(hi));
 }
+// The same split of an FP32 value (u - hi is exact in FP32: hi is u rounded to 8 bits).
+__device__ __forceinline__ void split_bf16f(float u, __nv_bfloat16 &hi, __nv_bfloat16 &lo) {
+    hi = __float2bfloat16_rn(u);
+    lo = __float2bfloat16_rn(u - __bfloat162float(hi));
+}
 
 typedef CUresult (*EncodeTiled)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
                                 const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
