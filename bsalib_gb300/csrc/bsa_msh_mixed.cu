@@ -351,11 +351,13 @@ __global__ void k_msh_frf(int nm, int nz, const ZoneM *__restrict__ zones, int n
 }
 
 constexpr int kQB = 24;  // BRM points per shared-memory round
+constexpr int kEPT = 2;  // term-tensor elements per thread
 
-// Block (g, chunk): elements e = chunk*256 + t of the term tensors (e = j'*nm^2 + a*nm + b),
-// cells g, g + G, ...  Each BRM point belongs to the cell (min(qi/Fi, ni-2), min(qj/Fj, nj-2))
-// and each BFM point to the cell (min(i, ni-2), min(j, nj-2)), so every lattice point is
-// counted once.  part[g][6][nm^3]: m3mf of T1, T3, T2, then m3mr of T1, T3, T2.
+// Block (g, chunk): elements e = chunk*512 + t + 256 u (u < 2) of the term tensors
+// (e = j'*nm^2 + a*nm + b), cells g, g + G, ...  Each BRM point belongs to the cell
+// (min(qi/Fi, ni-2), min(qj/Fj, nj-2)) and each BFM point to the cell (min(i, ni-2),
+// min(j, nj-2)), so every lattice point is counted once.  part[g][6][nm^3]: m3mf of T1, T3,
+// T2, then m3mr of T1, T3, T2.
 __global__ __launch_bounds__(256) void k_msh_moments(int nm, const ZoneM *__restrict__ zones,
                                                      const int *__restrict__ cell_zone, int ncells,
                                                      const float *__restrict__ T1, const float *__restrict__ T3,
@@ -364,44 +366,64 @@ __global__ __launch_bounds__(256) void k_msh_moments(int nm, const ZoneM *__rest
     __shared__ float2 H[kQB][3][64];
     __shared__ float wq[kQB], tiq[kQB], tjq[kQB];
     const int nm2 = nm * nm, nm3 = nm2 * nm;
-    const int e = blockIdx.y * 256 + threadIdx.x;
-    const bool ve = e < nm3;
-    const int ab = ve ? e % nm2 : 0, jj = ve ? e / nm2 : 0, a = ab / nm, b = ab % nm;
-    double mf[3] = {0.0, 0.0, 0.0}, mr[3] = {0.0, 0.0, 0.0};
+    int ev[kEPT], ia[kEPT], ib[kEPT], ij[kEPT];
+#pragma unroll
+    for (int u = 0; u < kEPT; ++u) {
+        ev[u] = blockIdx.y * (256 * kEPT) + threadIdx.x + 256 * u;
+        const int e = ev[u] < nm3 ? ev[u] : 0, ab = e % nm2;
+        ij[u] = e / nm2;
+        ia[u] = ab / nm;
+        ib[u] = ab % nm;
+    }
+    double mf[kEPT][3], mr[kEPT][3];
+#pragma unroll
+    for (int u = 0; u < kEPT; ++u)
+#pragma unroll
+        for (int t = 0; t < 3; ++t) mf[u][t] = mr[u][t] = 0.0;
+    const float *Ts[3] = {T1, T3, T2};
     for (int cid = blockIdx.x; cid < ncells; cid += gridDim.x) {
         const ZoneM z = zones[cell_zone[cid]];
         const int loc = cid - z.cbase, i0 = loc / (z.nj - 1), j0 = loc % (z.nj - 1);
-        const int NI = (z.ni - 1) * z.Fi, NJ = (z.nj - 1) * z.Fj;
+        const int NJ = (z.nj - 1) * z.Fj, NI = (z.ni - 1) * z.Fi;
         const int qi0 = i0 * z.Fi, qi1 = (i0 == z.ni - 2) ? NI : (i0 + 1) * z.Fi - 1;
         const int qj0 = j0 * z.Fj, qj1 = (j0 == z.nj - 2) ? NJ : (j0 + 1) * z.Fj - 1;
         const int nqj = qj1 - qj0 + 1, nq = (qi1 - qi0 + 1) * nqj;
         const float rFi = 1.f / (float)z.Fi, rFj = 1.f / (float)z.Fj;
         const size_t P00 = (size_t)z.pbase + (size_t)i0 * z.nj + j0, P01 = P00 + 1, P10 = P00 + z.nj, P11 = P10 + 1;
-        float c[3][4];
-        if (ve) {
-            const float *Ts[3] = {T1, T3, T2};
-#pragma unroll
-            for (int t = 0; t < 3; ++t) {
-                c[t][0] = Ts[t][P00 * nm3 + e];
-                c[t][1] = Ts[t][P01 * nm3 + e];
-                c[t][2] = Ts[t][P10 * nm3 + e];
-                c[t][3] = Ts[t][P11 * nm3 + e];
-            }
-            // BFM lattice trapezoid (m3mf): the BFM points this cell owns
-            const double wb = z.sym * z.wI * z.wJ;
-            const int corner_i[4] = {i0, i0, i0 + 1, i0 + 1}, corner_j[4] = {j0, j0 + 1, j0, j0 + 1};
+        // corner values of the three term tensors, and the BFM lattice trapezoid (m3mf) of
+        // the BFM points this cell owns
+        float c[kEPT][3][4];
+        const double wb = z.sym * z.wI * z.wJ;
+        double wp[4];
+        {
+            const int ci[4] = {i0, i0, i0 + 1, i0 + 1}, cj[4] = {j0, j0 + 1, j0, j0 + 1};
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
-                const int ii = corner_i[k], jc = corner_j[k];
-                const bool own = (ii == i0 || i0 == z.ni - 2) && (jc == j0 || j0 == z.nj - 2);
-                if (!own) continue;
-                const double ti = (ii == 0 || ii == z.ni - 1) ? 0.5 : 1.0, tj = (jc == 0 || jc == z.nj - 1) ? 0.5 : 1.0;
-                const double wp = wb * ti * tj;
-#pragma unroll
-                for (int t = 0; t < 3; ++t) mf[t] += wp * (double)c[t][k];
+                const bool own = (ci[k] == i0 || i0 == z.ni - 2) && (cj[k] == j0 || j0 == z.nj - 2);
+                const double ti = (ci[k] == 0 || ci[k] == z.ni - 1) ? 0.5 : 1.0;
+                const double tj = (cj[k] == 0 || cj[k] == z.nj - 1) ? 0.5 : 1.0;
+                wp[k] = own ? wb * ti * tj : 0.0;
             }
         }
-        float sr[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+        for (int u = 0; u < kEPT; ++u) {
+            const bool ve = ev[u] < nm3;
+            const size_t e = ve ? (size_t)ev[u] : 0;
+#pragma unroll
+            for (int t = 0; t < 3; ++t) {
+                c[u][t][0] = ve ? Ts[t][P00 * nm3 + e] : 0.f;
+                c[u][t][1] = ve ? Ts[t][P01 * nm3 + e] : 0.f;
+                c[u][t][2] = ve ? Ts[t][P10 * nm3 + e] : 0.f;
+                c[u][t][3] = ve ? Ts[t][P11 * nm3 + e] : 0.f;
+#pragma unroll
+                for (int k = 0; k < 4; ++k) mf[u][t] += wp[k] * (double)c[u][t][k];
+            }
+        }
+        float sr[kEPT][3];
+#pragma unroll
+        for (int u = 0; u < kEPT; ++u)
+#pragma unroll
+            for (int t = 0; t < 3; ++t) sr[u][t] = 0.f;
         for (int q0 = 0; q0 < nq; q0 += kQB) {
             const int nb = min(kQB, nq - q0);
             __syncthreads();
@@ -418,35 +440,43 @@ __global__ __launch_bounds__(256) void k_msh_moments(int nm, const ZoneM *__rest
                 tjq[ql] = (float)(qj - j0 * z.Fj) * rFj;
             }
             __syncthreads();
-            if (!ve) continue;
             for (int ql = 0; ql < nb; ++ql) {
                 const float ti = tiq[ql], tj = tjq[ql], w = wq[ql];
-                const float2 h1a = H[ql][0][a], h1j = H[ql][0][jj];
-                const float2 h2a = H[ql][1][a], h2b = H[ql][1][b];
-                const float2 h3a = H[ql][2][a], h3b = H[ql][2][b], h3j = H[ql][2][jj];
-                // Re[x y conj(z)] = (x.re y.re - x.im y.im) z.re + (x.re y.im + x.im y.re) z.im
-                const float f1 = (h1a.x * h2b.x - h1a.y * h2b.y) * h3j.x + (h1a.x * h2b.y + h1a.y * h2b.x) * h3j.y;
-                const float f3 = (h1j.x * h2b.x - h1j.y * h2b.y) * h3a.x + (h1j.x * h2b.y + h1j.y * h2b.x) * h3a.y;
-                const float f2 = (h1j.x * h2a.x - h1j.y * h2a.y) * h3b.x + (h1j.x * h2a.y + h1j.y * h2a.x) * h3b.y;
-                const float fs[3] = {f1, f3, f2};
 #pragma unroll
-                for (int t = 0; t < 3; ++t) {
-                    const float left = c[t][0] * (1.f - tj) + c[t][1] * tj;
-                    const float right = c[t][2] * (1.f - tj) + c[t][3] * tj;
-                    const float v = left * (1.f - ti) + right * ti;
-                    sr[t] = fmaf(w * fs[t], v, sr[t]);
+                for (int u = 0; u < kEPT; ++u) {
+                    const int a = ia[u], b = ib[u], jj = ij[u];
+                    const float2 h1a = H[ql][0][a], h1j = H[ql][0][jj];
+                    const float2 h2a = H[ql][1][a], h2b = H[ql][1][b];
+                    const float2 h3a = H[ql][2][a], h3b = H[ql][2][b], h3j = H[ql][2][jj];
+                    // Re[x y conj(z)] = (x.re y.re - x.im y.im) z.re + (x.re y.im + x.im y.re) z.im
+                    const float f1 = (h1a.x * h2b.x - h1a.y * h2b.y) * h3j.x + (h1a.x * h2b.y + h1a.y * h2b.x) * h3j.y;
+                    const float f3 = (h1j.x * h2b.x - h1j.y * h2b.y) * h3a.x + (h1j.x * h2b.y + h1j.y * h2b.x) * h3a.y;
+                    const float f2 = (h1j.x * h2a.x - h1j.y * h2a.y) * h3b.x + (h1j.x * h2a.y + h1j.y * h2a.x) * h3b.y;
+                    const float fs[3] = {f1, f3, f2};
+#pragma unroll
+                    for (int t = 0; t < 3; ++t) {
+                        const float left = c[u][t][0] * (1.f - tj) + c[u][t][1] * tj;
+                        const float right = c[u][t][2] * (1.f - tj) + c[u][t][3] * tj;
+                        const float v = left * (1.f - ti) + right * ti;
+                        sr[u][t] = fmaf(w * fs[t], v, sr[u][t]);
+                    }
                 }
             }
         }
 #pragma unroll
-        for (int t = 0; t < 3; ++t) mr[t] += (double)sr[t];
+        for (int u = 0; u < kEPT; ++u)
+#pragma unroll
+            for (int t = 0; t < 3; ++t) mr[u][t] += (double)sr[u][t];
     }
-    if (!ve) return;
     double *pg = part + (size_t)blockIdx.x * 6 * nm3;
 #pragma unroll
-    for (int t = 0; t < 3; ++t) {
-        pg[(size_t)t * nm3 + e] = mf[t];
-        pg[(size_t)(3 + t) * nm3 + e] = mr[t];
+    for (int u = 0; u < kEPT; ++u) {
+        if (ev[u] >= nm3) continue;
+#pragma unroll
+        for (int t = 0; t < 3; ++t) {
+            pg[(size_t)t * nm3 + ev[u]] = mf[u][t];
+            pg[(size_t)(3 + t) * nm3 + ev[u]] = mr[u][t];
+        }
     }
 }
 
@@ -574,7 +604,7 @@ int Engine::msh_mixed_batch(const std::vector<ZoneDev> &zs, std::vector<double> 
     int dev = 0, nsm = 0;
     if ((e = cudaGetDevice(&dev)) || (e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev)))
         return cuda_fail(e, "device query");
-    const int nchunks = (nm3 + 255) / 256;
+    const int nchunks = (nm3 + 256 * kEPT - 1) / (256 * kEPT);
     const int G = (int)std::max(1LL, std::min((long long)(4 * nsm + nchunks - 1) / nchunks, ncells));
     if ((e = dMixA.reserve(2 * uel * 2)) || (e = dMixB.reserve(2 * (gel + sel) * 2)) ||
         (e = dMshT.reserve(3 * tel * sizeof(float))) ||
