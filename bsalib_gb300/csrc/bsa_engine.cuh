@@ -6,6 +6,7 @@
 #include <string>
 #include <vector>
 
+#include "../../include/bsa_gpu.h"
 #include "bsa_common.cuh"
 
 namespace bsa {
@@ -121,15 +122,19 @@ struct Engine {
                    const int *zj = nullptr);
     int run_zones(const std::vector<ZoneDev> &zones, double *m3mf, double *m3mr, double *npts);
     int run_zones_fp64(const std::vector<ZoneDev> &zones, double *m3mf, double *m3mr, double *npts);
-    int run_zones_mixed(const std::vector<ZoneDev> &zones, double *m3mf, double *m3mr, double *npts);
+    int run_zones_mixed(const std::vector<ZoneDev> &zones, double *m3mf, double *m3mr, double *npts,
+                        double *zdiag = nullptr);
     int msh_mixed_batch(const std::vector<ZoneDev> &zones, std::vector<double> &accF, std::vector<double> &accR,
-                        float &ms_gemm, float &ms_all);
+                        float &ms_gemm, float &ms_all, double *zdiag);
     int mesher_zones(std::vector<ZoneDev> &zones, std::vector<int> &policy);
     int run_mesher(double *m3mf, double *m3mr);
     int br_decomp(const double *m2mf, double *bkg, double *res);
 };
 
 Engine &eng();
+
+// A zone of the C-ABI as the device zone record (lattice steps in rad/s for the weights).
+ZoneDev zone_from_abi(const bsa_zone &z);
 
 // Host vector -> device buffer on the engine's stream (counted in the H2D statistics).
 template <class T>

@@ -217,6 +217,15 @@ int Engine::run_zones_fp64(const std::vector<ZoneDev> &zones, double *m3mf, doub
     return BSA_OK;
 }
 
+ZoneDev zone_from_abi(const bsa_zone &z) {
+    ZoneDev d;
+    d.fi0 = z.fi0; d.fj0 = z.fj0; d.dIi = z.dIi; d.dIj = z.dIj; d.dJi = z.dJi; d.dJj = z.dJj;
+    d.ni = z.ni; d.nj = z.nj; d.Fi = z.Fi; d.Fj = z.Fj; d.sym = z.sym;
+    d.wI = std::sqrt(z.dIi * z.dIi + z.dIj * z.dIj) * kPi2;
+    d.wJ = std::sqrt(z.dJi * z.dJi + z.dJj * z.dJj) * kPi2;
+    return d;
+}
+
 int Engine::run_mesher(double *m3mf, double *m3mr) {
     std::vector<ZoneDev> zones;
     std::vector<int> pol;
@@ -236,14 +245,7 @@ int bsa_gpu_mshZones(const bsa_zone *zones, int nz, double *m3mf, double *m3mr, 
     if (E.halted) return BSA_ERR_STATE;
     if (!zones || nz <= 0) return E.fail(BSA_ERR_ARG, "empty zone list");
     std::vector<bsa::ZoneDev> zd(nz);
-    for (int k = 0; k < nz; ++k) {
-        const bsa_zone &z = zones[k];
-        bsa::ZoneDev &d = zd[k];
-        d.fi0 = z.fi0; d.fj0 = z.fj0; d.dIi = z.dIi; d.dIj = z.dIj; d.dJi = z.dJi; d.dJj = z.dJj;
-        d.ni = z.ni; d.nj = z.nj; d.Fi = z.Fi; d.Fj = z.Fj; d.sym = z.sym;
-        d.wI = std::sqrt(z.dIi * z.dIi + z.dIj * z.dIj) * bsa::kPi2;
-        d.wJ = std::sqrt(z.dJi * z.dJi + z.dJj * z.dJj) * bsa::kPi2;
-    }
+    for (int k = 0; k < nz; ++k) zd[k] = bsa::zone_from_abi(zones[k]);
     return E.run_zones(zd, m3mf, m3mr, npts);
 }
 

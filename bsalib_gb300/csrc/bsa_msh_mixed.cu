@@ -480,6 +480,48 @@ __global__ __launch_bounds__(256) void k_msh_moments(int nm, const ZoneM *__rest
     }
 }
 
+// Per-zone mode-diagonal response moments m3mr(m, m, m) of the zone alone (the refinement
+// criterion's quantity): one block per zone, threads over its BRM points, the three terms
+// summed at element (m, m, m) before the FRF (the same FRF for all three there).
+__global__ void k_msh_zone_diag(int nm, const ZoneM *__restrict__ zones, const float *__restrict__ T1,
+                                const float *__restrict__ T3, const float *__restrict__ T2,
+                                const float2 *__restrict__ Hq, const float *__restrict__ Wq,
+                                double *__restrict__ zdiag) {
+    const ZoneM z = zones[blockIdx.x];
+    const int nm2 = nm * nm, nm3 = nm2 * nm;
+    const int NI = (z.ni - 1) * z.Fi, NJ = (z.nj - 1) * z.Fj, nq = (NI + 1) * (NJ + 1);
+    __shared__ double red[256];
+    for (int m = 0; m < nm; ++m) {
+        const size_t em = (size_t)m * nm2 + (size_t)m * nm + m;
+        double s = 0.0;
+        for (int q = threadIdx.x; q < nq; q += blockDim.x) {
+            const int qi = q / (NJ + 1), qj = q % (NJ + 1);
+            const int i0 = min(qi / z.Fi, z.ni - 2), j0 = min(qj / z.Fj, z.nj - 2);
+            const float ti = (float)(qi - i0 * z.Fi) / (float)z.Fi, tj = (float)(qj - j0 * z.Fj) / (float)z.Fj;
+            const size_t P00 = (size_t)z.pbase + (size_t)i0 * z.nj + j0, P01 = P00 + 1, P10 = P00 + z.nj,
+                         P11 = P10 + 1;
+            float c[4];
+            const size_t P[4] = {P00, P01, P10, P11};
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                c[k] = T1[P[k] * nm3 + em] + T3[P[k] * nm3 + em] + T2[P[k] * nm3 + em];
+            const float v = (c[0] * (1.f - tj) + c[1] * tj) * (1.f - ti) + (c[2] * (1.f - tj) + c[3] * tj) * ti;
+            const size_t gq = (size_t)z.qbase + q;
+            const float2 h1 = Hq[gq * 3 * nm + m], h2 = Hq[gq * 3 * nm + nm + m], h3 = Hq[gq * 3 * nm + 2 * nm + m];
+            const float F = (h1.x * h2.x - h1.y * h2.y) * h3.x + (h1.x * h2.y + h1.y * h2.x) * h3.y;
+            s += (double)(Wq[gq] * F * v);
+        }
+        red[threadIdx.x] = s;
+        __syncthreads();
+        for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+            if ((int)threadIdx.x < h) red[threadIdx.x] += red[threadIdx.x + h];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) zdiag[(size_t)blockIdx.x * nm + m] = 2.0 * red[0];
+        __syncthreads();
+    }
+}
+
 // m3[m + nm n + nm^2 o] = 2 sum_g (T1 at (a,b,j') = (m,n,o) + T3 at (o,n,m) + T2 at (n,o,m)).
 __global__ void k_msh_reduce(int nm, int G, const double *__restrict__ part, double *__restrict__ m3mf,
                              double *__restrict__ m3mr) {
@@ -535,7 +577,7 @@ struct FreqIndex {
 }  // namespace
 
 int Engine::msh_mixed_batch(const std::vector<ZoneDev> &zs, std::vector<double> &accF, std::vector<double> &accR,
-                            float &ms_gemm, float &ms_all) {
+                            float &ms_gemm, float &ms_all, double *zdiag) {
     using namespace mshmix;
     const int nm = nme, nm2 = nm * nm, nm3 = nm2 * nm;
     const int NMT = ((nm + 7) / 8) * 8, NC = kBN / NMT, BROWS = NC * NMT;
@@ -610,7 +652,8 @@ int Engine::msh_mixed_batch(const std::vector<ZoneDev> &zs, std::vector<double> 
         (e = dMshT.reserve(3 * tel * sizeof(float))) ||
         (e = dMshIdx.reserve(nidx * sizeof(int) + tasks.size() * sizeof(Task) + zm.size() * sizeof(ZoneM) + 64)) ||
         (e = dMixPart.reserve((size_t)G * 6 * nm3 * sizeof(double) + 2 * (size_t)nm3 * sizeof(double) + 256)) ||
-        (e = dMixH.reserve((size_t)nbrm * 3 * nm * sizeof(float2) + (size_t)nbrm * sizeof(float) + 256)))
+        (e = dMixH.reserve((size_t)nbrm * 3 * nm * sizeof(float2) + (size_t)nbrm * sizeof(float) + 256 +
+                           (zdiag ? zm.size() * nm * sizeof(double) : 0))))
         return cuda_fail(e, "allocating Mesher BF16x3 operands");
     __nv_bfloat16 *Uh = dMixA.as<__nv_bfloat16>(), *Ul = Uh + uel;
     __nv_bfloat16 *Gh = dMixB.as<__nv_bfloat16>(), *Gl = Gh + gel, *Sh = Gl + gel, *Sl = Sh + sel;
@@ -666,12 +709,20 @@ int Engine::msh_mixed_batch(const std::vector<ZoneDev> &zs, std::vector<double> 
     }
     k_msh_moments<<<dim3(G, nchunks), 256, 0, stream>>>(nm, d_zones, d_cellz, (int)ncells, T1, T3, T2, Hq, Wq, part);
     k_msh_reduce<<<(nm3 + 127) / 128, 128, 0, stream>>>(nm, G, part, red, red + nm3);
+    double *d_zdiag = nullptr;
+    if (zdiag) {
+        d_zdiag = (double *)(((uintptr_t)(Wq + nbrm) + 255) & ~(uintptr_t)255);
+        k_msh_zone_diag<<<(unsigned)zm.size(), 256, 0, stream>>>(nm, d_zones, T1, T3, T2, Hq, Wq, d_zdiag);
+        kernels += 1;
+    }
     if ((e = cudaGetLastError())) return cuda_fail(e, "Mesher zone integration");
     kernels += 4;
     std::vector<double> h(2 * (size_t)nm3);
     int herr = 0;
     if ((e = cudaMemcpyAsync(h.data(), red, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, stream)) ||
         (e = cudaMemcpyAsync(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost, stream)) ||
+        (zdiag && (e = cudaMemcpyAsync(zdiag, d_zdiag, sizeof(double) * zm.size() * nm, cudaMemcpyDeviceToHost,
+                                       stream))) ||
         (e = cudaEventRecord(ev1, stream)) || (e = cudaStreamSynchronize(stream)))
         return cuda_fail(e, "Mesher BF16x3 evaluation");
     d2h += (double)sizeof(double) * h.size() + sizeof(int);
@@ -690,7 +741,8 @@ int Engine::msh_mixed_batch(const std::vector<ZoneDev> &zs, std::vector<double> 
 
 // Zones in the split precision: axis-aligned zones in batches through the tensor cores,
 // rotated ones through the FP64 point kernel.
-int Engine::run_zones_mixed(const std::vector<ZoneDev> &zones, double *m3mf, double *m3mr, double *npts) {
+int Engine::run_zones_mixed(const std::vector<ZoneDev> &zones, double *m3mf, double *m3mr, double *npts,
+                            double *zdiag) {
     int rc = upload_problem();
     if (rc) return rc;
     const int nm = nme;
@@ -706,6 +758,7 @@ int Engine::run_zones_mixed(const std::vector<ZoneDev> &zones, double *m3mf, dou
         nbfm += (double)z.ni * z.nj;
         nbrm += (double)((z.ni - 1) * z.Fi + 1) * ((z.nj - 1) * z.Fj + 1);
     }
+    if (zdiag && !rot.empty()) return fail(BSA_ERR_UNSUPPORTED, "per-zone moments need axis-aligned zones");
     std::vector<double> accF(nm3, 0.0), accR(nm3, 0.0);
     float ms_gemm = 0.f, ms_all = 0.f;
     int nk = 0;
@@ -756,7 +809,8 @@ int Engine::run_zones_mixed(const std::vector<ZoneDev> &zones, double *m3mf, dou
                 ++b1;
             }
             std::vector<ZoneDev> batch(axis.begin() + b0, axis.begin() + b1);
-            if ((rc = msh_mixed_batch(batch, accF, accR, ms_gemm, ms_all))) return rc;
+            if ((rc = msh_mixed_batch(batch, accF, accR, ms_gemm, ms_all, zdiag ? zdiag + b0 * nm : nullptr)))
+                return rc;
             b0 = b1;
         }
     }
@@ -777,3 +831,16 @@ int Engine::run_zones_mixed(const std::vector<ZoneDev> &zones, double *m3mf, dou
 }
 
 }  // namespace bsa
+
+using bsa::eng;
+
+extern "C" int bsa_gpu_mshZonesDiag(const bsa_zone *zones, int nz, double *m3mf, double *m3mr, double *zdiag) {
+    bsa::Engine &E = eng();
+    if (E.halted) return BSA_ERR_STATE;
+    if (!zones || nz <= 0 || !zdiag) return E.fail(BSA_ERR_ARG, "empty zone list or no per-zone output");
+    if (E.precision != BSA_PREC_BF16X3 || E.set.onlyd)
+        return E.fail(BSA_ERR_UNSUPPORTED, "per-zone moments are produced by the split-precision zone path");
+    std::vector<bsa::ZoneDev> zd(nz);
+    for (int k = 0; k < nz; ++k) zd[k] = bsa::zone_from_abi(zones[k]);
+    return E.run_zones_mixed(zd, m3mf, m3mr, nullptr, zdiag);
+}

@@ -251,6 +251,13 @@ typedef struct {
  * npts (optional, 2 doubles): BFM and BRM lattice point counts. */
 int bsa_gpu_mshZones(const bsa_zone *zones, int nz, double *m3mf, double *m3mr, double *npts);
 
+/* bsa_gpu_mshZones in the split precision, plus each zone's own mode-diagonal response
+ * moments zdiag[z * nm + m] = m3mr(m, m, m) of zone z (the quantity the zone-refinement
+ * criterion compares between lattice levels).  Needs bsa_gpu_setPrecision(BSA_PREC_BF16X3)
+ * and axis-aligned zones; no counterpart in the reference (its zones are not refined by an
+ * error criterion). */
+int bsa_gpu_mshZonesDiag(const bsa_zone *zones, int nz, double *m3mf, double *m3mr, double *zdiag);
+
 /* The zone layout the Mesher analysis (bsa_Run with analysis type 2) evaluates: restates
  * prefetchZoneLimits_ (BsaMesherImpl.F90:1638-1859) and the background peak zone of
  * PreMesh (:266-420), and lays rectangular zones over those limits on both axes.  Writes
