@@ -65,7 +65,7 @@ def load(path: Optional[str] = None):
     lib = C.CDLL(p)
     vp, i, d = C.c_void_p, C.c_int, C.c_double
     sig = {
-        "bsa_Init": [], "bsa_Finalise": [], "bsa_lastError": None,
+        "bsa_Init": [], "bsa_Finalise": [], "bsa_lastError": None, "bsa_mlp_lastError": None,
         "bsa_setAnalysisType": [i], "bsa_setVersion": [i], "bsa_setScalingConv": [i],
         "bsa_setSpectraComputation": [i, i], "bsa_setSpectraExtension": [i], "bsa_setSpatialSymmetry": [i],
         "bsa_setSpectraSymmetries": [i], "bsa_setTestMode": [i], "bsa_setupClassic": [i, d],
@@ -86,13 +86,21 @@ def load(path: Optional[str] = None):
         "bsa_gpu_pointMomentsNoAlloc": [vp, i, i, vp, vp, vp, vp, vp, vp, vp, i, vp, vp, vp, vp, vp, vp],
         "bsa_gpu_mshZones": [vp, i, vp, vp, vp], "bsa_gpu_mshGenerateZones": [vp, i, vp],
         "bsa_setPODTruncationThreshold": [d], "bsa_setPODNOfModesKept": [i],
+        "bsa_gpu_mshZonesDiag": [vp, i, vp, vp, vp],
+        "bsa_mlp_create": [i, i, C.c_ulonglong], "bsa_mlp_destroy": [i], "bsa_mlp_num_params": [i],
+        "bsa_mlp_get_params": [i, vp, i], "bsa_mlp_set_params": [i, vp], "bsa_mlp_forward": [i, vp, i, vp],
+        "bsa_mlp_gradients": [i, vp, vp, vp, i, vp, vp],
+        "bsa_mlp_train": [i, vp, vp, vp, i, i, i, C.c_float, C.c_ulonglong, vp],
         "bsa_computeBRdecomp": [vp, vp, vp], "bsa_computePeakFactors": [i, vp, vp, d, vp, vp, vp, vp],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)
-        if name == "bsa_lastError":
+        if name in ("bsa_lastError", "bsa_mlp_lastError"):
             fn.restype = C.c_char_p
             fn.argtypes = []
+        elif name == "bsa_mlp_num_params":
+            fn.restype = C.c_longlong
+            fn.argtypes = args
         else:
             fn.restype = C.c_int
             fn.argtypes = args
@@ -294,6 +302,72 @@ class BsaSession:
             check(rc, "bsa_computePeakFactors")
         return rc, g, pos, neg
 
+    def msh_zones_diag(self, zones):
+        """Split-precision zone integration with each zone's own m3mr(m, m, m):
+        (m3mf, m3mr, zdiag[nz][nm])."""
+        arr = (Zone * len(zones))(*zones)
+        nm3 = self.dims()[1]
+        nm = self.nmodes()
+        mf, mr, zd = np.zeros(nm3), np.zeros(nm3), np.zeros((len(zones), nm))
+        check(self.lib.bsa_gpu_mshZonesDiag(C.cast(arr, C.c_void_p), len(zones), _p(mf), _p(mr), _p(zd)),
+              "bsa_gpu_mshZonesDiag")
+        return mf, mr, zd
+
     def close(self):
         self.lib.bsa_Finalise()
         self._keep.clear()
+
+
+class Mlp:
+    """The zone-refinement proposer network on the device (bsa_mlp_*)."""
+
+    def __init__(self, din: int, width: int = 128, seed: int = 1):
+        self.lib = load()
+        h = self.lib.bsa_mlp_create(din, width, seed)
+        if h < 0:
+            raise BsaError(f"bsa_mlp_create failed ({h}): {self.lib.bsa_mlp_lastError().decode()}")
+        self.h, self.din, self.width = h, din, width
+        self.np = int(self.lib.bsa_mlp_num_params(h))
+
+    def _chk(self, rc, what):
+        if rc != BSA_OK:
+            raise BsaError(f"{what} failed ({rc}): {self.lib.bsa_mlp_lastError().decode()}")
+
+    def params(self, bf16=False):
+        p = np.zeros(self.np, dtype=np.float32)
+        self._chk(self.lib.bsa_mlp_get_params(self.h, _p(p), 1 if bf16 else 0), "bsa_mlp_get_params")
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        self._chk(self.lib.bsa_mlp_set_params(self.h, _p(p)), "bsa_mlp_set_params")
+
+    def forward(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        out = np.zeros(x.shape[0], dtype=np.float32)
+        self._chk(self.lib.bsa_mlp_forward(self.h, _p(x), x.shape[0], _p(out)), "bsa_mlp_forward")
+        return out
+
+    def gradients(self, x, y, w):
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        y = np.ascontiguousarray(y, dtype=np.float32)
+        w = np.ascontiguousarray(w, dtype=np.float32)
+        loss = np.zeros(1, dtype=np.float32)
+        g = np.zeros(self.np, dtype=np.float32)
+        self._chk(self.lib.bsa_mlp_gradients(self.h, _p(x), _p(y), _p(w), x.shape[0], _p(loss), _p(g)),
+                  "bsa_mlp_gradients")
+        return float(loss[0]), g
+
+    def train(self, x, y, w, epochs=20, batch=512, lr=1e-3, seed=7):
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        y = np.ascontiguousarray(y, dtype=np.float32)
+        w = np.ascontiguousarray(w, dtype=np.float32)
+        loss = np.zeros(1, dtype=np.float32)
+        self._chk(self.lib.bsa_mlp_train(self.h, _p(x), _p(y), _p(w), x.shape[0], epochs, batch, float(lr), seed,
+                                         _p(loss)), "bsa_mlp_train")
+        return float(loss[0])
+
+    def close(self):
+        if self.h is not None:
+            self.lib.bsa_mlp_destroy(self.h)
+            self.h = None

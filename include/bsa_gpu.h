@@ -258,6 +258,22 @@ int bsa_gpu_mshZones(const bsa_zone *zones, int nz, double *m3mf, double *m3mr, 
  * error criterion). */
 int bsa_gpu_mshZonesDiag(const bsa_zone *zones, int nz, double *m3mf, double *m3mr, double *zdiag);
 
+/* The zone-refinement proposer (no counterpart in the reference): an MLP
+ * din -> width -> width -> width (ReLU) -> 1 logit, BF16 weights, FP32 accumulation, trained on
+ * the device (weighted binary cross-entropy with hard or soft targets, Adam on FP32 master
+ * weights).  Parameters, flattened: W1[width][din] b1 W2[width][width] b2 W3[width][width] b3
+ * w4[width] b4.  bsa_mlp_create returns a handle (>= 0) or an error code; din, width <= 128. */
+int bsa_mlp_create(int din, int width, unsigned long long seed);
+int bsa_mlp_destroy(int h);
+long long bsa_mlp_num_params(int h);
+int bsa_mlp_get_params(int h, float *params, int bf16);  /* FP32 master, or the BF16 copy as floats */
+int bsa_mlp_set_params(int h, const float *params);
+int bsa_mlp_forward(int h, const float *x, int n, float *prob);  /* x[n][din] -> P(refine)[n] */
+int bsa_mlp_gradients(int h, const float *x, const float *y, const float *sw, int n, float *loss, float *grads);
+int bsa_mlp_train(int h, const float *x, const float *y, const float *sw, int n, int epochs, int batch, float lr,
+                  unsigned long long seed, float *loss_out);
+const char *bsa_mlp_lastError(void);
+
 /* The zone layout the Mesher analysis (bsa_Run with analysis type 2) evaluates: restates
  * prefetchZoneLimits_ (BsaMesherImpl.F90:1638-1859) and the background peak zone of
  * PreMesh (:266-420), and lays rectangular zones over those limits on both axes.  Writes
