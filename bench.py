@@ -215,6 +215,56 @@ def mesher_leg(prec):
                                  "skewness_rel": relm(sk[api.PREC_BF16X3], sk[api.PREC_FP64])}}
 
 
+def learned_leg():
+    """The adaptive Mesher on five structures of the proposer's held-out set (random
+    cantilevers, 50-300 nodes, 5-20 modes): plain refinement criterion vs the learned form
+    (packaged proposer), both in the split precision, and the FP64 GPU path integrating the
+    plain criterion's final mesh (no judging levels) as the reference for the errors."""
+    from bsalib_gb300 import api
+    from bsalib_gb300.refine import DEFAULT_WEIGHTS, Proposer, Refiner
+    from bsalib_gb300.train_proposer import second_moments, skew, structure
+    prop, thr, tol = Proposer.load(DEFAULT_WEIGHTS)
+    rel = lambda x, y: float(np.max(np.abs(x - y)) / np.max(np.abs(y)))
+    pts_ratio, ms_ratio, vs64, sk_err, exact, brm = [], [], [], [], [], 0
+    ms_learned = ms64_total = 0.0
+    try:
+        for seed in range(100000, 100005):
+            prob = structure(seed)
+            s = api.BsaSession(prob, precision=api.PREC_BF16X3)
+            try:
+                nm = s.nmodes()
+                plain = Refiner(s, tol, 2).run()
+                learned = Refiner(s, tol, 2).run(proposer=prop, threshold=thr)
+                _, _, cnt = s.msh_zones(learned.final_zones)
+            finally:
+                s.close()
+            s64 = api.BsaSession(prob, precision=api.PREC_FP64)
+            try:
+                _, mr64, _ = s64.msh_zones(plain.final_zones)
+                ms64 = s64.stats().ms_total
+            finally:
+                s64.close()
+            m2 = second_moments(prob)
+            pts_ratio.append(learned.points / plain.points)
+            ms_ratio.append(learned.ms / plain.ms)
+            exact.append(rel(learned.m3mr, plain.m3mr) < 1e-10)
+            sk_err.append(rel(skew(nm, m2, learned.m3mr), skew(nm, m2, mr64)))
+            ms_learned += learned.ms
+            ms64_total += ms64
+            brm += cnt[1]
+    finally:
+        prop.close()
+    return {"workload": "random cantilevers 100000-100004 (held out), tol 1e-3, 2 refinement levels",
+            "points_ratio_learned_over_plain_median": float(np.median(pts_ratio)),
+            "time_ratio_learned_over_plain_median": float(np.median(ms_ratio)),
+            "same_final_mesh_as_plain": f"{sum(exact)}/{len(exact)}",
+            "skewness_rel_vs_fp64_max": float(max(sk_err)),
+            "mixed_learned_ms": ms_learned, "fp64_final_mesh_only_ms": ms64_total,
+            "speedup_vs_fp64_final_mesh_only": ms64_total / ms_learned,
+            "final_mesh_brm_points": brm,
+            "value": brm / (ms_learned / 1e3), "unit": "BRM pts/s of the final mesh per second of the learned run"}
+
+
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
@@ -344,6 +394,7 @@ def run_ours(args):
         traffic = profiled_traffic()
         cpu = cpu_reference(prob, budget_s=15.0)
         msh = mesher_leg(prec)
+        msh["learned_refinement"] = learned_leg()
         out = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",

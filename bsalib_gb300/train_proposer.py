@@ -1,0 +1,144 @@
+"""Train the zone-refinement proposer on records of the plain refinement criterion and
+compare the learned form with the plain one on held-out structures.
+
+  python -m bsalib_gb300.train_proposer [--train 600] [--test 60] [--tol 1e-3]
+                                        [--thr-cap 0.02] [--out proposer.npz] [--json r.json]
+
+Structures are seeded random cantilevers (`problem.random_structure`, nodes 50-300, modes
+5-20, frequencies log-uniform 0.05-5 Hz, damping 0.3-3 %, U 15-50 m/s, I_u 0.08-0.2).
+Training records come from the plain criterion on the training seeds; the held-out seeds
+are evaluated with both forms in the split precision, and the plain form's final zone set
+once more with the FP64 path, the reference for the errors.  Skewness uses the second
+moments of the same structure (Classic PSD integration, FP64).
+"""
+from __future__ import annotations
+
+import argparse
+import copy
+import json
+import time
+
+import numpy as np
+
+from . import api, build
+from .problem import random_structure
+from .refine import Proposer, Refiner
+
+
+def structure(seed):
+    p = random_structure(seed, nodes=(50, 300), modes=(5, 20), nfreq_grid=(129, 129))
+    p.settings.suban = 2
+    return p
+
+
+def second_moments(prob):
+    q = copy.deepcopy(prob)
+    q.settings.suban, q.settings.ibisp = 1, 0
+    s = api.BsaSession(q, precision=api.PREC_FP64)
+    try:
+        return s.run()["m2mr_cls"]
+    finally:
+        s.close()
+
+
+def skew(nm, m2, m3):
+    sig = np.sqrt(np.abs(np.diag(m2.reshape(nm, nm))))
+    return m3 / np.einsum("i,j,k->ijk", sig, sig, sig).reshape(-1, order="F")
+
+
+def records(seeds, tol, levels):
+    X, Y, E = [], [], []
+    for seed in seeds:
+        s = api.BsaSession(structure(seed), precision=api.PREC_BF16X3)
+        try:
+            out = Refiner(s, tol, levels).run(keep_records=True)
+        finally:
+            s.close()
+        if out.records is not None:
+            X.append(out.records[0])
+            Y.append(out.records[1])
+            E.append(out.records[2])
+    return np.concatenate(X), np.concatenate(Y), np.concatenate(E)
+
+
+def compare(prop, thr, seeds, tol, levels):
+    rows = []
+    rel = lambda x, y: float(np.max(np.abs(x - y)) / np.max(np.abs(y)))
+    for seed in seeds:
+        prob = structure(seed)
+        s = api.BsaSession(prob, precision=api.PREC_BF16X3)
+        try:
+            nm = s.nmodes()
+            plain = Refiner(s, tol, levels).run()
+            learned = Refiner(s, tol, levels).run(proposer=prop, threshold=thr)
+        finally:
+            s.close()
+        s64 = api.BsaSession(prob, precision=api.PREC_FP64)
+        try:
+            _, mr64, _ = s64.msh_zones(plain.final_zones)
+            ms64 = s64.stats().ms_total
+        finally:
+            s64.close()
+        m2 = second_moments(prob)
+        rows.append({"seed": seed, "modes": nm, "nodes": prob.nnl,
+                     "plain_points": plain.points, "learned_points": learned.points,
+                     "plain_ms": plain.ms, "learned_ms": learned.ms, "fp64_final_ms": ms64,
+                     "m3mr_rel_learned_vs_plain": rel(learned.m3mr, plain.m3mr),
+                     "m3mr_rel_learned_vs_fp64": rel(learned.m3mr, mr64),
+                     "skew_rel_learned_vs_fp64": rel(skew(nm, m2, learned.m3mr), skew(nm, m2, mr64)),
+                     "skew_rel_plain_vs_fp64": rel(skew(nm, m2, plain.m3mr), skew(nm, m2, mr64))})
+    return rows
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--train", type=int, default=600)
+    ap.add_argument("--test", type=int, default=60)
+    ap.add_argument("--tol", type=float, default=1e-3)
+    ap.add_argument("--levels", type=int, default=2)
+    ap.add_argument("--epochs", type=int, default=40)
+    ap.add_argument("--thr-cap", type=float, default=0.02, help="upper bound of the proposal threshold")
+    ap.add_argument("--out", default="")
+    ap.add_argument("--json", default="")
+    ap.add_argument("--records", default="", help="write the training records (features, label, change)")
+    a = ap.parse_args()
+    build.build()
+    t0 = time.perf_counter()
+    X, Y, E = records(range(a.train), a.tol, a.levels)
+    t_rec = time.perf_counter() - t0
+    if a.records:
+        np.savez(a.records, X=X, Y=Y, E=E)
+    prop = Proposer()
+    t0 = time.perf_counter()
+    loss = prop.fit(X, E, a.tol, epochs=a.epochs)
+    t_fit = time.perf_counter() - t0
+    p = prop(X)
+    # threshold: half the lowest probability any needed refinement of the training records
+    # received, and at most thr_cap (every one of them proposed, with a margin for unseen
+    # structures)
+    thr = float(min(0.5 * np.min(p[Y > 0.5]), a.thr_cap)) if np.any(Y > 0.5) else a.thr_cap
+    recall = float(np.mean(p[Y > 0.5] > thr)) if np.any(Y > 0.5) else 1.0
+    skipped = float(np.mean(p[Y < 0.5] <= thr)) if np.any(Y < 0.5) else 0.0
+    rows = compare(prop, thr, range(100000, 100000 + a.test), a.tol, a.levels)
+    res = {"train_structures": a.train, "test_structures": a.test, "records": int(len(Y)),
+           "positive_fraction": float(Y.mean()), "record_s": t_rec, "fit_s": t_fit, "final_train_loss": loss,
+           "threshold": thr, "train_recall": recall, "train_skipped_negatives": skipped,
+           "points_ratio_learned_over_plain_median": float(np.median([r["learned_points"] / r["plain_points"]
+                                                                      for r in rows])),
+           "time_ratio_learned_over_plain_median": float(np.median([r["learned_ms"] / r["plain_ms"] for r in rows])),
+           "exact_match_fraction": float(np.mean([r["m3mr_rel_learned_vs_plain"] < 1e-10 for r in rows])),
+           "m3mr_rel_learned_vs_plain_max": float(max(r["m3mr_rel_learned_vs_plain"] for r in rows)),
+           "skew_rel_learned_vs_fp64_max": float(max(r["skew_rel_learned_vs_fp64"] for r in rows)),
+           "skew_rel_plain_vs_fp64_max": float(max(r["skew_rel_plain_vs_fp64"] for r in rows)),
+           "rows": rows}
+    if a.out:
+        prop.save(a.out, thr, a.tol)
+    prop.close()
+    if a.json:
+        with open(a.json, "w") as fh:
+            fh.write(json.dumps(res))
+    print(json.dumps({k: v for k, v in res.items() if k != "rows"}))
+
+
+if __name__ == "__main__":
+    main()
