@@ -28,6 +28,10 @@ PREC_BF16X3 = 1
 
 _lib = None
 
+# bsa_brm_export_fn: (npts, f1, f2, brm[npts][dim_bisp], user)
+EXPORT_FN = C.CFUNCTYPE(None, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double),
+                        C.c_void_p)
+
 
 class BsaError(RuntimeError):
     pass
@@ -86,7 +90,7 @@ def load(path: Optional[str] = None):
         "bsa_gpu_pointMomentsNoAlloc": [vp, i, i, vp, vp, vp, vp, vp, vp, vp, i, vp, vp, vp, vp, vp, vp],
         "bsa_gpu_mshZones": [vp, i, vp, vp, vp], "bsa_gpu_mshGenerateZones": [vp, i, vp],
         "bsa_setPODTruncationThreshold": [d], "bsa_setPODNOfModesKept": [i],
-        "bsa_gpu_mshZonesDiag": [vp, i, vp, vp, vp],
+        "bsa_gpu_mshZonesDiag": [vp, i, vp, vp, vp], "bsa_setBispExportCallback": [EXPORT_FN, vp],
         "bsa_mlp_create": [i, i, C.c_ulonglong], "bsa_mlp_destroy": [i], "bsa_mlp_num_params": [i],
         "bsa_mlp_get_params": [i, vp, i], "bsa_mlp_set_params": [i, vp], "bsa_mlp_forward": [i, vp, i, vp],
         "bsa_mlp_gradients": [i, vp, vp, vp, i, vp, vp],
@@ -301,6 +305,22 @@ class BsaSession:
         if rc < 0:
             check(rc, "bsa_computePeakFactors")
         return rc, g, pos, neg
+
+    def set_export(self, fn):
+        """bsa_setBispExportCallback: fn(f1, f2, brm[npts][dim_bisp]) receives the Classic
+        response bispectra during run(); None switches the export off."""
+        if fn is None:
+            self._export = None
+            check(self.lib.bsa_setBispExportCallback(C.cast(None, EXPORT_FN), None), "bsa_setBispExportCallback")
+            return
+        nb = self.dims()[1]
+
+        def tramp(n, f1, f2, brm, user):
+            fn(np.ctypeslib.as_array(f1, (n,)).copy(), np.ctypeslib.as_array(f2, (n,)).copy(),
+               np.ctypeslib.as_array(brm, (n * nb,)).reshape(n, nb).copy())
+
+        self._export = EXPORT_FN(tramp)  # kept alive with the session
+        check(self.lib.bsa_setBispExportCallback(self._export, None), "bsa_setBispExportCallback")
 
     def msh_zones_diag(self, zones):
         """Split-precision zone integration with each zone's own m3mr(m, m, m):

@@ -60,6 +60,7 @@ struct PointSrc {
     int trunc;              // 1: S(f1+f2) beyond the grid reads zero
     int sum_base;           // A-table row of the analytic sum table (s = i1 + i2)
     int r0, nr;             // grid rows (f1 index) of this run: i1 in [r0, r0 + nr)
+    long long pbase;        // kPointsGrid: point p of the launch is grid point pbase + p
     int wmode;
     double wval;            // uniform weight, or d^2 for the classic edge weights
     const double *fgrid;    // grid frequencies (kPointsGrid)
@@ -90,7 +91,8 @@ __device__ __forceinline__ void get_point(const PointSrc &ps, long long p, int &
                                           double &w, double &f1, double &f2) {
     if (ps.mode == kPointsGrid) {
         const int nf = ps.nf;
-        const int i1 = ps.r0 + (int)(p % ps.nr), i2 = (int)(p / ps.nr);
+        const long long q = p + ps.pbase;
+        const int i1 = ps.r0 + (int)(q % ps.nr), i2 = (int)(q / ps.nr);
         ix = i1;
         iy = i2;
         const int s = i1 + i2;

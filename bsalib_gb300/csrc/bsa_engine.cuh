@@ -66,6 +66,8 @@ struct Engine {
     bool classic_trunc = true;  // S(f1+f2) beyond the classic grid reads zero
     int shard_r0 = 0, shard_r1 = -1;  // classic grid rows evaluated (-1: to the end)
     // POD truncation requests (bsa_setPODTruncationThreshold / bsa_setPODNOfModesKept)
+    bsa_brm_export_fn export_fn = nullptr;  // bsa_setBispExportCallback
+    void *export_user = nullptr;
     double pod_trunc_lim = 0.0;
     int pod_nmodes = 0;
     // The Mesher's POD form truncates only when one of the two was set to a value that
@@ -112,6 +114,7 @@ struct Engine {
     int classic_grid(std::vector<double> &f);
     int run_classic(double *m2mf, double *m2mr, double *m2o2mr, double *m3mf, double *m3mr, double *bf_host,
                     double *br_host, std::vector<double> *grid_out);
+    int classic_export(PointSrc ps, const std::vector<double> &f, double *m3mf, double *m3mr);
     int contract(const PointSrc &ps, long long npts, double *m3mf, double *m3mr, double *bf_host, double *br_host);
     int contract_mixed(const PointSrc &ps, long long npts, double *m3mf, double *m3mr);
     int contract_diag(const PointSrc &ps, long long npts, int msh_form, double *m3mf, double *m3mr,

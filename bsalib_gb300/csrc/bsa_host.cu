@@ -68,6 +68,8 @@ void Engine::reset_inputs() {
     shard_r1 = -1;
     pod_trunc_lim = 0.0;
     pod_nmodes = 0;
+    export_fn = nullptr;
+    export_user = nullptr;
 }
 
 void Engine::free_device() {
@@ -416,9 +418,14 @@ int Engine::run_classic(double *m2mf, double *m2mr, double *m2o2mr, double *m3mf
         ps.r0 = r0;
         ps.nr = r1 - r0;
         const long long npts = (long long)(r1 - r0) * nf;
-        rc = diagonal ? contract_diag(ps, npts, 0, m3mf, m3mr, bf_host, br_host)
-             : mixed  ? contract_mixed(ps, npts, m3mf, m3mr)
-                      : contract(ps, npts, m3mf, m3mr, bf_host, br_host);
+        if (export_fn && !bf_host && !br_host) {
+            if (r0 != 0 || r1 != nf) return fail(BSA_ERR_ARG, "the bispectrum export needs the full grid");
+            rc = classic_export(ps, f, m3mf, m3mr);
+        } else {
+            rc = diagonal ? contract_diag(ps, npts, 0, m3mf, m3mr, bf_host, br_host)
+                 : mixed  ? contract_mixed(ps, npts, m3mf, m3mr)
+                          : contract(ps, npts, m3mf, m3mr, bf_host, br_host);
+        }
         if (rc) return rc;
         last_points = (double)npts;
     }
@@ -426,6 +433,46 @@ int Engine::run_classic(double *m2mf, double *m2mr, double *m2o2mr, double *m3mf
     float ms = 0.f;
     cudaEventElapsedTime(&ms, ev0, ev1);
     last_ms = ms;
+    return BSA_OK;
+}
+
+// The Classic grid in column blocks with materialised response bispectra, each block handed
+// to the export callback (BsaClassicImpl.F90:175-191); third moments summed over the blocks.
+// FP64 tables: the A table is rebuilt in FP64 when the analysis prepared the FP32 one.
+int Engine::classic_export(PointSrc ps, const std::vector<double> &f, double *m3mf, double *m3mr) {
+    const int nf = ps.nf;
+    const long long nb = dim_bisp();
+    int rc;
+    if (precision == BSA_PREC_BF16X3 && !set.onlyd) {
+        std::vector<double> ftab = f;
+        if (!ps.trunc)
+            for (int s = 0; s < 2 * nf - 1; ++s) ftab.push_back(2.0 * f[0] + s * (f[1] - f[0]));
+        if ((rc = build_atable(ftab, false))) return rc;
+        ps.fgrid = dFreq.as<double>();
+    }
+    const long long budget = 1LL << 30;  // bytes of one block's host bispectra
+    const int cols = (int)std::max(1LL, std::min((long long)nf, budget / (16LL * nf * nb)));
+    std::vector<double> br((size_t)cols * nf * nb), f1((size_t)cols * nf), f2((size_t)cols * nf);
+    std::vector<double> accF(nb, 0.0), accR(nb, 0.0), mf(nb), mr(nb);
+    for (int c0 = 0; c0 < nf; c0 += cols) {
+        const int nc = std::min(cols, nf - c0);
+        const long long npts = (long long)nc * nf;
+        ps.pbase = (long long)c0 * nf;
+        rc = set.onlyd ? contract_diag(ps, npts, 0, mf.data(), mr.data(), nullptr, br.data())
+                       : contract(ps, npts, mf.data(), mr.data(), nullptr, br.data());
+        if (rc) return rc;
+        for (long long p = 0; p < npts; ++p) {
+            f1[p] = f[p % nf];
+            f2[p] = f[c0 + p / nf];
+        }
+        export_fn((int)npts, f1.data(), f2.data(), br.data(), export_user);
+        for (long long x = 0; x < nb; ++x) {
+            accF[x] += mf[x];
+            accR[x] += mr[x];
+        }
+    }
+    if (m3mf) std::memcpy(m3mf, accF.data(), sizeof(double) * nb);
+    if (m3mr) std::memcpy(m3mr, accR.data(), sizeof(double) * nb);
     return BSA_OK;
 }
 
@@ -808,6 +855,13 @@ int bsa_getSpectraDims(int *dim_psd, int *dim_bisp) {
     if (rc) return rc;
     if (dim_psd) *dim_psd = (int)E.dim_psd();
     if (dim_bisp) *dim_bisp = (int)E.dim_bisp();
+    return BSA_OK;
+}
+
+int bsa_setBispExportCallback(bsa_brm_export_fn fn, void *user) {
+    GUARD();
+    eng().export_fn = fn;
+    eng().export_user = user;
     return BSA_OK;
 }
 

@@ -129,6 +129,15 @@ int bsa_computeSkewness(int nm, const double *m2, const double *m3, double *sk);
 
 const char *bsa_lastError(void);
 
+/* bsa_setBispExportCallback (src/bsa/BsaLibImpl.F90:1809-1816, called from the Classic
+ * analysis at BsaClassicImpl.F90:175-191): fn receives the response bispectra of the Classic
+ * grid, npts points at a time, f1 fastest then f2 (the reference's loop order), brm laid out
+ * [npts][dim_bisp].  With a callback set, bsa_Run evaluates the Classic bispectra in FP64 in
+ * column blocks of the grid (whatever bsa_gpu_setPrecision says), streams each block to fn and
+ * sums the third moments over the blocks.  NULL switches the export off. */
+typedef void (*bsa_brm_export_fn)(int npts, const double *f1, const double *f2, const double *brm, void *user);
+int bsa_setBispExportCallback(bsa_brm_export_fn fn, void *user);
+
 /* bsa_computeBRdecomp (src/bsa/BsaLibImpl.F90:1292-1420): background part
  * bkg[m] = m2mf(m,m) / K_m^2 and resonant part res[m] = pi 2pi f_m S_Fm(f_m) / (2 xsi_m K_m^2)
  * of each kept mode's response variance, S_Fm(f_m) the modal force PSD at the mode's own
