@@ -91,6 +91,7 @@ def load(path: Optional[str] = None):
         "bsa_gpu_mshZones": [vp, i, vp, vp, vp], "bsa_gpu_mshGenerateZones": [vp, i, vp],
         "bsa_setPODTruncationThreshold": [d], "bsa_setPODNOfModesKept": [i],
         "bsa_gpu_mshZonesDiag": [vp, i, vp, vp, vp], "bsa_setBispExportCallback": [EXPORT_FN, vp],
+        "bsa_gpu_setClassicSymmetry": [i],
         "bsa_mlp_create": [i, i, C.c_ulonglong], "bsa_mlp_destroy": [i], "bsa_mlp_num_params": [i],
         "bsa_mlp_get_params": [i, vp, i], "bsa_mlp_set_params": [i, vp], "bsa_mlp_forward": [i, vp, i, vp],
         "bsa_mlp_gradients": [i, vp, vp, vp, i, vp, vp],
@@ -192,6 +193,10 @@ class BsaSession:
     def set_precision(self, prec: int):
         self.precision = prec
         check(self.lib.bsa_gpu_setPrecision(prec), "bsa_gpu_setPrecision")
+
+    def set_symmetry(self, on: bool = True):
+        """bsa_gpu_setClassicSymmetry: evaluate half of the (symmetric) Classic grid."""
+        check(self.lib.bsa_gpu_setClassicSymmetry(1 if on else 0), "bsa_gpu_setClassicSymmetry")
 
     def set_rows(self, r_begin: int, r_end: int = -1):
         """Evaluate only Classic grid rows [r_begin, r_end) (f1 index)."""

@@ -61,6 +61,7 @@ struct PointSrc {
     int sum_base;           // A-table row of the analytic sum table (s = i1 + i2)
     int r0, nr;             // grid rows (f1 index) of this run: i1 in [r0, r0 + nr)
     long long pbase;        // kPointsGrid: point p of the launch is grid point pbase + p
+    int sym_rows;           // kPointsGrid, central symmetry: rows i1 < sym_rows weigh twice
     int wmode;
     double wval;            // uniform weight, or d^2 for the classic edge weights
     const double *fgrid;    // grid frequencies (kPointsGrid)
@@ -110,6 +111,7 @@ __device__ __forceinline__ void get_point(const PointSrc &ps, long long p, int &
         } else {
             w = ps.wval;
         }
+        if (i1 < ps.sym_rows) w *= 2.0;  // the mirror point (nf-1-i1, nf-1-i2) is not evaluated
     } else {
         ix = ps.ix[p];
         iy = ps.iy[p];

@@ -66,6 +66,7 @@ struct Engine {
     bool classic_trunc = true;  // S(f1+f2) beyond the classic grid reads zero
     int shard_r0 = 0, shard_r1 = -1;  // classic grid rows evaluated (-1: to the end)
     // POD truncation requests (bsa_setPODTruncationThreshold / bsa_setPODNOfModesKept)
+    bool classic_sym = false;   // bsa_gpu_setClassicSymmetry: evaluate half the Classic grid
     bsa_brm_export_fn export_fn = nullptr;  // bsa_setBispExportCallback
     void *export_user = nullptr;
     double pod_trunc_lim = 0.0;

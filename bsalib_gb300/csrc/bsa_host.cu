@@ -70,6 +70,7 @@ void Engine::reset_inputs() {
     pod_nmodes = 0;
     export_fn = nullptr;
     export_user = nullptr;
+    classic_sym = false;
 }
 
 void Engine::free_device() {
@@ -417,8 +418,24 @@ int Engine::run_classic(double *m2mf, double *m2mr, double *m2o2mr, double *m3mf
         ps.fgrid = dFreq.as<double>();
         ps.r0 = r0;
         ps.nr = r1 - r0;
-        const long long npts = (long long)(r1 - r0) * nf;
-        if (export_fn && !bf_host && !br_host) {
+        long long npts = (long long)(r1 - r0) * nf;
+        // Central symmetry (bsa_gpu_setClassicSymmetry): on the grid f = -N..N every quantity
+        // of the path is even in f (S and c^|f| depend on |f|, H(-w) = conj H(w), the sum
+        // truncation and the integration weights are symmetric), so B(f_r, f_c) equals
+        // B(f_nf-1-r, f_nf-1-c).  Rows r < n_pad then stand for their mirrors with twice the
+        // weight, the centre row (its own mirror) once; rows above it are not evaluated.
+        const bool sym = classic_sym && set.defsc == 1 && !bf_host && !br_host && !export_fn;
+        if (sym) {
+            ps.sym_rows = ps.n_pad;
+            ps.nr = std::max(0, std::min(r1, ps.n_pad + 1) - r0);
+            npts = (long long)ps.nr * nf;
+        }
+        if (sym && ps.nr == 0) {
+            const long long nb = dim_bisp();
+            if (m3mf) std::memset(m3mf, 0, sizeof(double) * nb);
+            if (m3mr) std::memset(m3mr, 0, sizeof(double) * nb);
+            rc = BSA_OK;
+        } else if (export_fn && !bf_host && !br_host) {
             if (r0 != 0 || r1 != nf) return fail(BSA_ERR_ARG, "the bispectrum export needs the full grid");
             rc = classic_export(ps, f, m3mf, m3mr);
         } else {
@@ -855,6 +872,12 @@ int bsa_getSpectraDims(int *dim_psd, int *dim_bisp) {
     if (rc) return rc;
     if (dim_psd) *dim_psd = (int)E.dim_psd();
     if (dim_bisp) *dim_bisp = (int)E.dim_bisp();
+    return BSA_OK;
+}
+
+int bsa_gpu_setClassicSymmetry(int on) {
+    GUARD();
+    eng().classic_sym = on != 0;
     return BSA_OK;
 }
 

@@ -47,6 +47,7 @@ constexpr int kFlushTiles = 64;                  // FP32 -> FP64 flush period (N
 struct Params {
     int nf;          // grid size
     int rb, re;      // grid rows r in [rb, re) evaluated by this launch
+    int sym_rows;    // central symmetry: rows r < sym_rows weigh twice (0: off)
     int nm;          // kept modes
     int Mp;          // rows per frequency in U (nm^2 rounded up to 128)
     int MT;          // Mp / 128
@@ -65,9 +66,10 @@ struct Params {
 __device__ __forceinline__ float point_weight(const Params &p, int r, int c) {
     if (p.wmode == kWeightClassicVect) {
         const bool b1 = (r == 0 || r == p.nf - 1), b2 = (c == 0 || c == p.nf - 1);
-        return (float)(p.wval * ((b1 && b2) ? -0.5 : ((b1 || b2) ? 0.5 : 1.0)));
+        const double m = r < p.sym_rows ? 2.0 : 1.0;
+        return (float)(m * p.wval * ((b1 && b2) ? -0.5 : ((b1 || b2) ? 0.5 : 1.0)));
     }
-    return (float)p.wval;
+    return (float)(r < p.sym_rows ? 2.0 * p.wval : p.wval);
 }
 
 template <int NMT>
@@ -471,6 +473,7 @@ int Engine::contract_mixed(const PointSrc &ps, long long npts, double *m3mf, dou
     prm.nf = nf;
     prm.rb = ps.r0;
     prm.re = ps.r0 + ps.nr;
+    prm.sym_rows = ps.sym_rows;
     prm.nm = nm;
     prm.Mp = Mp;
     prm.MT = MT;

@@ -200,6 +200,13 @@ int bsa_gpu_setClassicTruncation(int on);
  * the rows sum to the full grid's (multi-GPU / multi-process sharding, one host sum). */
 int bsa_gpu_setClassicRows(int r_begin, int r_end);
 
+/* No counterpart in the reference.  on != 0: on the symmetric Classic grid f = -N..N
+ * (circular-frequency scaling, the reference's default) every factor of the path is even in
+ * f, so B(f1, f2) = B(-f1, -f2); bsa_Run then evaluates the rows f1 <= 0 only, the rows f1 < 0
+ * with twice their integration weight.  The third moments equal the full grid's up to the
+ * summation order; materialised or exported bispectra always cover the full grid. */
+int bsa_gpu_setClassicSymmetry(int on);
+
 /* getBFMClsVect + getBRMClsVect materialised (functionsImpl.F90:1312-1738): force and
  * response bispectra on the classic grid, (nf, nf, dim_bisp) with f1 fastest, and the grid.
  * Runs validation and the grid set-up of bsa_Run; for small grids (tests). */
