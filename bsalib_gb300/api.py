@@ -91,7 +91,7 @@ def load(path: Optional[str] = None):
         "bsa_gpu_mshZones": [vp, i, vp, vp, vp], "bsa_gpu_mshGenerateZones": [vp, i, vp],
         "bsa_setPODTruncationThreshold": [d], "bsa_setPODNOfModesKept": [i],
         "bsa_gpu_mshZonesDiag": [vp, i, vp, vp, vp], "bsa_setBispExportCallback": [EXPORT_FN, vp],
-        "bsa_gpu_setClassicSymmetry": [i],
+        "bsa_gpu_setClassicSymmetry": [i], "bsa_loadInputFiles": [C.c_char_p],
         "bsa_mlp_create": [i, i, C.c_ulonglong], "bsa_mlp_destroy": [i], "bsa_mlp_num_params": [i],
         "bsa_mlp_get_params": [i, vp, i], "bsa_mlp_set_params": [i, vp], "bsa_mlp_forward": [i, vp, i, vp],
         "bsa_mlp_gradients": [i, vp, vp, vp, i, vp, vp],

@@ -66,6 +66,8 @@ struct Engine {
     bool classic_trunc = true;  // S(f1+f2) beyond the classic grid reads zero
     int shard_r0 = 0, shard_r1 = -1;  // classic grid rows evaluated (-1: to the end)
     // POD truncation requests (bsa_setPODTruncationThreshold / bsa_setPODNOfModesKept)
+    std::vector<std::vector<int>> own_i;     // arrays read by bsa_loadInputFiles (owned here)
+    std::vector<std::vector<double>> own_d;
     bool classic_sym = false;   // bsa_gpu_setClassicSymmetry: evaluate half the Classic grid
     bsa_brm_export_fn export_fn = nullptr;  // bsa_setBispExportCallback
     void *export_user = nullptr;

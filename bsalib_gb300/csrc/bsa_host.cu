@@ -59,6 +59,8 @@ cudaError_t DevBuf::reserve(size_t nbytes) {
 
 void Engine::reset_inputs() {
     in = Inputs();
+    own_i.clear();
+    own_d.clear();
     set = Settings();
     derived_ok = false;
     // controls of the GPU path return to their defaults with the inputs

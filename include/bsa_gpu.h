@@ -101,6 +101,13 @@ int bsa_setNodalWindAltitudes(const double *walt, int nn); /* BsaLibImpl.F90:111
 int bsa_setSpatialNodalCorr(const double *corr, int64_t ncorr); /* BsaLibImpl.F90:1125, (ncorr,3) */
 int bsa_setWindFCoeffs(const double *wfc, int nlibs_l, int ndegw3, int nn_l); /* BsaLibImpl.F90:1133, (nlibs_l,ndegw+3,nn_l) */
 
+/* The standalone driver's inputs read natively: bsa.bsadata (getBsaData, app/bsa.F90:877-930)
+ * and bsa.extdata (getExtData, app/bsa.F90:696-871; the files generateBSAInputFiles_,
+ * BsaLibImpl.F90:2065-2155, writes) from directory dir, followed by the driver's setter
+ * sequence (app/bsa.F90:525-606).  Call after bsa_Init; the library owns the arrays until
+ * bsa_Finalise. */
+int bsa_loadInputFiles(const char *dir);
+
 /* Validates the inputs (validateAll_, BsaLibImpl.F90:469-535: mode validation
  * validateModalInfo_ :545-599, projection setPhitimesCLocalInstance_ :611-671) and returns
  * the number of kept modes, which sizes bsa_Run's outputs. */
