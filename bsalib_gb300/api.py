@@ -97,6 +97,8 @@ def load(path: Optional[str] = None):
         "bsa_mlp_gradients": [i, vp, vp, vp, i, vp, vp],
         "bsa_mlp_train": [i, vp, vp, vp, i, i, i, C.c_float, C.c_ulonglong, vp],
         "bsa_computeBRdecomp": [vp, vp, vp], "bsa_computePeakFactors": [i, vp, vp, d, vp, vp, vp, vp],
+        "bsa_gpu_batchAdd": [vp], "bsa_gpu_batchCase": [i, vp, vp], "bsa_gpu_batchRun": [vp] * 5,
+        "bsa_gpu_batchClear": [],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)
@@ -341,6 +343,53 @@ class BsaSession:
     def close(self):
         self.lib.bsa_Finalise()
         self._keep.clear()
+
+
+class Sweep:
+    """Batched Classic sweep (bsa_gpu_batch*): cases are snapshotted as they are added, then
+    every case is evaluated by one split-precision launch per group of cases."""
+
+    def __init__(self):
+        self.lib = load()
+        check(self.lib.bsa_gpu_batchClear(), "bsa_gpu_batchClear")
+        self.nm, self.nf = [], []
+
+    def add_current(self) -> int:
+        """Snapshot the library's current inputs as the next case."""
+        cid, nm, nf = C.c_int(0), C.c_int(0), C.c_int(0)
+        check(self.lib.bsa_gpu_batchAdd(C.byref(cid)), "bsa_gpu_batchAdd")
+        check(self.lib.bsa_gpu_batchCase(cid.value, C.byref(nm), C.byref(nf)), "bsa_gpu_batchCase")
+        self.nm.append(nm.value)
+        self.nf.append(nf.value)
+        return cid.value
+
+    def add(self, prob: Problem) -> int:
+        """Set up `prob` (bsa_Init and the setters), snapshot it, release the setup."""
+        s = BsaSession(prob, precision=PREC_BF16X3)
+        try:
+            return self.add_current()
+        finally:
+            s.close()
+
+    def run(self):
+        """Per case: dict(m3mf, m3mr, m2mr, ms); and the sweep's total device ms."""
+        n3 = sum(n ** 3 for n in self.nm)
+        n2 = sum(n ** 2 for n in self.nm)
+        mf, mr, m2 = np.zeros(n3), np.zeros(n3), np.zeros(n2)
+        lat = np.zeros(len(self.nm))
+        tot = C.c_double(0.0)
+        check(self.lib.bsa_gpu_batchRun(_p(mf), _p(mr), _p(m2), _p(lat), C.byref(tot)), "bsa_gpu_batchRun")
+        out, o3, o2 = [], 0, 0
+        for c, n in enumerate(self.nm):
+            out.append({"m3mf": mf[o3:o3 + n ** 3], "m3mr": mr[o3:o3 + n ** 3], "m2mr": m2[o2:o2 + n ** 2],
+                        "ms": float(lat[c]), "nm": n, "nf": self.nf[c]})
+            o3 += n ** 3
+            o2 += n ** 2
+        return out, float(tot.value)
+
+    def clear(self):
+        check(self.lib.bsa_gpu_batchClear(), "bsa_gpu_batchClear")
+        self.nm, self.nf = [], []
 
 
 class Mlp:

@@ -1,0 +1,687 @@
+// bsa_batch.cu -- many Classic analyses (structures x wind cases) in one persistent
+// split-precision launch per group of cases.
+//
+// Each case is snapshotted when it is added (bsa_gpu_batchAdd: its validated inputs, the
+// derived tables and its grid), so the caller can set up the next case at once.  At
+// bsa_gpu_batchRun the cases are grouped by their FRF-table width NMT (8, 16, 24, 32 kept
+// modes) and by device memory; for each group the operands of every case are prepared into
+// shared tables (one U, G, S table each, rows of all cases stacked with a common K stride), and
+// one launch of k_bfm_batch walks a work list of (case, grid row, row tile) items with the
+// k_bfm_mixed pipeline (TMA warp, MMA warp, four TMEM-draining warps).  The epilogue adds its
+// FP32 partial moments into per-case FP64 accumulators (atomics: the summation order varies
+// from run to run in the last bits) and the last epilogue warp to finish a case stamps its
+// completion time, which gives per-case latencies within the launch.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "../../include/bsa_gpu.h"
+#include "bsa_engine.cuh"
+#include "bsa_kernels.cuh"
+#include "bsa_mixed.cuh"
+#include "bsa_tc.cuh"
+
+namespace bsa {
+namespace batch {
+
+using namespace tc;
+
+constexpr int kStages = 2;
+constexpr int kStageBytes = 6 * kTileBytes;
+constexpr int kKinds = 5;  // mr1, mr3, mr2, mf1, mf23
+constexpr int kFlushTiles = 64;
+
+struct CaseP {
+    int nf, nm, Mp, MT, nk, ks_last, n_ntiles, wmode;
+    double wval;
+    int u_row0;       // first U-table row of the case
+    int g_row0;       // first G-table row
+    int s_row0;       // first S-table row
+    int hg0, hs0;     // first FRF-table entries (float2)
+    long long part0;  // first accumulator (double) of the case: [kKinds][NMT][Mp]
+    unsigned nitems;  // work items of the case
+};
+
+struct BItem {
+    int c, r, mt, pad;
+};
+
+struct BParams {
+    const BItem *items;
+    int nitems;
+    const CaseP *cases;
+    const float2 *Hg, *Hs;
+    double *part;
+    unsigned *done_cnt;           // per case: epilogue warps that finished an item
+    unsigned long long *t_done;   // per case: completion time (global timer, ns)
+    unsigned long long *t_start;  // launch start (global timer, ns)
+    int *err;
+};
+
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+__device__ __forceinline__ float2 conjf2(float2 a) { return make_float2(a.x, -a.y); }
+
+__device__ __forceinline__ float case_weight(const CaseP &cs, int r, int c) {
+    if (cs.wmode == kWeightClassicVect) {
+        const bool b1 = (r == 0 || r == cs.nf - 1), b2 = (c == 0 || c == cs.nf - 1);
+        return (float)(cs.wval * ((b1 && b2) ? -0.5 : ((b1 || b2) ? 0.5 : 1.0)));
+    }
+    return (float)cs.wval;
+}
+
+template <int NMT>
+__global__ void __launch_bounds__(192, 1)
+    k_bfm_batch(const __grid_constant__ CUtensorMap tmUh, const __grid_constant__ CUtensorMap tmUl,
+                const __grid_constant__ CUtensorMap tmGh, const __grid_constant__ CUtensorMap tmGl,
+                const __grid_constant__ CUtensorMap tmSh, const __grid_constant__ CUtensorMap tmSl, const BParams p) {
+    constexpr int NC = kBN / NMT;
+    constexpr int BROWS = NC * NMT;
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint64_t *bars = (uint64_t *)(smem + kStages * kStageBytes);
+    uint64_t *full = bars, *empty = bars + kStages, *tfull = bars + 2 * kStages, *tempty = bars + 2 * kStages + 2;
+    uint64_t *done = bars + 2 * kStages + 4;
+    uint32_t *tmem_slot = (uint32_t *)(bars + 2 * kStages + 5);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int *err = p.err;
+    if (blockIdx.x == 0 && threadIdx.x == 0) *p.t_start = gtime();
+
+    for (int s = 0; s < kStages; ++s)
+        for (int t = 2; t < 6; ++t) {
+            uint8_t *tile = smem + s * kStageBytes + t * kTileBytes;
+            for (int x = threadIdx.x; x < (128 - BROWS) * 128 / 16; x += blockDim.x)
+                ((uint4 *)(tile + BROWS * 128))[x] = make_uint4(0, 0, 0, 0);
+        }
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kStages; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(&tfull[b], 1);
+            mbar_init(&tempty[b], 128);
+        }
+        mbar_init(done, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(su32(tmem_slot)) : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = *tmem_slot;
+    const uint32_t tx_bytes = 2u * kTileBytes + 4u * (uint32_t)(BROWS * 128);
+
+    if (warp == 0) {
+        // ---------------- TMA producer ----------------
+        if (lane == 0) {
+            uint32_t it = 0;
+            bool ok = true;
+            for (int w = blockIdx.x; w < p.nitems && ok; w += gridDim.x) {
+                const BItem im = p.items[w];
+                const CaseP cs = p.cases[im.c];
+                for (int nt = 0; nt < cs.n_ntiles && ok; ++nt)
+                    for (int kc = 0; kc < cs.nk && ok; ++kc, ++it) {
+                        const int s = it % kStages;
+                        const uint32_t ph = (it / kStages) & 1u;
+                        if (!mbar_wait(&empty[s], ph ^ 1u, err, 1)) { ok = false; break; }
+                        uint8_t *st = smem + s * kStageBytes;
+                        mbar_expect_tx(&full[s], tx_bytes);
+                        const int x = kc * kBK;
+                        const int yu = cs.u_row0 + im.r * cs.Mp + im.mt * kBM;
+                        tma_2d(st + 0 * kTileBytes, &tmUh, &full[s], x, yu);
+                        tma_2d(st + 1 * kTileBytes, &tmUl, &full[s], x, yu);
+                        const int yg = cs.g_row0 + nt * BROWS;
+                        tma_2d(st + 2 * kTileBytes, &tmGh, &full[s], x, yg);
+                        tma_2d(st + 3 * kTileBytes, &tmGl, &full[s], x, yg);
+                        const int ys = cs.s_row0 + (im.r + nt * NC) * NMT;
+                        tma_2d(st + 4 * kTileBytes, &tmSh, &full[s], x, ys);
+                        tma_2d(st + 5 * kTileBytes, &tmSl, &full[s], x, ys);
+                    }
+            }
+            const uint32_t last = it;
+            for (uint32_t q = (last > (uint32_t)kStages ? last - kStages : 0); q < last; ++q) {
+                const int s = q % kStages;
+                const uint32_t ph = (q / kStages) & 1u;
+                const uint64_t t0 = gtime();
+                while (!mbar_try(&full[s], ph) && gtime() - t0 < kWaitNs) {
+                }
+            }
+        }
+        __syncwarp();
+    } else if (warp == 1) {
+        // ---------------- MMA issuer ----------------
+        if (lane == 0) {
+            uint32_t it = 0, tile = 0;
+            bool ok = true;
+            for (int w = blockIdx.x; w < p.nitems && ok; w += gridDim.x) {
+                const CaseP cs = p.cases[p.items[w].c];
+                for (int nt = 0; nt < cs.n_ntiles && ok; ++nt, ++tile) {
+                    const int buf = tile & 1;
+                    const uint32_t tph = (tile >> 1) & 1u;
+                    if (!mbar_wait(&tempty[buf], tph ^ 1u, err, 2)) { ok = false; break; }
+                    fence_after();
+                    const uint32_t d1 = tmem + buf * 256, d3 = d1 + 128;
+                    for (int kc = 0; kc < cs.nk; ++kc, ++it) {
+                        const int s = it % kStages;
+                        const uint32_t ph = (it / kStages) & 1u;
+                        if (!mbar_wait(&full[s], ph, err, 3)) { ok = false; break; }
+                        fence_after();
+                        const uint32_t base = su32(smem + s * kStageBytes);
+                        const int nks = kc == cs.nk - 1 ? cs.ks_last : kBK / 16;
+                        for (int ks = 0; ks < nks; ++ks) {
+                            const uint32_t off = ks * 32;
+                            const uint64_t uh = sdesc(base + 0 * kTileBytes + off), ul = sdesc(base + 1 * kTileBytes + off);
+                            const uint64_t gh = sdesc(base + 2 * kTileBytes + off), gl = sdesc(base + 3 * kTileBytes + off);
+                            const uint64_t sh = sdesc(base + 4 * kTileBytes + off), sl = sdesc(base + 5 * kTileBytes + off);
+                            const uint32_t acc = (kc > 0 || ks > 0) ? 1u : 0u;
+                            mma(d1, uh, gh, acc);
+                            mma(d1, uh, gl, 1u);
+                            mma(d1, ul, gh, 1u);
+                            mma(d3, uh, sh, acc);
+                            mma(d3, uh, sl, 1u);
+                            mma(d3, ul, sh, 1u);
+                        }
+                        mma_commit(&empty[s]);
+                    }
+                    if (!ok) break;
+                    mma_commit(&tfull[buf]);
+                }
+            }
+            mma_commit(done);
+            const uint64_t t0 = gtime();
+            while (!mbar_try(done, 0) && gtime() - t0 < kWaitNs) {
+            }
+        }
+        __syncwarp();
+    } else {
+        // ---------------- epilogue: FRF x weight, partial moments per case ----------------
+        const int quarter = warp & 3;
+        const int row = quarter * 32 + lane;
+        const uint32_t lane_base = tmem + ((uint32_t)(quarter * 32) << 16);
+        float acc[kKinds][NMT];
+        uint32_t tile = 0;
+        bool ok = true;
+        for (int w = blockIdx.x; w < p.nitems && ok; w += gridDim.x) {
+            const BItem im = p.items[w];
+            const CaseP cs = p.cases[im.c];
+            const int r = im.r;
+            const int grow = im.mt * kBM + row;
+            const bool vrow = grow < cs.nm * cs.nm;
+            const int a = vrow ? grow / cs.nm : 0, b = vrow ? grow % cs.nm : 0;
+            const float2 *Hg = p.Hg + cs.hg0, *Hs = p.Hs + cs.hs0;
+            double *part = p.part + cs.part0 + grow;
+#pragma unroll
+            for (int k = 0; k < kKinds; ++k)
+#pragma unroll
+                for (int j = 0; j < NMT; ++j) acc[k][j] = 0.f;
+            const float2 hra = Hg[r * NMT + a];
+            for (int nt = 0; nt < cs.n_ntiles; ++nt, ++tile) {
+                const int buf = tile & 1;
+                const uint32_t tph = (tile >> 1) & 1u;
+                const bool got = __all_sync(0xffffffffu, mbar_wait(&tfull[buf], tph, err, 4));
+                if (!got) { ok = false; break; }
+                fence_after();
+                const int c0 = nt * NC;
+#pragma unroll
+                for (int q = 0; q < kBN / 32; ++q) {
+#pragma unroll
+                    for (int pass = 0; pass < 2; ++pass) {
+                        uint32_t v[32];
+                        tmem_ld32(lane_base + buf * 256 + pass * 128 + q * 32, v);
+                        tmem_wait_ld();
+                        float2 PA = make_float2(0.f, 0.f), PB = PA;
+                        float wc = 0.f;
+                        bool cval = false;
+                        int cg = 0, sidx = 0;
+#pragma unroll
+                        for (int e = 0; e < 32; ++e) {
+                            const int col = q * 32 + e;
+                            const int c = col / NMT, j = col % NMT;
+                            if (c >= NC) continue;
+                            if (j == 0 || e == 0) {
+                                cg = c0 + c;
+                                cval = cg < cs.nf;
+                                if (cval) {
+                                    sidx = r + cg;
+                                    wc = case_weight(cs, r, cg);
+                                    const float2 hcb = Hg[cg * NMT + b];
+                                    if (pass == 0) {
+                                        const float2 t1 = cmul(hra, hcb);
+                                        PA = make_float2(wc * t1.x, wc * t1.y);
+                                    } else {
+                                        const float2 hsa = Hs[sidx * NMT + a];
+                                        const float2 hsb = Hs[sidx * NMT + b];
+                                        const float2 t3 = cmul(hcb, conjf2(hsa));
+                                        PA = make_float2(wc * t3.x, wc * t3.y);
+                                        const float2 t2 = cmul(hra, conjf2(hsb));
+                                        PB = make_float2(wc * t2.x, wc * t2.y);
+                                    }
+                                }
+                            }
+                            if (cval && j < cs.nm) {
+                                const float x = __uint_as_float(v[e]);
+                                if (pass == 0) {
+                                    const float2 hs = Hs[sidx * NMT + j];
+                                    const float F1 = PA.x * hs.x + PA.y * hs.y;
+                                    acc[0][j] = fmaf(F1, x, acc[0][j]);
+                                    acc[3][j] = fmaf(wc, x, acc[3][j]);
+                                } else {
+                                    const float2 hr = Hg[r * NMT + j];
+                                    const float2 hc = Hg[cg * NMT + j];
+                                    const float F3 = hr.x * PA.x - hr.y * PA.y;
+                                    const float F2 = hc.x * PB.x - hc.y * PB.y;
+                                    acc[1][j] = fmaf(F3, x, acc[1][j]);
+                                    acc[2][j] = fmaf(F2, x, acc[2][j]);
+                                    acc[4][j] = fmaf(wc, x, acc[4][j]);
+                                }
+                            }
+                        }
+                    }
+                }
+                fence_before();
+                mbar_arrive(&tempty[buf]);
+                if ((nt + 1) % kFlushTiles == 0 || nt + 1 == cs.n_ntiles) {
+                    if (vrow) {
+#pragma unroll
+                        for (int k = 0; k < kKinds; ++k)
+#pragma unroll
+                            for (int j = 0; j < NMT; ++j) {
+                                if (acc[k][j] != 0.f) atomicAdd(part + (size_t)(k * NMT + j) * cs.Mp, (double)acc[k][j]);
+                                acc[k][j] = 0.f;
+                            }
+                    }
+                }
+            }
+            if (!ok) break;
+            // this warp's share of the item is in the accumulators: count it, stamp the case
+            __syncwarp();
+            if (lane == 0) {
+                __threadfence();
+                const unsigned old = atomicAdd(p.done_cnt + im.c, 1u);
+                if (old + 1 == 4u * cs.nitems) p.t_done[im.c] = gtime();
+            }
+        }
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem) : "memory");
+}
+
+// m3 of case c at out + out_off[c]: [m + nm n + nm^2 o] = 2 (T1 at (m,n,o) + T3 at (o,n,m) + T2 at (n,o,m))
+template <int NMT>
+__global__ void k_batch_reduce(const CaseP *__restrict__ cases, const long long *__restrict__ out_off,
+                               const double *__restrict__ part, double *__restrict__ m3mf, double *__restrict__ m3mr) {
+    const CaseP cs = cases[blockIdx.y];
+    const int nm = cs.nm, nm3 = nm * nm * nm;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= nm3) return;
+    const int m = x % nm, n = (x / nm) % nm, o = x / (nm * nm);
+    const double *pc = part + cs.part0;
+    auto s = [&](int kind, int aa, int bb, int j) { return pc[(size_t)(kind * NMT + j) * cs.Mp + aa * nm + bb]; };
+    const double mr = s(0, m, n, o) + s(1, o, n, m) + s(2, n, o, m);
+    const double mf = s(3, m, n, o) + s(4, o, n, m) + s(4, n, o, m);
+    m3mr[out_off[blockIdx.y] + x] = 2.0 * mr;
+    m3mf[out_off[blockIdx.y] + x] = 2.0 * mf;
+}
+
+}  // namespace batch
+
+// ------------------------------------------------------------------------------------
+// Host side
+// ------------------------------------------------------------------------------------
+struct BatchCase {
+    Settings set;
+    int nnl = 0, psd_type = 0, nme = 0, K = 0;
+    bool trunc = true;
+    std::vector<int> modes;
+    std::vector<double> hL, hQ, hLogc, hM, hK, hC, hWd3, hWd2;
+    std::vector<float> hLogc32, hL32;
+    std::vector<PsdNode> hPsd;
+    std::vector<double> f;  // Classic grid
+};
+
+static std::vector<BatchCase> g_batch;
+
+// Snapshot of the validated current inputs.
+int Engine::batch_add(int *id) {
+    int rc = validate();
+    if (rc) return rc;
+    if (set.onlyd) return fail(BSA_ERR_UNSUPPORTED, "the batched sweep runs the full-tensor Classic analysis");
+    if (nme > 32) return fail(BSA_ERR_UNSUPPORTED, "the batched sweep supports at most 32 kept modes");
+    BatchCase c;
+    if ((rc = classic_grid(c.f))) return rc;
+    if (c.f.size() < 2) return fail(BSA_ERR_ARG, "classic grid needs at least 2 frequencies");
+    c.set = set;
+    c.nnl = in.nnl;
+    c.psd_type = in.psd_type;
+    c.nme = nme;
+    c.K = K;
+    c.trunc = classic_trunc;
+    c.modes = modes;
+    c.hL = hL; c.hQ = hQ; c.hLogc = hLogc; c.hM = hM; c.hK = hK; c.hC = hC; c.hWd3 = hWd3; c.hWd2 = hWd2;
+    c.hLogc32 = hLogc32; c.hL32 = hL32; c.hPsd = hPsd;
+    g_batch.push_back(std::move(c));
+    if (id) *id = (int)g_batch.size() - 1;
+    return BSA_OK;
+}
+
+// Makes case c the engine's problem (derived tables only; no caller arrays are read).
+void Engine::batch_install(const BatchCase &c) {
+    in = Inputs();
+    in.nnl = c.nnl;
+    in.psd_type = c.psd_type;
+    set = c.set;
+    classic_trunc = c.trunc;
+    nme = c.nme;
+    K = c.K;
+    modes = c.modes;
+    hL = c.hL; hQ = c.hQ; hLogc = c.hLogc; hM = c.hM; hK = c.hK; hC = c.hC; hWd3 = c.hWd3; hWd2 = c.hWd2;
+    hLogc32 = c.hLogc32; hL32 = c.hL32; hPsd = c.hPsd;
+    derived_ok = true;
+    dev_uploaded = false;
+}
+
+int Engine::batch_run(double *m3mf, double *m3mr, double *m2mr, double *case_ms, double *total_ms) {
+    using namespace batch;
+    const int nc = (int)g_batch.size();
+    if (nc == 0) return fail(BSA_ERR_STATE, "empty batch");
+    kernels = 0;
+    h2d = d2h = 0;
+    std::vector<long long> off3(nc), off2(nc);
+    long long t3 = 0, t2 = 0;
+    for (int c = 0; c < nc; ++c) {
+        off3[c] = t3;
+        off2[c] = t2;
+        t3 += (long long)g_batch[c].nme * g_batch[c].nme * g_batch[c].nme;
+        t2 += (long long)g_batch[c].nme * g_batch[c].nme;
+    }
+    int rc = ensure_stream();
+    if (rc) return rc;
+    cudaError_t e;
+    int dev = 0, nsm = 0;
+    if ((e = cudaGetDevice(&dev)) || (e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev)))
+        return cuda_fail(e, "device query");
+    // groups: same NMT, cases in K order, device bytes bounded
+    auto nmt_of = [](int nm) { return nm <= 8 ? 8 : nm <= 16 ? 16 : nm <= 24 ? 24 : 32; };
+    std::vector<int> order(nc);
+    for (int c = 0; c < nc; ++c) order[c] = c;
+    std::sort(order.begin(), order.end(), [&](int x, int y) {
+        const int a = nmt_of(g_batch[x].nme), b = nmt_of(g_batch[y].nme);
+        return a != b ? a < b : g_batch[x].K < g_batch[y].K;
+    });
+    // the caller's problem is put back once the sweep is done
+    BatchCase saved;
+    saved.set = set;
+    saved.nnl = in.nnl;
+    saved.psd_type = in.psd_type;
+    saved.nme = nme;
+    saved.K = K;
+    saved.trunc = classic_trunc;
+    saved.modes = modes;
+    saved.hL = hL; saved.hQ = hQ; saved.hLogc = hLogc; saved.hM = hM; saved.hK = hK; saved.hC = hC;
+    saved.hWd3 = hWd3; saved.hWd2 = hWd2; saved.hLogc32 = hLogc32; saved.hL32 = hL32; saved.hPsd = hPsd;
+    const Inputs saved_in = in;
+    const bool saved_ok = derived_ok;
+    struct Restore {
+        Engine &E;
+        const BatchCase &c;
+        const Inputs &in;
+        bool ok;
+        ~Restore() {
+            E.batch_install(c);
+            E.in = in;
+            E.derived_ok = ok;
+        }
+    } restore{*this, saved, saved_in, saved_ok};
+    std::vector<double> h3f(t3), h3r(t3), h2(t2 * 3);
+    std::vector<double> lat(nc, 0.0);
+    double total = 0.0;
+    const double budget = 24e9;
+    size_t g0 = 0;
+    while (g0 < order.size()) {
+        const int NMT = nmt_of(g_batch[order[g0]].nme);
+        size_t g1 = g0;
+        double rows = 0.0;
+        while (g1 < order.size() && nmt_of(g_batch[order[g1]].nme) == NMT) {
+            // U, G and S rows of the case; hi + lo bf16 at the group's K stride, which is
+            // this case's (the group is in K order)
+            const BatchCase &c = g_batch[order[g1]];
+            const double Kp = (double)(((c.K + kBK - 1) / kBK) * kBK);
+            const double Mp = (double)(((c.nme * c.nme + kBM - 1) / kBM) * kBM);
+            const double nf = (double)c.f.size();
+            const double add = nf * Mp + (3 * nf - 1) * NMT;
+            if (g1 > g0 && 4.0 * Kp * (rows + add) > budget) break;
+            rows += add;
+            ++g1;
+        }
+        // common K stride: the largest case of the group (the group is in K order)
+        const int Kmax = g_batch[order[g1 - 1]].K;
+        const int Kp = ((Kmax + kBK - 1) / kBK) * kBK;
+        std::vector<CaseP> cp(g1 - g0);
+        std::vector<BItem> items;
+        long long urows = 0, grows = 0, srows = 0, hg = 0, hs = 0, parts = 0;
+        for (size_t k = g0; k < g1; ++k) {
+            const BatchCase &c = g_batch[order[k]];
+            CaseP &q = cp[k - g0];
+            const int nf = (int)c.f.size();
+            q.nf = nf;
+            q.nm = c.nme;
+            q.Mp = ((c.nme * c.nme + kBM - 1) / kBM) * kBM;
+            q.MT = q.Mp / kBM;
+            q.nk = ((c.K + kBK - 1) / kBK);
+            q.ks_last = (c.K - (q.nk - 1) * kBK + 15) / 16;
+            q.n_ntiles = (nf + (kBN / NMT) - 1) / (kBN / NMT);
+            const bool scalar = c.set.scalar != 0 ||
+                                (c.set.test == 0 && c.set.ibisp && (long long)nf * nf * c.nme * c.nme * c.nme > 1000000000LL);
+            q.wmode = scalar ? kWeightUniform : kWeightClassicVect;
+            double delta = c.f[1] - c.f[0];
+            if (c.set.defsc == 1) delta *= kPi2;
+            q.wval = delta * delta;
+            q.u_row0 = (int)urows;
+            q.g_row0 = (int)grows;
+            q.s_row0 = (int)srows;
+            q.hg0 = (int)hg;
+            q.hs0 = (int)hs;
+            q.part0 = parts;
+            q.nitems = (unsigned)(nf * q.MT);
+            urows += (long long)nf * q.Mp;
+            grows += (long long)nf * NMT;
+            srows += (long long)(2 * nf - 1) * NMT;
+            hg += (long long)nf * NMT;
+            hs += (long long)(2 * nf - 1) * NMT;
+            parts += (long long)kKinds * NMT * q.Mp;
+            for (int r = 0; r < nf; ++r)
+                for (int mt = 0; mt < q.MT; ++mt) items.push_back(BItem{(int)(k - g0), r, mt, 0});
+        }
+        if (urows > 0x7fffffffLL || srows > 0x7fffffffLL) return fail(BSA_ERR_ARG, "batch group too large");
+        const size_t uel = (size_t)urows * Kp, gel = (size_t)grows * Kp, sel = (size_t)srows * Kp;
+        if ((e = dMixA.reserve(2 * uel * 2)) || (e = dMixB.reserve(2 * (gel + sel) * 2)) ||
+            (e = dMixH.reserve(sizeof(float2) * (size_t)(hg + hs) + 256)) ||
+            (e = dMixPart.reserve(sizeof(double) * (size_t)parts + 4096)) ||
+            (e = dMshIdx.reserve(sizeof(CaseP) * cp.size() + sizeof(BItem) * items.size() +
+                                 (sizeof(unsigned) + 2 * sizeof(unsigned long long) + sizeof(long long)) * cp.size() + 1024)) ||
+            (e = dMshT.reserve(sizeof(double) * 3 * (size_t)t2 + 64)))
+            return cuda_fail(e, "allocating batch operands");
+        __nv_bfloat16 *Uh = dMixA.as<__nv_bfloat16>(), *Ul = Uh + uel;
+        __nv_bfloat16 *Gh = dMixB.as<__nv_bfloat16>(), *Gl = Gh + gel, *Sh = Gl + gel, *Sl = Sh + sel;
+        float2 *Hg = dMixH.as<float2>(), *Hs = Hg + hg;
+        double *part = dMixPart.as<double>();
+        int *derr = (int *)(part + parts);
+        char *ib = (char *)dMshIdx.p;
+        CaseP *d_cases = (CaseP *)ib;
+        BItem *d_items = (BItem *)(((uintptr_t)(d_cases + cp.size()) + 15) & ~(uintptr_t)15);
+        unsigned *d_cnt = (unsigned *)(d_items + items.size());
+        unsigned long long *d_tdone = (unsigned long long *)(((uintptr_t)(d_cnt + cp.size()) + 15) & ~(uintptr_t)15);
+        unsigned long long *d_tstart = d_tdone + cp.size();
+        long long *d_off = (long long *)(d_tstart + 1);
+        double *d_m2 = dMshT.as<double>();
+        if ((e = cudaEventRecord(ev2, stream))) return cuda_fail(e, "event");
+        if ((e = cudaMemsetAsync(part, 0, sizeof(double) * (size_t)parts + sizeof(int), stream)) ||
+            (e = cudaMemsetAsync(d_cnt, 0, sizeof(unsigned) * cp.size(), stream)) ||
+            (e = cudaMemsetAsync(d_tdone, 0, sizeof(unsigned long long) * (cp.size() + 1), stream)))
+            return cuda_fail(e, "batch memset");
+        // per case: its tables, A(f) in FP32, operands into the group tables, m2
+        for (size_t k = g0; k < g1; ++k) {
+            const BatchCase &c = g_batch[order[k]];
+            const CaseP &q = cp[k - g0];
+            batch_install(c);
+            if ((rc = upload_problem())) return rc;
+            const int nf = q.nf;
+            std::vector<double> ftab = c.f;
+            if (!c.trunc)
+                for (int s = 0; s < 2 * nf - 1; ++s) ftab.push_back(2.0 * c.f[0] + s * (c.f[1] - c.f[0]));
+            if ((rc = build_atable(ftab, true))) return rc;
+            const float *A = dA32.as<float>();
+            if ((e = mixed::prep_u(stream, nf, c.nme, c.K, Kp, q.Mp, A, dQ.as<double>(), Uh + (size_t)q.u_row0 * Kp,
+                                   Ul + (size_t)q.u_row0 * Kp)) ||
+                (e = mixed::prep_b(stream, nf, c.nme, NMT, c.K, Kp, nf, (nf - 1) / 2, c.trunc ? 1 : 0, nf, 0, A,
+                                   Gh + (size_t)q.g_row0 * Kp, Gl + (size_t)q.g_row0 * Kp)) ||
+                (e = mixed::prep_b(stream, 2 * nf - 1, c.nme, NMT, c.K, Kp, nf, (nf - 1) / 2, c.trunc ? 1 : 0, nf, 1,
+                                   A, Sh + (size_t)q.s_row0 * Kp, Sl + (size_t)q.s_row0 * Kp)) ||
+                (e = mixed::prep_h(stream, nf, c.nme, NMT, dFreq.as<double>(), frf(), Hg + q.hg0, Hs + q.hs0)))
+                return cuda_fail(e, "batch operand preparation");
+            // second-order moments (FP64 over the FP32 A table), rectangle or trapezoid weights
+            double delta = c.f[1] - c.f[0];
+            if (c.set.defsc == 1) delta *= kPi2;
+            std::vector<double> wf(nf, delta);
+            if (q.wmode == kWeightClassicVect) { wf[0] = delta / 2; wf[nf - 1] = delta / 2; }
+            const int nm2 = c.nme * c.nme;
+            if ((e = upload(dWf, wf, stream)) || (e = dPsdF.reserve(sizeof(double) * (size_t)nf * nm2)))
+                return cuda_fail(e, "batch m2");
+            double *m2o = d_m2 + 3 * off2[order[k]];
+            if ((e = launch_force_psd32(stream, nf, (int)c.set.tc.size(), c.nnl, c.nme, dL.as<double>(), A,
+                                        dPsdF.as<double>())) ||
+                (e = launch_m2(stream, 0, nf, c.nme, 0, dFreq.as<double>(), dWf.as<double>(), dPsdF.as<double>(), frf(),
+                               m2o, m2o + nm2, m2o + 2 * nm2)))
+                return cuda_fail(e, "batch m2");
+            kernels += 7;
+        }
+        std::vector<long long> offs(cp.size());
+        for (size_t k = g0; k < g1; ++k) offs[k - g0] = off3[order[k]];
+        if ((e = cudaMemcpyAsync(d_cases, cp.data(), sizeof(CaseP) * cp.size(), cudaMemcpyHostToDevice, stream)) ||
+            (e = cudaMemcpyAsync(d_items, items.data(), sizeof(BItem) * items.size(), cudaMemcpyHostToDevice, stream)) ||
+            (e = cudaMemcpyAsync(d_off, offs.data(), sizeof(long long) * offs.size(), cudaMemcpyHostToDevice, stream)))
+            return cuda_fail(e, "batch tables");
+        CUtensorMap maps[6];
+        const int BROWS = (kBN / NMT) * NMT;
+        if (!make_map(&maps[0], Uh, Kp, (uint64_t)urows, kBM) || !make_map(&maps[1], Ul, Kp, (uint64_t)urows, kBM) ||
+            !make_map(&maps[2], Gh, Kp, (uint64_t)grows, BROWS) || !make_map(&maps[3], Gl, Kp, (uint64_t)grows, BROWS) ||
+            !make_map(&maps[4], Sh, Kp, (uint64_t)srows, BROWS) || !make_map(&maps[5], Sl, Kp, (uint64_t)srows, BROWS))
+            return fail(BSA_ERR_CUDA, "cuTensorMapEncodeTiled failed");
+        BParams prm{d_items, (int)items.size(), d_cases, Hg, Hs, part, d_cnt, d_tdone, d_tstart, derr};
+        const size_t smem = (size_t)kStages * kStageBytes + 1024 + 256;
+        const int grid = (int)std::min<long long>((long long)items.size(), nsm);
+        if ((e = cudaEventRecord(evg0, stream))) return cuda_fail(e, "event");
+        switch (NMT) {
+        case 8:
+            cudaFuncSetAttribute(k_bfm_batch<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            k_bfm_batch<8><<<grid, 192, smem, stream>>>(maps[0], maps[1], maps[2], maps[3], maps[4], maps[5], prm);
+            break;
+        case 16:
+            cudaFuncSetAttribute(k_bfm_batch<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            k_bfm_batch<16><<<grid, 192, smem, stream>>>(maps[0], maps[1], maps[2], maps[3], maps[4], maps[5], prm);
+            break;
+        case 24:
+            cudaFuncSetAttribute(k_bfm_batch<24>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            k_bfm_batch<24><<<grid, 192, smem, stream>>>(maps[0], maps[1], maps[2], maps[3], maps[4], maps[5], prm);
+            break;
+        default:
+            cudaFuncSetAttribute(k_bfm_batch<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            k_bfm_batch<32><<<grid, 192, smem, stream>>>(maps[0], maps[1], maps[2], maps[3], maps[4], maps[5], prm);
+            break;
+        }
+        if ((e = cudaGetLastError())) return cuda_fail(e, "batched tcgen05 contraction kernel");
+        if ((e = cudaEventRecord(evg1, stream))) return cuda_fail(e, "event");
+        // reduce into the case-ordered output (device copy of the whole output, rows of this group)
+        if ((e = dOut.reserve(sizeof(double) * 2 * (size_t)t3))) return cuda_fail(e, "out");
+        double *o = dOut.as<double>();
+        int maxnm3 = 1;
+        for (const CaseP &q : cp) maxnm3 = std::max(maxnm3, q.nm * q.nm * q.nm);
+        dim3 rg((maxnm3 + 127) / 128, (unsigned)cp.size());
+        switch (NMT) {
+        case 8: k_batch_reduce<8><<<rg, 128, 0, stream>>>(d_cases, d_off, part, o, o + t3); break;
+        case 16: k_batch_reduce<16><<<rg, 128, 0, stream>>>(d_cases, d_off, part, o, o + t3); break;
+        case 24: k_batch_reduce<24><<<rg, 128, 0, stream>>>(d_cases, d_off, part, o, o + t3); break;
+        default: k_batch_reduce<32><<<rg, 128, 0, stream>>>(d_cases, d_off, part, o, o + t3); break;
+        }
+        if ((e = cudaGetLastError())) return cuda_fail(e, "batch reduction");
+        kernels += 2;
+        std::vector<unsigned long long> td(cp.size() + 1);
+        int herr = 0;
+        if ((e = cudaMemcpyAsync(td.data(), d_tdone, sizeof(unsigned long long) * (cp.size() + 1), cudaMemcpyDeviceToHost,
+                                 stream)) ||
+            (e = cudaMemcpyAsync(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost, stream)) ||
+            (e = cudaEventRecord(ev1, stream)) || (e = cudaStreamSynchronize(stream)))
+            return cuda_fail(e, "batch run");
+        if (herr) return fail(BSA_ERR_TIMEOUT, "batched kernel: a pipeline wait ran out of its budget (role %d)", herr);
+        // results of this group: moments and m2 of its cases
+        for (size_t k = g0; k < g1; ++k) {
+            const int c = order[k];
+            const long long n3 = (long long)g_batch[c].nme * g_batch[c].nme * g_batch[c].nme;
+            const long long n2 = (long long)g_batch[c].nme * g_batch[c].nme;
+            if ((e = cudaMemcpy(h3f.data() + off3[c], o + off3[c], sizeof(double) * n3, cudaMemcpyDeviceToHost)) ||
+                (e = cudaMemcpy(h3r.data() + off3[c], o + t3 + off3[c], sizeof(double) * n3, cudaMemcpyDeviceToHost)) ||
+                (e = cudaMemcpy(h2.data() + 3 * off2[c], d_m2 + 3 * off2[c], sizeof(double) * 3 * n2,
+                                cudaMemcpyDeviceToHost)))
+                return cuda_fail(e, "batch results");
+            lat[c] = (double)(td[k - g0] - td[cp.size()]) * 1e-6;  // ms from the launch start
+        }
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, ev2, ev1);
+        total += ms;
+        g0 = g1;
+    }
+    for (int c = 0; c < nc; ++c) {
+        const long long n3 = (long long)g_batch[c].nme * g_batch[c].nme * g_batch[c].nme;
+        const long long n2 = (long long)g_batch[c].nme * g_batch[c].nme;
+        if (m3mf) std::memcpy(m3mf + off3[c], h3f.data() + off3[c], sizeof(double) * n3);
+        if (m3mr) std::memcpy(m3mr + off3[c], h3r.data() + off3[c], sizeof(double) * n3);
+        if (m2mr) std::memcpy(m2mr + off2[c], h2.data() + 3 * off2[c] + n2, sizeof(double) * n2);
+        if (case_ms) case_ms[c] = lat[c];
+    }
+    if (total_ms) *total_ms = total;
+    last_ms = total;
+    return BSA_OK;
+}
+
+}  // namespace bsa
+
+using bsa::eng;
+
+extern "C" {
+
+int bsa_gpu_batchAdd(int *case_id) {
+    bsa::Engine &E = eng();
+    if (E.halted) return BSA_ERR_STATE;
+    return E.batch_add(case_id);
+}
+
+int bsa_gpu_batchCase(int c, int *nm, int *nf) {
+    if (c < 0 || c >= (int)bsa::g_batch.size()) return BSA_ERR_ARG;
+    if (nm) *nm = bsa::g_batch[c].nme;
+    if (nf) *nf = (int)bsa::g_batch[c].f.size();
+    return BSA_OK;
+}
+
+int bsa_gpu_batchRun(double *m3mf, double *m3mr, double *m2mr, double *case_ms, double *total_ms) {
+    bsa::Engine &E = eng();
+    if (E.halted) return BSA_ERR_STATE;
+    return E.batch_run(m3mf, m3mr, m2mr, case_ms, total_ms);
+}
+
+int bsa_gpu_batchClear(void) {
+    bsa::g_batch.clear();
+    return BSA_OK;
+}
+
+}  // extern "C"

@@ -57,6 +57,8 @@ struct Settings {
     std::vector<int> tc{1};
 };
 
+struct BatchCase;  // one case of the batched Classic sweep (bsa_batch.cu)
+
 struct Engine {
     Inputs in;
     Settings set;
@@ -135,6 +137,9 @@ struct Engine {
     int mesher_zones(std::vector<ZoneDev> &zones, std::vector<int> &policy);
     int run_mesher(double *m3mf, double *m3mr);
     int br_decomp(const double *m2mf, double *bkg, double *res);
+    int batch_add(int *id);
+    void batch_install(const BatchCase &c);
+    int batch_run(double *m3mf, double *m3mr, double *m2mr, double *case_ms, double *total_ms);
 };
 
 Engine &eng();

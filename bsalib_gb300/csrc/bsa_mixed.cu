@@ -412,6 +412,24 @@ __global__ void k_mixed_reduce(int nm, int NMT, int MT, int grid, const double *
     m3mf[x] = 2.0 * mf;
 }
 
+cudaError_t prep_u(cudaStream_t st, int nf, int nm, int K, int Kp, int Mp, const float *A, const double *Q,
+                   __nv_bfloat16 *Uh, __nv_bfloat16 *Ul) {
+    k_prep_u<<<dim3(nf, Kp / 64), 256, 0, st>>>(nm, K, Kp, Mp, A, Q, Uh, Ul);
+    return cudaGetLastError();
+}
+
+cudaError_t prep_b(cudaStream_t st, int rows, int nm, int NMT, int K, int Kp, int nf, int n_pad, int trunc,
+                   int sum_base, int is_sum, const float *A, __nv_bfloat16 *Th, __nv_bfloat16 *Tl) {
+    k_prep_b<<<dim3(rows, Kp / 64), 256, 0, st>>>(nm, NMT, K, Kp, nf, n_pad, trunc, sum_base, is_sum, A, Th, Tl);
+    return cudaGetLastError();
+}
+
+cudaError_t prep_h(cudaStream_t st, int nf, int nm, int NMT, const double *f, FrfPar frf, float2 *Hg, float2 *Hs) {
+    const int nh = (nf + 2 * nf - 1) * NMT;
+    k_prep_h<<<(nh + 255) / 256, 256, 0, st>>>(nf, nm, NMT, f, frf, Hg, Hs);
+    return cudaGetLastError();
+}
+
 template <int NMT>
 static cudaError_t launch_gemm(cudaStream_t st, const CUtensorMap *maps, const Params &p, int grid) {
     const size_t smem = (size_t)kStages * kStageBytes + 1024 + 256;

@@ -214,6 +214,24 @@ int bsa_gpu_setClassicRows(int r_begin, int r_end);
  * summation order; materialised or exported bispectra always cover the full grid. */
 int bsa_gpu_setClassicSymmetry(int on);
 
+/* Batched Classic sweep: many independent analyses (structures, wind cases) evaluated by one
+ * split-precision tensor-core launch per group of cases.  The reference runs one analysis per
+ * process (app/bsa.F90:72-110: setup, bsa_Run, finalise); a parametric study repeats that.
+ *
+ * bsa_gpu_batchAdd snapshots the current inputs as case *case_id (validated as by bsa_Run;
+ * full-tensor spectra, at most 32 kept modes); the caller may then change any input and add
+ * the next case.  bsa_gpu_batchRun evaluates every case added since the last
+ * bsa_gpu_batchClear on its full Classic grid (the split precision of bsa_gpu_setPrecision's
+ * BSA_PREC_BF16X3, whatever the current precision) and writes, concatenated in case order,
+ * m3mf / m3mr (nm_c^3 each) and m2mr (nm_c^2 each); case_ms[c] is the time from the start of
+ * the contraction launch of the case's group to the completion of case c, total_ms the
+ * device time of the whole sweep.  Any output may be NULL.  The current inputs are left as
+ * they were.  bsa_gpu_batchCase reports a case's kept modes and grid size. */
+int bsa_gpu_batchAdd(int *case_id);
+int bsa_gpu_batchCase(int case_id, int *nm, int *nf);
+int bsa_gpu_batchRun(double *m3mf, double *m3mr, double *m2mr, double *case_ms, double *total_ms);
+int bsa_gpu_batchClear(void);
+
 /* getBFMClsVect + getBRMClsVect materialised (functionsImpl.F90:1312-1738): force and
  * response bispectra on the classic grid, (nf, nf, dim_bisp) with f1 fastest, and the grid.
  * Runs validation and the grid set-up of bsa_Run; for small grids (tests). */

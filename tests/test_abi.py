@@ -28,3 +28,13 @@ def test_exports_are_plain_c(bsalib):
 def test_library_is_sm103a_only(bsalib):
     from bsalib_gb300 import build
     assert "arch=compute_103a,code=sm_103a" in " ".join(build.ARCH)
+
+
+def test_batch_host_checks(bsalib):
+    # host-side checks of the batched sweep, before any device work
+    assert bsalib.bsa_gpu_batchClear() == 0
+    nm, nf = ctypes.c_int(0), ctypes.c_int(0)
+    assert bsalib.bsa_gpu_batchCase(-1, ctypes.byref(nm), ctypes.byref(nf)) == -1
+    assert bsalib.bsa_gpu_batchCase(0, ctypes.byref(nm), ctypes.byref(nf)) == -1
+    assert bsalib.bsa_gpu_batchRun(None, None, None, None, None) == -2
+    assert b"empty batch" in bsalib.bsa_lastError()

@@ -1,0 +1,138 @@
+"""The batched Classic sweep (bsa_gpu_batch*) against one bsa_Run per case.
+
+Each case of a batch must give the moments its own split-precision analysis gives: the same
+FP32 partials are summed in FP64 in another order, so third moments agree to 1e-9 relative
+(max-norm), second moments to 1e-12.  Against the FP64 path the mixed-precision bar holds
+(third moments 1e-4 relative).  Cases of every FRF-table width (8, 16, 24, 32 kept modes),
+different grids and load sizes share one batch; the library's own inputs are left as they
+were.
+"""
+import copy
+
+import numpy as np
+import pytest
+
+from bsalib_gb300 import api
+from bsalib_gb300.problem import cantilever_tower, random_structure, tall_building
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+def single(prob, prec):
+    s = api.BsaSession(prob, precision=prec)
+    try:
+        return s.run()
+    finally:
+        s.close()
+
+
+CASES = [
+    cantilever_tower(nfreqs=17, df=0.25, nodes=30),
+    tall_building(nodes=64, modes=12, nfreqs=21, df=0.2, seed=3),
+    tall_building(nodes=100, modes=24, nfreqs=25, df=0.16, seed=5),
+    tall_building(nodes=50, modes=30, nfreqs=9, df=0.5, seed=8),
+    random_structure(11, nodes=(60, 60), modes=(7, 7), nfreq_grid=(65, 65)),
+    random_structure(12, nodes=(230, 230), modes=(16, 16), nfreq_grid=(129, 129)),
+    random_structure(13, nodes=(40, 40), modes=(5, 5), nfreq_grid=(33, 33)),
+    random_structure(14, nodes=(150, 150), modes=(20, 20), nfreq_grid=(97, 97)),
+]
+
+
+@pytest.fixture(scope="module")
+def batch(bsalib):
+    sw = api.Sweep()
+    for p in CASES:
+        sw.add(p)
+    out, total = sw.run()
+    sw.clear()
+    return out, total
+
+
+def test_batch_matches_single_analyses(batch):
+    out, _ = batch
+    assert len(out) == len(CASES)
+    for k, p in enumerate(CASES):
+        ref = single(p, api.PREC_BF16X3)
+        assert out[k]["nm"] ** 3 == ref["m3mr_cls"].size
+        assert rel(out[k]["m3mr"], ref["m3mr_cls"]) < 1e-9, k
+        assert rel(out[k]["m3mf"], ref["m3mf_cls"]) < 1e-9, k
+        assert rel(out[k]["m2mr"], ref["m2mr_cls"]) < 1e-12, k
+
+
+def test_batch_within_mixed_bar_of_fp64(batch):
+    out, _ = batch
+    for k in (1, 3, 5):
+        ref = single(CASES[k], api.PREC_FP64)
+        assert rel(out[k]["m3mr"], ref["m3mr_cls"]) < 1e-4, k
+        assert rel(out[k]["m3mf"], ref["m3mf_cls"]) < 1e-4, k
+
+
+def test_batch_latencies(batch):
+    out, total = batch
+    ms = np.array([o["ms"] for o in out])
+    assert np.all(ms > 0.0)
+    assert np.all(ms <= total)
+
+
+def test_batch_wind_cases_of_one_structure(bsalib):
+    # one structure under three mean wind speeds: the same modes, different forces
+    probs = [random_structure(21, nodes=(120, 120), modes=(10, 10), nfreq_grid=(65, 65), U_mean=u)
+             for u in (20.0, 30.0, 45.0)]
+    sw = api.Sweep()
+    for p in probs:
+        sw.add(p)
+    out, _ = sw.run()
+    sw.clear()
+    for k, p in enumerate(probs):
+        ref = single(p, api.PREC_BF16X3)
+        assert rel(out[k]["m3mr"], ref["m3mr_cls"]) < 1e-9
+    v = [float(np.max(np.abs(o["m3mr"]))) for o in out]
+    assert v[0] < v[1] < v[2]
+
+
+def test_batch_leaves_current_inputs(bsalib):
+    p = tall_building(nodes=64, modes=12, nfreqs=21, df=0.2, seed=3)
+    s = api.BsaSession(p, precision=api.PREC_FP64)
+    try:
+        before = s.run()
+        sw = api.Sweep()
+        sw.add_current()
+        other = copy.deepcopy(CASES[2])
+        # a case set up through the setters of the same library instance
+        s2 = api.BsaSession(other, precision=api.PREC_BF16X3)
+        sw.add_current()
+        s2.close()
+        s = api.BsaSession(p, precision=api.PREC_FP64)
+        sw.run()
+        after = s.run()
+        sw.clear()
+    finally:
+        s.close()
+    assert rel(after["m3mr_cls"], before["m3mr_cls"]) < 1e-12
+    assert rel(after["m2mr_cls"], before["m2mr_cls"]) < 1e-12
+
+
+def test_batch_rejects_unsupported_cases(bsalib):
+    sw = api.Sweep()
+    big = tall_building(nodes=60, modes=36, nfreqs=9, df=0.5, seed=2)
+    s = api.BsaSession(big, precision=api.PREC_BF16X3)
+    try:
+        if s.nmodes() > 32:
+            with pytest.raises(api.BsaError, match="32 kept modes"):
+                sw.add_current()
+    finally:
+        s.close()
+    d = copy.deepcopy(CASES[1])
+    d.settings.onlyd = 1
+    s = api.BsaSession(d, precision=api.PREC_BF16X3)
+    try:
+        with pytest.raises(api.BsaError, match="full-tensor"):
+            sw.add_current()
+    finally:
+        s.close()
+    with pytest.raises(api.BsaError, match="empty batch"):
+        sw.run()
