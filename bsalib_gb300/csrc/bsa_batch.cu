@@ -22,6 +22,7 @@
 
 #include "../../include/bsa_gpu.h"
 #include "bsa_engine.cuh"
+#include "bsa_epi.cuh"
 #include "bsa_kernels.cuh"
 #include "bsa_mixed.cuh"
 #include "bsa_tc.cuh"
@@ -35,6 +36,9 @@ constexpr int kStages = 2;
 constexpr int kStageBytes = 6 * kTileBytes;
 constexpr int kKinds = 5;  // mr1, mr3, mr2, mf1, mf23
 constexpr int kFlushTiles = 64;
+constexpr int kBarBytes = 256;                              // mbarriers + TMEM slot
+constexpr int kHBytes = 4 * 2 * (int)sizeof(epi::HTile);   // FRF staging, 2 tiles per epilogue warp
+constexpr size_t kSmem = (size_t)kStages * kStageBytes + 1024 + kBarBytes + kHBytes;
 
 struct CaseP {
     int nf, nm, Mp, MT, nk, ks_last, n_ntiles, wmode;
@@ -62,17 +66,6 @@ struct BParams {
     unsigned long long *t_start;  // launch start (global timer, ns)
     int *err;
 };
-
-__device__ __forceinline__ float2 cmul(float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
-__device__ __forceinline__ float2 conjf2(float2 a) { return make_float2(a.x, -a.y); }
-
-__device__ __forceinline__ float case_weight(const CaseP &cs, int r, int c) {
-    if (cs.wmode == kWeightClassicVect) {
-        const bool b1 = (r == 0 || r == cs.nf - 1), b2 = (c == 0 || c == cs.nf - 1);
-        return (float)(cs.wval * ((b1 && b2) ? -0.5 : ((b1 || b2) ? 0.5 : 1.0)));
-    }
-    return (float)cs.wval;
-}
 
 template <int NMT>
 __global__ void __launch_bounds__(192, 1)
@@ -207,9 +200,15 @@ __global__ void __launch_bounds__(192, 1)
         const int quarter = warp & 3;
         const int row = quarter * 32 + lane;
         const uint32_t lane_base = tmem + ((uint32_t)(quarter * 32) << 16);
+        epi::HTile *hbw = (epi::HTile *)(smem + kStages * kStageBytes + kBarBytes) + quarter * 2;
         float acc[kKinds][NMT];
         uint32_t tile = 0;
         bool ok = true;
+        if (blockIdx.x < p.nitems) {
+            const BItem i0 = p.items[blockIdx.x];
+            const CaseP s0 = p.cases[i0.c];
+            epi::stage<NMT>(hbw, p.Hg + s0.hg0, p.Hs + s0.hs0, s0.nf, i0.r, 0, lane);
+        }
         for (int w = blockIdx.x; w < p.nitems && ok; w += gridDim.x) {
             const BItem im = p.items[w];
             const CaseP cs = p.cases[im.c];
@@ -218,75 +217,30 @@ __global__ void __launch_bounds__(192, 1)
             const bool vrow = grow < cs.nm * cs.nm;
             const int a = vrow ? grow / cs.nm : 0, b = vrow ? grow % cs.nm : 0;
             const float2 *Hg = p.Hg + cs.hg0, *Hs = p.Hs + cs.hs0;
+            const float wvf = (float)cs.wval;
+            const bool vect = cs.wmode == kWeightClassicVect, b1 = (r == 0 || r == cs.nf - 1);
             double *part = p.part + cs.part0 + grow;
 #pragma unroll
             for (int k = 0; k < kKinds; ++k)
 #pragma unroll
                 for (int j = 0; j < NMT; ++j) acc[k][j] = 0.f;
-            const float2 hra = Hg[r * NMT + a];
             for (int nt = 0; nt < cs.n_ntiles; ++nt, ++tile) {
                 const int buf = tile & 1;
                 const uint32_t tph = (tile >> 1) & 1u;
+                epi::cp_async_wait_all();
+                __syncwarp();
+                // stage the next tile: this item's next one, or the first of the CTA's next item
+                if (nt + 1 < cs.n_ntiles) {
+                    epi::stage<NMT>(hbw + (buf ^ 1), Hg, Hs, cs.nf, r, (nt + 1) * NC, lane);
+                } else if (w + (int)gridDim.x < p.nitems) {
+                    const BItem in = p.items[w + gridDim.x];
+                    const CaseP sn = p.cases[in.c];
+                    epi::stage<NMT>(hbw + (buf ^ 1), p.Hg + sn.hg0, p.Hs + sn.hs0, sn.nf, in.r, 0, lane);
+                }
                 const bool got = __all_sync(0xffffffffu, mbar_wait(&tfull[buf], tph, err, 4));
                 if (!got) { ok = false; break; }
                 fence_after();
-                const int c0 = nt * NC;
-#pragma unroll
-                for (int q = 0; q < kBN / 32; ++q) {
-#pragma unroll
-                    for (int pass = 0; pass < 2; ++pass) {
-                        uint32_t v[32];
-                        tmem_ld32(lane_base + buf * 256 + pass * 128 + q * 32, v);
-                        tmem_wait_ld();
-                        float2 PA = make_float2(0.f, 0.f), PB = PA;
-                        float wc = 0.f;
-                        bool cval = false;
-                        int cg = 0, sidx = 0;
-#pragma unroll
-                        for (int e = 0; e < 32; ++e) {
-                            const int col = q * 32 + e;
-                            const int c = col / NMT, j = col % NMT;
-                            if (c >= NC) continue;
-                            if (j == 0 || e == 0) {
-                                cg = c0 + c;
-                                cval = cg < cs.nf;
-                                if (cval) {
-                                    sidx = r + cg;
-                                    wc = case_weight(cs, r, cg);
-                                    const float2 hcb = Hg[cg * NMT + b];
-                                    if (pass == 0) {
-                                        const float2 t1 = cmul(hra, hcb);
-                                        PA = make_float2(wc * t1.x, wc * t1.y);
-                                    } else {
-                                        const float2 hsa = Hs[sidx * NMT + a];
-                                        const float2 hsb = Hs[sidx * NMT + b];
-                                        const float2 t3 = cmul(hcb, conjf2(hsa));
-                                        PA = make_float2(wc * t3.x, wc * t3.y);
-                                        const float2 t2 = cmul(hra, conjf2(hsb));
-                                        PB = make_float2(wc * t2.x, wc * t2.y);
-                                    }
-                                }
-                            }
-                            if (cval && j < cs.nm) {
-                                const float x = __uint_as_float(v[e]);
-                                if (pass == 0) {
-                                    const float2 hs = Hs[sidx * NMT + j];
-                                    const float F1 = PA.x * hs.x + PA.y * hs.y;
-                                    acc[0][j] = fmaf(F1, x, acc[0][j]);
-                                    acc[3][j] = fmaf(wc, x, acc[3][j]);
-                                } else {
-                                    const float2 hr = Hg[r * NMT + j];
-                                    const float2 hc = Hg[cg * NMT + j];
-                                    const float F3 = hr.x * PA.x - hr.y * PA.y;
-                                    const float F2 = hc.x * PB.x - hc.y * PB.y;
-                                    acc[1][j] = fmaf(F3, x, acc[1][j]);
-                                    acc[2][j] = fmaf(F2, x, acc[2][j]);
-                                    acc[4][j] = fmaf(wc, x, acc[4][j]);
-                                }
-                            }
-                        }
-                    }
-                }
+                epi::tile<NMT>(hbw[buf], lane_base + buf * 256, a, b, nt * NC, cs.nf, vect, b1, wvf, acc);
                 fence_before();
                 mbar_arrive(&tempty[buf]);
                 if ((nt + 1) % kFlushTiles == 0 || nt + 1 == cs.n_ntiles) {
@@ -310,6 +264,7 @@ __global__ void __launch_bounds__(192, 1)
                 if (old + 1 == 4u * cs.nitems) p.t_done[im.c] = gtime();
             }
         }
+        epi::cp_async_wait_all();
     }
     fence_before();
     __syncthreads();
@@ -445,7 +400,7 @@ int Engine::batch_run(double *m3mf, double *m3mr, double *m2mr, double *case_ms,
     } restore{*this, saved, saved_in, saved_ok};
     std::vector<double> h3f(t3), h3r(t3), h2(t2 * 3);
     std::vector<double> lat(nc, 0.0);
-    double total = 0.0;
+    double total = 0.0, gemm = 0.0, points = 0.0;
     const double budget = 24e9;
     size_t g0 = 0;
     while (g0 < order.size()) {
@@ -564,7 +519,7 @@ int Engine::batch_run(double *m3mf, double *m3mr, double *m2mr, double *case_ms,
                 (e = launch_m2(stream, 0, nf, c.nme, 0, dFreq.as<double>(), dWf.as<double>(), dPsdF.as<double>(), frf(),
                                m2o, m2o + nm2, m2o + 2 * nm2)))
                 return cuda_fail(e, "batch m2");
-            kernels += 7;
+            kernels += 6;
         }
         std::vector<long long> offs(cp.size());
         for (size_t k = g0; k < g1; ++k) offs[k - g0] = off3[order[k]];
@@ -579,7 +534,7 @@ int Engine::batch_run(double *m3mf, double *m3mr, double *m2mr, double *case_ms,
             !make_map(&maps[4], Sh, Kp, (uint64_t)srows, BROWS) || !make_map(&maps[5], Sl, Kp, (uint64_t)srows, BROWS))
             return fail(BSA_ERR_CUDA, "cuTensorMapEncodeTiled failed");
         BParams prm{d_items, (int)items.size(), d_cases, Hg, Hs, part, d_cnt, d_tdone, d_tstart, derr};
-        const size_t smem = (size_t)kStages * kStageBytes + 1024 + 256;
+        const size_t smem = kSmem;
         const int grid = (int)std::min<long long>((long long)items.size(), nsm);
         if ((e = cudaEventRecord(evg0, stream))) return cuda_fail(e, "event");
         switch (NMT) {
@@ -639,6 +594,9 @@ int Engine::batch_run(double *m3mf, double *m3mr, double *m2mr, double *case_ms,
         float ms = 0.f;
         cudaEventElapsedTime(&ms, ev2, ev1);
         total += ms;
+        cudaEventElapsedTime(&ms, evg0, evg1);
+        gemm += ms;
+        for (const CaseP &q : cp) points += (double)q.nf * q.nf;
         g0 = g1;
     }
     for (int c = 0; c < nc; ++c) {
@@ -651,6 +609,9 @@ int Engine::batch_run(double *m3mf, double *m3mr, double *m2mr, double *case_ms,
     }
     if (total_ms) *total_ms = total;
     last_ms = total;
+    last_ms_contraction = total;
+    last_ms_gemm = gemm;
+    last_points = points;
     return BSA_OK;
 }
 

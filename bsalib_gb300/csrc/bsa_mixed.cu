@@ -32,6 +32,7 @@
 
 #include "../../include/bsa_gpu.h"
 #include "bsa_engine.cuh"
+#include "bsa_epi.cuh"
 #include "bsa_tc.cuh"
 
 namespace bsa {
@@ -43,6 +44,8 @@ constexpr int kStages = 2;
 constexpr int kStageBytes = 6 * kTileBytes;      // U hi/lo, Bg hi/lo, Bs hi/lo
 constexpr int kKinds = 5;                        // mr1, mr3, mr2, mf1, mf23
 constexpr int kFlushTiles = 64;                  // FP32 -> FP64 flush period (N tiles)
+constexpr int kBarBytes = 256;                   // mbarriers + TMEM slot
+constexpr int kHBytes = 4 * 2 * (int)sizeof(epi::HTile);  // FRF staging, 2 tiles per epilogue warp
 
 struct Params {
     int nf;          // grid size
@@ -62,15 +65,6 @@ struct Params {
     int *err;
 };
 
-
-__device__ __forceinline__ float point_weight(const Params &p, int r, int c) {
-    if (p.wmode == kWeightClassicVect) {
-        const bool b1 = (r == 0 || r == p.nf - 1), b2 = (c == 0 || c == p.nf - 1);
-        const double m = r < p.sym_rows ? 2.0 : 1.0;
-        return (float)(m * p.wval * ((b1 && b2) ? -0.5 : ((b1 || b2) ? 0.5 : 1.0)));
-    }
-    return (float)(r < p.sym_rows ? 2.0 * p.wval : p.wval);
-}
 
 template <int NMT>
 __global__ void __launch_bounds__(192, 1)
@@ -212,6 +206,9 @@ __global__ void __launch_bounds__(192, 1)
         const bool vrow = grow < p.nm * p.nm;
         const int a = vrow ? grow / p.nm : 0, b = vrow ? grow % p.nm : 0;
         const uint32_t lane_base = tmem + ((uint32_t)(quarter * 32) << 16);
+        const float wvf = (float)p.wval;
+        const bool vect = p.wmode == kWeightClassicVect;
+        epi::HTile *hbw = (epi::HTile *)(smem + kStages * kStageBytes + kBarBytes) + quarter * 2;
         double *part = p.part + (size_t)blockIdx.x * kKinds * NMT * 128 + row;
         for (int k = 0; k < kKinds * NMT; ++k) part[(size_t)k * 128] = 0.0;
         float acc[kKinds][NMT];
@@ -230,81 +227,32 @@ __global__ void __launch_bounds__(192, 1)
         };
         uint32_t tile = 0;
         bool ok = true;
+        if (p.rb + r0 < p.re) epi::stage<NMT>(hbw, p.Hg, p.Hs, p.nf, p.rb + r0, 0, lane);
         for (int r = p.rb + r0; r < p.re && ok; r += rstep) {
-            const float2 hra = p.Hg[r * NMT + a];
+            const bool b1 = (r == 0 || r == p.nf - 1);
+            const float wv_r = r < p.sym_rows ? 2.f * wvf : wvf;  // central symmetry: the mirror row
             for (int nt = 0; nt < p.n_ntiles; ++nt, ++tile) {
                 const int buf = tile & 1;
                 const uint32_t tph = (tile >> 1) & 1u;
+                epi::cp_async_wait_all();
+                __syncwarp();
+                // stage the next tile's FRF values while this one is reduced
+                if (nt + 1 < p.n_ntiles)
+                    epi::stage<NMT>(hbw + (buf ^ 1), p.Hg, p.Hs, p.nf, r, (nt + 1) * NC, lane);
+                else if (r + rstep < p.re)
+                    epi::stage<NMT>(hbw + (buf ^ 1), p.Hg, p.Hs, p.nf, r + rstep, 0, lane);
                 // warp-uniform outcome: tcgen05.ld below is .sync.aligned
                 const bool got = __all_sync(0xffffffffu, mbar_wait(&tfull[buf], tph, err, 4));
                 if (!got) { ok = false; break; }
                 fence_after();
-                const int c0 = nt * NC;
-                // Two passes per 32-column chunk (D1, then D3) keep one chunk of TMEM values
-                // live at a time.  Per grid column c the row-dependent FRF factors are formed
-                // once (j == 0) from FP32 copies of FP64-evaluated FRF tables.
-#pragma unroll
-                for (int q = 0; q < kBN / 32; ++q) {
-#pragma unroll
-                    for (int pass = 0; pass < 2; ++pass) {
-                        uint32_t v[32];
-                        tmem_ld32(lane_base + buf * 256 + pass * 128 + q * 32, v);
-                        tmem_wait_ld();
-                        float2 PA = make_float2(0.f, 0.f), PB = PA;
-                        float wc = 0.f;
-                        bool cval = false;
-                        int cg = 0, sidx = 0;
-#pragma unroll
-                        for (int e = 0; e < 32; ++e) {
-                            const int col = q * 32 + e;
-                            const int c = col / NMT, j = col % NMT;
-                            if (c >= NC) continue;
-                            if (j == 0 || e == 0) {
-                                cg = c0 + c;
-                                cval = cg < p.nf;
-                                if (cval) {
-                                    sidx = r + cg;
-                                    wc = point_weight(p, r, cg);
-                                    const float2 hcb = p.Hg[cg * NMT + b];
-                                    if (pass == 0) {
-                                        const float2 t1 = cmul(hra, hcb);          // term 1 at (r, c)
-                                        PA = make_float2(wc * t1.x, wc * t1.y);
-                                    } else {
-                                        const float2 hsa = p.Hs[sidx * NMT + a];
-                                        const float2 hsb = p.Hs[sidx * NMT + b];
-                                        const float2 t3 = cmul(hcb, conjf2(hsa));  // term 3 at (r, c)
-                                        PA = make_float2(wc * t3.x, wc * t3.y);
-                                        const float2 t2 = cmul(hra, conjf2(hsb));  // term 2 at (c, r)
-                                        PB = make_float2(wc * t2.x, wc * t2.y);
-                                    }
-                                }
-                            }
-                            if (cval && j < p.nm) {
-                                const float x = __uint_as_float(v[e]);
-                                if (pass == 0) {
-                                    const float2 hs = p.Hs[sidx * NMT + j];
-                                    const float F1 = PA.x * hs.x + PA.y * hs.y;    // Re[P1 conj(H_j(s))]
-                                    acc[0][j] = fmaf(F1, x, acc[0][j]);
-                                    acc[3][j] = fmaf(wc, x, acc[3][j]);
-                                } else {
-                                    const float2 hr = p.Hg[r * NMT + j];
-                                    const float2 hc = p.Hg[cg * NMT + j];
-                                    const float F3 = hr.x * PA.x - hr.y * PA.y;    // Re[H_j(w_r) P3]
-                                    const float F2 = hc.x * PB.x - hc.y * PB.y;    // Re[H_j(w_c) P2]
-                                    acc[1][j] = fmaf(F3, x, acc[1][j]);
-                                    acc[2][j] = fmaf(F2, x, acc[2][j]);
-                                    acc[4][j] = fmaf(wc, x, acc[4][j]);
-                                }
-                            }
-                        }
-                    }
-                }
+                epi::tile<NMT>(hbw[buf], lane_base + buf * 256, a, b, nt * NC, p.nf, vect, b1, wv_r, acc);
                 fence_before();
                 mbar_arrive(&tempty[buf]);
                 if ((nt + 1) % kFlushTiles == 0) flush();
             }
             flush();
         }
+        epi::cp_async_wait_all();
     }
     fence_before();
     __syncthreads();
@@ -432,7 +380,7 @@ cudaError_t prep_h(cudaStream_t st, int nf, int nm, int NMT, const double *f, Fr
 
 template <int NMT>
 static cudaError_t launch_gemm(cudaStream_t st, const CUtensorMap *maps, const Params &p, int grid) {
-    const size_t smem = (size_t)kStages * kStageBytes + 1024 + 256;
+    const size_t smem = (size_t)kStages * kStageBytes + 1024 + kBarBytes + kHBytes;
     cudaError_t e = cudaFuncSetAttribute(k_bfm_mixed<NMT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     k_bfm_mixed<NMT><<<grid, 192, smem, st>>>(maps[0], maps[1], maps[2], maps[3], maps[4], maps[5], p);

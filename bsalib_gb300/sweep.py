@@ -34,15 +34,19 @@ def run(n=96, seed0=5000, check=True):
     t0 = time.perf_counter()
     out, dev_ms = sw.run()
     wall_ms = (time.perf_counter() - t0) * 1e3
+    st = api.Stats()
+    api.check(api.load().bsa_gpu_getStats(api.C.byref(st)), "bsa_gpu_getStats")
+    batch_gemm_ms, batch_kernels = st.ms_gemm, st.kernels
     sw.clear()
     pts = float(sum(o["nf"] ** 2 for o in out))
-    seq_ms, worst = 0.0, 0.0
+    seq_ms, seq_gemm_ms, worst = 0.0, 0.0, 0.0
     if check:
         for k, p in enumerate(probs):
             s = api.BsaSession(p, precision=api.PREC_BF16X3)
             try:
                 r = s.run()
                 seq_ms += s.stats().ms_total
+                seq_gemm_ms += s.stats().ms_gemm
             finally:
                 s.close()
             ref = r["m3mr_cls"]
@@ -50,10 +54,11 @@ def run(n=96, seed0=5000, check=True):
     lat = np.array([o["ms"] for o in out])
     res = {"cases": n, "points": pts, "modes_min": min(o["nm"] for o in out),
            "modes_max": max(o["nm"] for o in out), "batch_device_ms": dev_ms, "batch_wall_ms": wall_ms,
-           "batch_pts_per_s": pts / (dev_ms * 1e-3), "latency_p50_ms": float(np.percentile(lat, 50)),
+           "batch_pts_per_s": pts / (dev_ms * 1e-3), "batch_contraction_launch_ms": batch_gemm_ms,
+           "batch_kernels": batch_kernels, "latency_p50_ms": float(np.percentile(lat, 50)),
            "latency_p99_ms": float(np.percentile(lat, 99))}
     if check:
-        res.update({"sequential_device_ms": seq_ms, "sequential_pts_per_s": pts / (seq_ms * 1e-3),
+        res.update({"sequential_device_ms": seq_ms, "sequential_contraction_launch_ms": seq_gemm_ms, "sequential_pts_per_s": pts / (seq_ms * 1e-3),
                     "speedup_device": seq_ms / dev_ms, "m3mr_rel_batch_vs_single_max": worst})
     return res
 
