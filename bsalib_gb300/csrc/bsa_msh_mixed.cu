@@ -316,6 +316,7 @@ struct ZoneM {
     double fi0, fj0, dI, dJ, wI, wJ, sym;
     int ni, nj, Fi, Fj;
     int pbase, cbase, qbase;
+    float wb;  // sym wI wJ rounded once: the BFM-lattice trapezoid weight of an interior point
 };
 
 __device__ __forceinline__ int zone_of(const ZoneM *__restrict__ zones, int nz, int idx, int which) {
@@ -353,6 +354,15 @@ __global__ void k_msh_frf(int nm, int nz, const ZoneM *__restrict__ zones, int n
 constexpr int kQB = 24;  // BRM points per shared-memory round
 constexpr int kEPT = 2;  // term-tensor elements per thread
 
+// s + c += x, compensated (Neumaier): the cell sums are added in FP32 with their rounding
+// errors carried, so the result does not depend on how cells are spread over blocks beyond
+// ~1e-13 relative, and no FP64 arithmetic (slow on GB300) runs per cell.
+__device__ __forceinline__ void csum(float &s, float &c, float x) {
+    const float t = s + x;
+    c += fabsf(s) >= fabsf(x) ? (s - t) + x : (x - t) + s;
+    s = t;
+}
+
 // Block (g, chunk): elements e = chunk*512 + t + 256 u (u < 2) of the term tensors
 // (e = j'*nm^2 + a*nm + b), cells g, g + G, ...  Each BRM point belongs to the cell
 // (min(qi/Fi, ni-2), min(qj/Fj, nj-2)) and each BFM point to the cell (min(i, ni-2),
@@ -375,11 +385,11 @@ __global__ __launch_bounds__(256) void k_msh_moments(int nm, const ZoneM *__rest
         ia[u] = ab / nm;
         ib[u] = ab % nm;
     }
-    double mf[kEPT][3], mr[kEPT][3];
+    float mf[kEPT][3], mfe[kEPT][3], mr[kEPT][3], mre[kEPT][3];  // compensated sums over cells
 #pragma unroll
     for (int u = 0; u < kEPT; ++u)
 #pragma unroll
-        for (int t = 0; t < 3; ++t) mf[u][t] = mr[u][t] = 0.0;
+        for (int t = 0; t < 3; ++t) mf[u][t] = mfe[u][t] = mr[u][t] = mre[u][t] = 0.f;
     const float *Ts[3] = {T1, T3, T2};
     for (int cid = blockIdx.x; cid < ncells; cid += gridDim.x) {
         const ZoneM z = zones[cell_zone[cid]];
@@ -392,17 +402,16 @@ __global__ __launch_bounds__(256) void k_msh_moments(int nm, const ZoneM *__rest
         const size_t P00 = (size_t)z.pbase + (size_t)i0 * z.nj + j0, P01 = P00 + 1, P10 = P00 + z.nj, P11 = P10 + 1;
         // corner values of the three term tensors, and the BFM lattice trapezoid (m3mf) of
         // the BFM points this cell owns
-        float c[kEPT][3][4];
-        const double wb = z.sym * z.wI * z.wJ;
-        double wp[4];
+        float c[kEPT][3][4], mfc[kEPT][3], sr[kEPT][3];
+        float wp[4];
         {
             const int ci[4] = {i0, i0, i0 + 1, i0 + 1}, cj[4] = {j0, j0 + 1, j0, j0 + 1};
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
                 const bool own = (ci[k] == i0 || i0 == z.ni - 2) && (cj[k] == j0 || j0 == z.nj - 2);
-                const double ti = (ci[k] == 0 || ci[k] == z.ni - 1) ? 0.5 : 1.0;
-                const double tj = (cj[k] == 0 || cj[k] == z.nj - 1) ? 0.5 : 1.0;
-                wp[k] = own ? wb * ti * tj : 0.0;
+                const float ti = (ci[k] == 0 || ci[k] == z.ni - 1) ? 0.5f : 1.f;
+                const float tj = (cj[k] == 0 || cj[k] == z.nj - 1) ? 0.5f : 1.f;
+                wp[k] = own ? z.wb * ti * tj : 0.f;
             }
         }
 #pragma unroll
@@ -415,15 +424,12 @@ __global__ __launch_bounds__(256) void k_msh_moments(int nm, const ZoneM *__rest
                 c[u][t][1] = ve ? Ts[t][P01 * nm3 + e] : 0.f;
                 c[u][t][2] = ve ? Ts[t][P10 * nm3 + e] : 0.f;
                 c[u][t][3] = ve ? Ts[t][P11 * nm3 + e] : 0.f;
+                mfc[u][t] = 0.f;
+                sr[u][t] = 0.f;
 #pragma unroll
-                for (int k = 0; k < 4; ++k) mf[u][t] += wp[k] * (double)c[u][t][k];
+                for (int k = 0; k < 4; ++k) mfc[u][t] = fmaf(wp[k], c[u][t][k], mfc[u][t]);
             }
         }
-        float sr[kEPT][3];
-#pragma unroll
-        for (int u = 0; u < kEPT; ++u)
-#pragma unroll
-            for (int t = 0; t < 3; ++t) sr[u][t] = 0.f;
         for (int q0 = 0; q0 < nq; q0 += kQB) {
             const int nb = min(kQB, nq - q0);
             __syncthreads();
@@ -466,7 +472,10 @@ __global__ __launch_bounds__(256) void k_msh_moments(int nm, const ZoneM *__rest
 #pragma unroll
         for (int u = 0; u < kEPT; ++u)
 #pragma unroll
-            for (int t = 0; t < 3; ++t) mr[u][t] += (double)sr[u][t];
+            for (int t = 0; t < 3; ++t) {
+                csum(mf[u][t], mfe[u][t], mfc[u][t]);
+                csum(mr[u][t], mre[u][t], sr[u][t]);
+            }
     }
     double *pg = part + (size_t)blockIdx.x * 6 * nm3;
 #pragma unroll
@@ -474,8 +483,8 @@ __global__ __launch_bounds__(256) void k_msh_moments(int nm, const ZoneM *__rest
         if (ev[u] >= nm3) continue;
 #pragma unroll
         for (int t = 0; t < 3; ++t) {
-            pg[(size_t)t * nm3 + ev[u]] = mf[u][t];
-            pg[(size_t)(3 + t) * nm3 + ev[u]] = mr[u][t];
+            pg[(size_t)t * nm3 + ev[u]] = (double)mf[u][t] + (double)mfe[u][t];
+            pg[(size_t)(3 + t) * nm3 + ev[u]] = (double)mr[u][t] + (double)mre[u][t];
         }
     }
 }
@@ -613,7 +622,8 @@ int Engine::msh_mixed_batch(const std::vector<ZoneDev> &zs, std::vector<double> 
     {
         long long pb = 0, cb = 0, gb = 0, qb = 0;
         for (const ZoneDev &z : zs) {
-            ZoneM m{z.fi0, z.fj0, z.dIi, z.dJj, z.wI, z.wJ, z.sym, z.ni, z.nj, z.Fi, z.Fj, (int)pb, (int)cb, (int)qb};
+            ZoneM m{z.fi0, z.fj0, z.dIi, z.dJj, z.wI, z.wJ, z.sym, z.ni, z.nj, z.Fi, z.Fj, (int)pb, (int)cb, (int)qb,
+                    (float)(z.sym * z.wI * z.wJ)};
             qb += (long long)((z.ni - 1) * z.Fi + 1) * ((z.nj - 1) * z.Fj + 1);
             zm.push_back(m);
             cellz.insert(cellz.end(), (size_t)(z.ni - 1) * (z.nj - 1), (int)zm.size() - 1);
