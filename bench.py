@@ -265,6 +265,15 @@ def learned_leg():
             "value": brm / (ms_learned / 1e3), "unit": "BRM pts/s of the final mesh per second of the learned run"}
 
 
+def sweep_leg():
+    """The batched Classic sweep (bsa_gpu_batch*): 8 seeded random structures x 8 mean wind
+    speeds (nodes 30-600, 4-32 kept modes, grids of 129-513 points), one batched evaluation
+    against one split-precision bsa_Run per case: Classic grid points per second of both,
+    per-case completion latencies inside the batched launch, largest relative difference."""
+    from bsalib_gb300 import sweep
+    return sweep.run(structures=8, winds=8, seed0=5000, check=True)
+
+
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
@@ -409,6 +418,7 @@ def run_ours(args):
         cpu = cpu_reference(prob, budget_s=15.0)
         msh = mesher_leg(prec)
         msh["learned_refinement"] = learned_leg()
+        swp = sweep_leg()
         out = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
@@ -429,6 +439,7 @@ def run_ours(args):
             "fp64_gpu_path": {"value": fp64_pts, "unit": UNIT, "sample": f"{ns} random grid points"},
             "mesher": msh,
             "classic_central_symmetry": sym,
+            "parametric_sweep": swp,
             "wall_s_timed": wall,
         }
         print(json.dumps(out))

@@ -1,9 +1,10 @@
 """Parametric sweep of Classic analyses: one batched evaluation against one bsa_Run per case.
 
-  python -m bsalib_gb300.sweep [--cases 96] [--seed0 5000] [--json out.json]
+  python -m bsalib_gb300.sweep [--structures 8] [--winds 8] [--seed0 5000] [--json out.json]
 
-Cases are seeded random cantilevers (`problem.random_structure`: nodes 30-400, kept modes
-4-32, Classic grids of 65-257 points, wind 15-50 m/s).  The batch is evaluated once untimed
+Cases are seeded random cantilevers (`problem.random_structure`: nodes 30-600, kept modes
+4-32, Classic grids of 129-513 points), each under `winds` mean wind speeds spread evenly
+over 15-50 m/s.  The batch is evaluated once untimed
 and once timed (device time of the whole sweep and wall time of the call); each case is then
 run on its own with the split precision, the sequential baseline.  Reported: aggregate Classic
 grid points per second of both, the per-case completion latencies inside the batched launch
@@ -21,12 +22,15 @@ from . import api, build
 from .problem import random_structure
 
 
-def cases(n, seed0):
-    return [random_structure(seed0 + k, nodes=(30, 400), modes=(4, 32), nfreq_grid=(65, 257)) for k in range(n)]
+def cases(structures, winds, seed0):
+    us = np.linspace(15.0, 50.0, winds) if winds > 1 else [30.0]
+    return [random_structure(seed0 + k, nodes=(30, 600), modes=(4, 32), nfreq_grid=(129, 513), U_mean=float(u))
+            for k in range(structures) for u in us]
 
 
-def run(n=96, seed0=5000, check=True):
-    probs = cases(n, seed0)
+def run(structures=8, winds=8, seed0=5000, check=True):
+    probs = cases(structures, winds, seed0)
+    n = len(probs)
     sw = api.Sweep()
     for p in probs:
         sw.add(p)
@@ -52,7 +56,7 @@ def run(n=96, seed0=5000, check=True):
             ref = r["m3mr_cls"]
             worst = max(worst, float(np.max(np.abs(out[k]["m3mr"] - ref)) / np.max(np.abs(ref))))
     lat = np.array([o["ms"] for o in out])
-    res = {"cases": n, "points": pts, "modes_min": min(o["nm"] for o in out),
+    res = {"cases": n, "structures": structures, "winds": winds, "points": pts, "modes_min": min(o["nm"] for o in out),
            "modes_max": max(o["nm"] for o in out), "batch_device_ms": dev_ms, "batch_wall_ms": wall_ms,
            "batch_pts_per_s": pts / (dev_ms * 1e-3), "batch_contraction_launch_ms": batch_gemm_ms,
            "batch_kernels": batch_kernels, "latency_p50_ms": float(np.percentile(lat, 50)),
@@ -65,12 +69,14 @@ def run(n=96, seed0=5000, check=True):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--cases", type=int, default=96)
+    ap.add_argument("--structures", type=int, default=8)
+    ap.add_argument("--winds", type=int, default=8)
     ap.add_argument("--seed0", type=int, default=5000)
+    ap.add_argument("--no-check", action="store_true", help="skip the one-analysis-per-case baseline")
     ap.add_argument("--json", default="")
     a = ap.parse_args()
     build.build()
-    res = run(a.cases, a.seed0)
+    res = run(a.structures, a.winds, a.seed0, check=not a.no_check)
     if a.json:
         with open(a.json, "w") as fh:
             fh.write(json.dumps(res))
