@@ -267,7 +267,7 @@ def learned_leg():
 
 def sweep_leg():
     """The batched Classic sweep (bsa_gpu_batch*): 8 seeded random structures x 8 mean wind
-    speeds (nodes 30-600, 4-32 kept modes, grids of 129-513 points), one batched evaluation
+    speeds (nodes 30-600, 4-40 kept modes, grids of 129-513 points), one batched evaluation
     against one split-precision bsa_Run per case: Classic grid points per second of both,
     per-case completion latencies inside the batched launch, largest relative difference."""
     from bsalib_gb300 import sweep

@@ -3,8 +3,8 @@
 //
 // Each case is snapshotted when it is added (bsa_gpu_batchAdd: its validated inputs, the
 // derived tables and its grid), so the caller can set up the next case at once.  At
-// bsa_gpu_batchRun the cases are grouped by their FRF-table width NMT (8, 16, 24, 32 kept
-// modes) and by device memory; for each group the operands of every case are prepared into
+// bsa_gpu_batchRun the cases are grouped by their FRF-table width (8, 16, 24, 32 kept modes,
+// or 64: two halves of 32) and by device memory; for each group the operands of every case are prepared into
 // shared tables (one U, G, S table each, rows of all cases stacked with a common K stride), and
 // one launch of k_bfm_batch walks a work list of (case, grid row, row tile) items with the
 // k_bfm_mixed pipeline (TMA warp, MMA warp, four TMEM-draining warps).  The epilogue adds its
@@ -37,7 +37,7 @@ constexpr int kStageBytes = 6 * kTileBytes;
 constexpr int kKinds = 5;  // mr1, mr3, mr2, mf1, mf23
 constexpr int kFlushTiles = 64;
 constexpr int kBarBytes = 256;                              // mbarriers + TMEM slot
-constexpr int kHBytes = 4 * 2 * (int)sizeof(epi::HTile);   // FRF staging, 2 tiles per epilogue warp
+constexpr int kHBytes = 2 * (int)sizeof(epi::HTile<32, 2>);  // FRF staging, 2 tiles (largest form)
 constexpr size_t kSmem = (size_t)kStages * kStageBytes + 1024 + kBarBytes + kHBytes;
 
 struct CaseP {
@@ -67,13 +67,16 @@ struct BParams {
     int *err;
 };
 
-template <int NMT>
+// Items w = blockIdx.x, blockIdx.x + gridDim.x, ...; per item the mode halves jh < JH, per half
+// the case's N tiles: the tile sequence of all three roles.
+template <int NMT, int JH>
 __global__ void __launch_bounds__(192, 1)
     k_bfm_batch(const __grid_constant__ CUtensorMap tmUh, const __grid_constant__ CUtensorMap tmUl,
                 const __grid_constant__ CUtensorMap tmGh, const __grid_constant__ CUtensorMap tmGl,
                 const __grid_constant__ CUtensorMap tmSh, const __grid_constant__ CUtensorMap tmSl, const BParams p) {
     constexpr int NC = kBN / NMT;
     constexpr int BROWS = NC * NMT;
+    constexpr int W = NMT * JH;
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint64_t *bars = (uint64_t *)(smem + kStages * kStageBytes);
@@ -121,24 +124,25 @@ __global__ void __launch_bounds__(192, 1)
             for (int w = blockIdx.x; w < p.nitems && ok; w += gridDim.x) {
                 const BItem im = p.items[w];
                 const CaseP cs = p.cases[im.c];
-                for (int nt = 0; nt < cs.n_ntiles && ok; ++nt)
-                    for (int kc = 0; kc < cs.nk && ok; ++kc, ++it) {
-                        const int s = it % kStages;
-                        const uint32_t ph = (it / kStages) & 1u;
-                        if (!mbar_wait(&empty[s], ph ^ 1u, err, 1)) { ok = false; break; }
-                        uint8_t *st = smem + s * kStageBytes;
-                        mbar_expect_tx(&full[s], tx_bytes);
-                        const int x = kc * kBK;
-                        const int yu = cs.u_row0 + im.r * cs.Mp + im.mt * kBM;
-                        tma_2d(st + 0 * kTileBytes, &tmUh, &full[s], x, yu);
-                        tma_2d(st + 1 * kTileBytes, &tmUl, &full[s], x, yu);
-                        const int yg = cs.g_row0 + nt * BROWS;
-                        tma_2d(st + 2 * kTileBytes, &tmGh, &full[s], x, yg);
-                        tma_2d(st + 3 * kTileBytes, &tmGl, &full[s], x, yg);
-                        const int ys = cs.s_row0 + (im.r + nt * NC) * NMT;
-                        tma_2d(st + 4 * kTileBytes, &tmSh, &full[s], x, ys);
-                        tma_2d(st + 5 * kTileBytes, &tmSl, &full[s], x, ys);
-                    }
+                for (int jh = 0; jh < JH && ok; ++jh)
+                    for (int nt = 0; nt < cs.n_ntiles && ok; ++nt)
+                        for (int kc = 0; kc < cs.nk && ok; ++kc, ++it) {
+                            const int s = it % kStages;
+                            const uint32_t ph = (it / kStages) & 1u;
+                            if (!mbar_wait(&empty[s], ph ^ 1u, err, 1)) { ok = false; break; }
+                            uint8_t *st = smem + s * kStageBytes;
+                            mbar_expect_tx(&full[s], tx_bytes);
+                            const int x = kc * kBK;
+                            const int yu = cs.u_row0 + im.r * cs.Mp + im.mt * kBM;
+                            tma_2d(st + 0 * kTileBytes, &tmUh, &full[s], x, yu);
+                            tma_2d(st + 1 * kTileBytes, &tmUl, &full[s], x, yu);
+                            const int yg = cs.g_row0 + jh * cs.nf * NMT + nt * BROWS;
+                            tma_2d(st + 2 * kTileBytes, &tmGh, &full[s], x, yg);
+                            tma_2d(st + 3 * kTileBytes, &tmGl, &full[s], x, yg);
+                            const int ys = cs.s_row0 + jh * (2 * cs.nf - 1) * NMT + (im.r + nt * NC) * NMT;
+                            tma_2d(st + 4 * kTileBytes, &tmSh, &full[s], x, ys);
+                            tma_2d(st + 5 * kTileBytes, &tmSl, &full[s], x, ys);
+                        }
             }
             const uint32_t last = it;
             for (uint32_t q = (last > (uint32_t)kStages ? last - kStages : 0); q < last; ++q) {
@@ -157,37 +161,38 @@ __global__ void __launch_bounds__(192, 1)
             bool ok = true;
             for (int w = blockIdx.x; w < p.nitems && ok; w += gridDim.x) {
                 const CaseP cs = p.cases[p.items[w].c];
-                for (int nt = 0; nt < cs.n_ntiles && ok; ++nt, ++tile) {
-                    const int buf = tile & 1;
-                    const uint32_t tph = (tile >> 1) & 1u;
-                    if (!mbar_wait(&tempty[buf], tph ^ 1u, err, 2)) { ok = false; break; }
-                    fence_after();
-                    const uint32_t d1 = tmem + buf * 256, d3 = d1 + 128;
-                    for (int kc = 0; kc < cs.nk; ++kc, ++it) {
-                        const int s = it % kStages;
-                        const uint32_t ph = (it / kStages) & 1u;
-                        if (!mbar_wait(&full[s], ph, err, 3)) { ok = false; break; }
+                for (int jh = 0; jh < JH && ok; ++jh)
+                    for (int nt = 0; nt < cs.n_ntiles && ok; ++nt, ++tile) {
+                        const int buf = tile & 1;
+                        const uint32_t tph = (tile >> 1) & 1u;
+                        if (!mbar_wait(&tempty[buf], tph ^ 1u, err, 2)) { ok = false; break; }
                         fence_after();
-                        const uint32_t base = su32(smem + s * kStageBytes);
-                        const int nks = kc == cs.nk - 1 ? cs.ks_last : kBK / 16;
-                        for (int ks = 0; ks < nks; ++ks) {
-                            const uint32_t off = ks * 32;
-                            const uint64_t uh = sdesc(base + 0 * kTileBytes + off), ul = sdesc(base + 1 * kTileBytes + off);
-                            const uint64_t gh = sdesc(base + 2 * kTileBytes + off), gl = sdesc(base + 3 * kTileBytes + off);
-                            const uint64_t sh = sdesc(base + 4 * kTileBytes + off), sl = sdesc(base + 5 * kTileBytes + off);
-                            const uint32_t acc = (kc > 0 || ks > 0) ? 1u : 0u;
-                            mma(d1, uh, gh, acc);
-                            mma(d1, uh, gl, 1u);
-                            mma(d1, ul, gh, 1u);
-                            mma(d3, uh, sh, acc);
-                            mma(d3, uh, sl, 1u);
-                            mma(d3, ul, sh, 1u);
+                        const uint32_t d1 = tmem + buf * 256, d3 = d1 + 128;
+                        for (int kc = 0; kc < cs.nk; ++kc, ++it) {
+                            const int s = it % kStages;
+                            const uint32_t ph = (it / kStages) & 1u;
+                            if (!mbar_wait(&full[s], ph, err, 3)) { ok = false; break; }
+                            fence_after();
+                            const uint32_t base = su32(smem + s * kStageBytes);
+                            const int nks = kc == cs.nk - 1 ? cs.ks_last : kBK / 16;
+                            for (int ks = 0; ks < nks; ++ks) {
+                                const uint32_t off = ks * 32;
+                                const uint64_t uh = sdesc(base + 0 * kTileBytes + off), ul = sdesc(base + 1 * kTileBytes + off);
+                                const uint64_t gh = sdesc(base + 2 * kTileBytes + off), gl = sdesc(base + 3 * kTileBytes + off);
+                                const uint64_t sh = sdesc(base + 4 * kTileBytes + off), sl = sdesc(base + 5 * kTileBytes + off);
+                                const uint32_t acc = (kc > 0 || ks > 0) ? 1u : 0u;
+                                mma(d1, uh, gh, acc);
+                                mma(d1, uh, gl, 1u);
+                                mma(d1, ul, gh, 1u);
+                                mma(d3, uh, sh, acc);
+                                mma(d3, uh, sl, 1u);
+                                mma(d3, ul, sh, 1u);
+                            }
+                            mma_commit(&empty[s]);
                         }
-                        mma_commit(&empty[s]);
+                        if (!ok) break;
+                        mma_commit(&tfull[buf]);
                     }
-                    if (!ok) break;
-                    mma_commit(&tfull[buf]);
-                }
             }
             mma_commit(done);
             const uint64_t t0 = gtime();
@@ -197,19 +202,24 @@ __global__ void __launch_bounds__(192, 1)
         __syncwarp();
     } else {
         // ---------------- epilogue: FRF x weight, partial moments per case ----------------
+        // One double-buffered FRF staging slot shared by the four warps (epi_sync orders it);
+        // after a failed wait a warp walks the tile sequence without work, so every warp
+        // reaches every epi_sync.
         const int quarter = warp & 3;
+        const int et = threadIdx.x - 64;
         const int row = quarter * 32 + lane;
         const uint32_t lane_base = tmem + ((uint32_t)(quarter * 32) << 16);
-        epi::HTile *hbw = (epi::HTile *)(smem + kStages * kStageBytes + kBarBytes) + quarter * 2;
+        using HT = epi::HTile<NMT, JH>;
+        HT *hbs = (HT *)(smem + kStages * kStageBytes + kBarBytes);
         float acc[kKinds][NMT];
         uint32_t tile = 0;
         bool ok = true;
         if (blockIdx.x < p.nitems) {
             const BItem i0 = p.items[blockIdx.x];
             const CaseP s0 = p.cases[i0.c];
-            epi::stage<NMT>(hbw, p.Hg + s0.hg0, p.Hs + s0.hs0, s0.nf, i0.r, 0, lane);
+            epi::stage<NMT, JH>(hbs, p.Hg + s0.hg0, p.Hs + s0.hs0, s0.nf, i0.r, 0, et, 128);
         }
-        for (int w = blockIdx.x; w < p.nitems && ok; w += gridDim.x) {
+        for (int w = blockIdx.x; w < p.nitems; w += gridDim.x) {
             const BItem im = p.items[w];
             const CaseP cs = p.cases[im.c];
             const int r = im.r;
@@ -220,42 +230,47 @@ __global__ void __launch_bounds__(192, 1)
             const float wvf = (float)cs.wval;
             const bool vect = cs.wmode == kWeightClassicVect, b1 = (r == 0 || r == cs.nf - 1);
             double *part = p.part + cs.part0 + grow;
+            for (int jh = 0; jh < JH; ++jh) {
 #pragma unroll
-            for (int k = 0; k < kKinds; ++k)
+                for (int k = 0; k < kKinds; ++k)
 #pragma unroll
-                for (int j = 0; j < NMT; ++j) acc[k][j] = 0.f;
-            for (int nt = 0; nt < cs.n_ntiles; ++nt, ++tile) {
-                const int buf = tile & 1;
-                const uint32_t tph = (tile >> 1) & 1u;
-                epi::cp_async_wait_all();
-                __syncwarp();
-                // stage the next tile: this item's next one, or the first of the CTA's next item
-                if (nt + 1 < cs.n_ntiles) {
-                    epi::stage<NMT>(hbw + (buf ^ 1), Hg, Hs, cs.nf, r, (nt + 1) * NC, lane);
-                } else if (w + (int)gridDim.x < p.nitems) {
-                    const BItem in = p.items[w + gridDim.x];
-                    const CaseP sn = p.cases[in.c];
-                    epi::stage<NMT>(hbw + (buf ^ 1), p.Hg + sn.hg0, p.Hs + sn.hs0, sn.nf, in.r, 0, lane);
-                }
-                const bool got = __all_sync(0xffffffffu, mbar_wait(&tfull[buf], tph, err, 4));
-                if (!got) { ok = false; break; }
-                fence_after();
-                epi::tile<NMT>(hbw[buf], lane_base + buf * 256, a, b, nt * NC, cs.nf, vect, b1, wvf, acc);
-                fence_before();
-                mbar_arrive(&tempty[buf]);
-                if ((nt + 1) % kFlushTiles == 0 || nt + 1 == cs.n_ntiles) {
-                    if (vrow) {
+                    for (int j = 0; j < NMT; ++j) acc[k][j] = 0.f;
+                for (int nt = 0; nt < cs.n_ntiles; ++nt, ++tile) {
+                    const int buf = tile & 1;
+                    const uint32_t tph = (tile >> 1) & 1u;
+                    epi::cp_async_wait_all();
+                    epi::epi_sync();  // this tile's values are in; the other slot is no longer read
+                    // stage the next tile: this half's next one, this item's next half, or the
+                    // first tile of the CTA's next item
+                    if (nt + 1 < cs.n_ntiles) {
+                        epi::stage<NMT, JH>(hbs + (buf ^ 1), Hg, Hs, cs.nf, r, (nt + 1) * NC, et, 128);
+                    } else if (jh + 1 < JH) {
+                        epi::stage<NMT, JH>(hbs + (buf ^ 1), Hg, Hs, cs.nf, r, 0, et, 128);
+                    } else if (w + (int)gridDim.x < p.nitems) {
+                        const BItem in = p.items[w + gridDim.x];
+                        const CaseP sn = p.cases[in.c];
+                        epi::stage<NMT, JH>(hbs + (buf ^ 1), p.Hg + sn.hg0, p.Hs + sn.hs0, sn.nf, in.r, 0, et, 128);
+                    }
+                    if (!ok) continue;
+                    ok = __all_sync(0xffffffffu, mbar_wait(&tfull[buf], tph, err, 4));
+                    if (!ok) continue;
+                    fence_after();
+                    epi::tile<NMT, JH>(hbs[buf], lane_base + buf * 256, a, b, nt * NC, cs.nf, vect, b1, wvf, jh, acc);
+                    fence_before();
+                    mbar_arrive(&tempty[buf]);
+                    if (((nt + 1) % kFlushTiles == 0 || nt + 1 == cs.n_ntiles) && vrow) {
 #pragma unroll
                         for (int k = 0; k < kKinds; ++k)
 #pragma unroll
                             for (int j = 0; j < NMT; ++j) {
-                                if (acc[k][j] != 0.f) atomicAdd(part + (size_t)(k * NMT + j) * cs.Mp, (double)acc[k][j]);
+                                if (acc[k][j] != 0.f)
+                                    atomicAdd(part + (size_t)(k * W + jh * NMT + j) * cs.Mp, (double)acc[k][j]);
                                 acc[k][j] = 0.f;
                             }
                     }
                 }
             }
-            if (!ok) break;
+            if (!ok) continue;
             // this warp's share of the item is in the accumulators: count it, stamp the case
             __syncwarp();
             if (lane == 0) {
@@ -312,7 +327,7 @@ int Engine::batch_add(int *id) {
     int rc = validate();
     if (rc) return rc;
     if (set.onlyd) return fail(BSA_ERR_UNSUPPORTED, "the batched sweep runs the full-tensor Classic analysis");
-    if (nme > 32) return fail(BSA_ERR_UNSUPPORTED, "the batched sweep supports at most 32 kept modes");
+    if (nme > 64) return fail(BSA_ERR_UNSUPPORTED, "the batched sweep supports at most 64 kept modes");
     BatchCase c;
     if ((rc = classic_grid(c.f))) return rc;
     if (c.f.size() < 2) return fail(BSA_ERR_ARG, "classic grid needs at least 2 frequencies");
@@ -367,7 +382,8 @@ int Engine::batch_run(double *m3mf, double *m3mr, double *m2mr, double *case_ms,
     if ((e = cudaGetDevice(&dev)) || (e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev)))
         return cuda_fail(e, "device query");
     // groups: same NMT, cases in K order, device bytes bounded
-    auto nmt_of = [](int nm) { return nm <= 8 ? 8 : nm <= 16 ? 16 : nm <= 24 ? 24 : 32; };
+    // FRF-table width of a case; above 32 modes two halves of 32 (JH = 2)
+    auto nmt_of = [](int nm) { return nm <= 8 ? 8 : nm <= 16 ? 16 : nm <= 24 ? 24 : nm <= 32 ? 32 : 64; };
     std::vector<int> order(nc);
     for (int c = 0; c < nc; ++c) order[c] = c;
     std::sort(order.begin(), order.end(), [&](int x, int y) {
@@ -404,17 +420,18 @@ int Engine::batch_run(double *m3mf, double *m3mr, double *m2mr, double *case_ms,
     const double budget = 24e9;
     size_t g0 = 0;
     while (g0 < order.size()) {
-        const int NMT = nmt_of(g_batch[order[g0]].nme);
+        const int Wd = nmt_of(g_batch[order[g0]].nme);
+        const int NMT = Wd > 32 ? 32 : Wd, JH = Wd / NMT;
         size_t g1 = g0;
         double rows = 0.0;
-        while (g1 < order.size() && nmt_of(g_batch[order[g1]].nme) == NMT) {
+        while (g1 < order.size() && nmt_of(g_batch[order[g1]].nme) == Wd) {
             // U, G and S rows of the case; hi + lo bf16 at the group's K stride, which is
             // this case's (the group is in K order)
             const BatchCase &c = g_batch[order[g1]];
             const double Kp = (double)(((c.K + kBK - 1) / kBK) * kBK);
             const double Mp = (double)(((c.nme * c.nme + kBM - 1) / kBM) * kBM);
             const double nf = (double)c.f.size();
-            const double add = nf * Mp + (3 * nf - 1) * NMT;
+            const double add = nf * Mp + (double)JH * (3 * nf - 1) * NMT;
             if (g1 > g0 && 4.0 * Kp * (rows + add) > budget) break;
             rows += add;
             ++g1;
@@ -450,11 +467,11 @@ int Engine::batch_run(double *m3mf, double *m3mr, double *m2mr, double *case_ms,
             q.part0 = parts;
             q.nitems = (unsigned)(nf * q.MT);
             urows += (long long)nf * q.Mp;
-            grows += (long long)nf * NMT;
-            srows += (long long)(2 * nf - 1) * NMT;
-            hg += (long long)nf * NMT;
-            hs += (long long)(2 * nf - 1) * NMT;
-            parts += (long long)kKinds * NMT * q.Mp;
+            grows += (long long)JH * nf * NMT;
+            srows += (long long)JH * (2 * nf - 1) * NMT;
+            hg += (long long)nf * Wd;
+            hs += (long long)(2 * nf - 1) * Wd;
+            parts += (long long)kKinds * Wd * q.Mp;
             for (int r = 0; r < nf; ++r)
                 for (int mt = 0; mt < q.MT; ++mt) items.push_back(BItem{(int)(k - g0), r, mt, 0});
         }
@@ -499,12 +516,17 @@ int Engine::batch_run(double *m3mf, double *m3mr, double *m2mr, double *case_ms,
             const float *A = dA32.as<float>();
             if ((e = mixed::prep_u(stream, nf, c.nme, c.K, Kp, q.Mp, A, dQ.as<double>(), Uh + (size_t)q.u_row0 * Kp,
                                    Ul + (size_t)q.u_row0 * Kp)) ||
-                (e = mixed::prep_b(stream, nf, c.nme, NMT, c.K, Kp, nf, (nf - 1) / 2, c.trunc ? 1 : 0, nf, 0, A,
-                                   Gh + (size_t)q.g_row0 * Kp, Gl + (size_t)q.g_row0 * Kp)) ||
-                (e = mixed::prep_b(stream, 2 * nf - 1, c.nme, NMT, c.K, Kp, nf, (nf - 1) / 2, c.trunc ? 1 : 0, nf, 1,
-                                   A, Sh + (size_t)q.s_row0 * Kp, Sl + (size_t)q.s_row0 * Kp)) ||
-                (e = mixed::prep_h(stream, nf, c.nme, NMT, dFreq.as<double>(), frf(), Hg + q.hg0, Hs + q.hs0)))
+                (e = mixed::prep_h(stream, nf, c.nme, Wd, dFreq.as<double>(), frf(), Hg + q.hg0, Hs + q.hs0)))
                 return cuda_fail(e, "batch operand preparation");
+            for (int jh = 0; jh < JH; ++jh) {
+                const size_t og = ((size_t)q.g_row0 + (size_t)jh * nf * NMT) * Kp;
+                const size_t os = ((size_t)q.s_row0 + (size_t)jh * (2 * nf - 1) * NMT) * Kp;
+                if ((e = mixed::prep_b(stream, nf, c.nme, NMT, jh * NMT, c.K, Kp, nf, (nf - 1) / 2, c.trunc ? 1 : 0, nf,
+                                       0, A, Gh + og, Gl + og)) ||
+                    (e = mixed::prep_b(stream, 2 * nf - 1, c.nme, NMT, jh * NMT, c.K, Kp, nf, (nf - 1) / 2,
+                                       c.trunc ? 1 : 0, nf, 1, A, Sh + os, Sl + os)))
+                    return cuda_fail(e, "batch operand preparation");
+            }
             // second-order moments (FP64 over the FP32 A table), rectangle or trapezoid weights
             double delta = c.f[1] - c.f[0];
             if (c.set.defsc == 1) delta *= kPi2;
@@ -519,7 +541,7 @@ int Engine::batch_run(double *m3mf, double *m3mr, double *m2mr, double *case_ms,
                 (e = launch_m2(stream, 0, nf, c.nme, 0, dFreq.as<double>(), dWf.as<double>(), dPsdF.as<double>(), frf(),
                                m2o, m2o + nm2, m2o + 2 * nm2)))
                 return cuda_fail(e, "batch m2");
-            kernels += 6;
+            kernels += 4 + 2 * JH;
         }
         std::vector<long long> offs(cp.size());
         for (size_t k = g0; k < g1; ++k) offs[k - g0] = off3[order[k]];
@@ -537,23 +559,16 @@ int Engine::batch_run(double *m3mf, double *m3mr, double *m2mr, double *case_ms,
         const size_t smem = kSmem;
         const int grid = (int)std::min<long long>((long long)items.size(), nsm);
         if ((e = cudaEventRecord(evg0, stream))) return cuda_fail(e, "event");
-        switch (NMT) {
-        case 8:
-            cudaFuncSetAttribute(k_bfm_batch<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            k_bfm_batch<8><<<grid, 192, smem, stream>>>(maps[0], maps[1], maps[2], maps[3], maps[4], maps[5], prm);
-            break;
-        case 16:
-            cudaFuncSetAttribute(k_bfm_batch<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            k_bfm_batch<16><<<grid, 192, smem, stream>>>(maps[0], maps[1], maps[2], maps[3], maps[4], maps[5], prm);
-            break;
-        case 24:
-            cudaFuncSetAttribute(k_bfm_batch<24>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            k_bfm_batch<24><<<grid, 192, smem, stream>>>(maps[0], maps[1], maps[2], maps[3], maps[4], maps[5], prm);
-            break;
-        default:
-            cudaFuncSetAttribute(k_bfm_batch<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            k_bfm_batch<32><<<grid, 192, smem, stream>>>(maps[0], maps[1], maps[2], maps[3], maps[4], maps[5], prm);
-            break;
+        auto launch = [&](auto kern) {
+            cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            kern<<<grid, 192, smem, stream>>>(maps[0], maps[1], maps[2], maps[3], maps[4], maps[5], prm);
+        };
+        switch (Wd) {
+        case 8: launch(k_bfm_batch<8, 1>); break;
+        case 16: launch(k_bfm_batch<16, 1>); break;
+        case 24: launch(k_bfm_batch<24, 1>); break;
+        case 32: launch(k_bfm_batch<32, 1>); break;
+        default: launch(k_bfm_batch<32, 2>); break;
         }
         if ((e = cudaGetLastError())) return cuda_fail(e, "batched tcgen05 contraction kernel");
         if ((e = cudaEventRecord(evg1, stream))) return cuda_fail(e, "event");
@@ -563,11 +578,12 @@ int Engine::batch_run(double *m3mf, double *m3mr, double *m2mr, double *case_ms,
         int maxnm3 = 1;
         for (const CaseP &q : cp) maxnm3 = std::max(maxnm3, q.nm * q.nm * q.nm);
         dim3 rg((maxnm3 + 127) / 128, (unsigned)cp.size());
-        switch (NMT) {
+        switch (Wd) {
         case 8: k_batch_reduce<8><<<rg, 128, 0, stream>>>(d_cases, d_off, part, o, o + t3); break;
         case 16: k_batch_reduce<16><<<rg, 128, 0, stream>>>(d_cases, d_off, part, o, o + t3); break;
         case 24: k_batch_reduce<24><<<rg, 128, 0, stream>>>(d_cases, d_off, part, o, o + t3); break;
-        default: k_batch_reduce<32><<<rg, 128, 0, stream>>>(d_cases, d_off, part, o, o + t3); break;
+        case 32: k_batch_reduce<32><<<rg, 128, 0, stream>>>(d_cases, d_off, part, o, o + t3); break;
+        default: k_batch_reduce<64><<<rg, 128, 0, stream>>>(d_cases, d_off, part, o, o + t3); break;
         }
         if ((e = cudaGetLastError())) return cuda_fail(e, "batch reduction");
         kernels += 2;

@@ -2,10 +2,13 @@
 // batched form k_bfm_batch): FRF products x integration weight x the two TMEM accumulators of
 // one N tile, reduced into per-thread FP32 moment partials.
 //
-// The FRF values one N tile reads are the same for every TMEM lane (row): H_j(w_c) and
-// H_j(w_r + w_c) for the tile's columns c and all j, and H_j(w_r).  Each epilogue warp
-// stages them in its own shared-memory buffer one tile ahead with cp.async (double
-// buffered), so the tile's arithmetic reads shared memory only; no barrier spans warps.
+// An N tile holds NC = 128 / NMT grid columns x NMT modes j.  With more than 32 kept modes the
+// modes are split into JH = 2 halves of NMT = 32 (the B tables hold one half per block of rows)
+// and every grid row is swept once per half, so a thread keeps 5 x 32 FP32 partials whatever
+// the mode count.  The FRF values one N tile reads are the same for every TMEM lane (row):
+// H_j(w_c) and H_j(w_r + w_c) for the tile's columns c and all W = NMT x JH modes, and H_j(w_r).
+// They are staged in shared memory one tile ahead with cp.async (double buffered), so the
+// tile's arithmetic reads shared memory only.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -19,12 +22,14 @@ namespace epi {
 
 using namespace tc;
 
-// The staged values of one N tile: hs[c*NMT + j] = H_j(w_r + w_c0+c), hg[c*NMT + j] =
-// H_j(w_c0+c), hr[j] = H_j(w_r).
+// The staged values of one N tile: hs[c*W + j] = H_j(w_r + w_c0+c), hg[c*W + j] = H_j(w_c0+c),
+// hr[j] = H_j(w_r), j < W = NMT x JH.
+template <int NMT, int JH>
 struct HTile {
-    float2 hs[128];
-    float2 hg[128];
-    float2 hr[32];
+    static constexpr int NC = kBN / NMT, W = NMT * JH;
+    float2 hs[NC * W];
+    float2 hg[NC * W];
+    float2 hr[W];
 };
 
 __device__ __forceinline__ void cp_async16(void *dst, const void *src, bool valid) {
@@ -35,38 +40,42 @@ __device__ __forceinline__ void cp_async16(void *dst, const void *src, bool vali
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
-// One warp stages the tile (r, columns c0 .. c0 + NC - 1) of a grid with nf columns; Hg has nf
-// rows and Hs 2 nf - 1 rows of NMT entries.  Entries past the tables are zero.
-template <int NMT>
-__device__ __forceinline__ void stage(HTile *dst, const float2 *Hg, const float2 *Hs, int nf, int r, int c0,
-                                      int lane) {
-    constexpr int NC = kBN / NMT;
-    constexpr int NCH = NC * NMT / 2;  // 16-byte chunks of hs (and of hg)
-    constexpr int NCR = NMT / 2;
-    for (int x = lane; x < 2 * NCH + NCR; x += 32) {
+// Named barrier of the four epilogue warps (barrier 0 is __syncthreads).
+__device__ __forceinline__ void epi_sync() { asm volatile("bar.sync 1, 128;" ::: "memory"); }
+
+// Threads t = 0 .. nt - 1 stage the tile (r, columns c0 .. c0 + NC - 1) of a grid with nf
+// columns; Hg has nf rows and Hs 2 nf - 1 rows of W entries.  Entries past the tables are zero.
+template <int NMT, int JH>
+__device__ __forceinline__ void stage(HTile<NMT, JH> *dst, const float2 *Hg, const float2 *Hs, int nf, int r,
+                                      int c0, int t, int nt) {
+    constexpr int NC = kBN / NMT, W = NMT * JH;
+    constexpr int NCH = NC * W / 2;  // 16-byte chunks of hs (and of hg)
+    constexpr int NCR = W / 2;
+    for (int x = t; x < 2 * NCH + NCR; x += nt) {
         if (x < NCH) {
-            const int row = r + c0 + (2 * x) / NMT;
-            const bool v = row < 2 * nf - 1;
-            cp_async16(dst->hs + 2 * x, v ? (const void *)(Hs + (size_t)(r + c0) * NMT + 2 * x) : (const void *)Hs, v);
+            const bool v = r + c0 + (2 * x) / W < 2 * nf - 1;
+            cp_async16(dst->hs + 2 * x, v ? (const void *)(Hs + (size_t)(r + c0) * W + 2 * x) : (const void *)Hs, v);
         } else if (x < 2 * NCH) {
             const int y = x - NCH;
-            const bool v = c0 + (2 * y) / NMT < nf;
-            cp_async16(dst->hg + 2 * y, v ? (const void *)(Hg + (size_t)c0 * NMT + 2 * y) : (const void *)Hg, v);
+            const bool v = c0 + (2 * y) / W < nf;
+            cp_async16(dst->hg + 2 * y, v ? (const void *)(Hg + (size_t)c0 * W + 2 * y) : (const void *)Hg, v);
         } else {
             const int y = x - 2 * NCH;
-            cp_async16(dst->hr + 2 * y, Hg + (size_t)r * NMT + 2 * y, true);
+            cp_async16(dst->hr + 2 * y, Hg + (size_t)r * W + 2 * y, true);
         }
     }
     cp_async_commit();
 }
 
-// The tile's contribution to the partial moments of TMEM lane (a, b).  taddr: TMEM address of
-// the lane's D1 accumulator (D3 follows 128 columns later).  Weight of point (r, c): wv_r times
-// the classic edge factor when vect (b1: r is an edge row), else wv_r.
-template <int NMT>
-__device__ __forceinline__ void tile(const HTile &hb, uint32_t taddr, int a, int b, int c0, int nf, bool vect,
-                                     bool b1, float wv_r, float (&acc)[5][NMT]) {
-    constexpr int NC = kBN / NMT;
+// The tile's contribution to the partial moments of TMEM lane (a, b), modes j = jh NMT + j' of
+// half jh.  taddr: TMEM address of the lane's D1 accumulator (D3 follows 128 columns later).
+// Weight of point (r, c): wv_r times the classic edge factor when vect (b1: r is an edge row),
+// else wv_r.
+template <int NMT, int JH>
+__device__ __forceinline__ void tile(const HTile<NMT, JH> &hb, uint32_t taddr, int a, int b, int c0, int nf,
+                                     bool vect, bool b1, float wv_r, int jh, float (&acc)[5][NMT]) {
+    constexpr int NC = kBN / NMT, W = NMT * JH;
+    const int jo = jh * NMT;
     const float2 hra = hb.hr[a];
 #pragma unroll
     for (int q = 0; q < kBN / 32; ++q) {
@@ -91,13 +100,13 @@ __device__ __forceinline__ void tile(const HTile &hb, uint32_t taddr, int a, int
                     if (cval) {
                         const bool b2 = (cg == 0 || cg == nf - 1);
                         wc = vect ? wv_r * ((b1 && b2) ? -0.5f : ((b1 || b2) ? 0.5f : 1.f)) : wv_r;
-                        const float2 hcb = hb.hg[cc * NMT + b];
+                        const float2 hcb = hb.hg[cc * W + b];
                         if (pass == 0) {
                             const float2 t1 = cmul(hra, hcb);  // term 1 at (r, c)
                             PA = make_float2(wc * t1.x, wc * t1.y);
                         } else {
-                            const float2 hsa = hb.hs[cc * NMT + a];
-                            const float2 hsb = hb.hs[cc * NMT + b];
+                            const float2 hsa = hb.hs[cc * W + a];
+                            const float2 hsb = hb.hs[cc * W + b];
                             const float2 t3 = cmul(hcb, conjf2(hsa));  // term 3 at (r, c)
                             PA = make_float2(wc * t3.x, wc * t3.y);
                             const float2 t2 = cmul(hra, conjf2(hsb));  // term 2 at (c, r)
@@ -105,17 +114,17 @@ __device__ __forceinline__ void tile(const HTile &hb, uint32_t taddr, int a, int
                         }
                     }
                 }
-                // columns j >= nm multiply zero B rows and zero FRF entries: they add zeros
+                // modes j >= nm multiply zero B rows and zero FRF entries: they add zeros
                 if (cval) {
                     const float x = __uint_as_float(v[e]);
                     if (pass == 0) {
-                        const float2 hs = hb.hs[c * NMT + j];
+                        const float2 hs = hb.hs[c * W + jo + j];
                         const float F1 = PA.x * hs.x + PA.y * hs.y;  // Re[P1 conj(H_j(s))]
                         acc[0][j] = fmaf(F1, x, acc[0][j]);
                         acc[3][j] = fmaf(wc, x, acc[3][j]);
                     } else {
-                        const float2 hr = hb.hr[j];
-                        const float2 hc = hb.hg[c * NMT + j];
+                        const float2 hr = hb.hr[jo + j];
+                        const float2 hc = hb.hg[c * W + jo + j];
                         const float F3 = hr.x * PA.x - hr.y * PA.y;  // Re[H_j(w_r) P3]
                         const float F2 = hc.x * PB.x - hc.y * PB.y;  // Re[H_j(w_c) P2]
                         acc[1][j] = fmaf(F3, x, acc[1][j]);

@@ -375,7 +375,7 @@ int Engine::run_classic(double *m2mf, double *m2mr, double *m2o2mr, double *m3mf
     const bool diagonal = set.onlyd != 0;
     // The split-precision contraction reduces to moments only; it reads an FP32 A table.
     const bool mixed = !diagonal && precision == BSA_PREC_BF16X3 && !bf_host && !br_host;
-    if (mixed && nme > 32) return fail(BSA_ERR_UNSUPPORTED, "BF16x3 contraction supports at most 32 kept modes");
+    if (mixed && nme > 64) return fail(BSA_ERR_UNSUPPORTED, "BF16x3 contraction supports at most 64 kept modes");
     cudaError_t e;
     if ((e = cudaEventRecord(ev0, stream))) return cuda_fail(e, "event");
     if ((rc = diagonal ? build_psd(ftab) : build_atable(ftab, mixed))) return rc;

@@ -45,7 +45,7 @@ constexpr int kStageBytes = 6 * kTileBytes;      // U hi/lo, Bg hi/lo, Bs hi/lo
 constexpr int kKinds = 5;                        // mr1, mr3, mr2, mf1, mf23
 constexpr int kFlushTiles = 64;                  // FP32 -> FP64 flush period (N tiles)
 constexpr int kBarBytes = 256;                   // mbarriers + TMEM slot
-constexpr int kHBytes = 4 * 2 * (int)sizeof(epi::HTile);  // FRF staging, 2 tiles per epilogue warp
+constexpr int kHBytes = 2 * (int)sizeof(epi::HTile<32, 2>);  // FRF staging, 2 tiles (largest form)
 
 struct Params {
     int nf;          // grid size
@@ -57,22 +57,26 @@ struct Params {
     int nk;          // K chunks (Kp / 64)
     int ks_last;     // 16-wide K steps of the last chunk that hold data (the rest is zero padding)
     int n_ntiles;    // ceil(nf / NC)
+    int g_half;      // B rows of one mode half in the grid table (nf NMT)
+    int s_half;      // B rows of one mode half in the sum table ((2 nf - 1) NMT)
     int wmode;       // kWeightClassicVect or kWeightUniform
     double wval;
-    const float2 *Hg;  // [nf][NMT]  H_j(w_c)
-    const float2 *Hs;  // [2nf-1][NMT]  H_j(w_r + w_c), s = r + c
-    double *part;      // [grid][kKinds][NMT][128]
+    const float2 *Hg;  // [nf][W]  H_j(w_c), W = NMT JH
+    const float2 *Hs;  // [2nf-1][W]  H_j(w_r + w_c), s = r + c
+    double *part;      // [grid][kKinds][W][128]
     int *err;
 };
 
-
-template <int NMT>
+// Grid rows r of CTA g: r = rb + g / MT, then every (grid / MT)-th row; row tile g % MT.  Per row
+// the mode halves jh < JH, per half the N tiles: the tile sequence of all three roles.
+template <int NMT, int JH>
 __global__ void __launch_bounds__(192, 1)
     k_bfm_mixed(const __grid_constant__ CUtensorMap tmUh, const __grid_constant__ CUtensorMap tmUl,
                 const __grid_constant__ CUtensorMap tmGh, const __grid_constant__ CUtensorMap tmGl,
                 const __grid_constant__ CUtensorMap tmSh, const __grid_constant__ CUtensorMap tmSl, const Params p) {
     constexpr int NC = kBN / NMT;         // grid columns per N tile
     constexpr int BROWS = NC * NMT;       // B rows loaded by TMA per tile
+    constexpr int W = NMT * JH;           // FRF table width
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint64_t *bars = (uint64_t *)(smem + kStages * kStageBytes);
@@ -122,24 +126,25 @@ __global__ void __launch_bounds__(192, 1)
             uint32_t it = 0;
             bool ok = true;
             for (int r = p.rb + r0; r < p.re && ok; r += rstep)
-                for (int nt = 0; nt < p.n_ntiles && ok; ++nt)
-                    for (int kc = 0; kc < p.nk && ok; ++kc, ++it) {
-                        const int s = it % kStages;
-                        const uint32_t ph = (it / kStages) & 1u;
-                        if (!mbar_wait(&empty[s], ph ^ 1u, err, 1)) { ok = false; break; }
-                        uint8_t *st = smem + s * kStageBytes;
-                        mbar_expect_tx(&full[s], tx_bytes);
-                        const int x = kc * kBK;
-                        const int yu = r * p.Mp + mt * kBM;
-                        tma_2d(st + 0 * kTileBytes, &tmUh, &full[s], x, yu);
-                        tma_2d(st + 1 * kTileBytes, &tmUl, &full[s], x, yu);
-                        const int yg = nt * BROWS;
-                        tma_2d(st + 2 * kTileBytes, &tmGh, &full[s], x, yg);
-                        tma_2d(st + 3 * kTileBytes, &tmGl, &full[s], x, yg);
-                        const int ys = (r + nt * NC) * NMT;
-                        tma_2d(st + 4 * kTileBytes, &tmSh, &full[s], x, ys);
-                        tma_2d(st + 5 * kTileBytes, &tmSl, &full[s], x, ys);
-                    }
+                for (int jh = 0; jh < JH && ok; ++jh)
+                    for (int nt = 0; nt < p.n_ntiles && ok; ++nt)
+                        for (int kc = 0; kc < p.nk && ok; ++kc, ++it) {
+                            const int s = it % kStages;
+                            const uint32_t ph = (it / kStages) & 1u;
+                            if (!mbar_wait(&empty[s], ph ^ 1u, err, 1)) { ok = false; break; }
+                            uint8_t *st = smem + s * kStageBytes;
+                            mbar_expect_tx(&full[s], tx_bytes);
+                            const int x = kc * kBK;
+                            const int yu = r * p.Mp + mt * kBM;
+                            tma_2d(st + 0 * kTileBytes, &tmUh, &full[s], x, yu);
+                            tma_2d(st + 1 * kTileBytes, &tmUl, &full[s], x, yu);
+                            const int yg = jh * p.g_half + nt * BROWS;
+                            tma_2d(st + 2 * kTileBytes, &tmGh, &full[s], x, yg);
+                            tma_2d(st + 3 * kTileBytes, &tmGl, &full[s], x, yg);
+                            const int ys = jh * p.s_half + (r + nt * NC) * NMT;
+                            tma_2d(st + 4 * kTileBytes, &tmSh, &full[s], x, ys);
+                            tma_2d(st + 5 * kTileBytes, &tmSl, &full[s], x, ys);
+                        }
             // Let the copies already issued land before the CTA can leave (bounded).
             const uint32_t last = it;
             for (uint32_t q = (last > (uint32_t)kStages ? last - kStages : 0); q < last; ++q) {
@@ -157,40 +162,41 @@ __global__ void __launch_bounds__(192, 1)
             uint32_t it = 0, tile = 0;
             bool ok = true;
             for (int r = p.rb + r0; r < p.re && ok; r += rstep)
-                for (int nt = 0; nt < p.n_ntiles && ok; ++nt, ++tile) {
-                    const int buf = tile & 1;
-                    const uint32_t tph = (tile >> 1) & 1u;
-                    if (!mbar_wait(&tempty[buf], tph ^ 1u, err, 2)) { ok = false; break; }
-                    fence_after();
-                    const uint32_t d1 = tmem + buf * 256, d3 = d1 + 128;
-                    for (int kc = 0; kc < p.nk; ++kc, ++it) {
-                        const int s = it % kStages;
-                        const uint32_t ph = (it / kStages) & 1u;
-                        if (!mbar_wait(&full[s], ph, err, 3)) { ok = false; break; }
+                for (int jh = 0; jh < JH && ok; ++jh)
+                    for (int nt = 0; nt < p.n_ntiles && ok; ++nt, ++tile) {
+                        const int buf = tile & 1;
+                        const uint32_t tph = (tile >> 1) & 1u;
+                        if (!mbar_wait(&tempty[buf], tph ^ 1u, err, 2)) { ok = false; break; }
                         fence_after();
-                        const uint32_t base = su32(smem + s * kStageBytes);
-                        // K steps past the data in the last chunk multiply zero padding: skip them
-                        const int nks = kc == p.nk - 1 ? p.ks_last : kBK / 16;
+                        const uint32_t d1 = tmem + buf * 256, d3 = d1 + 128;
+                        for (int kc = 0; kc < p.nk; ++kc, ++it) {
+                            const int s = it % kStages;
+                            const uint32_t ph = (it / kStages) & 1u;
+                            if (!mbar_wait(&full[s], ph, err, 3)) { ok = false; break; }
+                            fence_after();
+                            const uint32_t base = su32(smem + s * kStageBytes);
+                            // K steps past the data in the last chunk multiply zero padding: skip them
+                            const int nks = kc == p.nk - 1 ? p.ks_last : kBK / 16;
 #pragma unroll
-                        for (int ks = 0; ks < kBK / 16; ++ks) {
-                            if (ks >= nks) break;
-                            const uint32_t off = ks * 32;
-                            const uint64_t uh = sdesc(base + 0 * kTileBytes + off), ul = sdesc(base + 1 * kTileBytes + off);
-                            const uint64_t gh = sdesc(base + 2 * kTileBytes + off), gl = sdesc(base + 3 * kTileBytes + off);
-                            const uint64_t sh = sdesc(base + 4 * kTileBytes + off), sl = sdesc(base + 5 * kTileBytes + off);
-                            const uint32_t acc = (kc > 0 || ks > 0) ? 1u : 0u;
-                            mma(d1, uh, gh, acc);
-                            mma(d1, uh, gl, 1u);
-                            mma(d1, ul, gh, 1u);
-                            mma(d3, uh, sh, acc);
-                            mma(d3, uh, sl, 1u);
-                            mma(d3, ul, sh, 1u);
+                            for (int ks = 0; ks < kBK / 16; ++ks) {
+                                if (ks >= nks) break;
+                                const uint32_t off = ks * 32;
+                                const uint64_t uh = sdesc(base + 0 * kTileBytes + off), ul = sdesc(base + 1 * kTileBytes + off);
+                                const uint64_t gh = sdesc(base + 2 * kTileBytes + off), gl = sdesc(base + 3 * kTileBytes + off);
+                                const uint64_t sh = sdesc(base + 4 * kTileBytes + off), sl = sdesc(base + 5 * kTileBytes + off);
+                                const uint32_t acc = (kc > 0 || ks > 0) ? 1u : 0u;
+                                mma(d1, uh, gh, acc);
+                                mma(d1, uh, gl, 1u);
+                                mma(d1, ul, gh, 1u);
+                                mma(d3, uh, sh, acc);
+                                mma(d3, uh, sl, 1u);
+                                mma(d3, ul, sh, 1u);
+                            }
+                            mma_commit(&empty[s]);  // stage free once these MMAs have read it
                         }
-                        mma_commit(&empty[s]);  // stage free once these MMAs have read it
+                        if (!ok) break;
+                        mma_commit(&tfull[buf]);  // accumulators ready for the epilogue
                     }
-                    if (!ok) break;
-                    mma_commit(&tfull[buf]);  // accumulators ready for the epilogue
-                }
             // Every MMA issued so far completes before TMEM is released.
             mma_commit(done);
             const uint64_t t0 = gtime();
@@ -200,7 +206,11 @@ __global__ void __launch_bounds__(192, 1)
         __syncwarp();
     } else {
         // ---------------- epilogue: FRF x weight, reduce to moments ----------------
+        // The four warps share one double-buffered FRF staging slot (epi_sync orders it).  After
+        // a failed wait a warp keeps walking the tile sequence without work, so every warp
+        // reaches every epi_sync.
         const int quarter = warp & 3;
+        const int et = threadIdx.x - 64;               // 0 .. 127
         const int row = quarter * 32 + lane;          // TMEM lane = row of the M tile
         const int grow = mt * kBM + row;               // row of U(f_r): a * nm + b
         const bool vrow = grow < p.nm * p.nm;
@@ -208,49 +218,65 @@ __global__ void __launch_bounds__(192, 1)
         const uint32_t lane_base = tmem + ((uint32_t)(quarter * 32) << 16);
         const float wvf = (float)p.wval;
         const bool vect = p.wmode == kWeightClassicVect;
-        epi::HTile *hbw = (epi::HTile *)(smem + kStages * kStageBytes + kBarBytes) + quarter * 2;
-        double *part = p.part + (size_t)blockIdx.x * kKinds * NMT * 128 + row;
-        for (int k = 0; k < kKinds * NMT; ++k) part[(size_t)k * 128] = 0.0;
+        using HT = epi::HTile<NMT, JH>;
+        HT *hbs = (HT *)(smem + kStages * kStageBytes + kBarBytes);
+        double *part = p.part + (size_t)blockIdx.x * kKinds * W * 128 + row;
+        for (int k = 0; k < kKinds * W; ++k) part[(size_t)k * 128] = 0.0;
         float acc[kKinds][NMT];
+        auto zero = [&]() {
 #pragma unroll
-        for (int k = 0; k < kKinds; ++k)
+            for (int k = 0; k < kKinds; ++k)
 #pragma unroll
-            for (int j = 0; j < NMT; ++j) acc[k][j] = 0.f;
-        auto flush = [&]() {
+                for (int j = 0; j < NMT; ++j) acc[k][j] = 0.f;
+        };
+        // Only this thread adds into its partials; a reduction (fire and forget) keeps the
+        // 5 x NMT old values out of the registers, and one thread's adds to one address apply
+        // in program order, so the sums stay deterministic.
+        auto flush = [&](int jh) {
 #pragma unroll
             for (int k = 0; k < kKinds; ++k)
 #pragma unroll
                 for (int j = 0; j < NMT; ++j) {
-                    part[(size_t)(k * NMT + j) * 128] += (double)acc[k][j];
+                    atomicAdd(part + (size_t)(k * W + jh * NMT + j) * 128, (double)acc[k][j]);
                     acc[k][j] = 0.f;
                 }
         };
         uint32_t tile = 0;
         bool ok = true;
-        if (p.rb + r0 < p.re) epi::stage<NMT>(hbw, p.Hg, p.Hs, p.nf, p.rb + r0, 0, lane);
-        for (int r = p.rb + r0; r < p.re && ok; r += rstep) {
+        if (p.rb + r0 < p.re) epi::stage<NMT, JH>(hbs, p.Hg, p.Hs, p.nf, p.rb + r0, 0, et, 128);
+        for (int r = p.rb + r0; r < p.re; r += rstep) {
             const bool b1 = (r == 0 || r == p.nf - 1);
             const float wv_r = r < p.sym_rows ? 2.f * wvf : wvf;  // central symmetry: the mirror row
-            for (int nt = 0; nt < p.n_ntiles; ++nt, ++tile) {
-                const int buf = tile & 1;
-                const uint32_t tph = (tile >> 1) & 1u;
-                epi::cp_async_wait_all();
-                __syncwarp();
-                // stage the next tile's FRF values while this one is reduced
-                if (nt + 1 < p.n_ntiles)
-                    epi::stage<NMT>(hbw + (buf ^ 1), p.Hg, p.Hs, p.nf, r, (nt + 1) * NC, lane);
-                else if (r + rstep < p.re)
-                    epi::stage<NMT>(hbw + (buf ^ 1), p.Hg, p.Hs, p.nf, r + rstep, 0, lane);
-                // warp-uniform outcome: tcgen05.ld below is .sync.aligned
-                const bool got = __all_sync(0xffffffffu, mbar_wait(&tfull[buf], tph, err, 4));
-                if (!got) { ok = false; break; }
-                fence_after();
-                epi::tile<NMT>(hbw[buf], lane_base + buf * 256, a, b, nt * NC, p.nf, vect, b1, wv_r, acc);
-                fence_before();
-                mbar_arrive(&tempty[buf]);
-                if ((nt + 1) % kFlushTiles == 0) flush();
+            for (int jh = 0; jh < JH; ++jh) {
+                zero();
+                for (int nt = 0; nt < p.n_ntiles; ++nt, ++tile) {
+                    const int buf = tile & 1;
+                    const uint32_t tph = (tile >> 1) & 1u;
+                    epi::cp_async_wait_all();
+                    epi::epi_sync();  // this tile's values are in; the other slot is no longer read
+                    // stage the next tile's FRF values (they depend on the row and columns only)
+                    if (nt + 1 < p.n_ntiles)
+                        epi::stage<NMT, JH>(hbs + (buf ^ 1), p.Hg, p.Hs, p.nf, r, (nt + 1) * NC, et, 128);
+                    else if (jh + 1 < JH)
+                        epi::stage<NMT, JH>(hbs + (buf ^ 1), p.Hg, p.Hs, p.nf, r, 0, et, 128);
+                    else if (r + rstep < p.re)
+                        epi::stage<NMT, JH>(hbs + (buf ^ 1), p.Hg, p.Hs, p.nf, r + rstep, 0, et, 128);
+                    if (ok) {
+                        // warp-uniform outcome: tcgen05.ld below is .sync.aligned
+                        ok = __all_sync(0xffffffffu, mbar_wait(&tfull[buf], tph, err, 4));
+                        if (ok) {
+                            fence_after();
+                            epi::tile<NMT, JH>(hbs[buf], lane_base + buf * 256, a, b, nt * NC, p.nf, vect, b1, wv_r,
+                                               jh, acc);
+                            fence_before();
+                            mbar_arrive(&tempty[buf]);
+                            // one flush site: a second inlined copy of the flush made the
+                            // compiler spill the accumulators
+                            if ((nt + 1) % kFlushTiles == 0 || nt + 1 == p.n_ntiles) flush(jh);
+                        }
+                    }
+                }
             }
-            flush();
         }
         epi::cp_async_wait_all();
     }
@@ -269,7 +295,7 @@ __global__ void __launch_bounds__(192, 1)
 __global__ void k_prep_u(int nm, int K, int Kp, int Mp, const float *__restrict__ A, const double *__restrict__ Q,
                          __nv_bfloat16 *__restrict__ Uh, __nv_bfloat16 *__restrict__ Ul) {
     const int r = blockIdx.x, k0 = blockIdx.y * 64;
-    __shared__ float As[64][33], Qs[64][33];
+    __shared__ float As[64][65], Qs[64][65];  // nm <= 64
     const float *Ar = A + (size_t)r * K * nm;
     for (int e = threadIdx.x; e < 64 * nm; e += blockDim.x) {
         const int kk = e / nm, m = e % nm, k = k0 + kk;
@@ -292,9 +318,11 @@ __global__ void k_prep_u(int nm, int K, int Kp, int Mp, const float *__restrict_
     }
 }
 
-// T[(t*NMT + j)][k] = A(src(t))[k][j]; src(t) < 0 gives a zero row (j >= nm too).
-__global__ void k_prep_b(int nm, int NMT, int K, int Kp, int nf, int n_pad, int trunc, int sum_base, int is_sum,
-                         const float *__restrict__ A, __nv_bfloat16 *__restrict__ Th, __nv_bfloat16 *__restrict__ Tl) {
+// T[(t*NMT + j)][k] = A(src(t))[k][j0 + j], j < NMT <= 32; src(t) < 0 gives a zero row (j0 + j >= nm
+// too).
+__global__ void k_prep_b(int nm, int NMT, int j0, int K, int Kp, int nf, int n_pad, int trunc, int sum_base,
+                         int is_sum, const float *__restrict__ A, __nv_bfloat16 *__restrict__ Th,
+                         __nv_bfloat16 *__restrict__ Tl) {
     const int t = blockIdx.x, k0 = blockIdx.y * 64;
     int src = t;
     if (is_sum) {
@@ -306,16 +334,16 @@ __global__ void k_prep_b(int nm, int NMT, int K, int Kp, int nf, int n_pad, int 
         }
     }
     __shared__ float As[64][33];
-    for (int e = threadIdx.x; e < 64 * nm; e += blockDim.x) {
-        const int kk = e / nm, m = e % nm, k = k0 + kk;
-        As[kk][m] = (src >= 0 && k < K) ? A[((size_t)src * K + k) * nm + m] : 0.f;
+    for (int e = threadIdx.x; e < 64 * NMT; e += blockDim.x) {
+        const int kk = e / NMT, jj = e % NMT, m = j0 + jj, k = k0 + kk;
+        As[kk][jj] = (src >= 0 && k < K && m < nm) ? A[((size_t)src * K + k) * nm + m] : 0.f;
     }
     __syncthreads();
     for (int e = threadIdx.x; e < NMT * 8; e += blockDim.x) {
         const int j = e >> 3, kv = (e & 7) * 8;
         __align__(16) __nv_bfloat16 hi[8], lo[8];
 #pragma unroll
-        for (int q = 0; q < 8; ++q) split_bf16f(j < nm ? As[kv + q][j] : 0.f, hi[q], lo[q]);
+        for (int q = 0; q < 8; ++q) split_bf16f(As[kv + q][j], hi[q], lo[q]);
         const size_t o = ((size_t)t * NMT + j) * Kp + k0 + kv;
         *(uint4 *)(Th + o) = *(const uint4 *)hi;
         *(uint4 *)(Tl + o) = *(const uint4 *)lo;
@@ -366,9 +394,9 @@ cudaError_t prep_u(cudaStream_t st, int nf, int nm, int K, int Kp, int Mp, const
     return cudaGetLastError();
 }
 
-cudaError_t prep_b(cudaStream_t st, int rows, int nm, int NMT, int K, int Kp, int nf, int n_pad, int trunc,
+cudaError_t prep_b(cudaStream_t st, int rows, int nm, int NMT, int j0, int K, int Kp, int nf, int n_pad, int trunc,
                    int sum_base, int is_sum, const float *A, __nv_bfloat16 *Th, __nv_bfloat16 *Tl) {
-    k_prep_b<<<dim3(rows, Kp / 64), 256, 0, st>>>(nm, NMT, K, Kp, nf, n_pad, trunc, sum_base, is_sum, A, Th, Tl);
+    k_prep_b<<<dim3(rows, Kp / 64), 256, 0, st>>>(nm, NMT, j0, K, Kp, nf, n_pad, trunc, sum_base, is_sum, A, Th, Tl);
     return cudaGetLastError();
 }
 
@@ -378,12 +406,13 @@ cudaError_t prep_h(cudaStream_t st, int nf, int nm, int NMT, const double *f, Fr
     return cudaGetLastError();
 }
 
-template <int NMT>
+template <int NMT, int JH>
 static cudaError_t launch_gemm(cudaStream_t st, const CUtensorMap *maps, const Params &p, int grid) {
     const size_t smem = (size_t)kStages * kStageBytes + 1024 + kBarBytes + kHBytes;
-    cudaError_t e = cudaFuncSetAttribute(k_bfm_mixed<NMT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e =
+        cudaFuncSetAttribute(k_bfm_mixed<NMT, JH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    k_bfm_mixed<NMT><<<grid, 192, smem, st>>>(maps[0], maps[1], maps[2], maps[3], maps[4], maps[5], p);
+    k_bfm_mixed<NMT, JH><<<grid, 192, smem, st>>>(maps[0], maps[1], maps[2], maps[3], maps[4], maps[5], p);
     return cudaGetLastError();
 }
 
@@ -393,8 +422,11 @@ int Engine::contract_mixed(const PointSrc &ps, long long npts, double *m3mf, dou
     using namespace mixed;
     (void)npts;
     const int nf = ps.nf, nm = nme;
-    if (nm > 32) return fail(BSA_ERR_UNSUPPORTED, "BF16x3 contraction supports at most 32 kept modes");
+    if (nm > 64) return fail(BSA_ERR_UNSUPPORTED, "BF16x3 contraction supports at most 64 kept modes");
+    // FRF-table width per mode half; above 32 modes two halves of 32 (JH = 2)
     const int NMT = nm <= 8 ? 8 : nm <= 16 ? 16 : nm <= 24 ? 24 : 32;
+    const int JH = nm > 32 ? 2 : 1;
+    const int W = NMT * JH;
     const int NC = kBN / NMT;
     const int Kp = ((K + kBK - 1) / kBK) * kBK;
     const int Mp = ((nm * nm + kBM - 1) / kBM) * kBM;
@@ -406,34 +438,42 @@ int Engine::contract_mixed(const PointSrc &ps, long long npts, double *m3mf, dou
         return cuda_fail(e, "device query");
     int grid = (nsm / MT) * MT;
     if (grid < MT) grid = MT;
-    const size_t uel = (size_t)nf * Mp * Kp, gel = (size_t)nf * NMT * Kp, sel = (size_t)ns * NMT * Kp;
+    const size_t uel = (size_t)nf * Mp * Kp, gel = (size_t)JH * nf * NMT * Kp, sel = (size_t)JH * ns * NMT * Kp;
     const size_t bytesA = 2 * uel * 2, bytesB = 2 * (gel + sel) * 2;
-    const size_t bytesH = sizeof(float2) * (size_t)(nf + ns) * NMT;
-    const size_t bytesP = sizeof(double) * (size_t)grid * kKinds * NMT * 128;
+    const size_t bytesH = sizeof(float2) * (size_t)(nf + ns) * W;
+    const size_t bytesP = sizeof(double) * (size_t)grid * kKinds * W * 128;
     if ((e = dMixA.reserve(bytesA)) || (e = dMixB.reserve(bytesB)) || (e = dMixH.reserve(bytesH + 256)) ||
         (e = dMixPart.reserve(bytesP + 256)))
         return cuda_fail(e, "allocating BF16x3 operands");
     __nv_bfloat16 *Uh = dMixA.as<__nv_bfloat16>(), *Ul = Uh + uel;
     __nv_bfloat16 *Gh = dMixB.as<__nv_bfloat16>(), *Gl = Gh + gel, *Sh = Gl + gel, *Sl = Sh + sel;
-    float2 *Hg = dMixH.as<float2>(), *Hs = Hg + (size_t)nf * NMT;
+    float2 *Hg = dMixH.as<float2>(), *Hs = Hg + (size_t)nf * W;
     int *derr = (int *)((char *)dMixPart.p + bytesP);
     if ((e = cudaEventRecord(ev2, stream))) return cuda_fail(e, "event");
     if ((e = cudaMemsetAsync(derr, 0, sizeof(int), stream))) return cuda_fail(e, "memset");
     {
+        const float *A = dA32.as<float>();
         dim3 gu(nf, Kp / 64);
-        k_prep_u<<<gu, 256, 0, stream>>>(nm, K, Kp, Mp, dA32.as<float>(), dQ.as<double>(), Uh, Ul);
+        k_prep_u<<<gu, 256, 0, stream>>>(nm, K, Kp, Mp, A, dQ.as<double>(), Uh, Ul);
         dim3 gg(nf, Kp / 64), gs(ns, Kp / 64);
-        k_prep_b<<<gg, 256, 0, stream>>>(nm, NMT, K, Kp, nf, ps.n_pad, ps.trunc, ps.sum_base, 0, dA32.as<float>(), Gh, Gl);
-        k_prep_b<<<gs, 256, 0, stream>>>(nm, NMT, K, Kp, nf, ps.n_pad, ps.trunc, ps.sum_base, 1, dA32.as<float>(), Sh, Sl);
-        const int nh = (nf + ns) * NMT;
-        k_prep_h<<<(nh + 255) / 256, 256, 0, stream>>>(nf, nm, NMT, ps.fgrid, frf(), Hg, Hs);
+        // B tables: one block of rows per mode half, modes jh NMT .. jh NMT + NMT - 1
+        for (int jh = 0; jh < JH; ++jh) {
+            const size_t og = (size_t)jh * nf * NMT * Kp, os = (size_t)jh * ns * NMT * Kp;
+            k_prep_b<<<gg, 256, 0, stream>>>(nm, NMT, jh * NMT, K, Kp, nf, ps.n_pad, ps.trunc, ps.sum_base, 0, A,
+                                             Gh + og, Gl + og);
+            k_prep_b<<<gs, 256, 0, stream>>>(nm, NMT, jh * NMT, K, Kp, nf, ps.n_pad, ps.trunc, ps.sum_base, 1, A,
+                                             Sh + os, Sl + os);
+        }
+        const int nh = (nf + ns) * W;
+        k_prep_h<<<(nh + 255) / 256, 256, 0, stream>>>(nf, nm, W, ps.fgrid, frf(), Hg, Hs);
         if ((e = cudaGetLastError())) return cuda_fail(e, "BF16x3 operand preparation");
-        kernels += 4;
+        kernels += 2 + 2 * JH;
     }
     CUtensorMap maps[6];
+    const uint64_t grows = (uint64_t)JH * nf * NMT, srows = (uint64_t)JH * ns * NMT;
     if (!make_map(&maps[0], Uh, Kp, (uint64_t)nf * Mp, kBM) || !make_map(&maps[1], Ul, Kp, (uint64_t)nf * Mp, kBM) ||
-        !make_map(&maps[2], Gh, Kp, (uint64_t)nf * NMT, NC * NMT) || !make_map(&maps[3], Gl, Kp, (uint64_t)nf * NMT, NC * NMT) ||
-        !make_map(&maps[4], Sh, Kp, (uint64_t)ns * NMT, NC * NMT) || !make_map(&maps[5], Sl, Kp, (uint64_t)ns * NMT, NC * NMT))
+        !make_map(&maps[2], Gh, Kp, grows, NC * NMT) || !make_map(&maps[3], Gl, Kp, grows, NC * NMT) ||
+        !make_map(&maps[4], Sh, Kp, srows, NC * NMT) || !make_map(&maps[5], Sl, Kp, srows, NC * NMT))
         return fail(BSA_ERR_CUDA, "cuTensorMapEncodeTiled failed");
     Params prm{};
     prm.nf = nf;
@@ -446,6 +486,8 @@ int Engine::contract_mixed(const PointSrc &ps, long long npts, double *m3mf, dou
     prm.nk = Kp / kBK;
     prm.ks_last = (K - (prm.nk - 1) * kBK + 15) / 16;
     prm.n_ntiles = (nf + NC - 1) / NC;
+    prm.g_half = nf * NMT;
+    prm.s_half = ns * NMT;
     prm.wmode = ps.wmode;
     prm.wval = ps.wval;
     prm.Hg = Hg;
@@ -453,18 +495,19 @@ int Engine::contract_mixed(const PointSrc &ps, long long npts, double *m3mf, dou
     prm.part = dMixPart.as<double>();
     prm.err = derr;
     if ((e = cudaEventRecord(evg0, stream))) return cuda_fail(e, "event");
-    switch (NMT) {
-    case 8: e = launch_gemm<8>(stream, maps, prm, grid); break;
-    case 16: e = launch_gemm<16>(stream, maps, prm, grid); break;
-    case 24: e = launch_gemm<24>(stream, maps, prm, grid); break;
-    default: e = launch_gemm<32>(stream, maps, prm, grid); break;
+    switch (NMT * JH) {
+    case 8: e = launch_gemm<8, 1>(stream, maps, prm, grid); break;
+    case 16: e = launch_gemm<16, 1>(stream, maps, prm, grid); break;
+    case 24: e = launch_gemm<24, 1>(stream, maps, prm, grid); break;
+    case 32: e = launch_gemm<32, 1>(stream, maps, prm, grid); break;
+    default: e = launch_gemm<32, 2>(stream, maps, prm, grid); break;
     }
     if (e) return cuda_fail(e, "BF16x3 tcgen05 contraction kernel");
     if ((e = cudaEventRecord(evg1, stream))) return cuda_fail(e, "event");
     const long long nm3 = (long long)nm * nm * nm;
     if ((e = dOut.reserve(sizeof(double) * (3 * (size_t)nm * nm + 2 * (size_t)nm3)))) return cuda_fail(e, "out");
     double *o = dOut.as<double>() + 3 * (size_t)nm * nm;
-    k_mixed_reduce<<<(unsigned)((nm3 + 127) / 128), 128, 0, stream>>>(nm, NMT, MT, grid, prm.part, o, o + nm3);
+    k_mixed_reduce<<<(unsigned)((nm3 + 127) / 128), 128, 0, stream>>>(nm, W, MT, grid, prm.part, o, o + nm3);
     if ((e = cudaGetLastError())) return cuda_fail(e, "BF16x3 reduction");
     kernels += 2;
     std::vector<double> h(2 * (size_t)nm3);

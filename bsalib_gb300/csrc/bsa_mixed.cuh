@@ -12,8 +12,9 @@ namespace mixed {
 // U[(r*Mp + a*nm + b)][k] = Q[k][a] A(f_r)[k][b], r < nf, row stride Kp (k >= K zero)
 cudaError_t prep_u(cudaStream_t st, int nf, int nm, int K, int Kp, int Mp, const float *A, const double *Q,
                    __nv_bfloat16 *Uh, __nv_bfloat16 *Ul);
-// T[(t*NMT + j)][k] = A(row of t)[k][j] for `rows` row blocks (is_sum: the f1 + f2 table)
-cudaError_t prep_b(cudaStream_t st, int rows, int nm, int NMT, int K, int Kp, int nf, int n_pad, int trunc,
+// T[(t*NMT + j)][k] = A(row of t)[k][j0 + j] for `rows` row blocks (is_sum: the f1 + f2 table),
+// NMT <= 32
+cudaError_t prep_b(cudaStream_t st, int rows, int nm, int NMT, int j0, int K, int Kp, int nf, int n_pad, int trunc,
                    int sum_base, int is_sum, const float *A, __nv_bfloat16 *Th, __nv_bfloat16 *Tl);
 // FRF tables Hg[c][j] = H_j(w_c), Hs[s][j] = H_j(w_r + w_c), s = r + c < 2 nf - 1
 cudaError_t prep_h(cudaStream_t st, int nf, int nm, int NMT, const double *f, FrfPar frf, float2 *Hg, float2 *Hs);

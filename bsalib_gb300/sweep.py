@@ -3,7 +3,7 @@
   python -m bsalib_gb300.sweep [--structures 8] [--winds 8] [--seed0 5000] [--json out.json]
 
 Cases are seeded random cantilevers (`problem.random_structure`: nodes 30-600, kept modes
-4-32, Classic grids of 129-513 points), each under `winds` mean wind speeds spread evenly
+4-40, Classic grids of 129-513 points), each under `winds` mean wind speeds spread evenly
 over 15-50 m/s.  The batch is evaluated once untimed
 and once timed (device time of the whole sweep and wall time of the call); each case is then
 run on its own with the split precision, the sequential baseline.  Reported: aggregate Classic
@@ -24,7 +24,7 @@ from .problem import random_structure
 
 def cases(structures, winds, seed0):
     us = np.linspace(15.0, 50.0, winds) if winds > 1 else [30.0]
-    return [random_structure(seed0 + k, nodes=(30, 600), modes=(4, 32), nfreq_grid=(129, 513), U_mean=float(u))
+    return [random_structure(seed0 + k, nodes=(30, 600), modes=(4, 40), nfreq_grid=(129, 513), U_mean=float(u))
             for k in range(structures) for u in us]
 
 

@@ -219,7 +219,7 @@ int bsa_gpu_setClassicSymmetry(int on);
  * process (app/bsa.F90:72-110: setup, bsa_Run, finalise); a parametric study repeats that.
  *
  * bsa_gpu_batchAdd snapshots the current inputs as case *case_id (validated as by bsa_Run;
- * full-tensor spectra, at most 32 kept modes); the caller may then change any input and add
+ * full-tensor spectra, at most 64 kept modes); the caller may then change any input and add
  * the next case.  bsa_gpu_batchRun evaluates every case added since the last
  * bsa_gpu_batchClear on its full Classic grid (the split precision of bsa_gpu_setPrecision's
  * BSA_PREC_BF16X3, whatever the current precision) and writes, concatenated in case order,

@@ -3,7 +3,8 @@
 Each case of a batch must give the moments its own split-precision analysis gives: the same
 FP32 partials are summed in FP64 in another order, so third moments agree to 1e-9 relative
 (max-norm), second moments to 1e-12.  Against the FP64 path the mixed-precision bar holds
-(third moments 1e-4 relative).  Cases of every FRF-table width (8, 16, 24, 32 kept modes),
+(third moments 1e-4 relative).  Cases of every FRF-table width (8, 16, 24, 32 kept modes, and
+two halves of 32 above that),
 different grids and load sizes share one batch; the library's own inputs are left as they
 were.
 """
@@ -39,6 +40,9 @@ CASES = [
     random_structure(12, nodes=(230, 230), modes=(16, 16), nfreq_grid=(129, 129)),
     random_structure(13, nodes=(40, 40), modes=(5, 5), nfreq_grid=(33, 33)),
     random_structure(14, nodes=(150, 150), modes=(20, 20), nfreq_grid=(97, 97)),
+    # more than 32 kept modes: two mode halves per grid row
+    random_structure(15, nodes=(90, 90), modes=(40, 40), nfreq_grid=(33, 33)),
+    tall_building(nodes=48, modes=64, nfreqs=9, df=0.5, seed=14),
 ]
 
 
@@ -65,7 +69,7 @@ def test_batch_matches_single_analyses(batch):
 
 def test_batch_within_mixed_bar_of_fp64(batch):
     out, _ = batch
-    for k in (1, 3, 5):
+    for k in (1, 3, 5, 8):
         ref = single(CASES[k], api.PREC_FP64)
         assert rel(out[k]["m3mr"], ref["m3mr_cls"]) < 1e-4, k
         assert rel(out[k]["m3mf"], ref["m3mf_cls"]) < 1e-4, k
@@ -118,12 +122,11 @@ def test_batch_leaves_current_inputs(bsalib):
 
 def test_batch_rejects_unsupported_cases(bsalib):
     sw = api.Sweep()
-    big = tall_building(nodes=60, modes=36, nfreqs=9, df=0.5, seed=2)
+    big = tall_building(nodes=60, modes=70, nfreqs=9, df=0.5, seed=2)
     s = api.BsaSession(big, precision=api.PREC_BF16X3)
     try:
-        if s.nmodes() > 32:
-            with pytest.raises(api.BsaError, match="32 kept modes"):
-                sw.add_current()
+        with pytest.raises(api.BsaError, match="64 kept modes"):
+            sw.add_current()
     finally:
         s.close()
     d = copy.deepcopy(CASES[1])

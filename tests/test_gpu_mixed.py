@@ -39,6 +39,10 @@ CASES = [
     ("bldg_nm12", tall_building(nodes=64, modes=12, nfreqs=21, df=0.2, seed=3)),
     ("bldg_nm24", tall_building(nodes=100, modes=24, nfreqs=25, df=0.16, seed=5)),
     ("bldg_nm30", tall_building(nodes=50, modes=30, nfreqs=9, df=0.5, seed=8)),
+    # more than 32 kept modes: the modes split into two halves of 32, each row swept twice
+    ("bldg_nm33", tall_building(nodes=40, modes=33, nfreqs=11, df=0.4, seed=12)),
+    ("bldg_nm40_2tc", tall_building(nodes=70, modes=40, nfreqs=13, df=0.3, seed=13)),
+    ("bldg_nm64", tall_building(nodes=48, modes=64, nfreqs=9, df=0.5, seed=14)),
 ]
 
 
@@ -76,8 +80,9 @@ def test_mixed_building_129_grid():
     assert rel(mix["sk"], ref["sk"]) < TOL_SK
 
 
-def test_mixed_is_deterministic():
-    prob = tall_building(nodes=40, modes=16, nfreqs=17, df=0.25, seed=30)
+@pytest.mark.parametrize("modes", [16, 40])
+def test_mixed_is_deterministic(modes):
+    prob = tall_building(nodes=40, modes=modes, nfreqs=17, df=0.25, seed=30)
     s = api.BsaSession(prob, precision=api.PREC_BF16X3)
     try:
         a = s.run()["m3mr_cls"]
@@ -85,3 +90,23 @@ def test_mixed_is_deterministic():
     finally:
         s.close()
     assert np.array_equal(a, b)
+
+
+def test_mixed_more_than_32_modes_with_symmetry_and_shards():
+    """Two mode halves combined with the central symmetry and row shards."""
+    prob = tall_building(nodes=40, modes=36, nfreqs=13, df=0.3, seed=31)
+    ref, _ = both(prob)
+    s = api.BsaSession(prob, precision=api.PREC_BF16X3)
+    try:
+        s.set_symmetry(True)
+        sym = s.run()["m3mr_cls"]
+        s.set_symmetry(False)
+        nf = prob.classic_nf()
+        parts = []
+        for r0, r1 in ((0, 7), (7, nf)):
+            s.set_rows(r0, r1)
+            parts.append(s.run()["m3mr_cls"])
+    finally:
+        s.close()
+    assert rel(sym, ref["m3mr_cls"]) < TOL_M3
+    assert rel(parts[0] + parts[1], ref["m3mr_cls"]) < TOL_M3
