@@ -59,7 +59,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     with cf.ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 2)) as ex:
         objs = list(ex.map(one, sources()))
     tmp = LIB + ".tmp"
-    cmd = [exe, *ARCH, "-shared", "-cudart", "static", "-o", tmp, *objs]
+    cmd = [exe, *ARCH, "-shared", "-cudart", "static", "-o", tmp, *objs, "-ldl"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")

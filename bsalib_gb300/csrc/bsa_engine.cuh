@@ -94,7 +94,8 @@ struct Engine {
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr;
     DevBuf dL, dQ, dLogc, dPsdPar, dFrfM, dFrfK, dFrfC, dFreq, dS, dA, dPartF, dPartR, dOut, dPsdF, dWf, dPts,
-        dPtsD, dBF, dBR, dMixA, dMixB, dMixH, dMixPart, dA32, dZones, dZidx, dWd3, dWd2, dMshT, dMshIdx, dLogc32, dL32;
+        dPtsD, dBF, dBR, dMixA, dMixB, dMixH, dMixPart, dA32, dZones, dZidx, dWd3, dWd2, dMshT, dMshIdx, dLogc32, dL32,
+        dPod;
 
     // stats
     double last_ms = 0, last_ms_contraction = 0, last_ms_gemm = 0, last_points = 0;
@@ -110,7 +111,9 @@ struct Engine {
     int validate();
     int upload_problem();
     FrfPar frf() const;
-    int build_atable(const std::vector<double> &freqs, bool fp32 = false);
+    // msh: the table serves the Mesher functions, whose POD form may be truncated
+    int build_atable(const std::vector<double> &freqs, bool fp32 = false, bool msh = false);
+    int pod_atable(const std::vector<double> &freqs, bool fp32);
     int build_psd(const std::vector<double> &freqs);
     // dimM_psd_ / dimM_bisp_ (src/bsa/BsaLibImpl.F90:313-355): nm / nm for the diagonal-only
     // spectra, nm^2 / nm^3 otherwise.

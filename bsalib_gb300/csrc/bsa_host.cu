@@ -78,7 +78,7 @@ void Engine::reset_inputs() {
 void Engine::free_device() {
     for (DevBuf *b : {&dL, &dQ, &dLogc, &dPsdPar, &dFrfM, &dFrfK, &dFrfC, &dFreq, &dS, &dA, &dPartF, &dPartR,
                       &dOut, &dPsdF, &dWf, &dPts, &dPtsD, &dBF, &dBR, &dMixA, &dMixB, &dMixH, &dMixPart, &dA32,
-                      &dZones, &dZidx, &dWd3, &dWd2, &dMshT, &dMshIdx, &dLogc32, &dL32})
+                      &dZones, &dZidx, &dWd3, &dWd2, &dMshT, &dMshIdx, &dLogc32, &dL32, &dPod})
         b->release();
     if (stream) cudaStreamDestroy(stream);
     stream = nullptr;
@@ -278,7 +278,8 @@ int Engine::build_psd(const std::vector<double> &freqs) {
 }
 
 // Nodal PSD + A(f) for a host list of frequencies, into dA (FP64) or dA32 (FP32) rows.
-int Engine::build_atable(const std::vector<double> &freqs, bool fp32) {
+int Engine::build_atable(const std::vector<double> &freqs, bool fp32, bool msh) {
+    if (msh && pod_truncates()) return pod_atable(freqs, fp32);  // bsa_pod.cu
     const int nf = (int)freqs.size();
     const int ntc = (int)set.tc.size();
     cudaError_t e;
@@ -550,8 +551,6 @@ int Engine::run_points(const double *fi, const double *fj, const double *w, doub
     int rc = upload_problem();
     if (rc) return rc;
     if (npts <= 0) return fail(BSA_ERR_ARG, "empty point set");
-    if (pod_truncates())
-        return fail(BSA_ERR_UNSUPPORTED, "truncated POD (getFM_full_tm_scalar_msh_POD_ with dropped modes) is not on this path");
     // Distinct frequencies: f1, f2 and f1+f2 of every point share one A table.
     std::vector<double> ftab;
     ftab.reserve(3 * (size_t)npts);
@@ -579,7 +578,7 @@ int Engine::run_points(const double *fi, const double *fj, const double *w, doub
     }
     cudaError_t e;
     if ((e = cudaEventRecord(ev0, stream))) return cuda_fail(e, "event");
-    if ((rc = set.onlyd ? build_psd(ftab) : build_atable(ftab))) return rc;
+    if ((rc = set.onlyd ? build_psd(ftab) : build_atable(ftab, false, true))) return rc;
     std::vector<double> f1(fi, fi + npts), f2(fj, fj + npts);
     h2d += (double)npts * (3 * sizeof(int) + (w ? 3 : 2) * sizeof(double));
     const size_t n = (size_t)npts;

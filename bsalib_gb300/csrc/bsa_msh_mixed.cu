@@ -649,7 +649,7 @@ int Engine::msh_mixed_batch(const std::vector<ZoneDev> &zs, std::vector<double> 
     cudaError_t e;
     int rc;
     if ((e = cudaEventRecord(ev2, stream))) return cuda_fail(e, "event");
-    if ((rc = build_atable(F.v, true))) return rc;
+    if ((rc = build_atable(F.v, true, true))) return rc;
     const size_t uel = (size_t)nU * Mp * Kp, gel = (size_t)ncol * NMT * Kp, sel = 2 * (size_t)npts * NMT * Kp;
     const size_t tel = (size_t)npts * nm3;
     const size_t nidx = (size_t)nU + ncol + 2 * (size_t)npts + ncells;

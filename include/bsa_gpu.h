@@ -67,9 +67,12 @@ int bsa_setupClassic(int nfreqs, double df);   /* BsaLibImpl.F90:959            
 int bsa_setClassicMode(int imode);             /* BsaLibImpl.F90:916, 0 vectorised 1 scalar   */
 int bsa_setupMesher(int isvd, int bkgrfmt, double bkgaext, double genpaext, double maxaext,
                     int ifcov, int idumpmod);  /* BsaLibImpl.F90:966                          */
-/* POD truncation of the Mesher's POD form (BsaLibImpl.F90:97-115).  The default keeps every
- * POD mode, where the POD form equals the direct form evaluated here; a request that drops
- * modes makes the Mesher functions return BSA_ERR_UNSUPPORTED. */
+/* POD truncation of the Mesher's POD form (BsaLibImpl.F90:97-115, functionsImpl.F90:203-230,
+ * 474-1019).  The default keeps every POD mode, where the POD form equals the direct form.
+ * A request that drops modes makes the Mesher functions evaluate every nodal cross-PSD from
+ * its kept eigenpairs (cuSOLVER dsyevd, loaded on first use); the threshold count follows the
+ * reference's dsyev build (one mode, or none where the second smallest eigenvalue reaches the
+ * limit). */
 int bsa_setPODTruncationThreshold(double rval);  /* percent of the largest eigenvalue */
 int bsa_setPODNOfModesKept(int nmodes);
 int bsa_setWindDirections(const int *dirs, int ndirs);  /* BsaLibImpl.F90:983                 */

@@ -361,16 +361,28 @@ class Oracle:
             out += 2.0 * (t1 + t2 + t3)
         return out.reshape(-1, order="F")
 
-    def pod_point(self, f1, f2):
-        """Mesher POD form with all POD modes kept (numpy eigh as dsyev)."""
+    def pod_point(self, f1, f2, trunc_lim=0.0, nmodes=0):
+        """Mesher POD form (getFM_full_tm_scalar_msh_POD_, functionsImpl.F90:474-1019; numpy
+        eigh, ascending like dsyev).  trunc_lim: bsa_setPODTruncationThreshold's value / 100
+        (the count then follows pod_count, :203-230); nmodes: bsa_setPODNOfModesKept, used
+        when no threshold is set (:795-815).  Both zero: every POD mode."""
         nm = self.nme
+        nnl = self.prob.nnl
+        do_trunc = trunc_lim > 0.0 and trunc_lim != 1.0          # BsaLibImpl.F90:479-481
+        nfix = nmodes if 0 < nmodes < nnl else 0                  # :482-486
+
+        def top(D, V):
+            n = pod_count(D, trunc_lim) if do_trunc else (nfix if nfix else len(D))
+            k = len(D) - n
+            return D[k:], V[:, k:]
+
         out = np.zeros((nm, nm, nm))
         for tc in self.prob.settings.tc:
             l = self.phitc[:, :, tc - 1]
             q = self.phitc[:, :, tc + 2]
-            D1, V1 = np.linalg.eigh(self.cross_psd(f1, tc))
-            D2, V2 = np.linalg.eigh(self.cross_psd(f2, tc))
-            D3, V3 = np.linalg.eigh(self.cross_psd(f1 + f2, tc))
+            D1, V1 = top(*np.linalg.eigh(self.cross_psd(f1, tc)))
+            D2, V2 = top(*np.linalg.eigh(self.cross_psd(f2, tc)))
+            D3, V3 = top(*np.linalg.eigh(self.cross_psd(f1 + f2, tc)))
             for p in range(V1.shape[1]):
                 ep, Dp = V1[:, p], D1[p]
                 tm1 = l @ ep
@@ -407,6 +419,24 @@ class Oracle:
         w1, w2 = PI2 * f1, PI2 * f2
         h1, h2, h3 = self.frf(w1), self.frf(w2), self.frf(w1 + w2)
         return np.real(np.einsum("m,n,o->mno", h1, h2, np.conj(h3))).reshape(-1, order="F")
+
+
+def pod_count(eig, rlim):
+    """getNPODModesByThreshold_ (functionsImpl.F90:203-230) as the reference builds it by
+    default (dsyev, ascending eigenvalues eig(1) <= ... <= eig(n)): the count starts at 2 and
+    walks DOWN while eig(count) >= rlim * eig(n), then subtracts one.  With ascending
+    eigenvalues that inspects the two smallest ones, so the result is 1 when eig(2) is below
+    the limit (the usual case: one POD mode kept) and 0 when eig(2) reaches it but eig(1) does
+    not.  Where eig(1) reaches it too the reference reads eig(0), outside the array; that case
+    is taken as 0 modes here."""
+    eig = np.asarray(eig, dtype=np.float64)
+    if not np.any(eig != eig[-1]):
+        return 1
+    limval = rlim * eig[-1]
+    n = 2
+    while n >= 1 and eig[n - 1] >= limval:
+        n -= 1
+    return max(n - 1, 0)
 
 
 def classic_weights(nf, df, scaling=1):

@@ -113,19 +113,53 @@ def test_mesher_run_vs_oracle_on_its_zones(bsalib):
     assert np.all(out["m3mr_cls"] == 0.0)  # analysis type 2 runs the Mesher only
 
 
-def test_pod_truncation_requests(bsalib):
-    """The default POD form keeps every mode (== the direct form evaluated here); a request
-    that drops POD modes is refused with BSA_ERR_UNSUPPORTED instead of being ignored."""
-    prob = cantilever_tower(nfreqs=5, df=0.5, nodes=6)
+def test_pod_truncation(bsalib):
+    """Truncated POD (bsa_setPODNOfModesKept, bsa_setPODTruncationThreshold) against the
+    oracle's restatement of getFM_full_tm_scalar_msh_POD_ with numpy's eigensolver; full-rank
+    requests keep the direct form."""
+    prob = tall_building(nodes=9, modes=3, nfreqs=4, df=0.5, seed=4)
     prob.settings.svd = 1  # the POD form (the reference's default Mesher function)
+    o = Oracle(prob)
+    fi, fj = np.array([0.3, -1.1, 0.05]), np.array([0.9, 0.4, 0.0])
     s = api.BsaSession(prob)
     try:
         L = s.lib
         assert L.bsa_setPODTruncationThreshold(100.0) == 0    # 100 % keeps every mode
         assert L.bsa_setPODNOfModesKept(prob.nnl) == 0
-        s.msh_bispectra(np.array([0.3]), np.array([0.4]))
-        assert L.bsa_setPODTruncationThreshold(5.0) == 0
-        with pytest.raises(api.BsaError, match="-4"):
-            s.msh_bispectra(np.array([0.3]), np.array([0.4]))
+        bf, _ = s.msh_bispectra(fi, fj)
+        for k in range(fi.size):
+            assert rel(bf[k], o.direct_point(fi[k], fj[k])) < TOL
+        for nkeep in (4, 1):
+            assert L.bsa_setPODNOfModesKept(nkeep) == 0
+            bf, _ = s.msh_bispectra(fi, fj)
+            for k in range(fi.size):
+                assert rel(bf[k], o.pod_point(fi[k], fj[k], nmodes=nkeep)) < 1e-9
+        # the threshold takes precedence over the fixed count
+        assert L.bsa_setPODTruncationThreshold(50.0) == 0
+        bf, _ = s.msh_bispectra(fi, fj)
+        for k in range(fi.size):
+            assert rel(bf[k], o.pod_point(fi[k], fj[k], trunc_lim=0.5)) < 1e-9
     finally:
         s.close()
+
+
+def test_pod_truncation_zones_split_precision(bsalib):
+    """The split-precision zone path reads the same truncated expansions."""
+    prob = tall_building(nodes=12, modes=4, nfreqs=5, df=0.3, seed=31)
+    prob.settings.svd = 1
+    out = {}
+    for prec in (api.PREC_FP64, api.PREC_BF16X3):
+        s = api.BsaSession(prob, precision=prec)
+        try:
+            assert s.lib.bsa_setPODNOfModesKept(3) == 0
+            out[prec] = s.msh_zones(ZONES[:2])
+        finally:
+            s.close()
+    full = api.BsaSession(prob, precision=api.PREC_FP64)
+    try:
+        mf_full, mr_full, _ = full.msh_zones(ZONES[:2])
+    finally:
+        full.close()
+    assert rel(out[api.PREC_BF16X3][1], out[api.PREC_FP64][1]) < 1e-4
+    assert rel(out[api.PREC_BF16X3][0], out[api.PREC_FP64][0]) < 1e-4
+    assert rel(out[api.PREC_FP64][1], mr_full) > 1e-6

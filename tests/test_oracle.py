@@ -47,6 +47,48 @@ def test_pod_full_rank_equals_direct():
         assert rel(o.pod_point(a, b), o.direct_point(a, b)) < 1e-10
 
 
+def test_pod_count_quirk():
+    """getNPODModesByThreshold_ as built with dsyev (ascending eigenvalues): it inspects the
+    two smallest eigenvalues, so it keeps 1 POD mode unless the second smallest reaches the
+    limit."""
+    from oracle.oracle import pod_count
+    assert pod_count([1e-9, 1e-6, 0.5, 2.0], 0.05) == 1          # usual: one mode
+    assert pod_count([1e-9, 0.2, 0.5, 2.0], 0.05) == 0           # eig(2) >= 0.05 * 2
+    assert pod_count([0.3, 0.3, 0.3], 0.05) == 1                 # all equal
+    assert pod_count([0.2, 0.3, 0.5, 2.0], 0.05) == 0            # reference reads eig(0): 0 here
+
+
+def _truncated(o, f, tc, n):
+    D, V = np.linalg.eigh(o.cross_psd(f, tc))
+    return (V[:, -n:] * D[-n:]) @ V[:, -n:].T
+
+
+def test_pod_truncated_is_direct_with_truncated_spectra():
+    """The truncated POD sum equals the direct triple sum with each S(f) replaced by its
+    expansion over the kept eigenpairs -- the identity the device path is built on (the A
+    table of the Mesher frequencies from the truncated S)."""
+    o = Oracle(tall_building(nodes=9, modes=3, nfreqs=4, df=0.5, seed=4))
+    nm = o.nme
+    for f1, f2, nkeep in [(0.3, 0.9, 4), (-1.1, 0.4, 2)]:
+        pod = o.pod_point(f1, f2, nmodes=nkeep)
+        out = np.zeros((nm, nm, nm))
+        for tc in o.prob.settings.tc:
+            l = o.phitc[:, :, tc - 1]
+            q = o.phitc[:, :, tc + 2]
+            S1, S2, S3 = (_truncated(o, f, tc, nkeep) for f in (f1, f2, f1 + f2))
+            t1 = np.einsum("mi,nj,ok,ij,ik->mno", q, l, l, S1, S2)
+            t2 = np.einsum("mi,nj,ok,ij,jk->mno", l, q, l, S3, S2)
+            t3 = np.einsum("mi,nj,ok,jk,ik->mno", l, l, q, S1, S3)
+            out += 2.0 * (t1 + t2 + t3)
+        assert rel(pod, out.reshape(-1, order="F")) < 1e-10
+        assert rel(pod, o.direct_point(f1, f2)) > 1e-6   # the truncation changes the result
+    # threshold form: one POD mode per spectrum where the second smallest eigenvalue is below
+    # the limit (the quirk above), none where it reaches it
+    pod1 = o.pod_point(0.3, 0.9, trunc_lim=0.5)
+    assert rel(pod1, o.pod_point(0.3, 0.9, nmodes=1)) < 1e-12
+    assert not np.any(o.pod_point(0.3, 0.9, trunc_lim=1e-12))
+
+
 def test_scalar_classic_is_uniform_weight_sum():
     """Scalar Classic (BsaClassicImpl.F90:255-363): every pair weighted dw^2."""
     p = cantilever_tower(nfreqs=4, df=0.5, nodes=5)
