@@ -98,7 +98,8 @@ def load(path: Optional[str] = None):
         "bsa_mlp_train": [i, vp, vp, vp, i, i, i, C.c_float, C.c_ulonglong, vp],
         "bsa_computeBRdecomp": [vp, vp, vp], "bsa_computePeakFactors": [i, vp, vp, d, vp, vp, vp, vp],
         "bsa_gpu_batchAdd": [vp], "bsa_gpu_batchCase": [i, vp, vp], "bsa_gpu_batchRun": [vp] * 5,
-        "bsa_gpu_batchClear": [],
+        "bsa_gpu_batchClear": [], "bsa_doValidateZoneDeltas": [i], "bsa_setBfmMLR": [i],
+        "bsa_setMaxBkgPeakRestriction": [i], "bsa_setPremeshScheme": [i], "bsa_setPremeshMode": [i],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)
@@ -199,6 +200,19 @@ class BsaSession:
     def set_symmetry(self, on: bool = True):
         """bsa_gpu_setClassicSymmetry: evaluate half of the (symmetric) Classic grid."""
         check(self.lib.bsa_gpu_setClassicSymmetry(1 if on else 0), "bsa_gpu_setClassicSymmetry")
+
+    def set_mesher_controls(self, validate: bool = True, mlr: bool = True, restrict: bool = False):
+        """Mesher controls: zone-delta validation, BFM multi-level refinement, background peak
+        restricted to the first direction (bsa_doValidateZoneDeltas, bsa_setBfmMLR,
+        bsa_setMaxBkgPeakRestriction; the arguments' defaults are the library's)."""
+        check(self.lib.bsa_doValidateZoneDeltas(1 if validate else 0), "bsa_doValidateZoneDeltas")
+        check(self.lib.bsa_setBfmMLR(1 if mlr else 0), "bsa_setBfmMLR")
+        check(self.lib.bsa_setMaxBkgPeakRestriction(1 if restrict else 0), "bsa_setMaxBkgPeakRestriction")
+
+    def use_driver_controls(self):
+        """The standalone driver's Mesher controls (app/bsa.F90:544-549): no delta validation,
+        no BFM multi-level refinement, background peak from the first direction."""
+        self.set_mesher_controls(False, False, True)
 
     def set_rows(self, r_begin: int, r_end: int = -1):
         """Evaluate only Classic grid rows [r_begin, r_end) (f1 index)."""

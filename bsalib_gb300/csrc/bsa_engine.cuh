@@ -71,6 +71,9 @@ struct Engine {
     std::vector<std::vector<int>> own_i;     // arrays read by bsa_loadInputFiles (owned here)
     std::vector<std::vector<double>> own_d;
     bool classic_sym = false;   // bsa_gpu_setClassicSymmetry: evaluate half the Classic grid
+    // Mesher controls (BsaLibData.F90:219-233, 273): delta validation, BFM multi-level
+    // refinement, background peak restricted to the first direction, diagonal-crest scheme
+    bool validate_deltas = true, bfm_mlr = true, bkg_restrict = false, premesh_diag_crest = false;
     bsa_brm_export_fn export_fn = nullptr;  // bsa_setBispExportCallback
     void *export_user = nullptr;
     double pod_trunc_lim = 0.0;

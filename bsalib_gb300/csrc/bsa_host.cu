@@ -73,6 +73,10 @@ void Engine::reset_inputs() {
     export_fn = nullptr;
     export_user = nullptr;
     classic_sym = false;
+    validate_deltas = true;
+    bfm_mlr = true;
+    bkg_restrict = false;
+    premesh_diag_crest = false;
 }
 
 void Engine::free_device() {
@@ -727,6 +731,33 @@ int bsa_setPODTruncationThreshold(double rval) {
 int bsa_setPODNOfModesKept(int nmodes) {
     GUARD();
     eng().pod_nmodes = nmodes;
+    return BSA_OK;
+}
+int bsa_doValidateZoneDeltas(int on) {
+    GUARD();
+    eng().validate_deltas = on != 0;
+    return BSA_OK;
+}
+int bsa_setBfmMLR(int on) {
+    GUARD();
+    eng().bfm_mlr = on != 0;
+    return BSA_OK;
+}
+int bsa_setMaxBkgPeakRestriction(int on) {
+    GUARD();
+    eng().bkg_restrict = on != 0;
+    return BSA_OK;
+}
+// bsa_setPremeshScheme (BsaLibImpl.F90:796-810): 1 selects the diagonal-crest scheme; any
+// other value leaves the scheme as it is.
+int bsa_setPremeshScheme(int itype) {
+    GUARD();
+    if (itype == 1) eng().premesh_diag_crest = true;
+    return BSA_OK;
+}
+int bsa_setPremeshMode(int imode) {
+    GUARD();
+    (void)imode;  // read by the diagonal-crest scheme only
     return BSA_OK;
 }
 int bsa_setWindDirections(const int *dirs, int ndirs) {

@@ -1,8 +1,8 @@
 // bsa_io.cu -- the standalone driver's input files, read natively: bsa.bsadata (settings,
 // getBsaData, app/bsa.F90:877-930) and bsa.extdata (structure, wind and modal data,
 // getExtData, app/bsa.F90:696-871, written by generateBSAInputFiles_,
-// src/bsa/BsaLibImpl.F90:2065-2155), then the setter sequence of the driver's setup
-// (app/bsa.F90:525-606).  The arrays are owned by the library until bsa_Finalise.
+// src/bsa/BsaLibImpl.F90:2065-2155), then the driver's library controls and setter sequence
+// (app/bsa.F90:544-606).  The arrays are owned by the library until bsa_Finalise.
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -146,6 +146,11 @@ extern "C" int bsa_loadInputFiles(const char *dir) {
     do {                        \
         if ((rc = (x))) return rc; \
     } while (0)
+    // the driver's library controls (app/bsa.F90:544-552)
+    CALL(bsa_doValidateZoneDeltas(0));
+    CALL(bsa_setBfmMLR(0));
+    CALL(bsa_setMaxBkgPeakRestriction(1));
+    CALL(bsa_setPODNOfModesKept(0));
     if (suban) CALL(bsa_setAnalysisType(suban));
     if (vers) CALL(bsa_setVersion(vers));
     if (defsc) CALL(bsa_setScalingConv(defsc));

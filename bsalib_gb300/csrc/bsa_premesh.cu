@@ -1,0 +1,573 @@
+// bsa_premesh.cu -- the Mesher's zone layout (pre-mesh) and each zone's post-mesh lattice,
+// restated from BsaLib so that the Mesher evaluates the reference's zones.
+//
+// Pre-mesh (PreMesh, src/bsa/meshing/BsaMesherImpl.F90:266-1393, the default scheme without
+// diagonal crests): the background peak zone centred at the origin, the four crest bands along
+// the axes (one zone per zone limit and a closing one), the four quadrants as nested L-shapes
+// (a diagonal square and two side strips per limit) and, with full coverage, four external
+// padding bands up to max(natf) * max_area_ext.  Zone limits, policies and interest modes come
+// from prefetchZoneLimits_ (:1638-1859) over the peak extensions of
+// getActualPeakZoneExtensionLimits_ (:1864-1890).  The geometry follows MRectZone
+// (zones/MRectZoneImpl.F90), M2DPolygZone (zones/M2DPolygZone.F90) and MPoint
+// (point/MPoint.F90), with one zone object reused from zone to zone as the reference does, so
+// that state a call does not set carries over; each parallel direction loop of the reference
+// starts from a fresh object (OpenMP firstprivate), and so does each loop here.
+//
+// Post-mesh (interpolateRZ_HTPC_v3, zones/_shared_poly2d.fi:470-900): the dumped zone (init
+// point, rotation, bases, refinements, policy, interest-mode pointer) gets its deltas back from
+// bases / (n - 1), its BFM lattice refined by the policy's BFM factors (multi-level
+// refinement, bsa_setBfmMLR) and, with bsa_doValidateZoneDeltas, re-refined until its step
+// resolves the narrowest peak of its interest modes; the BRM lattice refines the BFM one by the
+// policy's BRM factors.  The result is the device zone record the integration kernels read.
+//
+// Settings of the reference's standalone driver (app/bsa.F90:544-552) differ from the library
+// defaults used here: bsa_loadInputFiles applies the driver's (no delta validation, no BFM
+// multi-level refinement, background peak restricted to the first direction).
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "../../include/bsa_gpu.h"
+#include "bsa_engine.cuh"
+
+namespace bsa {
+namespace premesh {
+
+// _CONSTANTS.F90:196-209
+const double PI = 4.0 * std::atan(1.0);
+const double PId2 = PI / 2.0, PIt3d2 = PI * (3.0 / 2.0), PIt2 = PI * 2.0;
+constexpr double MACHINE_PRECISION = 1e-12;
+
+// MPolicy ids and MPolicy_fromID (policy/MPolicy.F90:34-43, 130-168)
+enum { kNull = 0, kDef = 1, kConst = 2, kPrePeak1 = 3, kPrePeak2 = 4, kPeak = 5, kCrest = 6, kBasin = 7,
+       kPadIntern = 8, kPadExtern = 9 };
+
+struct Policy {
+    int dfI = 0, dfJ = 0, bfm_i = 1, bfm_j = 1, brm_i = 1, brm_j = 1, nlevs = 0, id = kNull;
+};
+
+Policy policy(int id) {
+    auto P = [](int a, int b, int c, int d, int e, int f, int g, int h) {
+        Policy p;
+        p.dfI = a; p.dfJ = b; p.bfm_i = c; p.bfm_j = d; p.brm_i = e; p.brm_j = f; p.nlevs = g; p.id = h;
+        return p;
+    };
+    switch (id) {
+    case kNull: return P(0, 0, 0, 0, 0, 0, 0, kNull);
+    case kConst: return P(1, 1, 1, 1, 1, 1, 1, kConst);
+    case kPrePeak1: return P(1, 4, 4, 4, 4, 2, 1, kPrePeak1);
+    case kPrePeak2: return P(1, 8, 2, 2, 4, 2, 1, kPrePeak2);
+    case kPeak: return P(1, 1, 4, 4, 4, 4, 1, kPeak);
+    case kCrest: return P(1, 4, 4, 4, 4, 2, 1, kCrest);
+    case kBasin: return P(1, 4, 2, 2, 2, 2, 1, kBasin);
+    case kPadIntern: return P(4, 4, 1, 1, 2, 2, 1, kPadIntern);
+    case kPadExtern: return P(8, 8, 1, 1, 2, 2, 1, kPadExtern);
+    default: return P(2, 2, 2, 2, 2, 2, 1, kDef);
+    }
+}
+
+constexpr int CODE_PRE_PEAK_OK = -1, CODE_PRE_PEAK_KO = -2;  // BsaLibData.F90:248-257
+
+struct Pt {
+    double fi = 0.0, fj = 0.0;
+};
+
+double distance(const Pt &a, const Pt &b) {  // getPointsDistance
+    const double dx = std::fabs(a.fi - b.fi), dy = std::fabs(a.fj - b.fj);
+    return std::sqrt(dx * dx + dy * dy);
+}
+
+// MPoint getNewPointFromDistAndRot (rotations in [0, 2 pi] here)
+Pt from_dist_rot(const Pt &p, double dist, double rot) {
+    double dI, dJ;
+    if (rot < PId2) {
+        dI = std::sin(rot);
+        dJ = std::cos(rot);
+    } else if (rot < PI) {
+        const double ang = rot - PId2;
+        dI = std::cos(ang);
+        dJ = -std::sin(ang);
+    } else if (rot < PIt3d2) {
+        const double ang = rot - PI;
+        dI = -std::sin(ang);
+        dJ = -std::cos(ang);
+    } else {
+        const double ang = rot - PIt3d2;
+        dI = -std::cos(ang);
+        dJ = std::sin(ang);
+    }
+    return Pt{dI * dist + p.fi, dJ * dist + p.fj};
+}
+
+// A dumped zone: what post-mesh reads back (MRectZone dumpRZ and DumpZone).
+struct Dumped {
+    Pt I;
+    double rot, baseI, baseJ;
+    int ni, nj, pol, id_im;
+};
+
+struct Fail {
+    const char *msg;
+};
+
+// MRectZone_t with the state the pre-mesh reads and writes.
+struct RZ {
+    Pt I, E;
+    double rot = 0.0, baseI = 0.0, baseJ = 0.0, dI = 0.0, dJ = 0.0;
+    int ni = 0, nj = 0, pol = kNull, id_im = 0;
+
+    void setRotation(double r) {  // M2DPolygZone setRotation (r < 2 pi here)
+        if (r >= PIt2) r -= std::floor(r / PIt2) * PIt2;
+        rot = r;
+    }
+    bool aligned() const { return rot == 0.0 || rot == PId2 || rot == PI || rot == PIt3d2; }
+    void deduceDeltas() {  // deduceDeltas_rect
+        dI = baseI / (ni - 1);
+        dJ = baseJ / (nj - 1);
+    }
+    void setRefinements(int n_i, int n_j) {  // non-forced: odd counts
+        ni = n_i % 2 == 0 ? n_i + 1 : n_i;
+        nj = n_j % 2 == 0 ? n_j + 1 : n_j;
+        deduceDeltas();
+    }
+    void setDeltas(double dfi, double dfj) {  // setDeltas(.., adapt=.true.) -> deduceRefinements
+        dI = dfi;
+        dJ = dfj;
+        int si = (int)std::floor(baseI / dI), sj = (int)std::floor(baseJ / dJ);
+        if (si % 2 != 0) ++si;
+        if (sj % 2 != 0) ++sj;
+        if (si == 0) si = 1;
+        if (sj == 0) sj = 1;
+        dI = baseI / si;
+        dJ = baseJ / sj;
+        ni = si + 1;
+        nj = sj + 1;
+    }
+    void setIEpts(const Pt &p) {  // loc = 'i'
+        double c, s, di = 0.0, dj = 0.0;
+        if (rot < PId2) {
+            c = std::cos(rot); s = std::sin(rot);
+            di = baseI * c + baseJ * s;
+            dj = baseJ * c - baseI * s;
+        } else if (rot < PI) {
+            const double a = rot - PId2;
+            c = std::cos(a); s = std::sin(a);
+            di = baseJ * c - baseI * s;
+            dj = -(baseJ * s + baseI * c);
+        } else if (rot < PIt3d2) {
+            const double a = rot - PI;
+            c = std::cos(a); s = std::sin(a);
+            di = -(baseJ * s + baseI * c);
+            dj = -baseJ * c + baseI * s;
+        } else if (rot < PIt2) {
+            const double a = rot - PIt3d2;
+            c = std::cos(a); s = std::sin(a);
+            di = -baseJ * c + baseI * s;
+            dj = baseJ * s + baseI * c;
+        }
+        I = p;
+        E = Pt{p.fi + di, p.fj + dj};
+    }
+    // define(pt, loc, base_i, base_j): 'c' centres the zone on pt, 'i' starts it there
+    void define(const Pt &p, char loc, double bi, double bj) {
+        baseI = bi;
+        baseJ = bj;
+        if (loc == 'c') {
+            I = Pt{p.fi - bi / 2, p.fj - bj / 2};
+            E = Pt{p.fi + bi / 2, p.fj + bj / 2};
+        } else {
+            setIEpts(p);
+        }
+    }
+    Pt getA() const { return from_dist_rot(I, baseJ, rot); }
+    Pt getB() const { return from_dist_rot(I, baseI, rot > PIt3d2 ? rot - PIt3d2 : rot + PId2); }
+
+    // getOtherBase: the end point from the side point pt (B for base_dir 'i', A for 'j') and
+    // the known end coordinate; the forms per (side, known coordinate, quadrant) as written.
+    void otherBase(const Pt &pt, char base_dir, char known, double coord) {
+        const double kd = std::fabs(known == 'i' ? coord - pt.fi : coord - pt.fj);
+        double cd = 0.0;
+        if (kd >= MACHINE_PRECISION) {
+            int q;
+            double r;
+            if (rot < PId2) { q = 1; r = rot; }
+            else if (rot < PI) { q = 2; r = rot - PId2; }
+            else if (rot < PIt3d2) { q = 3; r = rot - PI; }
+            else { q = 4; r = rot - PIt3d2; }
+            const double t = std::tan(r);
+            if (base_dir == 'i' && known == 'i') {
+                cd = q == 1 ? kd / t : q == 2 ? -kd * t : q == 3 ? -kd / t : kd * t;
+            } else if (base_dir == 'i') {  // known 'j'
+                cd = q == 1 ? kd * t : q == 2 ? kd / t : q == 3 ? -kd * t : -kd / t;
+            } else if (known == 'i') {     // base_dir 'j'
+                cd = q == 1 ? kd * t : q == 2 ? -kd / t : q == 3 ? -kd * t : kd / t;
+            } else {                       // base_dir 'j', known 'j'
+                cd = q == 1 ? kd / t : q == 2 ? -kd * t : q == 3 ? -kd / t : kd * t;
+            }
+        }
+        const Pt Pe = known == 'i' ? Pt{coord, pt.fj + cd} : Pt{pt.fi + cd, coord};
+        if (base_dir == 'i')
+            baseJ = distance(pt, Pe);
+        else
+            baseI = distance(pt, Pe);
+        E = Pe;
+    }
+    // defineFromEndPtCoordAndBase_forceDeltas
+    void fromEndCoordAndBase(const Pt &Pi, double coord, char coord_ty, double base, char base_dir, double dfi,
+                             double dfj) {
+        I = Pi;
+        double ang;
+        if (base_dir == 'i') {
+            baseI = base;
+            ang = rot >= PIt3d2 ? rot - PIt3d2 : rot + PId2;
+        } else {
+            baseJ = base;
+            ang = rot;
+        }
+        const Pt pt = from_dist_rot(I, base, ang);
+        otherBase(pt, base_dir, coord_ty, coord);
+        setDeltas(dfi, dfj);
+    }
+    // defineFromDeltas_maxvalues(pt, 'i', dfi, dfj, maxF_i, maxF_j, force=.true.)
+    void fromDeltasMax(const Pt &p, double dfi, double dfj, double mi, double mj) {
+        if (!aligned()) throw Fail{"padding zone is not aligned with the frequency axes"};
+        const double fi = p.fi, fj = p.fj;
+        double bi = 0.0, bj = 0.0;
+        const Fail bad{"external padding: max_area_ext does not reach beyond the last zone limit"};
+        if (rot == 0.0) {
+            if (mi <= fi || mj <= fj) throw bad;
+            bi = mi - fi; bj = mj - fj;
+        } else if (rot == PId2) {
+            if (mi <= fi || mj >= fj) throw bad;
+            bj = mi - fi; bi = fj - mj;
+        } else if (rot == PI) {
+            if (mi >= fi || mj >= fj) throw bad;
+            bi = fi - mi; bj = fj - mj;
+        } else {
+            if (mi >= fi || mj <= fj) throw bad;
+            bj = fi - mi; bi = mj - fj;
+        }
+        if (!(rot == 0.0 || rot == PI)) std::swap(dfi, dfj);
+        int si = (int)std::ceil(bi / dfi), sj = (int)std::ceil(bj / dfj);
+        dfi = bi / si;
+        dfj = bj / sj;
+        ni = si + 1;
+        nj = sj + 1;
+        dI = dfi;
+        dJ = dfj;
+        define(p, 'i', bi, bj);
+    }
+    Dumped dump() const { return Dumped{I, rot, baseI, baseJ, ni, nj, pol, id_im}; }
+};
+
+// MRectZone directions in the (f1, f2) plane of an axis-aligned zone: the I and J axes of
+// getUnaryDeltas with the frequency swap interpolateRZ_HTPC_v3 applies for rot in
+// [pi/2, pi) and [3 pi/2, 2 pi).
+void axes(double rot, double &Ii, double &Ij, double &Ji, double &Jj) {
+    if (rot < PId2) {
+        const double c = std::cos(rot), s = std::sin(rot);
+        Ii = c; Ij = -s; Ji = s; Jj = c;
+    } else if (rot < PI) {
+        const double a = rot - PId2, c = std::cos(a), s = std::sin(a);
+        Ii = -s; Ij = -c; Ji = c; Jj = -s;
+    } else if (rot < PIt3d2) {
+        const double a = rot - PI, c = std::cos(a), s = std::sin(a);
+        Ii = -c; Ij = s; Ji = -s; Jj = -c;
+    } else {
+        const double a = rot - PIt3d2, c = std::cos(a), s = std::sin(a);
+        Ii = s; Ij = c; Ji = -c; Jj = s;
+    }
+}
+
+}  // namespace premesh
+
+int Engine::mesher_zones(std::vector<ZoneDev> &zones, std::vector<int> &policy_out) {
+    using namespace premesh;
+    int rc = validate();
+    if (rc) return rc;
+    if (set.bispsym != 0)
+        return fail(BSA_ERR_UNSUPPORTED, "Mesher with spatial symmetry %d is not on this path", set.bispsym);
+    if (premesh_diag_crest)
+        return fail(BSA_ERR_UNSUPPORTED, "the pre-mesh scheme with diagonal crests (triangular zones) is not on this path");
+    if (!in.natf || !in.xsi) return fail(BSA_ERR_STATE, "natural frequencies / damping not set");
+    if (!in.ubref) return fail(BSA_ERR_STATE, "zone mean wind speeds not set");
+    // bkg_peak_width_(i, j) = 1 / max_z L(i, j, z) / U(z) (computeBKGPeakWidths,
+    // StructureImpl.F90:225-260, from validateAll_, BsaLibImpl.F90:513-524); the background
+    // peak width is its maximum, over the first direction only when restricted (PreMesh :302)
+    double bkgw = 0.0;
+    for (int j = 0; j < (bkg_restrict ? 1 : 3); ++j)
+        for (int i = 0; i < 3; ++i) {
+            double mx = -INFINITY;
+            for (int z = 0; z < in.nz; ++z) mx = std::max(mx, in.L[(size_t)i + 3 * (size_t)j + 9 * (size_t)z] / in.ubref[z]);
+            if (mx != 0.0 && std::isfinite(mx)) bkgw = std::max(bkgw, 1.0 / mx);
+        }
+    if (!(bkgw > 0.0)) return fail(BSA_ERR_ARG, "background peak width is zero");
+    if (set.bkgrfmt < 2) return fail(BSA_ERR_ARG, "background zone refinement must be >= 2");
+    const double base_i = bkgw * set.bkgaext;
+    const double dS2_2 = base_i * (std::sqrt(2.0) / 2.0), d2S2_2 = dS2_2 / 2.0;
+    double max_ext = -INFINITY;
+    for (int m = 0; m < in.nm; ++m) max_ext = std::max(max_ext, in.natf[m]);
+    max_ext *= set.maxaext;  // getMaxSpaceExtension_ (:1626-1631)
+
+    // ---- prefetchZoneLimits_ / getActualPeakZoneExtensionLimits_ ----
+    const int NM = (int)modes.size();
+    std::vector<double> peak_ext(in.nm + 1, -1.0);  // peak_exts_(mode), 1-based
+    std::vector<double> pbf(NM + 1), pff(NM + 1);
+    for (int im = 1; im <= NM; ++im) {
+        const int nmode = modes[im - 1];
+        const double f = in.natf[nmode - 1], ext = in.xsi[nmode - 1] * f * set.genpaext;
+        pbf[im] = f - ext;
+        pff[im] = f + ext;
+        peak_ext[nmode] = ext + ext;
+    }
+    const double bpw2 = base_i / 2.0;
+    std::vector<double> lim(1, 0.0);   // 1-based
+    std::vector<int> pol(1, kDef), IM(1, 0);
+    int NLims = 0;
+    {
+        int skip = 1;
+        while (pff[skip] <= bpw2) {
+            ++skip;
+            if (skip > NM) break;
+        }
+        skip -= 1;
+        if (NM - skip > 0) {
+            const int cap = (NM - skip) * 2 + 1;
+            lim.assign(cap + 1, 0.0);
+            pol.assign(cap + 1, kDef);
+            IM.assign(201, 0);
+            int NL, iim, jim;
+            skip += 1;
+            if (bpw2 < pbf[skip]) {
+                lim[1] = pbf[skip]; lim[2] = pff[skip];
+                NL = 2;
+                pol[1] = kPrePeak1; pol[2] = kPeak;
+                IM[1] = skip == 1 ? CODE_PRE_PEAK_OK : CODE_PRE_PEAK_KO;
+                iim = 2; IM[iim] = 1;
+                jim = 3; IM[jim] = modes[skip - 1];
+            } else {
+                lim[1] = pff[skip]; pol[1] = kPeak; NL = 1;
+                IM[1] = 1; IM[2] = modes[skip - 1];
+                iim = 1; jim = 2;
+            }
+            for (int im = skip + 1; im <= NM; ++im) {
+                const int nmode = modes[im - 1];
+                const double BF = pbf[im], FF = pff[im];
+                if (jim + 3 > 200) return fail(BSA_ERR_UNSUPPORTED, "too many interest-mode entries for the zone layout");
+                if (BF < lim[NL]) {
+                    if (NL == 2 && BF <= lim[NL - 1]) {
+                        lim[NL - 1] = BF; pol[NL - 1] = kPrePeak2;
+                        lim[NL] = FF; pol[NL] = kPeak;
+                    } else {
+                        lim[NL] = FF; pol[NL] = kPeak;
+                    }
+                    IM[iim] += 1;
+                    IM[++jim] = nmode;
+                } else {
+                    lim[++NL] = BF; pol[NL] = kPrePeak2;
+                    lim[++NL] = FF; pol[NL] = kPeak;
+                    iim = jim + 1; IM[iim] = CODE_PRE_PEAK_OK;
+                    ++iim; IM[iim] = 1;
+                    jim = iim + 1; IM[jim] = nmode;
+                }
+            }
+            iim = jim + 1; IM[iim] = 1;
+            jim = iim + 1; IM[jim] = modes[NM - 1];
+            NLims = NL;
+            lim.resize(NL + 2);
+            pol.resize(NL + 2);
+            IM.resize(jim + 1);
+        }
+    }
+
+    // ---- pre-mesh ----
+    std::vector<Dumped> dz;
+    RZ bkgz;
+    bkgz.define(Pt{0.0, 0.0}, 'c', base_i, base_i);
+    bkgz.pol = kPeak;
+    bkgz.id_im = 0;
+    bkgz.setRefinements(set.bkgrfmt, set.bkgrfmt);
+    const double df_I_ref = bkgz.dI, df_J_ref = bkgz.dJ;
+    if (!(std::fabs(df_I_ref - df_J_ref) < MACHINE_PRECISION))
+        return fail(BSA_ERR_ARG, "freq deltas of the background peak zone differ");
+    dz.push_back(bkgz.dump());
+    try {
+        if (NLims > 0) {
+            const int NLimsP1 = NLims + 1;
+            const double maxF = lim[NLims] + d2S2_2;
+            const int id_im_last = (int)IM.size() - 1 - 1;  // size(msh_ZoneLimsInterestModes) - 1
+            lim[NLimsP1] = maxF;
+            pol[NLimsP1] = kPrePeak2;
+            std::vector<double> dlt1(NLimsP1 + 1), dlt2(NLimsP1 + 1);
+            std::vector<int> ref1(NLimsP1 + 1), ref2(NLimsP1 + 1), imz(NLimsP1 + 1, 0);
+            const double ROT[7] = {0.0, PIt3d2, 0.0, PId2, PI, PIt3d2, 0.0};  // ROTATIONS(1:6)
+            const char CDIR[5] = {0, 'j', 'i', 'j', 'i'};                     // COORDS_DIR_CH
+            const int LSIGN[5] = {0, 1, 1, -1, -1};                           // LIM_SIGN_DIRS
+            const int LEFT[5] = {0, 1, -1, -1, 1};                            // LEFT_RZ_SIGNS
+            Pt basePts[5] = {Pt{}, bkgz.getA(), bkgz.E, bkgz.getB(), bkgz.I};
+            // crest bands (directions N, E, S, W)
+            for (int idir = 1; idir <= 4; ++idir) {
+                RZ rz;
+                rz.setRotation(ROT[idir + 1]);
+                Pt ptI = basePts[idir];
+                const char cdir = CDIR[idir];
+                const int sgn = LSIGN[idir];
+                int iim = 1;
+                for (int ilim = 1; ilim <= NLims; ++ilim) {
+                    const double l = lim[ilim];
+                    const Policy P = premesh::policy(pol[ilim]);
+                    const double dfI = df_I_ref * P.dfI, dfJ = df_J_ref * P.dfJ;
+                    rz.pol = pol[ilim];
+                    if (idir == 2) imz[ilim] = iim;
+                    if (ilim == 1 || pol[ilim + 1] == kPeak) {
+                        int nim = IM[iim];
+                        if (nim < 0) nim = IM[++iim];
+                        rz.id_im = iim;
+                        iim = iim + nim + 1;
+                    }
+                    rz.fromEndCoordAndBase(ptI, sgn * l, cdir, base_i, 'i', dfI, dfJ);
+                    if (idir == 1 || idir == 3)
+                        ptI.fj += sgn * l - ptI.fj;
+                    else
+                        ptI.fi += sgn * l - ptI.fi;
+                    if (idir == 2) {
+                        ref1[ilim] = rz.ni; ref2[ilim] = rz.nj;
+                        dlt1[ilim] = rz.dI; dlt2[ilim] = rz.dJ;
+                    }
+                    dz.push_back(rz.dump());
+                }
+                const Policy P = premesh::policy(kPrePeak2);
+                rz.pol = kPrePeak2;
+                rz.id_im = id_im_last;
+                rz.fromEndCoordAndBase(ptI, sgn * maxF, cdir, base_i, 'i', df_I_ref * P.dfI, df_J_ref * P.dfJ);
+                if (idir == 2) {
+                    ref1[NLimsP1] = rz.ni; ref2[NLimsP1] = rz.nj;
+                    dlt1[NLimsP1] = rz.dI; dlt2[NLimsP1] = rz.dJ;
+                }
+                dz.push_back(rz.dump());
+            }
+            imz[NLimsP1] = id_im_last;
+            // quadrants (scheme without diagonal crests, BsaMesherImpl.F90:743-920)
+            {
+                const Pt p1 = basePts[1];
+                basePts[1] = basePts[2]; basePts[2] = basePts[3]; basePts[3] = basePts[4]; basePts[4] = p1;
+                const double init_freq = basePts[1].fi;
+                const int main_refs = std::max(ref1[1], ref2[1]);
+                const char bases_ch[5] = {0, 'i', 'j', 'i', 'j'};
+                for (int idir = 1; idir <= 4; ++idir) {
+                    RZ rz;
+                    const double lrot = ROT[idir], mrot = ROT[idir + 1], rrot = ROT[idir + 2];
+                    rz.setRotation(mrot);
+                    rz.pol = pol[1];
+                    Pt ptI = basePts[idir];
+                    double rbase = lim[1] - init_freq;
+                    if (rbase <= 0.0) throw Fail{"negative base of the first quadrant zone"};
+                    rz.define(ptI, 'i', rbase, rbase);
+                    rz.setRefinements(main_refs, main_refs);
+                    rz.id_im = 1;
+                    dz.push_back(rz.dump());
+                    Pt ptE = rz.E;
+                    const int lsgn = LEFT[idir], rsgn = LSIGN[idir];
+                    const char lknown = bases_ch[idir], rknown = bases_ch[5 - idir];
+                    for (int ilim = 2; ilim <= NLimsP1; ++ilim) {
+                        rz.id_im = imz[ilim];
+                        const double rl = lim[ilim];
+                        rbase = rl - lim[ilim - 1];
+                        ptI = ptE;
+                        rz.pol = pol[ilim];
+                        double dm = std::min(dlt1[ilim], dlt2[ilim]);
+                        rz.setRotation(mrot);
+                        rz.fromEndCoordAndBase(ptI, lsgn * rl, 'j', rbase, lknown, dm, dm);
+                        dz.push_back(rz.dump());
+                        ptE = rz.E;
+                        dm = dlt2[ilim];
+                        rz.setRotation(lrot);
+                        rz.fromEndCoordAndBase(ptI, lsgn * init_freq, lknown, rbase, 'i', dm, dm);
+                        dz.push_back(rz.dump());
+                        rz.setRotation(rrot);
+                        rz.fromEndCoordAndBase(ptI, rsgn * init_freq, rknown, rbase, 'j', dm, dm);
+                        dz.push_back(rz.dump());
+                    }
+                }
+            }
+            // external padding (BsaMesherImpl.F90:1286-1350)
+            if (set.fcov == 1) {
+                const Policy P = premesh::policy(kPadExtern);
+                const double dfI = df_I_ref * P.dfI, dfJ = df_J_ref * P.dfJ;
+                const Pt bp[5] = {Pt{}, Pt{-maxF, maxF}, Pt{maxF, maxF}, Pt{maxF, -maxF}, Pt{-maxF, -maxF}};
+                for (int idir = 1; idir <= 4; ++idir) {
+                    RZ rz;
+                    rz.id_im = id_im_last;
+                    rz.pol = kPadExtern;
+                    rz.setRotation(ROT[idir + 1]);
+                    rz.fromDeltasMax(bp[idir], dfI, dfJ, LSIGN[idir] * max_ext, LEFT[idir] * max_ext);
+                    dz.push_back(rz.dump());
+                }
+            }
+        }
+    } catch (const Fail &f) {
+        return fail(BSA_ERR_ARG, "zone layout: %s", f.msg);
+    }
+
+    // ---- post-mesh lattice of every zone (interpolateRZ_HTPC_v3, _shared_poly2d.fi:588-870) ----
+    zones.clear();
+    policy_out.clear();
+    for (const Dumped &d : dz) {
+        if (d.ni < 2 || d.nj < 2) return fail(BSA_ERR_ARG, "zone with fewer than 2 lattice points per side");
+        const double dI0 = d.baseI / (d.ni - 1), dJ0 = d.baseJ / (d.nj - 1);  // setRefinements(.., force)
+        Policy P = premesh::policy(d.pol);
+        if (!bfm_mlr) {  // disableZonePolicyBfmMLR (MZone.F90)
+            P.nlevs = 0;
+            P.bfm_i = 1;
+            P.bfm_j = 1;
+        }
+        int si = 1, sj = 1;
+        for (int l = 0; l < P.nlevs; ++l) {
+            si *= P.bfm_i;
+            sj *= P.bfm_j;
+        }
+        double dIr = dI0 / si, dJr = dJ0 / sj;
+        if (validate_deltas) {
+            int idx = d.id_im == 0 ? 1 : d.id_im;
+            int nim = IM.size() > (size_t)idx ? IM[idx] : 0;
+            double dwI;
+            if (nim == CODE_PRE_PEAK_OK) {
+                dwI = bkgw;
+            } else {
+                if (nim < 0) nim = IM[++idx];
+                dwI = INFINITY;
+                for (int k = idx + 1; k <= idx + nim; ++k) dwI = std::min(dwI, peak_ext[IM[k]]);
+            }
+            const double dwJ = dwI;
+            if (dIr > dwI / P.bfm_i) {
+                while (dIr > dwI / P.bfm_i) dIr = dI0 / ++si;
+            } else {
+                while (dIr < dwI / P.bfm_i && si > 1) dIr = dI0 / --si;
+            }
+            if (dJr > dwJ / P.bfm_j) {
+                while (dJr > dwJ / P.bfm_j) dJr = dJ0 / ++sj;
+            } else {
+                while (dJr < dwJ / P.bfm_j && sj > 1) dJr = dJ0 / --sj;
+            }
+        }
+        double Ii, Ij, Ji, Jj;
+        axes(d.rot, Ii, Ij, Ji, Jj);
+        ZoneDev z{};
+        z.fi0 = d.I.fi;
+        z.fj0 = d.I.fj;
+        z.dIi = Ii * dIr; z.dIj = Ij * dIr;
+        z.dJi = Ji * dJr; z.dJj = Jj * dJr;
+        z.ni = (d.ni - 1) * si + 1;
+        z.nj = (d.nj - 1) * sj + 1;
+        z.Fi = P.brm_i;
+        z.Fj = P.brm_j;
+        z.wI = dIr * kPi2;
+        z.wJ = dJr * kPi2;
+        z.sym = 1.0;  // i_bisp_sym_ = 1 without spatial symmetry (BsaLibImpl.F90:498)
+        zones.push_back(z);
+        policy_out.push_back(d.pol);
+    }
+    return BSA_OK;
+}
+
+}  // namespace bsa

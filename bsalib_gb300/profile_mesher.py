@@ -31,12 +31,16 @@ def main():
     ap.add_argument("--precision", default="bf16x3", choices=["bf16x3", "fp64"])
     ap.add_argument("--steps", type=int, default=2)
     ap.add_argument("--zones-only", action="store_true")
+    ap.add_argument("--controls", default="driver", choices=["driver", "library"],
+                    help="Mesher controls: the standalone driver's (default) or the library's")
     a = ap.parse_args()
     build.build()
     prob = make(a)
     prec = api.PREC_BF16X3 if a.precision == "bf16x3" else api.PREC_FP64
     s = api.BsaSession(prob, precision=prec)
     try:
+        if a.controls == "driver":
+            s.use_driver_controls()
         zs = s.generate_zones()
         nbfm = sum(z.ni * z.nj for z in zs)
         nbrm = sum(((z.ni - 1) * z.Fi + 1) * ((z.nj - 1) * z.Fj + 1) for z in zs)

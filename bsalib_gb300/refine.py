@@ -83,7 +83,12 @@ class Outcome:
 
 
 class Refiner:
+    """Adaptive refinement of the pre-mesh zones.  It stands in for the reference's fixed
+    refinement policies, so the session is switched to the driver's Mesher controls (no delta
+    validation, no BFM multi-level refinement): the level-0 zones are the pre-mesh lattices."""
+
     def __init__(self, session: api.BsaSession, tol: float = 1e-3, max_levels: int = 2):
+        session.use_driver_controls()
         self.s = session
         self.tol = tol
         self.max_levels = max_levels

@@ -75,6 +75,19 @@ int bsa_setupMesher(int isvd, int bkgrfmt, double bkgaext, double genpaext, doub
  * limit). */
 int bsa_setPODTruncationThreshold(double rval);  /* percent of the largest eigenvalue */
 int bsa_setPODNOfModesKept(int nmodes);
+/* Mesher controls (BsaLibImpl.F90:90-93, 789-810, 840-843; defaults BsaLibData.F90:219-233,
+ * 273): validation of each zone's post-mesh BFM step against the narrowest peak of its interest
+ * modes (default on), BFM multi-level refinement by the zone policies (default on), background
+ * peak width from the first turbulence direction only (default off), pre-mesh scheme
+ * (0 = without diagonal crests, the default; 1 = with diagonal crests and triangular zones,
+ * which the Mesher functions refuse with BSA_ERR_UNSUPPORTED) and pre-mesh mode (used by
+ * scheme 1 only).  bsa_loadInputFiles applies the standalone driver's choices
+ * (app/bsa.F90:544-552): no validation, no multi-level refinement, restricted peak. */
+int bsa_doValidateZoneDeltas(int on);
+int bsa_setBfmMLR(int on);
+int bsa_setMaxBkgPeakRestriction(int on);
+int bsa_setPremeshScheme(int itype);
+int bsa_setPremeshMode(int imode);
 int bsa_setWindDirections(const int *dirs, int ndirs);  /* BsaLibImpl.F90:983                 */
 int bsa_setWindTurbComps(const int *tc, int ntc);       /* BsaLibImpl.F90:991                 */
 

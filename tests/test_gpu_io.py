@@ -1,5 +1,6 @@
 """bsa_loadInputFiles: the driver's bsa.bsadata / bsa.extdata read by the library itself give
-the same analysis as the same problem set through the setters (bitwise)."""
+the same analysis as the same problem set through the setters with the driver's Mesher
+controls (bitwise)."""
 import ctypes as C
 
 import numpy as np
@@ -17,6 +18,7 @@ def test_input_files_round_trip(bsalib, tmp_path):
     write_inputs(prob, str(tmp_path))
     s = api.BsaSession(prob)
     try:
+        s.use_driver_controls()   # bsa_loadInputFiles applies the driver's Mesher controls
         ref = s.run()
     finally:
         s.close()

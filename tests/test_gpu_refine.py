@@ -21,8 +21,9 @@ def test_learned_reaches_the_plain_mesh_with_fewer_points(bsalib, seed):
     prop, thr, tol = Proposer.load(DEFAULT_WEIGHTS)
     s = api.BsaSession(structure(seed), precision=api.PREC_BF16X3)
     try:
+        plain_r = Refiner(s, tol, 2)             # switches the session to the pre-mesh lattices
         level0 = zone_points(s.generate_zones())
-        plain = Refiner(s, tol, 2).run()
+        plain = plain_r.run()
         learned = Refiner(s, tol, 2).run(proposer=prop, threshold=thr)
     finally:
         s.close()
@@ -38,8 +39,9 @@ def test_plain_criterion_keeps_coarse_zones_within_tolerance(bsalib):
     """With a tolerance nothing reaches, no zone is refined: the final mesh is the layout."""
     s = api.BsaSession(structure(7), precision=api.PREC_BF16X3)
     try:
+        ref = Refiner(s, 1e9, 2)
         zs = s.generate_zones()
-        out = Refiner(s, 1e9, 2).run()
+        out = ref.run()
         mf, mr, _ = s.msh_zones(zs)
     finally:
         s.close()
