@@ -98,7 +98,7 @@ struct Engine {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr;
     DevBuf dL, dQ, dLogc, dPsdPar, dFrfM, dFrfK, dFrfC, dFreq, dS, dA, dPartF, dPartR, dOut, dPsdF, dWf, dPts,
         dPtsD, dBF, dBR, dMixA, dMixB, dMixH, dMixPart, dA32, dZones, dZidx, dWd3, dWd2, dMshT, dMshIdx, dLogc32, dL32,
-        dPod;
+        dPod, dFlag;
 
     // stats
     double last_ms = 0, last_ms_contraction = 0, last_ms_gemm = 0, last_points = 0;

@@ -82,7 +82,7 @@ void Engine::reset_inputs() {
 void Engine::free_device() {
     for (DevBuf *b : {&dL, &dQ, &dLogc, &dPsdPar, &dFrfM, &dFrfK, &dFrfC, &dFreq, &dS, &dA, &dPartF, &dPartR,
                       &dOut, &dPsdF, &dWf, &dPts, &dPtsD, &dBF, &dBR, &dMixA, &dMixB, &dMixH, &dMixPart, &dA32,
-                      &dZones, &dZidx, &dWd3, &dWd2, &dMshT, &dMshIdx, &dLogc32, &dL32, &dPod})
+                      &dZones, &dZidx, &dWd3, &dWd2, &dMshT, &dMshIdx, &dLogc32, &dL32, &dPod, &dFlag})
         b->release();
     if (stream) cudaStreamDestroy(stream);
     stream = nullptr;
@@ -290,9 +290,22 @@ int Engine::build_atable(const std::vector<double> &freqs, bool fp32, bool msh) 
     int rc = build_psd(freqs);
     if (rc) return rc;
     if (fp32) {
-        if ((e = dA32.reserve(sizeof(float) * (size_t)nf * K * nme))) return cuda_fail(e, "allocating A");
-        e = launch_atable32(stream, nf, dFreq.as<double>(), ntc, in.nnl, nme, dLogc32.as<float>(), dS.as<double>(),
-                            dL32.as<float>(), dA32.as<float>());
+        // FP32 table on the tensor cores (tf32 hi/lo split, FP32-level accuracy)
+        if ((e = dA32.reserve(sizeof(float) * (size_t)nf * K * nme)) ||
+            (e = dFlag.reserve(256 + atable_tc_scratch(ntc, in.nnl, nme))))
+            return cuda_fail(e, "allocating A");
+        int *flag = dFlag.as<int>();
+        if ((e = cudaMemsetAsync(flag, 0, sizeof(int), stream))) return cuda_fail(e, "memset");
+        e = launch_atable_tc(stream, nf, dFreq.as<double>(), ntc, in.nnl, nme, dLogc32.as<float>(), dS.as<double>(),
+                             dL32.as<float>(), dA32.as<float>(), (char *)dFlag.p + 256, flag);
+        if (e) return cuda_fail(e, "A-table kernel");
+        kernels += 2;
+        int hflag = 0;
+        if ((e = cudaMemcpyAsync(&hflag, flag, sizeof(int), cudaMemcpyDeviceToHost, stream)) ||
+            (e = cudaStreamSynchronize(stream)))
+            return cuda_fail(e, "A-table kernel");
+        if (hflag) return fail(BSA_ERR_TIMEOUT, "A-table kernel: a pipeline wait ran out of its budget (role %d)", hflag);
+        return BSA_OK;
     } else {
         if ((e = dA.reserve(sizeof(double) * (size_t)nf * K * nme))) return cuda_fail(e, "allocating A");
         e = launch_atable(stream, nf, dFreq.as<double>(), ntc, in.nnl, nme, dLogc.as<double>(), dS.as<double>(),

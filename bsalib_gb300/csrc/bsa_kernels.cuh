@@ -18,6 +18,13 @@ cudaError_t launch_atable(cudaStream_t st, int nf, const double *f, int ntc, int
 cudaError_t launch_atable32(cudaStream_t st, int nf, const double *f, int ntc, int nnl, int nm,
                             const float *logc, const double *S, const float *L, float *A);
 
+// The FP32 table on the tensor cores (bsa_atable_tc.cu): tf32 hi/lo split, FP32 accumulation;
+// err receives a nonzero code if a pipeline wait ran out of its budget.  nm <= 64.
+// scratch: atable_tc_scratch(ntc, nnl, nm) bytes (the split B tables).
+size_t atable_tc_scratch(int ntc, int nnl, int nm);
+cudaError_t launch_atable_tc(cudaStream_t st, int nf, const double *f, int ntc, int nnl, int nm,
+                             const float *logc, const double *S, const float *L, float *A, void *scratch, int *err);
+
 // Force PSD on the grid psd[f][n + nm*o] = sum_k L[k][o] A[f][k][n]
 // (functionsImpl.F90:1548-1560), then the second-order moments
 // m2mf, m2mr (x Re[H_o conj H_n]), m2o2mr (x w^2) with per-frequency weights wf.
