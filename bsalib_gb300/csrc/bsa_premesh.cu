@@ -125,9 +125,18 @@ struct RZ {
         dI = baseI / (ni - 1);
         dJ = baseJ / (nj - 1);
     }
-    void setRefinements(int n_i, int n_j) {  // non-forced: odd counts
-        ni = n_i % 2 == 0 ? n_i + 1 : n_i;
-        nj = n_j % 2 == 0 ? n_j + 1 : n_j;
+    // setRefinements(ni, nj, force): its force flag is a saved local in the reference
+    // (M2DPolygZone.F90), so after the first forced call every call behaves as forced; *sticky
+    // carries that state through one layout.
+    void setRefinements(int n_i, int n_j, bool force, bool *sticky) {
+        if (force) *sticky = true;
+        if (*sticky) {
+            ni = n_i;
+            nj = n_j;
+        } else {
+            ni = n_i % 2 == 0 ? n_i + 1 : n_i;
+            nj = n_j % 2 == 0 ? n_j + 1 : n_j;
+        }
         deduceDeltas();
     }
     void setDeltas(double dfi, double dfj) {  // setDeltas(.., adapt=.true.) -> deduceRefinements
@@ -285,8 +294,12 @@ int Engine::mesher_zones(std::vector<ZoneDev> &zones, std::vector<int> &policy_o
     using namespace premesh;
     int rc = validate();
     if (rc) return rc;
-    if (set.bispsym != 0)
-        return fail(BSA_ERR_UNSUPPORTED, "Mesher with spatial symmetry %d is not on this path", set.bispsym);
+    // spatial symmetry (validateAll_, BsaLibImpl.F90:488-498): none counts once, HALF lays out
+    // the half plane f1 >= 0 and counts twice, FOURTH lays out the whole plane and counts four
+    // times (the reference has no layout of its own for it)
+    const bool half = set.bispsym == 2;
+    const double isym = set.bispsym == 0 ? 1.0 : (double)set.bispsym;
+    bool sticky = false;  // setRefinements' saved force flag
     if (premesh_diag_crest)
         return fail(BSA_ERR_UNSUPPORTED, "the pre-mesh scheme with diagonal crests (triangular zones) is not on this path");
     if (!in.natf || !in.xsi) return fail(BSA_ERR_STATE, "natural frequencies / damping not set");
@@ -383,10 +396,27 @@ int Engine::mesher_zones(std::vector<ZoneDev> &zones, std::vector<int> &policy_o
     // ---- pre-mesh ----
     std::vector<Dumped> dz;
     RZ bkgz;
-    bkgz.define(Pt{0.0, 0.0}, 'c', base_i, base_i);
+    const double base_j = base_i;
+    double base_ib = base_i;  // HALF halves the background zone's I side (PreMesh :372-378)
+    if (half) {
+        base_ib = base_i / 2.0;
+        bkgz.define(Pt{0.0, -base_ib}, 'i', base_ib, base_j);
+    } else {
+        bkgz.define(Pt{0.0, 0.0}, 'c', base_i, base_j);
+    }
     bkgz.pol = kPeak;
     bkgz.id_im = 0;
-    bkgz.setRefinements(set.bkgrfmt, set.bkgrfmt);
+    {
+        const int iost = set.bkgrfmt;
+        if (half)
+            bkgz.setRefinements((iost - 1) / 2 + 1, iost, false, &sticky);
+        else
+            bkgz.setRefinements(iost, iost, false, &sticky);
+        if (half) {
+            const int io2 = (bkgz.nj - 1) / 2 + 1;
+            if (bkgz.ni != io2) bkgz.setRefinements(io2, bkgz.nj, true, &sticky);
+        }
+    }
     const double df_I_ref = bkgz.dI, df_J_ref = bkgz.dJ;
     if (!(std::fabs(df_I_ref - df_J_ref) < MACHINE_PRECISION))
         return fail(BSA_ERR_ARG, "freq deltas of the background peak zone differ");
@@ -406,12 +436,15 @@ int Engine::mesher_zones(std::vector<ZoneDev> &zones, std::vector<int> &policy_o
             const int LEFT[5] = {0, 1, -1, -1, 1};                            // LEFT_RZ_SIGNS
             Pt basePts[5] = {Pt{}, bkgz.getA(), bkgz.E, bkgz.getB(), bkgz.I};
             // crest bands (directions N, E, S, W)
-            for (int idir = 1; idir <= 4; ++idir) {
+            const int n_dirs = half ? 3 : 4;
+            const double bases_i[5] = {0.0, base_ib, half ? base_j : base_ib, base_ib, base_ib};
+            for (int idir = 1; idir <= n_dirs; ++idir) {
                 RZ rz;
                 rz.setRotation(ROT[idir + 1]);
                 Pt ptI = basePts[idir];
                 const char cdir = CDIR[idir];
                 const int sgn = LSIGN[idir];
+                const double bi_dir = bases_i[idir];
                 int iim = 1;
                 for (int ilim = 1; ilim <= NLims; ++ilim) {
                     const double l = lim[ilim];
@@ -425,7 +458,7 @@ int Engine::mesher_zones(std::vector<ZoneDev> &zones, std::vector<int> &policy_o
                         rz.id_im = iim;
                         iim = iim + nim + 1;
                     }
-                    rz.fromEndCoordAndBase(ptI, sgn * l, cdir, base_i, 'i', dfI, dfJ);
+                    rz.fromEndCoordAndBase(ptI, sgn * l, cdir, bi_dir, 'i', dfI, dfJ);
                     if (idir == 1 || idir == 3)
                         ptI.fj += sgn * l - ptI.fj;
                     else
@@ -439,7 +472,7 @@ int Engine::mesher_zones(std::vector<ZoneDev> &zones, std::vector<int> &policy_o
                 const Policy P = premesh::policy(kPrePeak2);
                 rz.pol = kPrePeak2;
                 rz.id_im = id_im_last;
-                rz.fromEndCoordAndBase(ptI, sgn * maxF, cdir, base_i, 'i', df_I_ref * P.dfI, df_J_ref * P.dfJ);
+                rz.fromEndCoordAndBase(ptI, sgn * maxF, cdir, bi_dir, 'i', df_I_ref * P.dfI, df_J_ref * P.dfJ);
                 if (idir == 2) {
                     ref1[NLimsP1] = rz.ni; ref2[NLimsP1] = rz.nj;
                     dlt1[NLimsP1] = rz.dI; dlt2[NLimsP1] = rz.dJ;
@@ -454,7 +487,7 @@ int Engine::mesher_zones(std::vector<ZoneDev> &zones, std::vector<int> &policy_o
                 const double init_freq = basePts[1].fi;
                 const int main_refs = std::max(ref1[1], ref2[1]);
                 const char bases_ch[5] = {0, 'i', 'j', 'i', 'j'};
-                for (int idir = 1; idir <= 4; ++idir) {
+                for (int idir = 1; idir <= (half ? 2 : 4); ++idir) {
                     RZ rz;
                     const double lrot = ROT[idir], mrot = ROT[idir + 1], rrot = ROT[idir + 2];
                     rz.setRotation(mrot);
@@ -463,7 +496,7 @@ int Engine::mesher_zones(std::vector<ZoneDev> &zones, std::vector<int> &policy_o
                     double rbase = lim[1] - init_freq;
                     if (rbase <= 0.0) throw Fail{"negative base of the first quadrant zone"};
                     rz.define(ptI, 'i', rbase, rbase);
-                    rz.setRefinements(main_refs, main_refs);
+                    rz.setRefinements(main_refs, main_refs, false, &sticky);
                     rz.id_im = 1;
                     dz.push_back(rz.dump());
                     Pt ptE = rz.E;
@@ -494,13 +527,15 @@ int Engine::mesher_zones(std::vector<ZoneDev> &zones, std::vector<int> &policy_o
             if (set.fcov == 1) {
                 const Policy P = premesh::policy(kPadExtern);
                 const double dfI = df_I_ref * P.dfI, dfJ = df_J_ref * P.dfJ;
-                const Pt bp[5] = {Pt{}, Pt{-maxF, maxF}, Pt{maxF, maxF}, Pt{maxF, -maxF}, Pt{-maxF, -maxF}};
-                for (int idir = 1; idir <= 4; ++idir) {
+                const Pt bp[5] = {Pt{}, Pt{half ? 0.0 : -maxF, maxF}, Pt{maxF, maxF}, Pt{maxF, -maxF},
+                                  Pt{-maxF, -maxF}};
+                const double mext[5] = {0.0, max_ext, max_ext, half ? 0.0 : max_ext, max_ext};
+                for (int idir = 1; idir <= (half ? 3 : 4); ++idir) {
                     RZ rz;
                     rz.id_im = id_im_last;
                     rz.pol = kPadExtern;
                     rz.setRotation(ROT[idir + 1]);
-                    rz.fromDeltasMax(bp[idir], dfI, dfJ, LSIGN[idir] * max_ext, LEFT[idir] * max_ext);
+                    rz.fromDeltasMax(bp[idir], dfI, dfJ, LSIGN[idir] * mext[idir], LEFT[idir] * max_ext);
                     dz.push_back(rz.dump());
                 }
             }
@@ -563,7 +598,7 @@ int Engine::mesher_zones(std::vector<ZoneDev> &zones, std::vector<int> &policy_o
         z.Fj = P.brm_j;
         z.wI = dIr * kPi2;
         z.wJ = dJr * kPi2;
-        z.sym = 1.0;  // i_bisp_sym_ = 1 without spatial symmetry (BsaLibImpl.F90:498)
+        z.sym = isym;  // m3 += intg * i_bisp_sym_ (_shared_poly2d.fi:2117-2119)
         zones.push_back(z);
         policy_out.push_back(d.pol);
     }

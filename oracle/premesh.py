@@ -13,8 +13,9 @@ library's (bsalib_gb300/csrc/bsa_premesh.cu) zone by zone:
   (getNewPointFromDistAndRot), MPolicy_fromID (policy/MPolicy.F90:130-168);
 * post-mesh refinement of every zone: interpolateRZ_HTPC_v3 (zones/_shared_poly2d.fi:588-870).
 
-Each zone comes out as (fi0, fj0, dIi, dIj, dJi, dJj, ni, nj, Fi, Fj, policy), the lattice the
-integration evaluates.
+Each zone comes out as (fi0, fj0, dIi, dIj, dJi, dJj, ni, nj, Fi, Fj, policy, sym), the lattice
+the integration evaluates and its weight (i_bisp_sym_: 1 without spatial symmetry, 2 for HALF,
+whose layout covers f1 >= 0, 4 for FOURTH, whose layout is the whole plane).
 """
 from __future__ import annotations
 
@@ -100,9 +101,16 @@ class Rect:
         else:
             self.set_ie(p)
 
-    def set_refinements(self, ni, nj):
-        self.ni = ni + 1 if ni % 2 == 0 else ni
-        self.nj = nj + 1 if nj % 2 == 0 else nj
+    def set_refinements(self, ni, nj, force, sticky):
+        """M2DPolygZone setRefinements; its force flag is a saved local: after one forced call
+        every call is forced (sticky[0] carries it through a layout)."""
+        if force:
+            sticky[0] = True
+        if sticky[0]:
+            self.ni, self.nj = ni, nj
+        else:
+            self.ni = ni + 1 if ni % 2 == 0 else ni
+            self.nj = nj + 1 if nj % 2 == 0 else nj
         self.dI = self.bI / (self.ni - 1)
         self.dJ = self.bJ / (self.nj - 1)
 
@@ -232,7 +240,7 @@ def zone_limits(modes, natf, xsi, peak_area_ext, bpw2):
 
 
 def layout(modes, natf, xsi, L, ubref, bkgrfmt, bkgaext, peak_area_ext, maxaext, fcov=1,
-           validate=True, mlr=True, restrict=False):
+           validate=True, mlr=True, restrict=False, bispsym=0):
     """Zones of the Mesher analysis, as (fi0, fj0, dIi, dIj, dJi, dJj, ni, nj, Fi, Fj, policy).
     L: turbulence length scales (3, 3, nz) column-major flattened; ubref: zone mean speeds."""
     nz = len(ubref)
@@ -247,10 +255,21 @@ def layout(modes, natf, xsi, L, ubref, bkgrfmt, bkgaext, peak_area_ext, maxaext,
     max_ext = max(natf) * maxaext
     NL, lim, pol, im = zone_limits(modes, natf, xsi, peak_area_ext, base / 2.0)
     peak_ext = {m: 2.0 * xsi[m - 1] * natf[m - 1] * peak_area_ext for m in modes}
+    half = bispsym == 2
+    isym = 1.0 if bispsym == 0 else float(bispsym)
+    sticky = [False]
     bkg = Rect()
-    bkg.define((0.0, 0.0), "c", base, base)
+    base_b = base / 2.0 if half else base
+    if half:
+        bkg.define((0.0, -base_b), "i", base_b, base)
+        bkg.set_refinements((bkgrfmt - 1) // 2 + 1, bkgrfmt, False, sticky)
+        n2 = (bkg.nj - 1) // 2 + 1
+        if bkg.ni != n2:
+            bkg.set_refinements(n2, bkg.nj, True, sticky)
+    else:
+        bkg.define((0.0, 0.0), "c", base, base)
+        bkg.set_refinements(bkgrfmt, bkgrfmt, False, sticky)
     bkg.pol, bkg.im = PEAK, 0
-    bkg.set_refinements(bkgrfmt, bkgrfmt)
     dfI0, dfJ0 = bkg.dI, bkg.dJ
     dumped = [bkg.dump()]
     if NL > 0:
@@ -266,7 +285,8 @@ def layout(modes, natf, xsi, L, ubref, bkgrfmt, bkgaext, peak_area_ext, maxaext,
         refm = {}
         dlt = {}
         izm = {}
-        for d in range(1, 5):                                   # crest bands
+        bases = [None, base_b, base if half else base_b, base_b, base_b]
+        for d in range(1, 4 if half else 5):                   # crest bands
             rz = Rect()
             rz.rot = ROT[d + 1]
             p = base_pts[d]
@@ -283,14 +303,14 @@ def layout(modes, natf, xsi, L, ubref, bkgrfmt, bkgaext, peak_area_ext, maxaext,
                         n = im[iim]
                     rz.im = iim
                     iim += n + 1
-                rz.from_end_coord_base(p, SGN[d] * lim[k], CDIR[d], base, "i", dfI0 * P[0], dfJ0 * P[1])
+                rz.from_end_coord_base(p, SGN[d] * lim[k], CDIR[d], bases[d], "i", dfI0 * P[0], dfJ0 * P[1])
                 p = (p[0], p[1] + (SGN[d] * lim[k] - p[1])) if d in (1, 3) else (p[0] + (SGN[d] * lim[k] - p[0]), p[1])
                 if d == 2:
                     refm[k], dlt[k] = (rz.ni, rz.nj), (rz.dI, rz.dJ)
                 dumped.append(rz.dump())
             P = POLICY[PRE2]
             rz.pol, rz.im = PRE2, last
-            rz.from_end_coord_base(p, SGN[d] * maxF, CDIR[d], base, "i", dfI0 * P[0], dfJ0 * P[1])
+            rz.from_end_coord_base(p, SGN[d] * maxF, CDIR[d], bases[d], "i", dfI0 * P[0], dfJ0 * P[1])
             if d == 2:
                 refm[P1], dlt[P1] = (rz.ni, rz.nj), (rz.dI, rz.dJ)
             dumped.append(rz.dump())
@@ -299,14 +319,14 @@ def layout(modes, natf, xsi, L, ubref, bkgrfmt, bkgaext, peak_area_ext, maxaext,
         init = bp[1][0]
         mrefs = max(refm[1])
         bch = [None, "i", "j", "i", "j"]
-        for d in range(1, 5):
+        for d in range(1, 3 if half else 5):                   # quadrants
             rz = Rect()
             rz.rot = ROT[d + 1]
             rz.pol = pol[1]
             rb = lim[1] - init
             assert rb > 0.0
             rz.define(bp[d], "i", rb, rb)
-            rz.set_refinements(mrefs, mrefs)
+            rz.set_refinements(mrefs, mrefs, False, sticky)
             rz.im = 1
             dumped.append(rz.dump())
             pe = rz.E
@@ -329,11 +349,12 @@ def layout(modes, natf, xsi, L, ubref, bkgrfmt, bkgaext, peak_area_ext, maxaext,
                 dumped.append(rz.dump())
         if fcov == 1:                                           # external padding
             P = POLICY[PADE]
-            bpp = [None, (-maxF, maxF), (maxF, maxF), (maxF, -maxF), (-maxF, -maxF)]
-            for d in range(1, 5):
+            bpp = [None, (0.0 if half else -maxF, maxF), (maxF, maxF), (maxF, -maxF), (-maxF, -maxF)]
+            mext = [None, max_ext, max_ext, 0.0 if half else max_ext, max_ext]
+            for d in range(1, 4 if half else 5):
                 rz = Rect()
                 rz.im, rz.pol, rz.rot = last, PADE, ROT[d + 1]
-                rz.from_deltas_max(bpp[d], dfI0 * P[0], dfJ0 * P[1], SGN[d] * max_ext, LEFT[d] * max_ext)
+                rz.from_deltas_max(bpp[d], dfI0 * P[0], dfJ0 * P[1], SGN[d] * mext[d], LEFT[d] * max_ext)
                 dumped.append(rz.dump())
     out = []
     for z in dumped:                                            # post-mesh lattices
@@ -386,14 +407,14 @@ def layout(modes, natf, xsi, L, ubref, bkgrfmt, bkgaext, peak_area_ext, maxaext,
             c, s = math.cos(a), math.sin(a)
             ax = (s, c, -c, s)
         out.append((z["I"][0], z["I"][1], ax[0] * dIr, ax[1] * dIr, ax[2] * dJr, ax[3] * dJr,
-                    (z["ni"] - 1) * si + 1, (z["nj"] - 1) * sj + 1, ri, rj, z["pol"]))
+                    (z["ni"] - 1) * si + 1, (z["nj"] - 1) * sj + 1, ri, rj, z["pol"], isym))
     return out
 
 
-def layout_for(prob, modes, validate=True, mlr=True, restrict=False):
+def layout_for(prob, modes, validate=True, mlr=True, restrict=False):  # spatial symmetry: prob.settings.bispsym
     """layout() for a bsalib_gb300 Problem and its kept modes (1-based)."""
     import numpy as np
     s = prob.settings
     return layout([int(m) for m in modes], list(prob.natf), list(prob.xsi),
                   list(np.asarray(prob.L, dtype=float).reshape(-1, order="F")), list(prob.UBref), s.bkgrfmt,
-                  s.bkgaext, s.genpaext, s.maxaext, s.fcov, validate, mlr, restrict)
+                  s.bkgaext, s.genpaext, s.maxaext, s.fcov, validate, mlr, restrict, s.bispsym)

@@ -79,12 +79,14 @@ def _controls(s, ctl):
 
 
 @pytest.mark.parametrize("ctl", LAYOUT_CTL, ids=["library", "driver"])
-def test_mesher_layout_vs_oracle(bsalib, ctl):
-    """The library's zone layout (pre-mesh and post-mesh lattices) against the oracle's
-    restatement, zone by zone."""
+@pytest.mark.parametrize("sym", [0, 2, 4], ids=["full", "half", "fourth"])
+def test_mesher_layout_vs_oracle(bsalib, ctl, sym):
+    """The library's zone layout (pre-mesh and post-mesh lattices, spatial-symmetry weight)
+    against the oracle's restatement, zone by zone."""
     from oracle.premesh import layout_for
     for prob in (cantilever_tower(nodes=8), tall_building(nodes=20, modes=6, nfreqs=9, df=0.5, seed=3)):
         prob.settings.suban = 2
+        prob.settings.bispsym = sym
         s = api.BsaSession(prob)
         try:
             _controls(s, ctl)
@@ -96,7 +98,7 @@ def test_mesher_layout_vs_oracle(bsalib, ctl):
         for z, r in zip(zs, ref):
             got = (z.fi0, z.fj0, z.dIi, z.dIj, z.dJi, z.dJj)
             assert np.allclose(got, r[:6], rtol=1e-12, atol=1e-14), (got, r)
-            assert (z.ni, z.nj, z.Fi, z.Fj, z.policy) == tuple(r[6:11])
+            assert (z.ni, z.nj, z.Fi, z.Fj, z.policy, z.sym) == tuple(r[6:12])
 
 
 def test_mesher_layout_covers_the_plane(bsalib):

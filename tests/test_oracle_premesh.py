@@ -27,14 +27,18 @@ def cases():
 
 @pytest.mark.parametrize("name,prob", cases(), ids=[c[0] for c in cases()])
 @pytest.mark.parametrize("ctl", [dict(), dict(validate=False, mlr=False, restrict=True)], ids=["lib", "driver"])
-def test_layout_tiles_the_square(name, prob, ctl):
+@pytest.mark.parametrize("sym", [0, 2], ids=["full", "half"])
+def test_layout_tiles_the_square(name, prob, ctl, sym):
+    prob.settings.bispsym = sym
     o = Oracle(prob)
     zs = layout_for(prob, o.modes, **ctl)
     X = prob.natf.max() * prob.settings.maxaext
     area = sum(abs(u[0] * v[1] - u[1] * v[0]) for _, u, v in map(corners, zs))
-    assert np.isclose(area, (2 * X) ** 2, rtol=1e-10)
+    lo = 0.0 if sym == 2 else -X                 # HALF lays out f1 >= 0
+    assert np.isclose(area, (X - lo) * 2 * X, rtol=1e-10)
+    assert all(z[11] == (2.0 if sym == 2 else 1.0) for z in zs)
     rng = np.random.default_rng(1)
-    pts = rng.uniform(-X, X, size=(4000, 2))
+    pts = np.column_stack([rng.uniform(lo, X, 4000), rng.uniform(-X, X, 4000)])
     cnt = np.zeros(len(pts), dtype=int)
     for z in zs:
         a, u, v = corners(z)
