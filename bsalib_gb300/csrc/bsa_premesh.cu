@@ -395,6 +395,13 @@ int Engine::mesher_zones(std::vector<ZoneDev> &zones, std::vector<int> &policy_o
 
     // ---- pre-mesh ----
     std::vector<Dumped> dz;
+    // compute_rz_ (_shared_poly2d.fi:76-88, 433-449): a zone with a side of zero length is
+    // skipped (not dumped); a zero delta aborts the reference
+    auto emit = [&](const RZ &z) {
+        if (z.baseI <= MACHINE_PRECISION || z.baseJ <= MACHINE_PRECISION) return;
+        if (z.dI <= MACHINE_PRECISION || z.dJ <= MACHINE_PRECISION) throw Fail{"a zone delta is zero"};
+        dz.push_back(z.dump());
+    };
     RZ bkgz;
     const double base_j = base_i;
     double base_ib = base_i;  // HALF halves the background zone's I side (PreMesh :372-378)
@@ -420,8 +427,8 @@ int Engine::mesher_zones(std::vector<ZoneDev> &zones, std::vector<int> &policy_o
     const double df_I_ref = bkgz.dI, df_J_ref = bkgz.dJ;
     if (!(std::fabs(df_I_ref - df_J_ref) < MACHINE_PRECISION))
         return fail(BSA_ERR_ARG, "freq deltas of the background peak zone differ");
-    dz.push_back(bkgz.dump());
     try {
+        emit(bkgz);
         if (NLims > 0) {
             const int NLimsP1 = NLims + 1;
             const double maxF = lim[NLims] + d2S2_2;
@@ -467,7 +474,7 @@ int Engine::mesher_zones(std::vector<ZoneDev> &zones, std::vector<int> &policy_o
                         ref1[ilim] = rz.ni; ref2[ilim] = rz.nj;
                         dlt1[ilim] = rz.dI; dlt2[ilim] = rz.dJ;
                     }
-                    dz.push_back(rz.dump());
+                    emit(rz);
                 }
                 const Policy P = premesh::policy(kPrePeak2);
                 rz.pol = kPrePeak2;
@@ -477,7 +484,7 @@ int Engine::mesher_zones(std::vector<ZoneDev> &zones, std::vector<int> &policy_o
                     ref1[NLimsP1] = rz.ni; ref2[NLimsP1] = rz.nj;
                     dlt1[NLimsP1] = rz.dI; dlt2[NLimsP1] = rz.dJ;
                 }
-                dz.push_back(rz.dump());
+                emit(rz);
             }
             imz[NLimsP1] = id_im_last;
             // quadrants (scheme without diagonal crests, BsaMesherImpl.F90:743-920)
@@ -498,7 +505,7 @@ int Engine::mesher_zones(std::vector<ZoneDev> &zones, std::vector<int> &policy_o
                     rz.define(ptI, 'i', rbase, rbase);
                     rz.setRefinements(main_refs, main_refs, false, &sticky);
                     rz.id_im = 1;
-                    dz.push_back(rz.dump());
+                    emit(rz);
                     Pt ptE = rz.E;
                     const int lsgn = LEFT[idir], rsgn = LSIGN[idir];
                     const char lknown = bases_ch[idir], rknown = bases_ch[5 - idir];
@@ -511,15 +518,15 @@ int Engine::mesher_zones(std::vector<ZoneDev> &zones, std::vector<int> &policy_o
                         double dm = std::min(dlt1[ilim], dlt2[ilim]);
                         rz.setRotation(mrot);
                         rz.fromEndCoordAndBase(ptI, lsgn * rl, 'j', rbase, lknown, dm, dm);
-                        dz.push_back(rz.dump());
+                        emit(rz);
                         ptE = rz.E;
                         dm = dlt2[ilim];
                         rz.setRotation(lrot);
                         rz.fromEndCoordAndBase(ptI, lsgn * init_freq, lknown, rbase, 'i', dm, dm);
-                        dz.push_back(rz.dump());
+                        emit(rz);
                         rz.setRotation(rrot);
                         rz.fromEndCoordAndBase(ptI, rsgn * init_freq, rknown, rbase, 'j', dm, dm);
-                        dz.push_back(rz.dump());
+                        emit(rz);
                     }
                 }
             }
@@ -536,7 +543,7 @@ int Engine::mesher_zones(std::vector<ZoneDev> &zones, std::vector<int> &policy_o
                     rz.pol = kPadExtern;
                     rz.setRotation(ROT[idir + 1]);
                     rz.fromDeltasMax(bp[idir], dfI, dfJ, LSIGN[idir] * mext[idir], LEFT[idir] * max_ext);
-                    dz.push_back(rz.dump());
+                    emit(rz);
                 }
             }
         }

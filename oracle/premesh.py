@@ -271,7 +271,15 @@ def layout(modes, natf, xsi, L, ubref, bkgrfmt, bkgaext, peak_area_ext, maxaext,
         bkg.set_refinements(bkgrfmt, bkgrfmt, False, sticky)
     bkg.pol, bkg.im = PEAK, 0
     dfI0, dfJ0 = bkg.dI, bkg.dJ
-    dumped = [bkg.dump()]
+    dumped = []
+
+    def emit(z):  # compute_rz_: a zone with an empty side is not dumped; a zero delta aborts
+        if z.bI <= MACHINE_PRECISION or z.bJ <= MACHINE_PRECISION:
+            return
+        assert z.dI > MACHINE_PRECISION and z.dJ > MACHINE_PRECISION
+        dumped.append(z.dump())
+
+    emit(bkg)
     if NL > 0:
         P1 = NL + 1
         maxF = lim[NL] + d2
@@ -307,13 +315,13 @@ def layout(modes, natf, xsi, L, ubref, bkgrfmt, bkgaext, peak_area_ext, maxaext,
                 p = (p[0], p[1] + (SGN[d] * lim[k] - p[1])) if d in (1, 3) else (p[0] + (SGN[d] * lim[k] - p[0]), p[1])
                 if d == 2:
                     refm[k], dlt[k] = (rz.ni, rz.nj), (rz.dI, rz.dJ)
-                dumped.append(rz.dump())
+                emit(rz)
             P = POLICY[PRE2]
             rz.pol, rz.im = PRE2, last
             rz.from_end_coord_base(p, SGN[d] * maxF, CDIR[d], bases[d], "i", dfI0 * P[0], dfJ0 * P[1])
             if d == 2:
                 refm[P1], dlt[P1] = (rz.ni, rz.nj), (rz.dI, rz.dJ)
-            dumped.append(rz.dump())
+            emit(rz)
         izm[P1] = last
         bp = [None, base_pts[2], base_pts[3], base_pts[4], base_pts[1]]    # quadrants
         init = bp[1][0]
@@ -328,7 +336,7 @@ def layout(modes, natf, xsi, L, ubref, bkgrfmt, bkgaext, peak_area_ext, maxaext,
             rz.define(bp[d], "i", rb, rb)
             rz.set_refinements(mrefs, mrefs, False, sticky)
             rz.im = 1
-            dumped.append(rz.dump())
+            emit(rz)
             pe = rz.E
             for k in range(2, P1 + 1):
                 rz.im = izm[k]
@@ -338,15 +346,15 @@ def layout(modes, natf, xsi, L, ubref, bkgrfmt, bkgaext, peak_area_ext, maxaext,
                 dm = min(dlt[k])
                 rz.rot = ROT[d + 1]
                 rz.from_end_coord_base(p, LEFT[d] * lim[k], "j", rb, bch[d], dm, dm)
-                dumped.append(rz.dump())
+                emit(rz)
                 pe = rz.E
                 dm = dlt[k][1]
                 rz.rot = ROT[d]
                 rz.from_end_coord_base(p, LEFT[d] * init, bch[d], rb, "i", dm, dm)
-                dumped.append(rz.dump())
+                emit(rz)
                 rz.rot = ROT[d + 2]
                 rz.from_end_coord_base(p, SGN[d] * init, bch[5 - d], rb, "j", dm, dm)
-                dumped.append(rz.dump())
+                emit(rz)
         if fcov == 1:                                           # external padding
             P = POLICY[PADE]
             bpp = [None, (0.0 if half else -maxF, maxF), (maxF, maxF), (maxF, -maxF), (-maxF, -maxF)]
@@ -355,7 +363,7 @@ def layout(modes, natf, xsi, L, ubref, bkgrfmt, bkgaext, peak_area_ext, maxaext,
                 rz = Rect()
                 rz.im, rz.pol, rz.rot = last, PADE, ROT[d + 1]
                 rz.from_deltas_max(bpp[d], dfI0 * P[0], dfJ0 * P[1], SGN[d] * mext[d], LEFT[d] * max_ext)
-                dumped.append(rz.dump())
+                emit(rz)
     out = []
     for z in dumped:                                            # post-mesh lattices
         dI0, dJ0 = z["bI"] / (z["ni"] - 1), z["bJ"] / (z["nj"] - 1)
