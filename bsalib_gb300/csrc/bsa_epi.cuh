@@ -71,9 +71,15 @@ __device__ __forceinline__ void stage(HTile<NMT, JH> *dst, const float2 *Hg, con
 // half jh.  taddr: TMEM address of the lane's D1 accumulator (D3 follows 128 columns later).
 // Weight of point (r, c): wv_r times the classic edge factor when vect (b1: r is an edge row),
 // else wv_r.
-template <int NMT, int JH>
+//
+// SYM (symmetric D1): D1(r, c)[(a, b), j] = D1(c, r)[(a, j), b], so D1 is formed for columns
+// c >= r only (d1 false: not formed for this tile) and each value also stands for term 1 at
+// (c, r) with (m, n, o) = (a, j, b): weight w(c, r) = w(r, c), FRF Re[H_a(w_c) H_j(w_r)
+// conj H_b(w_r + w_c)]; those go to acc[5] (response) and acc[6] (force), c > r only.
+template <int NMT, int JH, bool SYM = false, int KINDS = 5>
 __device__ __forceinline__ void tile(const HTile<NMT, JH> &hb, uint32_t taddr, int a, int b, int c0, int nf,
-                                     bool vect, bool b1, float wv_r, int jh, float (&acc)[5][NMT]) {
+                                     bool vect, bool b1, float wv_r, int jh, float (&acc)[KINDS][NMT], int r = 0,
+                                     bool d1 = true) {
     constexpr int NC = kBN / NMT, W = NMT * JH;
     const int jo = jh * NMT;
     const float2 hra = hb.hr[a];
@@ -81,11 +87,12 @@ __device__ __forceinline__ void tile(const HTile<NMT, JH> &hb, uint32_t taddr, i
     for (int q = 0; q < kBN / 32; ++q) {
 #pragma unroll
         for (int pass = 0; pass < 2; ++pass) {
+            if (SYM && pass == 0 && !d1) continue;  // warp-uniform: no D1 in this tile
             uint32_t v[32];
             tmem_ld32(taddr + pass * 128 + q * 32, v);
             tmem_wait_ld();
             float2 PA = make_float2(0.f, 0.f), PB = PA;
-            float wc = 0.f;
+            float wc = 0.f, wn = 0.f, wt = 0.f;
             bool cval = false;
             int c = 0;
 #pragma unroll
@@ -102,8 +109,15 @@ __device__ __forceinline__ void tile(const HTile<NMT, JH> &hb, uint32_t taddr, i
                         wc = vect ? wv_r * ((b1 && b2) ? -0.5f : ((b1 || b2) ? 0.5f : 1.f)) : wv_r;
                         const float2 hcb = hb.hg[cc * W + b];
                         if (pass == 0) {
+                            // SYM: term 1 at (r, c) for c >= r, its mirror at (c, r) for c > r
+                            wn = SYM ? (cg >= 0 && cg >= r ? wc : 0.f) : wc;
                             const float2 t1 = cmul(hra, hcb);  // term 1 at (r, c)
-                            PA = make_float2(wc * t1.x, wc * t1.y);
+                            PA = make_float2(wn * t1.x, wn * t1.y);
+                            if (SYM) {
+                                wt = cg > r ? wc : 0.f;
+                                const float2 tt = cmul(hb.hg[cc * W + a], conjf2(hb.hs[cc * W + b]));
+                                PB = make_float2(wt * tt.x, wt * tt.y);
+                            }
                         } else {
                             const float2 hsa = hb.hs[cc * W + a];
                             const float2 hsb = hb.hs[cc * W + b];
@@ -121,7 +135,13 @@ __device__ __forceinline__ void tile(const HTile<NMT, JH> &hb, uint32_t taddr, i
                         const float2 hs = hb.hs[c * W + jo + j];
                         const float F1 = PA.x * hs.x + PA.y * hs.y;  // Re[P1 conj(H_j(s))]
                         acc[0][j] = fmaf(F1, x, acc[0][j]);
-                        acc[3][j] = fmaf(wc, x, acc[3][j]);
+                        acc[3][j] = fmaf(wn, x, acc[3][j]);
+                        if constexpr (SYM) {
+                            const float2 hr = hb.hr[jo + j];
+                            const float FT = PB.x * hr.x - PB.y * hr.y;  // Re[P1T H_j(w_r)]
+                            acc[5][j] = fmaf(FT, x, acc[5][j]);
+                            acc[6][j] = fmaf(wt, x, acc[6][j]);
+                        }
                     } else {
                         const float2 hr = hb.hr[jo + j];
                         const float2 hc = hb.hg[c * W + jo + j];

@@ -42,7 +42,7 @@ using namespace tc;
 
 constexpr int kStages = 2;
 constexpr int kStageBytes = 6 * kTileBytes;      // U hi/lo, Bg hi/lo, Bs hi/lo
-constexpr int kKinds = 5;                        // mr1, mr3, mr2, mf1, mf23
+constexpr int kKinds = 5;                        // mr1, mr3, mr2, mf1, mf23 (+ mr1T, mf1T with SYM)
 constexpr int kFlushTiles = 64;                  // FP32 -> FP64 flush period (N tiles)
 constexpr int kBarBytes = 256;                   // mbarriers + TMEM slot
 constexpr int kHBytes = 2 * (int)sizeof(epi::HTile<32, 2>);  // FRF staging, 2 tiles (largest form)
@@ -69,7 +69,7 @@ struct Params {
 
 // Grid rows r of CTA g: r = rb + g / MT, then every (grid / MT)-th row; row tile g % MT.  Per row
 // the mode halves jh < JH, per half the N tiles: the tile sequence of all three roles.
-template <int NMT, int JH>
+template <int NMT, int JH, bool SYM>
 __global__ void __launch_bounds__(192, 1)
     k_bfm_mixed(const __grid_constant__ CUtensorMap tmUh, const __grid_constant__ CUtensorMap tmUl,
                 const __grid_constant__ CUtensorMap tmGh, const __grid_constant__ CUtensorMap tmGl,
@@ -77,6 +77,7 @@ __global__ void __launch_bounds__(192, 1)
     constexpr int NC = kBN / NMT;         // grid columns per N tile
     constexpr int BROWS = NC * NMT;       // B rows loaded by TMA per tile
     constexpr int W = NMT * JH;           // FRF table width
+    constexpr int KINDS = SYM ? kKinds + 2 : kKinds;
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint64_t *bars = (uint64_t *)(smem + kStages * kStageBytes);
@@ -185,9 +186,11 @@ __global__ void __launch_bounds__(192, 1)
                                 const uint64_t gh = sdesc(base + 2 * kTileBytes + off), gl = sdesc(base + 3 * kTileBytes + off);
                                 const uint64_t sh = sdesc(base + 4 * kTileBytes + off), sl = sdesc(base + 5 * kTileBytes + off);
                                 const uint32_t acc = (kc > 0 || ks > 0) ? 1u : 0u;
-                                mma(d1, uh, gh, acc);
-                                mma(d1, uh, gl, 1u);
-                                mma(d1, ul, gh, 1u);
+                                if (!SYM || nt * NC + NC - 1 >= r) {  // SYM: D1 for columns c >= r only
+                                    mma(d1, uh, gh, acc);
+                                    mma(d1, uh, gl, 1u);
+                                    mma(d1, ul, gh, 1u);
+                                }
                                 mma(d3, uh, sh, acc);
                                 mma(d3, uh, sl, 1u);
                                 mma(d3, ul, sh, 1u);
@@ -220,12 +223,12 @@ __global__ void __launch_bounds__(192, 1)
         const bool vect = p.wmode == kWeightClassicVect;
         using HT = epi::HTile<NMT, JH>;
         HT *hbs = (HT *)(smem + kStages * kStageBytes + kBarBytes);
-        double *part = p.part + (size_t)blockIdx.x * kKinds * W * 128 + row;
-        for (int k = 0; k < kKinds * W; ++k) part[(size_t)k * 128] = 0.0;
-        float acc[kKinds][NMT];
+        double *part = p.part + (size_t)blockIdx.x * KINDS * W * 128 + row;
+        for (int k = 0; k < KINDS * W; ++k) part[(size_t)k * 128] = 0.0;
+        float acc[KINDS][NMT];
         auto zero = [&]() {
 #pragma unroll
-            for (int k = 0; k < kKinds; ++k)
+            for (int k = 0; k < KINDS; ++k)
 #pragma unroll
                 for (int j = 0; j < NMT; ++j) acc[k][j] = 0.f;
         };
@@ -234,7 +237,7 @@ __global__ void __launch_bounds__(192, 1)
         // in program order, so the sums stay deterministic.
         auto flush = [&](int jh) {
 #pragma unroll
-            for (int k = 0; k < kKinds; ++k)
+            for (int k = 0; k < KINDS; ++k)
 #pragma unroll
                 for (int j = 0; j < NMT; ++j) {
                     atomicAdd(part + (size_t)(k * W + jh * NMT + j) * 128, (double)acc[k][j]);
@@ -266,8 +269,8 @@ __global__ void __launch_bounds__(192, 1)
                         ok = __all_sync(0xffffffffu, mbar_wait(&tfull[buf], tph, err, 4));
                         if (ok) {
                             fence_after();
-                            epi::tile<NMT, JH>(hbs[buf], lane_base + buf * 256, a, b, nt * NC, p.nf, vect, b1, wv_r,
-                                               jh, acc);
+                            epi::tile<NMT, JH, SYM, KINDS>(hbs[buf], lane_base + buf * 256, a, b, nt * NC, p.nf,
+                                                           vect, b1, wv_r, jh, acc, r, nt * NC + NC - 1 >= r);
                             fence_before();
                             mbar_arrive(&tempty[buf]);
                             // one flush site: a second inlined copy of the flush made the
@@ -369,8 +372,9 @@ __global__ void k_prep_h(int nf, int nm, int NMT, const double *__restrict__ f, 
     }
 }
 
-// m3[m + nm n + nm^2 o] from the per-CTA FP64 partials: three term contributions each.
-__global__ void k_mixed_reduce(int nm, int NMT, int MT, int grid, const double *__restrict__ part,
+// m3[m + nm n + nm^2 o] from the per-CTA FP64 partials: three term contributions each, and
+// with the symmetric D1 (kinds 7) term 1's mirror, kept at (m, o, n).
+__global__ void k_mixed_reduce(int nm, int NMT, int MT, int grid, int kinds, const double *__restrict__ part,
                                double *__restrict__ m3mf, double *__restrict__ m3mr) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int nm3 = nm * nm * nm;
@@ -379,11 +383,15 @@ __global__ void k_mixed_reduce(int nm, int NMT, int MT, int grid, const double *
     auto sum = [&](int kind, int a, int b, int j) {
         const int R = a * nm + b, mtile = R / 128, lane = R % 128;
         double s = 0.0;
-        for (int g = mtile; g < grid; g += MT) s += part[(((size_t)g * kKinds + kind) * NMT + j) * 128 + lane];
+        for (int g = mtile; g < grid; g += MT) s += part[(((size_t)g * kinds + kind) * NMT + j) * 128 + lane];
         return s;
     };
-    const double mr = sum(0, m, n, o) + sum(1, o, n, m) + sum(2, n, o, m);
-    const double mf = sum(3, m, n, o) + sum(4, o, n, m) + sum(4, n, o, m);
+    double mr = sum(0, m, n, o) + sum(1, o, n, m) + sum(2, n, o, m);
+    double mf = sum(3, m, n, o) + sum(4, o, n, m) + sum(4, n, o, m);
+    if (kinds > kKinds) {
+        mr += sum(5, m, o, n);
+        mf += sum(6, m, o, n);
+    }
     m3mr[x] = 2.0 * mr;  // B_F = 2 * (term1 + term2 + term3)
     m3mf[x] = 2.0 * mf;
 }
@@ -406,13 +414,13 @@ cudaError_t prep_h(cudaStream_t st, int nf, int nm, int NMT, const double *f, Fr
     return cudaGetLastError();
 }
 
-template <int NMT, int JH>
+template <int NMT, int JH, bool SYM>
 static cudaError_t launch_gemm(cudaStream_t st, const CUtensorMap *maps, const Params &p, int grid) {
     const size_t smem = (size_t)kStages * kStageBytes + 1024 + kBarBytes + kHBytes;
     cudaError_t e =
-        cudaFuncSetAttribute(k_bfm_mixed<NMT, JH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(k_bfm_mixed<NMT, JH, SYM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    k_bfm_mixed<NMT, JH><<<grid, 192, smem, st>>>(maps[0], maps[1], maps[2], maps[3], maps[4], maps[5], p);
+    k_bfm_mixed<NMT, JH, SYM><<<grid, 192, smem, st>>>(maps[0], maps[1], maps[2], maps[3], maps[4], maps[5], p);
     return cudaGetLastError();
 }
 
@@ -441,7 +449,11 @@ int Engine::contract_mixed(const PointSrc &ps, long long npts, double *m3mf, dou
     const size_t uel = (size_t)nf * Mp * Kp, gel = (size_t)JH * nf * NMT * Kp, sel = (size_t)JH * ns * NMT * Kp;
     const size_t bytesA = 2 * uel * 2, bytesB = 2 * (gel + sel) * 2;
     const size_t bytesH = sizeof(float2) * (size_t)(nf + ns) * W;
-    const size_t bytesP = sizeof(double) * (size_t)grid * kKinds * W * 128;
+    // symmetric D1 (term 1 from the columns c >= r only): one launch over the whole grid, up to
+    // 24 kept modes (two more partial kinds per lane fit the registers there)
+    const bool symd1 = JH == 1 && NMT <= 24 && ps.r0 == 0 && ps.nr == nf && ps.sym_rows == 0;
+    const int kinds = symd1 ? kKinds + 2 : kKinds;
+    const size_t bytesP = sizeof(double) * (size_t)grid * kinds * W * 128;
     if ((e = dMixA.reserve(bytesA)) || (e = dMixB.reserve(bytesB)) || (e = dMixH.reserve(bytesH + 256)) ||
         (e = dMixPart.reserve(bytesP + 256)))
         return cuda_fail(e, "allocating BF16x3 operands");
@@ -496,18 +508,18 @@ int Engine::contract_mixed(const PointSrc &ps, long long npts, double *m3mf, dou
     prm.err = derr;
     if ((e = cudaEventRecord(evg0, stream))) return cuda_fail(e, "event");
     switch (NMT * JH) {
-    case 8: e = launch_gemm<8, 1>(stream, maps, prm, grid); break;
-    case 16: e = launch_gemm<16, 1>(stream, maps, prm, grid); break;
-    case 24: e = launch_gemm<24, 1>(stream, maps, prm, grid); break;
-    case 32: e = launch_gemm<32, 1>(stream, maps, prm, grid); break;
-    default: e = launch_gemm<32, 2>(stream, maps, prm, grid); break;
+    case 8: e = symd1 ? launch_gemm<8, 1, true>(stream, maps, prm, grid) : launch_gemm<8, 1, false>(stream, maps, prm, grid); break;
+    case 16: e = symd1 ? launch_gemm<16, 1, true>(stream, maps, prm, grid) : launch_gemm<16, 1, false>(stream, maps, prm, grid); break;
+    case 24: e = symd1 ? launch_gemm<24, 1, true>(stream, maps, prm, grid) : launch_gemm<24, 1, false>(stream, maps, prm, grid); break;
+    case 32: e = launch_gemm<32, 1, false>(stream, maps, prm, grid); break;
+    default: e = launch_gemm<32, 2, false>(stream, maps, prm, grid); break;
     }
     if (e) return cuda_fail(e, "BF16x3 tcgen05 contraction kernel");
     if ((e = cudaEventRecord(evg1, stream))) return cuda_fail(e, "event");
     const long long nm3 = (long long)nm * nm * nm;
     if ((e = dOut.reserve(sizeof(double) * (3 * (size_t)nm * nm + 2 * (size_t)nm3)))) return cuda_fail(e, "out");
     double *o = dOut.as<double>() + 3 * (size_t)nm * nm;
-    k_mixed_reduce<<<(unsigned)((nm3 + 127) / 128), 128, 0, stream>>>(nm, W, MT, grid, prm.part, o, o + nm3);
+    k_mixed_reduce<<<(unsigned)((nm3 + 127) / 128), 128, 0, stream>>>(nm, W, MT, grid, kinds, prm.part, o, o + nm3);
     if ((e = cudaGetLastError())) return cuda_fail(e, "BF16x3 reduction");
     kernels += 2;
     std::vector<double> h(2 * (size_t)nm3);

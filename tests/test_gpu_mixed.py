@@ -110,3 +110,22 @@ def test_mixed_more_than_32_modes_with_symmetry_and_shards():
         s.close()
     assert rel(sym, ref["m3mr_cls"]) < TOL_M3
     assert rel(parts[0] + parts[1], ref["m3mr_cls"]) < TOL_M3
+
+
+@pytest.mark.parametrize("modes", [6, 12, 24])
+def test_symmetric_d1_matches_the_full_form(modes):
+    """A launch over the whole grid forms D1 for the columns c >= r only and adds term 1's
+    mirror at (c, r); row shards run the full form.  Same moments up to FP32 summation order."""
+    prob = tall_building(nodes=40, modes=modes, nfreqs=17, df=0.25, seed=32)
+    s = api.BsaSession(prob, precision=api.PREC_BF16X3)
+    try:
+        full = s.run()
+        nf = prob.classic_nf()
+        parts = []
+        for r0, r1 in ((0, 11), (11, nf)):
+            s.set_rows(r0, r1)
+            parts.append(s.run())
+    finally:
+        s.close()
+    for k in ("m3mr_cls", "m3mf_cls"):
+        assert rel(full[k], parts[0][k] + parts[1][k]) < 2e-6, k
