@@ -134,14 +134,18 @@ __global__ void __launch_bounds__(192, 1)
                             const uint32_t ph = (it / kStages) & 1u;
                             if (!mbar_wait(&empty[s], ph ^ 1u, err, 1)) { ok = false; break; }
                             uint8_t *st = smem + s * kStageBytes;
-                            mbar_expect_tx(&full[s], tx_bytes);
+                            // SYM: no D1 in this tile, so no grid-column (G) tiles to load
+                            const bool d1 = !SYM || nt * NC + NC - 1 >= r;
+                            mbar_expect_tx(&full[s], d1 ? tx_bytes : tx_bytes - 2u * (uint32_t)(BROWS * 128));
                             const int x = kc * kBK;
                             const int yu = r * p.Mp + mt * kBM;
                             tma_2d(st + 0 * kTileBytes, &tmUh, &full[s], x, yu);
                             tma_2d(st + 1 * kTileBytes, &tmUl, &full[s], x, yu);
                             const int yg = jh * p.g_half + nt * BROWS;
-                            tma_2d(st + 2 * kTileBytes, &tmGh, &full[s], x, yg);
-                            tma_2d(st + 3 * kTileBytes, &tmGl, &full[s], x, yg);
+                            if (d1) {
+                                tma_2d(st + 2 * kTileBytes, &tmGh, &full[s], x, yg);
+                                tma_2d(st + 3 * kTileBytes, &tmGl, &full[s], x, yg);
+                            }
                             const int ys = jh * p.s_half + (r + nt * NC) * NMT;
                             tma_2d(st + 4 * kTileBytes, &tmSh, &full[s], x, ys);
                             tma_2d(st + 5 * kTileBytes, &tmSl, &full[s], x, ys);
