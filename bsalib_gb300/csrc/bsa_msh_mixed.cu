@@ -55,14 +55,17 @@ struct Task {
 
 struct MParams {
     int nm, NMT, NC, BROWS, Mp, MT, nk, ks_last;
-    int ntasks;
+    int nitems;
     const Task *tasks;
+    const int4 *items;  // (task, row tile, first N tile, end N tile)
     float *T1, *T3, *T2;  // [point][j'][a*nm + b]
     int *err;
 };
 
-// Work item w = (task w / MT, row tile w % MT), CTAs stride over work items; all three
-// roles walk the same (item, N tile, K chunk) sequence.
+// Work item w = (task, row tile, N tiles [nt0, nt1)), CTAs stride over work items; all three
+// roles walk the same (item, N tile, K chunk) sequence.  The items of one task are consecutive
+// (row tile major, one N tile each), so the CTAs running at the same time share its U row
+// blocks and its B tiles through L2 instead of each streaming them from HBM.
 __global__ void __launch_bounds__(192, 1)
     k_msh_mixed(const __grid_constant__ CUtensorMap tmUh, const __grid_constant__ CUtensorMap tmUl,
                 const __grid_constant__ CUtensorMap tmGh, const __grid_constant__ CUtensorMap tmGl,
@@ -75,7 +78,7 @@ __global__ void __launch_bounds__(192, 1)
     uint32_t *tmem_slot = (uint32_t *)(bars + 2 * kStages + 5);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     int *err = p.err;
-    const int nwork = p.ntasks * p.MT;
+    const int nwork = p.nitems;
 
     // B-tile rows that TMA never writes (BROWS..127) stay zero for the whole run.
     for (int s = 0; s < kStages; ++s)
@@ -112,12 +115,12 @@ __global__ void __launch_bounds__(192, 1)
             uint32_t it = 0;
             bool ok = true;
             for (int w = blockIdx.x; w < nwork && ok; w += gridDim.x) {
-                const Task tk = p.tasks[w / p.MT];
-                const int mt = w % p.MT;
-                const int ntiles = (tk.ncols + p.NC - 1) / p.NC;
+                const int4 wi = p.items[w];
+                const Task tk = p.tasks[wi.x];
+                const int mt = wi.y;
                 const bool hg = tk.kind == 0;
                 const uint32_t tx = 2u * kTileBytes + (hg ? 4u : 2u) * (uint32_t)(p.BROWS * 128);
-                for (int nt = 0; nt < ntiles && ok; ++nt)
+                for (int nt = wi.z; nt < wi.w && ok; ++nt)
                     for (int kc = 0; kc < p.nk && ok; ++kc, ++it) {
                         const int s = it % kStages;
                         const uint32_t ph = (it / kStages) & 1u;
@@ -155,10 +158,10 @@ __global__ void __launch_bounds__(192, 1)
             uint32_t it = 0, tile = 0;
             bool ok = true;
             for (int w = blockIdx.x; w < nwork && ok; w += gridDim.x) {
-                const Task tk = p.tasks[w / p.MT];
-                const int ntiles = (tk.ncols + p.NC - 1) / p.NC;
+                const int4 wi = p.items[w];
+                const Task tk = p.tasks[wi.x];
                 const bool hg = tk.kind == 0;
-                for (int nt = 0; nt < ntiles && ok; ++nt, ++tile) {
+                for (int nt = wi.z; nt < wi.w && ok; ++nt, ++tile) {
                     const int buf = tile & 1;
                     const uint32_t tph = (tile >> 1) & 1u;
                     if (!mbar_wait(&tempty[buf], tph ^ 1u, err, 2)) { ok = false; break; }
@@ -209,14 +212,14 @@ __global__ void __launch_bounds__(192, 1)
         uint32_t tile = 0;
         bool ok = true;
         for (int w = blockIdx.x; w < nwork && ok; w += gridDim.x) {
-            const Task tk = p.tasks[w / p.MT];
-            const int mt = w % p.MT;
+            const int4 wi = p.items[w];
+            const Task tk = p.tasks[wi.x];
+            const int mt = wi.y;
             const int grow = mt * kBM + row;  // row of U: a * nm + b
             const bool vrow = grow < nm2;
-            const int ntiles = (tk.ncols + p.NC - 1) / p.NC;
             float *const outA = tk.kind == 0 ? p.T1 : nullptr;
             float *const outB = tk.kind == 0 ? p.T3 : p.T2;
-            for (int nt = 0; nt < ntiles; ++nt, ++tile) {
+            for (int nt = wi.z; nt < wi.w; ++nt, ++tile) {
                 const int buf = tile & 1;
                 const uint32_t tph = (tile >> 1) & 1u;
                 // warp-uniform outcome: tcgen05.ld below is .sync.aligned
@@ -653,6 +656,14 @@ int Engine::msh_mixed_batch(const std::vector<ZoneDev> &zs, std::vector<double> 
     const size_t uel = (size_t)nU * Mp * Kp, gel = (size_t)ncol * NMT * Kp, sel = 2 * (size_t)npts * NMT * Kp;
     const size_t tel = (size_t)npts * nm3;
     const size_t nidx = (size_t)nU + ncol + 2 * (size_t)npts + ncells;
+    // work items: per task, its row tiles x N tiles, one N tile each, consecutive
+    std::vector<int4> witems;
+    for (size_t t = 0; t < tasks.size(); ++t) {
+        const int ntl = (tasks[t].ncols + NC - 1) / NC;
+        for (int mt = 0; mt < MT; ++mt)
+            for (int nt = 0; nt < ntl; ++nt) witems.push_back(make_int4((int)t, mt, nt, nt + 1));
+    }
+    if (witems.size() > (size_t)0x7fffffff) return fail(BSA_ERR_ARG, "too many Mesher work items");
     int dev = 0, nsm = 0;
     if ((e = cudaGetDevice(&dev)) || (e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev)))
         return cuda_fail(e, "device query");
@@ -660,7 +671,8 @@ int Engine::msh_mixed_batch(const std::vector<ZoneDev> &zs, std::vector<double> 
     const int G = (int)std::max(1LL, std::min((long long)(4 * nsm + nchunks - 1) / nchunks, ncells));
     if ((e = dMixA.reserve(2 * uel * 2)) || (e = dMixB.reserve(2 * (gel + sel) * 2)) ||
         (e = dMshT.reserve(3 * tel * sizeof(float))) ||
-        (e = dMshIdx.reserve(nidx * sizeof(int) + tasks.size() * sizeof(Task) + zm.size() * sizeof(ZoneM) + 64)) ||
+        (e = dMshIdx.reserve(nidx * sizeof(int) + tasks.size() * sizeof(Task) + zm.size() * sizeof(ZoneM) +
+                             witems.size() * sizeof(int4) + 64)) ||
         (e = dMixPart.reserve((size_t)G * 6 * nm3 * sizeof(double) + 2 * (size_t)nm3 * sizeof(double) + 256)) ||
         (e = dMixH.reserve((size_t)nbrm * 3 * nm * sizeof(float2) + (size_t)nbrm * sizeof(float) + 256 +
                            (zdiag ? zm.size() * nm * sizeof(double) : 0))))
@@ -672,6 +684,7 @@ int Engine::msh_mixed_batch(const std::vector<ZoneDev> &zs, std::vector<double> 
     int *d_usrc = (int *)ib, *d_gsrc = d_usrc + nU, *d_ssrc = d_gsrc + ncol, *d_cellz = d_ssrc + 2 * npts;
     Task *d_tasks = (Task *)(((uintptr_t)(d_cellz + ncells) + 15) & ~(uintptr_t)15);
     ZoneM *d_zones = (ZoneM *)(((uintptr_t)(d_tasks + tasks.size()) + 15) & ~(uintptr_t)15);
+    int4 *d_items = (int4 *)(((uintptr_t)(d_zones + zm.size()) + 15) & ~(uintptr_t)15);
     double *part = dMixPart.as<double>(), *red = part + (size_t)G * 6 * nm3;
     int *derr = (int *)(red + 2 * (size_t)nm3);
     if ((e = cudaMemcpyAsync(d_usrc, usrc.data(), nU * sizeof(int), cudaMemcpyHostToDevice, stream)) ||
@@ -680,9 +693,11 @@ int Engine::msh_mixed_batch(const std::vector<ZoneDev> &zs, std::vector<double> 
         (e = cudaMemcpyAsync(d_cellz, cellz.data(), ncells * sizeof(int), cudaMemcpyHostToDevice, stream)) ||
         (e = cudaMemcpyAsync(d_tasks, tasks.data(), tasks.size() * sizeof(Task), cudaMemcpyHostToDevice, stream)) ||
         (e = cudaMemcpyAsync(d_zones, zm.data(), zm.size() * sizeof(ZoneM), cudaMemcpyHostToDevice, stream)) ||
+        (e = cudaMemcpyAsync(d_items, witems.data(), witems.size() * sizeof(int4), cudaMemcpyHostToDevice, stream)) ||
         (e = cudaMemsetAsync(derr, 0, sizeof(int), stream)))
         return cuda_fail(e, "Mesher task upload");
-    h2d += (double)(nidx * sizeof(int) + tasks.size() * sizeof(Task) + zm.size() * sizeof(ZoneM));
+    h2d += (double)(nidx * sizeof(int) + tasks.size() * sizeof(Task) + zm.size() * sizeof(ZoneM) +
+                    witems.size() * sizeof(int4));
     k_prep_u_rows<<<dim3(nU, Kp / 32), 256, 0, stream>>>(nm, K, Kp, Mp, d_usrc, dA32.as<float>(), dQ.as<double>(), Uh, Ul);
     k_prep_b_rows<<<dim3((unsigned)ncol, Kp / 64), 256, 0, stream>>>(nm, NMT, K, Kp, d_gsrc, dA32.as<float>(), Gh, Gl);
     k_prep_b_rows<<<dim3((unsigned)(2 * npts), Kp / 64), 256, 0, stream>>>(nm, NMT, K, Kp, d_ssrc, dA32.as<float>(), Sh, Sl);
@@ -698,11 +713,12 @@ int Engine::msh_mixed_batch(const std::vector<ZoneDev> &zs, std::vector<double> 
     prm.nm = nm; prm.NMT = NMT; prm.NC = NC; prm.BROWS = BROWS; prm.Mp = Mp; prm.MT = MT;
     prm.nk = Kp / kBK;
     prm.ks_last = (K - (prm.nk - 1) * kBK + 15) / 16;
-    prm.ntasks = (int)tasks.size();
+    prm.nitems = (int)witems.size();
     prm.tasks = d_tasks;
+    prm.items = d_items;
     prm.T1 = T1; prm.T3 = T3; prm.T2 = T2;
     prm.err = derr;
-    const long long nwork = (long long)tasks.size() * MT;
+    const long long nwork = (long long)witems.size();
     const int grid = (int)std::min<long long>(nwork, nsm);
     const size_t smem = (size_t)kStages * kStageBytes + 1024 + 256;
     if ((e = cudaFuncSetAttribute(k_msh_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)))
