@@ -354,8 +354,9 @@ __global__ void k_msh_frf(int nm, int nz, const ZoneM *__restrict__ zones, int n
     }
 }
 
-constexpr int kQB = 24;  // BRM points per shared-memory round
-constexpr int kEPT = 2;  // term-tensor elements per thread
+constexpr int kQB = 16;  // BRM points per shared-memory round
+constexpr int kMomEPT = 3;  // term-tensor elements per thread (same j', b; consecutive a)
+constexpr int kVY = 64;     // staged (j', mode) pairs per point
 
 // s + c += x, compensated (Neumaier): the cell sums are added in FP32 with their rounding
 // errors carried, so the result does not depend on how cells are spread over blocks beyond
@@ -366,128 +367,267 @@ __device__ __forceinline__ void csum(float &s, float &c, float x) {
     s = t;
 }
 
-// Block (g, chunk): elements e = chunk*512 + t + 256 u (u < 2) of the term tensors
-// (e = j'*nm^2 + a*nm + b), cells g, g + G, ...  Each BRM point belongs to the cell
-// (min(qi/Fi, ni-2), min(qj/Fj, nj-2)) and each BFM point to the cell (min(i, ni-2),
+__device__ __forceinline__ void cp_async4(void *dst, const void *src, bool valid) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)),
+                 "l"(src), "r"(valid ? 4 : 0)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async8(void *dst, const void *src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit_wait() {
+    asm volatile("cp.async.commit_group;\ncp.async.wait_all;" ::: "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+
+// Element layout of the moment pass: a block covers JB consecutive modes j' (JB > 1 only when
+// one j' leaves most of the block idle) and, per j', the pairs (arow, b) of AR = ceil(nm / EPT)
+// a-rows x nm columns; a thread holds the EPT elements (j', a = arow EPT + u, b), u < EPT, of the
+// term tensors (e = j' nm^2 + a nm + b).
+struct MomLayout {
+    int JB, AR, nchj;  // modes per block, a-rows, blocks per j' group
+    static MomLayout make(int nm) {
+        MomLayout L;
+        L.AR = (nm + kMomEPT - 1) / kMomEPT;
+        const int per_j = L.AR * nm;
+        L.JB = std::max(1, std::min(256 / per_j, kVY / nm));
+        L.nchj = (L.JB * per_j + 255) / 256;
+        return L;
+    }
+    int groups(int nm) const { return (nm + JB - 1) / JB; }
+    // dynamic shared memory of k_msh_moments
+    static size_t smem() {
+        return (size_t)kQB * kVY * 16 + (size_t)kQB * 64 * 16 + (size_t)kQB * 3 * 64 * 8 + (size_t)kQB * 4 +
+               (size_t)12 * kMomEPT * 256 * 4;
+    }
+};
+
+// One unit of a block's work: the BRM points q0 .. q0 + nb - 1 (in the cell's row-major order)
+// of cell cid, with the cell geometry they need.
+struct MomItem {
+    int cid, q0, nb, nq, nqj, qi0, qj0, i0, j0, rowq;  // rowq: BRM points per zone lattice row
+    size_t qbase, P00;
+    int nj;  // BFM lattice columns of the zone
+    const ZoneM *z;
+};
+
+__device__ __forceinline__ bool mom_item(const ZoneM *__restrict__ zones, const int *__restrict__ cell_zone,
+                                         int ncells, int cid, int q0, MomItem &it) {
+    if (cid >= ncells) return false;
+    const ZoneM *z = zones + cell_zone[cid];
+    const int ni = z->ni, nj = z->nj, Fi = z->Fi, Fj = z->Fj;
+    const int loc = cid - z->cbase, i0 = loc / (nj - 1), j0 = loc - i0 * (nj - 1);
+    const int NJ = (nj - 1) * Fj, NI = (ni - 1) * Fi;
+    const int qi0 = i0 * Fi, qi1 = (i0 == ni - 2) ? NI : (i0 + 1) * Fi - 1;
+    const int qj0 = j0 * Fj, qj1 = (j0 == nj - 2) ? NJ : (j0 + 1) * Fj - 1;
+    it.cid = cid;
+    it.q0 = q0;
+    it.nqj = qj1 - qj0 + 1;
+    it.nq = (qi1 - qi0 + 1) * it.nqj;
+    it.nb = min(kQB, it.nq - q0);
+    it.qi0 = qi0;
+    it.qj0 = qj0;
+    it.i0 = i0;
+    it.j0 = j0;
+    it.rowq = NJ + 1;
+    it.qbase = (size_t)z->qbase;
+    it.P00 = (size_t)z->pbase + (size_t)i0 * nj + j0;
+    it.nj = nj;
+    it.z = z;
+    return true;
+}
+
+// Block (g, y), y = group * nchj + chunk, cells g, g + G, ...  Each BRM point belongs to the
+// cell (min(qi/Fi, ni-2), min(qj/Fj, nj-2)) and each BFM point to the cell (min(i, ni-2),
 // min(j, nj-2)), so every lattice point is counted once.  part[g][6][nm^3]: m3mf of T1, T3,
 // T2, then m3mr of T1, T3, T2.
-__global__ __launch_bounds__(256) void k_msh_moments(int nm, const ZoneM *__restrict__ zones,
-                                                     const int *__restrict__ cell_zone, int ncells,
-                                                     const float *__restrict__ T1, const float *__restrict__ T3,
-                                                     const float *__restrict__ T2, const float2 *__restrict__ Hq,
-                                                     const float *__restrict__ Wq, double *__restrict__ part) {
-    __shared__ float2 H[kQB][3][64];
-    __shared__ float wq[kQB], tiq[kQB], tjq[kQB];
-    const int nm2 = nm * nm, nm3 = nm2 * nm;
-    int ev[kEPT], ia[kEPT], ib[kEPT], ij[kEPT];
-#pragma unroll
-    for (int u = 0; u < kEPT; ++u) {
-        ev[u] = blockIdx.y * (256 * kEPT) + threadIdx.x + 256 * u;
-        const int e = ev[u] < nm3 ? ev[u] : 0, ab = e % nm2;
-        ij[u] = e / nm2;
-        ia[u] = ab / nm;
-        ib[u] = ab % nm;
-    }
-    float mf[kEPT][3], mfe[kEPT][3], mr[kEPT][3], mre[kEPT][3];  // compensated sums over cells
-#pragma unroll
-    for (int u = 0; u < kEPT; ++u)
-#pragma unroll
-        for (int t = 0; t < 3; ++t) mf[u][t] = mfe[u][t] = mr[u][t] = mre[u][t] = 0.f;
+//
+// The FRF products factor through per-point vectors staged in shared memory: with w the
+// point's weight, V_j'(a) = w H1(a) conj H3(j'), Y_j'(b) = w H1(j') H2(b),
+//   T1: Re[H1(a) H2(b) conj H3(j')] w = Re[H2(b) V_j'(a)]
+//   T3: Re[H1(j') H2(b) conj H3(a)] w = Re[Y_j'(b) conj H3(a)]
+//   T2: Re[H1(j') H2(a) conj H3(b)] w = Re[Y_j'(a) conj H3(b)]
+// and the bilinear interpolation of each term over the cell is c0 + ti (c2 - c0) + tj (c1 - c0)
+// + ti tj (c0 - c1 - c2 + c3), its coefficients formed once per cell.  The b-indexed values are
+// read once per point for the thread's EPT elements.
+//
+// Pipeline: the raw FRF rows of the next work item's points and, at a cell's first item, the
+// thread's own corner values of the next cell are copied (cp.async) into shared memory while
+// the current item computes, so each item waits only for the two block barriers around the
+// conversion of its raw rows into the V, Y vectors.
+__global__ __launch_bounds__(256, 2) void k_msh_moments(int nm, MomLayout L, const ZoneM *__restrict__ zones,
+                                                        const int *__restrict__ cell_zone, int ncells,
+                                                        const float *__restrict__ T1, const float *__restrict__ T3,
+                                                        const float *__restrict__ T2, const float2 *__restrict__ Hq,
+                                                        const float *__restrict__ Wq, double *__restrict__ part) {
+    constexpr int EPT = kMomEPT;
+    extern __shared__ __align__(16) unsigned char msm[];
+    float4(*VY)[kVY] = reinterpret_cast<float4(*)[kVY]>(msm);                            // {V_j'(m), Y_j'(m)}
+    float4(*H23)[64] = reinterpret_cast<float4(*)[64]>(msm + kQB * kVY * 16);            // {H2(m), H3(m)}
+    float2 *Hraw = reinterpret_cast<float2 *>(msm + kQB * kVY * 16 + kQB * 64 * 16);     // [kQB][3 nm]
+    float *Wraw = reinterpret_cast<float *>(Hraw + kQB * 3 * 64);                        // [kQB]
+    float *Cs = Wraw + kQB;                                                              // [12 EPT][256]
+    __shared__ float2 tq[kQB];  // (ti, tj)
+    const int nm2 = nm * nm, nm3 = nm2 * nm, tid = threadIdx.x;
+    const int grp = blockIdx.y / L.nchj, chunk = blockIdx.y % L.nchj;
+    const int jg0 = grp * L.JB, njb = min(L.JB, nm - jg0), per_j = L.AR * nm;
+    // this thread's elements: (jl, a = arow EPT + u, b)
+    const int pidx = chunk * 256 + tid;
+    const int jl = pidx / per_j, rem = pidx % per_j, arow = rem / nm, b = rem % nm;
+    const bool tval = jl < njb;
+    const int nval = tval ? min(EPT, nm - arow * EPT) : 0;  // valid elements
+    const int ev0 = tval ? (jg0 + jl) * nm2 + arow * EPT * nm + b : 0;  // element u: ev0 + u nm
+    // elements past a = nm - 1 (u >= nval) read the next staged entries, which lie inside the
+    // dynamic shared memory (VY is followed by H23, H23 by Hraw); their sums are never stored
+    const int ia0 = tval ? jl * nm + arow * EPT : 0, ih0 = tval ? arow * EPT : 0;
+    const int yb = tval ? jl * nm + b : 0, bb = tval ? b : 0;
+    // conversion roles: (jl, m) pairs of VY, modes of H23
+    const int st = tid & (kVY - 1), sq0 = tid / kVY;
+    const int sjl = st / nm, sm = st - sjl * nm;
+    const bool svy = sjl < njb;
+    // raw-copy roles: row entry sc of points sr0, sr0 + srp, ...
+    const int srow = 3 * nm, srp = 256 / srow, sr0 = tid / srow, sc = tid - sr0 * srow;
     const float *Ts[3] = {T1, T3, T2};
-    for (int cid = blockIdx.x; cid < ncells; cid += gridDim.x) {
-        const ZoneM z = zones[cell_zone[cid]];
-        const int loc = cid - z.cbase, i0 = loc / (z.nj - 1), j0 = loc % (z.nj - 1);
-        const int NJ = (z.nj - 1) * z.Fj, NI = (z.ni - 1) * z.Fi;
-        const int qi0 = i0 * z.Fi, qi1 = (i0 == z.ni - 2) ? NI : (i0 + 1) * z.Fi - 1;
-        const int qj0 = j0 * z.Fj, qj1 = (j0 == z.nj - 2) ? NJ : (j0 + 1) * z.Fj - 1;
-        const int nqj = qj1 - qj0 + 1, nq = (qi1 - qi0 + 1) * nqj;
-        const float rFi = 1.f / (float)z.Fi, rFj = 1.f / (float)z.Fj;
-        const size_t P00 = (size_t)z.pbase + (size_t)i0 * z.nj + j0, P01 = P00 + 1, P10 = P00 + z.nj, P11 = P10 + 1;
-        // corner values of the three term tensors, and the BFM lattice trapezoid (m3mf) of
-        // the BFM points this cell owns
-        float c[kEPT][3][4], mfc[kEPT][3], sr[kEPT][3];
-        float wp[4];
-        {
-            const int ci[4] = {i0, i0, i0 + 1, i0 + 1}, cj[4] = {j0, j0 + 1, j0, j0 + 1};
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const bool own = (ci[k] == i0 || i0 == z.ni - 2) && (cj[k] == j0 || j0 == z.nj - 2);
-                const float ti = (ci[k] == 0 || ci[k] == z.ni - 1) ? 0.5f : 1.f;
-                const float tj = (cj[k] == 0 || cj[k] == z.nj - 1) ? 0.5f : 1.f;
-                wp[k] = own ? z.wb * ti * tj : 0.f;
-            }
-        }
-#pragma unroll
-        for (int u = 0; u < kEPT; ++u) {
-            const bool ve = ev[u] < nm3;
-            const size_t e = ve ? (size_t)ev[u] : 0;
-#pragma unroll
-            for (int t = 0; t < 3; ++t) {
-                c[u][t][0] = ve ? Ts[t][P00 * nm3 + e] : 0.f;
-                c[u][t][1] = ve ? Ts[t][P01 * nm3 + e] : 0.f;
-                c[u][t][2] = ve ? Ts[t][P10 * nm3 + e] : 0.f;
-                c[u][t][3] = ve ? Ts[t][P11 * nm3 + e] : 0.f;
-                mfc[u][t] = 0.f;
-                sr[u][t] = 0.f;
-#pragma unroll
-                for (int k = 0; k < 4; ++k) mfc[u][t] = fmaf(wp[k], c[u][t][k], mfc[u][t]);
-            }
-        }
-        for (int q0 = 0; q0 < nq; q0 += kQB) {
-            const int nb = min(kQB, nq - q0);
-            __syncthreads();
-            for (int x = threadIdx.x; x < nb * 3 * nm; x += blockDim.x) {
-                const int ql = x / (3 * nm), r = x % (3 * nm), qq = q0 + ql;
-                const int qi = qi0 + qq / nqj, qj = qj0 + qq % nqj;
-                const size_t gq = (size_t)z.qbase + (size_t)qi * (NJ + 1) + qj;
-                H[ql][r / nm][r % nm] = Hq[gq * 3 * nm + r];
-            }
-            for (int ql = threadIdx.x; ql < nb; ql += blockDim.x) {
-                const int qq = q0 + ql, qi = qi0 + qq / nqj, qj = qj0 + qq % nqj;
-                wq[ql] = Wq[(size_t)z.qbase + (size_t)qi * (NJ + 1) + qj];
-                tiq[ql] = (float)(qi - i0 * z.Fi) * rFi;
-                tjq[ql] = (float)(qj - j0 * z.Fj) * rFj;
-            }
-            __syncthreads();
-            for (int ql = 0; ql < nb; ++ql) {
-                const float ti = tiq[ql], tj = tjq[ql], w = wq[ql];
-#pragma unroll
-                for (int u = 0; u < kEPT; ++u) {
-                    const int a = ia[u], b = ib[u], jj = ij[u];
-                    const float2 h1a = H[ql][0][a], h1j = H[ql][0][jj];
-                    const float2 h2a = H[ql][1][a], h2b = H[ql][1][b];
-                    const float2 h3a = H[ql][2][a], h3b = H[ql][2][b], h3j = H[ql][2][jj];
-                    // Re[x y conj(z)] = (x.re y.re - x.im y.im) z.re + (x.re y.im + x.im y.re) z.im
-                    const float f1 = (h1a.x * h2b.x - h1a.y * h2b.y) * h3j.x + (h1a.x * h2b.y + h1a.y * h2b.x) * h3j.y;
-                    const float f3 = (h1j.x * h2b.x - h1j.y * h2b.y) * h3a.x + (h1j.x * h2b.y + h1j.y * h2b.x) * h3a.y;
-                    const float f2 = (h1j.x * h2a.x - h1j.y * h2a.y) * h3b.x + (h1j.x * h2a.y + h1j.y * h2a.x) * h3b.y;
-                    const float fs[3] = {f1, f3, f2};
-#pragma unroll
-                    for (int t = 0; t < 3; ++t) {
-                        const float left = c[u][t][0] * (1.f - tj) + c[u][t][1] * tj;
-                        const float right = c[u][t][2] * (1.f - tj) + c[u][t][3] * tj;
-                        const float v = left * (1.f - ti) + right * ti;
-                        sr[u][t] = fmaf(w * fs[t], v, sr[u][t]);
-                    }
+
+    // issue the copies of item it: raw FRF rows and weights; corners at a cell's first item
+    auto issue = [&](const MomItem &it) {
+        if (sr0 < srp) {
+            int ql = sr0, qq = it.q0 + sr0, qr = qq / it.nqj, qc = qq - qr * it.nqj;
+            for (; ql < it.nb; ql += srp) {
+                const size_t gq = it.qbase + (size_t)(it.qi0 + qr) * it.rowq + (it.qj0 + qc);
+                cp_async8(Hraw + ql * srow + sc, Hq + gq * srow + sc);
+                if (sc == 0) cp_async4(Wraw + ql, Wq + gq, true);
+                qc += srp;
+                while (qc >= it.nqj) {
+                    qc -= it.nqj;
+                    ++qr;
                 }
             }
         }
+        if (it.q0 == 0) {
+            const size_t Pc[4] = {it.P00, it.P00 + 1, it.P00 + it.nj, it.P00 + it.nj + 1};
 #pragma unroll
-        for (int u = 0; u < kEPT; ++u)
+            for (int t = 0; t < 3; ++t)
 #pragma unroll
-            for (int t = 0; t < 3; ++t) {
-                csum(mf[u][t], mfe[u][t], mfc[u][t]);
-                csum(mr[u][t], mre[u][t], sr[u][t]);
+                for (int k = 0; k < 4; ++k)
+#pragma unroll
+                    for (int u = 0; u < EPT; ++u) {
+                        const bool v = u < nval;
+                        const float *src = v ? Ts[t] + Pc[k] * nm3 + ev0 + u * nm : Ts[t];
+                        cp_async4(Cs + ((t * 4 + k) * EPT + u) * 256 + tid, src, v);
+                    }
+        }
+        cp_async_commit();
+    };
+
+    float mf[EPT][3], mfe[EPT][3], mr[EPT][3], mre[EPT][3];  // compensated sums over cells
+    float cA[EPT][3], cB[EPT][3], cC[EPT][3], cD[EPT][3], sr[EPT][3];
+#pragma unroll
+    for (int u = 0; u < EPT; ++u)
+#pragma unroll
+        for (int t = 0; t < 3; ++t) mf[u][t] = mfe[u][t] = mr[u][t] = mre[u][t] = sr[u][t] = 0.f;
+
+    MomItem cur;
+    bool have = mom_item(zones, cell_zone, ncells, blockIdx.x, 0, cur);
+    if (have) issue(cur);
+    while (have) {
+        asm volatile("cp.async.wait_all;" ::: "memory");
+        __syncthreads();  // raw rows of cur visible; VY, H23 and tq free
+        const ZoneM *z = cur.z;
+        if (cur.q0 == 0) {
+            // BFM lattice trapezoid weights of the corners this cell owns
+            float wp[4];
+            {
+                const int ni = z->ni, nj = z->nj, i0 = cur.i0, j0 = cur.j0;
+                const int ci[4] = {i0, i0, i0 + 1, i0 + 1}, cj[4] = {j0, j0 + 1, j0, j0 + 1};
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const bool own = (ci[k] == i0 || i0 == ni - 2) && (cj[k] == j0 || j0 == nj - 2);
+                    const float ti = (ci[k] == 0 || ci[k] == ni - 1) ? 0.5f : 1.f;
+                    const float tj = (cj[k] == 0 || cj[k] == nj - 1) ? 0.5f : 1.f;
+                    wp[k] = own ? z->wb * ti * tj : 0.f;
+                }
             }
+#pragma unroll
+            for (int u = 0; u < EPT; ++u)
+#pragma unroll
+                for (int t = 0; t < 3; ++t) {
+                    const float *cs = Cs + ((t * 4) * EPT + u) * 256 + tid;
+                    const float c0 = cs[0], c1 = cs[EPT * 256], c2 = cs[2 * EPT * 256], c3 = cs[3 * EPT * 256];
+                    cA[u][t] = c0;
+                    cB[u][t] = c2 - c0;
+                    cC[u][t] = c1 - c0;
+                    cD[u][t] = (c0 - c1) - (c2 - c3);
+                    csum(mf[u][t], mfe[u][t], fmaf(wp[3], c3, fmaf(wp[2], c2, fmaf(wp[1], c1, wp[0] * c0))));
+                    sr[u][t] = 0.f;
+                }
+        }
+        // raw rows -> V, Y, H2, H3 of the item's points; (ti, tj)
+        for (int ql = sq0; ql < cur.nb; ql += 256 / kVY) {
+            const float2 *h = Hraw + ql * 3 * nm;
+            if (svy) {
+                const float w = Wraw[ql];
+                const int jg = jg0 + sjl;
+                const float2 h1 = h[sm], h2 = h[nm + sm];
+                const float2 h1j = h[jg], h3j = h[2 * nm + jg];
+                // V = w H1(m) conj H3(j'),  Y = w H1(j') H2(m)
+                VY[ql][st] = make_float4(w * (h1.x * h3j.x + h1.y * h3j.y), w * (h1.y * h3j.x - h1.x * h3j.y),
+                                         w * (h1j.x * h2.x - h1j.y * h2.y), w * (h1j.x * h2.y + h1j.y * h2.x));
+            }
+            if (st < nm) {
+                const float2 h2 = h[nm + st], h3 = h[2 * nm + st];
+                H23[ql][st] = make_float4(h2.x, h2.y, h3.x, h3.y);
+            }
+        }
+        if (tid < cur.nb) {
+            const int qq = cur.q0 + tid, qr = qq / cur.nqj, qc = qq - qr * cur.nqj;
+            tq[tid] = make_float2((float)(cur.qi0 + qr - cur.i0 * z->Fi) / (float)z->Fi,
+                                  (float)(cur.qj0 + qc - cur.j0 * z->Fj) / (float)z->Fj);
+        }
+        __syncthreads();  // VY, H23, tq ready; raw rows and corners consumed
+        // next item: its copies run under this item's arithmetic
+        MomItem nxt;
+        const bool last = cur.q0 + kQB >= cur.nq;
+        have = last ? mom_item(zones, cell_zone, ncells, cur.cid + gridDim.x, 0, nxt)
+                    : mom_item(zones, cell_zone, ncells, cur.cid, cur.q0 + kQB, nxt);
+        if (have) issue(nxt);
+        for (int ql = 0; ql < cur.nb; ++ql) {
+            const float2 tt = tq[ql];
+            const float ti = tt.x, tj = tt.y, tij = ti * tj;
+            const float4 hb = H23[ql][bb];                                         // H2(b), H3(b)
+            const float2 ybv = reinterpret_cast<const float2 *>(&VY[ql][yb])[1];  // Y_j'(b)
+#pragma unroll
+            for (int u = 0; u < EPT; ++u) {
+                const float4 va = VY[ql][ia0 + u];                                              // V_j'(a), Y_j'(a)
+                const float2 h3a = reinterpret_cast<const float2 *>(&H23[ql][ih0 + u])[1];  // H3(a)
+                const float f1 = hb.x * va.x - hb.y * va.y;
+                const float f3 = ybv.x * h3a.x + ybv.y * h3a.y;
+                const float f2 = va.z * hb.z + va.w * hb.w;
+                const float fs[3] = {f1, f3, f2};
+#pragma unroll
+                for (int t = 0; t < 3; ++t) {
+                    const float v = fmaf(tij, cD[u][t], fmaf(tj, cC[u][t], fmaf(ti, cB[u][t], cA[u][t])));
+                    sr[u][t] = fmaf(fs[t], v, sr[u][t]);
+                }
+            }
+        }
+        if (last) {
+#pragma unroll
+            for (int u = 0; u < EPT; ++u)
+#pragma unroll
+                for (int t = 0; t < 3; ++t) csum(mr[u][t], mre[u][t], sr[u][t]);
+        }
+        cur = nxt;
     }
     double *pg = part + (size_t)blockIdx.x * 6 * nm3;
 #pragma unroll
-    for (int u = 0; u < kEPT; ++u) {
-        if (ev[u] >= nm3) continue;
+    for (int u = 0; u < EPT; ++u) {
+        if (u >= nval) continue;
 #pragma unroll
         for (int t = 0; t < 3; ++t) {
-            pg[(size_t)t * nm3 + ev[u]] = (double)mf[u][t] + (double)mfe[u][t];
-            pg[(size_t)(3 + t) * nm3 + ev[u]] = (double)mr[u][t] + (double)mre[u][t];
+            pg[(size_t)t * nm3 + ev0 + u * nm] = (double)mf[u][t] + (double)mfe[u][t];
+            pg[(size_t)(3 + t) * nm3 + ev0 + u * nm] = (double)mr[u][t] + (double)mre[u][t];
         }
     }
 }
@@ -667,8 +807,10 @@ int Engine::msh_mixed_batch(const std::vector<ZoneDev> &zs, std::vector<double> 
     int dev = 0, nsm = 0;
     if ((e = cudaGetDevice(&dev)) || (e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev)))
         return cuda_fail(e, "device query");
-    const int nchunks = (nm3 + 256 * kEPT - 1) / (256 * kEPT);
-    const int G = (int)std::max(1LL, std::min((long long)(4 * nsm + nchunks - 1) / nchunks, ncells));
+    const MomLayout ML = MomLayout::make(nm);
+    const int nchunks = ML.groups(nm) * ML.nchj;
+    // one wave of two resident blocks per SM where the element chunks allow it
+    const int G = (int)std::max(1LL, std::min((long long)(2 * nsm) / nchunks, ncells));
     if ((e = dMixA.reserve(2 * uel * 2)) || (e = dMixB.reserve(2 * (gel + sel) * 2)) ||
         (e = dMshT.reserve(3 * tel * sizeof(float))) ||
         (e = dMshIdx.reserve(nidx * sizeof(int) + tasks.size() * sizeof(Task) + zm.size() * sizeof(ZoneM) +
@@ -733,7 +875,10 @@ int Engine::msh_mixed_batch(const std::vector<ZoneDev> &zs, std::vector<double> 
         const long long nt = nbrm * 3 * nm;
         k_msh_frf<<<(unsigned)((nt + 255) / 256), 256, 0, stream>>>(nm, (int)zm.size(), d_zones, (int)nbrm, frf(), Hq, Wq);
     }
-    k_msh_moments<<<dim3(G, nchunks), 256, 0, stream>>>(nm, d_zones, d_cellz, (int)ncells, T1, T3, T2, Hq, Wq, part);
+    if ((e = cudaFuncSetAttribute(k_msh_moments, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)MomLayout::smem())))
+        return cuda_fail(e, "kernel attribute");
+    k_msh_moments<<<dim3(G, nchunks), 256, MomLayout::smem(), stream>>>(nm, ML, d_zones, d_cellz, (int)ncells, T1, T3,
+                                                                       T2, Hq, Wq, part);
     k_msh_reduce<<<(nm3 + 127) / 128, 128, 0, stream>>>(nm, G, part, red, red + nm3);
     double *d_zdiag = nullptr;
     if (zdiag) {
