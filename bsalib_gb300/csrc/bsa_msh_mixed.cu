@@ -58,7 +58,8 @@ struct MParams {
     int nitems;
     const Task *tasks;
     const int4 *items;  // (task, row tile, first N tile, end N tile)
-    float *T1, *T3, *T2;  // [point][j'][a*nm + b]
+    float *T1, *T3, *T2;  // [point][j'][a*nm + b], points nm3p (nm^3 rounded up to 4) apart
+    int nm3p;
     int *err;
 };
 
@@ -239,7 +240,7 @@ __global__ void __launch_bounds__(192, 1)
                             const int c = col / p.NMT, j = col - c * p.NMT;
                             if (!vrow || c >= p.NC || j >= nm || c0 + c >= tk.ncols) continue;
                             const size_t pt = (size_t)tk.p0 + (size_t)(c0 + c) * tk.pstride;
-                            out[(pt * nm + j) * nm2 + grow] = __uint_as_float(v[e]);
+                            out[pt * p.nm3p + (size_t)j * nm2 + grow] = __uint_as_float(v[e]);
                         }
                     }
                 }
@@ -332,8 +333,13 @@ __device__ __forceinline__ int zone_of(const ZoneM *__restrict__ zones, int nz, 
     return lo;
 }
 
+// FRF row of a BRM point: H_m(w1), H_m(w2), H_m(w1 + w2) (3 nm values), the point's weight
+// as (w, 0), and a zero pad to an even count, so rows start on 16-byte boundaries.
+__host__ __device__ __forceinline__ int frf_row(int nm) { return (3 * nm + 2) & ~1; }
+
 // Per BRM point q: H_m(w1), H_m(w2), H_m(w1 + w2) evaluated in FP64 and rounded once
-// (Hq[q][3][nm]), and its integration weight sym (wI/Fi)(wJ/Fj) t_i t_j (Wq[q]).
+// (Hq[q][frf_row], the weight at 3 nm), and its integration weight sym (wI/Fi)(wJ/Fj) t_i t_j
+// (also Wq[q]).
 __global__ void k_msh_frf(int nm, int nz, const ZoneM *__restrict__ zones, int nq, FrfPar frf,
                           float2 *__restrict__ Hq, float *__restrict__ Wq) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -347,101 +353,143 @@ __global__ void k_msh_frf(int nm, int nz, const ZoneM *__restrict__ zones, int n
     const double w = which == 0 ? v1 : which == 1 ? v2 : v1 + v2;
     double hr, hi;
     frf_eval(frf.M[m], frf.K[m], frf.C[m], w, hr, hi);
-    Hq[t] = make_float2((float)hr, (float)hi);
+    const int hs = frf_row(nm);
+    float2 *row = Hq + (size_t)q * hs;
+    row[r] = make_float2((float)hr, (float)hi);
     if (r == 0) {
         const double ti = (qi == 0 || qi == NI) ? 0.5 : 1.0, tj = (qj == 0 || qj == NJ) ? 0.5 : 1.0;
-        Wq[q] = (float)(z.sym * (z.wI / z.Fi) * (z.wJ / z.Fj) * ti * tj);
+        const float wq = (float)(z.sym * (z.wI / z.Fi) * (z.wJ / z.Fj) * ti * tj);
+        Wq[q] = wq;
+        row[3 * nm] = make_float2(wq, 0.f);
+        if (hs > 3 * nm + 1) row[3 * nm + 1] = make_float2(0.f, 0.f);
     }
 }
 
-constexpr int kQB = 16;  // BRM points per shared-memory round
-constexpr int kMomEPT = 3;  // term-tensor elements per thread (same j', b; consecutive a)
-constexpr int kVY = 64;     // staged (j', mode) pairs per point
+constexpr int kQB = 16;      // BRM points per work item
+constexpr int kMomEPT = 3;   // term-tensor elements per thread (same j', b; consecutive a)
+constexpr int kVY = 64;      // staged (j', mode) pairs per point
+constexpr int kWin = 776;    // corner window (floats): 3 x 256 elements + alignment slack
+constexpr int kHrow = 194;   // FRF row capacity (float2): frf_row(64)
 
-// s + c += x, compensated (Neumaier): the cell sums are added in FP32 with their rounding
-// errors carried, so the result does not depend on how cells are spread over blocks beyond
-// ~1e-13 relative, and no FP64 arithmetic (slow on GB300) runs per cell.
+// s + c += x, compensated (Neumaier): the zone sums are added in FP32 with their rounding
+// errors carried, so no FP64 arithmetic (slow on GB300) runs in the moment pass.
 __device__ __forceinline__ void csum(float &s, float &c, float x) {
     const float t = s + x;
     c += fabsf(s) >= fabsf(x) ? (s - t) + x : (x - t) + s;
     s = t;
 }
 
-__device__ __forceinline__ void cp_async4(void *dst, const void *src, bool valid) {
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)),
-                 "l"(src), "r"(valid ? 4 : 0)
+// Bulk copy global -> shared (16-byte aligned, size a multiple of 16), completing on bar.
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     su32(dst)),
+                 "l"(src), "r"(bytes), "r"(su32(bar))
                  : "memory");
 }
-__device__ __forceinline__ void cp_async8(void *dst, const void *src) {
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src)
-                 : "memory");
-}
-__device__ __forceinline__ void cp_async_commit_wait() {
-    asm volatile("cp.async.commit_group;\ncp.async.wait_all;" ::: "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 
-// Element layout of the moment pass: a block covers JB consecutive modes j' (JB > 1 only when
-// one j' leaves most of the block idle) and, per j', the pairs (arow, b) of AR = ceil(nm / EPT)
-// a-rows x nm columns; a thread holds the EPT elements (j', a = arow EPT + u, b), u < EPT, of the
-// term tensors (e = j' nm^2 + a nm + b).
+// Element layout of the moment pass.  A thread holds the EPT elements (j', a = arow EPT + u, b),
+// u < EPT, of the term tensors (e = j' nm^2 + a nm + b), AR = ceil(nm / EPT) a-rows per j'.
+//   JB = 1 (nm > ~19): a block covers RB = 256 / nm whole a-rows of one j' (thread t: a-row
+//     t / nm of the chunk, b = t % nm), nchj blocks per j';
+//   JB > 1: a block covers JB consecutive modes j' whole (thread t: jl = t / (AR nm)).
+// Either way the block's elements are one contiguous range of each point's term tensor, which
+// one bulk copy per (term, corner) brings in.
 struct MomLayout {
-    int JB, AR, nchj;  // modes per block, a-rows, blocks per j' group
+    int JB, AR, RB, nchj;
     static MomLayout make(int nm) {
         MomLayout L;
         L.AR = (nm + kMomEPT - 1) / kMomEPT;
         const int per_j = L.AR * nm;
         L.JB = std::max(1, std::min(256 / per_j, kVY / nm));
-        L.nchj = (L.JB * per_j + 255) / 256;
+        L.RB = L.JB > 1 ? L.AR : 256 / nm;
+        L.nchj = L.JB > 1 ? 1 : (L.AR + L.RB - 1) / L.RB;
         return L;
     }
     int groups(int nm) const { return (nm + JB - 1) / JB; }
     // dynamic shared memory of k_msh_moments
     static size_t smem() {
-        return (size_t)kQB * kVY * 16 + (size_t)kQB * 64 * 16 + (size_t)kQB * 3 * 64 * 8 + (size_t)kQB * 4 +
-               (size_t)12 * kMomEPT * 256 * 4;
+        return (size_t)kQB * kVY * 16 + (size_t)kQB * 64 * 16 + (size_t)kQB * kHrow * 8 + (size_t)12 * kWin * 4 + 16;
     }
 };
 
 // One unit of a block's work: the BRM points q0 .. q0 + nb - 1 (in the cell's row-major order)
-// of cell cid, with the cell geometry they need.
+// of cell loc of zone z, with the cell geometry they need.  Built by one thread and read by all
+// from shared memory.
 struct MomItem {
-    int cid, q0, nb, nq, nqj, qi0, qj0, i0, j0, rowq;  // rowq: BRM points per zone lattice row
-    size_t qbase, P00;
-    int nj;  // BFM lattice columns of the zone
-    const ZoneM *z;
+    int z, loc, q0, nb, nq, nqj, qi0, qj0, rowq, nj;  // rowq: BRM points per zone lattice row
+    int valid, zend;                                  // zend: the zone's last item of this block
+    long long qbase, P00;
+    float wp[4];  // BFM lattice trapezoid weights of the corners the cell owns
+    float rFi, rFj;
 };
 
-__device__ __forceinline__ bool mom_item(const ZoneM *__restrict__ zones, const int *__restrict__ cell_zone,
-                                         int ncells, int cid, int q0, MomItem &it) {
-    if (cid >= ncells) return false;
-    const ZoneM *z = zones + cell_zone[cid];
-    const int ni = z->ni, nj = z->nj, Fi = z->Fi, Fj = z->Fj;
-    const int loc = cid - z->cbase, i0 = loc / (nj - 1), j0 = loc - i0 * (nj - 1);
+// The item (z, loc, q0) of a cell that exists.
+__device__ __forceinline__ void mom_fill(const ZoneM *__restrict__ zones, int z, int loc, int q0, MomItem &it) {
+    const ZoneM &Z = zones[z];
+    const int ni = Z.ni, nj = Z.nj, Fi = Z.Fi, Fj = Z.Fj;
+    const int i0 = loc / (nj - 1), j0 = loc - i0 * (nj - 1);
     const int NJ = (nj - 1) * Fj, NI = (ni - 1) * Fi;
     const int qi0 = i0 * Fi, qi1 = (i0 == ni - 2) ? NI : (i0 + 1) * Fi - 1;
     const int qj0 = j0 * Fj, qj1 = (j0 == nj - 2) ? NJ : (j0 + 1) * Fj - 1;
-    it.cid = cid;
+    it.z = z;
+    it.loc = loc;
     it.q0 = q0;
     it.nqj = qj1 - qj0 + 1;
     it.nq = (qi1 - qi0 + 1) * it.nqj;
     it.nb = min(kQB, it.nq - q0);
     it.qi0 = qi0;
     it.qj0 = qj0;
-    it.i0 = i0;
-    it.j0 = j0;
     it.rowq = NJ + 1;
-    it.qbase = (size_t)z->qbase;
-    it.P00 = (size_t)z->pbase + (size_t)i0 * nj + j0;
     it.nj = nj;
-    it.z = z;
-    return true;
+    it.valid = 1;
+    it.zend = 0;
+    it.qbase = Z.qbase;
+    it.P00 = (long long)Z.pbase + (long long)i0 * nj + j0;
+    const int ci[4] = {i0, i0, i0 + 1, i0 + 1}, cj[4] = {j0, j0 + 1, j0, j0 + 1};
+    for (int k = 0; k < 4; ++k) {
+        const bool own = (ci[k] == i0 || i0 == ni - 2) && (cj[k] == j0 || j0 == nj - 2);
+        const float ti = (ci[k] == 0 || ci[k] == ni - 1) ? 0.5f : 1.f;
+        const float tj = (cj[k] == 0 || cj[k] == nj - 1) ? 0.5f : 1.f;
+        it.wp[k] = own ? Z.wb * ti * tj : 0.f;
+    }
+    it.rFi = 1.f / (float)Fi;
+    it.rFj = 1.f / (float)Fj;
 }
 
-// Block (g, y), y = group * nchj + chunk, cells g, g + G, ...  Each BRM point belongs to the
-// cell (min(qi/Fi, ni-2), min(qj/Fj, nj-2)) and each BFM point to the cell (min(i, ni-2),
-// min(j, nj-2)), so every lattice point is counted once.  part[g][6][nm^3]: m3mf of T1, T3,
-// T2, then m3mr of T1, T3, T2.
+// Block column g of G owns the cells loc = r, r + G, ... of each zone, r = (g + s_z) mod G with
+// s_z a hash of the zone's frequency origin (so every block column gets its share of the
+// zones' first cells, and the split of a zone depends on the zone alone).
+__device__ __forceinline__ int mom_first(const ZoneM &Z, int G, int g) {
+    const unsigned long long h = (unsigned long long)__double_as_longlong(Z.fi0) * 0x9E3779B97F4A7C15ull ^
+                                 (unsigned long long)__double_as_longlong(Z.fj0) * 0xC2B2AE3D27D4EB4Full;
+    const int sz = (int)((h >> 33) % (unsigned long long)G);
+    return (g + sz) % G;
+}
+
+// First cell at or after (z, loc) that block column g owns, as an item at q0 = 0; valid = 0
+// past the last zone.  newz: loc is to be taken from zone z's own start.
+__device__ __forceinline__ void mom_seek(const ZoneM *__restrict__ zones, int nz, int G, int g, int z, int loc,
+                                         bool newz, MomItem &it) {
+    while (z < nz) {
+        if (newz) loc = mom_first(zones[z], G, g);
+        if (loc < (zones[z].ni - 1) * (zones[z].nj - 1)) break;
+        ++z;
+        newz = true;
+    }
+    if (z < nz) {
+        mom_fill(zones, z, loc, 0, it);
+    } else {
+        it.valid = 0;
+        it.z = nz;
+    }
+}
+
+// Block (g, y), y = group * nchj + chunk: the cells of every zone that block column g owns
+// (mom_first).  Each BRM point belongs to the cell (min(qi/Fi, ni-2), min(qj/Fj, nj-2)) and
+// each BFM point to the cell (min(i, ni-2), min(j, nj-2)), so every lattice point is counted
+// once.  part[g][6][nm^3]: m3mf of T1, T3, T2, then m3mr of T1, T3, T2.  A zone's cells are
+// summed in FP32 and the zone sums added with compensation, so each zone's share depends on that
+// zone alone and the result is the same, to ~1e-13, for any zone order.
 //
 // The FRF products factor through per-point vectors staged in shared memory: with w the
 // point's weight, V_j'(a) = w H1(a) conj H3(j'), Y_j'(b) = w H1(j') H2(b),
@@ -452,122 +500,131 @@ __device__ __forceinline__ bool mom_item(const ZoneM *__restrict__ zones, const 
 // + ti tj (c0 - c1 - c2 + c3), its coefficients formed once per cell.  The b-indexed values are
 // read once per point for the thread's EPT elements.
 //
-// Pipeline: the raw FRF rows of the next work item's points and, at a cell's first item, the
-// thread's own corner values of the next cell are copied (cp.async) into shared memory while
-// the current item computes, so each item waits only for the two block barriers around the
-// conversion of its raw rows into the V, Y vectors.
-__global__ __launch_bounds__(256, 2) void k_msh_moments(int nm, MomLayout L, const ZoneM *__restrict__ zones,
-                                                        const int *__restrict__ cell_zone, int ncells,
-                                                        const float *__restrict__ T1, const float *__restrict__ T3,
-                                                        const float *__restrict__ T2, const float2 *__restrict__ Hq,
-                                                        const float *__restrict__ Wq, double *__restrict__ part) {
+// Pipeline: thread 0 builds the work items and issues bulk copies (one mbarrier phase per
+// item): the FRF rows of the next item's points (one copy per lattice-row segment) and, at a
+// cell's first item, the block's element window of the 4 corners x 3 terms.  They land while
+// the current item computes.  The waits are bounded (err code 5 on timeout).
+__global__ __launch_bounds__(256, 2) void k_msh_moments(int nm, int nm3p, MomLayout L, const ZoneM *__restrict__ zones,
+                                                        int nz, const float *__restrict__ T1,
+                                                        const float *__restrict__ T3, const float *__restrict__ T2,
+                                                        const float2 *__restrict__ Hq, double *__restrict__ part,
+                                                        int *__restrict__ err) {
     constexpr int EPT = kMomEPT;
     extern __shared__ __align__(16) unsigned char msm[];
     float4(*VY)[kVY] = reinterpret_cast<float4(*)[kVY]>(msm);                            // {V_j'(m), Y_j'(m)}
     float4(*H23)[64] = reinterpret_cast<float4(*)[64]>(msm + kQB * kVY * 16);            // {H2(m), H3(m)}
-    float2 *Hraw = reinterpret_cast<float2 *>(msm + kQB * kVY * 16 + kQB * 64 * 16);     // [kQB][3 nm]
-    float *Wraw = reinterpret_cast<float *>(Hraw + kQB * 3 * 64);                        // [kQB]
-    float *Cs = Wraw + kQB;                                                              // [12 EPT][256]
+    float2 *Hraw = reinterpret_cast<float2 *>(msm + kQB * kVY * 16 + kQB * 64 * 16);     // [kQB][hs]
+    float *Cs = reinterpret_cast<float *>(Hraw + kQB * kHrow);                           // [12][kWin]
+    uint64_t *bar = reinterpret_cast<uint64_t *>(Cs + 12 * kWin);
     __shared__ float2 tq[kQB];  // (ti, tj)
-    const int nm2 = nm * nm, nm3 = nm2 * nm, tid = threadIdx.x;
+    __shared__ MomItem sit[2];  // the current and the next item
+    const int nm2 = nm * nm, nm3 = nm2 * nm, tid = threadIdx.x, hs = frf_row(nm);
     const int grp = blockIdx.y / L.nchj, chunk = blockIdx.y % L.nchj;
     const int jg0 = grp * L.JB, njb = min(L.JB, nm - jg0), per_j = L.AR * nm;
-    // this thread's elements: (jl, a = arow EPT + u, b)
-    const int pidx = chunk * 256 + tid;
-    const int jl = pidx / per_j, rem = pidx % per_j, arow = rem / nm, b = rem % nm;
-    const bool tval = jl < njb;
+    // this thread's elements and the block's window [win0, win0 + wlen) of a point's tensor
+    int jl, arow, b;
+    bool tval;
+    int win0, wlen;
+    if (L.JB > 1) {
+        jl = tid / per_j;
+        const int rem = tid - jl * per_j;
+        arow = rem / nm;
+        b = rem - arow * nm;
+        tval = jl < njb;
+        win0 = (jg0 * nm2) & ~3;
+        wlen = (((jg0 + njb) * nm2 + 3) & ~3) - win0;
+    } else {
+        jl = 0;
+        arow = chunk * L.RB + tid / nm;
+        b = tid % nm;
+        tval = tid < L.RB * nm && arow < L.AR;
+        const int a0 = chunk * L.RB * EPT, a1 = min(nm, (chunk + 1) * L.RB * EPT);
+        win0 = (jg0 * nm2 + a0 * nm) & ~3;
+        wlen = ((jg0 * nm2 + a1 * nm + 3) & ~3) - win0;
+    }
     const int nval = tval ? min(EPT, nm - arow * EPT) : 0;  // valid elements
     const int ev0 = tval ? (jg0 + jl) * nm2 + arow * EPT * nm + b : 0;  // element u: ev0 + u nm
-    // elements past a = nm - 1 (u >= nval) read the next staged entries, which lie inside the
-    // dynamic shared memory (VY is followed by H23, H23 by Hraw); their sums are never stored
+    const int wofs = tval ? ev0 - win0 : 0;                           // in the window
+    // elements past a = nm - 1 (u >= nval) read the next staged V, Y, H entries, which lie inside
+    // the dynamic shared memory (VY is followed by H23, H23 by Hraw); their sums are never stored
     const int ia0 = tval ? jl * nm + arow * EPT : 0, ih0 = tval ? arow * EPT : 0;
     const int yb = tval ? jl * nm + b : 0, bb = tval ? b : 0;
     // conversion roles: (jl, m) pairs of VY, modes of H23
     const int st = tid & (kVY - 1), sq0 = tid / kVY;
     const int sjl = st / nm, sm = st - sjl * nm;
     const bool svy = sjl < njb;
-    // raw-copy roles: row entry sc of points sr0, sr0 + srp, ...
-    const int srow = 3 * nm, srp = 256 / srow, sr0 = tid / srow, sc = tid - sr0 * srow;
     const float *Ts[3] = {T1, T3, T2};
 
-    // issue the copies of item it: raw FRF rows and weights; corners at a cell's first item
+    // thread 0: the copies of item it (one mbarrier phase)
     auto issue = [&](const MomItem &it) {
-        if (sr0 < srp) {
-            int ql = sr0, qq = it.q0 + sr0, qr = qq / it.nqj, qc = qq - qr * it.nqj;
-            for (; ql < it.nb; ql += srp) {
-                const size_t gq = it.qbase + (size_t)(it.qi0 + qr) * it.rowq + (it.qj0 + qc);
-                cp_async8(Hraw + ql * srow + sc, Hq + gq * srow + sc);
-                if (sc == 0) cp_async4(Wraw + ql, Wq + gq, true);
-                qc += srp;
-                while (qc >= it.nqj) {
-                    qc -= it.nqj;
-                    ++qr;
-                }
+        uint32_t bytes = 0;
+        {
+            int qq = it.q0;
+            const int qe = it.q0 + it.nb;
+            while (qq < qe) {
+                const int qr = qq / it.nqj, qc = qq - qr * it.nqj, n = min(it.nqj - qc, qe - qq);
+                bytes += (uint32_t)n * hs * 8;
+                qq += n;
             }
         }
-        if (it.q0 == 0) {
-            const size_t Pc[4] = {it.P00, it.P00 + 1, it.P00 + it.nj, it.P00 + it.nj + 1};
-#pragma unroll
-            for (int t = 0; t < 3; ++t)
-#pragma unroll
-                for (int k = 0; k < 4; ++k)
-#pragma unroll
-                    for (int u = 0; u < EPT; ++u) {
-                        const bool v = u < nval;
-                        const float *src = v ? Ts[t] + Pc[k] * nm3 + ev0 + u * nm : Ts[t];
-                        cp_async4(Cs + ((t * 4 + k) * EPT + u) * 256 + tid, src, v);
-                    }
+        if (it.q0 == 0) bytes += 12u * (uint32_t)wlen * 4;
+        mbar_expect_tx(bar, bytes);
+        int qq = it.q0;
+        const int qe = it.q0 + it.nb;
+        while (qq < qe) {
+            const int qr = qq / it.nqj, qc = qq - qr * it.nqj, n = min(it.nqj - qc, qe - qq);
+            const size_t gq = (size_t)it.qbase + (size_t)(it.qi0 + qr) * it.rowq + (it.qj0 + qc);
+            bulk_g2s(Hraw + (qq - it.q0) * hs, Hq + gq * hs, (uint32_t)n * hs * 8, bar);
+            qq += n;
         }
-        cp_async_commit();
+        if (it.q0 == 0) {
+            const size_t P0 = (size_t)it.P00;
+            const size_t Pc[4] = {P0, P0 + 1, P0 + it.nj, P0 + it.nj + 1};
+            for (int t = 0; t < 3; ++t)
+                for (int k = 0; k < 4; ++k)
+                    bulk_g2s(Cs + (t * 4 + k) * kWin, Ts[t] + Pc[k] * nm3p + win0, (uint32_t)wlen * 4, bar);
+        }
     };
 
-    float mf[EPT][3], mfe[EPT][3], mr[EPT][3], mre[EPT][3];  // compensated sums over cells
-    float cA[EPT][3], cB[EPT][3], cC[EPT][3], cD[EPT][3], sr[EPT][3];
+    float mf[EPT][3], mfe[EPT][3], mr[EPT][3], mre[EPT][3];  // compensated sums over zones
+    float cA[EPT][3], cB[EPT][3], cC[EPT][3], cD[EPT][3];    // the cell's bilinear coefficients
+    float zf[EPT][3], zr[EPT][3];                             // the zone's FP32 sums
 #pragma unroll
     for (int u = 0; u < EPT; ++u)
 #pragma unroll
-        for (int t = 0; t < 3; ++t) mf[u][t] = mfe[u][t] = mr[u][t] = mre[u][t] = sr[u][t] = 0.f;
+        for (int t = 0; t < 3; ++t) mf[u][t] = mfe[u][t] = mr[u][t] = mre[u][t] = zf[u][t] = zr[u][t] = 0.f;
 
-    MomItem cur;
-    bool have = mom_item(zones, cell_zone, ncells, blockIdx.x, 0, cur);
-    if (have) issue(cur);
-    while (have) {
-        asm volatile("cp.async.wait_all;" ::: "memory");
-        __syncthreads();  // raw rows of cur visible; VY, H23 and tq free
-        const ZoneM *z = cur.z;
+    if (tid == 0) {
+        mbar_init(bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        mom_seek(zones, nz, gridDim.x, blockIdx.x, 0, 0, true, sit[0]);
+        if (sit[0].valid) issue(sit[0]);
+    }
+    __syncthreads();
+    MomItem cur = sit[0];
+    bool ok = true;
+    for (int k = 0; cur.valid; ++k) {
+        if (!mbar_wait(bar, (uint32_t)(k & 1), err, 5)) ok = false;
+        __syncthreads();  // every thread done with the previous item's VY, H23, tq and items
         if (cur.q0 == 0) {
-            // BFM lattice trapezoid weights of the corners this cell owns
-            float wp[4];
-            {
-                const int ni = z->ni, nj = z->nj, i0 = cur.i0, j0 = cur.j0;
-                const int ci[4] = {i0, i0, i0 + 1, i0 + 1}, cj[4] = {j0, j0 + 1, j0, j0 + 1};
-#pragma unroll
-                for (int k = 0; k < 4; ++k) {
-                    const bool own = (ci[k] == i0 || i0 == ni - 2) && (cj[k] == j0 || j0 == nj - 2);
-                    const float ti = (ci[k] == 0 || ci[k] == ni - 1) ? 0.5f : 1.f;
-                    const float tj = (cj[k] == 0 || cj[k] == nj - 1) ? 0.5f : 1.f;
-                    wp[k] = own ? z->wb * ti * tj : 0.f;
-                }
-            }
 #pragma unroll
             for (int u = 0; u < EPT; ++u)
 #pragma unroll
                 for (int t = 0; t < 3; ++t) {
-                    const float *cs = Cs + ((t * 4) * EPT + u) * 256 + tid;
-                    const float c0 = cs[0], c1 = cs[EPT * 256], c2 = cs[2 * EPT * 256], c3 = cs[3 * EPT * 256];
+                    const float *cs = Cs + (t * 4) * kWin + (u < nval ? wofs + u * nm : wofs);
+                    const float c0 = cs[0], c1 = cs[kWin], c2 = cs[2 * kWin], c3 = cs[3 * kWin];
                     cA[u][t] = c0;
                     cB[u][t] = c2 - c0;
                     cC[u][t] = c1 - c0;
                     cD[u][t] = (c0 - c1) - (c2 - c3);
-                    csum(mf[u][t], mfe[u][t], fmaf(wp[3], c3, fmaf(wp[2], c2, fmaf(wp[1], c1, wp[0] * c0))));
-                    sr[u][t] = 0.f;
+                    zf[u][t] += fmaf(cur.wp[3], c3, fmaf(cur.wp[2], c2, fmaf(cur.wp[1], c1, cur.wp[0] * c0)));
                 }
         }
-        // raw rows -> V, Y, H2, H3 of the item's points; (ti, tj)
+        // FRF rows -> V, Y, H2, H3 of the item's points; (ti, tj)
         for (int ql = sq0; ql < cur.nb; ql += 256 / kVY) {
-            const float2 *h = Hraw + ql * 3 * nm;
+            const float2 *h = Hraw + ql * hs;
             if (svy) {
-                const float w = Wraw[ql];
+                const float w = h[3 * nm].x;
                 const int jg = jg0 + sjl;
                 const float2 h1 = h[sm], h2 = h[nm + sm];
                 const float2 h1j = h[jg], h3j = h[2 * nm + jg];
@@ -582,16 +639,23 @@ __global__ __launch_bounds__(256, 2) void k_msh_moments(int nm, MomLayout L, con
         }
         if (tid < cur.nb) {
             const int qq = cur.q0 + tid, qr = qq / cur.nqj, qc = qq - qr * cur.nqj;
-            tq[tid] = make_float2((float)(cur.qi0 + qr - cur.i0 * z->Fi) / (float)z->Fi,
-                                  (float)(cur.qj0 + qc - cur.j0 * z->Fj) / (float)z->Fj);
+            tq[tid] = make_float2((float)qr * cur.rFi, (float)qc * cur.rFj);
         }
-        __syncthreads();  // VY, H23, tq ready; raw rows and corners consumed
-        // next item: its copies run under this item's arithmetic
-        MomItem nxt;
-        const bool last = cur.q0 + kQB >= cur.nq;
-        have = last ? mom_item(zones, cell_zone, ncells, cur.cid + gridDim.x, 0, nxt)
-                    : mom_item(zones, cell_zone, ncells, cur.cid, cur.q0 + kQB, nxt);
-        if (have) issue(nxt);
+        MomItem &nx = sit[(k + 1) & 1];
+        if (tid == 32) {
+            // the next item; cur's zone ends with it when nx is in another zone
+            if (cur.q0 + kQB < cur.nq)
+                mom_fill(zones, cur.z, cur.loc, cur.q0 + kQB, nx);
+            else
+                mom_seek(zones, nz, gridDim.x, blockIdx.x, cur.z, cur.loc + gridDim.x, false, nx);
+            sit[k & 1].zend = nx.z != cur.z;
+        }
+        // VY, H23, tq and the next item ready; FRF rows and corners consumed
+        if (__syncthreads_or(!ok)) break;  // a copy did not arrive: leave with the error code set
+        const bool zend = sit[k & 1].zend;
+        const MomItem nxt = nx;
+        // the next item's copies run under this item's arithmetic
+        if (tid == 0 && nxt.valid) issue(nxt);
         for (int ql = 0; ql < cur.nb; ++ql) {
             const float2 tt = tq[ql];
             const float ti = tt.x, tj = tt.y, tij = ti * tj;
@@ -599,7 +663,7 @@ __global__ __launch_bounds__(256, 2) void k_msh_moments(int nm, MomLayout L, con
             const float2 ybv = reinterpret_cast<const float2 *>(&VY[ql][yb])[1];  // Y_j'(b)
 #pragma unroll
             for (int u = 0; u < EPT; ++u) {
-                const float4 va = VY[ql][ia0 + u];                                              // V_j'(a), Y_j'(a)
+                const float4 va = VY[ql][ia0 + u];                                          // V_j'(a), Y_j'(a)
                 const float2 h3a = reinterpret_cast<const float2 *>(&H23[ql][ih0 + u])[1];  // H3(a)
                 const float f1 = hb.x * va.x - hb.y * va.y;
                 const float f3 = ybv.x * h3a.x + ybv.y * h3a.y;
@@ -608,15 +672,19 @@ __global__ __launch_bounds__(256, 2) void k_msh_moments(int nm, MomLayout L, con
 #pragma unroll
                 for (int t = 0; t < 3; ++t) {
                     const float v = fmaf(tij, cD[u][t], fmaf(tj, cC[u][t], fmaf(ti, cB[u][t], cA[u][t])));
-                    sr[u][t] = fmaf(fs[t], v, sr[u][t]);
+                    zr[u][t] = fmaf(fs[t], v, zr[u][t]);
                 }
             }
         }
-        if (last) {
+        if (zend) {
 #pragma unroll
             for (int u = 0; u < EPT; ++u)
 #pragma unroll
-                for (int t = 0; t < 3; ++t) csum(mr[u][t], mre[u][t], sr[u][t]);
+                for (int t = 0; t < 3; ++t) {
+                    csum(mf[u][t], mfe[u][t], zf[u][t]);
+                    csum(mr[u][t], mre[u][t], zr[u][t]);
+                    zf[u][t] = zr[u][t] = 0.f;
+                }
         }
         cur = nxt;
     }
@@ -635,12 +703,12 @@ __global__ __launch_bounds__(256, 2) void k_msh_moments(int nm, MomLayout L, con
 // Per-zone mode-diagonal response moments m3mr(m, m, m) of the zone alone (the refinement
 // criterion's quantity): one block per zone, threads over its BRM points, the three terms
 // summed at element (m, m, m) before the FRF (the same FRF for all three there).
-__global__ void k_msh_zone_diag(int nm, const ZoneM *__restrict__ zones, const float *__restrict__ T1,
+__global__ void k_msh_zone_diag(int nm, size_t nm3p, const ZoneM *__restrict__ zones, const float *__restrict__ T1,
                                 const float *__restrict__ T3, const float *__restrict__ T2,
                                 const float2 *__restrict__ Hq, const float *__restrict__ Wq,
                                 double *__restrict__ zdiag) {
     const ZoneM z = zones[blockIdx.x];
-    const int nm2 = nm * nm, nm3 = nm2 * nm;
+    const int nm2 = nm * nm;
     const int NI = (z.ni - 1) * z.Fi, NJ = (z.nj - 1) * z.Fj, nq = (NI + 1) * (NJ + 1);
     __shared__ double red[256];
     for (int m = 0; m < nm; ++m) {
@@ -656,10 +724,11 @@ __global__ void k_msh_zone_diag(int nm, const ZoneM *__restrict__ zones, const f
             const size_t P[4] = {P00, P01, P10, P11};
 #pragma unroll
             for (int k = 0; k < 4; ++k)
-                c[k] = T1[P[k] * nm3 + em] + T3[P[k] * nm3 + em] + T2[P[k] * nm3 + em];
+                c[k] = T1[P[k] * nm3p + em] + T3[P[k] * nm3p + em] + T2[P[k] * nm3p + em];
             const float v = (c[0] * (1.f - tj) + c[1] * tj) * (1.f - ti) + (c[2] * (1.f - tj) + c[3] * tj) * ti;
             const size_t gq = (size_t)z.qbase + q;
-            const float2 h1 = Hq[gq * 3 * nm + m], h2 = Hq[gq * 3 * nm + nm + m], h3 = Hq[gq * 3 * nm + 2 * nm + m];
+            const float2 *hrow = Hq + gq * frf_row(nm);
+            const float2 h1 = hrow[m], h2 = hrow[nm + m], h3 = hrow[2 * nm + m];
             const float F = (h1.x * h2.x - h1.y * h2.y) * h3.x + (h1.x * h2.y + h1.y * h2.x) * h3.y;
             s += (double)(Wq[gq] * F * v);
         }
@@ -760,8 +829,6 @@ int Engine::msh_mixed_batch(const std::vector<ZoneDev> &zs, std::vector<double> 
     for (int u = 0; u < nU; ++u) usrc[u] = F.at(UF.v[u]);
     std::vector<Task> tasks;
     std::vector<ZoneM> zm;
-    std::vector<int> cellz;
-    cellz.reserve((size_t)ncells);
     {
         long long pb = 0, cb = 0, gb = 0, qb = 0;
         for (const ZoneDev &z : zs) {
@@ -769,7 +836,6 @@ int Engine::msh_mixed_batch(const std::vector<ZoneDev> &zs, std::vector<double> 
                     (float)(z.sym * z.wI * z.wJ)};
             qb += (long long)((z.ni - 1) * z.Fi + 1) * ((z.nj - 1) * z.Fj + 1);
             zm.push_back(m);
-            cellz.insert(cellz.end(), (size_t)(z.ni - 1) * (z.nj - 1), (int)zm.size() - 1);
             for (int j = 0; j < z.nj; ++j) gsrc[gb + j] = F.at(z.fj0 + j * z.dJj);
             for (int i = 0; i < z.ni; ++i) {
                 const double r = z.fi0 + i * z.dIi;
@@ -794,8 +860,9 @@ int Engine::msh_mixed_batch(const std::vector<ZoneDev> &zs, std::vector<double> 
     if ((e = cudaEventRecord(ev2, stream))) return cuda_fail(e, "event");
     if ((rc = build_atable(F.v, true, true))) return rc;
     const size_t uel = (size_t)nU * Mp * Kp, gel = (size_t)ncol * NMT * Kp, sel = 2 * (size_t)npts * NMT * Kp;
-    const size_t tel = (size_t)npts * nm3;
-    const size_t nidx = (size_t)nU + ncol + 2 * (size_t)npts + ncells;
+    const int nm3p = (nm3 + 3) & ~3, hs = frf_row(nm);
+    const size_t tel = (size_t)npts * nm3p;
+    const size_t nidx = (size_t)nU + ncol + 2 * (size_t)npts;
     // work items: per task, its row tiles x N tiles, one N tile each, consecutive
     std::vector<int4> witems;
     for (size_t t = 0; t < tasks.size(); ++t) {
@@ -816,15 +883,15 @@ int Engine::msh_mixed_batch(const std::vector<ZoneDev> &zs, std::vector<double> 
         (e = dMshIdx.reserve(nidx * sizeof(int) + tasks.size() * sizeof(Task) + zm.size() * sizeof(ZoneM) +
                              witems.size() * sizeof(int4) + 64)) ||
         (e = dMixPart.reserve((size_t)G * 6 * nm3 * sizeof(double) + 2 * (size_t)nm3 * sizeof(double) + 256)) ||
-        (e = dMixH.reserve((size_t)nbrm * 3 * nm * sizeof(float2) + (size_t)nbrm * sizeof(float) + 256 +
+        (e = dMixH.reserve((size_t)nbrm * hs * sizeof(float2) + (size_t)nbrm * sizeof(float) + 256 +
                            (zdiag ? zm.size() * nm * sizeof(double) : 0))))
         return cuda_fail(e, "allocating Mesher BF16x3 operands");
     __nv_bfloat16 *Uh = dMixA.as<__nv_bfloat16>(), *Ul = Uh + uel;
     __nv_bfloat16 *Gh = dMixB.as<__nv_bfloat16>(), *Gl = Gh + gel, *Sh = Gl + gel, *Sl = Sh + sel;
     float *T1 = dMshT.as<float>(), *T3 = T1 + tel, *T2 = T3 + tel;
     char *ib = (char *)dMshIdx.p;
-    int *d_usrc = (int *)ib, *d_gsrc = d_usrc + nU, *d_ssrc = d_gsrc + ncol, *d_cellz = d_ssrc + 2 * npts;
-    Task *d_tasks = (Task *)(((uintptr_t)(d_cellz + ncells) + 15) & ~(uintptr_t)15);
+    int *d_usrc = (int *)ib, *d_gsrc = d_usrc + nU, *d_ssrc = d_gsrc + ncol;
+    Task *d_tasks = (Task *)(((uintptr_t)(d_ssrc + 2 * npts) + 15) & ~(uintptr_t)15);
     ZoneM *d_zones = (ZoneM *)(((uintptr_t)(d_tasks + tasks.size()) + 15) & ~(uintptr_t)15);
     int4 *d_items = (int4 *)(((uintptr_t)(d_zones + zm.size()) + 15) & ~(uintptr_t)15);
     double *part = dMixPart.as<double>(), *red = part + (size_t)G * 6 * nm3;
@@ -832,7 +899,6 @@ int Engine::msh_mixed_batch(const std::vector<ZoneDev> &zs, std::vector<double> 
     if ((e = cudaMemcpyAsync(d_usrc, usrc.data(), nU * sizeof(int), cudaMemcpyHostToDevice, stream)) ||
         (e = cudaMemcpyAsync(d_gsrc, gsrc.data(), ncol * sizeof(int), cudaMemcpyHostToDevice, stream)) ||
         (e = cudaMemcpyAsync(d_ssrc, ssrc.data(), 2 * npts * sizeof(int), cudaMemcpyHostToDevice, stream)) ||
-        (e = cudaMemcpyAsync(d_cellz, cellz.data(), ncells * sizeof(int), cudaMemcpyHostToDevice, stream)) ||
         (e = cudaMemcpyAsync(d_tasks, tasks.data(), tasks.size() * sizeof(Task), cudaMemcpyHostToDevice, stream)) ||
         (e = cudaMemcpyAsync(d_zones, zm.data(), zm.size() * sizeof(ZoneM), cudaMemcpyHostToDevice, stream)) ||
         (e = cudaMemcpyAsync(d_items, witems.data(), witems.size() * sizeof(int4), cudaMemcpyHostToDevice, stream)) ||
@@ -859,6 +925,7 @@ int Engine::msh_mixed_batch(const std::vector<ZoneDev> &zs, std::vector<double> 
     prm.tasks = d_tasks;
     prm.items = d_items;
     prm.T1 = T1; prm.T3 = T3; prm.T2 = T2;
+    prm.nm3p = nm3p;
     prm.err = derr;
     const long long nwork = (long long)witems.size();
     const int grid = (int)std::min<long long>(nwork, nsm);
@@ -870,20 +937,20 @@ int Engine::msh_mixed_batch(const std::vector<ZoneDev> &zs, std::vector<double> 
     if ((e = cudaGetLastError())) return cuda_fail(e, "Mesher BF16x3 contraction kernel");
     if ((e = cudaEventRecord(evg1, stream))) return cuda_fail(e, "event");
     float2 *Hq = dMixH.as<float2>();
-    float *Wq = (float *)(Hq + (size_t)nbrm * 3 * nm);
+    float *Wq = (float *)(Hq + (size_t)nbrm * hs);
     {
         const long long nt = nbrm * 3 * nm;
         k_msh_frf<<<(unsigned)((nt + 255) / 256), 256, 0, stream>>>(nm, (int)zm.size(), d_zones, (int)nbrm, frf(), Hq, Wq);
     }
     if ((e = cudaFuncSetAttribute(k_msh_moments, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)MomLayout::smem())))
         return cuda_fail(e, "kernel attribute");
-    k_msh_moments<<<dim3(G, nchunks), 256, MomLayout::smem(), stream>>>(nm, ML, d_zones, d_cellz, (int)ncells, T1, T3,
-                                                                       T2, Hq, Wq, part);
+    k_msh_moments<<<dim3(G, nchunks), 256, MomLayout::smem(), stream>>>(nm, nm3p, ML, d_zones, (int)zm.size(), T1,
+                                                                       T3, T2, Hq, part, derr);
     k_msh_reduce<<<(nm3 + 127) / 128, 128, 0, stream>>>(nm, G, part, red, red + nm3);
     double *d_zdiag = nullptr;
     if (zdiag) {
         d_zdiag = (double *)(((uintptr_t)(Wq + nbrm) + 255) & ~(uintptr_t)255);
-        k_msh_zone_diag<<<(unsigned)zm.size(), 256, 0, stream>>>(nm, d_zones, T1, T3, T2, Hq, Wq, d_zdiag);
+        k_msh_zone_diag<<<(unsigned)zm.size(), 256, 0, stream>>>(nm, (size_t)nm3p, d_zones, T1, T3, T2, Hq, Wq, d_zdiag);
         kernels += 1;
     }
     if ((e = cudaGetLastError())) return cuda_fail(e, "Mesher zone integration");
