@@ -147,81 +147,6 @@ cudaError_t launch_atable(cudaStream_t st, int nf, const double *f, int ntc, int
     return cudaGetLastError();
 }
 
-// Same factor in FP32 (operand source of the split-precision contractions, whose operands
-// are rounded to bf16 hi + lo anyway): A(f) = diag(s) C(f) diag(s) L with s = sqrt(S(f)) and
-// C(f) = [c_ij^|f|] generated on the fly, as a register-tiled FP32 product.  Block: BM rows i
-// x BN modes, j streamed in tiles of 32 through shared memory; thread tile 4 x 4.
-template <int BN>
-__global__ __launch_bounds__(256) void k_atable32(int nf, const double *__restrict__ f, int ntc, int nnl, int nm,
-                                                  const float *__restrict__ logc, const double *__restrict__ S,
-                                                  const float *__restrict__ L, float *__restrict__ A) {
-    constexpr int BM = 4096 / BN, BK = 32, NTN = BN / 4;
-    __shared__ __align__(16) float Gs[BK][BM + 4];  // [j][i]
-    __shared__ __align__(16) float Ls[BK][BN + 4];  // [j][m]
-    const int fi = blockIdx.x / ntc, itc = blockIdx.x % ntc;
-    const int i0 = blockIdx.y * BM, m0 = blockIdx.z * BN;
-    const float af = (float)fabs(f[fi]);
-    const double *Sf = S + ((size_t)fi * ntc + itc) * nnl;
-    const float *lc = logc + (size_t)itc * nnl * nnl;
-    const float *Lt = L + (size_t)itc * nnl * nm;
-    const int t = threadIdx.x, tm = t / NTN, tn = t % NTN;
-    float acc[4][4];
-#pragma unroll
-    for (int r = 0; r < 4; ++r)
-#pragma unroll
-        for (int c = 0; c < 4; ++c) acc[r][c] = 0.f;
-    for (int j0 = 0; j0 < nnl; j0 += BK) {
-        for (int e = t; e < BM * BK; e += 256) {
-            const int ii = e / BK, jj = e % BK, gi = i0 + ii, gj = j0 + jj;
-            float g = 0.f;
-            if (gi < nnl && gj < nnl) g = (af == 0.f) ? 1.f : expf(af * lc[(size_t)gi * nnl + gj]);  // c^0 = 1
-            Gs[jj][ii] = g;
-        }
-        for (int e = t; e < BK * BN; e += 256) {
-            const int jj = e / BN, mm = e % BN, gj = j0 + jj, m = m0 + mm;
-            Ls[jj][mm] = (gj < nnl && m < nm) ? sqrtf((float)Sf[gj]) * Lt[(size_t)gj * nm + m] : 0.f;
-        }
-        __syncthreads();
-#pragma unroll
-        for (int jj = 0; jj < BK; ++jj) {
-            const float4 gv = *(const float4 *)&Gs[jj][tm * 4];
-            const float4 lv = *(const float4 *)&Ls[jj][tn * 4];
-            const float g4[4] = {gv.x, gv.y, gv.z, gv.w}, l4[4] = {lv.x, lv.y, lv.z, lv.w};
-#pragma unroll
-            for (int r = 0; r < 4; ++r)
-#pragma unroll
-                for (int c = 0; c < 4; ++c) acc[r][c] = fmaf(g4[r], l4[c], acc[r][c]);
-        }
-        __syncthreads();
-    }
-#pragma unroll
-    for (int r = 0; r < 4; ++r) {
-        const int gi = i0 + tm * 4 + r;
-        if (gi >= nnl) continue;
-        const float si = sqrtf((float)Sf[gi]);
-        float *out = A + (((size_t)fi * ntc + itc) * nnl + gi) * nm;
-#pragma unroll
-        for (int c = 0; c < 4; ++c) {
-            const int m = m0 + tn * 4 + c;
-            if (m < nm) out[m] = si * acc[r][c];
-        }
-    }
-}
-
-cudaError_t launch_atable32(cudaStream_t st, int nf, const double *f, int ntc, int nnl, int nm,
-                            const float *logc, const double *S, const float *L, float *A) {
-    if (nf == 0) return cudaSuccess;
-    if (nm > 64) return cudaErrorInvalidValue;
-    if (nm <= 32) {
-        dim3 grid((unsigned)nf * ntc, (unsigned)((nnl + 127) / 128), 1);
-        k_atable32<32><<<grid, 256, 0, st>>>(nf, f, ntc, nnl, nm, logc, S, L, A);
-    } else {
-        dim3 grid((unsigned)nf * ntc, (unsigned)((nnl + 63) / 64), 1);
-        k_atable32<64><<<grid, 256, 0, st>>>(nf, f, ntc, nnl, nm, logc, S, L, A);
-    }
-    return cudaGetLastError();
-}
-
 // ------------------------------------------------------------------------------------
 // Second-order path: force PSD and m2 moments (functionsImpl.F90:1548-1560, 1653-1676;
 // BsaClassicImpl.F90:149-154, 197-210).

@@ -13,10 +13,6 @@ cudaError_t launch_nodal_psd(cudaStream_t st, int nf, const double *f, int ntc, 
 cudaError_t launch_atable(cudaStream_t st, int nf, const double *f, int ntc, int nnl, int nm,
                           const double *logc, const double *S, const double *L, double *A);
 
-// The same factor in FP32 (source of the split-precision contractions' operands), from FP32
-// copies of log c and L.
-cudaError_t launch_atable32(cudaStream_t st, int nf, const double *f, int ntc, int nnl, int nm,
-                            const float *logc, const double *S, const float *L, float *A);
 
 // The FP32 table on the tensor cores (bsa_atable_tc.cu): tf32 hi/lo split, FP32 accumulation;
 // err receives a nonzero code if a pipeline wait ran out of its budget.  nm <= 64.
