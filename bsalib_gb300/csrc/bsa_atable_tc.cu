@@ -127,19 +127,34 @@ __global__ void __launch_bounds__(kThreads) k_atable_tc(int ntc, int n, int nm, 
     // A tasks of a thread: (row r, 4-wide chunk c) = (t >> 3, t & 7), t = tid + 256 u, u < 4
     constexpr int NU = kRows * 8 / kThreads;
     const float *rowp[NU];
-    float rmask[NU];
+    bool rval[NU];
+    const int cofs = (tid & 7) * 4;  // the same for every u (256 is a multiple of 8)
 #pragma unroll
     for (int u = 0; u < NU; ++u) {
         const int tt = tid + kThreads * u, gi = i0 + (tt >> 3);
-        rowp[u] = lc + (size_t)min(gi, n - 1) * n + (tt & 7) * 4;
-        rmask[u] = gi < n ? 1.f : 0.f;
+        rowp[u] = lc + (size_t)min(gi, n - 1) * n;
+        rval[u] = gi < n;
     }
+    // n a multiple of 4: one 16-byte load per task (rows of log c 16-byte aligned); columns past
+    // n read the row's last four values (s_j = 0 there)
+    const bool vec = (n & 3) == 0;
     float pre[NU][4];
     auto load_chunk = [&](int j0) {  // log c of the chunk, columns clamped (s_j = 0 there)
+        if (vec) {
 #pragma unroll
-        for (int u = 0; u < NU; ++u)
+            for (int u = 0; u < NU; ++u) {
+                const float4 x = __ldg((const float4 *)(rowp[u] + min(j0 + cofs, n - 4)));
+                pre[u][0] = x.x;
+                pre[u][1] = x.y;
+                pre[u][2] = x.z;
+                pre[u][3] = x.w;
+            }
+        } else {
 #pragma unroll
-            for (int q = 0; q < 4; ++q) pre[u][q] = rowp[u][min(j0 + q, n - 1 - (((tid + kThreads * u) & 7) * 4))];
+            for (int u = 0; u < NU; ++u)
+#pragma unroll
+                for (int q = 0; q < 4; ++q) pre[u][q] = rowp[u][min(j0 + cofs + q, n - 1)];
+        }
     };
     auto copy_b = [&](int kc, int s) {  // B tile of chunk kc into stage s (swizzled 16-byte pieces)
         uint8_t *Bh = smem + s * LY::kStage + 2 * kATile, *Bl = Bh + LY::kBTile;
@@ -172,9 +187,11 @@ __global__ void __launch_bounds__(kThreads) k_atable_tc(int ntc, int n, int nm, 
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
                 const float g = af == 0.f ? 1.f : ex2_approx(sc * pre[u][q]);  // c^0 = 1
-                const float v = g * s4[q] * rmask[u];
+                const float v = rval[u] ? g * s4[q] : 0.f;
                 h[q] = tf32_rna(v);
-                l[q] = tf32_rna(v - __uint_as_float(h[q]));
+                // the remainder is exact in FP32; the MMA reads its top 19 bits (truncation
+                // costs at most 2^-10 of the remainder, ~2^-21 of v)
+                l[q] = __float_as_uint(v - __uint_as_float(h[q]));
             }
             *(uint4 *)(Ah + swz(r, c)) = make_uint4(h[0], h[1], h[2], h[3]);
             *(uint4 *)(Al + swz(r, c)) = make_uint4(l[0], l[1], l[2], l[3]);
