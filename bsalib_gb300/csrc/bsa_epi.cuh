@@ -76,10 +76,13 @@ __device__ __forceinline__ void stage(HTile<NMT, JH> *dst, const float2 *Hg, con
 // c >= r only (d1 false: not formed for this tile) and each value also stands for term 1 at
 // (c, r) with (m, n, o) = (a, j, b): weight w(c, r) = w(r, c), FRF Re[H_a(w_c) H_j(w_r)
 // conj H_b(w_r + w_c)]; those go to acc[5] (response) and acc[6] (force), c > r only.
+//
+// d3off: TMEM column offset of the D3 accumulator from taddr (128; 0 when the tile's D3 sits
+// where a D1 would, the first half of an N = 256 pair).
 template <int NMT, int JH, bool SYM = false, int KINDS = 5>
 __device__ __forceinline__ void tile(const HTile<NMT, JH> &hb, uint32_t taddr, int a, int b, int c0, int nf,
                                      bool vect, bool b1, float wv_r, int jh, float (&acc)[KINDS][NMT], int r = 0,
-                                     bool d1 = true) {
+                                     bool d1 = true, uint32_t d3off = 128) {
     constexpr int NC = kBN / NMT, W = NMT * JH;
     const int jo = jh * NMT;
     const float2 hra = hb.hr[a];
@@ -89,7 +92,7 @@ __device__ __forceinline__ void tile(const HTile<NMT, JH> &hb, uint32_t taddr, i
         for (int pass = 0; pass < 2; ++pass) {
             if (SYM && pass == 0 && !d1) continue;  // warp-uniform: no D1 in this tile
             uint32_t v[32];
-            tmem_ld32(taddr + pass * 128 + q * 32, v);
+            tmem_ld32(taddr + (pass ? d3off : 0u) + q * 32, v);
             tmem_wait_ld();
             float2 PA = make_float2(0.f, 0.f), PB = PA;
             float wc = 0.f, wn = 0.f, wt = 0.f;

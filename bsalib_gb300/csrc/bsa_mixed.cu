@@ -45,7 +45,7 @@ constexpr int kStageBytes = 6 * kTileBytes;      // U hi/lo, Bg hi/lo, Bs hi/lo
 constexpr int kKinds = 5;                        // mr1, mr3, mr2, mf1, mf23 (+ mr1T, mf1T with SYM)
 constexpr int kFlushTiles = 64;                  // FP32 -> FP64 flush period (N tiles)
 constexpr int kBarBytes = 256;                   // mbarriers + TMEM slot
-constexpr int kHBytes = 2 * (int)sizeof(epi::HTile<32, 2>);  // FRF staging, 2 tiles (largest form)
+constexpr int kHBytes = 4 * (int)sizeof(epi::HTile<32, 2>);  // FRF staging, 2 x 2 tiles (largest form)
 
 struct Params {
     int nf;          // grid size
@@ -67,8 +67,38 @@ struct Params {
     int *err;
 };
 
+// Work units of one (grid row r, mode half): the N tiles of the row as
+//   kind 1: two N tiles nt, nt + 1 without D1, their D3 in one N = 256 MMA (B = S(nt) | S(nt + 1));
+//   kind 2: one N tile without D1 (D3 alone, N = 128);
+//   kind 0: an N tile with D1 and D3 in one N = 256 MMA (B = G(nt) | S(nt)).
+// Without SYM every tile is kind 0.  With SYM the tiles nt < ntr = r / NC hold only columns
+// c < r (no D1): they come first, in pairs, an odd one alone.  Pairing them keeps 24 MMAs per
+// 96 KB stage, where a lone D3 tile has 12 per 64 KB and waits on its operands.
+struct Units {
+    int ntr, npair, single, n;
+    __device__ __forceinline__ Units(int r, int ntl, bool sym, int NC) {
+        ntr = sym ? min(ntl, r / NC) : 0;
+        npair = ntr >> 1;
+        single = ntr & 1;
+        n = npair + single + (ntl - ntr);
+    }
+    __device__ __forceinline__ void at(int u, int &kind, int &nt) const {
+        if (u < npair) {
+            kind = 1;
+            nt = 2 * u;
+        } else if (u < npair + single) {
+            kind = 2;
+            nt = ntr - 1;
+        } else {
+            kind = 0;
+            nt = ntr + (u - npair - single);
+        }
+    }
+};
+
 // Grid rows r of CTA g: r = rb + g / MT, then every (grid / MT)-th row; row tile g % MT.  Per row
-// the mode halves jh < JH, per half the N tiles: the tile sequence of all three roles.
+// the mode halves jh < JH, per half the work units: the sequence of all three roles.
+// Stage layout: U hi, U lo, B0 hi, B1 hi, B0 lo, B1 lo (B0 | B1 the 256 B rows of a unit).
 template <int NMT, int JH, bool SYM>
 __global__ void __launch_bounds__(192, 1)
     k_bfm_mixed(const __grid_constant__ CUtensorMap tmUh, const __grid_constant__ CUtensorMap tmUl,
@@ -119,7 +149,7 @@ __global__ void __launch_bounds__(192, 1)
     const int mt = blockIdx.x % p.MT;
     const int rstep = gridDim.x / p.MT;
     const int r0 = blockIdx.x / p.MT;
-    const uint32_t tx_bytes = 2u * kTileBytes + 4u * (uint32_t)(BROWS * 128);
+    const uint32_t tx_bytes = 2u * kTileBytes + 4u * (uint32_t)(BROWS * 128);  // kind 0, 1; kind 2 has 2 B tiles
 
     if (warp == 0) {
         // ---------------- TMA producer ----------------
@@ -127,29 +157,40 @@ __global__ void __launch_bounds__(192, 1)
             uint32_t it = 0;
             bool ok = true;
             for (int r = p.rb + r0; r < p.re && ok; r += rstep)
-                for (int jh = 0; jh < JH && ok; ++jh)
-                    for (int nt = 0; nt < p.n_ntiles && ok; ++nt)
+                for (int jh = 0; jh < JH && ok; ++jh) {
+                    const Units un(r, p.n_ntiles, SYM, NC);
+                    for (int u = 0; u < un.n && ok; ++u) {
+                        int kind, nt;
+                        un.at(u, kind, nt);
                         for (int kc = 0; kc < p.nk && ok; ++kc, ++it) {
                             const int s = it % kStages;
                             const uint32_t ph = (it / kStages) & 1u;
                             if (!mbar_wait(&empty[s], ph ^ 1u, err, 1)) { ok = false; break; }
                             uint8_t *st = smem + s * kStageBytes;
-                            // SYM: no D1 in this tile, so no grid-column (G) tiles to load
-                            const bool d1 = !SYM || nt * NC + NC - 1 >= r;
-                            mbar_expect_tx(&full[s], d1 ? tx_bytes : tx_bytes - 2u * (uint32_t)(BROWS * 128));
+                            mbar_expect_tx(&full[s], kind == 2 ? tx_bytes - 2u * (uint32_t)(BROWS * 128) : tx_bytes);
                             const int x = kc * kBK;
                             const int yu = r * p.Mp + mt * kBM;
                             tma_2d(st + 0 * kTileBytes, &tmUh, &full[s], x, yu);
                             tma_2d(st + 1 * kTileBytes, &tmUl, &full[s], x, yu);
-                            const int yg = jh * p.g_half + nt * BROWS;
-                            if (d1) {
+                            const int ys = jh * p.s_half + (r + nt * NC) * NMT;  // S(nt)
+                            if (kind == 0) {
+                                const int yg = jh * p.g_half + nt * BROWS;
                                 tma_2d(st + 2 * kTileBytes, &tmGh, &full[s], x, yg);
-                                tma_2d(st + 3 * kTileBytes, &tmGl, &full[s], x, yg);
+                                tma_2d(st + 4 * kTileBytes, &tmGl, &full[s], x, yg);
+                                tma_2d(st + 3 * kTileBytes, &tmSh, &full[s], x, ys);
+                                tma_2d(st + 5 * kTileBytes, &tmSl, &full[s], x, ys);
+                            } else if (kind == 1) {
+                                tma_2d(st + 2 * kTileBytes, &tmSh, &full[s], x, ys);
+                                tma_2d(st + 4 * kTileBytes, &tmSl, &full[s], x, ys);
+                                tma_2d(st + 3 * kTileBytes, &tmSh, &full[s], x, ys + BROWS);  // S(nt + 1)
+                                tma_2d(st + 5 * kTileBytes, &tmSl, &full[s], x, ys + BROWS);
+                            } else {
+                                tma_2d(st + 3 * kTileBytes, &tmSh, &full[s], x, ys);
+                                tma_2d(st + 5 * kTileBytes, &tmSl, &full[s], x, ys);
                             }
-                            const int ys = jh * p.s_half + (r + nt * NC) * NMT;
-                            tma_2d(st + 4 * kTileBytes, &tmSh, &full[s], x, ys);
-                            tma_2d(st + 5 * kTileBytes, &tmSl, &full[s], x, ys);
                         }
+                    }
+                }
             // Let the copies already issued land before the CTA can leave (bounded).
             const uint32_t last = it;
             for (uint32_t q = (last > (uint32_t)kStages ? last - kStages : 0); q < last; ++q) {
@@ -167,8 +208,11 @@ __global__ void __launch_bounds__(192, 1)
             uint32_t it = 0, tile = 0;
             bool ok = true;
             for (int r = p.rb + r0; r < p.re && ok; r += rstep)
-                for (int jh = 0; jh < JH && ok; ++jh)
-                    for (int nt = 0; nt < p.n_ntiles && ok; ++nt, ++tile) {
+                for (int jh = 0; jh < JH && ok; ++jh) {
+                    const Units un(r, p.n_ntiles, SYM, NC);
+                    for (int u = 0; u < un.n && ok; ++u, ++tile) {
+                        int kind, nt;
+                        un.at(u, kind, nt);
                         const int buf = tile & 1;
                         const uint32_t tph = (tile >> 1) & 1u;
                         if (!mbar_wait(&tempty[buf], tph ^ 1u, err, 2)) { ok = false; break; }
@@ -187,23 +231,25 @@ __global__ void __launch_bounds__(192, 1)
                                 if (ks >= nks) break;
                                 const uint32_t off = ks * 32;
                                 const uint64_t uh = sdesc(base + 0 * kTileBytes + off), ul = sdesc(base + 1 * kTileBytes + off);
-                                const uint64_t gh = sdesc(base + 2 * kTileBytes + off), gl = sdesc(base + 3 * kTileBytes + off);
-                                const uint64_t sh = sdesc(base + 4 * kTileBytes + off), sl = sdesc(base + 5 * kTileBytes + off);
                                 const uint32_t acc = (kc > 0 || ks > 0) ? 1u : 0u;
-                                if (!SYM || nt * NC + NC - 1 >= r) {  // SYM: D1 for columns c >= r only
-                                    mma(d1, uh, gh, acc);
-                                    mma(d1, uh, gl, 1u);
-                                    mma(d1, ul, gh, 1u);
+                                if (kind != 2) {  // [D1 | D3] or [D3(nt) | D3(nt + 1)]: B0 | B1, N = 256
+                                    const uint64_t bh = sdesc(base + 2 * kTileBytes + off), bl = sdesc(base + 4 * kTileBytes + off);
+                                    mma256(d1, uh, bh, acc);
+                                    mma256(d1, uh, bl, 1u);
+                                    mma256(d1, ul, bh, 1u);
+                                } else {  // D3 alone: B1, N = 128
+                                    const uint64_t bh = sdesc(base + 3 * kTileBytes + off), bl = sdesc(base + 5 * kTileBytes + off);
+                                    mma(d3, uh, bh, acc);
+                                    mma(d3, uh, bl, 1u);
+                                    mma(d3, ul, bh, 1u);
                                 }
-                                mma(d3, uh, sh, acc);
-                                mma(d3, uh, sl, 1u);
-                                mma(d3, ul, sh, 1u);
                             }
                             mma_commit(&empty[s]);  // stage free once these MMAs have read it
                         }
                         if (!ok) break;
                         mma_commit(&tfull[buf]);  // accumulators ready for the epilogue
                     }
+                }
             // Every MMA issued so far completes before TMEM is released.
             mma_commit(done);
             const uint64_t t0 = gtime();
@@ -250,36 +296,62 @@ __global__ void __launch_bounds__(192, 1)
         };
         uint32_t tile = 0;
         bool ok = true;
-        if (p.rb + r0 < p.re) epi::stage<NMT, JH>(hbs, p.Hg, p.Hs, p.nf, p.rb + r0, 0, et, 128);
+        // FRF staging of unit (r, jh, u) into slot pair hb[0..1] (the tiles the unit covers)
+        auto stage_unit = [&](HT *hb, int r, int u) {
+            const Units un(r, p.n_ntiles, SYM, NC);
+            int kind, nt;
+            un.at(u, kind, nt);
+            epi::stage<NMT, JH>(hb, p.Hg, p.Hs, p.nf, r, nt * NC, et, 128);
+            if (kind == 1) epi::stage<NMT, JH>(hb + 1, p.Hg, p.Hs, p.nf, r, (nt + 1) * NC, et, 128);
+        };
+        if (p.rb + r0 < p.re) stage_unit(hbs, p.rb + r0, 0);
+        int since = 0;  // tiles accumulated since the last flush
         for (int r = p.rb + r0; r < p.re; r += rstep) {
             const bool b1 = (r == 0 || r == p.nf - 1);
             const float wv_r = r < p.sym_rows ? 2.f * wvf : wvf;  // central symmetry: the mirror row
+            const Units un(r, p.n_ntiles, SYM, NC);
             for (int jh = 0; jh < JH; ++jh) {
                 zero();
-                for (int nt = 0; nt < p.n_ntiles; ++nt, ++tile) {
+                since = 0;
+                for (int u = 0; u < un.n; ++u, ++tile) {
+                    int kind, nt;
+                    un.at(u, kind, nt);
                     const int buf = tile & 1;
                     const uint32_t tph = (tile >> 1) & 1u;
                     epi::cp_async_wait_all();
-                    epi::epi_sync();  // this tile's values are in; the other slot is no longer read
-                    // stage the next tile's FRF values (they depend on the row and columns only)
-                    if (nt + 1 < p.n_ntiles)
-                        epi::stage<NMT, JH>(hbs + (buf ^ 1), p.Hg, p.Hs, p.nf, r, (nt + 1) * NC, et, 128);
+                    epi::epi_sync();  // this unit's values are in; the other slot pair is no longer read
+                    // stage the next unit's FRF values (they depend on the row and columns only)
+                    if (u + 1 < un.n)
+                        stage_unit(hbs + 2 * (buf ^ 1), r, u + 1);
                     else if (jh + 1 < JH)
-                        epi::stage<NMT, JH>(hbs + (buf ^ 1), p.Hg, p.Hs, p.nf, r, 0, et, 128);
+                        stage_unit(hbs + 2 * (buf ^ 1), r, 0);
                     else if (r + rstep < p.re)
-                        epi::stage<NMT, JH>(hbs + (buf ^ 1), p.Hg, p.Hs, p.nf, r + rstep, 0, et, 128);
+                        stage_unit(hbs + 2 * (buf ^ 1), r + rstep, 0);
                     if (ok) {
                         // warp-uniform outcome: tcgen05.ld below is .sync.aligned
                         ok = __all_sync(0xffffffffu, mbar_wait(&tfull[buf], tph, err, 4));
                         if (ok) {
                             fence_after();
-                            epi::tile<NMT, JH, SYM, KINDS>(hbs[buf], lane_base + buf * 256, a, b, nt * NC, p.nf,
-                                                           vect, b1, wv_r, jh, acc, r, nt * NC + NC - 1 >= r);
+                            const uint32_t ta = lane_base + buf * 256;
+                            const HT *hb = hbs + 2 * buf;
+                            if (kind == 1) {
+                                epi::tile<NMT, JH, SYM, KINDS>(hb[0], ta, a, b, nt * NC, p.nf, vect, b1, wv_r, jh, acc, r,
+                                                               false, 0u);
+                                epi::tile<NMT, JH, SYM, KINDS>(hb[1], ta, a, b, (nt + 1) * NC, p.nf, vect, b1, wv_r, jh,
+                                                               acc, r, false);
+                            } else {
+                                epi::tile<NMT, JH, SYM, KINDS>(hb[0], ta, a, b, nt * NC, p.nf, vect, b1, wv_r, jh, acc, r,
+                                                               kind == 0);
+                            }
                             fence_before();
                             mbar_arrive(&tempty[buf]);
+                            since += kind == 1 ? 2 : 1;
                             // one flush site: a second inlined copy of the flush made the
                             // compiler spill the accumulators
-                            if ((nt + 1) % kFlushTiles == 0 || nt + 1 == p.n_ntiles) flush(jh);
+                            if (since >= kFlushTiles || u + 1 == un.n) {
+                                flush(jh);
+                                since = 0;
+                            }
                         }
                     }
                 }

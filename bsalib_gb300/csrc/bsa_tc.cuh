@@ -89,6 +89,14 @@ __device__ __forceinline__ void mma(uint32_t d, uint64_t a, uint64_t b, uint32_t
         "l"(a), "l"(b), "r"(kIdesc), "r"(acc)
         : "memory");
 }
+// The same with N = 256: B is 256 K-major rows (two 128-row tiles back to back), D 256 columns.
+constexpr uint32_t kIdesc256 = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(256 >> 3) << 17) | ((uint32_t)(kBM >> 4) << 24);
+__device__ __forceinline__ void mma256(uint32_t d, uint64_t a, uint64_t b, uint32_t acc) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
+        "l"(a), "l"(b), "r"(kIdesc256), "r"(acc)
+        : "memory");
+}
 __device__ __forceinline__ void mma_commit(uint64_t *b) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(su32(b)) : "memory");
 }
