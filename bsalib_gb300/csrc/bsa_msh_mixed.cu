@@ -64,9 +64,15 @@ struct MParams {
 };
 
 // Work item w = (task, row tile, N tiles [nt0, nt1)), CTAs stride over work items; all three
-// roles walk the same (item, N tile, K chunk) sequence.  The items of one task are consecutive
-// (row tile major, one N tile each), so the CTAs running at the same time share its U row
-// blocks and its B tiles through L2 instead of each streaming them from HBM.
+// roles walk the same (item, K chunk) sequence, one TMEM buffer per item.  The items of one
+// task are consecutive (row tile major), so the CTAs running at the same time share its U row
+// blocks and its B tiles through L2 instead of each streaming them from HBM.  Stage layout:
+// U hi, U lo, B0 hi, B1 hi, B0 lo, B1 lo, the unit's 256 B rows B0 | B1 in one N = 256 MMA:
+//   kind 0 items (one N tile): B0 = G(nt), B1 = S(nt) -> [D1 | D3];
+//   kind 1 items of two N tiles: B0 = S(nt), B1 = S(nt + 1) -> [D3(nt) | D3(nt + 1)];
+//   kind 1 items of one N tile: B1 = S(nt), N = 128 into the D3 half.
+// A lone D3 tile has 12 MMAs per 64 KB stage and waits on its operands; paired it has 24 per
+// 96 KB, as a line tile.
 __global__ void __launch_bounds__(192, 1)
     k_msh_mixed(const __grid_constant__ CUtensorMap tmUh, const __grid_constant__ CUtensorMap tmUl,
                 const __grid_constant__ CUtensorMap tmGh, const __grid_constant__ CUtensorMap tmGl,
@@ -119,28 +125,36 @@ __global__ void __launch_bounds__(192, 1)
                 const int4 wi = p.items[w];
                 const Task tk = p.tasks[wi.x];
                 const int mt = wi.y;
-                const bool hg = tk.kind == 0;
-                const uint32_t tx = 2u * kTileBytes + (hg ? 4u : 2u) * (uint32_t)(p.BROWS * 128);
-                for (int nt = wi.z; nt < wi.w && ok; ++nt)
-                    for (int kc = 0; kc < p.nk && ok; ++kc, ++it) {
-                        const int s = it % kStages;
-                        const uint32_t ph = (it / kStages) & 1u;
-                        if (!mbar_wait(&empty[s], ph ^ 1u, err, 1)) { ok = false; break; }
-                        uint8_t *st = smem + s * kStageBytes;
-                        mbar_expect_tx(&full[s], tx);
-                        const int x = kc * kBK;
-                        const int yu = tk.u_row + mt * kBM;
-                        tma_2d(st + 0 * kTileBytes, &tmUh, &full[s], x, yu);
-                        tma_2d(st + 1 * kTileBytes, &tmUl, &full[s], x, yu);
-                        if (hg) {
-                            const int yg = tk.g_row + nt * p.BROWS;
-                            tma_2d(st + 2 * kTileBytes, &tmGh, &full[s], x, yg);
-                            tma_2d(st + 3 * kTileBytes, &tmGl, &full[s], x, yg);
-                        }
-                        const int ys = tk.s_row + nt * p.BROWS;
-                        tma_2d(st + 4 * kTileBytes, &tmSh, &full[s], x, ys);
+                const int nt = wi.z, cnt = wi.w - wi.z;
+                const bool wide = tk.kind == 0 || cnt == 2;  // two B tiles, N = 256
+                const uint32_t tx = 2u * kTileBytes + (wide ? 4u : 2u) * (uint32_t)(p.BROWS * 128);
+                for (int kc = 0; kc < p.nk && ok; ++kc, ++it) {
+                    const int s = it % kStages;
+                    const uint32_t ph = (it / kStages) & 1u;
+                    if (!mbar_wait(&empty[s], ph ^ 1u, err, 1)) { ok = false; break; }
+                    uint8_t *st = smem + s * kStageBytes;
+                    mbar_expect_tx(&full[s], tx);
+                    const int x = kc * kBK;
+                    const int yu = tk.u_row + mt * kBM;
+                    tma_2d(st + 0 * kTileBytes, &tmUh, &full[s], x, yu);
+                    tma_2d(st + 1 * kTileBytes, &tmUl, &full[s], x, yu);
+                    const int ys = tk.s_row + nt * p.BROWS;
+                    if (tk.kind == 0) {
+                        const int yg = tk.g_row + nt * p.BROWS;
+                        tma_2d(st + 2 * kTileBytes, &tmGh, &full[s], x, yg);
+                        tma_2d(st + 4 * kTileBytes, &tmGl, &full[s], x, yg);
+                        tma_2d(st + 3 * kTileBytes, &tmSh, &full[s], x, ys);
+                        tma_2d(st + 5 * kTileBytes, &tmSl, &full[s], x, ys);
+                    } else if (cnt == 2) {
+                        tma_2d(st + 2 * kTileBytes, &tmSh, &full[s], x, ys);
+                        tma_2d(st + 4 * kTileBytes, &tmSl, &full[s], x, ys);
+                        tma_2d(st + 3 * kTileBytes, &tmSh, &full[s], x, ys + p.BROWS);
+                        tma_2d(st + 5 * kTileBytes, &tmSl, &full[s], x, ys + p.BROWS);
+                    } else {
+                        tma_2d(st + 3 * kTileBytes, &tmSh, &full[s], x, ys);
                         tma_2d(st + 5 * kTileBytes, &tmSl, &full[s], x, ys);
                     }
+                }
             }
             // Let the copies already issued land before the CTA can leave (bounded).
             const uint32_t last = it;
@@ -161,10 +175,11 @@ __global__ void __launch_bounds__(192, 1)
             for (int w = blockIdx.x; w < nwork && ok; w += gridDim.x) {
                 const int4 wi = p.items[w];
                 const Task tk = p.tasks[wi.x];
-                const bool hg = tk.kind == 0;
-                for (int nt = wi.z; nt < wi.w && ok; ++nt, ++tile) {
+                const bool wide = tk.kind == 0 || wi.w - wi.z == 2;
+                {
                     const int buf = tile & 1;
                     const uint32_t tph = (tile >> 1) & 1u;
+                    ++tile;
                     if (!mbar_wait(&tempty[buf], tph ^ 1u, err, 2)) { ok = false; break; }
                     fence_after();
                     const uint32_t d1 = tmem + buf * 256, d3 = d1 + 128;
@@ -179,17 +194,18 @@ __global__ void __launch_bounds__(192, 1)
                         for (int ks = 0; ks < nks; ++ks) {
                             const uint32_t off = ks * 32;
                             const uint64_t uh = sdesc(base + 0 * kTileBytes + off), ul = sdesc(base + 1 * kTileBytes + off);
-                            const uint64_t sh = sdesc(base + 4 * kTileBytes + off), sl = sdesc(base + 5 * kTileBytes + off);
                             const uint32_t acc = (kc > 0 || ks > 0) ? 1u : 0u;
-                            if (hg) {
-                                const uint64_t gh = sdesc(base + 2 * kTileBytes + off), gl = sdesc(base + 3 * kTileBytes + off);
-                                mma(d1, uh, gh, acc);
-                                mma(d1, uh, gl, 1u);
-                                mma(d1, ul, gh, 1u);
+                            if (wide) {  // B0 | B1, N = 256
+                                const uint64_t bh = sdesc(base + 2 * kTileBytes + off), bl = sdesc(base + 4 * kTileBytes + off);
+                                mma256(d1, uh, bh, acc);
+                                mma256(d1, uh, bl, 1u);
+                                mma256(d1, ul, bh, 1u);
+                            } else {  // B1 alone into the D3 half
+                                const uint64_t bh = sdesc(base + 3 * kTileBytes + off), bl = sdesc(base + 5 * kTileBytes + off);
+                                mma(d3, uh, bh, acc);
+                                mma(d3, uh, bl, 1u);
+                                mma(d3, ul, bh, 1u);
                             }
-                            mma(d3, uh, sh, acc);
-                            mma(d3, uh, sl, 1u);
-                            mma(d3, ul, sh, 1u);
                         }
                         mma_commit(&empty[s]);  // stage free once these MMAs have read it
                     }
@@ -218,18 +234,22 @@ __global__ void __launch_bounds__(192, 1)
             const int mt = wi.y;
             const int grow = mt * kBM + row;  // row of U: a * nm + b
             const bool vrow = grow < nm2;
-            float *const outA = tk.kind == 0 ? p.T1 : nullptr;
+            const int cnt = wi.w - wi.z;
+            // the two accumulator halves: [T1 | T3] of one N tile (kind 0), [T2 | T2] of two
+            // N tiles, or the second half alone
+            float *const outA = tk.kind == 0 ? p.T1 : p.T2;
             float *const outB = tk.kind == 0 ? p.T3 : p.T2;
-            for (int nt = wi.z; nt < wi.w; ++nt, ++tile) {
+            {
                 const int buf = tile & 1;
                 const uint32_t tph = (tile >> 1) & 1u;
+                ++tile;
                 // warp-uniform outcome: tcgen05.ld below is .sync.aligned
                 const bool got = __all_sync(0xffffffffu, mbar_wait(&tfull[buf], tph, err, 4));
                 if (!got) { ok = false; break; }
                 fence_after();
-                const int c0 = nt * p.NC;
-                for (int acc = (tk.kind == 0 ? 0 : 1); acc < 2; ++acc) {
+                for (int acc = (tk.kind == 0 || cnt == 2 ? 0 : 1); acc < 2; ++acc) {
                     float *const out = acc == 0 ? outA : outB;
+                    const int c0 = (wi.z + (tk.kind == 1 && cnt == 2 ? acc : 0)) * p.NC;
                     for (int q = 0; q < kBN / 32; ++q) {
                         uint32_t v[32];
                         tmem_ld32(lane_base + buf * 256 + acc * 128 + q * 32, v);
@@ -863,12 +883,13 @@ int Engine::msh_mixed_batch(const std::vector<ZoneDev> &zs, std::vector<double> 
     const int nm3p = (nm3 + 3) & ~3, hs = frf_row(nm);
     const size_t tel = (size_t)npts * nm3p;
     const size_t nidx = (size_t)nU + ncol + 2 * (size_t)npts;
-    // work items: per task, its row tiles x N tiles, one N tile each, consecutive
+    // work items: per task, its row tiles x N tiles (one, or two for column tasks), consecutive
     std::vector<int4> witems;
     for (size_t t = 0; t < tasks.size(); ++t) {
         const int ntl = (tasks[t].ncols + NC - 1) / NC;
+        const int step = tasks[t].kind == 1 ? 2 : 1;  // column tasks: two N tiles per item
         for (int mt = 0; mt < MT; ++mt)
-            for (int nt = 0; nt < ntl; ++nt) witems.push_back(make_int4((int)t, mt, nt, nt + 1));
+            for (int nt = 0; nt < ntl; nt += step) witems.push_back(make_int4((int)t, mt, nt, std::min(nt + step, ntl)));
     }
     if (witems.size() > (size_t)0x7fffffff) return fail(BSA_ERR_ARG, "too many Mesher work items");
     int dev = 0, nsm = 0;
