@@ -314,8 +314,8 @@ struct BatchCase {
     int nnl = 0, psd_type = 0, nme = 0, K = 0;
     bool trunc = true;
     std::vector<int> modes;
-    std::vector<double> hL, hQ, hLogc, hM, hK, hC, hWd3, hWd2;
-    std::vector<float> hLogc32, hL32;
+    std::vector<double> hL, hQ, hCoh, hM, hK, hC, hWd3, hWd2;
+    std::vector<float> hL32;
     std::vector<PsdNode> hPsd;
     std::vector<double> f;  // Classic grid
 };
@@ -338,8 +338,8 @@ int Engine::batch_add(int *id) {
     c.K = K;
     c.trunc = classic_trunc;
     c.modes = modes;
-    c.hL = hL; c.hQ = hQ; c.hLogc = hLogc; c.hM = hM; c.hK = hK; c.hC = hC; c.hWd3 = hWd3; c.hWd2 = hWd2;
-    c.hLogc32 = hLogc32; c.hL32 = hL32; c.hPsd = hPsd;
+    c.hL = hL; c.hQ = hQ; c.hCoh = hCoh; c.hM = hM; c.hK = hK; c.hC = hC; c.hWd3 = hWd3; c.hWd2 = hWd2;
+    c.hL32 = hL32; c.hPsd = hPsd;
     g_batch.push_back(std::move(c));
     if (id) *id = (int)g_batch.size() - 1;
     return BSA_OK;
@@ -355,8 +355,8 @@ void Engine::batch_install(const BatchCase &c) {
     nme = c.nme;
     K = c.K;
     modes = c.modes;
-    hL = c.hL; hQ = c.hQ; hLogc = c.hLogc; hM = c.hM; hK = c.hK; hC = c.hC; hWd3 = c.hWd3; hWd2 = c.hWd2;
-    hLogc32 = c.hLogc32; hL32 = c.hL32; hPsd = c.hPsd;
+    hL = c.hL; hQ = c.hQ; hCoh = c.hCoh; hM = c.hM; hK = c.hK; hC = c.hC; hWd3 = c.hWd3; hWd2 = c.hWd2;
+    hL32 = c.hL32; hPsd = c.hPsd;
     derived_ok = true;
     dev_uploaded = false;
 }
@@ -399,8 +399,8 @@ int Engine::batch_run(double *m3mf, double *m3mr, double *m2mr, double *case_ms,
     saved.K = K;
     saved.trunc = classic_trunc;
     saved.modes = modes;
-    saved.hL = hL; saved.hQ = hQ; saved.hLogc = hLogc; saved.hM = hM; saved.hK = hK; saved.hC = hC;
-    saved.hWd3 = hWd3; saved.hWd2 = hWd2; saved.hLogc32 = hLogc32; saved.hL32 = hL32; saved.hPsd = hPsd;
+    saved.hL = hL; saved.hQ = hQ; saved.hCoh = hCoh; saved.hM = hM; saved.hK = hK; saved.hC = hC;
+    saved.hWd3 = hWd3; saved.hWd2 = hWd2; saved.hL32 = hL32; saved.hPsd = hPsd;
     const Inputs saved_in = in;
     const bool saved_ok = derived_ok;
     struct Restore {

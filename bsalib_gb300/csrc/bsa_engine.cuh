@@ -12,6 +12,9 @@
 namespace bsa {
 
 // Device buffer that only grows (kept across runs; freed by bsa_Finalise).
+// Frees the device blocks the engine keeps for reuse after bsa_Finalise.
+void release_device_cache();
+
 struct DevBuf {
     void *p = nullptr;
     size_t bytes = 0;
@@ -88,9 +91,10 @@ struct Engine {
     // derived (validate)
     std::vector<int> modes;
     int nme = 0, K = 0;
-    std::vector<double> phitc, hL, hQ, hLogc, hM, hK, hC;
+    std::vector<double> phitc, hL, hQ, hM, hK, hC;
+    std::vector<double> hCoh;          // coherence bases c_ij [comp][i][j]; log c formed on the device
     std::vector<double> hWd3, hWd2;  // diagonal-only weights Q L^2 and L^2, [k][m]
-    std::vector<float> hLogc32, hL32;  // FP32 copies for the split-precision A(f) table
+    std::vector<float> hL32;         // FP32 copy of L for the split-precision A(f) table
     std::vector<PsdNode> hPsd;
 
     // device

@@ -8,6 +8,8 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -41,8 +43,45 @@ int Engine::cuda_fail(cudaError_t e, const char *what) {
                 cudaGetErrorString(e));
 }
 
+// Device blocks released by the engine are kept for the next request of a similar size
+// (bsa_Init ... bsa_Finalise cycles would otherwise pay cudaMalloc / cudaFree of the operand
+// tables every analysis).  Blocks are 2 MB multiples; a request takes the smallest cached block
+// that holds it and is at most twice its size.  At most a quarter of the device memory stays
+// cached; a failed cudaMalloc frees the cache and retries; bsa_gpu_releaseDeviceCache frees it.
+// The engine's work is ordered on its one stream, and released blocks are handed out again only
+// to later work of that stream (bsa_Finalise synchronises it before releasing).
+namespace {
+struct BlockCache {
+    std::mutex m;
+    std::multimap<size_t, void *> blocks;
+    size_t cached = 0, limit = 0;
+    void flush() {
+        for (auto &b : blocks) cudaFree(b.second);
+        blocks.clear();
+        cached = 0;
+    }
+};
+BlockCache &cache() {
+    static BlockCache c;
+    return c;
+}
+}  // namespace
+
 void DevBuf::release() {
-    if (p) cudaFree(p);
+    if (p) {
+        BlockCache &c = cache();
+        std::lock_guard<std::mutex> lk(c.m);
+        if (c.limit == 0) {
+            size_t fr = 0, tot = 0;
+            c.limit = cudaMemGetInfo(&fr, &tot) == cudaSuccess ? tot / 4 : (size_t)1 << 30;
+        }
+        if (c.cached + bytes <= c.limit) {
+            c.blocks.emplace(bytes, p);
+            c.cached += bytes;
+        } else {
+            cudaFree(p);
+        }
+    }
     p = nullptr;
     bytes = 0;
 }
@@ -51,10 +90,37 @@ cudaError_t DevBuf::reserve(size_t nbytes) {
     if (nbytes <= bytes && p) return cudaSuccess;
     release();
     if (nbytes == 0) return cudaSuccess;
-    cudaError_t e = cudaMalloc(&p, nbytes);
-    if (e == cudaSuccess) bytes = nbytes;
+    const size_t want = (nbytes + ((size_t)2 << 20) - 1) & ~(((size_t)2 << 20) - 1);
+    BlockCache &c = cache();
+    {
+        std::lock_guard<std::mutex> lk(c.m);
+        auto it = c.blocks.lower_bound(want);
+        if (it != c.blocks.end() && it->first <= 2 * want) {
+            p = it->second;
+            bytes = it->first;
+            c.cached -= bytes;
+            c.blocks.erase(it);
+            return cudaSuccess;
+        }
+    }
+    cudaError_t e = cudaMalloc(&p, want);
+    if (e == cudaErrorMemoryAllocation) {
+        cudaGetLastError();
+        {
+            std::lock_guard<std::mutex> lk(c.m);
+            c.flush();
+        }
+        e = cudaMalloc(&p, want);
+    }
+    if (e == cudaSuccess) bytes = want;
     else p = nullptr;
     return e;
+}
+
+void release_device_cache() {
+    BlockCache &c = cache();
+    std::lock_guard<std::mutex> lk(c.m);
+    c.flush();
 }
 
 void Engine::reset_inputs() {
@@ -80,6 +146,7 @@ void Engine::reset_inputs() {
 }
 
 void Engine::free_device() {
+    if (stream) cudaStreamSynchronize(stream);  // the blocks go back to the cache for reuse
     for (DevBuf *b : {&dL, &dQ, &dLogc, &dPsdPar, &dFrfM, &dFrfK, &dFrfC, &dFreq, &dS, &dA, &dPartF, &dPartR,
                       &dOut, &dPsdF, &dWf, &dPts, &dPtsD, &dBF, &dBR, &dMixA, &dMixB, &dMixH, &dMixPart, &dA32,
                       &dZones, &dZidx, &dWd3, &dWd2, &dMshT, &dMshIdx, &dLogc32, &dL32, &dPod, &dFlag})
@@ -210,15 +277,14 @@ int Engine::validate() {
         hWd2[x] = hL[x] * hL[x];
     }
     const long ncorr = (long)I.ncorr;
-    hLogc.assign((size_t)ntc * nnl * nnl, 0.0);
+    hCoh.assign((size_t)ntc * nnl * nnl, 0.0);
     for (int itc = 0; itc < ntc; ++itc)
         for (int i = 0; i < nnl; ++i)
             for (int j = 0; j < nnl; ++j) {
                 const long id = corr_index(I.n_load[i], I.n_load[j], I.nn);
                 const double c = I.corr[(size_t)(id - 1) + (size_t)ncorr * (set.tc[itc] - 1)];
-                hLogc[((size_t)itc * nnl + i) * nnl + j] = std::log(c);
+                hCoh[((size_t)itc * nnl + i) * nnl + j] = c;
             }
-    hLogc32.assign(hLogc.begin(), hLogc.end());
     hL32.assign(hL.begin(), hL.end());
     const int idir = set.dirs.empty() ? 1 : set.dirs[0];
     hPsd.assign((size_t)ntc * nnl, PsdNode{});
@@ -256,11 +322,15 @@ int Engine::upload_problem() {
     if ((rc = ensure_stream())) return rc;
     if (dev_uploaded) return BSA_OK;
     cudaError_t e;
-    if ((e = upload(dL, hL, stream)) || (e = upload(dQ, hQ, stream)) || (e = upload(dLogc, hLogc, stream)) ||
+    if ((e = upload(dL, hL, stream)) || (e = upload(dQ, hQ, stream)) || (e = upload(dLogc, hCoh, stream)) ||
         (e = upload(dPsdPar, hPsd, stream)) || (e = upload(dFrfM, hM, stream)) || (e = upload(dFrfK, hK, stream)) ||
         (e = upload(dFrfC, hC, stream)) || (e = upload(dWd3, hWd3, stream)) || (e = upload(dWd2, hWd2, stream)) ||
-        (e = upload(dLogc32, hLogc32, stream)) || (e = upload(dL32, hL32, stream)))
+        (e = upload(dL32, hL32, stream)) || (e = dLogc32.reserve(sizeof(float) * hCoh.size())))
         return cuda_fail(e, "uploading problem data");
+    // log c in place (FP64) and its FP32 copy
+    if ((e = launch_log_coh(stream, hCoh.size(), dLogc.as<double>(), dLogc32.as<float>())))
+        return cuda_fail(e, "coherence table");
+    kernels += 1;
     dev_uploaded = true;
     return BSA_OK;
 }
@@ -994,6 +1064,11 @@ int bsa_gpu_getStats(bsa_gpu_stats *st) {
     st->d2h_bytes = eng().d2h;
     st->kernels = eng().kernels;
     st->precision = eng().precision;
+    return BSA_OK;
+}
+
+int bsa_gpu_releaseDeviceCache(void) {
+    bsa::release_device_cache();
     return BSA_OK;
 }
 

@@ -138,6 +138,20 @@ __global__ __launch_bounds__(256) void k_atable(int nf, const double *__restrict
     }
 }
 
+__global__ void k_log_coh(size_t n, double *__restrict__ lc, float *__restrict__ lc32) {
+    const size_t x = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= n) return;
+    const double v = log(lc[x]);
+    lc[x] = v;
+    lc32[x] = (float)v;
+}
+
+cudaError_t launch_log_coh(cudaStream_t st, size_t n, double *lc, float *lc32) {
+    if (n == 0) return cudaSuccess;
+    k_log_coh<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, lc, lc32);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_atable(cudaStream_t st, int nf, const double *f, int ntc, int nnl, int nm,
                           const double *logc, const double *S, const double *L, double *A) {
     if (nf == 0) return cudaSuccess;

@@ -10,6 +10,9 @@ cudaError_t launch_nodal_psd(cudaStream_t st, int nf, const double *f, int ntc, 
                              int nnl, const PsdNode *par, int psd_type, int scaling, double *S);
 
 // A[f][k][m] = sqrt(S_i(f)) sum_j c_ij^|f| sqrt(S_j(f)) L[(itc,j)][m]  (FP64).
+// lc[x] = log(lc[x]) in place (FP64) and lc32[x] = (float)lc[x]: the coherence table log c.
+cudaError_t launch_log_coh(cudaStream_t st, size_t n, double *lc, float *lc32);
+
 cudaError_t launch_atable(cudaStream_t st, int nf, const double *f, int ntc, int nnl, int nm,
                           const double *logc, const double *S, const double *L, double *A);
 

@@ -350,6 +350,12 @@ typedef struct {
 } bsa_gpu_stats;
 int bsa_gpu_getStats(bsa_gpu_stats *st);
 
+/* Device memory.  Blocks the library releases (bsa_Finalise, buffer growth) are kept for reuse
+ * by the next analysis, up to a quarter of the device memory, so repeated bsa_Init ...
+ * bsa_Finalise cycles do not pay cudaMalloc / cudaFree of the operand tables each time.  This
+ * frees them (no reference counterpart: the reference holds no device memory). */
+int bsa_gpu_releaseDeviceCache(void);
+
 #ifdef __cplusplus
 }
 #endif
