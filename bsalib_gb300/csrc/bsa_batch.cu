@@ -34,10 +34,10 @@ using namespace tc;
 
 constexpr int kStages = 2;
 constexpr int kStageBytes = 6 * kTileBytes;
-constexpr int kKinds = 5;  // mr1, mr3, mr2, mf1, mf23
+constexpr int kKinds = 5;  // mr1, mr3, mr2, mf1, mf23 (+ mr1T, mf1T with SYM)
 constexpr int kFlushTiles = 64;
 constexpr int kBarBytes = 256;                              // mbarriers + TMEM slot
-constexpr int kHBytes = 2 * (int)sizeof(epi::HTile<32, 2>);  // FRF staging, 2 tiles (largest form)
+constexpr int kHBytes = 4 * (int)sizeof(epi::HTile<32, 2>);  // FRF staging, 2 x 2 tiles (largest form)
 constexpr size_t kSmem = (size_t)kStages * kStageBytes + 1024 + kBarBytes + kHBytes;
 
 struct CaseP {
@@ -47,7 +47,7 @@ struct CaseP {
     int g_row0;       // first G-table row
     int s_row0;       // first S-table row
     int hg0, hs0;     // first FRF-table entries (float2)
-    long long part0;  // first accumulator (double) of the case: [kKinds][NMT][Mp]
+    long long part0;  // first accumulator (double) of the case: [KINDS][NMT][Mp]
     unsigned nitems;  // work items of the case
 };
 
@@ -67,9 +67,35 @@ struct BParams {
     int *err;
 };
 
+// Work units of one (grid row r, mode half), as in the single-analysis kernel (bsa_mixed.cu):
+// kind 0 one N tile with [D1 | D3] (N = 256), kind 1 two N tiles without D1 (symmetric D1) with
+// [D3(nt) | D3(nt + 1)], kind 2 one N tile without D1 (D3 alone, N = 128).
+struct Units {
+    int ntr, npair, single, n;
+    __device__ __forceinline__ Units(int r, int ntl, bool sym, int NC) {
+        ntr = sym ? min(ntl, r / NC) : 0;
+        npair = ntr >> 1;
+        single = ntr & 1;
+        n = npair + single + (ntl - ntr);
+    }
+    __device__ __forceinline__ void at(int u, int &kind, int &nt) const {
+        if (u < npair) {
+            kind = 1;
+            nt = 2 * u;
+        } else if (u < npair + single) {
+            kind = 2;
+            nt = ntr - 1;
+        } else {
+            kind = 0;
+            nt = ntr + (u - npair - single);
+        }
+    }
+};
+
 // Items w = blockIdx.x, blockIdx.x + gridDim.x, ...; per item the mode halves jh < JH, per half
-// the case's N tiles: the tile sequence of all three roles.
-template <int NMT, int JH>
+// the row's work units: the sequence of all three roles.  Stage layout: U hi, U lo, B0 hi, B1
+// hi, B0 lo, B1 lo.  SYM (every case a whole grid, at most 24 kept modes): symmetric D1.
+template <int NMT, int JH, bool SYM>
 __global__ void __launch_bounds__(192, 1)
     k_bfm_batch(const __grid_constant__ CUtensorMap tmUh, const __grid_constant__ CUtensorMap tmUl,
                 const __grid_constant__ CUtensorMap tmGh, const __grid_constant__ CUtensorMap tmGl,
@@ -77,6 +103,7 @@ __global__ void __launch_bounds__(192, 1)
     constexpr int NC = kBN / NMT;
     constexpr int BROWS = NC * NMT;
     constexpr int W = NMT * JH;
+    constexpr int KINDS = SYM ? kKinds + 2 : kKinds;
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint64_t *bars = (uint64_t *)(smem + kStages * kStageBytes);
@@ -124,25 +151,39 @@ __global__ void __launch_bounds__(192, 1)
             for (int w = blockIdx.x; w < p.nitems && ok; w += gridDim.x) {
                 const BItem im = p.items[w];
                 const CaseP cs = p.cases[im.c];
+                const Units un(im.r, cs.n_ntiles, SYM, NC);
                 for (int jh = 0; jh < JH && ok; ++jh)
-                    for (int nt = 0; nt < cs.n_ntiles && ok; ++nt)
+                    for (int u = 0; u < un.n && ok; ++u) {
+                        int kind, nt;
+                        un.at(u, kind, nt);
                         for (int kc = 0; kc < cs.nk && ok; ++kc, ++it) {
                             const int s = it % kStages;
                             const uint32_t ph = (it / kStages) & 1u;
                             if (!mbar_wait(&empty[s], ph ^ 1u, err, 1)) { ok = false; break; }
                             uint8_t *st = smem + s * kStageBytes;
-                            mbar_expect_tx(&full[s], tx_bytes);
+                            mbar_expect_tx(&full[s], kind == 2 ? tx_bytes - 2u * (uint32_t)(BROWS * 128) : tx_bytes);
                             const int x = kc * kBK;
                             const int yu = cs.u_row0 + im.r * cs.Mp + im.mt * kBM;
                             tma_2d(st + 0 * kTileBytes, &tmUh, &full[s], x, yu);
                             tma_2d(st + 1 * kTileBytes, &tmUl, &full[s], x, yu);
-                            const int yg = cs.g_row0 + jh * cs.nf * NMT + nt * BROWS;
-                            tma_2d(st + 2 * kTileBytes, &tmGh, &full[s], x, yg);
-                            tma_2d(st + 3 * kTileBytes, &tmGl, &full[s], x, yg);
                             const int ys = cs.s_row0 + jh * (2 * cs.nf - 1) * NMT + (im.r + nt * NC) * NMT;
-                            tma_2d(st + 4 * kTileBytes, &tmSh, &full[s], x, ys);
-                            tma_2d(st + 5 * kTileBytes, &tmSl, &full[s], x, ys);
+                            if (kind == 0) {
+                                const int yg = cs.g_row0 + jh * cs.nf * NMT + nt * BROWS;
+                                tma_2d(st + 2 * kTileBytes, &tmGh, &full[s], x, yg);
+                                tma_2d(st + 4 * kTileBytes, &tmGl, &full[s], x, yg);
+                                tma_2d(st + 3 * kTileBytes, &tmSh, &full[s], x, ys);
+                                tma_2d(st + 5 * kTileBytes, &tmSl, &full[s], x, ys);
+                            } else if (kind == 1) {
+                                tma_2d(st + 2 * kTileBytes, &tmSh, &full[s], x, ys);
+                                tma_2d(st + 4 * kTileBytes, &tmSl, &full[s], x, ys);
+                                tma_2d(st + 3 * kTileBytes, &tmSh, &full[s], x, ys + BROWS);
+                                tma_2d(st + 5 * kTileBytes, &tmSl, &full[s], x, ys + BROWS);
+                            } else {
+                                tma_2d(st + 3 * kTileBytes, &tmSh, &full[s], x, ys);
+                                tma_2d(st + 5 * kTileBytes, &tmSl, &full[s], x, ys);
+                            }
                         }
+                    }
             }
             const uint32_t last = it;
             for (uint32_t q = (last > (uint32_t)kStages ? last - kStages : 0); q < last; ++q) {
@@ -160,9 +201,13 @@ __global__ void __launch_bounds__(192, 1)
             uint32_t it = 0, tile = 0;
             bool ok = true;
             for (int w = blockIdx.x; w < p.nitems && ok; w += gridDim.x) {
-                const CaseP cs = p.cases[p.items[w].c];
+                const BItem im = p.items[w];
+                const CaseP cs = p.cases[im.c];
+                const Units un(im.r, cs.n_ntiles, SYM, NC);
                 for (int jh = 0; jh < JH && ok; ++jh)
-                    for (int nt = 0; nt < cs.n_ntiles && ok; ++nt, ++tile) {
+                    for (int u = 0; u < un.n && ok; ++u, ++tile) {
+                        int kind, nt;
+                        un.at(u, kind, nt);
                         const int buf = tile & 1;
                         const uint32_t tph = (tile >> 1) & 1u;
                         if (!mbar_wait(&tempty[buf], tph ^ 1u, err, 2)) { ok = false; break; }
@@ -178,15 +223,18 @@ __global__ void __launch_bounds__(192, 1)
                             for (int ks = 0; ks < nks; ++ks) {
                                 const uint32_t off = ks * 32;
                                 const uint64_t uh = sdesc(base + 0 * kTileBytes + off), ul = sdesc(base + 1 * kTileBytes + off);
-                                const uint64_t gh = sdesc(base + 2 * kTileBytes + off), gl = sdesc(base + 3 * kTileBytes + off);
-                                const uint64_t sh = sdesc(base + 4 * kTileBytes + off), sl = sdesc(base + 5 * kTileBytes + off);
                                 const uint32_t acc = (kc > 0 || ks > 0) ? 1u : 0u;
-                                mma(d1, uh, gh, acc);
-                                mma(d1, uh, gl, 1u);
-                                mma(d1, ul, gh, 1u);
-                                mma(d3, uh, sh, acc);
-                                mma(d3, uh, sl, 1u);
-                                mma(d3, ul, sh, 1u);
+                                if (kind != 2) {  // B0 | B1, N = 256
+                                    const uint64_t bh = sdesc(base + 2 * kTileBytes + off), bl = sdesc(base + 4 * kTileBytes + off);
+                                    mma256(d1, uh, bh, acc);
+                                    mma256(d1, uh, bl, 1u);
+                                    mma256(d1, ul, bh, 1u);
+                                } else {  // D3 alone: B1, N = 128
+                                    const uint64_t bh = sdesc(base + 3 * kTileBytes + off), bl = sdesc(base + 5 * kTileBytes + off);
+                                    mma(d3, uh, bh, acc);
+                                    mma(d3, uh, bl, 1u);
+                                    mma(d3, ul, bh, 1u);
+                                }
                             }
                             mma_commit(&empty[s]);
                         }
@@ -211,13 +259,20 @@ __global__ void __launch_bounds__(192, 1)
         const uint32_t lane_base = tmem + ((uint32_t)(quarter * 32) << 16);
         using HT = epi::HTile<NMT, JH>;
         HT *hbs = (HT *)(smem + kStages * kStageBytes + kBarBytes);
-        float acc[kKinds][NMT];
+        float acc[KINDS][NMT];
         uint32_t tile = 0;
         bool ok = true;
+        // FRF staging of unit u of row r of a case into the slot pair hb[0..1]
+        auto stage_unit = [&](HT *hb, const CaseP &c, int r, int u) {
+            const Units un(r, c.n_ntiles, SYM, NC);
+            int kind, nt;
+            un.at(u, kind, nt);
+            epi::stage<NMT, JH>(hb, p.Hg + c.hg0, p.Hs + c.hs0, c.nf, r, nt * NC, et, 128);
+            if (kind == 1) epi::stage<NMT, JH>(hb + 1, p.Hg + c.hg0, p.Hs + c.hs0, c.nf, r, (nt + 1) * NC, et, 128);
+        };
         if (blockIdx.x < p.nitems) {
             const BItem i0 = p.items[blockIdx.x];
-            const CaseP s0 = p.cases[i0.c];
-            epi::stage<NMT, JH>(hbs, p.Hg + s0.hg0, p.Hs + s0.hs0, s0.nf, i0.r, 0, et, 128);
+            stage_unit(hbs, p.cases[i0.c], i0.r, 0);
         }
         for (int w = blockIdx.x; w < p.nitems; w += gridDim.x) {
             const BItem im = p.items[w];
@@ -226,47 +281,61 @@ __global__ void __launch_bounds__(192, 1)
             const int grow = im.mt * kBM + row;
             const bool vrow = grow < cs.nm * cs.nm;
             const int a = vrow ? grow / cs.nm : 0, b = vrow ? grow % cs.nm : 0;
-            const float2 *Hg = p.Hg + cs.hg0, *Hs = p.Hs + cs.hs0;
             const float wvf = (float)cs.wval;
             const bool vect = cs.wmode == kWeightClassicVect, b1 = (r == 0 || r == cs.nf - 1);
             double *part = p.part + cs.part0 + grow;
+            const Units un(r, cs.n_ntiles, SYM, NC);
             for (int jh = 0; jh < JH; ++jh) {
 #pragma unroll
-                for (int k = 0; k < kKinds; ++k)
+                for (int k = 0; k < KINDS; ++k)
 #pragma unroll
                     for (int j = 0; j < NMT; ++j) acc[k][j] = 0.f;
-                for (int nt = 0; nt < cs.n_ntiles; ++nt, ++tile) {
+                int since = 0;  // tiles accumulated since the last flush
+                for (int u = 0; u < un.n; ++u, ++tile) {
+                    int kind, nt;
+                    un.at(u, kind, nt);
                     const int buf = tile & 1;
                     const uint32_t tph = (tile >> 1) & 1u;
                     epi::cp_async_wait_all();
-                    epi::epi_sync();  // this tile's values are in; the other slot is no longer read
-                    // stage the next tile: this half's next one, this item's next half, or the
-                    // first tile of the CTA's next item
-                    if (nt + 1 < cs.n_ntiles) {
-                        epi::stage<NMT, JH>(hbs + (buf ^ 1), Hg, Hs, cs.nf, r, (nt + 1) * NC, et, 128);
+                    epi::epi_sync();  // this unit's values are in; the other slot pair is no longer read
+                    // stage the next unit: this half's next one, this item's next half, or the
+                    // first unit of the CTA's next item
+                    if (u + 1 < un.n) {
+                        stage_unit(hbs + 2 * (buf ^ 1), cs, r, u + 1);
                     } else if (jh + 1 < JH) {
-                        epi::stage<NMT, JH>(hbs + (buf ^ 1), Hg, Hs, cs.nf, r, 0, et, 128);
+                        stage_unit(hbs + 2 * (buf ^ 1), cs, r, 0);
                     } else if (w + (int)gridDim.x < p.nitems) {
                         const BItem in = p.items[w + gridDim.x];
-                        const CaseP sn = p.cases[in.c];
-                        epi::stage<NMT, JH>(hbs + (buf ^ 1), p.Hg + sn.hg0, p.Hs + sn.hs0, sn.nf, in.r, 0, et, 128);
+                        stage_unit(hbs + 2 * (buf ^ 1), p.cases[in.c], in.r, 0);
                     }
                     if (!ok) continue;
                     ok = __all_sync(0xffffffffu, mbar_wait(&tfull[buf], tph, err, 4));
                     if (!ok) continue;
                     fence_after();
-                    epi::tile<NMT, JH>(hbs[buf], lane_base + buf * 256, a, b, nt * NC, cs.nf, vect, b1, wvf, jh, acc);
+                    const uint32_t ta = lane_base + buf * 256;
+                    const HT *hb = hbs + 2 * buf;
+                    if (kind == 1) {
+                        epi::tile<NMT, JH, SYM, KINDS>(hb[0], ta, a, b, nt * NC, cs.nf, vect, b1, wvf, jh, acc, r, false,
+                                                       0u);
+                        epi::tile<NMT, JH, SYM, KINDS>(hb[1], ta, a, b, (nt + 1) * NC, cs.nf, vect, b1, wvf, jh, acc, r,
+                                                       false);
+                    } else {
+                        epi::tile<NMT, JH, SYM, KINDS>(hb[0], ta, a, b, nt * NC, cs.nf, vect, b1, wvf, jh, acc, r,
+                                                       kind == 0);
+                    }
                     fence_before();
                     mbar_arrive(&tempty[buf]);
-                    if (((nt + 1) % kFlushTiles == 0 || nt + 1 == cs.n_ntiles) && vrow) {
+                    since += kind == 1 ? 2 : 1;
+                    if ((since >= kFlushTiles || u + 1 == un.n) && vrow) {
 #pragma unroll
-                        for (int k = 0; k < kKinds; ++k)
+                        for (int k = 0; k < KINDS; ++k)
 #pragma unroll
                             for (int j = 0; j < NMT; ++j) {
                                 if (acc[k][j] != 0.f)
                                     atomicAdd(part + (size_t)(k * W + jh * NMT + j) * cs.Mp, (double)acc[k][j]);
                                 acc[k][j] = 0.f;
                             }
+                        since = 0;
                     }
                 }
             }
@@ -288,7 +357,7 @@ __global__ void __launch_bounds__(192, 1)
 }
 
 // m3 of case c at out + out_off[c]: [m + nm n + nm^2 o] = 2 (T1 at (m,n,o) + T3 at (o,n,m) + T2 at (n,o,m))
-template <int NMT>
+template <int NMT, int KINDS>
 __global__ void k_batch_reduce(const CaseP *__restrict__ cases, const long long *__restrict__ out_off,
                                const double *__restrict__ part, double *__restrict__ m3mf, double *__restrict__ m3mr) {
     const CaseP cs = cases[blockIdx.y];
@@ -298,8 +367,12 @@ __global__ void k_batch_reduce(const CaseP *__restrict__ cases, const long long 
     const int m = x % nm, n = (x / nm) % nm, o = x / (nm * nm);
     const double *pc = part + cs.part0;
     auto s = [&](int kind, int aa, int bb, int j) { return pc[(size_t)(kind * NMT + j) * cs.Mp + aa * nm + bb]; };
-    const double mr = s(0, m, n, o) + s(1, o, n, m) + s(2, n, o, m);
-    const double mf = s(3, m, n, o) + s(4, o, n, m) + s(4, n, o, m);
+    double mr = s(0, m, n, o) + s(1, o, n, m) + s(2, n, o, m);
+    double mf = s(3, m, n, o) + s(4, o, n, m) + s(4, n, o, m);
+    if (KINDS > kKinds) {  // symmetric D1: term 1 of the mirrored points
+        mr += s(5, m, o, n);
+        mf += s(6, m, o, n);
+    }
     m3mr[out_off[blockIdx.y] + x] = 2.0 * mr;
     m3mf[out_off[blockIdx.y] + x] = 2.0 * mf;
 }
@@ -471,7 +544,7 @@ int Engine::batch_run(double *m3mf, double *m3mr, double *m2mr, double *case_ms,
             srows += (long long)JH * (2 * nf - 1) * NMT;
             hg += (long long)nf * Wd;
             hs += (long long)(2 * nf - 1) * Wd;
-            parts += (long long)kKinds * Wd * q.Mp;
+            parts += (long long)(Wd <= 24 ? kKinds + 2 : kKinds) * Wd * q.Mp;
             for (int r = 0; r < nf; ++r)
                 for (int mt = 0; mt < q.MT; ++mt) items.push_back(BItem{(int)(k - g0), r, mt, 0});
         }
@@ -564,11 +637,11 @@ int Engine::batch_run(double *m3mf, double *m3mr, double *m2mr, double *case_ms,
             kern<<<grid, 192, smem, stream>>>(maps[0], maps[1], maps[2], maps[3], maps[4], maps[5], prm);
         };
         switch (Wd) {
-        case 8: launch(k_bfm_batch<8, 1>); break;
-        case 16: launch(k_bfm_batch<16, 1>); break;
-        case 24: launch(k_bfm_batch<24, 1>); break;
-        case 32: launch(k_bfm_batch<32, 1>); break;
-        default: launch(k_bfm_batch<32, 2>); break;
+        case 8: launch(k_bfm_batch<8, 1, true>); break;
+        case 16: launch(k_bfm_batch<16, 1, true>); break;
+        case 24: launch(k_bfm_batch<24, 1, true>); break;
+        case 32: launch(k_bfm_batch<32, 1, false>); break;
+        default: launch(k_bfm_batch<32, 2, false>); break;
         }
         if ((e = cudaGetLastError())) return cuda_fail(e, "batched tcgen05 contraction kernel");
         if ((e = cudaEventRecord(evg1, stream))) return cuda_fail(e, "event");
@@ -579,11 +652,11 @@ int Engine::batch_run(double *m3mf, double *m3mr, double *m2mr, double *case_ms,
         for (const CaseP &q : cp) maxnm3 = std::max(maxnm3, q.nm * q.nm * q.nm);
         dim3 rg((maxnm3 + 127) / 128, (unsigned)cp.size());
         switch (Wd) {
-        case 8: k_batch_reduce<8><<<rg, 128, 0, stream>>>(d_cases, d_off, part, o, o + t3); break;
-        case 16: k_batch_reduce<16><<<rg, 128, 0, stream>>>(d_cases, d_off, part, o, o + t3); break;
-        case 24: k_batch_reduce<24><<<rg, 128, 0, stream>>>(d_cases, d_off, part, o, o + t3); break;
-        case 32: k_batch_reduce<32><<<rg, 128, 0, stream>>>(d_cases, d_off, part, o, o + t3); break;
-        default: k_batch_reduce<64><<<rg, 128, 0, stream>>>(d_cases, d_off, part, o, o + t3); break;
+        case 8: k_batch_reduce<8, kKinds + 2><<<rg, 128, 0, stream>>>(d_cases, d_off, part, o, o + t3); break;
+        case 16: k_batch_reduce<16, kKinds + 2><<<rg, 128, 0, stream>>>(d_cases, d_off, part, o, o + t3); break;
+        case 24: k_batch_reduce<24, kKinds + 2><<<rg, 128, 0, stream>>>(d_cases, d_off, part, o, o + t3); break;
+        case 32: k_batch_reduce<32, kKinds><<<rg, 128, 0, stream>>>(d_cases, d_off, part, o, o + t3); break;
+        default: k_batch_reduce<64, kKinds><<<rg, 128, 0, stream>>>(d_cases, d_off, part, o, o + t3); break;
         }
         if ((e = cudaGetLastError())) return cuda_fail(e, "batch reduction");
         kernels += 2;
