@@ -6,11 +6,13 @@
  * against it.  Nothing in the product links or calls this file: only the tests, the
  * smoke check and the CPU-baseline leg of the benchmark load it.
  *
- * Parity status: the reference is modern Fortran and cannot be built in this environment
- * (no Fortran compiler, no LAPACK), and it ships no tests or golden vectors.  This oracle
- * is therefore cross-checked by an independent numpy direct-sum restatement on small
- * cases (tests/golden/make_golden.py) -- parity against the reference binary itself is
- * UNPINNED.
+ * Parity status: the reference's Fortran cannot be built in this environment (no Fortran
+ * compiler, no LAPACK) and ships no tests or golden vectors.  Its GPU offload kernel
+ * (BsaCL/src/bsacl.cl, OpenCL C) is compiled for the host by oracle/bsacl_ref.py: this
+ * oracle's Classic force / response bispectra over frequency pairs and its nodal PSD are
+ * PINNED against that reference code (tests/test_oracle_bsacl_pin.py, 2e-7; fixtures in
+ * tests/golden/bsacl_ref.npz).  The rest (grid weights, Mesher zones, POD) is cross-checked
+ * by independent numpy restatements (tests/golden/make_golden.py).
  *
  * Array conventions follow the Fortran reference: every multi-dimensional array is
  * column-major, node / mode / lib / zone identifiers passed in are 1-based.

@@ -10,6 +10,10 @@ independent numpy restatements used to cross-check it on small cases:
   dsyev; with every POD mode kept it must equal the direct form.
 
 Only tests, the smoke check and the benchmark's CPU-baseline leg import this module.
+
+Parity: pinned for the Classic bispectra over frequency pairs and the nodal PSD against the
+reference's BsaCL kernel compiled for the host (oracle/bsacl_ref.py,
+tests/test_oracle_bsacl_pin.py); the rest through the restatements above.
 """
 from __future__ import annotations
 
