@@ -60,7 +60,9 @@ def build(ntc: int, nnl: int, nm: int, nn: int, nfi: int, nfj: int, psd_id: int 
            f"-DNN__={nn}", "-DNDEGW__=6", f"-DNNOD_CORR__={(nn * nn + nn) // 2}", f"-DNFI__={nfi}",
            f"-DNFJ__={nfj}", "-o", so, os.path.join(HERE, "bsacl_ref_driver.c"), "-lm"]
     try:
-        subprocess.run(cmd, check=True)
+        r = subprocess.run(cmd, capture_output=True, text=True)  # the source prints #pragma messages
+        if r.returncode:
+            raise RuntimeError(f"building the reference kernel failed:\n{r.stderr[-4000:]}")
     finally:
         if tmp is not None:
             tmp.cleanup()
