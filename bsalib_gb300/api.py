@@ -86,7 +86,7 @@ def load(path: Optional[str] = None):
         "bsa_Run": [vp] * 7, "bsa_computeSkewness": [i, vp, vp, vp],
         "bsa_gpu_setPrecision": [i], "bsa_gpu_setClassicTruncation": [i], "bsa_gpu_setClassicRows": [i, i],
         "bsa_gpu_clsBispectra": [vp, i, vp, vp, vp], "bsa_gpu_mshBispectra": [vp, vp, i, vp, vp],
-        "bsa_gpu_mshMoments": [vp, vp, vp, i, vp, vp], "bsa_gpu_getStats": [vp], "bsa_gpu_releaseDeviceCache": [],
+        "bsa_gpu_mshMoments": [vp, vp, vp, i, vp, vp], "bsa_gpu_getStats": [vp], "bsa_gpu_releaseDeviceCache": [], "bsa_gpu_setClassicForm": [i],
         "bsa_gpu_pointMomentsNoAlloc": [vp, i, i, vp, vp, vp, vp, vp, vp, vp, i, vp, vp, vp, vp, vp, vp],
         "bsa_gpu_mshZones": [vp, i, vp, vp, vp], "bsa_gpu_mshGenerateZones": [vp, i, vp],
         "bsa_setPODTruncationThreshold": [d], "bsa_setPODNOfModesKept": [i],
@@ -213,6 +213,10 @@ class BsaSession:
         """The standalone driver's Mesher controls (app/bsa.F90:544-549): no delta validation,
         no BFM multi-level refinement, background peak from the first direction."""
         self.set_mesher_controls(False, False, True)
+
+    def set_classic_form(self, form: int):
+        """1: the E form of the split contraction where it applies (default); 0: D1 / D3 form."""
+        check(self.lib.bsa_gpu_setClassicForm(int(form)), "bsa_gpu_setClassicForm")
 
     def set_rows(self, r_begin: int, r_end: int = -1):
         """Evaluate only Classic grid rows [r_begin, r_end) (f1 index)."""

@@ -1,0 +1,546 @@
+// bsa_classic_e.cu -- the Classic split-precision contraction in its E form.
+//
+// With A(f) = S(f) L and E(x, y)[(a, b), j] = sum_k Q[k][a] A(x)[k][b] A(y)[k][j], the three
+// terms of the BFM at a grid point (f1, f2) (functionsImpl.F90:1494-1538) are
+//   T1(f1, f2)[m, n, o] = E(f1, f2)[(m, n), o]
+//   T2(f1, f2)[m, n, o] = E(f1 + f2, f2)[(n, m), o]
+//   T3(f1, f2)[m, n, o] = E(f1, f1 + f2)[(o, n), m]
+// and E is symmetric: E(x, y)[(a, b), j] = E(y, x)[(a, j), b].  On the Classic grid
+// (f_i = (i - h) df, h = (nf - 1) / 2) with S(f1 + f2) read as zero beyond the grid (the
+// reference's truncation, BsaClassicImpl.F90:103-119), every E that T2 and T3 need is an E of
+// two grid frequencies.  So the whole grid needs E(f_p, f_q) for q >= p only: one GEMM family
+// over half the grid pairs instead of D1 on half and D3 on all of them (a third of the MMAs of
+// bsa_mixed.cu's form).  Each element x = E(f_p, f_q)[(a, b), j] (u = f_p, v = f_q) then feeds
+//   (i)   T1 at (p, q):              m n o = a b j   Re[H_a(u) H_b(v) conj H_j(u + v)]
+//   (iv)  T1 at (q, p), q > p:       a j b           Re[H_a(v) H_j(u) conj H_b(u + v)]
+//   (iii) T3 at (p, c), f_c = v - u: j b a           Re[H_j(u) H_b(v - u) conj H_a(v)]
+//   (v)   T2 at (c, p):              j a b           Re[H_j(v - u) H_a(u) conj H_b(v)]
+//   (ii)  T2 at (d, q), f_d = u - v: b a j           Re[H_b(u - v) H_a(v) conj H_j(u)]
+//   (vi)  T3 at (q, d):              b j a           Re[H_b(v) H_j(u - v) conj H_a(u)]
+// each with its point's integration weight; (iii)-(vi) exist where q - p <= h.  A diagonal
+// element (q = p) feeds all six at half weight (its transpose is in the same tile).
+//
+// The kernel is bsa_mixed.cu's pipeline (warp 0 TMA, warp 1 tcgen05 MMA, BF16x3, FP32 TMEM
+// accumulators, 2 stages of 96 KB, N = 256 MMAs over two N tiles of grid columns) with three
+// epilogue warpgroups on the same TMEM buffer, one per weight: warps 2-5 accumulate (i), (iv)
+// and their force moment, warps 6-9 (iii), (v) and theirs, warps 10-13 (ii), (vi) and theirs.  The FRF values a unit reads (H at the row, at the unit's columns, at
+// the row + column sums and at the column - row and row - column differences) are staged in
+// shared memory one unit ahead.  Used for whole-grid launches with the truncated sum, up to
+// 24 kept modes and no central symmetry; bsa_mixed.cu's form otherwise.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "../../include/bsa_gpu.h"
+#include "bsa_engine.cuh"
+#include "bsa_epi.cuh"
+#include "bsa_mixed.cuh"
+#include "bsa_tc.cuh"
+
+namespace bsa {
+namespace ecls {
+
+using namespace tc;
+
+constexpr int kStages = 2;
+constexpr int kStageBytes = 6 * kTileBytes;  // U hi, U lo, B0 hi, B1 hi, B0 lo, B1 lo
+constexpr int kKindsWG = 3;  // per epilogue warpgroup: two response kinds and one force kind
+constexpr int kKinds = 3 * kKindsWG;  // 0 K_i, 1 K_iv, 2 F14, 3 K_iii, 4 K_v, 5 F35, 6 K_ii, 7 K_vi, 8 F26
+constexpr int kFlushTiles = 64;
+constexpr int kBarBytes = 256;
+constexpr int kThreads = 448;  // TMA warp, MMA warp, 3 x 4 epilogue warps
+constexpr int kEpi = 384;
+
+// FRF values of one unit (row p, columns q0 .. q0 + 2 NC - 1): H_j at the row, and per
+// column H_j(v), H_j(u + v), H_j(v - u), H_j(u - v).
+template <int NMT>
+struct UTile {
+    static constexpr int NC2 = 2 * (kBN / NMT);
+    float2 hr[NMT];
+    float2 hg[NC2 * NMT];
+    float2 hs[NC2 * NMT];
+    float2 hdp[NC2 * NMT];
+    float2 hdm[NC2 * NMT];
+};
+
+struct EParams {
+    int nf, h, nm, Mp, MT, nk, ks_last, n_ntiles;
+    int wmode;
+    double wval;
+    const float2 *Hg;  // [nf][NMT]
+    const float2 *Hs;  // [2 nf - 1][NMT]
+    double *part;      // [grid][kKinds][NMT][128]
+    int *err;
+};
+
+// Shared-memory float2 load the compiler does not hoist (keeps the per-mode FRF values out
+// of the registers the accumulators need).
+__device__ __forceinline__ float2 lds2(const float2 *p) {
+    float2 r;
+    asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(r.x), "=f"(r.y) : "r"(su32(p)));
+    return r;
+}
+
+__device__ __forceinline__ void epi_sync384() { asm volatile("bar.sync 1, 384;" ::: "memory"); }
+
+// Units of grid row p: pairs of N tiles from the one holding column p (columns q < p masked).
+__device__ __forceinline__ int n_units(int p, int ntl, int NC) { return (ntl - p / NC + 1) / 2; }
+
+// Integration weight of grid point (r, c) (intgSpectraVect_, BsaClassicImpl.F90:596-632, with
+// the reference's vertex weight -d^2 / 2).
+__device__ __forceinline__ float wpt(int r, int c, int nf, bool vect, float wv) {
+    if (!vect) return wv;
+    const bool b1 = r == 0 || r == nf - 1, b2 = c == 0 || c == nf - 1;
+    return wv * ((b1 && b2) ? -0.5f : ((b1 || b2) ? 0.5f : 1.f));
+}
+
+// Stage unit (p, N tiles nt, nt + 1) with threads t < nt_ (cp.async, zero where out of range).
+template <int NMT>
+__device__ __forceinline__ void stage_unit(UTile<NMT> *dst, const EParams &P, int p, int nt, int t, int nt_) {
+    constexpr int NC = kBN / NMT, NC2 = 2 * NC, CH = NMT / 2;  // 16-byte chunks per column row
+    const int q0 = nt * NC;
+    const int nch = CH + 4 * NC2 * CH;
+    for (int x = t; x < nch; x += nt_) {
+        if (x < CH) {
+            epi::cp_async16(dst->hr + 2 * x, P.Hg + (size_t)p * NMT + 2 * x, true);
+            continue;
+        }
+        const int y = x - CH, which = y / (NC2 * CH), z = y - which * NC2 * CH, cc = z / CH, k = z - cc * CH;
+        const int q = q0 + cc;
+        int row;
+        bool v;
+        float2 *d;
+        const float2 *tab = P.Hg;
+        if (which == 0) {
+            row = q;
+            v = q < P.nf;
+            d = dst->hg;
+        } else if (which == 1) {
+            row = p + q;
+            v = row <= 2 * P.nf - 2;
+            tab = P.Hs;
+            d = dst->hs;
+        } else if (which == 2) {
+            row = q - p + P.h;
+            v = row >= 0 && row < P.nf;
+            d = dst->hdp;
+        } else {
+            row = p - q + P.h;
+            v = row >= 0 && row < P.nf;
+            d = dst->hdm;
+        }
+        epi::cp_async16(d + cc * NMT + 2 * k, v ? (const void *)(tab + (size_t)row * NMT + 2 * k) : (const void *)tab,
+                        v);
+    }
+    epi::cp_async_commit();
+}
+
+// One N tile of a unit (TMEM columns taddr .. taddr + 127): grid columns q = q0 + slot0 + ci,
+// staged at column slot slot0 + ci.  Warpgroup WG accumulates kinds 3 WG .. 3 WG + 2:
+//   WG 0: (i)   Re[w_pq H_a(u) H_b(v) conj H_j(u+v)],   (iv) Re[w_pq H_a(v) conj H_b(u+v) H_j(u)],   w_pq
+//   WG 1: (iii) Re[w_pc H_b(v-u) conj H_a(v) H_j(u)],   (v)  Re[w_pc H_a(u) conj H_b(v) H_j(v-u)],   w_pc
+//   WG 2: (ii)  Re[w_dq H_b(u-v) H_a(v) conj H_j(u)],   (vi) Re[w_dq H_b(v) conj H_a(u) H_j(u-v)],   w_dq
+// each times x.
+template <int NMT, int WG>
+__device__ __forceinline__ void unit_half(const UTile<NMT> &hb, uint32_t taddr, int a, int b, int p, int q0,
+                                          int slot0, const EParams &P, bool vect, float wv,
+                                          float (&acc)[kKindsWG][NMT]) {
+    constexpr int NC = kBN / NMT;
+    const float2 hra = hb.hr[a];
+#pragma unroll
+    for (int qc = 0; qc < kBN / 16; ++qc) {
+        uint32_t v[16];
+        tmem_ld16(taddr + qc * 16, v);
+        tmem_wait_ld();
+        float2 P1 = make_float2(0.f, 0.f), P2 = P1;
+        float wk = 0.f;
+        int sl = 0;
+#pragma unroll
+        for (int e = 0; e < 16; ++e) {
+            const int col = qc * 16 + e;
+            const int ci = col / NMT, j = col % NMT;
+            if (ci >= NC) continue;
+            if (j == 0 || e == 0) {
+                sl = (slot0 + ci) * NMT;
+                const int q = q0 + slot0 + ci;
+                const bool valid = q >= p && q < P.nf;
+                const float dl = q == p ? 0.5f : 1.f;
+                const float2 Hbv = hb.hg[sl + b], Hav = hb.hg[sl + a];
+                if constexpr (WG == 0) {
+                    wk = valid ? dl * wpt(p, q, P.nf, vect, wv) : 0.f;
+                    const float2 t1 = cmul(hra, Hbv), t4 = cmul(Hav, conjf2(hb.hs[sl + b]));
+                    P1 = make_float2(wk * t1.x, wk * t1.y);
+                    P2 = make_float2(wk * t4.x, wk * t4.y);
+                } else if constexpr (WG == 1) {
+                    const bool vd = valid && q - p <= P.h;
+                    wk = vd ? dl * wpt(p, q - p + P.h, P.nf, vect, wv) : 0.f;
+                    const float2 t3 = cmul(hb.hdp[sl + b], conjf2(Hav)), t5 = cmul(hra, conjf2(Hbv));
+                    P1 = make_float2(wk * t3.x, wk * t3.y);
+                    P2 = make_float2(wk * t5.x, wk * t5.y);
+                } else {
+                    const bool vd = valid && q - p <= P.h;
+                    wk = vd ? dl * wpt(p - q + P.h, q, P.nf, vect, wv) : 0.f;
+                    const float2 t2 = cmul(hb.hdm[sl + b], Hav), t6 = cmul(Hbv, conjf2(hra));
+                    P1 = make_float2(wk * t2.x, wk * t2.y);
+                    P2 = make_float2(wk * t6.x, wk * t6.y);
+                }
+            }
+            const float x = __uint_as_float(v[e]);
+            const float2 hrj = lds2(hb.hr + j);
+            if constexpr (WG == 0) {
+                const float2 hsj = lds2(hb.hs + sl + j);
+                acc[0][j] = fmaf(P1.x * hsj.x + P1.y * hsj.y, x, acc[0][j]);  // Re[P1 conj H_j(u+v)]
+                acc[1][j] = fmaf(P2.x * hrj.x - P2.y * hrj.y, x, acc[1][j]);  // Re[P2 H_j(u)]
+            } else if constexpr (WG == 1) {
+                const float2 hdpj = lds2(hb.hdp + sl + j);
+                acc[0][j] = fmaf(P1.x * hrj.x - P1.y * hrj.y, x, acc[0][j]);    // Re[P1 H_j(u)]
+                acc[1][j] = fmaf(P2.x * hdpj.x - P2.y * hdpj.y, x, acc[1][j]);  // Re[P2 H_j(v-u)]
+            } else {
+                const float2 hdmj = lds2(hb.hdm + sl + j);
+                acc[0][j] = fmaf(P1.x * hrj.x + P1.y * hrj.y, x, acc[0][j]);    // Re[P1 conj H_j(u)]
+                acc[1][j] = fmaf(P2.x * hdmj.x - P2.y * hdmj.y, x, acc[1][j]);  // Re[P2 H_j(u-v)]
+            }
+            acc[2][j] = fmaf(wk, x, acc[2][j]);
+        }
+    }
+}
+
+template <int NMT>
+__global__ void __launch_bounds__(kThreads, 1)  // 14 warps: at most 128 registers a thread
+    k_bfm_e(const __grid_constant__ CUtensorMap tmUh, const __grid_constant__ CUtensorMap tmUl,
+            const __grid_constant__ CUtensorMap tmGh, const __grid_constant__ CUtensorMap tmGl, const EParams P) {
+    constexpr int NC = kBN / NMT;
+    constexpr int BROWS = NC * NMT;
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint64_t *bars = (uint64_t *)(smem + kStages * kStageBytes);
+    uint64_t *full = bars, *empty = bars + kStages, *tfull = bars + 2 * kStages, *tempty = bars + 2 * kStages + 2;
+    uint64_t *done = bars + 2 * kStages + 4;
+    uint32_t *tmem_slot = (uint32_t *)(bars + 2 * kStages + 5);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int *err = P.err;
+
+    for (int s = 0; s < kStages; ++s)
+        for (int t = 2; t < 6; ++t) {
+            uint8_t *tile = smem + s * kStageBytes + t * kTileBytes;
+            for (int x = threadIdx.x; x < (128 - BROWS) * 128 / 16; x += blockDim.x)
+                ((uint4 *)(tile + BROWS * 128))[x] = make_uint4(0, 0, 0, 0);
+        }
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kStages; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(&tfull[b], 1);
+            mbar_init(&tempty[b], kEpi);
+        }
+        mbar_init(done, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(su32(tmem_slot)) : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    const int mt = blockIdx.x % P.MT;
+    const int rstep = gridDim.x / P.MT;
+    const int r0 = blockIdx.x / P.MT;
+    const uint32_t tx_bytes = 2u * kTileBytes + 4u * (uint32_t)(BROWS * 128);
+
+    if (warp == 0) {
+        // ---------------- TMA producer ----------------
+        if (lane == 0) {
+            uint32_t it = 0;
+            bool ok = true;
+            for (int p = r0; p < P.nf && ok; p += rstep) {
+                const int nu = n_units(p, P.n_ntiles, NC), nt0 = p / NC;
+                for (int u = 0; u < nu && ok; ++u)
+                    for (int kc = 0; kc < P.nk && ok; ++kc, ++it) {
+                        const int s = it % kStages;
+                        const uint32_t ph = (it / kStages) & 1u;
+                        if (!mbar_wait(&empty[s], ph ^ 1u, err, 1)) { ok = false; break; }
+                        uint8_t *st = smem + s * kStageBytes;
+                        mbar_expect_tx(&full[s], tx_bytes);
+                        const int x = kc * kBK;
+                        const int yu = p * P.Mp + mt * kBM;
+                        const int yg = (nt0 + 2 * u) * BROWS;  // rows past the table read zeros
+                        tma_2d(st + 0 * kTileBytes, &tmUh, &full[s], x, yu);
+                        tma_2d(st + 1 * kTileBytes, &tmUl, &full[s], x, yu);
+                        tma_2d(st + 2 * kTileBytes, &tmGh, &full[s], x, yg);
+                        tma_2d(st + 4 * kTileBytes, &tmGl, &full[s], x, yg);
+                        tma_2d(st + 3 * kTileBytes, &tmGh, &full[s], x, yg + BROWS);
+                        tma_2d(st + 5 * kTileBytes, &tmGl, &full[s], x, yg + BROWS);
+                    }
+            }
+            const uint32_t last = it;
+            for (uint32_t q = (last > (uint32_t)kStages ? last - kStages : 0); q < last; ++q) {
+                const int s = q % kStages;
+                const uint32_t ph = (q / kStages) & 1u;
+                const uint64_t t0 = gtime();
+                while (!mbar_try(&full[s], ph) && gtime() - t0 < kWaitNs) {
+                }
+            }
+        }
+        __syncwarp();
+    } else if (warp == 1) {
+        // ---------------- MMA issuer ----------------
+        if (lane == 0) {
+            uint32_t it = 0, tile = 0;
+            bool ok = true;
+            for (int p = r0; p < P.nf && ok; p += rstep) {
+                const int nu = n_units(p, P.n_ntiles, NC);
+                for (int u = 0; u < nu && ok; ++u, ++tile) {
+                    const int buf = tile & 1;
+                    const uint32_t tph = (tile >> 1) & 1u;
+                    if (!mbar_wait(&tempty[buf], tph ^ 1u, err, 2)) { ok = false; break; }
+                    fence_after();
+                    const uint32_t d = tmem + buf * 256;
+                    for (int kc = 0; kc < P.nk; ++kc, ++it) {
+                        const int s = it % kStages;
+                        const uint32_t ph = (it / kStages) & 1u;
+                        if (!mbar_wait(&full[s], ph, err, 3)) { ok = false; break; }
+                        fence_after();
+                        const uint32_t base = su32(smem + s * kStageBytes);
+                        const int nks = kc == P.nk - 1 ? P.ks_last : kBK / 16;
+#pragma unroll
+                        for (int ks = 0; ks < kBK / 16; ++ks) {
+                            if (ks >= nks) break;
+                            const uint32_t off = ks * 32;
+                            const uint64_t uh = sdesc(base + 0 * kTileBytes + off), ul = sdesc(base + 1 * kTileBytes + off);
+                            const uint64_t bh = sdesc(base + 2 * kTileBytes + off), bl = sdesc(base + 4 * kTileBytes + off);
+                            const uint32_t acc = (kc > 0 || ks > 0) ? 1u : 0u;
+                            mma256(d, uh, bh, acc);
+                            mma256(d, uh, bl, 1u);
+                            mma256(d, ul, bh, 1u);
+                        }
+                        mma_commit(&empty[s]);
+                    }
+                    if (!ok) break;
+                    mma_commit(&tfull[buf]);
+                }
+            }
+            mma_commit(done);
+            const uint64_t t0 = gtime();
+            while (!mbar_try(done, 0) && gtime() - t0 < kWaitNs) {
+            }
+        }
+        __syncwarp();
+    } else {
+        // ---------------- three epilogue warpgroups ----------------
+        const int wg = (warp - 2) >> 2;        // 0: warps 2-5, 1: warps 6-9, 2: warps 10-13
+        const int quarter = warp & 3;          // TMEM lane quarter of this warp
+        const int et = threadIdx.x - 64;       // 0 .. 383
+        const int row = quarter * 32 + lane;
+        const int grow = mt * kBM + row;
+        const bool vrow = grow < P.nm * P.nm;
+        const int a = vrow ? grow / P.nm : 0, b = vrow ? grow % P.nm : 0;
+        const uint32_t lane_base = tmem + ((uint32_t)(quarter * 32) << 16);
+        const float wv = (float)P.wval;
+        const bool vect = P.wmode == kWeightClassicVect;
+        using UT = UTile<NMT>;
+        UT *hbs = (UT *)(smem + kStages * kStageBytes + kBarBytes);
+        double *part = P.part + (size_t)blockIdx.x * kKinds * NMT * 128 + row;
+        const int k0 = wg * kKindsWG;
+        for (int k = 0; k < kKindsWG * NMT; ++k) part[(size_t)(k0 * NMT + k) * 128] = 0.0;
+        float acc[kKindsWG][NMT];
+#pragma unroll
+        for (int k = 0; k < kKindsWG; ++k)
+#pragma unroll
+            for (int j = 0; j < NMT; ++j) acc[k][j] = 0.f;
+        uint32_t tile = 0;
+        bool ok = true;
+        int since = 0;
+        if (r0 < P.nf) stage_unit<NMT>(hbs, P, r0, r0 / NC, et, kEpi);
+        for (int p = r0; p < P.nf; p += rstep) {
+            const int nu = n_units(p, P.n_ntiles, NC), nt0 = p / NC;
+            for (int u = 0; u < nu; ++u, ++tile) {
+                const int buf = tile & 1;
+                const uint32_t tph = (tile >> 1) & 1u;
+                epi::cp_async_wait_all();
+                epi_sync384();  // this unit's values are in; the other slot is free
+                if (u + 1 < nu)
+                    stage_unit<NMT>(hbs + (buf ^ 1), P, p, nt0 + 2 * (u + 1), et, kEpi);
+                else if (p + rstep < P.nf)
+                    stage_unit<NMT>(hbs + (buf ^ 1), P, p + rstep, (p + rstep) / NC, et, kEpi);
+                if (ok) {
+                    ok = __all_sync(0xffffffffu, mbar_wait(&tfull[buf], tph, err, 4));
+                    if (ok) {
+                        fence_after();
+                        const UT &hb = hbs[buf];
+                        const int q0 = (nt0 + 2 * u) * NC;
+                        // two N tiles: TMEM columns 0-127 hold columns q0 .., 128-255 q0 + NC ..
+                        for (int h2 = 0; h2 < 2; ++h2) {
+                            const uint32_t ta = lane_base + buf * 256 + h2 * 128;
+                            if (wg == 0)
+                                unit_half<NMT, 0>(hb, ta, a, b, p, q0, h2 * NC, P, vect, wv, acc);
+                            else if (wg == 1)
+                                unit_half<NMT, 1>(hb, ta, a, b, p, q0, h2 * NC, P, vect, wv, acc);
+                            else
+                                unit_half<NMT, 2>(hb, ta, a, b, p, q0, h2 * NC, P, vect, wv, acc);
+                        }
+                        fence_before();
+                        mbar_arrive(&tempty[buf]);
+                        since += 2;
+                        if ((since >= kFlushTiles || (u + 1 == nu && p + rstep >= P.nf)) && vrow) {
+#pragma unroll
+                            for (int k = 0; k < kKindsWG; ++k)
+#pragma unroll
+                                for (int j = 0; j < NMT; ++j) {
+                                    if (acc[k][j] != 0.f)
+                                        atomicAdd(part + (size_t)((k0 + k) * NMT + j) * 128, (double)acc[k][j]);
+                                    acc[k][j] = 0.f;
+                                }
+                            since = 0;
+                        }
+                    }
+                }
+            }
+        }
+        epi::cp_async_wait_all();
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem) : "memory");
+}
+
+}  // namespace ecls
+}  // namespace bsa
+
+namespace bsa {
+namespace ecls {
+
+// m3[m + nm n + nm^2 o] from the per-CTA FP64 partials of the E form (kinds: 0 K_i, 1 K_iv,
+// 2 F14, 3 K_iii, 4 K_v, 5 F35, 6 K_ii, 7 K_vi, 8 F26, each kept at the lane's (a, b) and j).
+__global__ void k_e_reduce(int nm, int NMT, int MT, int grid, const double *__restrict__ part,
+                           double *__restrict__ m3mf, double *__restrict__ m3mr) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nm3 = nm * nm * nm;
+    if (x >= nm3) return;
+    const int m = x % nm, n = (x / nm) % nm, o = x / (nm * nm);
+    auto sum = [&](int kind, int a, int b, int j) {
+        const int R = a * nm + b, mtile = R / 128, lane = R % 128;
+        double s = 0.0;
+        for (int g = mtile; g < grid; g += MT) s += part[(((size_t)g * kKinds + kind) * NMT + j) * 128 + lane];
+        return s;
+    };
+    const double mr = sum(0, m, n, o) + sum(1, m, o, n) + sum(3, o, n, m) + sum(4, n, o, m) + sum(6, n, m, o) +
+                      sum(7, o, m, n);
+    const double mf = sum(2, m, n, o) + sum(2, m, o, n) + sum(5, o, n, m) + sum(5, n, o, m) + sum(8, n, m, o) +
+                      sum(8, o, m, n);
+    m3mr[x] = 2.0 * mr;  // B_F = 2 (T1 + T2 + T3)
+    m3mf[x] = 2.0 * mf;
+}
+
+template <int NMT>
+static cudaError_t launch_k(cudaStream_t st, const CUtensorMap *maps, const EParams &p, int grid) {
+    const size_t smem = (size_t)kStages * kStageBytes + 1024 + kBarBytes + 2 * sizeof(UTile<NMT>);
+    cudaError_t e = cudaFuncSetAttribute(k_bfm_e<NMT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k_bfm_e<NMT><<<grid, kThreads, smem, st>>>(maps[0], maps[1], maps[2], maps[3], p);
+    return cudaGetLastError();
+}
+
+}  // namespace ecls
+
+// The E form of the Classic contraction (see the top of this file): whole grid, truncated
+// S(f1 + f2), at most 24 kept modes.  Called by contract_mixed.
+int Engine::contract_e(const PointSrc &ps, double *m3mf, double *m3mr) {
+    using namespace ecls;
+    const int nf = ps.nf, nm = nme;
+    const int NMT = nm <= 8 ? 8 : nm <= 16 ? 16 : 24;
+    const int NC = kBN / NMT;
+    const int Kp = ((K + kBK - 1) / kBK) * kBK;
+    const int Mp = ((nm * nm + kBM - 1) / kBM) * kBM;
+    const int MT = Mp / kBM;
+    const int ns = 2 * nf - 1;
+    int dev = 0, nsm = 0;
+    cudaError_t e;
+    if ((e = cudaGetDevice(&dev)) || (e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev)))
+        return cuda_fail(e, "device query");
+    int grid = (nsm / MT) * MT;
+    if (grid < MT) grid = MT;
+    const size_t uel = (size_t)nf * Mp * Kp, gel = (size_t)nf * NMT * Kp;
+    const size_t bytesA = 2 * uel * 2, bytesB = 2 * gel * 2;
+    const size_t bytesH = sizeof(float2) * (size_t)(nf + ns) * NMT;
+    const size_t bytesP = sizeof(double) * (size_t)grid * kKinds * NMT * 128;
+    if ((e = dMixA.reserve(bytesA)) || (e = dMixB.reserve(bytesB)) || (e = dMixH.reserve(bytesH + 256)) ||
+        (e = dMixPart.reserve(bytesP + 256)))
+        return cuda_fail(e, "allocating BF16x3 operands");
+    __nv_bfloat16 *Uh = dMixA.as<__nv_bfloat16>(), *Ul = Uh + uel;
+    __nv_bfloat16 *Gh = dMixB.as<__nv_bfloat16>(), *Gl = Gh + gel;
+    float2 *Hg = dMixH.as<float2>(), *Hs = Hg + (size_t)nf * NMT;
+    int *derr = (int *)((char *)dMixPart.p + bytesP);
+    if ((e = cudaEventRecord(ev2, stream))) return cuda_fail(e, "event");
+    if ((e = cudaMemsetAsync(derr, 0, sizeof(int), stream))) return cuda_fail(e, "memset");
+    {
+        const float *A = dA32.as<float>();
+        if ((e = mixed::prep_u(stream, nf, nm, K, Kp, Mp, A, dQ.as<double>(), Uh, Ul)) ||
+            (e = mixed::prep_b(stream, nf, nm, NMT, 0, K, Kp, nf, ps.n_pad, ps.trunc, ps.sum_base, 0, A, Gh, Gl)) ||
+            (e = mixed::prep_h(stream, nf, nm, NMT, ps.fgrid, frf(), Hg, Hs)))
+            return cuda_fail(e, "BF16x3 operand preparation");
+        kernels += 3;
+    }
+    CUtensorMap maps[4];
+    if (!make_map(&maps[0], Uh, Kp, (uint64_t)nf * Mp, kBM) || !make_map(&maps[1], Ul, Kp, (uint64_t)nf * Mp, kBM) ||
+        !make_map(&maps[2], Gh, Kp, (uint64_t)nf * NMT, NC * NMT) ||
+        !make_map(&maps[3], Gl, Kp, (uint64_t)nf * NMT, NC * NMT))
+        return fail(BSA_ERR_CUDA, "cuTensorMapEncodeTiled failed");
+    EParams prm{};
+    prm.nf = nf;
+    prm.h = (nf - 1) / 2;
+    prm.nm = nm;
+    prm.Mp = Mp;
+    prm.MT = MT;
+    prm.nk = Kp / kBK;
+    prm.ks_last = (K - (prm.nk - 1) * kBK + 15) / 16;
+    prm.n_ntiles = (nf + NC - 1) / NC;
+    prm.wmode = ps.wmode;
+    prm.wval = ps.wval;
+    prm.Hg = Hg;
+    prm.Hs = Hs;
+    prm.part = dMixPart.as<double>();
+    prm.err = derr;
+    if ((e = cudaEventRecord(evg0, stream))) return cuda_fail(e, "event");
+    switch (NMT) {
+    case 8: e = launch_k<8>(stream, maps, prm, grid); break;
+    case 16: e = launch_k<16>(stream, maps, prm, grid); break;
+    default: e = launch_k<24>(stream, maps, prm, grid); break;
+    }
+    if (e) return cuda_fail(e, "BF16x3 tcgen05 contraction kernel (E form)");
+    if ((e = cudaEventRecord(evg1, stream))) return cuda_fail(e, "event");
+    const long long nm3 = (long long)nm * nm * nm;
+    if ((e = dOut.reserve(sizeof(double) * (3 * (size_t)nm * nm + 2 * (size_t)nm3)))) return cuda_fail(e, "out");
+    double *o = dOut.as<double>() + 3 * (size_t)nm * nm;
+    k_e_reduce<<<(unsigned)((nm3 + 127) / 128), 128, 0, stream>>>(nm, NMT, MT, grid, prm.part, o, o + nm3);
+    if ((e = cudaGetLastError())) return cuda_fail(e, "BF16x3 reduction");
+    kernels += 2;
+    std::vector<double> h(2 * (size_t)nm3);
+    int herr = 0;
+    if ((e = cudaMemcpyAsync(h.data(), o, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, stream)) ||
+        (e = cudaMemcpyAsync(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost, stream)) ||
+        (e = cudaEventRecord(ev1, stream)) || (e = cudaStreamSynchronize(stream)))
+        return cuda_fail(e, "BF16x3 contraction");
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ev2, ev1);
+    last_ms_contraction = ms;
+    cudaEventElapsedTime(&ms, evg0, evg1);
+    last_ms_gemm = ms;
+    d2h += (double)sizeof(double) * h.size() + sizeof(int);
+    if (herr) return fail(BSA_ERR_TIMEOUT, "BF16x3 kernel: a pipeline wait ran out of its budget (role %d)", herr);
+    if (m3mf) std::memcpy(m3mf, h.data(), sizeof(double) * nm3);
+    if (m3mr) std::memcpy(m3mr, h.data() + nm3, sizeof(double) * nm3);
+    return BSA_OK;
+}
+
+}  // namespace bsa

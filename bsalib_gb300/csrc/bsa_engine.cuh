@@ -74,6 +74,7 @@ struct Engine {
     std::vector<std::vector<int>> own_i;     // arrays read by bsa_loadInputFiles (owned here)
     std::vector<std::vector<double>> own_d;
     bool classic_sym = false;   // bsa_gpu_setClassicSymmetry: evaluate half the Classic grid
+    bool use_e_form = true;     // bsa_gpu_setClassicForm: E form of the split contraction where it applies
     // Mesher controls (BsaLibData.F90:219-233, 273): delta validation, BFM multi-level
     // refinement, background peak restricted to the first direction, diagonal-crest scheme
     bool validate_deltas = true, bfm_mlr = true, bkg_restrict = false, premesh_diag_crest = false;
@@ -132,6 +133,7 @@ struct Engine {
     int classic_export(PointSrc ps, const std::vector<double> &f, double *m3mf, double *m3mr);
     int contract(const PointSrc &ps, long long npts, double *m3mf, double *m3mr, double *bf_host, double *br_host);
     int contract_mixed(const PointSrc &ps, long long npts, double *m3mf, double *m3mr);
+    int contract_e(const PointSrc &ps, double *m3mf, double *m3mr);  // bsa_classic_e.cu
     int contract_diag(const PointSrc &ps, long long npts, int msh_form, double *m3mf, double *m3mr,
                       double *bf_host, double *br_host);
     int run_points(const double *fi, const double *fj, const double *w, double wuniform, long long npts,

@@ -139,6 +139,7 @@ void Engine::reset_inputs() {
     export_fn = nullptr;
     export_user = nullptr;
     classic_sym = false;
+    use_e_form = true;
     validate_deltas = true;
     bfm_mlr = true;
     bkg_restrict = false;
@@ -1064,6 +1065,12 @@ int bsa_gpu_getStats(bsa_gpu_stats *st) {
     st->d2h_bytes = eng().d2h;
     st->kernels = eng().kernels;
     st->precision = eng().precision;
+    return BSA_OK;
+}
+
+int bsa_gpu_setClassicForm(int form) {
+    if (form != 0 && form != 1) return BSA_ERR_ARG;
+    eng().use_e_form = form == 1;
     return BSA_OK;
 }
 

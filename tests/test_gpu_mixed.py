@@ -129,3 +129,24 @@ def test_symmetric_d1_matches_the_full_form(modes):
         s.close()
     for k in ("m3mr_cls", "m3mf_cls"):
         assert rel(full[k], parts[0][k] + parts[1][k]) < 2e-6, k
+
+
+@pytest.mark.parametrize("nodes,modes,nfreqs,tc", [(30, 4, 33, (1,)), (60, 8, 41, (1, 3)), (80, 12, 65, (1, 3)),
+                                                     (100, 16, 33, (1,)), (120, 24, 49, (1, 3))])
+def test_e_form_matches_the_d_form(bsalib, nodes, modes, nfreqs, tc):
+    """The E form (one GEMM family over half the grid pairs, six contributions per product)
+    against the D1 / D3 form on the same grid: the same products, summed in another order
+    (FP32 partials), so 2e-6 relative."""
+    import dataclasses
+    prob = tall_building(nodes=nodes, modes=modes, nfreqs=nfreqs, df=4.0 / (nfreqs - 1), seed=nodes)
+    prob.settings = dataclasses.replace(prob.settings, tc=tc)
+    out = []
+    for form in (1, 0):
+        s = api.BsaSession(prob, precision=api.PREC_BF16X3)
+        try:
+            s.set_classic_form(form)
+            out.append(s.run())
+        finally:
+            s.close()
+    for k in ("m3mr_cls", "m3mf_cls"):
+        assert rel(out[0][k], out[1][k]) < 2e-6, k
