@@ -140,14 +140,16 @@ __device__ __forceinline__ void stage_unit(UTile<NMT> *dst, const EParams &P, in
 }
 
 // One N tile of a unit (TMEM columns taddr .. taddr + 127): grid columns q = q0 + slot0 + ci,
-// staged at column slot slot0 + ci.  Warpgroup WG accumulates kinds 3 WG .. 3 WG + 2:
-//   WG 0: (i)   Re[w_pq H_a(u) H_b(v) conj H_j(u+v)],   (iv) Re[w_pq H_a(v) conj H_b(u+v) H_j(u)],   w_pq
-//   WG 1: (iii) Re[w_pc H_b(v-u) conj H_a(v) H_j(u)],   (v)  Re[w_pc H_a(u) conj H_b(v) H_j(v-u)],   w_pc
-//   WG 2: (ii)  Re[w_dq H_b(u-v) H_a(v) conj H_j(u)],   (vi) Re[w_dq H_b(v) conj H_a(u) H_j(u-v)],   w_dq
-// each times x.
-template <int NMT, int WG>
-__device__ __forceinline__ void unit_half(const UTile<NMT> &hb, uint32_t taddr, int a, int b, int p, int q0,
-                                          int slot0, const EParams &P, bool vect, float wv,
+// staged at column slot slot0 + ci.  Warpgroup wg accumulates kinds 3 wg .. 3 wg + 2:
+//   wg 0: (i)   Re[w_pq H_a(u) H_b(v) conj H_j(u+v)],   (iv) Re[w_pq H_a(v) conj H_b(u+v) H_j(u)],   w_pq
+//   wg 1: (iii) Re[w_pc H_b(v-u) conj H_a(v) H_j(u)],   (v)  Re[w_pc H_a(u) conj H_b(v) H_j(v-u)],   w_pc
+//   wg 2: (ii)  Re[w_dq H_b(u-v) H_a(v) conj H_j(u)],   (vi) Re[w_dq H_b(v) conj H_a(u) H_j(u-v)],   w_dq
+// each times x.  One code path for the three (the per-column setup picks the factors and the
+// staged rows; a conj on H_j is folded into the factor), so the three warpgroups share one
+// instruction stream.
+template <int NMT>
+__device__ __forceinline__ void unit_half(const UTile<NMT> &hb, uint32_t taddr, int wg, int a, int b, int p,
+                                          int q0, int slot0, const EParams &P, bool vect, float wv,
                                           float (&acc)[kKindsWG][NMT]) {
     constexpr int NC = kBN / NMT;
     const float2 hra = hb.hr[a];
@@ -158,52 +160,46 @@ __device__ __forceinline__ void unit_half(const UTile<NMT> &hb, uint32_t taddr, 
         tmem_wait_ld();
         float2 P1 = make_float2(0.f, 0.f), P2 = P1;
         float wk = 0.f;
-        int sl = 0;
+        const float2 *X = hb.hr, *Y = hb.hr;  // per-mode factors of the two response kinds
 #pragma unroll
         for (int e = 0; e < 16; ++e) {
             const int col = qc * 16 + e;
             const int ci = col / NMT, j = col % NMT;
             if (ci >= NC) continue;
             if (j == 0 || e == 0) {
-                sl = (slot0 + ci) * NMT;
+                const int sl = (slot0 + ci) * NMT;
                 const int q = q0 + slot0 + ci;
                 const bool valid = q >= p && q < P.nf;
+                const bool vd = valid && q - p <= P.h;
                 const float dl = q == p ? 0.5f : 1.f;
                 const float2 Hbv = hb.hg[sl + b], Hav = hb.hg[sl + a];
-                if constexpr (WG == 0) {
+                float2 t1, t2;
+                if (wg == 0) {
                     wk = valid ? dl * wpt(p, q, P.nf, vect, wv) : 0.f;
-                    const float2 t1 = cmul(hra, Hbv), t4 = cmul(Hav, conjf2(hb.hs[sl + b]));
-                    P1 = make_float2(wk * t1.x, wk * t1.y);
-                    P2 = make_float2(wk * t4.x, wk * t4.y);
-                } else if constexpr (WG == 1) {
-                    const bool vd = valid && q - p <= P.h;
+                    t1 = conjf2(cmul(hra, Hbv));               // conj: pairs with conj H_j(u+v)
+                    t2 = cmul(Hav, conjf2(hb.hs[sl + b]));
+                    X = hb.hs + sl;
+                    Y = hb.hr;
+                } else if (wg == 1) {
                     wk = vd ? dl * wpt(p, q - p + P.h, P.nf, vect, wv) : 0.f;
-                    const float2 t3 = cmul(hb.hdp[sl + b], conjf2(Hav)), t5 = cmul(hra, conjf2(Hbv));
-                    P1 = make_float2(wk * t3.x, wk * t3.y);
-                    P2 = make_float2(wk * t5.x, wk * t5.y);
+                    t1 = cmul(hb.hdp[sl + b], conjf2(Hav));
+                    t2 = cmul(hra, conjf2(Hbv));
+                    X = hb.hr;
+                    Y = hb.hdp + sl;
                 } else {
-                    const bool vd = valid && q - p <= P.h;
                     wk = vd ? dl * wpt(p - q + P.h, q, P.nf, vect, wv) : 0.f;
-                    const float2 t2 = cmul(hb.hdm[sl + b], Hav), t6 = cmul(Hbv, conjf2(hra));
-                    P1 = make_float2(wk * t2.x, wk * t2.y);
-                    P2 = make_float2(wk * t6.x, wk * t6.y);
+                    t1 = conjf2(cmul(hb.hdm[sl + b], Hav));    // conj: pairs with conj H_j(u)
+                    t2 = cmul(Hbv, conjf2(hra));
+                    X = hb.hr;
+                    Y = hb.hdm + sl;
                 }
+                P1 = make_float2(wk * t1.x, wk * t1.y);
+                P2 = make_float2(wk * t2.x, wk * t2.y);
             }
             const float x = __uint_as_float(v[e]);
-            const float2 hrj = lds2(hb.hr + j);
-            if constexpr (WG == 0) {
-                const float2 hsj = lds2(hb.hs + sl + j);
-                acc[0][j] = fmaf(P1.x * hsj.x + P1.y * hsj.y, x, acc[0][j]);  // Re[P1 conj H_j(u+v)]
-                acc[1][j] = fmaf(P2.x * hrj.x - P2.y * hrj.y, x, acc[1][j]);  // Re[P2 H_j(u)]
-            } else if constexpr (WG == 1) {
-                const float2 hdpj = lds2(hb.hdp + sl + j);
-                acc[0][j] = fmaf(P1.x * hrj.x - P1.y * hrj.y, x, acc[0][j]);    // Re[P1 H_j(u)]
-                acc[1][j] = fmaf(P2.x * hdpj.x - P2.y * hdpj.y, x, acc[1][j]);  // Re[P2 H_j(v-u)]
-            } else {
-                const float2 hdmj = lds2(hb.hdm + sl + j);
-                acc[0][j] = fmaf(P1.x * hrj.x + P1.y * hrj.y, x, acc[0][j]);    // Re[P1 conj H_j(u)]
-                acc[1][j] = fmaf(P2.x * hdmj.x - P2.y * hdmj.y, x, acc[1][j]);  // Re[P2 H_j(u-v)]
-            }
+            const float2 xj = lds2(X + j), yj = lds2(Y + j);
+            acc[0][j] = fmaf(P1.x * xj.x - P1.y * xj.y, x, acc[0][j]);  // Re[P1 X_j]
+            acc[1][j] = fmaf(P2.x * yj.x - P2.y * yj.y, x, acc[1][j]);  // Re[P2 Y_j]
             acc[2][j] = fmaf(wk, x, acc[2][j]);
         }
     }
@@ -379,15 +375,9 @@ __global__ void __launch_bounds__(kThreads, 1)  // 14 warps: at most 128 registe
                         const UT &hb = hbs[buf];
                         const int q0 = (nt0 + 2 * u) * NC;
                         // two N tiles: TMEM columns 0-127 hold columns q0 .., 128-255 q0 + NC ..
-                        for (int h2 = 0; h2 < 2; ++h2) {
-                            const uint32_t ta = lane_base + buf * 256 + h2 * 128;
-                            if (wg == 0)
-                                unit_half<NMT, 0>(hb, ta, a, b, p, q0, h2 * NC, P, vect, wv, acc);
-                            else if (wg == 1)
-                                unit_half<NMT, 1>(hb, ta, a, b, p, q0, h2 * NC, P, vect, wv, acc);
-                            else
-                                unit_half<NMT, 2>(hb, ta, a, b, p, q0, h2 * NC, P, vect, wv, acc);
-                        }
+                        for (int h2 = 0; h2 < 2; ++h2)
+                            unit_half<NMT>(hb, lane_base + buf * 256 + h2 * 128, wg, a, b, p, q0, h2 * NC, P, vect, wv,
+                                           acc);
                         fence_before();
                         mbar_arrive(&tempty[buf]);
                         since += 2;

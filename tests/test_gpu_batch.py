@@ -1,9 +1,11 @@
 """The batched Classic sweep (bsa_gpu_batch*) against one bsa_Run per case.
 
-Each case of a batch must give the moments its own split-precision analysis gives: both
-kernels form the same work units (symmetric D1 with paired N tiles up to 24 kept modes) and
-the same FP32 partials, summed in FP64 in another order, so third moments agree to 1e-9
-relative (max-norm), second moments to 1e-12.  Against the FP64 path the mixed-precision bar holds
+Each case of a batch must give the moments its own split-precision analysis gives.  Up to 24
+kept modes the single analysis uses the E form of the contraction (each product of one GEMM
+family feeding the three terms at up to six grid points) and the batch the D1 / D3 form: the
+same products summed in another order in FP32, so third moments agree to ~1e-6 (both lie
+~3e-6 from the FP64 path); the bar is 1e-5 relative (max-norm, 10x inside the split-precision
+bar).  Second moments agree to 1e-12.  Against the FP64 path the mixed-precision bar holds
 (third moments 1e-4 relative).  Cases of every FRF-table width (8, 16, 24, 32 kept modes, and
 two halves of 32 above that),
 different grids and load sizes share one batch; the library's own inputs are left as they
@@ -63,8 +65,8 @@ def test_batch_matches_single_analyses(batch):
     for k, p in enumerate(CASES):
         ref = single(p, api.PREC_BF16X3)
         assert out[k]["nm"] ** 3 == ref["m3mr_cls"].size
-        assert rel(out[k]["m3mr"], ref["m3mr_cls"]) < 1e-9, k
-        assert rel(out[k]["m3mf"], ref["m3mf_cls"]) < 1e-9, k
+        assert rel(out[k]["m3mr"], ref["m3mr_cls"]) < 1e-5, k
+        assert rel(out[k]["m3mf"], ref["m3mf_cls"]) < 1e-5, k
         assert rel(out[k]["m2mr"], ref["m2mr_cls"]) < 1e-12, k
 
 
@@ -94,7 +96,7 @@ def test_batch_wind_cases_of_one_structure(bsalib):
     sw.clear()
     for k, p in enumerate(probs):
         ref = single(p, api.PREC_BF16X3)
-        assert rel(out[k]["m3mr"], ref["m3mr_cls"]) < 1e-9
+        assert rel(out[k]["m3mr"], ref["m3mr_cls"]) < 1e-5
     v = [float(np.max(np.abs(o["m3mr"]))) for o in out]
     assert v[0] < v[1] < v[2]
 
