@@ -609,7 +609,7 @@ int Engine::batch_run(double *m3mf, double *m3mr, double *m2mr, double *case_ms,
             if ((e = upload(dWf, wf, stream)) || (e = dPsdF.reserve(sizeof(double) * (size_t)nf * nm2)))
                 return cuda_fail(e, "batch m2");
             double *m2o = d_m2 + 3 * off2[order[k]];
-            if ((e = launch_force_psd32(stream, nf, (int)c.set.tc.size(), c.nnl, c.nme, dL.as<double>(), A,
+            if ((e = launch_force_psd32(stream, nf, (int)c.set.tc.size(), c.nnl, c.nme, dL32.as<float>(), A,
                                         dPsdF.as<double>())) ||
                 (e = launch_m2(stream, 0, nf, c.nme, 0, dFreq.as<double>(), dWf.as<double>(), dPsdF.as<double>(), frf(),
                                m2o, m2o + nm2, m2o + 2 * nm2)))

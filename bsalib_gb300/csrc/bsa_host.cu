@@ -477,7 +477,7 @@ int Engine::run_classic(double *m2mf, double *m2mr, double *m2o2mr, double *m3mf
         if ((e = dOut.reserve(sizeof(double) * (3 * (size_t)nm2 + 2 * (size_t)dim_bisp()))))
             return cuda_fail(e, "out");
         e = diagonal ? launch_force_psd_diag(stream, nf, K, nme, dS.as<double>(), dWd2.as<double>(), dPsdF.as<double>())
-            : mixed  ? launch_force_psd32(stream, nf, (int)set.tc.size(), in.nnl, nme, dL.as<double>(),
+            : mixed  ? launch_force_psd32(stream, nf, (int)set.tc.size(), in.nnl, nme, dL32.as<float>(),
                                           dA32.as<float>(), dPsdF.as<double>())
                      : launch_force_psd(stream, nf, (int)set.tc.size(), in.nnl, nme, dL.as<double>(), dA.as<double>(),
                                         dPsdF.as<double>());
@@ -515,7 +515,11 @@ int Engine::run_classic(double *m2mf, double *m2mr, double *m2o2mr, double *m3mf
         // truncation and the integration weights are symmetric), so B(f_r, f_c) equals
         // B(f_nf-1-r, f_nf-1-c).  Rows r < n_pad then stand for their mirrors with twice the
         // weight, the centre row (its own mirror) once; rows above it are not evaluated.
-        const bool sym = classic_sym && set.defsc == 1 && !bf_host && !br_host && !export_fn;
+        // The split path's E form (bsa_classic_e.cu) already forms each distinct product of the
+        // whole grid once, which half the rows would not improve on: there the symmetry is not
+        // applied.
+        const bool e_form = mixed && use_e_form && nme <= 24 && !analytic && (nf & 1) && r0 == 0 && r1 == nf;
+        const bool sym = classic_sym && set.defsc == 1 && !bf_host && !br_host && !export_fn && !e_form;
         if (sym) {
             ps.sym_rows = ps.n_pad;
             ps.nr = std::max(0, std::min(r1, ps.n_pad + 1) - r0);

@@ -186,10 +186,31 @@ cudaError_t launch_force_psd(cudaStream_t st, int nf, int ntc, int nnl, int nm, 
     return cudaGetLastError();
 }
 
-cudaError_t launch_force_psd32(cudaStream_t st, int nf, int ntc, int nnl, int nm, const double *L,
+// The same from the FP32 tables of the split path: FP32 products summed in FP32 over runs of
+// 32 k and the runs in FP64 (GB300's FP64 rate makes the all-FP64 form the slow one; the
+// operands are FP32-rounded anyway, and the runs keep the sum to ~1e-7).
+__global__ void k_force_psd32(int ntc, int nnl, int nm, const float *__restrict__ L, const float *__restrict__ A,
+                              double *__restrict__ psd) {
+    const int fi = blockIdx.x;
+    const int nm2 = nm * nm, K = ntc * nnl;
+    const float *Af = A + (size_t)fi * K * nm;
+    for (int pr = threadIdx.x; pr < nm2; pr += blockDim.x) {
+        const int n = pr % nm, o = pr / nm;
+        double s = 0.0;
+        for (int k0 = 0; k0 < K; k0 += 32) {
+            const int k1 = min(K, k0 + 32);
+            float r = 0.f;
+            for (int k = k0; k < k1; ++k) r = fmaf(L[(size_t)k * nm + o], Af[(size_t)k * nm + n], r);
+            s += (double)r;
+        }
+        psd[(size_t)fi * nm2 + pr] = s;
+    }
+}
+
+cudaError_t launch_force_psd32(cudaStream_t st, int nf, int ntc, int nnl, int nm, const float *L,
                                const float *A, double *psd) {
     if (nf == 0) return cudaSuccess;
-    k_force_psd<float><<<nf, 256, 0, st>>>(ntc, nnl, nm, L, A, psd);
+    k_force_psd32<<<nf, 256, 0, st>>>(ntc, nnl, nm, L, A, psd);
     return cudaGetLastError();
 }
 

@@ -29,7 +29,7 @@ cudaError_t launch_atable_tc(cudaStream_t st, int nf, const double *f, int ntc, 
 // m2mf, m2mr (x Re[H_o conj H_n]), m2o2mr (x w^2) with per-frequency weights wf.
 cudaError_t launch_force_psd(cudaStream_t st, int nf, int ntc, int nnl, int nm, const double *L,
                              const double *A, double *psd);
-cudaError_t launch_force_psd32(cudaStream_t st, int nf, int ntc, int nnl, int nm, const double *L,
+cudaError_t launch_force_psd32(cudaStream_t st, int nf, int ntc, int nnl, int nm, const float *L,
                                const float *A, double *psd);
 // Second-order moments over the grid frequencies k in [k0, k1); diag != 0 for the
 // same-mode spectra psd[f][m].
