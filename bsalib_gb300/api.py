@@ -389,8 +389,17 @@ class Sweep:
         finally:
             s.close()
 
-    def run(self):
-        """Per case: dict(m3mf, m3mr, m2mr, ms); and the sweep's total device ms."""
+    def run(self, form: int = 1):
+        """Per case: dict(m3mf, m3mr, m2mr, ms); and the sweep's total device ms.  form 1: the
+        E form of the contraction for cases of at most 24 kept modes on odd grids (default);
+        0: the D1 / D3 form for every case."""
+        check(self.lib.bsa_gpu_setClassicForm(int(form)), "bsa_gpu_setClassicForm")
+        try:
+            return self._run()
+        finally:
+            check(self.lib.bsa_gpu_setClassicForm(1), "bsa_gpu_setClassicForm")
+
+    def _run(self):
         n3 = sum(n ** 3 for n in self.nm)
         n2 = sum(n ** 2 for n in self.nm)
         mf, mr, m2 = np.zeros(n3), np.zeros(n3), np.zeros(n2)

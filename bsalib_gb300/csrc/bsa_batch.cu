@@ -21,6 +21,7 @@
 #include <vector>
 
 #include "../../include/bsa_gpu.h"
+#include "bsa_eform.cuh"
 #include "bsa_engine.cuh"
 #include "bsa_epi.cuh"
 #include "bsa_kernels.cuh"
@@ -377,6 +378,256 @@ __global__ void k_batch_reduce(const CaseP *__restrict__ cases, const long long 
     m3mf[out_off[blockIdx.y] + x] = 2.0 * mf;
 }
 
+
+// E form over a work list (cases of at most 24 kept modes on odd whole grids with the
+// truncated sum): per (case, grid row p, row tile) item the row's units (pairs of N tiles of
+// columns q >= p) of bsa_classic_e.cu's pipeline, whose three epilogue warpgroups add the six
+// contributions of each E(f_p, f_q) element into the case's accumulators [9 kinds][NMT][Mp].
+// Only the U and G tables are read (no S table).
+template <int NMT>
+__global__ void __launch_bounds__(ecls::kThreads, 1)  // 14 warps: at most 128 registers a thread
+    k_bfm_e_batch(const __grid_constant__ CUtensorMap tmUh, const __grid_constant__ CUtensorMap tmUl,
+                  const __grid_constant__ CUtensorMap tmGh, const __grid_constant__ CUtensorMap tmGl, const BParams p) {
+    using namespace ecls;
+    constexpr int NC = kBN / NMT;
+    constexpr int BROWS = NC * NMT;
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint64_t *bars = (uint64_t *)(smem + ecls::kStages * ecls::kStageBytes);
+    uint64_t *full = bars, *empty = bars + ecls::kStages, *tfull = bars + 2 * ecls::kStages,
+             *tempty = bars + 2 * ecls::kStages + 2;
+    uint64_t *done = bars + 2 * ecls::kStages + 4;
+    uint32_t *tmem_slot = (uint32_t *)(bars + 2 * ecls::kStages + 5);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int *err = p.err;
+    if (blockIdx.x == 0 && threadIdx.x == 0) *p.t_start = gtime();
+
+    for (int s = 0; s < ecls::kStages; ++s)
+        for (int t = 2; t < 6; ++t) {
+            uint8_t *tile = smem + s * ecls::kStageBytes + t * kTileBytes;
+            for (int x = threadIdx.x; x < (128 - BROWS) * 128 / 16; x += blockDim.x)
+                ((uint4 *)(tile + BROWS * 128))[x] = make_uint4(0, 0, 0, 0);
+        }
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < ecls::kStages; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(&tfull[b], 1);
+            mbar_init(&tempty[b], kEpi);
+        }
+        mbar_init(done, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(su32(tmem_slot)) : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = *tmem_slot;
+    const uint32_t tx_bytes = 2u * kTileBytes + 4u * (uint32_t)(BROWS * 128);
+
+    if (warp == 0) {
+        // ---------------- TMA producer ----------------
+        if (lane == 0) {
+            uint32_t it = 0;
+            bool ok = true;
+            for (int w = blockIdx.x; w < p.nitems && ok; w += gridDim.x) {
+                const BItem im = p.items[w];
+                const CaseP cs = p.cases[im.c];
+                const int nu = n_units(im.r, cs.n_ntiles, NC), nt0 = im.r / NC;
+                const int yu = cs.u_row0 + im.r * cs.Mp + im.mt * kBM;
+                for (int u = 0; u < nu && ok; ++u)
+                    for (int kc = 0; kc < cs.nk && ok; ++kc, ++it) {
+                        const int s = it % ecls::kStages;
+                        const uint32_t ph = (it / ecls::kStages) & 1u;
+                        if (!mbar_wait(&empty[s], ph ^ 1u, err, 1)) { ok = false; break; }
+                        uint8_t *st = smem + s * ecls::kStageBytes;
+                        mbar_expect_tx(&full[s], tx_bytes);
+                        const int x = kc * kBK;
+                        // rows past the case's columns read the next case's rows (masked)
+                        const int yg = cs.g_row0 + (nt0 + 2 * u) * BROWS;
+                        tma_2d(st + 0 * kTileBytes, &tmUh, &full[s], x, yu);
+                        tma_2d(st + 1 * kTileBytes, &tmUl, &full[s], x, yu);
+                        tma_2d(st + 2 * kTileBytes, &tmGh, &full[s], x, yg);
+                        tma_2d(st + 4 * kTileBytes, &tmGl, &full[s], x, yg);
+                        tma_2d(st + 3 * kTileBytes, &tmGh, &full[s], x, yg + BROWS);
+                        tma_2d(st + 5 * kTileBytes, &tmGl, &full[s], x, yg + BROWS);
+                    }
+            }
+            const uint32_t last = it;
+            for (uint32_t q = (last > (uint32_t)ecls::kStages ? last - ecls::kStages : 0); q < last; ++q) {
+                const int s = q % ecls::kStages;
+                const uint32_t ph = (q / ecls::kStages) & 1u;
+                const uint64_t t0 = gtime();
+                while (!mbar_try(&full[s], ph) && gtime() - t0 < kWaitNs) {
+                }
+            }
+        }
+        __syncwarp();
+    } else if (warp == 1) {
+        // ---------------- MMA issuer ----------------
+        if (lane == 0) {
+            uint32_t it = 0, tile = 0;
+            bool ok = true;
+            for (int w = blockIdx.x; w < p.nitems && ok; w += gridDim.x) {
+                const BItem im = p.items[w];
+                const CaseP cs = p.cases[im.c];
+                const int nu = n_units(im.r, cs.n_ntiles, NC);
+                for (int u = 0; u < nu && ok; ++u, ++tile) {
+                    const int buf = tile & 1;
+                    const uint32_t tph = (tile >> 1) & 1u;
+                    if (!mbar_wait(&tempty[buf], tph ^ 1u, err, 2)) { ok = false; break; }
+                    fence_after();
+                    const uint32_t d = tmem + buf * 256;
+                    for (int kc = 0; kc < cs.nk; ++kc, ++it) {
+                        const int s = it % ecls::kStages;
+                        const uint32_t ph = (it / ecls::kStages) & 1u;
+                        if (!mbar_wait(&full[s], ph, err, 3)) { ok = false; break; }
+                        fence_after();
+                        const uint32_t base = su32(smem + s * ecls::kStageBytes);
+                        const int nks = kc == cs.nk - 1 ? cs.ks_last : kBK / 16;
+                        for (int ks = 0; ks < nks; ++ks) {
+                            const uint32_t off = ks * 32;
+                            const uint64_t uh = sdesc(base + 0 * kTileBytes + off), ul = sdesc(base + 1 * kTileBytes + off);
+                            const uint64_t bh = sdesc(base + 2 * kTileBytes + off), bl = sdesc(base + 4 * kTileBytes + off);
+                            const uint32_t acc = (kc > 0 || ks > 0) ? 1u : 0u;
+                            mma256(d, uh, bh, acc);
+                            mma256(d, uh, bl, 1u);
+                            mma256(d, ul, bh, 1u);
+                        }
+                        mma_commit(&empty[s]);
+                    }
+                    if (!ok) break;
+                    mma_commit(&tfull[buf]);
+                }
+            }
+            mma_commit(done);
+            const uint64_t t0 = gtime();
+            while (!mbar_try(done, 0) && gtime() - t0 < kWaitNs) {
+            }
+        }
+        __syncwarp();
+    } else {
+        // ---------------- three epilogue warpgroups ----------------
+        // After a failed wait a warp walks the unit sequence without work, so every warp
+        // reaches every epi_sync384.
+        const int wg = (warp - 2) >> 2;
+        const int quarter = warp & 3;
+        const int et = threadIdx.x - 64;
+        const int row = quarter * 32 + lane;
+        const uint32_t lane_base = tmem + ((uint32_t)(quarter * 32) << 16);
+        using UT = UTile<NMT>;
+        UT *hbs = (UT *)(smem + ecls::kStages * ecls::kStageBytes + ecls::kBarBytes);
+        const int k0 = wg * kKindsWG;
+        float acc[kKindsWG][NMT];
+#pragma unroll
+        for (int k = 0; k < kKindsWG; ++k)
+#pragma unroll
+            for (int j = 0; j < NMT; ++j) acc[k][j] = 0.f;
+        // FRF staging of unit u of item im
+        auto stage = [&](UT *dst, const BItem &im, int u) {
+            const CaseP c = p.cases[im.c];
+            EParams ep{};
+            ep.nf = c.nf;
+            ep.h = (c.nf - 1) / 2;
+            ep.Hg = p.Hg + c.hg0;
+            ep.Hs = p.Hs + c.hs0;
+            stage_unit<NMT>(dst, ep, im.r, im.r / NC + 2 * u, et, kEpi);
+        };
+        uint32_t tile = 0;
+        bool ok = true;
+        if (blockIdx.x < p.nitems) stage(hbs, p.items[blockIdx.x], 0);
+        for (int w = blockIdx.x; w < p.nitems; w += gridDim.x) {
+            const BItem im = p.items[w];
+            const CaseP *csp = p.cases + im.c;  // fields read where used (register pressure)
+            const int r = im.r;
+            const int grow = im.mt * kBM + row;
+            const int nm = csp->nm;
+            const bool vrow = grow < nm * nm;
+            const int a = vrow ? grow / nm : 0, b = vrow ? grow % nm : 0;
+            const float wv = (float)csp->wval;
+            const bool vect = csp->wmode == kWeightClassicVect;
+            EParams ep{};
+            ep.nf = csp->nf;
+            ep.h = (ep.nf - 1) / 2;
+            const int nu = n_units(r, csp->n_ntiles, NC), nt0 = r / NC;
+            int since = 0;
+            for (int u = 0; u < nu; ++u, ++tile) {
+                const int buf = tile & 1;
+                const uint32_t tph = (tile >> 1) & 1u;
+                epi::cp_async_wait_all();
+                epi_sync384();  // this unit's values are in; the other slot is free
+                if (u + 1 < nu)
+                    stage(hbs + (buf ^ 1), im, u + 1);
+                else if (w + (int)gridDim.x < p.nitems)
+                    stage(hbs + (buf ^ 1), p.items[w + gridDim.x], 0);
+                if (!ok) continue;
+                ok = __all_sync(0xffffffffu, mbar_wait(&tfull[buf], tph, err, 4));
+                if (!ok) continue;
+                fence_after();
+                const UT &hb = hbs[buf];
+                const int q0 = (nt0 + 2 * u) * NC;
+                for (int h2 = 0; h2 < 2; ++h2)
+                    unit_half<NMT>(hb, lane_base + buf * 256 + h2 * 128, wg, a, b, r, q0, h2 * NC, ep, vect, wv, acc);
+                fence_before();
+                mbar_arrive(&tempty[buf]);
+                since += 2;
+                // flush at the end of every item (the next item may be another case's, or
+                // leave this lane without a row)
+                if (since >= kFlushTiles || u + 1 == nu) {
+                    const int Mp = csp->Mp;
+                    double *part = p.part + csp->part0 + grow;
+#pragma unroll
+                    for (int k = 0; k < kKindsWG; ++k)
+#pragma unroll
+                        for (int j = 0; j < NMT; ++j) {
+                            if (vrow && acc[k][j] != 0.f)
+                                atomicAdd(part + (size_t)((k0 + k) * NMT + j) * Mp, (double)acc[k][j]);
+                            acc[k][j] = 0.f;
+                        }
+                    since = 0;
+                }
+            }
+            if (!ok) continue;
+            // this warp's share of the item is in the accumulators: count it, stamp the case
+            __syncwarp();
+            if (lane == 0) {
+                __threadfence();
+                const unsigned old = atomicAdd(p.done_cnt + im.c, 1u);
+                if (old + 1 == 12u * csp->nitems) p.t_done[im.c] = gtime();
+            }
+        }
+        epi::cp_async_wait_all();
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem) : "memory");
+}
+
+// m3 of case c from the E-form accumulators (kinds: 0 K_i, 1 K_iv, 2 F14, 3 K_iii, 4 K_v,
+// 5 F35, 6 K_ii, 7 K_vi, 8 F26, each at the lane's (a, b) and j).
+template <int NMT>
+__global__ void k_batch_reduce_e(const CaseP *__restrict__ cases, const long long *__restrict__ out_off,
+                                 const double *__restrict__ part, double *__restrict__ m3mf, double *__restrict__ m3mr) {
+    const CaseP cs = cases[blockIdx.y];
+    const int nm = cs.nm, nm3 = nm * nm * nm;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= nm3) return;
+    const int m = x % nm, n = (x / nm) % nm, o = x / (nm * nm);
+    const double *pc = part + cs.part0;
+    auto s = [&](int kind, int aa, int bb, int j) { return pc[(size_t)(kind * NMT + j) * cs.Mp + aa * nm + bb]; };
+    const double mr = s(0, m, n, o) + s(1, m, o, n) + s(3, o, n, m) + s(4, n, o, m) + s(6, n, m, o) + s(7, o, m, n);
+    const double mf = s(2, m, n, o) + s(2, m, o, n) + s(5, o, n, m) + s(5, n, o, m) + s(8, n, m, o) + s(8, o, m, n);
+    m3mr[out_off[blockIdx.y] + x] = 2.0 * mr;  // B_F = 2 (T1 + T2 + T3)
+    m3mf[out_off[blockIdx.y] + x] = 2.0 * mf;
+}
+
 }  // namespace batch
 
 // ------------------------------------------------------------------------------------
@@ -459,9 +710,17 @@ int Engine::batch_run(double *m3mf, double *m3mr, double *m2mr, double *case_ms,
     auto nmt_of = [](int nm) { return nm <= 8 ? 8 : nm <= 16 ? 16 : nm <= 24 ? 24 : nm <= 32 ? 32 : 64; };
     std::vector<int> order(nc);
     for (int c = 0; c < nc; ++c) order[c] = c;
+    // E form (bsa_classic_e.cu) for cases of at most 24 kept modes on odd grids with the
+    // truncated sum; those form groups of their own
+    auto e_ok = [&](int c) {
+        const BatchCase &b = g_batch[c];
+        return use_e_form && b.nme <= 24 && b.trunc && (b.f.size() & 1) != 0;
+    };
     std::sort(order.begin(), order.end(), [&](int x, int y) {
         const int a = nmt_of(g_batch[x].nme), b = nmt_of(g_batch[y].nme);
-        return a != b ? a < b : g_batch[x].K < g_batch[y].K;
+        if (a != b) return a < b;
+        if (e_ok(x) != e_ok(y)) return e_ok(x);
+        return g_batch[x].K < g_batch[y].K;
     });
     // the caller's problem is put back once the sweep is done
     BatchCase saved;
@@ -495,16 +754,17 @@ int Engine::batch_run(double *m3mf, double *m3mr, double *m2mr, double *case_ms,
     while (g0 < order.size()) {
         const int Wd = nmt_of(g_batch[order[g0]].nme);
         const int NMT = Wd > 32 ? 32 : Wd, JH = Wd / NMT;
+        const bool eform = e_ok(order[g0]);
         size_t g1 = g0;
         double rows = 0.0;
-        while (g1 < order.size() && nmt_of(g_batch[order[g1]].nme) == Wd) {
+        while (g1 < order.size() && nmt_of(g_batch[order[g1]].nme) == Wd && e_ok(order[g1]) == eform) {
             // U, G and S rows of the case; hi + lo bf16 at the group's K stride, which is
             // this case's (the group is in K order)
             const BatchCase &c = g_batch[order[g1]];
             const double Kp = (double)(((c.K + kBK - 1) / kBK) * kBK);
             const double Mp = (double)(((c.nme * c.nme + kBM - 1) / kBM) * kBM);
             const double nf = (double)c.f.size();
-            const double add = nf * Mp + (double)JH * (3 * nf - 1) * NMT;
+            const double add = nf * Mp + (double)JH * (eform ? nf : 3 * nf - 1) * NMT;
             if (g1 > g0 && 4.0 * Kp * (rows + add) > budget) break;
             rows += add;
             ++g1;
@@ -541,10 +801,10 @@ int Engine::batch_run(double *m3mf, double *m3mr, double *m2mr, double *case_ms,
             q.nitems = (unsigned)(nf * q.MT);
             urows += (long long)nf * q.Mp;
             grows += (long long)JH * nf * NMT;
-            srows += (long long)JH * (2 * nf - 1) * NMT;
+            if (!eform) srows += (long long)JH * (2 * nf - 1) * NMT;
             hg += (long long)nf * Wd;
             hs += (long long)(2 * nf - 1) * Wd;
-            parts += (long long)(Wd <= 24 ? kKinds + 2 : kKinds) * Wd * q.Mp;
+            parts += (long long)(eform ? ecls::kKinds : Wd <= 24 ? kKinds + 2 : kKinds) * Wd * q.Mp;
             for (int r = 0; r < nf; ++r)
                 for (int mt = 0; mt < q.MT; ++mt) items.push_back(BItem{(int)(k - g0), r, mt, 0});
         }
@@ -596,8 +856,8 @@ int Engine::batch_run(double *m3mf, double *m3mr, double *m2mr, double *case_ms,
                 const size_t os = ((size_t)q.s_row0 + (size_t)jh * (2 * nf - 1) * NMT) * Kp;
                 if ((e = mixed::prep_b(stream, nf, c.nme, NMT, jh * NMT, c.K, Kp, nf, (nf - 1) / 2, c.trunc ? 1 : 0, nf,
                                        0, A, Gh + og, Gl + og)) ||
-                    (e = mixed::prep_b(stream, 2 * nf - 1, c.nme, NMT, jh * NMT, c.K, Kp, nf, (nf - 1) / 2,
-                                       c.trunc ? 1 : 0, nf, 1, A, Sh + os, Sl + os)))
+                    (!eform && (e = mixed::prep_b(stream, 2 * nf - 1, c.nme, NMT, jh * NMT, c.K, Kp, nf, (nf - 1) / 2,
+                                       c.trunc ? 1 : 0, nf, 1, A, Sh + os, Sl + os))))
                     return cuda_fail(e, "batch operand preparation");
             }
             // second-order moments (FP64 over the FP32 A table), rectangle or trapezoid weights
@@ -614,7 +874,7 @@ int Engine::batch_run(double *m3mf, double *m3mr, double *m2mr, double *case_ms,
                 (e = launch_m2(stream, 0, nf, c.nme, 0, dFreq.as<double>(), dWf.as<double>(), dPsdF.as<double>(), frf(),
                                m2o, m2o + nm2, m2o + 2 * nm2)))
                 return cuda_fail(e, "batch m2");
-            kernels += 4 + 2 * JH;
+            kernels += 4 + (eform ? 1 : 2) * JH;
         }
         std::vector<long long> offs(cp.size());
         for (size_t k = g0; k < g1; ++k) offs[k - g0] = off3[order[k]];
@@ -626,7 +886,8 @@ int Engine::batch_run(double *m3mf, double *m3mr, double *m2mr, double *case_ms,
         const int BROWS = (kBN / NMT) * NMT;
         if (!make_map(&maps[0], Uh, Kp, (uint64_t)urows, kBM) || !make_map(&maps[1], Ul, Kp, (uint64_t)urows, kBM) ||
             !make_map(&maps[2], Gh, Kp, (uint64_t)grows, BROWS) || !make_map(&maps[3], Gl, Kp, (uint64_t)grows, BROWS) ||
-            !make_map(&maps[4], Sh, Kp, (uint64_t)srows, BROWS) || !make_map(&maps[5], Sl, Kp, (uint64_t)srows, BROWS))
+            (!eform && (!make_map(&maps[4], Sh, Kp, (uint64_t)srows, BROWS) ||
+                        !make_map(&maps[5], Sl, Kp, (uint64_t)srows, BROWS))))
             return fail(BSA_ERR_CUDA, "cuTensorMapEncodeTiled failed");
         BParams prm{d_items, (int)items.size(), d_cases, Hg, Hs, part, d_cnt, d_tdone, d_tstart, derr};
         const size_t smem = kSmem;
@@ -636,7 +897,17 @@ int Engine::batch_run(double *m3mf, double *m3mr, double *m2mr, double *case_ms,
             cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             kern<<<grid, 192, smem, stream>>>(maps[0], maps[1], maps[2], maps[3], maps[4], maps[5], prm);
         };
-        switch (Wd) {
+        auto launch_e = [&](auto kern, size_t ut) {
+            const size_t sm = (size_t)ecls::kStages * ecls::kStageBytes + 1024 + ecls::kBarBytes + 2 * ut;
+            cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+            kern<<<grid, ecls::kThreads, sm, stream>>>(maps[0], maps[1], maps[2], maps[3], prm);
+        };
+        if (eform) switch (Wd) {
+        case 8: launch_e(k_bfm_e_batch<8>, sizeof(ecls::UTile<8>)); break;
+        case 16: launch_e(k_bfm_e_batch<16>, sizeof(ecls::UTile<16>)); break;
+        default: launch_e(k_bfm_e_batch<24>, sizeof(ecls::UTile<24>)); break;
+        }
+        else switch (Wd) {
         case 8: launch(k_bfm_batch<8, 1, true>); break;
         case 16: launch(k_bfm_batch<16, 1, true>); break;
         case 24: launch(k_bfm_batch<24, 1, true>); break;
@@ -651,7 +922,12 @@ int Engine::batch_run(double *m3mf, double *m3mr, double *m2mr, double *case_ms,
         int maxnm3 = 1;
         for (const CaseP &q : cp) maxnm3 = std::max(maxnm3, q.nm * q.nm * q.nm);
         dim3 rg((maxnm3 + 127) / 128, (unsigned)cp.size());
-        switch (Wd) {
+        if (eform) switch (Wd) {
+        case 8: k_batch_reduce_e<8><<<rg, 128, 0, stream>>>(d_cases, d_off, part, o, o + t3); break;
+        case 16: k_batch_reduce_e<16><<<rg, 128, 0, stream>>>(d_cases, d_off, part, o, o + t3); break;
+        default: k_batch_reduce_e<24><<<rg, 128, 0, stream>>>(d_cases, d_off, part, o, o + t3); break;
+        }
+        else switch (Wd) {
         case 8: k_batch_reduce<8, kKinds + 2><<<rg, 128, 0, stream>>>(d_cases, d_off, part, o, o + t3); break;
         case 16: k_batch_reduce<16, kKinds + 2><<<rg, 128, 0, stream>>>(d_cases, d_off, part, o, o + t3); break;
         case 24: k_batch_reduce<24, kKinds + 2><<<rg, 128, 0, stream>>>(d_cases, d_off, part, o, o + t3); break;

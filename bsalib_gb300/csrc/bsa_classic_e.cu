@@ -37,6 +37,7 @@
 
 #include "../../include/bsa_gpu.h"
 #include "bsa_engine.cuh"
+#include "bsa_eform.cuh"
 #include "bsa_epi.cuh"
 #include "bsa_mixed.cuh"
 #include "bsa_tc.cuh"
@@ -45,165 +46,6 @@ namespace bsa {
 namespace ecls {
 
 using namespace tc;
-
-constexpr int kStages = 2;
-constexpr int kStageBytes = 6 * kTileBytes;  // U hi, U lo, B0 hi, B1 hi, B0 lo, B1 lo
-constexpr int kKindsWG = 3;  // per epilogue warpgroup: two response kinds and one force kind
-constexpr int kKinds = 3 * kKindsWG;  // 0 K_i, 1 K_iv, 2 F14, 3 K_iii, 4 K_v, 5 F35, 6 K_ii, 7 K_vi, 8 F26
-constexpr int kFlushTiles = 64;
-constexpr int kBarBytes = 256;
-constexpr int kThreads = 448;  // TMA warp, MMA warp, 3 x 4 epilogue warps
-constexpr int kEpi = 384;
-
-// FRF values of one unit (row p, columns q0 .. q0 + 2 NC - 1): H_j at the row, and per
-// column H_j(v), H_j(u + v), H_j(v - u), H_j(u - v).
-template <int NMT>
-struct UTile {
-    static constexpr int NC2 = 2 * (kBN / NMT);
-    float2 hr[NMT];
-    float2 hg[NC2 * NMT];
-    float2 hs[NC2 * NMT];
-    float2 hdp[NC2 * NMT];
-    float2 hdm[NC2 * NMT];
-};
-
-struct EParams {
-    int nf, h, nm, Mp, MT, nk, ks_last, n_ntiles;
-    int wmode;
-    double wval;
-    const float2 *Hg;  // [nf][NMT]
-    const float2 *Hs;  // [2 nf - 1][NMT]
-    double *part;      // [grid][kKinds][NMT][128]
-    int *err;
-};
-
-// Shared-memory float2 load the compiler does not hoist (keeps the per-mode FRF values out
-// of the registers the accumulators need).
-__device__ __forceinline__ float2 lds2(const float2 *p) {
-    float2 r;
-    asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(r.x), "=f"(r.y) : "r"(su32(p)));
-    return r;
-}
-
-__device__ __forceinline__ void epi_sync384() { asm volatile("bar.sync 1, 384;" ::: "memory"); }
-
-// Units of grid row p: pairs of N tiles from the one holding column p (columns q < p masked).
-__device__ __forceinline__ int n_units(int p, int ntl, int NC) { return (ntl - p / NC + 1) / 2; }
-
-// Integration weight of grid point (r, c) (intgSpectraVect_, BsaClassicImpl.F90:596-632, with
-// the reference's vertex weight -d^2 / 2).
-__device__ __forceinline__ float wpt(int r, int c, int nf, bool vect, float wv) {
-    if (!vect) return wv;
-    const bool b1 = r == 0 || r == nf - 1, b2 = c == 0 || c == nf - 1;
-    return wv * ((b1 && b2) ? -0.5f : ((b1 || b2) ? 0.5f : 1.f));
-}
-
-// Stage unit (p, N tiles nt, nt + 1) with threads t < nt_ (cp.async, zero where out of range).
-template <int NMT>
-__device__ __forceinline__ void stage_unit(UTile<NMT> *dst, const EParams &P, int p, int nt, int t, int nt_) {
-    constexpr int NC = kBN / NMT, NC2 = 2 * NC, CH = NMT / 2;  // 16-byte chunks per column row
-    const int q0 = nt * NC;
-    const int nch = CH + 4 * NC2 * CH;
-    for (int x = t; x < nch; x += nt_) {
-        if (x < CH) {
-            epi::cp_async16(dst->hr + 2 * x, P.Hg + (size_t)p * NMT + 2 * x, true);
-            continue;
-        }
-        const int y = x - CH, which = y / (NC2 * CH), z = y - which * NC2 * CH, cc = z / CH, k = z - cc * CH;
-        const int q = q0 + cc;
-        int row;
-        bool v;
-        float2 *d;
-        const float2 *tab = P.Hg;
-        if (which == 0) {
-            row = q;
-            v = q < P.nf;
-            d = dst->hg;
-        } else if (which == 1) {
-            row = p + q;
-            v = row <= 2 * P.nf - 2;
-            tab = P.Hs;
-            d = dst->hs;
-        } else if (which == 2) {
-            row = q - p + P.h;
-            v = row >= 0 && row < P.nf;
-            d = dst->hdp;
-        } else {
-            row = p - q + P.h;
-            v = row >= 0 && row < P.nf;
-            d = dst->hdm;
-        }
-        epi::cp_async16(d + cc * NMT + 2 * k, v ? (const void *)(tab + (size_t)row * NMT + 2 * k) : (const void *)tab,
-                        v);
-    }
-    epi::cp_async_commit();
-}
-
-// One N tile of a unit (TMEM columns taddr .. taddr + 127): grid columns q = q0 + slot0 + ci,
-// staged at column slot slot0 + ci.  Warpgroup wg accumulates kinds 3 wg .. 3 wg + 2:
-//   wg 0: (i)   Re[w_pq H_a(u) H_b(v) conj H_j(u+v)],   (iv) Re[w_pq H_a(v) conj H_b(u+v) H_j(u)],   w_pq
-//   wg 1: (iii) Re[w_pc H_b(v-u) conj H_a(v) H_j(u)],   (v)  Re[w_pc H_a(u) conj H_b(v) H_j(v-u)],   w_pc
-//   wg 2: (ii)  Re[w_dq H_b(u-v) H_a(v) conj H_j(u)],   (vi) Re[w_dq H_b(v) conj H_a(u) H_j(u-v)],   w_dq
-// each times x.  One code path for the three (the per-column setup picks the factors and the
-// staged rows; a conj on H_j is folded into the factor), so the three warpgroups share one
-// instruction stream.
-template <int NMT>
-__device__ __forceinline__ void unit_half(const UTile<NMT> &hb, uint32_t taddr, int wg, int a, int b, int p,
-                                          int q0, int slot0, const EParams &P, bool vect, float wv,
-                                          float (&acc)[kKindsWG][NMT]) {
-    constexpr int NC = kBN / NMT;
-    const float2 hra = hb.hr[a];
-#pragma unroll
-    for (int qc = 0; qc < kBN / 16; ++qc) {
-        uint32_t v[16];
-        tmem_ld16(taddr + qc * 16, v);
-        tmem_wait_ld();
-        float2 P1 = make_float2(0.f, 0.f), P2 = P1;
-        float wk = 0.f;
-        const float2 *X = hb.hr, *Y = hb.hr;  // per-mode factors of the two response kinds
-#pragma unroll
-        for (int e = 0; e < 16; ++e) {
-            const int col = qc * 16 + e;
-            const int ci = col / NMT, j = col % NMT;
-            if (ci >= NC) continue;
-            if (j == 0 || e == 0) {
-                const int sl = (slot0 + ci) * NMT;
-                const int q = q0 + slot0 + ci;
-                const bool valid = q >= p && q < P.nf;
-                const bool vd = valid && q - p <= P.h;
-                const float dl = q == p ? 0.5f : 1.f;
-                const float2 Hbv = hb.hg[sl + b], Hav = hb.hg[sl + a];
-                float2 t1, t2;
-                if (wg == 0) {
-                    wk = valid ? dl * wpt(p, q, P.nf, vect, wv) : 0.f;
-                    t1 = conjf2(cmul(hra, Hbv));               // conj: pairs with conj H_j(u+v)
-                    t2 = cmul(Hav, conjf2(hb.hs[sl + b]));
-                    X = hb.hs + sl;
-                    Y = hb.hr;
-                } else if (wg == 1) {
-                    wk = vd ? dl * wpt(p, q - p + P.h, P.nf, vect, wv) : 0.f;
-                    t1 = cmul(hb.hdp[sl + b], conjf2(Hav));
-                    t2 = cmul(hra, conjf2(Hbv));
-                    X = hb.hr;
-                    Y = hb.hdp + sl;
-                } else {
-                    wk = vd ? dl * wpt(p - q + P.h, q, P.nf, vect, wv) : 0.f;
-                    t1 = conjf2(cmul(hb.hdm[sl + b], Hav));    // conj: pairs with conj H_j(u)
-                    t2 = cmul(Hbv, conjf2(hra));
-                    X = hb.hr;
-                    Y = hb.hdm + sl;
-                }
-                P1 = make_float2(wk * t1.x, wk * t1.y);
-                P2 = make_float2(wk * t2.x, wk * t2.y);
-            }
-            const float x = __uint_as_float(v[e]);
-            const float2 xj = lds2(X + j), yj = lds2(Y + j);
-            acc[0][j] = fmaf(P1.x * xj.x - P1.y * xj.y, x, acc[0][j]);  // Re[P1 X_j]
-            acc[1][j] = fmaf(P2.x * yj.x - P2.y * yj.y, x, acc[1][j]);  // Re[P2 Y_j]
-            acc[2][j] = fmaf(wk, x, acc[2][j]);
-        }
-    }
-}
 
 template <int NMT>
 __global__ void __launch_bounds__(kThreads, 1)  // 14 warps: at most 128 registers a thread

@@ -1,11 +1,13 @@
 """The batched Classic sweep (bsa_gpu_batch*) against one bsa_Run per case.
 
 Each case of a batch must give the moments its own split-precision analysis gives.  Up to 24
-kept modes the single analysis uses the E form of the contraction (each product of one GEMM
-family feeding the three terms at up to six grid points) and the batch the D1 / D3 form: the
-same products summed in another order in FP32, so third moments agree to ~1e-6 (both lie
-~3e-6 from the FP64 path); the bar is 1e-5 relative (max-norm, 10x inside the split-precision
-bar).  Second moments agree to 1e-12.  Against the FP64 path the mixed-precision bar holds
+kept modes on odd grids both use the E form of the contraction (each product of one GEMM
+family feeding the three terms at up to six grid points); the batch flushes its FP32 partials
+at other points and adds them with atomics, so third moments agree to ~1e-7.  The batch's
+D1 / D3 form (`Sweep.run(form=0)`, and every case above 24 modes or on an even grid) sums the
+same products in another order: ~1e-6 from the E form (both lie ~3e-6 from the FP64 path).
+The bar is 1e-5 relative (max-norm, 10x inside the split-precision bar).  Second moments
+agree to 1e-12.  Against the FP64 path the mixed-precision bar holds
 (third moments 1e-4 relative).  Cases of every FRF-table width (8, 16, 24, 32 kept modes, and
 two halves of 32 above that),
 different grids and load sizes share one batch; the library's own inputs are left as they
@@ -68,6 +70,21 @@ def test_batch_matches_single_analyses(batch):
         assert rel(out[k]["m3mr"], ref["m3mr_cls"]) < 1e-5, k
         assert rel(out[k]["m3mf"], ref["m3mf_cls"]) < 1e-5, k
         assert rel(out[k]["m2mr"], ref["m2mr_cls"]) < 1e-12, k
+
+
+def test_batch_d_form_matches_the_e_form(bsalib, batch):
+    """The whole batch again in the D1 / D3 form (k_bfm_batch with symmetric D1 up to 24
+    modes): the same moments to the split-precision reassociation."""
+    out, _ = batch
+    sw = api.Sweep()
+    for p in CASES:
+        sw.add(p)
+    outd, _ = sw.run(form=0)
+    sw.clear()
+    for k in range(len(CASES)):
+        assert rel(outd[k]["m3mr"], out[k]["m3mr"]) < 1e-5, k
+        assert rel(outd[k]["m3mf"], out[k]["m3mf"]) < 1e-5, k
+        assert rel(outd[k]["m2mr"], out[k]["m2mr"]) < 1e-12, k
 
 
 def test_batch_within_mixed_bar_of_fp64(batch):
