@@ -369,7 +369,9 @@ def run_ours(args):
            "evaluated_points_per_s": sym_pts / (float(np.mean(sym_ms)) / 1e3),
            "m3mr_rel_vs_full_grid": float(np.max(np.abs(rs["m3mr_cls"] - r["m3mr_cls"])) /
                                           np.max(np.abs(r["m3mr_cls"]))),
-           "note": "bsa_gpu_setClassicSymmetry: rows f1 <= 0 only, mirrored weights; not the headline"}
+           "note": ("bsa_gpu_setClassicSymmetry: rows f1 <= 0 only, mirrored weights, in the D1 / D3 form; "
+                    "where the E form applies (at most 48 kept modes, as here) it already forms each distinct "
+                    "product once and the setting leaves the whole grid to it; not the headline")}
     s.close()
 
     # ---- e2e: the public call sequence with host buffers, per step ----

@@ -332,8 +332,9 @@ class BsaSession:
         return rc, g, pos, neg
 
     def set_export(self, fn):
-        """bsa_setBispExportCallback: fn(f1, f2, brm[npts][dim_bisp]) receives the Classic
-        response bispectra during run(); None switches the export off."""
+        """bsa_setBispExportCallback: fn(f1, f2, brm[npts][dim_bisp]) receives the response
+        bispectra during run(): the Classic grid in column blocks, the Mesher's BRM lattice one
+        zone at a time; None switches the export off."""
         if fn is None:
             self._export = None
             check(self.lib.bsa_setBispExportCallback(C.cast(None, EXPORT_FN), None), "bsa_setBispExportCallback")

@@ -379,18 +379,19 @@ __global__ void k_batch_reduce(const CaseP *__restrict__ cases, const long long 
 }
 
 
-// E form over a work list (cases of at most 24 kept modes on odd whole grids with the
+// E form over a work list (cases of at most 48 kept modes on odd whole grids with the
 // truncated sum): per (case, grid row p, row tile) item the row's units (pairs of N tiles of
-// columns q >= p) of bsa_classic_e.cu's pipeline, whose three epilogue warpgroups add the six
-// contributions of each E(f_p, f_q) element into the case's accumulators [9 kinds][NMT][Mp].
-// Only the U and G tables are read (no S table).
-template <int NMT>
+// columns q >= p, once per mode half) of bsa_classic_e.cu's pipeline, whose three epilogue
+// warpgroups add the six contributions of each E(f_p, f_q) element into the case's
+// accumulators [9 kinds][W][Mp].  Only the U and G tables are read (no S table).
+template <int NMT, int JH>
 __global__ void __launch_bounds__(ecls::kThreads, 1)  // 14 warps: at most 128 registers a thread
     k_bfm_e_batch(const __grid_constant__ CUtensorMap tmUh, const __grid_constant__ CUtensorMap tmUl,
                   const __grid_constant__ CUtensorMap tmGh, const __grid_constant__ CUtensorMap tmGl, const BParams p) {
     using namespace ecls;
     constexpr int NC = kBN / NMT;
     constexpr int BROWS = NC * NMT;
+    constexpr int W = NMT * JH;
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint64_t *bars = (uint64_t *)(smem + ecls::kStages * ecls::kStageBytes);
@@ -441,6 +442,7 @@ __global__ void __launch_bounds__(ecls::kThreads, 1)  // 14 warps: at most 128 r
                 const CaseP cs = p.cases[im.c];
                 const int nu = n_units(im.r, cs.n_ntiles, NC), nt0 = im.r / NC;
                 const int yu = cs.u_row0 + im.r * cs.Mp + im.mt * kBM;
+                for (int jh = 0; jh < JH && ok; ++jh)
                 for (int u = 0; u < nu && ok; ++u)
                     for (int kc = 0; kc < cs.nk && ok; ++kc, ++it) {
                         const int s = it % ecls::kStages;
@@ -450,7 +452,7 @@ __global__ void __launch_bounds__(ecls::kThreads, 1)  // 14 warps: at most 128 r
                         mbar_expect_tx(&full[s], tx_bytes);
                         const int x = kc * kBK;
                         // rows past the case's columns read the next case's rows (masked)
-                        const int yg = cs.g_row0 + (nt0 + 2 * u) * BROWS;
+                        const int yg = cs.g_row0 + jh * cs.nf * NMT + (nt0 + 2 * u) * BROWS;
                         tma_2d(st + 0 * kTileBytes, &tmUh, &full[s], x, yu);
                         tma_2d(st + 1 * kTileBytes, &tmUl, &full[s], x, yu);
                         tma_2d(st + 2 * kTileBytes, &tmGh, &full[s], x, yg);
@@ -477,7 +479,7 @@ __global__ void __launch_bounds__(ecls::kThreads, 1)  // 14 warps: at most 128 r
             for (int w = blockIdx.x; w < p.nitems && ok; w += gridDim.x) {
                 const BItem im = p.items[w];
                 const CaseP cs = p.cases[im.c];
-                const int nu = n_units(im.r, cs.n_ntiles, NC);
+                const int nu = n_units(im.r, cs.n_ntiles, NC) * JH;  // units of every mode half
                 for (int u = 0; u < nu && ok; ++u, ++tile) {
                     const int buf = tile & 1;
                     const uint32_t tph = (tile >> 1) & 1u;
@@ -521,7 +523,7 @@ __global__ void __launch_bounds__(ecls::kThreads, 1)  // 14 warps: at most 128 r
         const int et = threadIdx.x - 64;
         const int row = quarter * 32 + lane;
         const uint32_t lane_base = tmem + ((uint32_t)(quarter * 32) << 16);
-        using UT = UTile<NMT>;
+        using UT = UTile<NMT, JH>;
         UT *hbs = (UT *)(smem + ecls::kStages * ecls::kStageBytes + ecls::kBarBytes);
         const int k0 = wg * kKindsWG;
         float acc[kKindsWG][NMT];
@@ -537,7 +539,7 @@ __global__ void __launch_bounds__(ecls::kThreads, 1)  // 14 warps: at most 128 r
             ep.h = (c.nf - 1) / 2;
             ep.Hg = p.Hg + c.hg0;
             ep.Hs = p.Hs + c.hs0;
-            stage_unit<NMT>(dst, ep, im.r, im.r / NC + 2 * u, et, kEpi);
+            stage_unit<NMT, JH>(dst, ep, im.r, im.r / NC + 2 * u, et, kEpi);
         };
         uint32_t tile = 0;
         bool ok = true;
@@ -557,6 +559,7 @@ __global__ void __launch_bounds__(ecls::kThreads, 1)  // 14 warps: at most 128 r
             ep.h = (ep.nf - 1) / 2;
             const int nu = n_units(r, csp->n_ntiles, NC), nt0 = r / NC;
             int since = 0;
+            for (int jh = 0; jh < JH; ++jh)
             for (int u = 0; u < nu; ++u, ++tile) {
                 const int buf = tile & 1;
                 const uint32_t tph = (tile >> 1) & 1u;
@@ -564,6 +567,8 @@ __global__ void __launch_bounds__(ecls::kThreads, 1)  // 14 warps: at most 128 r
                 epi_sync384();  // this unit's values are in; the other slot is free
                 if (u + 1 < nu)
                     stage(hbs + (buf ^ 1), im, u + 1);
+                else if (jh + 1 < JH)
+                    stage(hbs + (buf ^ 1), im, 0);
                 else if (w + (int)gridDim.x < p.nitems)
                     stage(hbs + (buf ^ 1), p.items[w + gridDim.x], 0);
                 if (!ok) continue;
@@ -573,12 +578,13 @@ __global__ void __launch_bounds__(ecls::kThreads, 1)  // 14 warps: at most 128 r
                 const UT &hb = hbs[buf];
                 const int q0 = (nt0 + 2 * u) * NC;
                 for (int h2 = 0; h2 < 2; ++h2)
-                    unit_half<NMT>(hb, lane_base + buf * 256 + h2 * 128, wg, a, b, r, q0, h2 * NC, ep, vect, wv, acc);
+                    unit_half<NMT, JH>(hb, lane_base + buf * 256 + h2 * 128, wg, a, b, r, q0, h2 * NC, ep, vect, wv, acc,
+                                       jh * NMT);
                 fence_before();
                 mbar_arrive(&tempty[buf]);
                 since += 2;
-                // flush at the end of every item (the next item may be another case's, or
-                // leave this lane without a row)
+                // flush at the end of every mode half of every item (the next item may be
+                // another case's, or leave this lane without a row)
                 if (since >= kFlushTiles || u + 1 == nu) {
                     const int Mp = csp->Mp;
                     double *part = p.part + csp->part0 + grow;
@@ -587,7 +593,7 @@ __global__ void __launch_bounds__(ecls::kThreads, 1)  // 14 warps: at most 128 r
 #pragma unroll
                         for (int j = 0; j < NMT; ++j) {
                             if (vrow && acc[k][j] != 0.f)
-                                atomicAdd(part + (size_t)((k0 + k) * NMT + j) * Mp, (double)acc[k][j]);
+                                atomicAdd(part + (size_t)((k0 + k) * W + jh * NMT + j) * Mp, (double)acc[k][j]);
                             acc[k][j] = 0.f;
                         }
                     since = 0;
@@ -612,7 +618,7 @@ __global__ void __launch_bounds__(ecls::kThreads, 1)  // 14 warps: at most 128 r
 
 // m3 of case c from the E-form accumulators (kinds: 0 K_i, 1 K_iv, 2 F14, 3 K_iii, 4 K_v,
 // 5 F35, 6 K_ii, 7 K_vi, 8 F26, each at the lane's (a, b) and j).
-template <int NMT>
+template <int W>
 __global__ void k_batch_reduce_e(const CaseP *__restrict__ cases, const long long *__restrict__ out_off,
                                  const double *__restrict__ part, double *__restrict__ m3mf, double *__restrict__ m3mr) {
     const CaseP cs = cases[blockIdx.y];
@@ -621,7 +627,7 @@ __global__ void k_batch_reduce_e(const CaseP *__restrict__ cases, const long lon
     if (x >= nm3) return;
     const int m = x % nm, n = (x / nm) % nm, o = x / (nm * nm);
     const double *pc = part + cs.part0;
-    auto s = [&](int kind, int aa, int bb, int j) { return pc[(size_t)(kind * NMT + j) * cs.Mp + aa * nm + bb]; };
+    auto s = [&](int kind, int aa, int bb, int j) { return pc[(size_t)(kind * W + j) * cs.Mp + aa * nm + bb]; };
     const double mr = s(0, m, n, o) + s(1, m, o, n) + s(3, o, n, m) + s(4, n, o, m) + s(6, n, m, o) + s(7, o, m, n);
     const double mf = s(2, m, n, o) + s(2, m, o, n) + s(5, o, n, m) + s(5, n, o, m) + s(8, n, m, o) + s(8, o, m, n);
     m3mr[out_off[blockIdx.y] + x] = 2.0 * mr;  // B_F = 2 (T1 + T2 + T3)
@@ -710,14 +716,20 @@ int Engine::batch_run(double *m3mf, double *m3mr, double *m2mr, double *case_ms,
     auto nmt_of = [](int nm) { return nm <= 8 ? 8 : nm <= 16 ? 16 : nm <= 24 ? 24 : nm <= 32 ? 32 : 64; };
     std::vector<int> order(nc);
     for (int c = 0; c < nc; ++c) order[c] = c;
-    // E form (bsa_classic_e.cu) for cases of at most 24 kept modes on odd grids with the
+    // E form (bsa_classic_e.cu) for cases of at most 48 kept modes on odd grids with the
     // truncated sum; those form groups of their own
     auto e_ok = [&](int c) {
         const BatchCase &b = g_batch[c];
-        return use_e_form && b.nme <= 24 && b.trunc && (b.f.size() & 1) != 0;
+        return use_e_form && b.nme <= kEFormMaxModes && b.trunc && (b.f.size() & 1) != 0;
+    };
+    // group width: the FRF-table width of the D1 / D3 form, or of the E form (8, 16, 24; 32 and
+    // 48 as two mode halves of 16 and 24)
+    auto width = [&](int c) {
+        const int nm = g_batch[c].nme;
+        return e_ok(c) ? (nm <= 8 ? 8 : nm <= 16 ? 16 : nm <= 24 ? 24 : nm <= 32 ? 32 : 48) : nmt_of(nm);
     };
     std::sort(order.begin(), order.end(), [&](int x, int y) {
-        const int a = nmt_of(g_batch[x].nme), b = nmt_of(g_batch[y].nme);
+        const int a = width(x), b = width(y);
         if (a != b) return a < b;
         if (e_ok(x) != e_ok(y)) return e_ok(x);
         return g_batch[x].K < g_batch[y].K;
@@ -752,12 +764,12 @@ int Engine::batch_run(double *m3mf, double *m3mr, double *m2mr, double *case_ms,
     const double budget = 24e9;
     size_t g0 = 0;
     while (g0 < order.size()) {
-        const int Wd = nmt_of(g_batch[order[g0]].nme);
-        const int NMT = Wd > 32 ? 32 : Wd, JH = Wd / NMT;
+        const int Wd = width(order[g0]);
         const bool eform = e_ok(order[g0]);
+        const int NMT = eform ? (Wd == 32 ? 16 : Wd == 48 ? 24 : Wd) : (Wd > 32 ? 32 : Wd), JH = Wd / NMT;
         size_t g1 = g0;
         double rows = 0.0;
-        while (g1 < order.size() && nmt_of(g_batch[order[g1]].nme) == Wd && e_ok(order[g1]) == eform) {
+        while (g1 < order.size() && width(order[g1]) == Wd && e_ok(order[g1]) == eform) {
             // U, G and S rows of the case; hi + lo bf16 at the group's K stride, which is
             // this case's (the group is in K order)
             const BatchCase &c = g_batch[order[g1]];
@@ -897,15 +909,17 @@ int Engine::batch_run(double *m3mf, double *m3mr, double *m2mr, double *case_ms,
             cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             kern<<<grid, 192, smem, stream>>>(maps[0], maps[1], maps[2], maps[3], maps[4], maps[5], prm);
         };
-        auto launch_e = [&](auto kern, size_t ut) {
+        auto launch_e = [&](auto kern, size_t ut) {  // UTile bytes ut: fits with the stages (static_assert in bsa_classic_e.cu)
             const size_t sm = (size_t)ecls::kStages * ecls::kStageBytes + 1024 + ecls::kBarBytes + 2 * ut;
             cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
             kern<<<grid, ecls::kThreads, sm, stream>>>(maps[0], maps[1], maps[2], maps[3], prm);
         };
         if (eform) switch (Wd) {
-        case 8: launch_e(k_bfm_e_batch<8>, sizeof(ecls::UTile<8>)); break;
-        case 16: launch_e(k_bfm_e_batch<16>, sizeof(ecls::UTile<16>)); break;
-        default: launch_e(k_bfm_e_batch<24>, sizeof(ecls::UTile<24>)); break;
+        case 8: launch_e(k_bfm_e_batch<8, 1>, sizeof(ecls::UTile<8, 1>)); break;
+        case 16: launch_e(k_bfm_e_batch<16, 1>, sizeof(ecls::UTile<16, 1>)); break;
+        case 24: launch_e(k_bfm_e_batch<24, 1>, sizeof(ecls::UTile<24, 1>)); break;
+        case 32: launch_e(k_bfm_e_batch<16, 2>, sizeof(ecls::UTile<16, 2>)); break;
+        default: launch_e(k_bfm_e_batch<24, 2>, sizeof(ecls::UTile<24, 2>)); break;
         }
         else switch (Wd) {
         case 8: launch(k_bfm_batch<8, 1, true>); break;
@@ -925,7 +939,9 @@ int Engine::batch_run(double *m3mf, double *m3mr, double *m2mr, double *case_ms,
         if (eform) switch (Wd) {
         case 8: k_batch_reduce_e<8><<<rg, 128, 0, stream>>>(d_cases, d_off, part, o, o + t3); break;
         case 16: k_batch_reduce_e<16><<<rg, 128, 0, stream>>>(d_cases, d_off, part, o, o + t3); break;
-        default: k_batch_reduce_e<24><<<rg, 128, 0, stream>>>(d_cases, d_off, part, o, o + t3); break;
+        case 24: k_batch_reduce_e<24><<<rg, 128, 0, stream>>>(d_cases, d_off, part, o, o + t3); break;
+        case 32: k_batch_reduce_e<32><<<rg, 128, 0, stream>>>(d_cases, d_off, part, o, o + t3); break;
+        default: k_batch_reduce_e<48><<<rg, 128, 0, stream>>>(d_cases, d_off, part, o, o + t3); break;
         }
         else switch (Wd) {
         case 8: k_batch_reduce<8, kKinds + 2><<<rg, 128, 0, stream>>>(d_cases, d_off, part, o, o + t3); break;

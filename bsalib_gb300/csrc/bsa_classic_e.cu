@@ -26,7 +26,8 @@
 // and their force moment, warps 6-9 (iii), (v) and theirs, warps 10-13 (ii), (vi) and theirs.  The FRF values a unit reads (H at the row, at the unit's columns, at
 // the row + column sums and at the column - row and row - column differences) are staged in
 // shared memory one unit ahead.  Used for whole-grid launches with the truncated sum, up to
-// 24 kept modes and no central symmetry; bsa_mixed.cu's form otherwise.
+// 48 kept modes (above 24 the G rows hold one half of the modes, JH = 2, and each unit is
+// swept once per half) and no central symmetry; bsa_mixed.cu's form otherwise.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -47,12 +48,13 @@ namespace ecls {
 
 using namespace tc;
 
-template <int NMT>
+template <int NMT, int JH>
 __global__ void __launch_bounds__(kThreads, 1)  // 14 warps: at most 128 registers a thread
     k_bfm_e(const __grid_constant__ CUtensorMap tmUh, const __grid_constant__ CUtensorMap tmUl,
             const __grid_constant__ CUtensorMap tmGh, const __grid_constant__ CUtensorMap tmGl, const EParams P) {
     constexpr int NC = kBN / NMT;
     constexpr int BROWS = NC * NMT;
+    constexpr int W = NMT * JH;
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint64_t *bars = (uint64_t *)(smem + kStages * kStageBytes);
@@ -102,6 +104,7 @@ __global__ void __launch_bounds__(kThreads, 1)  // 14 warps: at most 128 registe
             bool ok = true;
             for (int p = r0; p < P.nf && ok; p += rstep) {
                 const int nu = n_units(p, P.n_ntiles, NC), nt0 = p / NC;
+                for (int jh = 0; jh < JH && ok; ++jh)
                 for (int u = 0; u < nu && ok; ++u)
                     for (int kc = 0; kc < P.nk && ok; ++kc, ++it) {
                         const int s = it % kStages;
@@ -111,7 +114,9 @@ __global__ void __launch_bounds__(kThreads, 1)  // 14 warps: at most 128 registe
                         mbar_expect_tx(&full[s], tx_bytes);
                         const int x = kc * kBK;
                         const int yu = p * P.Mp + mt * kBM;
-                        const int yg = (nt0 + 2 * u) * BROWS;  // rows past the table read zeros
+                        // G rows of mode half jh; rows past a half's columns read the next
+                        // half's rows or zeros (masked in the epilogue)
+                        const int yg = jh * P.nf * NMT + (nt0 + 2 * u) * BROWS;
                         tma_2d(st + 0 * kTileBytes, &tmUh, &full[s], x, yu);
                         tma_2d(st + 1 * kTileBytes, &tmUl, &full[s], x, yu);
                         tma_2d(st + 2 * kTileBytes, &tmGh, &full[s], x, yg);
@@ -136,7 +141,7 @@ __global__ void __launch_bounds__(kThreads, 1)  // 14 warps: at most 128 registe
             uint32_t it = 0, tile = 0;
             bool ok = true;
             for (int p = r0; p < P.nf && ok; p += rstep) {
-                const int nu = n_units(p, P.n_ntiles, NC);
+                const int nu = n_units(p, P.n_ntiles, NC) * JH;  // units of every mode half
                 for (int u = 0; u < nu && ok; ++u, ++tile) {
                     const int buf = tile & 1;
                     const uint32_t tph = (tile >> 1) & 1u;
@@ -185,11 +190,11 @@ __global__ void __launch_bounds__(kThreads, 1)  // 14 warps: at most 128 registe
         const uint32_t lane_base = tmem + ((uint32_t)(quarter * 32) << 16);
         const float wv = (float)P.wval;
         const bool vect = P.wmode == kWeightClassicVect;
-        using UT = UTile<NMT>;
+        using UT = UTile<NMT, JH>;
         UT *hbs = (UT *)(smem + kStages * kStageBytes + kBarBytes);
-        double *part = P.part + (size_t)blockIdx.x * kKinds * NMT * 128 + row;
+        double *part = P.part + (size_t)blockIdx.x * kKinds * W * 128 + row;
         const int k0 = wg * kKindsWG;
-        for (int k = 0; k < kKindsWG * NMT; ++k) part[(size_t)(k0 * NMT + k) * 128] = 0.0;
+        for (int k = 0; k < kKindsWG * W; ++k) part[(size_t)(k0 * W + k) * 128] = 0.0;
         float acc[kKindsWG][NMT];
 #pragma unroll
         for (int k = 0; k < kKindsWG; ++k)
@@ -198,18 +203,21 @@ __global__ void __launch_bounds__(kThreads, 1)  // 14 warps: at most 128 registe
         uint32_t tile = 0;
         bool ok = true;
         int since = 0;
-        if (r0 < P.nf) stage_unit<NMT>(hbs, P, r0, r0 / NC, et, kEpi);
+        if (r0 < P.nf) stage_unit<NMT, JH>(hbs, P, r0, r0 / NC, et, kEpi);
         for (int p = r0; p < P.nf; p += rstep) {
             const int nu = n_units(p, P.n_ntiles, NC), nt0 = p / NC;
+            for (int jh = 0; jh < JH; ++jh)
             for (int u = 0; u < nu; ++u, ++tile) {
                 const int buf = tile & 1;
                 const uint32_t tph = (tile >> 1) & 1u;
                 epi::cp_async_wait_all();
                 epi_sync384();  // this unit's values are in; the other slot is free
                 if (u + 1 < nu)
-                    stage_unit<NMT>(hbs + (buf ^ 1), P, p, nt0 + 2 * (u + 1), et, kEpi);
+                    stage_unit<NMT, JH>(hbs + (buf ^ 1), P, p, nt0 + 2 * (u + 1), et, kEpi);
+                else if (jh + 1 < JH)
+                    stage_unit<NMT, JH>(hbs + (buf ^ 1), P, p, nt0, et, kEpi);
                 else if (p + rstep < P.nf)
-                    stage_unit<NMT>(hbs + (buf ^ 1), P, p + rstep, (p + rstep) / NC, et, kEpi);
+                    stage_unit<NMT, JH>(hbs + (buf ^ 1), P, p + rstep, (p + rstep) / NC, et, kEpi);
                 if (ok) {
                     ok = __all_sync(0xffffffffu, mbar_wait(&tfull[buf], tph, err, 4));
                     if (ok) {
@@ -218,18 +226,22 @@ __global__ void __launch_bounds__(kThreads, 1)  // 14 warps: at most 128 registe
                         const int q0 = (nt0 + 2 * u) * NC;
                         // two N tiles: TMEM columns 0-127 hold columns q0 .., 128-255 q0 + NC ..
                         for (int h2 = 0; h2 < 2; ++h2)
-                            unit_half<NMT>(hb, lane_base + buf * 256 + h2 * 128, wg, a, b, p, q0, h2 * NC, P, vect, wv,
-                                           acc);
+                            unit_half<NMT, JH>(hb, lane_base + buf * 256 + h2 * 128, wg, a, b, p, q0, h2 * NC, P, vect,
+                                               wv, acc, jh * NMT);
                         fence_before();
                         mbar_arrive(&tempty[buf]);
                         since += 2;
-                        if ((since >= kFlushTiles || (u + 1 == nu && p + rstep >= P.nf)) && vrow) {
+                        // flush every kFlushTiles tiles, at the end of each mode half (JH > 1) and
+                        // at the end of the CTA's rows
+                        const bool last = u + 1 == nu && ((JH > 1) || p + rstep >= P.nf);
+                        if ((since >= kFlushTiles || last) && vrow) {
 #pragma unroll
                             for (int k = 0; k < kKindsWG; ++k)
 #pragma unroll
                                 for (int j = 0; j < NMT; ++j) {
                                     if (acc[k][j] != 0.f)
-                                        atomicAdd(part + (size_t)((k0 + k) * NMT + j) * 128, (double)acc[k][j]);
+                                        atomicAdd(part + (size_t)((k0 + k) * W + jh * NMT + j) * 128,
+                                                  (double)acc[k][j]);
                                     acc[k][j] = 0.f;
                                 }
                             since = 0;
@@ -254,7 +266,7 @@ namespace ecls {
 
 // m3[m + nm n + nm^2 o] from the per-CTA FP64 partials of the E form (kinds: 0 K_i, 1 K_iv,
 // 2 F14, 3 K_iii, 4 K_v, 5 F35, 6 K_ii, 7 K_vi, 8 F26, each kept at the lane's (a, b) and j).
-__global__ void k_e_reduce(int nm, int NMT, int MT, int grid, const double *__restrict__ part,
+__global__ void k_e_reduce(int nm, int W, int MT, int grid, const double *__restrict__ part,
                            double *__restrict__ m3mf, double *__restrict__ m3mr) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int nm3 = nm * nm * nm;
@@ -263,7 +275,7 @@ __global__ void k_e_reduce(int nm, int NMT, int MT, int grid, const double *__re
     auto sum = [&](int kind, int a, int b, int j) {
         const int R = a * nm + b, mtile = R / 128, lane = R % 128;
         double s = 0.0;
-        for (int g = mtile; g < grid; g += MT) s += part[(((size_t)g * kKinds + kind) * NMT + j) * 128 + lane];
+        for (int g = mtile; g < grid; g += MT) s += part[(((size_t)g * kKinds + kind) * W + j) * 128 + lane];
         return s;
     };
     const double mr = sum(0, m, n, o) + sum(1, m, o, n) + sum(3, o, n, m) + sum(4, n, o, m) + sum(6, n, m, o) +
@@ -274,23 +286,27 @@ __global__ void k_e_reduce(int nm, int NMT, int MT, int grid, const double *__re
     m3mf[x] = 2.0 * mf;
 }
 
-template <int NMT>
+template <int NMT, int JH>
 static cudaError_t launch_k(cudaStream_t st, const CUtensorMap *maps, const EParams &p, int grid) {
-    const size_t smem = (size_t)kStages * kStageBytes + 1024 + kBarBytes + 2 * sizeof(UTile<NMT>);
-    cudaError_t e = cudaFuncSetAttribute(k_bfm_e<NMT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const size_t smem = (size_t)kStages * kStageBytes + 1024 + kBarBytes + 2 * sizeof(UTile<NMT, JH>);
+    static_assert((size_t)kStages * kStageBytes + 1024 + kBarBytes + 2 * sizeof(UTile<NMT, JH>) <= 232448,
+                  "shared memory of one CTA");
+    cudaError_t e = cudaFuncSetAttribute(k_bfm_e<NMT, JH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    k_bfm_e<NMT><<<grid, kThreads, smem, st>>>(maps[0], maps[1], maps[2], maps[3], p);
+    k_bfm_e<NMT, JH><<<grid, kThreads, smem, st>>>(maps[0], maps[1], maps[2], maps[3], p);
     return cudaGetLastError();
 }
 
 }  // namespace ecls
 
 // The E form of the Classic contraction (see the top of this file): whole grid, truncated
-// S(f1 + f2), at most 24 kept modes.  Called by contract_mixed.
+// S(f1 + f2), at most 48 kept modes (above 24 in two mode halves of 16 or 24).  Called by
+// contract_mixed.
 int Engine::contract_e(const PointSrc &ps, double *m3mf, double *m3mr) {
     using namespace ecls;
     const int nf = ps.nf, nm = nme;
-    const int NMT = nm <= 8 ? 8 : nm <= 16 ? 16 : 24;
+    const int NMT = nm <= 8 ? 8 : nm <= 16 ? 16 : nm <= 24 ? 24 : nm <= 32 ? 16 : 24;
+    const int JH = nm <= 24 ? 1 : 2, W = NMT * JH;
     const int NC = kBN / NMT;
     const int Kp = ((K + kBK - 1) / kBK) * kBK;
     const int Mp = ((nm * nm + kBM - 1) / kBM) * kBM;
@@ -302,31 +318,36 @@ int Engine::contract_e(const PointSrc &ps, double *m3mf, double *m3mr) {
         return cuda_fail(e, "device query");
     int grid = (nsm / MT) * MT;
     if (grid < MT) grid = MT;
-    const size_t uel = (size_t)nf * Mp * Kp, gel = (size_t)nf * NMT * Kp;
+    const size_t uel = (size_t)nf * Mp * Kp, gel = (size_t)JH * nf * NMT * Kp;
     const size_t bytesA = 2 * uel * 2, bytesB = 2 * gel * 2;
-    const size_t bytesH = sizeof(float2) * (size_t)(nf + ns) * NMT;
-    const size_t bytesP = sizeof(double) * (size_t)grid * kKinds * NMT * 128;
+    const size_t bytesH = sizeof(float2) * (size_t)(nf + ns) * W;
+    const size_t bytesP = sizeof(double) * (size_t)grid * kKinds * W * 128;
     if ((e = dMixA.reserve(bytesA)) || (e = dMixB.reserve(bytesB)) || (e = dMixH.reserve(bytesH + 256)) ||
         (e = dMixPart.reserve(bytesP + 256)))
         return cuda_fail(e, "allocating BF16x3 operands");
     __nv_bfloat16 *Uh = dMixA.as<__nv_bfloat16>(), *Ul = Uh + uel;
     __nv_bfloat16 *Gh = dMixB.as<__nv_bfloat16>(), *Gl = Gh + gel;
-    float2 *Hg = dMixH.as<float2>(), *Hs = Hg + (size_t)nf * NMT;
+    float2 *Hg = dMixH.as<float2>(), *Hs = Hg + (size_t)nf * W;
     int *derr = (int *)((char *)dMixPart.p + bytesP);
     if ((e = cudaEventRecord(ev2, stream))) return cuda_fail(e, "event");
     if ((e = cudaMemsetAsync(derr, 0, sizeof(int), stream))) return cuda_fail(e, "memset");
     {
         const float *A = dA32.as<float>();
         if ((e = mixed::prep_u(stream, nf, nm, K, Kp, Mp, A, dQ.as<double>(), Uh, Ul)) ||
-            (e = mixed::prep_b(stream, nf, nm, NMT, 0, K, Kp, nf, ps.n_pad, ps.trunc, ps.sum_base, 0, A, Gh, Gl)) ||
-            (e = mixed::prep_h(stream, nf, nm, NMT, ps.fgrid, frf(), Hg, Hs)))
+            (e = mixed::prep_h(stream, nf, nm, W, ps.fgrid, frf(), Hg, Hs)))
             return cuda_fail(e, "BF16x3 operand preparation");
-        kernels += 3;
+        for (int jh = 0; jh < JH; ++jh) {  // G rows of mode half jh at jh nf NMT
+            const size_t og = (size_t)jh * nf * NMT * Kp;
+            if ((e = mixed::prep_b(stream, nf, nm, NMT, jh * NMT, K, Kp, nf, ps.n_pad, ps.trunc, ps.sum_base, 0, A,
+                                   Gh + og, Gl + og)))
+                return cuda_fail(e, "BF16x3 operand preparation");
+        }
+        kernels += 2 + JH;
     }
     CUtensorMap maps[4];
     if (!make_map(&maps[0], Uh, Kp, (uint64_t)nf * Mp, kBM) || !make_map(&maps[1], Ul, Kp, (uint64_t)nf * Mp, kBM) ||
-        !make_map(&maps[2], Gh, Kp, (uint64_t)nf * NMT, NC * NMT) ||
-        !make_map(&maps[3], Gl, Kp, (uint64_t)nf * NMT, NC * NMT))
+        !make_map(&maps[2], Gh, Kp, (uint64_t)JH * nf * NMT, NC * NMT) ||
+        !make_map(&maps[3], Gl, Kp, (uint64_t)JH * nf * NMT, NC * NMT))
         return fail(BSA_ERR_CUDA, "cuTensorMapEncodeTiled failed");
     EParams prm{};
     prm.nf = nf;
@@ -344,17 +365,19 @@ int Engine::contract_e(const PointSrc &ps, double *m3mf, double *m3mr) {
     prm.part = dMixPart.as<double>();
     prm.err = derr;
     if ((e = cudaEventRecord(evg0, stream))) return cuda_fail(e, "event");
-    switch (NMT) {
-    case 8: e = launch_k<8>(stream, maps, prm, grid); break;
-    case 16: e = launch_k<16>(stream, maps, prm, grid); break;
-    default: e = launch_k<24>(stream, maps, prm, grid); break;
+    switch (W) {
+    case 8: e = launch_k<8, 1>(stream, maps, prm, grid); break;
+    case 16: e = launch_k<16, 1>(stream, maps, prm, grid); break;
+    case 24: e = launch_k<24, 1>(stream, maps, prm, grid); break;
+    case 32: e = launch_k<16, 2>(stream, maps, prm, grid); break;
+    default: e = launch_k<24, 2>(stream, maps, prm, grid); break;
     }
     if (e) return cuda_fail(e, "BF16x3 tcgen05 contraction kernel (E form)");
     if ((e = cudaEventRecord(evg1, stream))) return cuda_fail(e, "event");
     const long long nm3 = (long long)nm * nm * nm;
     if ((e = dOut.reserve(sizeof(double) * (3 * (size_t)nm * nm + 2 * (size_t)nm3)))) return cuda_fail(e, "out");
     double *o = dOut.as<double>() + 3 * (size_t)nm * nm;
-    k_e_reduce<<<(unsigned)((nm3 + 127) / 128), 128, 0, stream>>>(nm, NMT, MT, grid, prm.part, o, o + nm3);
+    k_e_reduce<<<(unsigned)((nm3 + 127) / 128), 128, 0, stream>>>(nm, W, MT, grid, prm.part, o, o + nm3);
     if ((e = cudaGetLastError())) return cuda_fail(e, "BF16x3 reduction");
     kernels += 2;
     std::vector<double> h(2 * (size_t)nm3);

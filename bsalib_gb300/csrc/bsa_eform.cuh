@@ -31,24 +31,26 @@ constexpr int kThreads = 448;  // TMA warp, MMA warp, 3 x 4 epilogue warps
 constexpr int kEpi = 384;
 
 // FRF values of one unit (row p, columns q0 .. q0 + 2 NC - 1): H_j at the row, and per
-// column H_j(v), H_j(u + v), H_j(v - u), H_j(u - v).
-template <int NMT>
+// column H_j(v), H_j(u + v), H_j(v - u), H_j(u - v), all W = NMT x JH modes (above 24 kept
+// modes the G rows hold one half of NMT modes at a time, JH = 2, and every unit is swept
+// once per half; the row modes a, b of a TMEM lane range over all W).
+template <int NMT, int JH = 1>
 struct UTile {
-    static constexpr int NC2 = 2 * (kBN / NMT);
-    float2 hr[NMT];
-    float2 hg[NC2 * NMT];
-    float2 hs[NC2 * NMT];
-    float2 hdp[NC2 * NMT];
-    float2 hdm[NC2 * NMT];
+    static constexpr int NC2 = 2 * (kBN / NMT), W = NMT * JH;
+    float2 hr[W];
+    float2 hg[NC2 * W];
+    float2 hs[NC2 * W];
+    float2 hdp[NC2 * W];
+    float2 hdm[NC2 * W];
 };
 
 struct EParams {
     int nf, h, nm, Mp, MT, nk, ks_last, n_ntiles;
     int wmode;
     double wval;
-    const float2 *Hg;  // [nf][NMT]
-    const float2 *Hs;  // [2 nf - 1][NMT]
-    double *part;      // [grid][kKinds][NMT][128]
+    const float2 *Hg;  // [nf][W]
+    const float2 *Hs;  // [2 nf - 1][W]
+    double *part;      // [grid][kKinds][W][128]
     int *err;
 };
 
@@ -74,14 +76,14 @@ __device__ __forceinline__ float wpt(int r, int c, int nf, bool vect, float wv) 
 }
 
 // Stage unit (p, N tiles nt, nt + 1) with threads t < nt_ (cp.async, zero where out of range).
-template <int NMT>
-__device__ __forceinline__ void stage_unit(UTile<NMT> *dst, const EParams &P, int p, int nt, int t, int nt_) {
-    constexpr int NC = kBN / NMT, NC2 = 2 * NC, CH = NMT / 2;  // 16-byte chunks per column row
+template <int NMT, int JH = 1>
+__device__ __forceinline__ void stage_unit(UTile<NMT, JH> *dst, const EParams &P, int p, int nt, int t, int nt_) {
+    constexpr int NC = kBN / NMT, NC2 = 2 * NC, W = NMT * JH, CH = W / 2;  // 16-byte chunks per column row
     const int q0 = nt * NC;
     const int nch = CH + 4 * NC2 * CH;
     for (int x = t; x < nch; x += nt_) {
         if (x < CH) {
-            epi::cp_async16(dst->hr + 2 * x, P.Hg + (size_t)p * NMT + 2 * x, true);
+            epi::cp_async16(dst->hr + 2 * x, P.Hg + (size_t)p * W + 2 * x, true);
             continue;
         }
         const int y = x - CH, which = y / (NC2 * CH), z = y - which * NC2 * CH, cc = z / CH, k = z - cc * CH;
@@ -108,7 +110,7 @@ __device__ __forceinline__ void stage_unit(UTile<NMT> *dst, const EParams &P, in
             v = row >= 0 && row < P.nf;
             d = dst->hdm;
         }
-        epi::cp_async16(d + cc * NMT + 2 * k, v ? (const void *)(tab + (size_t)row * NMT + 2 * k) : (const void *)tab,
+        epi::cp_async16(d + cc * W + 2 * k, v ? (const void *)(tab + (size_t)row * W + 2 * k) : (const void *)tab,
                         v);
     }
     epi::cp_async_commit();
@@ -122,11 +124,11 @@ __device__ __forceinline__ void stage_unit(UTile<NMT> *dst, const EParams &P, in
 // each times x.  One code path for the three (the per-column setup picks the factors and the
 // staged rows; a conj on H_j is folded into the factor), so the three warpgroups share one
 // instruction stream.
-template <int NMT>
-__device__ __forceinline__ void unit_half(const UTile<NMT> &hb, uint32_t taddr, int wg, int a, int b, int p,
+template <int NMT, int JH = 1>
+__device__ __forceinline__ void unit_half(const UTile<NMT, JH> &hb, uint32_t taddr, int wg, int a, int b, int p,
                                           int q0, int slot0, const EParams &P, bool vect, float wv,
-                                          float (&acc)[kKindsWG][NMT]) {
-    constexpr int NC = kBN / NMT;
+                                          float (&acc)[kKindsWG][NMT], int jo = 0) {
+    constexpr int NC = kBN / NMT, W = NMT * JH;
     const float2 hra = hb.hr[a];
 #pragma unroll
     for (int qc = 0; qc < kBN / 16; ++qc) {
@@ -142,7 +144,7 @@ __device__ __forceinline__ void unit_half(const UTile<NMT> &hb, uint32_t taddr, 
             const int ci = col / NMT, j = col % NMT;
             if (ci >= NC) continue;
             if (j == 0 || e == 0) {
-                const int sl = (slot0 + ci) * NMT;
+                const int sl = (slot0 + ci) * W;
                 const int q = q0 + slot0 + ci;
                 const bool valid = q >= p && q < P.nf;
                 const bool vd = valid && q - p <= P.h;
@@ -168,6 +170,8 @@ __device__ __forceinline__ void unit_half(const UTile<NMT> &hb, uint32_t taddr, 
                     X = hb.hr;
                     Y = hb.hdm + sl;
                 }
+                X += jo;  // this pass's half of the modes j
+                Y += jo;
                 P1 = make_float2(wk * t1.x, wk * t1.y);
                 P2 = make_float2(wk * t2.x, wk * t2.y);
             }

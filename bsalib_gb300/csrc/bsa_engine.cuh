@@ -11,6 +11,10 @@
 
 namespace bsa {
 
+// Kept modes up to which the split contraction takes its E form (bsa_classic_e.cu; above 24
+// in two mode halves).
+constexpr int kEFormMaxModes = 48;
+
 // Device buffer that only grows (kept across runs; freed by bsa_Finalise).
 // Frees the device blocks the engine keeps for reuse after bsa_Finalise.
 void release_device_cache();
@@ -148,6 +152,7 @@ struct Engine {
                         float &ms_gemm, float &ms_all, double *zdiag);
     int mesher_zones(std::vector<ZoneDev> &zones, std::vector<int> &policy);
     int run_mesher(double *m3mf, double *m3mr);
+    int zones_export(const std::vector<ZoneDev> &zones);
     int br_decomp(const double *m2mf, double *bkg, double *res);
     int batch_add(int *id);
     void batch_install(const BatchCase &c);

@@ -518,7 +518,7 @@ int Engine::run_classic(double *m2mf, double *m2mr, double *m2o2mr, double *m3mf
         // The split path's E form (bsa_classic_e.cu) already forms each distinct product of the
         // whole grid once, which half the rows would not improve on: there the symmetry is not
         // applied.
-        const bool e_form = mixed && use_e_form && nme <= 24 && !analytic && (nf & 1) && r0 == 0 && r1 == nf;
+        const bool e_form = mixed && use_e_form && nme <= kEFormMaxModes && !analytic && (nf & 1) && r0 == 0 && r1 == nf;
         const bool sym = classic_sym && set.defsc == 1 && !bf_host && !br_host && !export_fn && !e_form;
         if (sym) {
             ps.sym_rows = ps.n_pad;

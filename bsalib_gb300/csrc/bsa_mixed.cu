@@ -508,8 +508,8 @@ int Engine::contract_mixed(const PointSrc &ps, long long npts, double *m3mf, dou
     const int nf = ps.nf, nm = nme;
     if (nm > 64) return fail(BSA_ERR_UNSUPPORTED, "BF16x3 contraction supports at most 64 kept modes");
     // the E form (bsa_classic_e.cu): one GEMM family over half the grid pairs; whole odd grid,
-    // truncated S(f1 + f2), at most 24 kept modes, no central symmetry
-    if (nm <= 24 && ps.mode == kPointsGrid && ps.r0 == 0 && ps.nr == nf && ps.sym_rows == 0 && ps.trunc == 1 &&
+    // truncated S(f1 + f2), at most 48 kept modes, no central symmetry
+    if (nm <= kEFormMaxModes && ps.mode == kPointsGrid && ps.r0 == 0 && ps.nr == nf && ps.sym_rows == 0 && ps.trunc == 1 &&
         (nf & 1) && use_e_form)
         return contract_e(ps, m3mf, m3mr);
     // FRF-table width per mode half; above 32 modes two halves of 32 (JH = 2)

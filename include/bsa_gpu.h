@@ -153,11 +153,15 @@ int bsa_computeSkewness(int nm, const double *m2, const double *m3, double *sk);
 const char *bsa_lastError(void);
 
 /* bsa_setBispExportCallback (src/bsa/BsaLibImpl.F90:1809-1816, called from the Classic
- * analysis at BsaClassicImpl.F90:175-191): fn receives the response bispectra of the Classic
- * grid, npts points at a time, f1 fastest then f2 (the reference's loop order), brm laid out
- * [npts][dim_bisp].  With a callback set, bsa_Run evaluates the Classic bispectra in FP64 in
- * column blocks of the grid (whatever bsa_gpu_setPrecision says), streams each block to fn and
- * sums the third moments over the blocks.  NULL switches the export off. */
+ * analysis at BsaClassicImpl.F90:175-191 and from the Mesher's post-mesh interpolation at
+ * zones/_shared_poly2d.fi:1040-1210): fn receives response bispectra, npts points at a time,
+ * brm laid out [npts][dim_bisp].  Classic: the grid, f1 fastest then f2 (the reference's loop
+ * order); with a callback set, bsa_Run evaluates the Classic bispectra in FP64 in column blocks
+ * of the grid (whatever bsa_gpu_setPrecision says), streams each block to fn and sums the third
+ * moments over the blocks.  Mesher: after the zone integration (moments in the selected
+ * precision), one call per zone with every point of its BRM lattice (i fastest, then j): the
+ * bilinear interpolation of the zone's FP64 force bispectra at its BFM lattice times
+ * Re[H_m(w1) H_n(w2) conj H_o(w1 + w2)].  NULL switches the export off. */
 typedef void (*bsa_brm_export_fn)(int npts, const double *f1, const double *f2, const double *brm, void *user);
 int bsa_setBispExportCallback(bsa_brm_export_fn fn, void *user);
 

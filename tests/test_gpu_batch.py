@@ -1,10 +1,10 @@
 """The batched Classic sweep (bsa_gpu_batch*) against one bsa_Run per case.
 
-Each case of a batch must give the moments its own split-precision analysis gives.  Up to 24
+Each case of a batch must give the moments its own split-precision analysis gives.  Up to 48
 kept modes on odd grids both use the E form of the contraction (each product of one GEMM
 family feeding the three terms at up to six grid points); the batch flushes its FP32 partials
 at other points and adds them with atomics, so third moments agree to ~1e-7.  The batch's
-D1 / D3 form (`Sweep.run(form=0)`, and every case above 24 modes or on an even grid) sums the
+D1 / D3 form (`Sweep.run(form=0)`, and every case above 48 modes or on an even grid) sums the
 same products in another order: ~1e-6 from the E form (both lie ~3e-6 from the FP64 path).
 The bar is 1e-5 relative (max-norm, 10x inside the split-precision bar).  Second moments
 agree to 1e-12.  Against the FP64 path the mixed-precision bar holds

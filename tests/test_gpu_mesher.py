@@ -191,3 +191,46 @@ def test_pod_truncation_zones_split_precision(bsalib):
     assert rel(out[api.PREC_BF16X3][1], out[api.PREC_FP64][1]) < 1e-4
     assert rel(out[api.PREC_BF16X3][0], out[api.PREC_FP64][0]) < 1e-4
     assert rel(out[api.PREC_FP64][1], mr_full) > 1e-6
+
+
+@pytest.mark.parametrize("prec,tol", [(api.PREC_FP64, 1e-10), (api.PREC_BF16X3, 1e-4)], ids=["fp64", "bf16x3"])
+def test_mesher_export(bsalib, prec, tol):
+    """bsa_setBispExportCallback in the Mesher analysis: one block per zone holding every BRM
+    lattice point (i fastest, then j) with the bilinear interpolation of the zone's BFM lattice
+    times the FRF product.  At the BFM lattice points it equals the point bispectra; summed
+    with the zone integration weights it gives the analysis' m3mr (FP64 export; the analysis
+    in the selected precision)."""
+    prob = cantilever_tower(nodes=5)
+    prob.settings.suban = 2
+    prob.settings.bkgrfmt = 6
+    got = []
+    s = api.BsaSession(prob, precision=prec)
+    try:
+        _controls(s, LAYOUT_CTL[1])
+        zs = s.generate_zones()
+        s.set_export(lambda f1, f2, brm: got.append((f1.copy(), f2.copy(), brm.copy())))
+        out = s.run()
+        s.set_export(None)
+        ref = s.run()
+        assert len(got) == len(zs)
+        acc = np.zeros_like(out["m3mr_msh"])
+        for z, (f1, f2, b) in zip(zs, got):
+            NI, NJ = (z.ni - 1) * z.Fi + 1, (z.nj - 1) * z.Fj + 1
+            assert f1.size == NI * NJ
+            qi, qj = np.meshgrid(np.arange(NI), np.arange(NJ))  # qi fastest
+            qi, qj = qi.ravel(), qj.ravel()
+            a, c = qi / z.Fi, qj / z.Fj
+            np.testing.assert_allclose(f1, z.fi0 + a * z.dIi + c * z.dJi, rtol=0, atol=1e-12)
+            np.testing.assert_allclose(f2, z.fj0 + a * z.dIj + c * z.dJj, rtol=0, atol=1e-12)
+            ti = np.where((qi == 0) | (qi == NI - 1), 0.5, 1.0)
+            tj = np.where((qj == 0) | (qj == NJ - 1), 0.5, 1.0)
+            wI = np.hypot(z.dIi, z.dIj) * 2 * np.pi / z.Fi
+            wJ = np.hypot(z.dJi, z.dJj) * 2 * np.pi / z.Fj
+            acc += (z.sym * wI * wJ * ti * tj) @ b
+            lat = (qi % z.Fi == 0) & (qj % z.Fj == 0)
+            _, br = s.msh_bispectra(f1[lat], f2[lat])
+            assert rel(b[lat], br) < 1e-12
+    finally:
+        s.close()
+    assert rel(acc, out["m3mr_msh"]) < tol
+    assert rel(out["m3mr_msh"], ref["m3mr_msh"]) < 1e-12

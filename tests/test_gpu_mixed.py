@@ -132,11 +132,12 @@ def test_symmetric_d1_matches_the_full_form(modes):
 
 
 @pytest.mark.parametrize("nodes,modes,nfreqs,tc", [(30, 4, 33, (1,)), (60, 8, 41, (1, 3)), (80, 12, 65, (1, 3)),
-                                                     (100, 16, 33, (1,)), (120, 24, 49, (1, 3))])
+                                                     (100, 16, 33, (1,)), (120, 24, 49, (1, 3)), (70, 28, 25, (1, 3)),
+                                                     (90, 40, 21, (1,)), (64, 48, 17, (1, 3))])
 def test_e_form_matches_the_d_form(bsalib, nodes, modes, nfreqs, tc):
-    """The E form (one GEMM family over half the grid pairs, six contributions per product)
-    against the D1 / D3 form on the same grid: the same products, summed in another order
-    (FP32 partials), so 2e-6 relative."""
+    """The E form (one GEMM family over half the grid pairs, six contributions per product;
+    above 24 kept modes in two mode halves) against the D1 / D3 form on the same grid: the
+    same products, summed in another order (FP32 partials), so 2e-6 relative."""
     import dataclasses
     prob = tall_building(nodes=nodes, modes=modes, nfreqs=nfreqs, df=4.0 / (nfreqs - 1), seed=nodes)
     prob.settings = dataclasses.replace(prob.settings, tc=tc)
