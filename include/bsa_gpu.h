@@ -356,9 +356,10 @@ int bsa_gpu_getStats(bsa_gpu_stats *st);
 
 /* Form of the split-precision Classic contraction: 1 (default) the E form -- one GEMM family
  * over half the grid pairs, each product feeding the three terms at up to six grid points --
- * where it applies (whole odd grid, truncated S(f1 + f2), at most 24 kept modes, no central
- * symmetry); 0 the D1 / D3 form everywhere.  Both give the same moments to FP32 rounding.  No
- * reference counterpart (reset by bsa_Finalise). */
+ * where it applies (whole odd grid, truncated S(f1 + f2), at most 48 kept modes; central
+ * symmetry is then not applied); 0 the D1 / D3 form everywhere.  Both give the same moments to
+ * FP32 rounding.  Also read by bsa_gpu_batchRun.  No reference counterpart (reset by
+ * bsa_Finalise). */
 int bsa_gpu_setClassicForm(int form);
 
 /* Device memory.  Blocks the library releases (bsa_Finalise, buffer growth) are kept for reuse
