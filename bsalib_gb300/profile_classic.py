@@ -17,9 +17,10 @@ def main():
     ap.add_argument("--nfreqs", type=int, default=513)
     ap.add_argument("--steps", type=int, default=2)
     ap.add_argument("--precision", default="bf16x3", choices=["bf16x3", "fp64"])
+    ap.add_argument("--modes", type=int, default=24, help="kept modes of the building")
     a = ap.parse_args()
     build.build()
-    prob = tall_building(nfreqs=a.nfreqs, df=4.0 / (a.nfreqs - 1))
+    prob = tall_building(modes=a.modes, nfreqs=a.nfreqs, df=4.0 / (a.nfreqs - 1))
     prec = api.PREC_BF16X3 if a.precision == "bf16x3" else api.PREC_FP64
     s = api.BsaSession(prob, precision=prec)
     try:
