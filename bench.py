@@ -128,52 +128,68 @@ def profiled_traffic():
     return None
 
 
-def cpu_reference(prob, budget_s=20.0, threads=None):
+class CpuReference:
     """The reference's Classic scalar algorithm (BsaClassicImpl.F90:255-363 with
-    getFM_full_tnm_scalar_cls_, functionsImpl.F90:2122-2318) restated in the C oracle, on a
-    bounded sample: `npairs` grid pairs evaluated in parallel, each over a slice of k-nodes,
-    the per-pair cost extrapolated linearly in k (it is uniform in k)."""
-    import ctypes as C
+    getFM_full_tnm_scalar_cls_, functionsImpl.F90:2122-2318) restated in the C oracle, timed on
+    the host cores on a bounded sample: one grid pair per thread, each over a slice of the
+    k-node loop, the per-pair cost extrapolated linearly in k (the loop's cost is uniform in k:
+    k x NNL^2 inner updates).  One step = one round of the pairs; its grid-point equivalent is
+    pairs x kk / NNL."""
 
-    from oracle import oracle as orc
-    o = orc.Oracle(prob)
-    f = o.freqs()
-    nf = f.size
-    S = o.suvw(f)
-    npsd = S.shape[1]
-    lp = (nf - 1) // 2
-    Spad = np.zeros((npsd, 2 * lp + nf), order="F")
-    Spad[:, lp:lp + nf] = S.T
-    nthreads = threads or os.cpu_count() or 1
-    lib = orc.lib()
-    nnl = prob.nnl
-    # size the k-slice so one round of pairs (one per thread) takes ~budget/3
-    kk = 1
-    rng = np.random.default_rng(0)
-    pairs = [(int(rng.integers(nf)), int(rng.integers(nf))) for _ in range(nthreads)]
-    from concurrent.futures import ThreadPoolExecutor
+    def __init__(self, prob, threads=None):
+        from oracle import oracle as orc
+        self.o = orc.Oracle(prob)
+        self.f = self.o.freqs()
+        nf = self.f.size
+        self.S = self.o.suvw(self.f)
+        lp = (nf - 1) // 2
+        self.Spad = np.zeros((self.S.shape[1], 2 * lp + nf), order="F")
+        self.Spad[:, lp:lp + nf] = self.S.T
+        self.threads = threads or os.cpu_count() or 1
+        self.nnl = prob.nnl
+        rng = np.random.default_rng(0)
+        self.pairs = [(int(rng.integers(nf)), int(rng.integers(nf))) for _ in range(self.threads)]
+        self.kk = 1
 
-    def one(pr, k_hi):
-        ii, ij = pr
-        return o.scalar_pair_slice(f, S, np.asfortranarray(Spad[:, ii + ij]), ii, ij, 0, k_hi)
+    def _round(self, kk):
+        from concurrent.futures import ThreadPoolExecutor
 
-    t = time.perf_counter()
-    with ThreadPoolExecutor(nthreads) as ex:
-        list(ex.map(lambda pr: one(pr, kk), pairs))
-    dt = time.perf_counter() - t
-    kk = max(1, min(nnl, int(kk * (budget_s / 3) / max(dt, 1e-6))))
-    t = time.perf_counter()
+        def one(pr):
+            ii, ij = pr
+            return self.o.scalar_pair_slice(self.f, self.S, np.asfortranarray(self.Spad[:, ii + ij]), ii, ij, 0, kk)
+
+        t = time.perf_counter()
+        with ThreadPoolExecutor(self.threads) as ex:
+            list(ex.map(one, self.pairs))
+        return time.perf_counter() - t
+
+    def calibrate(self, step_s):
+        dt = self._round(1)
+        self.kk = max(1, min(self.nnl, int(step_s / max(dt, 1e-6))))
+
+    def step(self):
+        """(grid points equivalent, seconds) of one round."""
+        dt = self._round(self.kk)
+        return len(self.pairs) * self.kk / self.nnl, dt
+
+    def describe(self, rounds, seconds):
+        return (f"{rounds} rounds of {len(self.pairs)} grid pairs of the scalar Classic BFM+BRM (one per thread), "
+                f"k-node loop cut to {self.kk}/{self.nnl} nodes and extrapolated linearly, {self.threads} threads, "
+                f"{seconds:.1f} s")
+
+
+def cpu_reference(prob, budget_s=15.0):
+    ref = CpuReference(prob)
+    ref.calibrate(budget_s / 3)
+    pts = secs = 0.0
     rounds = 0
-    while time.perf_counter() - t < budget_s * 2 / 3 or rounds == 0:
-        with ThreadPoolExecutor(nthreads) as ex:
-            list(ex.map(lambda pr: one(pr, kk), pairs))
+    while secs < budget_s * 2 / 3 or rounds == 0:
+        p, dt = ref.step()
+        pts += p
+        secs += dt
         rounds += 1
-    dt = time.perf_counter() - t
-    pair_s = dt / (rounds * len(pairs)) * (nnl / kk) * nthreads  # per pair, one thread
-    pts_per_s = nthreads / pair_s
-    return {"value": pts_per_s, "unit": UNIT, "cores": nthreads, "kind": "port",
-            "sample": f"{rounds * len(pairs)} grid pairs of the scalar Classic BFM+BRM, k-node loop cut to "
-                      f"{kk}/{nnl} nodes and extrapolated linearly, {nthreads} threads, {dt:.1f} s"}
+    return {"value": pts / secs, "unit": UNIT, "cores": ref.threads, "kind": "port",
+            "sample": ref.describe(rounds, secs)}
 
 
 def mesher_leg(prec):
@@ -189,13 +205,15 @@ def mesher_leg(prec):
     try:
         s.use_driver_controls()  # the reference driver's Mesher controls (app/bsa.F90:544-549)
         s.run()
-        ms, pts = [], 0.0
+        ms, gms, pts = [], [], 0.0
         for _ in range(2):
             s.run()
             st = s.stats()
             ms.append(st.ms_total)
+            gms.append(st.ms_gemm)
             pts = st.points
         zones = s.generate_zones()
+        nm = s.nmodes()
     finally:
         s.close()
     sample = zones[::8]
@@ -220,11 +238,21 @@ def mesher_leg(prec):
     relm = lambda a, b: float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
     v = pts / (float(np.mean(ms)) / 1e3)
     fp64 = res[api.PREC_FP64][3] / (res[api.PREC_FP64][2] / 1e3)
+    # roofline of the Mesher contraction: F_pt per BFM lattice point / the contraction kernels' time
+    nbfm = float(sum(z.ni * z.nj for z in zones))
+    g_ms = float(np.mean(gms))
+    peak_tf, _, peak_src = peaks()
+    achieved = algorithmic_flops_per_point(prob.nnl, nm, prob.ntc) * nbfm / (g_ms / 1e3) / 1e12
     return {"workload": "bridge_deck_1200nodes_60modes_2tc_mesher", "controls": "driver (app/bsa.F90:544-549)",
             "zones": len(zones), "brm_points": pts,
             "value": v, "unit": "BRM pts/s", "ms_per_analysis": float(np.mean(ms)),
             "fp64_gpu_path": {"value": fp64, "unit": "BRM pts/s", "sample": f"every 8th zone ({len(sample)} zones)"},
             "speedup_vs_fp64": v / fp64,
+            "roofline": {"bound": "tensor", "kernel": "k_msh_mixed", "kernel_ms": g_ms, "bfm_points": nbfm,
+                         "achieved": achieved, "peak": peak_tf, "unit": "TFLOP/s", "frac": achieved / peak_tf,
+                         "peak_source": peak_src,
+                         "note": "F_pt = NTC 3 2 NNL NM^3 per BFM lattice point over the contraction kernels' "
+                                 "CUDA-event time"},
             "accuracy_vs_fp64": {"sample": f"every 8th zone ({len(sample)} zones)",
                                  "m3mr_rel": relm(res[api.PREC_BF16X3][1], res[api.PREC_FP64][1]),
                                  "m3mf_rel": relm(res[api.PREC_BF16X3][0], res[api.PREC_FP64][0]),
@@ -290,26 +318,85 @@ def sweep_leg():
     return sweep.run(structures=8, winds=8, seed0=5000, check=True)
 
 
+CONFIG = {"workload": WORKLOAD, "nodes": 400, "modes": 24, "ntc": 2, "grid": 1025,
+          "l2": "inputs larger than L2 (operand tables ~2.4 GB)"}
+
+
 def run_reference(args):
+    """The reference's CPU algorithm on the host cores: each step one bounded sample of the
+    workload (about 3 s), value = grid points (equivalent) per second over the timed steps."""
     ws, rank, _ = dist_env()
     if rank != 0:
         return
     from bsalib_gb300.problem import tall_building
     prob = tall_building()
-    vals = []
+    ref = CpuReference(prob)
+    ref.calibrate(3.0)
     for _ in range(args.warmup):
-        cpu_reference(prob, budget_s=3.0)
-    info = None
+        ref.step()
+    pts = secs = 0.0
     for _ in range(args.steps):
-        info = cpu_reference(prob, budget_s=max(5.0, 60.0 / max(args.steps, 1)))
-        vals.append(info["value"])
-    v = float(np.mean(vals))
+        p, dt = ref.step()
+        pts += p
+        secs += dt
+    v = pts / secs
+    info = {"value": v, "unit": UNIT, "cores": ref.threads, "kind": "port", "sample": ref.describe(args.steps, secs)}
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 1e3 * prob.classic_nf() ** 2 / v, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "nodes": 400, "modes": 24, "ntc": 2, "grid": 1025},
-            "cpu_baseline": info, "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": dict(CONFIG),
+            "cpu_baseline": info, "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "ms_per_step is the wall time of one bounded sample (a slice of the k-node loop of one grid pair "
+                    "per host thread); value extrapolates the sample to whole grid points"}
     print(json.dumps(line))
+
+
+def accuracy_leg(prob, r_mixed, sk_mixed):
+    """The split path against the plain FP64 path on the benchmark's own structure and grid:
+    third moments and skewness of the full 1025 x 1025 analysis (the FP64 analysis with the
+    grid's central symmetry, rows f1 <= 0: the same moments up to the summation order, half the
+    time), and the force / response bispectra at 4096 seeded grid points (bsa_gpu_clsBispectraAt:
+    in BF16x3 the E-form analysis's own per-point products)."""
+    from bsalib_gb300 import api
+    nf = prob.classic_nf()
+    relm = lambda a, b: float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
+    s = api.BsaSession(prob, precision=api.PREC_FP64)
+    try:
+        s.set_symmetry(True)
+        t0 = time.perf_counter()
+        r64 = s.run()
+        wall64 = time.perf_counter() - t0
+        ms64 = s.stats().ms_total
+        sk64 = s.skewness(r64["m2mr_cls"], r64["m3mr_cls"])
+        s.set_symmetry(False)
+        rng = np.random.default_rng(7)
+        flat = rng.choice(nf * nf, size=4096, replace=False)
+        i1, i2 = flat % nf, flat // nf
+        bf64, br64 = s.classic_points(i1, i2)
+    finally:
+        s.close()
+    s = api.BsaSession(prob, precision=api.PREC_BF16X3)
+    try:
+        bfx, brx = s.classic_points(i1, i2)
+    finally:
+        s.close()
+
+    def pointwise(x, ref):
+        e = np.max(np.abs(x - ref), axis=1) / np.maximum(np.max(np.abs(ref), axis=1), 1e-300)
+        return {"max": float(np.max(e)), "median": float(np.median(e)), "p99": float(np.percentile(e, 99))}
+
+    acc = {"grid": f"{nf}x{nf}",
+           "m3mr_rel": relm(r_mixed["m3mr_cls"], r64["m3mr_cls"]),
+           "m3mf_rel": relm(r_mixed["m3mf_cls"], r64["m3mf_cls"]),
+           "m2mr_rel": relm(r_mixed["m2mr_cls"], r64["m2mr_cls"]),
+           "skewness_rel": relm(sk_mixed, sk64),
+           "points": {"n": 4096, "sample": "seeded distinct grid points of the full grid",
+                      "bf_rel_maxnorm": relm(bfx, bf64), "br_rel_maxnorm": relm(brx, br64),
+                      "bf_rel_per_point": pointwise(bfx, bf64), "br_rel_per_point": pointwise(brx, br64)},
+           "bars": {"bispectra": 1e-4, "skewness": 1e-3}}
+    npts = nf * nf
+    full = {"ms_device": ms64, "wall_s": wall64, "value": npts / (ms64 / 1e3), "unit": UNIT,
+            "form": "FP64 kernel, central symmetry of the grid (rows f1 <= 0 evaluated, mirrored weights)"}
+    return acc, full
 
 
 def run_ours(args):
@@ -401,20 +488,7 @@ def run_ours(args):
 
     out = None
     if rank == 0:
-        # ---- accuracy of the mixed path vs the plain FP64 path on the same structure,
-        #      129 x 129 grid (the FP64 path takes minutes on the full grid) ----
-        acc = {}
-        small = tall_building(nfreqs=65, df=4.0 / 64, seed=2024)
-        res = {}
-        for pr in (api.PREC_FP64, api.PREC_BF16X3):
-            ss = api.BsaSession(small, precision=pr)
-            rr = ss.run()
-            res[pr] = (rr, ss.skewness(rr["m2mr_cls"], rr["m3mr_cls"]))
-            ss.close()
-        (r64, sk64), (rmx, skmx) = res[api.PREC_FP64], res[api.PREC_BF16X3]
-        relm = lambda a, b: float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
-        acc = {"grid": "129x129", "m3mr_rel": relm(rmx["m3mr_cls"], r64["m3mr_cls"]),
-               "m3mf_rel": relm(rmx["m3mf_cls"], r64["m3mf_cls"]), "skewness_rel": relm(skmx, sk64)}
+        acc, fp64_full = accuracy_leg(prob, r, sk_mixed)
         # ---- the plain FP64 GPU path on a sample of the full grid's points ----
         rng = np.random.default_rng(1)
         f = np.arange(-(nf // 2), nf // 2 + 1) * (8.0 / (nf - 1))
@@ -422,7 +496,6 @@ def run_ours(args):
         i1, i2 = rng.integers(nf, size=ns), rng.integers(nf, size=ns)
         s3 = api.BsaSession(prob, precision=api.PREC_FP64)
         s3.msh_moments(f[i1], f[i2], np.ones(ns))
-        t0 = time.perf_counter()
         s3.msh_moments(f[i1], f[i2], np.ones(ns))
         st3 = s3.stats()
         s3.close()
@@ -443,8 +516,7 @@ def run_ours(args):
             "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "bf16x3 contraction (fp32 accumulate), fp64 FRF/moments"
             if prec == api.PREC_BF16X3 else "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "nodes": 400, "modes": 24, "ntc": 2, "grid": 1025,
-                       "precision": args.precision, "l2": "inputs larger than L2 (operand tables ~2.4 GB)"},
+            "config": dict(CONFIG),
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d + h2d_in),
                     "d2h_bytes_per_step": int(d2h)},
             "gpu_launches": launches,
@@ -461,7 +533,8 @@ def run_ours(args):
             "clocks": clk.summary(),
             "cpu_baseline": cpu,
             "accuracy_vs_fp64": acc,
-            "fp64_gpu_path": {"value": fp64_pts, "unit": UNIT, "sample": f"{ns} random grid points"},
+            "fp64_gpu_path": {"value": fp64_pts, "unit": UNIT, "sample": f"{ns} random grid points",
+                              "full_grid": fp64_full},
             "mesher": msh,
             "classic_central_symmetry": sym,
             "parametric_sweep": swp,

@@ -86,6 +86,7 @@ def load(path: Optional[str] = None):
         "bsa_Run": [vp] * 7, "bsa_computeSkewness": [i, vp, vp, vp],
         "bsa_gpu_setPrecision": [i], "bsa_gpu_setClassicTruncation": [i], "bsa_gpu_setClassicRows": [i, i],
         "bsa_gpu_clsBispectra": [vp, i, vp, vp, vp], "bsa_gpu_mshBispectra": [vp, vp, i, vp, vp],
+        "bsa_gpu_clsBispectraAt": [vp, vp, i, vp, vp],
         "bsa_gpu_mshMoments": [vp, vp, vp, i, vp, vp], "bsa_gpu_getStats": [vp], "bsa_gpu_releaseDeviceCache": [], "bsa_gpu_setClassicForm": [i],
         "bsa_gpu_pointMomentsNoAlloc": [vp, i, i, vp, vp, vp, vp, vp, vp, vp, i, vp, vp, vp, vp, vp, vp],
         "bsa_gpu_mshZones": [vp, i, vp, vp, vp], "bsa_gpu_mshGenerateZones": [vp, i, vp],
@@ -260,6 +261,17 @@ class BsaSession:
         bf = bf[: n * n * nm3].reshape(n, n, nm3).transpose(1, 0, 2)
         br = br[: n * n * nm3].reshape(n, n, nm3).transpose(1, 0, 2)
         return f[:n].copy(), bf, br
+
+    def classic_points(self, i1, i2):
+        """Force / response bispectra (npts, dim_bisp) at Classic grid points (i1[p], i2[p]) in the
+        session's precision (bsa_gpu_clsBispectraAt)."""
+        i1 = np.ascontiguousarray(i1, dtype=np.int32)
+        i2 = np.ascontiguousarray(i2, dtype=np.int32)
+        nm3 = self.dims()[1]
+        bf = np.zeros((i1.size, nm3))
+        br = np.zeros((i1.size, nm3))
+        check(self.lib.bsa_gpu_clsBispectraAt(_p(i1), _p(i2), i1.size, _p(bf), _p(br)), "bsa_gpu_clsBispectraAt")
+        return bf, br
 
     def msh_bispectra(self, fi, fj):
         fi = np.ascontiguousarray(fi, dtype=np.float64)

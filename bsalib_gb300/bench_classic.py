@@ -1,6 +1,7 @@
-"""Run the Classic analysis of the tall-building workload a few times (for profilers).
+"""Timing tool: the Classic analysis of the tall-building workload, run a few times (also the
+command the committed ncu summaries under profiles/ were taken with).
 
-  python -m bsalib_gb300.profile_classic [--nfreqs 513] [--steps 2] [--precision bf16x3]
+  python -m bsalib_gb300.bench_classic [--nfreqs 513] [--steps 2] [--precision bf16x3]
 
 Defaults give the full 400-node, 24-mode, two-component building on the 1025 x 1025 grid;
 --nfreqs 65 gives the same structure on a 129 x 129 grid (a few hundred MB on the device).

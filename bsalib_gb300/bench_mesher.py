@@ -1,6 +1,7 @@
-"""Run the Mesher analysis (zone layout + zone integration) of a structure a few times.
+"""Timing tool: the Mesher analysis (zone layout + zone integration) of a structure, run a few
+times (also the command the committed ncu summaries under profiles/ were taken with).
 
-  python -m bsalib_gb300.profile_mesher [--structure bridge|building|tower] [--nodes N]
+  python -m bsalib_gb300.bench_mesher [--structure bridge|building|tower] [--nodes N]
                                         [--modes M] [--precision bf16x3|fp64] [--steps 2]
 
 Prints the zone and lattice-point counts and, per run, the library statistics and the

@@ -48,7 +48,10 @@ namespace ecls {
 
 using namespace tc;
 
-template <int NMT, int JH>
+// SAMPLE = true is the diagnostic instantiation: the same products, with the epilogue writing
+// the unweighted per-point bispectra of the grid points P.slot lists (unit_half_sample) instead
+// of the weighted moment partials.
+template <int NMT, int JH, bool SAMPLE>
 __global__ void __launch_bounds__(kThreads, 1)  // 14 warps: at most 128 registers a thread
     k_bfm_e(const __grid_constant__ CUtensorMap tmUh, const __grid_constant__ CUtensorMap tmUl,
             const __grid_constant__ CUtensorMap tmGh, const __grid_constant__ CUtensorMap tmGl, const EParams P) {
@@ -225,16 +228,21 @@ __global__ void __launch_bounds__(kThreads, 1)  // 14 warps: at most 128 registe
                         const UT &hb = hbs[buf];
                         const int q0 = (nt0 + 2 * u) * NC;
                         // two N tiles: TMEM columns 0-127 hold columns q0 .., 128-255 q0 + NC ..
-                        for (int h2 = 0; h2 < 2; ++h2)
-                            unit_half<NMT, JH>(hb, lane_base + buf * 256 + h2 * 128, wg, a, b, p, q0, h2 * NC, P, vect,
-                                               wv, acc, jh * NMT);
+                        for (int h2 = 0; h2 < 2; ++h2) {
+                            if constexpr (SAMPLE)
+                                unit_half_sample<NMT, JH>(hb, lane_base + buf * 256 + h2 * 128, wg, a, b, p, q0,
+                                                          h2 * NC, P, jh * NMT, vrow);
+                            else
+                                unit_half<NMT, JH>(hb, lane_base + buf * 256 + h2 * 128, wg, a, b, p, q0, h2 * NC, P,
+                                                   vect, wv, acc, jh * NMT);
+                        }
                         fence_before();
                         mbar_arrive(&tempty[buf]);
                         since += 2;
                         // flush every kFlushTiles tiles, at the end of each mode half (JH > 1) and
                         // at the end of the CTA's rows
                         const bool last = u + 1 == nu && ((JH > 1) || p + rstep >= P.nf);
-                        if ((since >= kFlushTiles || last) && vrow) {
+                        if (!SAMPLE && (since >= kFlushTiles || last) && vrow) {
 #pragma unroll
                             for (int k = 0; k < kKindsWG; ++k)
 #pragma unroll
@@ -286,14 +294,15 @@ __global__ void k_e_reduce(int nm, int W, int MT, int grid, const double *__rest
     m3mf[x] = 2.0 * mf;
 }
 
-template <int NMT, int JH>
+template <int NMT, int JH, bool SAMPLE = false>
 static cudaError_t launch_k(cudaStream_t st, const CUtensorMap *maps, const EParams &p, int grid) {
     const size_t smem = (size_t)kStages * kStageBytes + 1024 + kBarBytes + 2 * sizeof(UTile<NMT, JH>);
     static_assert((size_t)kStages * kStageBytes + 1024 + kBarBytes + 2 * sizeof(UTile<NMT, JH>) <= 232448,
                   "shared memory of one CTA");
-    cudaError_t e = cudaFuncSetAttribute(k_bfm_e<NMT, JH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e =
+        cudaFuncSetAttribute(k_bfm_e<NMT, JH, SAMPLE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    k_bfm_e<NMT, JH><<<grid, kThreads, smem, st>>>(maps[0], maps[1], maps[2], maps[3], p);
+    k_bfm_e<NMT, JH, SAMPLE><<<grid, kThreads, smem, st>>>(maps[0], maps[1], maps[2], maps[3], p);
     return cudaGetLastError();
 }
 
@@ -301,8 +310,9 @@ static cudaError_t launch_k(cudaStream_t st, const CUtensorMap *maps, const EPar
 
 // The E form of the Classic contraction (see the top of this file): whole grid, truncated
 // S(f1 + f2), at most 48 kept modes (above 24 in two mode halves of 16 or 24).  Called by
-// contract_mixed.
-int Engine::contract_e(const PointSrc &ps, double *m3mf, double *m3mr) {
+// contract_mixed; with smp, the sampled instantiation writes the per-point bispectra of the
+// grid points smp->slot lists into smp->sF / smp->sR (zeroed here) and no moments.
+int Engine::contract_e(const PointSrc &ps, double *m3mf, double *m3mr, const ESample *smp) {
     using namespace ecls;
     const int nf = ps.nf, nm = nme;
     const int NMT = nm <= 8 ? 8 : nm <= 16 ? 16 : nm <= 24 ? 24 : nm <= 32 ? 16 : 24;
@@ -364,17 +374,47 @@ int Engine::contract_e(const PointSrc &ps, double *m3mf, double *m3mr) {
     prm.Hs = Hs;
     prm.part = dMixPart.as<double>();
     prm.err = derr;
+    const long long nm3 = (long long)nm * nm * nm;
+    if (smp) {
+        prm.slot = smp->slot;
+        prm.sF = smp->sF;
+        prm.sR = smp->sR;
+        if ((e = cudaMemsetAsync(smp->sF, 0, sizeof(double) * (size_t)smp->nslot * nm3, stream)) ||
+            (e = cudaMemsetAsync(smp->sR, 0, sizeof(double) * (size_t)smp->nslot * nm3, stream)))
+            return cuda_fail(e, "memset");
+    }
     if ((e = cudaEventRecord(evg0, stream))) return cuda_fail(e, "event");
-    switch (W) {
-    case 8: e = launch_k<8, 1>(stream, maps, prm, grid); break;
-    case 16: e = launch_k<16, 1>(stream, maps, prm, grid); break;
-    case 24: e = launch_k<24, 1>(stream, maps, prm, grid); break;
-    case 32: e = launch_k<16, 2>(stream, maps, prm, grid); break;
-    default: e = launch_k<24, 2>(stream, maps, prm, grid); break;
+    if (smp) {
+        switch (W) {
+        case 8: e = launch_k<8, 1, true>(stream, maps, prm, grid); break;
+        case 16: e = launch_k<16, 1, true>(stream, maps, prm, grid); break;
+        case 24: e = launch_k<24, 1, true>(stream, maps, prm, grid); break;
+        case 32: e = launch_k<16, 2, true>(stream, maps, prm, grid); break;
+        default: e = launch_k<24, 2, true>(stream, maps, prm, grid); break;
+        }
+    } else {
+        switch (W) {
+        case 8: e = launch_k<8, 1>(stream, maps, prm, grid); break;
+        case 16: e = launch_k<16, 1>(stream, maps, prm, grid); break;
+        case 24: e = launch_k<24, 1>(stream, maps, prm, grid); break;
+        case 32: e = launch_k<16, 2>(stream, maps, prm, grid); break;
+        default: e = launch_k<24, 2>(stream, maps, prm, grid); break;
+        }
     }
     if (e) return cuda_fail(e, "BF16x3 tcgen05 contraction kernel (E form)");
     if ((e = cudaEventRecord(evg1, stream))) return cuda_fail(e, "event");
-    const long long nm3 = (long long)nm * nm * nm;
+    if (smp) {
+        int herr = 0;
+        if ((e = cudaMemcpyAsync(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost, stream)) ||
+            (e = cudaEventRecord(ev1, stream)) || (e = cudaStreamSynchronize(stream)))
+            return cuda_fail(e, "BF16x3 contraction (sampled)");
+        kernels += 1;
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, evg0, evg1);
+        last_ms_gemm = ms;
+        if (herr) return fail(BSA_ERR_TIMEOUT, "BF16x3 kernel: a pipeline wait ran out of its budget (role %d)", herr);
+        return BSA_OK;
+    }
     if ((e = dOut.reserve(sizeof(double) * (3 * (size_t)nm * nm + 2 * (size_t)nm3)))) return cuda_fail(e, "out");
     double *o = dOut.as<double>() + 3 * (size_t)nm * nm;
     k_e_reduce<<<(unsigned)((nm3 + 127) / 128), 128, 0, stream>>>(nm, W, MT, grid, prm.part, o, o + nm3);

@@ -52,6 +52,10 @@ struct EParams {
     const float2 *Hs;  // [2 nf - 1][W]
     double *part;      // [grid][kKinds][W][128]
     int *err;
+    // Sampled form only (k_bfm_e with SAMPLE): slot[i1 + nf i2] = row of grid point (i1, i2)
+    // in sF / sR ([slot][nm^3], m fastest), or -1 where the point is not sampled.
+    const int *slot;
+    double *sF, *sR;
 };
 
 // Shared-memory float2 load the compiler does not hoist (keeps the per-mode FRF values out
@@ -180,6 +184,78 @@ __device__ __forceinline__ void unit_half(const UTile<NMT, JH> &hb, uint32_t tad
             acc[0][j] = fmaf(P1.x * xj.x - P1.y * xj.y, x, acc[0][j]);  // Re[P1 X_j]
             acc[1][j] = fmaf(P2.x * yj.x - P2.y * yj.y, x, acc[1][j]);  // Re[P2 Y_j]
             acc[2][j] = fmaf(wk, x, acc[2][j]);
+        }
+    }
+}
+
+// Sampled form of unit_half (the diagnostic instantiation of k_bfm_e): each contribution of
+// the tile to a grid point listed in P.slot is added, unweighted, to that point's force and
+// response bispectra (B = 2 (T1 + T2 + T3), FP64 atomics), with the same FRF factors as the
+// moment epilogue (FP32 from the staged rows).  Targets per warpgroup as in unit_half:
+//   wg 0: (i) T1 at (p, q), m n o = a b j;   (iv) T1 at (q, p), a j b
+//   wg 1: (iii) T3 at (p, c), j b a;          (v) T2 at (c, p), j a b        (f_c = f_q - f_p)
+//   wg 2: (ii) T2 at (d, q), b a j;           (vi) T3 at (q, d), b j a       (f_d = f_p - f_q)
+// A diagonal product (q = p) feeds them at half weight, as in the moment form.
+template <int NMT, int JH = 1>
+__device__ __forceinline__ void unit_half_sample(const UTile<NMT, JH> &hb, uint32_t taddr, int wg, int a, int b,
+                                                 int p, int q0, int slot0, const EParams &P, int jo, bool vrow) {
+    constexpr int NC = kBN / NMT, W = NMT * JH;
+    const int nm = P.nm, nm2 = nm * nm;
+    const size_t nm3 = (size_t)nm2 * nm;
+    const float2 hra = hb.hr[a];
+#pragma unroll 1
+    for (int qc = 0; qc < kBN / 16; ++qc) {
+        uint32_t v[16];
+        tmem_ld16(taddr + qc * 16, v);  // warp-collective: every lane loads
+        tmem_wait_ld();
+        if (!vrow) continue;
+#pragma unroll 1
+        for (int e = 0; e < 16; ++e) {
+            const int col = qc * 16 + e;
+            const int ci = col / NMT, j = col % NMT, jg = jo + j;
+            if (ci >= NC || jg >= nm) continue;
+            const int q = q0 + slot0 + ci;
+            const bool valid = q >= p && q < P.nf;
+            if (!(wg == 0 ? valid : (valid && q - p <= P.h))) continue;
+            const int sl = (slot0 + ci) * W;
+            const float2 Hbv = hb.hg[sl + b], Hav = hb.hg[sl + a];
+            int i1a, i2a, i1b, i2b, ia, ib;
+            float2 t1, t2, xj, yj;
+            if (wg == 0) {
+                i1a = p, i2a = q, ia = a + nm * b + nm2 * jg;
+                i1b = q, i2b = p, ib = a + nm * jg + nm2 * b;
+                t1 = conjf2(cmul(hra, Hbv));
+                t2 = cmul(Hav, conjf2(hb.hs[sl + b]));
+                xj = hb.hs[sl + jg];
+                yj = hb.hr[jg];
+            } else if (wg == 1) {
+                const int c = q - p + P.h;
+                i1a = p, i2a = c, ia = jg + nm * b + nm2 * a;
+                i1b = c, i2b = p, ib = jg + nm * a + nm2 * b;
+                t1 = cmul(hb.hdp[sl + b], conjf2(Hav));
+                t2 = cmul(hra, conjf2(Hbv));
+                xj = hb.hr[jg];
+                yj = hb.hdp[sl + jg];
+            } else {
+                const int d = p - q + P.h;
+                i1a = d, i2a = q, ia = b + nm * a + nm2 * jg;
+                i1b = q, i2b = d, ib = b + nm * jg + nm2 * a;
+                t1 = conjf2(cmul(hb.hdm[sl + b], Hav));
+                t2 = cmul(Hbv, conjf2(hra));
+                xj = hb.hr[jg];
+                yj = hb.hdm[sl + jg];
+            }
+            const float x = __uint_as_float(v[e]);
+            const double f = (q == p ? 1.0 : 2.0) * (double)x;  // 2 x, half weight on the diagonal
+            const int sa = P.slot[i1a + P.nf * i2a], sb = P.slot[i1b + P.nf * i2b];
+            if (sa >= 0) {
+                atomicAdd(P.sF + (size_t)sa * nm3 + ia, f);
+                atomicAdd(P.sR + (size_t)sa * nm3 + ia, f * (double)(t1.x * xj.x - t1.y * xj.y));
+            }
+            if (sb >= 0) {
+                atomicAdd(P.sF + (size_t)sb * nm3 + ib, f);
+                atomicAdd(P.sR + (size_t)sb * nm3 + ib, f * (double)(t2.x * yj.x - t2.y * yj.y));
+            }
         }
     }
 }

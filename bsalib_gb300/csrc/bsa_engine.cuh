@@ -66,6 +66,14 @@ struct Settings {
 
 struct BatchCase;  // one case of the batched Classic sweep (bsa_batch.cu)
 
+// Sampled grid points of the E-form contraction: slot[i1 + nf i2] = row in sF / sR
+// ([nslot][nm^3] FP64, device) of grid point (i1, i2), or -1.
+struct ESample {
+    const int *slot;
+    double *sF, *sR;
+    int nslot;
+};
+
 struct Engine {
     Inputs in;
     Settings set;
@@ -107,7 +115,7 @@ struct Engine {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr;
     DevBuf dL, dQ, dLogc, dPsdPar, dFrfM, dFrfK, dFrfC, dFreq, dS, dA, dPartF, dPartR, dOut, dPsdF, dWf, dPts,
         dPtsD, dBF, dBR, dMixA, dMixB, dMixH, dMixPart, dA32, dZones, dZidx, dWd3, dWd2, dMshT, dMshIdx, dLogc32, dL32,
-        dPod, dFlag;
+        dPod, dFlag, dSlot;
 
     // stats
     double last_ms = 0, last_ms_contraction = 0, last_ms_gemm = 0, last_points = 0;
@@ -137,7 +145,9 @@ struct Engine {
     int classic_export(PointSrc ps, const std::vector<double> &f, double *m3mf, double *m3mr);
     int contract(const PointSrc &ps, long long npts, double *m3mf, double *m3mr, double *bf_host, double *br_host);
     int contract_mixed(const PointSrc &ps, long long npts, double *m3mf, double *m3mr);
-    int contract_e(const PointSrc &ps, double *m3mf, double *m3mr);  // bsa_classic_e.cu
+    int contract_e(const PointSrc &ps, double *m3mf, double *m3mr, const ESample *smp = nullptr);  // bsa_classic_e.cu
+    // bsa_gpu_clsBispectraAt: Classic bispectra at listed grid points in the selected precision
+    int classic_points(const int *i1, const int *i2, long long npts, double *bf, double *br);
     int contract_diag(const PointSrc &ps, long long npts, int msh_form, double *m3mf, double *m3mr,
                       double *bf_host, double *br_host);
     int run_points(const double *fi, const double *fj, const double *w, double wuniform, long long npts,

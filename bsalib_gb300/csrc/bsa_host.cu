@@ -716,6 +716,112 @@ int Engine::run_points(const double *fi, const double *fj, const double *w, doub
     return BSA_OK;
 }
 
+// Classic bispectra at listed grid points (bsa_gpu_clsBispectraAt): FP64 through the point
+// form of the FP64 kernel on the grid's A table (S(f1 + f2) truncated or analytic as the
+// analysis reads it); BF16x3 through the sampled instantiation of the E-form contraction, the
+// analysis's own products (whole odd grid, truncated sum, at most 48 kept modes).
+int Engine::classic_points(const int *i1, const int *i2, long long npts, double *bf, double *br) {
+    kernels = 0;
+    h2d = d2h = 0;
+    last_ms_gemm = 0;
+    int rc = upload_problem();
+    if (rc) return rc;
+    if (set.onlyd) return fail(BSA_ERR_UNSUPPORTED, "per-point Classic bispectra need the full-tensor spectra");
+    std::vector<double> f;
+    if ((rc = classic_grid(f))) return rc;
+    const int nf = (int)f.size(), h = (nf - 1) / 2;
+    for (long long p = 0; p < npts; ++p)
+        if (i1[p] < 0 || i1[p] >= nf || i2[p] < 0 || i2[p] >= nf)
+            return fail(BSA_ERR_ARG, "grid point %lld = (%d, %d) outside the %d-point grid", p, i1[p], i2[p], nf);
+    const long long nm3 = dim_bisp();
+    const bool analytic = !classic_trunc;
+    cudaError_t e;
+    if ((e = cudaEventRecord(ev0, stream))) return cuda_fail(e, "event");
+    if (precision == BSA_PREC_BF16X3) {
+        if (analytic || !(nf & 1) || nme > kEFormMaxModes)
+            return fail(BSA_ERR_UNSUPPORTED,
+                        "split-precision point bispectra come from the E-form contraction: truncated S(f1+f2), odd "
+                        "grid, at most %d kept modes", kEFormMaxModes);
+        if ((rc = build_atable(f, true))) return rc;
+        // slot of every grid point (first occurrence of a repeated point)
+        std::vector<int> slot((size_t)nf * nf, -1), first((size_t)npts);
+        int nslot = 0;
+        for (long long p = 0; p < npts; ++p) {
+            int &s = slot[(size_t)i1[p] + (size_t)nf * i2[p]];
+            if (s < 0) s = nslot++;
+            first[p] = s;
+        }
+        if ((e = upload(dSlot, slot, stream)) || (e = dBF.reserve(sizeof(double) * (size_t)nslot * nm3)) ||
+            (e = dBR.reserve(sizeof(double) * (size_t)nslot * nm3)))
+            return cuda_fail(e, "allocating sampled bispectra");
+        PointSrc ps{};
+        ps.mode = kPointsGrid;
+        ps.nf = nf;
+        ps.n_pad = h;
+        ps.trunc = 1;
+        ps.sum_base = nf;
+        ps.wmode = kWeightUniform;
+        ps.wval = 1.0;
+        ps.fgrid = dFreq.as<double>();
+        ps.r0 = 0;
+        ps.nr = nf;
+        ESample smp{dSlot.as<int>(), dBF.as<double>(), dBR.as<double>(), nslot};
+        if ((rc = contract_e(ps, nullptr, nullptr, &smp))) return rc;
+        std::vector<double> hf((size_t)nslot * nm3), hr((size_t)nslot * nm3);
+        if ((e = cudaMemcpyAsync(hf.data(), smp.sF, sizeof(double) * hf.size(), cudaMemcpyDeviceToHost, stream)) ||
+            (e = cudaMemcpyAsync(hr.data(), smp.sR, sizeof(double) * hr.size(), cudaMemcpyDeviceToHost, stream)) ||
+            (e = cudaStreamSynchronize(stream)))
+            return cuda_fail(e, "sampled bispectra copy");
+        d2h += 16.0 * nslot * nm3;
+        for (long long p = 0; p < npts; ++p) {
+            if (bf) std::memcpy(bf + p * nm3, hf.data() + (size_t)first[p] * nm3, sizeof(double) * nm3);
+            if (br) std::memcpy(br + p * nm3, hr.data() + (size_t)first[p] * nm3, sizeof(double) * nm3);
+        }
+    } else {
+        std::vector<double> ftab = f;
+        if (analytic)
+            for (int s2 = 0; s2 < 2 * nf - 1; ++s2) ftab.push_back(2.0 * f[0] + s2 * (f[1] - f[0]));
+        if ((rc = build_atable(ftab, false))) return rc;
+        const size_t n = (size_t)npts;
+        std::vector<int> iz(n);
+        std::vector<double> f1(n), f2(n);
+        for (size_t p = 0; p < n; ++p) {
+            const int s2 = i1[p] + i2[p];
+            iz[p] = analytic ? nf + s2 : ((s2 - h >= 0 && s2 - h < nf) ? s2 - h : -1);
+            f1[p] = f[i1[p]];
+            f2[p] = f[i2[p]];
+        }
+        if ((e = dPts.reserve(n * 3 * sizeof(int))) || (e = dPtsD.reserve(n * 3 * sizeof(double))))
+            return cuda_fail(e, "points");
+        int *dix = dPts.as<int>(), *diy = dix + n, *diz = diy + n;
+        double *df1 = dPtsD.as<double>(), *df2 = df1 + n;
+        if ((e = cudaMemcpyAsync(dix, i1, n * sizeof(int), cudaMemcpyHostToDevice, stream)) ||
+            (e = cudaMemcpyAsync(diy, i2, n * sizeof(int), cudaMemcpyHostToDevice, stream)) ||
+            (e = cudaMemcpyAsync(diz, iz.data(), n * sizeof(int), cudaMemcpyHostToDevice, stream)) ||
+            (e = cudaMemcpyAsync(df1, f1.data(), n * sizeof(double), cudaMemcpyHostToDevice, stream)) ||
+            (e = cudaMemcpyAsync(df2, f2.data(), n * sizeof(double), cudaMemcpyHostToDevice, stream)))
+            return cuda_fail(e, "point upload");
+        h2d += (double)n * (3 * sizeof(int) + 2 * sizeof(double));
+        PointSrc ps{};
+        ps.mode = kPointsList;
+        ps.wmode = kWeightUniform;
+        ps.wval = 1.0;
+        ps.ix = dix;
+        ps.iy = diy;
+        ps.iz = diz;
+        ps.f1 = df1;
+        ps.f2 = df2;
+        std::vector<double> mf(nm3), mr(nm3);
+        if ((rc = contract(ps, npts, mf.data(), mr.data(), bf, br))) return rc;
+    }
+    last_points = (double)npts;
+    if ((e = cudaEventRecord(ev1, stream)) || (e = cudaEventSynchronize(ev1))) return cuda_fail(e, "event");
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ev0, ev1);
+    last_ms = ms;
+    return BSA_OK;
+}
+
 }  // namespace bsa
 
 using bsa::eng;
@@ -1045,6 +1151,12 @@ int bsa_gpu_clsBispectra(double *f_out, int nf_cap, int *nf, double *bisp_f, dou
     if (rc) return rc;
     if (f_out) std::memcpy(f_out, grid.data(), sizeof(double) * grid.size());
     return BSA_OK;
+}
+
+int bsa_gpu_clsBispectraAt(const int *i1, const int *i2, int npts, double *bisp_f, double *bisp_r) {
+    GUARD();
+    if (!i1 || !i2 || npts <= 0) return eng().fail(BSA_ERR_ARG, "empty point list");
+    return eng().classic_points(i1, i2, npts, bisp_f, bisp_r);
 }
 
 int bsa_gpu_mshBispectra(const double *fi, const double *fj, int npts, double *bfm, double *brm) {

@@ -9,12 +9,18 @@
 // array, so it never calls cudaMalloc, cudaFree or any allocating routine.
 //
 // The scratch array holds kScratchDoubles doubles (4 MiB) on every GPU that loads the
-// library, for the life of the process.  Every call shares it and overwrites it completely
+// library, for the life of the process.  It bounds the number of point groups the FP64
+// contraction runs in parallel: G = min(the allocating path's group count, 2^18 / nm^3).
+// Up to about 20 kept modes that is the allocating path's count; above it the launch has
+// fewer CTAs (nm = 32: 8 groups, 128 CTAs instead of about 1200; nm = 64: one group of 64
+// CTAs striding over every point), so for large mode counts and many points the allocating
+// entry point bsa_gpu_mshMoments is the faster choice.  Every call shares it and overwrites it completely
 // before reading it (each group writes all of its nm^3 partials), so nothing needs
 // clearing between calls; calls that overlap on the GPU (different streams, or other host
 // threads) race on it and must be serialised by the caller.
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstdio>
 
 #include "../../include/bsa_gpu.h"
@@ -29,8 +35,10 @@ constexpr int kMaxDevices = 64;
 static __device__ __align__(256) double g_noalloc_scratch[kScratchDoubles];
 
 // Device address of the scratch array, resolved once per device.  In host code the name
-// g_noalloc_scratch is only a host-side stand-in, not a device address.
-double *g_scratch_ptr[kMaxDevices] = {nullptr};
+// g_noalloc_scratch is only a host-side stand-in, not a device address.  Atomic so that two
+// host threads making the first call on one device both store the same resolved address
+// without a data race.
+std::atomic<double *> g_scratch_ptr[kMaxDevices] = {};
 
 int set_error(int code, const char *msg) {
     bsa::eng().last_error = msg;
@@ -56,7 +64,8 @@ extern "C" int bsa_gpu_pointMomentsNoAlloc(const double *A, int K, int nm, const
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return set_error(BSA_ERR_CUDA, "bsa_gpu_pointMomentsNoAlloc: cudaGetDevice failed");
     if (dev < 0 || dev >= kMaxDevices) return set_error(BSA_ERR_UNSUPPORTED, "bsa_gpu_pointMomentsNoAlloc: device ordinal too large");
-    if (!g_scratch_ptr[dev]) {
+    double *scratch = g_scratch_ptr[dev].load(std::memory_order_acquire);
+    if (!scratch) {
         // Set-up, once per device, with that device current.
         double *ptr = nullptr;
         e = cudaGetSymbolAddress((void **)&ptr, g_noalloc_scratch);
@@ -65,9 +74,9 @@ extern "C" int bsa_gpu_pointMomentsNoAlloc(const double *A, int K, int nm, const
             snprintf(buf, sizeof buf, "bsa_gpu_pointMomentsNoAlloc: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
             return set_error(BSA_ERR_CUDA, buf);
         }
-        g_scratch_ptr[dev] = ptr;
+        g_scratch_ptr[dev].store(ptr, std::memory_order_release);
+        scratch = ptr;
     }
-    double *scratch = g_scratch_ptr[dev];
 
     long long g = bsa::bfm_fp64_groups(npts, nm);
     const long long gmax = kScratchDoubles / (2 * nm3);

@@ -257,6 +257,17 @@ int bsa_gpu_batchClear(void);
  * Runs validation and the grid set-up of bsa_Run; for small grids (tests). */
 int bsa_gpu_clsBispectra(double *f_out, int nf_cap, int *nf, double *bisp_f, double *bisp_r);
 
+/* getBFMClsVect + getBRMClsVect at listed points of the Classic grid (functionsImpl.F90:1494-1538
+ * for B_F, :1598-1738 for B_R): grid point p is (f[i1[p]], f[i2[p]]), 0-based indices into the
+ * grid bsa_gpu_clsBispectra reports; bisp_f, bisp_r are (dim_bisp, npts), either may be NULL.
+ * Computed in the precision of bsa_gpu_setPrecision: BSA_PREC_FP64 evaluates the points with
+ * the FP64 kernel; BSA_PREC_BF16X3 returns the split-precision analysis's own per-point values
+ * -- the E-form tensor-core products of the whole grid, with the epilogue writing the listed
+ * points' bispectra instead of the moments (needs the truncated S(f1+f2), an odd grid and at
+ * most 48 kept modes; BSA_ERR_UNSUPPORTED otherwise).  Runs validation and the grid set-up of
+ * bsa_Run.  For measuring the split path's per-point error against the FP64 path. */
+int bsa_gpu_clsBispectraAt(const int *i1, const int *i2, int npts, double *bisp_f, double *bisp_r);
+
 /* getMshBFM / getMshBRM batched over npts arbitrary points (getFM_full_tnm_scalar_msh_,
  * functionsImpl.F90:247-465; getRM_full_scalar_msh_, :1031-1115, point-wise): bfm and brm
  * are (dim_bisp, npts); either may be NULL.  With the diagonal-only spectra these are the
@@ -281,10 +292,14 @@ int bsa_gpu_mshMoments(const double *fi, const double *fj, const double *w, int 
  *   m3mf, m3mr [nm^3]  outputs (m fastest); stream: a cudaStream_t (NULL = legacy stream).
  * Its scratch (per-group partial sums) is a fixed 4 MiB device array held by every GPU
  * that loads the library until the process exits; nm is limited to 64, where 2*nm^3
- * doubles fill it.  The first call on each device resolves the array's device address
- * (cudaGetSymbolAddress) and should be made before any stream capture.  All calls share
- * the array: calls that overlap on the GPU race and must be serialised by the caller.
- * Returns BSA_OK or BSA_ERR_ARG / BSA_ERR_CUDA (message in bsa_lastError). */
+ * doubles fill it.  The array bounds the contraction's point groups to
+ * G = min(bsa_gpu_mshMoments' group count, 2^18 / nm^3): the same parallelism up to about
+ * 20 kept modes, fewer CTAs above (nm = 32: 128 instead of about 1200; nm = 64: 64), where
+ * bsa_gpu_mshMoments is the faster choice for large point sets.  The first call on each
+ * device resolves the array's device address (cudaGetSymbolAddress) and should be made
+ * before any stream capture.  All calls share the array: calls that overlap on the GPU race
+ * and must be serialised by the caller.  Returns BSA_OK, BSA_ERR_ARG, BSA_ERR_CUDA, or
+ * BSA_ERR_UNSUPPORTED for a device ordinal of 64 or more (message in bsa_lastError). */
 int bsa_gpu_pointMomentsNoAlloc(const double *A, int K, int nm, const double *Q, const int *ix,
                                 const int *iy, const int *iz, const double *f1, const double *f2,
                                 const double *w, int npts, const double *Mm, const double *Km,

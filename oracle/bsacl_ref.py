@@ -12,7 +12,13 @@ loops then visit the triples (k, k, k), (j, j, k), (j, k, j), (k, j, j) and the 
 i > j > k, but not (k, k, j), (k, j, k), (j, k, k) for k < j, so it sums n^3 - 3 n (n - 1) / 2
 of the n^3 node triples.  plain_loop=True builds the kernel's other branch (the full
 triple loop, bsacl.cl:780-865): the recipe writes the source without that one #define line
-into a scratch folder, compiles it and deletes it."""
+into a scratch folder, compiles it and deletes it.  exact_literals=True likewise writes the
+kernel's two float PSD constants (70.7f, 2.f/3.f) in double precision, so that a comparison
+shows what else, if anything, separates the kernel from the oracle.
+
+`BsaclRef.groups` returns the kernel's per-work-group partials (sums over 16 consecutive pairs
+of the list, the finest output the kernel has: every work item writes its own pair's value
+only into the work group's local reduction array)."""
 from __future__ import annotations
 
 import ctypes as C
@@ -24,7 +30,9 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
-REF_SRC = "/root/reference/BsaCL/src"
+# The reference tree: BSALIB_REFERENCE names its root (default: where this build keeps it).
+REF_ROOT = os.environ.get("BSALIB_REFERENCE", "/root/reference")
+REF_SRC = os.path.join(REF_ROOT, "BsaCL", "src")
 WIPWG = 16  # work items per work group (power of two, >= 9 for the kernel's prefetch)
 
 
@@ -32,9 +40,16 @@ def available() -> bool:
     return os.path.exists(os.path.join(REF_SRC, "bsacl.cl")) and os.path.exists(os.path.join(REF_SRC, "_base.h"))
 
 
+# The kernel's two PSD constants written as float literals (evalFct, bsacl.cl:104, :118):
+# exact_literals=True builds a scratch copy with them written in double precision, which
+# isolates their effect (4.3e-8 on the spectra) from everything else the kernel computes.
+LITERALS = (("(BSACL_REAL)70.7f", "(BSACL_REAL)70.7", 1), ("2.f/3.f", "((BSACL_REAL)2/(BSACL_REAL)3)", 2))
+
+
 def build(ntc: int, nnl: int, nm: int, nn: int, nfi: int, nfj: int, psd_id: int = 1,
-          plain_loop: bool = False) -> str:
-    tag = f"tc{ntc}_nl{nnl}_nm{nm}_nn{nn}_f{nfi}x{nfj}_p{psd_id}" + ("_plain" if plain_loop else "")
+          plain_loop: bool = False, exact_literals: bool = False) -> str:
+    tag = (f"tc{ntc}_nl{nnl}_nm{nm}_nn{nn}_f{nfi}x{nfj}_p{psd_id}" + ("_plain" if plain_loop else "")
+           + ("_exact" if exact_literals else ""))
     so = os.path.join(OUT, f"libbsacl_ref_{tag}.so")
     deps = [os.path.join(HERE, "bsacl_shim.h"), os.path.join(HERE, "bsacl_ref_driver.c")]
     if os.path.exists(so) and all(os.path.getmtime(so) >= os.path.getmtime(d) for d in deps):
@@ -42,16 +57,23 @@ def build(ntc: int, nnl: int, nm: int, nn: int, nfi: int, nfj: int, psd_id: int 
     os.makedirs(OUT, exist_ok=True)
     src = os.path.join(REF_SRC, "bsacl.cl")
     tmp = None
-    if plain_loop:  # the source without its one optimised-loop #define, in a scratch folder
+    if plain_loop or exact_literals:  # an edited copy of the source, in a scratch folder
         with open(src) as fh:
             text = fh.read()
-        line = "#define _use_optimised_loop_\n"
-        if text.count(line) != 1:
-            raise RuntimeError("bsacl.cl: the optimised-loop switch is not where expected")
+        if plain_loop:  # without its one optimised-loop #define
+            line = "#define _use_optimised_loop_\n"
+            if text.count(line) != 1:
+                raise RuntimeError("bsacl.cl: the optimised-loop switch is not where expected")
+            text = text.replace(line, "\n")
+        if exact_literals:
+            for old, new, count in LITERALS:
+                if text.count(old) != count:
+                    raise RuntimeError(f"bsacl.cl: the literal {old} is not where expected")
+                text = text.replace(old, new)
         tmp = tempfile.TemporaryDirectory()
-        src = os.path.join(tmp.name, "bsacl_plain_loop.cl")
+        src = os.path.join(tmp.name, "bsacl_edited.cl")
         with open(src, "w") as fh:
-            fh.write(text.replace(line, "\n"))
+            fh.write(text)
     cmd = ["gcc", "-O2", "-fPIC", "-shared", "-pthread", "-w", "-ffp-contract=off",
            "-include", os.path.join(HERE, "bsacl_shim.h"),
            f"-DBSACL_CL_SOURCE=\"{src}\"", f"-DBSACL_BASE_DIR={REF_SRC}",
@@ -76,10 +98,12 @@ def _p(a):
 class BsaclRef:
     """The reference kernel for one problem size."""
 
-    def __init__(self, ntc, nnl, nm, nn, nfi, nfj, psd_id=1, plain_loop=False):
-        self.lib = C.CDLL(build(ntc, nnl, nm, nn, nfi, nfj, psd_id, plain_loop))
-        self.lib.bsacl_ref_run.argtypes = [C.c_void_p] * 14
-        self.lib.bsacl_ref_run.restype = C.c_int
+    def __init__(self, ntc, nnl, nm, nn, nfi, nfj, psd_id=1, plain_loop=False, exact_literals=False):
+        self.lib = C.CDLL(build(ntc, nnl, nm, nn, nfi, nfj, psd_id, plain_loop, exact_literals))
+        for fn in (self.lib.bsacl_ref_run, self.lib.bsacl_ref_groups):
+            fn.argtypes = [C.c_void_p] * 14
+            fn.restype = C.c_int
+        self.nwg = nfi * nfj // WIPWG + 1
         self.lib.bsacl_ref_psd.argtypes = [C.c_double] * 4
         self.lib.bsacl_ref_psd.restype = C.c_double
         self.nm = nm
@@ -88,6 +112,17 @@ class BsaclRef:
         return self.lib.bsacl_ref_psd(float(f), float(scl), float(std), float(ubar))
 
     def m3mr(self, tc, nodes_load, phitc, nod_corr, u, scl, std, winz, Mg, Cg, Kg, fi, fj):
+        return self._call(self.lib.bsacl_ref_run, self.nm ** 3, tc, nodes_load, phitc, nod_corr, u, scl, std, winz,
+                          Mg, Cg, Kg, fi, fj)
+
+    def groups(self, tc, nodes_load, phitc, nod_corr, u, scl, std, winz, Mg, Cg, Kg, fi, fj):
+        """Per-work-group partials (nwg, nm^3) before the host's weight: group g sums the
+        kernel's values of pairs g WIPWG .. g WIPWG + WIPWG - 1 of the list fi x fj (fi fastest)."""
+        out = self._call(self.lib.bsacl_ref_groups, self.nwg * self.nm ** 3, tc, nodes_load, phitc, nod_corr, u,
+                         scl, std, winz, Mg, Cg, Kg, fi, fj)
+        return out.reshape(self.nwg, self.nm ** 3)
+
+    def _call(self, fn, nout, tc, nodes_load, phitc, nod_corr, u, scl, std, winz, Mg, Cg, Kg, fi, fj):
         keep = [np.ascontiguousarray(tc, dtype=np.uint32), np.ascontiguousarray(nodes_load, dtype=np.uint32),
                 np.asfortranarray(phitc, dtype=np.float64), np.ascontiguousarray(nod_corr, dtype=np.float64),
                 np.ascontiguousarray(u, dtype=np.float64), np.ascontiguousarray(scl, dtype=np.float64),
@@ -95,8 +130,8 @@ class BsaclRef:
                 np.ascontiguousarray(Mg, dtype=np.float64), np.asfortranarray(Cg, dtype=np.float64),
                 np.ascontiguousarray(Kg, dtype=np.float64), np.ascontiguousarray(fi, dtype=np.float64),
                 np.ascontiguousarray(fj, dtype=np.float64)]
-        out = np.zeros(self.nm ** 3)
-        rc = self.lib.bsacl_ref_run(*[_p(a) for a in keep], _p(out))
+        out = np.zeros(nout)
+        rc = fn(*[_p(a) for a in keep], _p(out))
         if rc:
-            raise RuntimeError(f"bsacl_ref_run failed ({rc})")
+            raise RuntimeError(f"the reference kernel's driver failed ({rc})")
         return out

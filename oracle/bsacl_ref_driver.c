@@ -78,29 +78,48 @@ static void *work_item(void *p) {
     return NULL;
 }
 
+/* Runs every work group of the NDRange; m3out[g + i nwg] receives work group g's partial of
+ * modal triple i (the kernel's own output buffer). */
+static int run_all(const uint *tc, const uint *nodes_load, const double *phiTc, const double *nod_corr,
+                   const double *u, const double *scl, const double *std, const int *winz, const double *Mg,
+                   const double *Cg, const double *Kg, double *fi, double *fj, double *m3out) {
+    const size_t dim = (size_t)NM_EFF__ * NM_EFF__ * NM_EFF__;
+    const size_t nwg = (size_t)(NFI__ * NFJ__) / BSACL_WIpWG + 1;
+    g_ngrp0 = nwg;
+    item_t it[BSACL_WIpWG];
+    pthread_t th[BSACL_WIpWG];
+    for (size_t g1 = 0; g1 < dim; ++g1)
+        for (size_t g0 = 0; g0 < nwg; ++g0) {
+            b_expected = BSACL_WIpWG;
+            b_arrived = 0;
+            int started = 0;
+            for (int l = 0; l < BSACL_WIpWG; ++l) {
+                item_t a = {tc, nodes_load, phiTc, nod_corr, u, scl, std, winz, Mg, Cg, Kg, fi, fj, m3out, g0, g1,
+                            (size_t)l};
+                it[l] = a;
+                if (pthread_create(&th[l], NULL, work_item, &it[l])) break;
+                ++started;
+            }
+            for (int l = started; l < BSACL_WIpWG; ++l) barrier_leave();  /* items never started */
+            for (int l = 0; l < started; ++l) pthread_join(th[l], NULL);
+            if (started < BSACL_WIpWG) return -2;
+        }
+    return 0;
+}
+
 /* m3mr (NM^3, the kernel's modal order) of the frequency pairs fi x fj (NFI__ x NFJ__). */
 int bsacl_ref_run(const uint *tc, const uint *nodes_load, const double *phiTc, const double *nod_corr,
                   const double *u, const double *scl, const double *std, const int *winz, const double *Mg,
                   const double *Cg, const double *Kg, double *fi, double *fj, double *h_res) {
     const size_t dim = (size_t)NM_EFF__ * NM_EFF__ * NM_EFF__;
     const size_t nwg = (size_t)(NFI__ * NFJ__) / BSACL_WIpWG + 1;
-    g_ngrp0 = nwg;
     double *m3out = (double *)calloc(dim * nwg, sizeof(double));
-    item_t it[BSACL_WIpWG];
-    pthread_t th[BSACL_WIpWG];
     if (!m3out) return -1;
-    for (size_t g1 = 0; g1 < dim; ++g1)
-        for (size_t g0 = 0; g0 < nwg; ++g0) {
-            b_expected = BSACL_WIpWG;
-            b_arrived = 0;
-            for (int l = 0; l < BSACL_WIpWG; ++l) {
-                item_t a = {tc, nodes_load, phiTc, nod_corr, u, scl, std, winz, Mg, Cg, Kg, fi, fj, m3out, g0, g1,
-                            (size_t)l};
-                it[l] = a;
-                if (pthread_create(&th[l], NULL, work_item, &it[l])) return -2;
-            }
-            for (int l = 0; l < BSACL_WIpWG; ++l) pthread_join(th[l], NULL);
-        }
+    const int rc = run_all(tc, nodes_load, phiTc, nod_corr, u, scl, std, winz, Mg, Cg, Kg, fi, fj, m3out);
+    if (rc) {
+        free(m3out);
+        return rc;
+    }
     double dinfl = (fi[1] - fi[0]) * (fj[1] - fj[0]) * 4.0 * (M_PI * M_PI);
     for (size_t i = 0; i < dim; ++i) {
         double s = 0.0;
@@ -109,6 +128,25 @@ int bsacl_ref_run(const uint *tc, const uint *nodes_load, const double *phiTc, c
     }
     free(m3out);
     return 0;
+}
+
+/* The kernel's per-work-group partials before the host reduction and weight:
+ * groups[g dim + i] = sum over work group g's BSACL_WIpWG pairs (work item l of group g takes
+ * pair p = g BSACL_WIpWG + l, fi[p % NFI__], fj[p / NFI__]) of the kernel's value for modal
+ * triple i.  nwg = NFI__ NFJ__ / BSACL_WIpWG + 1 groups; pairs past the list contribute 0. */
+int bsacl_ref_groups(const uint *tc, const uint *nodes_load, const double *phiTc, const double *nod_corr,
+                     const double *u, const double *scl, const double *std, const int *winz, const double *Mg,
+                     const double *Cg, const double *Kg, double *fi, double *fj, double *groups) {
+    const size_t dim = (size_t)NM_EFF__ * NM_EFF__ * NM_EFF__;
+    const size_t nwg = (size_t)(NFI__ * NFJ__) / BSACL_WIpWG + 1;
+    double *m3out = (double *)calloc(dim * nwg, sizeof(double));
+    if (!m3out) return -1;
+    const int rc = run_all(tc, nodes_load, phiTc, nod_corr, u, scl, std, winz, Mg, Cg, Kg, fi, fj, m3out);
+    if (!rc)
+        for (size_t g = 0; g < nwg; ++g)
+            for (size_t i = 0; i < dim; ++i) groups[g * dim + i] = m3out[g + i * nwg];
+    free(m3out);
+    return rc;
 }
 
 /* The kernel's nodal wind PSD (evalFct) at one frequency. */

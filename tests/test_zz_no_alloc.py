@@ -88,6 +88,57 @@ def test_no_alloc_matches_allocating_entry_point(bsalib):
         sess.close()
 
 
+def test_no_alloc_clamped_groups_allocate_nothing(bsalib):
+    """33 kept modes: the fixed scratch holds 2^18 / 33^3 = 7 point groups where the allocating
+    path would run one per point (40 here), so this is the entry point's own clamped branch.
+    The device's free memory is read around the second call (the first one may load the
+    library's kernels): a call that allocates nothing leaves it unchanged."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("needs a CUDA device")
+    prob = tall_building(nodes=30, modes=33, nfreqs=5, df=0.3, seed=23)
+    o = Oracle(prob)
+    nm = o.nme
+    assert nm == 33 and (1 << 18) // nm ** 3 == 7
+    Q = np.ascontiguousarray(np.concatenate([o.phitc[:, :, tc + 2].T for tc in prob.settings.tc], axis=0))
+    K = Q.shape[0]
+    m = o.modes - 1
+    dev = torch.device("cuda:0")
+    T = lambda a, dt=torch.float64: torch.tensor(np.ascontiguousarray(a), dtype=dt, device=dev)
+    dM, dK, dC, dQ = T(prob.Mg[m]), T(prob.Kg[m]), T(prob.Cg[m, m]), T(Q)
+    rng = np.random.default_rng(9)
+    n = 40
+    fi, fj = rng.uniform(-1.2, 1.2, n), rng.uniform(-1.2, 1.2, n)
+    w = rng.uniform(0.2, 1.0, n)
+    dA = T(a_table(o, np.concatenate([fi, fj, fi + fj])))
+    d_ix, d_iy, d_iz = (T(v, torch.int32) for v in (np.arange(n), n + np.arange(n), 2 * n + np.arange(n)))
+    d_f1, d_f2, d_w = T(fi), T(fj), T(w)
+    out_f = torch.zeros(nm ** 3, dtype=torch.float64, device=dev)
+    out_r = torch.zeros(nm ** 3, dtype=torch.float64, device=dev)
+    p = lambda t: C.c_void_p(t.data_ptr())
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    args = (p(dA), K, nm, p(dQ), p(d_ix), p(d_iy), p(d_iz), p(d_f1), p(d_f2), p(d_w), n, p(dM), p(dK), p(dC),
+            p(out_f), p(out_r), stream)
+    sess = api.BsaSession(prob)
+    try:
+        ref_f, ref_r = sess.msh_moments(fi, fj, w)
+    finally:
+        sess.close()
+    for call in range(2):
+        out_f.fill_(float("nan"))
+        out_r.fill_(float("nan"))
+        torch.cuda.synchronize()
+        free0 = torch.cuda.mem_get_info()[0]
+        rc = bsalib.bsa_gpu_pointMomentsNoAlloc(*args)
+        assert rc == 0, bsalib.bsa_lastError()
+        torch.cuda.synchronize()
+        free1 = torch.cuda.mem_get_info()[0]
+        if call == 1:
+            assert free1 == free0
+        assert rel(out_f.cpu().numpy(), ref_f) < TOL
+        assert rel(out_r.cpu().numpy(), ref_r) < TOL
+
+
 def test_no_alloc_rejects_bad_sizes(bsalib):
     n = C.c_void_p(0)
     rc = bsalib.bsa_gpu_pointMomentsNoAlloc(n, 4, 65, n, n, n, n, n, n, n, 1, n, n, n, n, n, n)
