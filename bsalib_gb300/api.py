@@ -34,7 +34,11 @@ EXPORT_FN = C.CFUNCTYPE(None, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_doub
 
 
 class BsaError(RuntimeError):
-    pass
+    """A failed library call; `code` is the BSA_ERR_* status it returned."""
+
+    def __init__(self, msg, code=None):
+        super().__init__(msg)
+        self.code = code
 
 
 class Zone(C.Structure):
@@ -86,7 +90,7 @@ def load(path: Optional[str] = None):
         "bsa_Run": [vp] * 7, "bsa_computeSkewness": [i, vp, vp, vp],
         "bsa_gpu_setPrecision": [i], "bsa_gpu_setClassicTruncation": [i], "bsa_gpu_setClassicRows": [i, i],
         "bsa_gpu_clsBispectra": [vp, i, vp, vp, vp], "bsa_gpu_mshBispectra": [vp, vp, i, vp, vp],
-        "bsa_gpu_clsBispectraAt": [vp, vp, i, vp, vp],
+        "bsa_gpu_clsBispectraAt": [vp, vp, i, vp, vp], "bsa_gpu_setWaitTest": [i],
         "bsa_gpu_mshMoments": [vp, vp, vp, i, vp, vp], "bsa_gpu_getStats": [vp], "bsa_gpu_releaseDeviceCache": [], "bsa_gpu_setClassicForm": [i],
         "bsa_gpu_pointMomentsNoAlloc": [vp, i, i, vp, vp, vp, vp, vp, vp, vp, i, vp, vp, vp, vp, vp, vp],
         "bsa_gpu_mshZones": [vp, i, vp, vp, vp], "bsa_gpu_mshGenerateZones": [vp, i, vp],
@@ -97,7 +101,7 @@ def load(path: Optional[str] = None):
         "bsa_mlp_get_params": [i, vp, i], "bsa_mlp_set_params": [i, vp], "bsa_mlp_forward": [i, vp, i, vp],
         "bsa_mlp_gradients": [i, vp, vp, vp, i, vp, vp],
         "bsa_mlp_train": [i, vp, vp, vp, i, i, i, C.c_float, C.c_ulonglong, vp],
-        "bsa_computeBRdecomp": [vp, vp, vp], "bsa_computePeakFactors": [i, vp, vp, d, vp, vp, vp, vp],
+        "bsa_computeBRdecomp": [vp, vp, vp], "bsa_modalRecombination": [vp] * 11, "bsa_computePeakFactors": [i, vp, vp, d, vp, vp, vp, vp],
         "bsa_gpu_batchAdd": [vp], "bsa_gpu_batchCase": [i, vp, vp], "bsa_gpu_batchRun": [vp] * 5,
         "bsa_gpu_batchClear": [], "bsa_doValidateZoneDeltas": [i], "bsa_setBfmMLR": [i],
         "bsa_setMaxBkgPeakRestriction": [i], "bsa_setPremeshScheme": [i], "bsa_setPremeshMode": [i],
@@ -124,7 +128,7 @@ def _p(a):
 def check(rc: int, what: str = ""):
     if rc != BSA_OK:
         msg = load().bsa_lastError().decode(errors="replace")
-        raise BsaError(f"{what} failed ({rc}): {msg}")
+        raise BsaError(f"{what} failed ({rc}): {msg}", rc)
 
 
 class BsaSession:
@@ -321,6 +325,21 @@ class BsaSession:
         check(self.lib.bsa_computeSkewness(nm, _p(np.ascontiguousarray(m2)), _p(np.ascontiguousarray(m3)),
                                            _p(sk)), "bsa_computeSkewness")
         return sk
+
+    def modal_recombination(self, m2mr, m3mr, m2o2mr=None):
+        """bsa_modalRecombination: nodal m2 / m3 / m2o2 / sk per DOF, diag and CCC branches."""
+        nd = self.prob.phi.shape[0]
+        keys = ("m2_diag", "m3_diag", "m2o2_diag", "sk_diag", "m2_ccc", "m3_ccc", "m2o2_ccc", "sk_ccc")
+        out = {k: np.zeros(nd) for k in keys}
+        m2o2 = None if m2o2mr is None else np.ascontiguousarray(m2o2mr, dtype=np.float64)
+        check(self.lib.bsa_modalRecombination(_p(np.ascontiguousarray(m2mr, dtype=np.float64)),
+                                              _p(np.ascontiguousarray(m3mr, dtype=np.float64)),
+                                              None if m2o2 is None else _p(m2o2), *[_p(out[k]) for k in keys]),
+              "bsa_modalRecombination")
+        if self.dims()[1] == self.nmodes():
+            for k in keys[4:]:
+                del out[k]
+        return out
 
     def br_decomp(self, m2mf):
         """bsa_computeBRdecomp: (background, resonant) parts of each kept mode's variance."""

@@ -56,6 +56,9 @@ struct EParams {
     // in sF / sR ([slot][nm^3], m fastest), or -1 where the point is not sampled.
     const int *slot;
     double *sF, *sR;
+    // Diagnostics (bsa_gpu_setWaitTest): t + 1 makes CTA 0's MMA warp omit the accumulator-ready
+    // signal of its tile t, so the epilogue's bounded wait runs out; 0 = off.
+    int test_skip_tile1;
 };
 
 // Shared-memory float2 load the compiler does not hoist (keeps the per-mode FRF values out

@@ -87,6 +87,7 @@ struct Engine {
     std::vector<std::vector<double>> own_d;
     bool classic_sym = false;   // bsa_gpu_setClassicSymmetry: evaluate half the Classic grid
     bool use_e_form = true;     // bsa_gpu_setClassicForm: E form of the split contraction where it applies
+    int wait_test_tile1 = 0;    // bsa_gpu_setWaitTest: tile + 1 whose ready signal CTA 0 omits (0 = off)
     // Mesher controls (BsaLibData.F90:219-233, 273): delta validation, BFM multi-level
     // refinement, background peak restricted to the first direction, diagonal-crest scheme
     bool validate_deltas = true, bfm_mlr = true, bkg_restrict = false, premesh_diag_crest = false;
@@ -164,6 +165,7 @@ struct Engine {
     int run_mesher(double *m3mf, double *m3mr);
     int zones_export(const std::vector<ZoneDev> &zones);
     int br_decomp(const double *m2mf, double *bkg, double *res);
+    int modal_recomb(const double *m2mr, const double *m3mr, const double *m2o2mr, double *const *outs);
     int batch_add(int *id);
     void batch_install(const BatchCase &c);
     int batch_run(double *m3mf, double *m3mr, double *m2mr, double *case_ms, double *total_ms);

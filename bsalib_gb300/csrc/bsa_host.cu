@@ -1153,6 +1153,13 @@ int bsa_gpu_clsBispectra(double *f_out, int nf_cap, int *nf, double *bisp_f, dou
     return BSA_OK;
 }
 
+int bsa_gpu_setWaitTest(int tile) {
+    GUARD();
+    if (tile < -1) return eng().fail(BSA_ERR_ARG, "tile must be >= -1");
+    eng().wait_test_tile1 = tile + 1;
+    return BSA_OK;
+}
+
 int bsa_gpu_clsBispectraAt(const int *i1, const int *i2, int npts, double *bisp_f, double *bisp_r) {
     GUARD();
     if (!i1 || !i2 || npts <= 0) return eng().fail(BSA_ERR_ARG, "empty point list");

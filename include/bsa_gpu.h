@@ -172,6 +172,20 @@ int bsa_setBispExportCallback(bsa_brm_export_fn fn, void *user);
  * m2mf is bsa_Run's m2mf_cls (dim_psd); bkg, res have nm entries. */
 int bsa_computeBRdecomp(const double *m2mf, double *bkg, double *res);
 
+/* Nodal response moments by modal recombination (modalRecombination, app/bsa.F90:935-1053, the
+ * standalone driver's post-processing, which passes the kept modes' shapes over every DOF): for
+ * each DOF d of the modal matrix (bsa_setModalInfo's ndofs entries per output)
+ *   diag: m2 = sum_m m2mr(m, m) phi_dm^2, m3 = sum_m m3mr(m, m, m) phi_dm^3, m2o2 as m2;
+ *   CCC (complete cubic combination): m2 = sum_{j,k} m2mr(j, k) phi_dj phi_dk,
+ *         m3 = sum_{i,j,k} m3mr(i, j, k) phi_di phi_dj phi_dk, m2o2 as m2;
+ *   sk = m3 / m2^(3/2) for each.
+ * m2mr, m3mr (and m2o2mr, which may be NULL: its outputs are then zero) are bsa_Run's modal
+ * moments (dim_psd, dim_bisp).  Any output may be NULL.  With the diagonal-only spectra only
+ * the diag outputs are formed (the reference returns before the CCC). */
+int bsa_modalRecombination(const double *m2mr, const double *m3mr, const double *m2o2mr, double *m2_diag,
+                           double *m3_diag, double *m2o2_diag, double *sk_diag, double *m2_ccc, double *m3_ccc,
+                           double *m2o2_ccc, double *sk_ccc);
+
 /* bsa_computePeakFactors (BsaLibImpl.F90:1428-1517): Gaussian peak factor
  * g = gamma / beta + beta, beta = sqrt(2 ln(sqrt(m2o2 / m2) / 2pi * T)), and, when sk is
  * given, the non-Gaussian (Hermite model) positive / negative peak factors.  n entries.
@@ -376,6 +390,15 @@ int bsa_gpu_getStats(bsa_gpu_stats *st);
  * FP32 rounding.  Also read by bsa_gpu_batchRun.  No reference counterpart (reset by
  * bsa_Finalise). */
 int bsa_gpu_setClassicForm(int form);
+
+/* Diagnostics, no counterpart in the reference: exercises the bounded device waits.  Every
+ * mbarrier wait of the tensor-core kernels gives up after 2 s (or at once when another role of the
+ * launch has already given up), lets its in-flight copies and MMAs land, frees its TMEM and
+ * returns; the host then reports BSA_ERR_TIMEOUT and halts until bsa_Finalise.  tile >= 0 makes
+ * the next split-precision Classic analysis in the E form omit, in CTA 0, the MMA warp's
+ * accumulator-ready signal of that CTA's accumulator tile, so the epilogue's wait runs out (no
+ * fault, no copy left in flight); -1 switches it off.  Applies to one analysis. */
+int bsa_gpu_setWaitTest(int tile);
 
 /* Device memory.  Blocks the library releases (bsa_Finalise, buffer growth) are kept for reuse
  * by the next analysis, up to a quarter of the device memory, so repeated bsa_Init ...

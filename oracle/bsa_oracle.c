@@ -805,6 +805,57 @@ void orc_modal_recomb(int ndofs, int nmodes, const double *phi, const double *m2
     for (int d = 0; d < ndofs; ++d) sk_r[d] = m3_r[d] / pow(m2_r[d], 1.5);
 }
 
+/*
+ * modalRecombination, both branches (app/bsa.F90:935-1053), in the routine's loop order:
+ * out[0..5][ndofs] = m2 diag, m3 diag, m2o2 diag, m2 CCC, m3 CCC, m2o2 CCC; sk[0..1][ndofs] =
+ * diag and CCC skewness m3 / m2^(3/2).  is_diag: the spectra have one entry per mode (then the
+ * CCC rows are not formed).  m2o2mr may be NULL (its rows stay zero).  phi(ndofs, nmodes).
+ */
+void orc_modal_recomb_all(int ndofs, int nmodes, int is_diag, const double *phi, const double *m2mr,
+                          const double *m3mr, const double *m2o2mr, double *out, double *sk)
+{
+    for (int r = 0; r < 6 * ndofs; ++r) out[r] = 0.0;
+    double *m2d = out, *m3d = out + ndofs, *mod = out + 2 * ndofs;
+    double *m2f = out + 3 * ndofs, *m3f = out + 4 * ndofs, *mof = out + 5 * ndofs;
+    for (int im = 0; im < nmodes; ++im) {
+        size_t p2, p3;
+        if (is_diag) {
+            p2 = (size_t)im;
+            p3 = (size_t)im;
+        } else {
+            const size_t t = (size_t)im * nmodes;
+            p2 = t + im;
+            p3 = t * nmodes + p2;
+        }
+        for (int d = 0; d < ndofs; ++d) {
+            const double p1 = phi[I2(d, im, ndofs)];
+            double r = p1 * p1;
+            m2d[d] = m2d[d] + m2mr[p2] * r;
+            if (m2o2mr) mod[d] = mod[d] + m2o2mr[p2] * r;
+            r = r * p1;
+            m3d[d] = m3d[d] + m3mr[p3] * r;
+        }
+    }
+    for (int d = 0; d < ndofs; ++d) sk[d] = m3d[d] / pow(m2d[d], 1.5);
+    if (is_diag) return;
+    for (int k = 0; k < nmodes; ++k) {
+        const size_t t12 = (size_t)k * nmodes, t13 = t12 * nmodes;
+        for (int j = 0; j < nmodes; ++j) {
+            const size_t t23 = (size_t)j * nmodes, p2 = t12 + j;
+            for (int d = 0; d < ndofs; ++d) {
+                m2f[d] = m2f[d] + m2mr[p2] * phi[I2(d, j, ndofs)] * phi[I2(d, k, ndofs)];
+                if (m2o2mr) mof[d] = mof[d] + m2o2mr[p2] * phi[I2(d, j, ndofs)] * phi[I2(d, k, ndofs)];
+            }
+            for (int i = 0; i < nmodes; ++i) {
+                const size_t p3 = t13 + t23 + i;
+                for (int d = 0; d < ndofs; ++d)
+                    m3f[d] = m3f[d] + m3mr[p3] * phi[I2(d, i, ndofs)] * phi[I2(d, j, ndofs)] * phi[I2(d, k, ndofs)];
+            }
+        }
+    }
+    for (int d = 0; d < ndofs; ++d) sk[ndofs + d] = m3f[d] / pow(m2f[d], 1.5);
+}
+
 int orc_num_threads(void)
 {
 #ifdef _OPENMP

@@ -67,6 +67,7 @@ def lib():
         _lib.orc_msh_brm.argtypes = [vp, C.c_int, vp, C.c_int, vp, vp, vp]
         _lib.orc_skewness.argtypes = [C.c_int, vp, vp, vp]
         _lib.orc_modal_recomb.argtypes = [C.c_int, C.c_int, vp, vp, vp, vp, vp, vp]
+        _lib.orc_modal_recomb_all.argtypes = [C.c_int, C.c_int, C.c_int, vp, vp, vp, vp, vp, vp]
         _lib.orc_rect_zone.argtypes = [vp] + [C.c_double] * 6 + [C.c_int] * 4 + [C.c_double, vp, vp]
         _lib.orc_rect_zone_diag.argtypes = _lib.orc_rect_zone.argtypes
         _lib.orc_classic_vect_diag.argtypes = [vp, C.c_int, vp] + [vp] * 7
@@ -327,6 +328,22 @@ class Oracle:
         lib().orc_modal_recomb(nd, phi.shape[1], _p(phi), _p(np.ascontiguousarray(m2mr)),
                                _p(np.ascontiguousarray(m3mr)), _p(m2), _p(m3), _p(sk))
         return m2, m3, sk
+
+    def modal_recomb_all(self, m2mr, m3mr, m2o2mr=None):
+        """modalRecombination, both branches (app/bsa.F90:935-1053): dict of m2 / m3 / m2o2 / sk,
+        diag and ccc, per DOF of the modal matrix."""
+        phi = np.asfortranarray(self.prob.phi[:, self.modes - 1])
+        nd = phi.shape[0]
+        is_diag = int(np.size(m3mr) == phi.shape[1])
+        out, sk = np.zeros(6 * nd), np.zeros(2 * nd)
+        lib().orc_modal_recomb_all(nd, phi.shape[1], is_diag, _p(phi), _p(np.ascontiguousarray(m2mr)),
+                                   _p(np.ascontiguousarray(m3mr)),
+                                   None if m2o2mr is None else _p(np.ascontiguousarray(m2o2mr)), _p(out), _p(sk))
+        out = out.reshape(6, nd)
+        res = {"m2_diag": out[0], "m3_diag": out[1], "m2o2_diag": out[2], "sk_diag": sk[:nd]}
+        if not is_diag:
+            res.update({"m2_ccc": out[3], "m3_ccc": out[4], "m2o2_ccc": out[5], "sk_ccc": sk[nd:]})
+        return res
 
     # -- independent numpy restatements -----------------------------------------------------
     def coherence_matrix(self, tc):

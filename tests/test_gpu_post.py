@@ -74,3 +74,24 @@ def test_peak_factors_vs_oracle(bsalib):
     assert rc0 == api.BSA_OK and rel(g0, eg) < 1e-14
     assert skip1 == 1 and skip2 == 1
     assert np.array_equal(after["m3mr_cls"], out["m3mr_cls"])
+
+
+@pytest.mark.parametrize("onlyd", [0, 1])
+def test_modal_recombination_vs_oracle(bsalib, onlyd):
+    """bsa_modalRecombination (app/bsa.F90:935-1053) on the modal moments of an FP64 analysis,
+    against the oracle's restatement: nodal m2 / m3 / m2o2 / skewness of both branches."""
+    prob = tall_building(nodes=40, modes=6, nfreqs=9, df=0.3, seed=4)
+    prob.settings = dataclasses.replace(prob.settings, onlyd=onlyd)
+    s = api.BsaSession(prob, precision=api.PREC_FP64)
+    try:
+        r = s.run()
+        got = s.modal_recombination(r["m2mr_cls"], r["m3mr_cls"], r["m2o2mr_cls"])
+        no_m2o2 = s.modal_recombination(r["m2mr_cls"], r["m3mr_cls"])
+    finally:
+        s.close()
+    ref = Oracle(prob).modal_recomb_all(r["m2mr_cls"], r["m3mr_cls"], r["m2o2mr_cls"])
+    assert sorted(got) == sorted(ref)
+    for k in ref:
+        assert rel(got[k], ref[k]) < TOL, k
+    assert np.all(no_m2o2["m2o2_diag"] == 0.0)
+    assert rel(no_m2o2["m3_diag"], ref["m3_diag"]) < TOL

@@ -65,3 +65,43 @@ def test_peak_factors_skip_cases():
     o = Oracle(cantilever_tower(nfreqs=5, df=0.4, nodes=4))
     assert o.peak_factors(np.ones(3), np.zeros(3), 600.0)[0] == 1
     assert o.peak_factors(np.ones(3), np.full(3, 1e-4), 1.0)[0] == 2
+
+
+@pytest.mark.parametrize("diag", [False, True])
+def test_modal_recombination_vs_numpy(diag):
+    """modalRecombination (app/bsa.F90:935-1053) restated in the oracle, against einsum sums
+    written from the formulas: diag = sum_m M(m..m) phi_m^p, CCC = the full contraction."""
+    prob = tall_building(nodes=12, modes=5, nfreqs=7, df=0.3, seed=8)
+    o = Oracle(prob)
+    nm = o.nme
+    rng = np.random.default_rng(3)
+    if diag:
+        m2, m3, m2o2 = rng.uniform(0.5, 2, nm), rng.normal(size=nm), rng.uniform(0.5, 2, nm)
+    else:
+        A = rng.normal(size=(nm, nm))
+        m2 = (A @ A.T + nm * np.eye(nm)).ravel(order="F")
+        m3 = rng.normal(size=nm ** 3)
+        m2o2 = (A.T @ A + np.eye(nm)).ravel(order="F")
+    out = o.modal_recomb_all(m2, m3, m2o2)
+    phi = prob.phi[:, o.modes - 1]
+    if diag:
+        e2, e3 = m2, m3
+    else:
+        M2, M3 = m2.reshape(nm, nm, order="F"), m3.reshape(nm, nm, nm, order="F")
+        e2, e3 = np.diagonal(M2), np.array([M3[m, m, m] for m in range(nm)])
+    d2 = (phi ** 2) @ e2
+    d3 = (phi ** 3) @ e3
+    assert rel(out["m2_diag"], d2) < 1e-13 and rel(out["m3_diag"], d3) < 1e-13
+    assert rel(out["sk_diag"], d3 / d2 ** 1.5) < 1e-12
+    if diag:
+        assert "m2_ccc" not in out
+        return
+    c2 = np.einsum("dj,dk,jk->d", phi, phi, M2)
+    c3 = np.einsum("di,dj,dk,ijk->d", phi, phi, phi, M3)
+    co = np.einsum("dj,dk,jk->d", phi, phi, m2o2.reshape(nm, nm, order="F"))
+    assert rel(out["m2_ccc"], c2) < 1e-12 and rel(out["m3_ccc"], c3) < 1e-12
+    assert rel(out["m2o2_ccc"], co) < 1e-12
+    assert rel(out["sk_ccc"], c3 / c2 ** 1.5) < 1e-11
+    # the CCC branch of the older restatement agrees
+    m2o, m3o, sko = o.modal_recomb(m2, m3)
+    assert rel(out["m3_ccc"], m3o) < 1e-14 and rel(out["sk_ccc"], sko) < 1e-14
