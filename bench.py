@@ -310,12 +310,16 @@ def learned_leg():
 
 
 def sweep_leg():
-    """The batched Classic sweep (bsa_gpu_batch*): 8 seeded random structures x 8 mean wind
-    speeds (nodes 30-600, 4-40 kept modes, grids of 129-513 points), one batched evaluation
-    against one split-precision bsa_Run per case: Classic grid points per second of both,
-    per-case completion latencies inside the batched launch, largest relative difference."""
+    """The batched Classic sweep (bsa_gpu_batch*) at the parametric-sweep configuration: 512
+    seeded random structures x 8 mean wind speeds 15-50 m/s (nodes 30-600, 4-40 kept modes,
+    grids of 129-513 points), one batched evaluation against one split-precision bsa_Run per
+    case, and the plain FP64 GPU path on 64 seeded cases: Classic grid points per second of
+    each, per-case completion latencies inside the batched launch, largest relative difference."""
     from bsalib_gb300 import sweep
-    return sweep.run(structures=8, winds=8, seed0=5000, check=True)
+    t0 = time.perf_counter()
+    res = sweep.run(structures=512, winds=8, seed0=5000, check=True, fp64_cases=64)
+    res["leg_wall_s"] = time.perf_counter() - t0
+    return res
 
 
 CONFIG = {"workload": WORKLOAD, "nodes": 400, "modes": 24, "ntc": 2, "grid": 1025,

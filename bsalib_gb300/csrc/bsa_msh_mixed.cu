@@ -805,14 +805,29 @@ bool axis_aligned(const ZoneDev &z, ZoneDev &out) {
     return false;
 }
 
+// Distinct frequencies of a zone batch.  Values closer than kFreqTol (1 + |f|) are one entry:
+// the sums r_i + c_j of lattices with equal steps on both axes repeat up to the last bits of
+// their rounding, and one A(f) row serves them all (A(f) moves on the scale of the spectra's
+// bandwidths, ~1e-3 Hz, not 1e-12 Hz).  A run of sorted values within the tolerance of its
+// first element keeps that first element; at() returns the nearest kept value.
+constexpr double kFreqTol = 1e-12;
+
 struct FreqIndex {
     std::vector<double> v;
     void add(double f) { v.push_back(f); }
     void seal() {
         std::sort(v.begin(), v.end());
-        v.erase(std::unique(v.begin(), v.end()), v.end());
+        size_t w = 0;
+        for (size_t r = 0; r < v.size(); ++r)
+            if (w == 0 || v[r] - v[w - 1] > kFreqTol * (1.0 + std::fabs(v[w - 1]))) v[w++] = v[r];
+        v.resize(w);
     }
-    int at(double f) const { return (int)(std::lower_bound(v.begin(), v.end(), f) - v.begin()); }
+    int at(double f) const {
+        const size_t i = (size_t)(std::lower_bound(v.begin(), v.end(), f) - v.begin());
+        if (i == v.size()) return (int)i - 1;
+        if (i > 0 && f - v[i - 1] <= v[i] - f) return (int)i - 1;
+        return (int)i;
+    }
 };
 
 }  // namespace
@@ -1042,7 +1057,13 @@ int Engine::run_zones_mixed(const std::vector<ZoneDev> &zones, double *m3mf, dou
         const double Kp = (double)(((K + 63) / 64) * 64), Mp = (double)(((nm * nm + 127) / 128) * 128);
         const double per_u = Mp * Kp * 4.0, per_col = NMT * Kp * 4.0;
         const double per_pt = 2.0 * NMT * Kp * 4.0 + 3.0 * nm3 * 4.0, per_q = 3.0 * nm * 8.0 + 4.0;
-        const double budget = 12e9;
+        // as much of the zone list per pass as 40 % of the device memory holds (one pass for the
+        // reference layouts of the bench's structures on a GB300: the 60-mode bridge needs about
+        // 88 GB), at least 4 GB; from the total, not the free memory, so the batching of a zone
+        // list does not depend on what earlier analyses left allocated
+        size_t fr = 0, tot = 0;
+        if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) tot = 0;
+        const double budget = std::max(4e9, 0.4 * (double)tot);
         size_t b0 = 0;
         while (b0 < axis.size()) {
             std::vector<double> uf;

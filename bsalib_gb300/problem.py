@@ -285,14 +285,8 @@ def packed_coherence(z: np.ndarray, U: np.ndarray, C: float) -> np.ndarray:
     """Davenport coherence base c_ij = exp(-C |z_i - z_j| / Ubar_ij), packed upper
     triangle in the order of util_getCorrVectIndex (src/utils/utility.F90:60-71)."""
     nn = z.size
-    out = np.empty((nn * nn + nn) // 2, dtype=F64)
-    p = 0
-    for i in range(nn):
-        dz = np.abs(z[i] - z[i:])
-        ub = 0.5 * (U[i] + U[i:])
-        out[p:p + nn - i] = np.exp(-C * dz / ub)
-        p += nn - i
-    return out
+    i, j = np.triu_indices(nn)  # row-major upper triangle: (0,0..nn-1), (1,1..nn-1), ...
+    return np.exp(-C * np.abs(z[i] - z[j]) / (0.5 * (U[i] + U[j])))
 
 
 def _unit_max(phi: np.ndarray) -> np.ndarray:
