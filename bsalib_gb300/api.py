@@ -33,6 +33,16 @@ EXPORT_FN = C.CFUNCTYPE(None, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_doub
                         C.c_void_p)
 
 
+PLAN_CLS_FORM, PLAN_CLS_E_WIDTH, PLAN_CLS_D_WIDTH, PLAN_MSH_WIDTH = 1, 2, 3, 4
+
+
+def tile_plan(family: int, nm: int, K: int, nf: int = 0) -> int:
+    """The tile-plan value the library uses for a case (bsa_gpu_getTilePlan)."""
+    v = C.c_int(0)
+    check(load().bsa_gpu_getTilePlan(family, nm, K, nf, C.byref(v)), "bsa_gpu_getTilePlan")
+    return v.value
+
+
 class BsaError(RuntimeError):
     """A failed library call; `code` is the BSA_ERR_* status it returned."""
 
@@ -51,7 +61,7 @@ class Zone(C.Structure):
 class Stats(C.Structure):
     _fields_ = [("ms_total", C.c_double), ("ms_contraction", C.c_double), ("ms_gemm", C.c_double),
                 ("points", C.c_double), ("h2d_bytes", C.c_double), ("d2h_bytes", C.c_double),
-                ("kernels", C.c_int), ("precision", C.c_int)]
+                ("kernels", C.c_int), ("precision", C.c_int), ("graphs", C.c_int)]
 
 
 def header_symbols():
@@ -91,6 +101,9 @@ def load(path: Optional[str] = None):
         "bsa_gpu_setPrecision": [i], "bsa_gpu_setClassicTruncation": [i], "bsa_gpu_setClassicRows": [i, i],
         "bsa_gpu_clsBispectra": [vp, i, vp, vp, vp], "bsa_gpu_mshBispectra": [vp, vp, i, vp, vp],
         "bsa_gpu_clsBispectraAt": [vp, vp, i, vp, vp], "bsa_gpu_setWaitTest": [i],
+        "bsa_gpu_setMesherGraphs": [i], "bsa_enableVisualMode": [], "bsa_setVisualIndexes": [vp, i], "bsa_setBRMExportDefaultMode": [i],
+        "bsa_gpu_setTilePlan": [i] * 8, "bsa_gpu_clearTilePlans": [], "bsa_gpu_loadTilePlans": [C.c_char_p],
+        "bsa_gpu_getTilePlan": [i, i, i, i, vp],
         "bsa_gpu_mshMoments": [vp, vp, vp, i, vp, vp], "bsa_gpu_getStats": [vp], "bsa_gpu_releaseDeviceCache": [], "bsa_gpu_setClassicForm": [i],
         "bsa_gpu_pointMomentsNoAlloc": [vp, i, i, vp, vp, vp, vp, vp, vp, vp, i, vp, vp, vp, vp, vp, vp],
         "bsa_gpu_mshZones": [vp, i, vp, vp, vp], "bsa_gpu_mshGenerateZones": [vp, i, vp],
@@ -378,6 +391,18 @@ class BsaSession:
 
         self._export = EXPORT_FN(tramp)  # kept alive with the session
         check(self.lib.bsa_setBispExportCallback(self._export, None), "bsa_setBispExportCallback")
+
+    def set_visual(self, indexes, modal=True):
+        """bsa_enableVisualMode + bsa_setVisualIndexes: bsa_Run writes bsaexport_cls.brm (modal,
+        Classic), bsaexport_msh.brm / .brn (Mesher) in the working directory."""
+        idx = np.ascontiguousarray(indexes, dtype=np.int32)
+        self._keep.append(idx)
+        check(self.lib.bsa_enableVisualMode(), "bsa_enableVisualMode")
+        check(self.lib.bsa_setVisualIndexes(_p(idx), int(bool(modal))), "bsa_setVisualIndexes")
+
+    def set_brm_export_mode(self, mode=1):
+        """bsa_setBRMExportDefaultMode: 1 (base) writes the Mesher's bsaexport_msh.brm."""
+        check(self.lib.bsa_setBRMExportDefaultMode(int(mode)), "bsa_setBRMExportDefaultMode")
 
     def msh_zones_diag(self, zones):
         """Split-precision zone integration with each zone's own m3mr(m, m, m):

@@ -696,6 +696,7 @@ int Engine::batch_run(double *m3mf, double *m3mr, double *m2mr, double *case_ms,
     const int nc = (int)g_batch.size();
     if (nc == 0) return fail(BSA_ERR_STATE, "empty batch");
     kernels = 0;
+    graph_launches = 0;
     h2d = d2h = 0;
     std::vector<long long> off3(nc), off2(nc);
     long long t3 = 0, t2 = 0;
@@ -713,20 +714,20 @@ int Engine::batch_run(double *m3mf, double *m3mr, double *m2mr, double *case_ms,
         return cuda_fail(e, "device query");
     // groups: same NMT, cases in K order, device bytes bounded
     // FRF-table width of a case; above 32 modes two halves of 32 (JH = 2)
-    auto nmt_of = [](int nm) { return nm <= 8 ? 8 : nm <= 16 ? 16 : nm <= 24 ? 24 : nm <= 32 ? 32 : 64; };
     std::vector<int> order(nc);
     for (int c = 0; c < nc; ++c) order[c] = c;
     // E form (bsa_classic_e.cu) for cases of at most 48 kept modes on odd grids with the
     // truncated sum; those form groups of their own
     auto e_ok = [&](int c) {
         const BatchCase &b = g_batch[c];
-        return use_e_form && b.nme <= kEFormMaxModes && b.trunc && (b.f.size() & 1) != 0;
+        return use_e_form && b.nme <= kEFormMaxModes && b.trunc && (b.f.size() & 1) != 0 &&
+               plan_prefer_e(b.nme, b.K, (int)b.f.size());
     };
     // group width: the FRF-table width of the D1 / D3 form, or of the E form (8, 16, 24; 32 and
     // 48 as two mode halves of 16 and 24)
     auto width = [&](int c) {
-        const int nm = g_batch[c].nme;
-        return e_ok(c) ? (nm <= 8 ? 8 : nm <= 16 ? 16 : nm <= 24 ? 24 : nm <= 32 ? 32 : 48) : nmt_of(nm);
+        const BatchCase &b = g_batch[c];
+        return e_ok(c) ? plan_e_width(b.nme, b.K, (int)b.f.size()) : plan_d_width(b.nme, b.K, (int)b.f.size());
     };
     std::sort(order.begin(), order.end(), [&](int x, int y) {
         const int a = width(x), b = width(y);

@@ -315,8 +315,8 @@ static cudaError_t launch_k(cudaStream_t st, const CUtensorMap *maps, const EPar
 int Engine::contract_e(const PointSrc &ps, double *m3mf, double *m3mr, const ESample *smp) {
     using namespace ecls;
     const int nf = ps.nf, nm = nme;
-    const int NMT = nm <= 8 ? 8 : nm <= 16 ? 16 : nm <= 24 ? 24 : nm <= 32 ? 16 : 24;
-    const int JH = nm <= 24 ? 1 : 2, W = NMT * JH;
+    const int W = plan_e_width(nm, K, nf);  // 8, 16, 24; 32 and 48 as two mode halves
+    const int JH = W <= 24 ? 1 : 2, NMT = W / JH;
     const int NC = kBN / NMT;
     const int Kp = ((K + kBK - 1) / kBK) * kBK;
     const int Mp = ((nm * nm + kBM - 1) / kBM) * kBM;

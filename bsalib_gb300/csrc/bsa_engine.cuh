@@ -15,6 +15,14 @@ namespace bsa {
 // in two mode halves).
 constexpr int kEFormMaxModes = 48;
 
+// Tile plans (bsa_plans.cu): the autotuned shape of each split-precision contraction, or the
+// default rule.  Widths: E form 8 / 16 / 24 / 32 (2 x 16) / 48 (2 x 24); D1 / D3 form 8 / 16 / 24 /
+// 32 / 64 (2 x 32); Mesher NMT a multiple of 8 in [nm, 64].
+int plan_e_width(int nm, int K, int nf);
+int plan_d_width(int nm, int K, int nf);
+bool plan_prefer_e(int nm, int K, int nf);
+int plan_msh_width(int nm, int K);
+
 // Device buffer that only grows (kept across runs; freed by bsa_Finalise).
 // Frees the device blocks the engine keeps for reuse after bsa_Finalise.
 void release_device_cache();
@@ -65,6 +73,7 @@ struct Settings {
 };
 
 struct BatchCase;  // one case of the batched Classic sweep (bsa_batch.cu)
+struct BrmSink;    // an open response-bispectrum export file (bsa_brmfile.cu)
 
 // Sampled grid points of the E-form contraction: slot[i1 + nf i2] = row in sF / sR
 // ([nslot][nm^3] FP64, device) of grid point (i1, i2), or -1.
@@ -88,11 +97,17 @@ struct Engine {
     bool classic_sym = false;   // bsa_gpu_setClassicSymmetry: evaluate half the Classic grid
     bool use_e_form = true;     // bsa_gpu_setClassicForm: E form of the split contraction where it applies
     int wait_test_tile1 = 0;    // bsa_gpu_setWaitTest: tile + 1 whose ready signal CTA 0 omits (0 = off)
+    bool msh_graphs = true;     // bsa_gpu_setMesherGraphs: each Mesher zone pass as one CUDA graph
     // Mesher controls (BsaLibData.F90:219-233, 273): delta validation, BFM multi-level
     // refinement, background peak restricted to the first direction, diagonal-crest scheme
     bool validate_deltas = true, bfm_mlr = true, bkg_restrict = false, premesh_diag_crest = false;
     bsa_brm_export_fn export_fn = nullptr;  // bsa_setBispExportCallback
     void *export_user = nullptr;
+    // bsa_enableVisualMode / bsa_setVisualIndexes / bsa_setBRMExportDefaultMode (bsa_brmfile.cu)
+    bool visual = false, visual_modal = true;
+    int visual_idx[3] = {1, 1, 1};
+    int brm_export_mode = 0;
+    BrmSink *brm_sink = nullptr;
     double pod_trunc_lim = 0.0;
     int pod_nmodes = 0;
     // The Mesher's POD form truncates only when one of the two was set to a value that
@@ -122,6 +137,7 @@ struct Engine {
     double last_ms = 0, last_ms_contraction = 0, last_ms_gemm = 0, last_points = 0;
     double h2d = 0, d2h = 0;
     int kernels = 0;
+    int graph_launches = 0;     // CUDA graphs launched by the last run
     cudaEvent_t evg0 = nullptr, evg1 = nullptr;
 
     int fail(int code, const char *fmt, ...);
@@ -164,6 +180,12 @@ struct Engine {
     int mesher_zones(std::vector<ZoneDev> &zones, std::vector<int> &policy);
     int run_mesher(double *m3mf, double *m3mr);
     int zones_export(const std::vector<ZoneDev> &zones);
+    // response-bispectrum export files (bsa_brmfile.cu); emit_brm also feeds the callback
+    bool brm_file_wanted(bool classic) const;
+    int brm_file_open(bool classic, int nzones);
+    int brm_file_zone(int id, int nI, int nJ);
+    int emit_brm(int npts, const double *f1, const double *f2, const double *brm);
+    int brm_file_close(long long total);
     int br_decomp(const double *m2mf, double *bkg, double *res);
     int modal_recomb(const double *m2mr, const double *m3mr, const double *m2o2mr, double *const *outs);
     int batch_add(int *id);

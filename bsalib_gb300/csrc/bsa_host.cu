@@ -138,6 +138,11 @@ void Engine::reset_inputs() {
     pod_nmodes = 0;
     export_fn = nullptr;
     export_user = nullptr;
+    brm_file_close(-1);
+    visual = false;
+    visual_modal = true;
+    visual_idx[0] = visual_idx[1] = visual_idx[2] = 1;
+    brm_export_mode = 0;
     classic_sym = false;
     use_e_form = true;
     validate_deltas = true;
@@ -150,7 +155,7 @@ void Engine::free_device() {
     if (stream) cudaStreamSynchronize(stream);  // the blocks go back to the cache for reuse
     for (DevBuf *b : {&dL, &dQ, &dLogc, &dPsdPar, &dFrfM, &dFrfK, &dFrfC, &dFreq, &dS, &dA, &dPartF, &dPartR,
                       &dOut, &dPsdF, &dWf, &dPts, &dPtsD, &dBF, &dBR, &dMixA, &dMixB, &dMixH, &dMixPart, &dA32,
-                      &dZones, &dZidx, &dWd3, &dWd2, &dMshT, &dMshIdx, &dLogc32, &dL32, &dPod, &dFlag})
+                      &dZones, &dZidx, &dWd3, &dWd2, &dMshT, &dMshIdx, &dLogc32, &dL32, &dPod, &dFlag, &dSlot})
         b->release();
     if (stream) cudaStreamDestroy(stream);
     stream = nullptr;
@@ -432,6 +437,7 @@ int Engine::classic_grid(std::vector<double> &f) {
 int Engine::run_classic(double *m2mf, double *m2mr, double *m2o2mr, double *m3mf, double *m3mr, double *bf_host,
                         double *br_host, std::vector<double> *grid_out) {
     kernels = 0;
+    graph_launches = 0;
     h2d = d2h = 0;
     last_ms_gemm = 0;
     int rc = upload_problem();
@@ -519,7 +525,9 @@ int Engine::run_classic(double *m2mf, double *m2mr, double *m2o2mr, double *m3mf
         // whole grid once, which half the rows would not improve on: there the symmetry is not
         // applied.
         const bool e_form = mixed && use_e_form && nme <= kEFormMaxModes && !analytic && (nf & 1) && r0 == 0 && r1 == nf;
-        const bool sym = classic_sym && set.defsc == 1 && !bf_host && !br_host && !export_fn && !e_form;
+        const bool file_export = brm_file_wanted(true);
+        const bool sym =
+            classic_sym && set.defsc == 1 && !bf_host && !br_host && !export_fn && !file_export && !e_form;
         if (sym) {
             ps.sym_rows = ps.n_pad;
             ps.nr = std::max(0, std::min(r1, ps.n_pad + 1) - r0);
@@ -530,7 +538,7 @@ int Engine::run_classic(double *m2mf, double *m2mr, double *m2o2mr, double *m3mf
             if (m3mf) std::memset(m3mf, 0, sizeof(double) * nb);
             if (m3mr) std::memset(m3mr, 0, sizeof(double) * nb);
             rc = BSA_OK;
-        } else if (export_fn && !bf_host && !br_host) {
+        } else if ((export_fn || file_export) && !bf_host && !br_host) {
             if (r0 != 0 || r1 != nf) return fail(BSA_ERR_ARG, "the bispectrum export needs the full grid");
             rc = classic_export(ps, f, m3mf, m3mr);
         } else {
@@ -564,6 +572,8 @@ int Engine::classic_export(PointSrc ps, const std::vector<double> &f, double *m3
     }
     const long long budget = 1LL << 30;  // bytes of one block's host bispectra
     const int cols = (int)std::max(1LL, std::min((long long)nf, budget / (16LL * nf * nb)));
+    // the export file, if this analysis writes one: the grid as one rectangular zone
+    if ((rc = brm_file_open(true, 1)) || (rc = brm_file_zone(1, nf, nf))) return rc;
     std::vector<double> br((size_t)cols * nf * nb), f1((size_t)cols * nf), f2((size_t)cols * nf);
     std::vector<double> accF(nb, 0.0), accR(nb, 0.0), mf(nb), mr(nb);
     for (int c0 = 0; c0 < nf; c0 += cols) {
@@ -577,12 +587,13 @@ int Engine::classic_export(PointSrc ps, const std::vector<double> &f, double *m3
             f1[p] = f[p % nf];
             f2[p] = f[c0 + p / nf];
         }
-        export_fn((int)npts, f1.data(), f2.data(), br.data(), export_user);
+        if ((rc = emit_brm((int)npts, f1.data(), f2.data(), br.data()))) return rc;
         for (long long x = 0; x < nb; ++x) {
             accF[x] += mf[x];
             accR[x] += mr[x];
         }
     }
+    if ((rc = brm_file_close((long long)nf * nf))) return rc;
     if (m3mf) std::memcpy(m3mf, accF.data(), sizeof(double) * nb);
     if (m3mr) std::memcpy(m3mr, accR.data(), sizeof(double) * nb);
     return BSA_OK;
@@ -638,6 +649,7 @@ int Engine::run_points(const double *fi, const double *fj, const double *w, doub
                        double *m3mf, double *m3mr, double *bfm, double *brm, const std::vector<ZoneDev> *zones,
                        const int *zid, const int *zi, const int *zj) {
     kernels = 0;
+    graph_launches = 0;
     h2d = d2h = 0;
     last_ms_gemm = 0;
     int rc = upload_problem();
@@ -722,6 +734,7 @@ int Engine::run_points(const double *fi, const double *fj, const double *w, doub
 // analysis's own products (whole odd grid, truncated sum, at most 48 kept modes).
 int Engine::classic_points(const int *i1, const int *i2, long long npts, double *bf, double *br) {
     kernels = 0;
+    graph_launches = 0;
     h2d = d2h = 0;
     last_ms_gemm = 0;
     int rc = upload_problem();
@@ -1188,6 +1201,13 @@ int bsa_gpu_getStats(bsa_gpu_stats *st) {
     st->d2h_bytes = eng().d2h;
     st->kernels = eng().kernels;
     st->precision = eng().precision;
+    st->graphs = eng().graph_launches;
+    return BSA_OK;
+}
+
+int bsa_gpu_setMesherGraphs(int on) {
+    GUARD();
+    eng().msh_graphs = on != 0;
     return BSA_OK;
 }
 

@@ -75,7 +75,7 @@ int Engine::run_mesher(double *m3mf, double *m3mr) {
     std::vector<int> pol;
     int rc = mesher_zones(zones, pol);
     if (rc) return rc;
-    if ((rc = run_zones(zones, m3mf, m3mr, nullptr)) || !export_fn) return rc;
+    if ((rc = run_zones(zones, m3mf, m3mr, nullptr)) || !(export_fn || brm_file_wanted(false))) return rc;
     const double pts = last_points;
     const float ms = last_ms;
     rc = zones_export(zones);
@@ -96,6 +96,9 @@ int Engine::zones_export(const std::vector<ZoneDev> &zones) {
     const int nm = nme;
     const bool diag = set.onlyd != 0;
     std::vector<double> bfm, brm, f1, f2, pi, pj, mf(nb), mr(nb), H(6 * (size_t)nm);
+    int rc0 = brm_file_open(false, (int)zones.size());
+    if (rc0) return rc0;
+    long long total = 0;
     for (const ZoneDev &z : zones) {
         if (z.ni < 2 || z.nj < 2 || z.Fi < 1 || z.Fj < 1)
             return fail(BSA_ERR_ARG, "zone lattice needs ni, nj >= 2 and Fi, Fj >= 1");
@@ -150,8 +153,13 @@ int Engine::zones_export(const std::vector<ZoneDev> &zones) {
                     out[x] = fr * (c00 * B00[x] + c10 * B10[x] + c01 * B01[x] + c11 * B11[x]);
                 }
             }
-        export_fn((int)nq, f1.data(), f2.data(), brm.data(), export_user);
+        if ((rc = brm_file_zone(1, NI, NJ)) || (rc = emit_brm((int)nq, f1.data(), f2.data(), brm.data()))) {
+            brm_file_close(-1);
+            return rc;
+        }
+        total += (long long)nq;
     }
+    if ((rc0 = brm_file_close(total))) return rc0;
     return BSA_OK;
 }
 

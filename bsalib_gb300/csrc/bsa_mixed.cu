@@ -510,11 +510,13 @@ int Engine::contract_mixed(const PointSrc &ps, long long npts, double *m3mf, dou
     // the E form (bsa_classic_e.cu): one GEMM family over half the grid pairs; whole odd grid,
     // truncated S(f1 + f2), at most 48 kept modes, no central symmetry
     if (nm <= kEFormMaxModes && ps.mode == kPointsGrid && ps.r0 == 0 && ps.nr == nf && ps.sym_rows == 0 && ps.trunc == 1 &&
-        (nf & 1) && use_e_form)
+        (nf & 1) && use_e_form && plan_prefer_e(nm, K, nf))
         return contract_e(ps, m3mf, m3mr);
-    // FRF-table width per mode half; above 32 modes two halves of 32 (JH = 2)
-    const int NMT = nm <= 8 ? 8 : nm <= 16 ? 16 : nm <= 24 ? 24 : 32;
-    const int JH = nm > 32 ? 2 : 1;
+    // FRF-table width per mode half (tile plan; default the narrowest that holds the modes);
+    // 64 = two halves of 32 (JH = 2)
+    const int Wd = plan_d_width(nm, K, nf);
+    const int JH = Wd > 32 ? 2 : 1;
+    const int NMT = Wd / JH;
     const int W = NMT * JH;
     const int NC = kBN / NMT;
     const int Kp = ((K + kBK - 1) / kBK) * kBK;

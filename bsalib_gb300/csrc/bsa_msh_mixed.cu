@@ -836,7 +836,7 @@ int Engine::msh_mixed_batch(const std::vector<ZoneDev> &zs, std::vector<double> 
                             float &ms_gemm, float &ms_all, double *zdiag) {
     using namespace mshmix;
     const int nm = nme, nm2 = nm * nm, nm3 = nm2 * nm;
-    const int NMT = ((nm + 7) / 8) * 8, NC = kBN / NMT, BROWS = NC * NMT;
+    const int NMT = plan_msh_width(nm, K), NC = kBN / NMT, BROWS = NC * NMT;
     const int Kp = ((K + kBK - 1) / kBK) * kBK, Mp = ((nm2 + kBM - 1) / kBM) * kBM, MT = Mp / kBM;
     // frequencies of lines, columns and points
     FreqIndex F, UF;
@@ -942,11 +942,6 @@ int Engine::msh_mixed_batch(const std::vector<ZoneDev> &zs, std::vector<double> 
         return cuda_fail(e, "Mesher task upload");
     h2d += (double)(nidx * sizeof(int) + tasks.size() * sizeof(Task) + zm.size() * sizeof(ZoneM) +
                     witems.size() * sizeof(int4));
-    k_prep_u_rows<<<dim3(nU, Kp / 32), 256, 0, stream>>>(nm, K, Kp, Mp, d_usrc, dA32.as<float>(), dQ.as<double>(), Uh, Ul);
-    k_prep_b_rows<<<dim3((unsigned)ncol, Kp / 64), 256, 0, stream>>>(nm, NMT, K, Kp, d_gsrc, dA32.as<float>(), Gh, Gl);
-    k_prep_b_rows<<<dim3((unsigned)(2 * npts), Kp / 64), 256, 0, stream>>>(nm, NMT, K, Kp, d_ssrc, dA32.as<float>(), Sh, Sl);
-    if ((e = cudaGetLastError())) return cuda_fail(e, "Mesher operand preparation");
-    kernels += 3;
     CUtensorMap maps[6];
     if (!make_map(&maps[0], Uh, Kp, (uint64_t)nU * Mp, kBM) || !make_map(&maps[1], Ul, Kp, (uint64_t)nU * Mp, kBM) ||
         !make_map(&maps[2], Gh, Kp, (uint64_t)ncol * NMT, BROWS) || !make_map(&maps[3], Gl, Kp, (uint64_t)ncol * NMT, BROWS) ||
@@ -966,31 +961,61 @@ int Engine::msh_mixed_batch(const std::vector<ZoneDev> &zs, std::vector<double> 
     const long long nwork = (long long)witems.size();
     const int grid = (int)std::min<long long>(nwork, nsm);
     const size_t smem = (size_t)kStages * kStageBytes + 1024 + 256;
-    if ((e = cudaFuncSetAttribute(k_msh_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)))
+    if ((e = cudaFuncSetAttribute(k_msh_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) ||
+        (e = cudaFuncSetAttribute(k_msh_moments, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)MomLayout::smem())))
         return cuda_fail(e, "kernel attribute");
-    if ((e = cudaEventRecord(evg0, stream))) return cuda_fail(e, "event");
-    k_msh_mixed<<<grid, 192, smem, stream>>>(maps[0], maps[1], maps[2], maps[3], maps[4], maps[5], prm);
-    if ((e = cudaGetLastError())) return cuda_fail(e, "Mesher BF16x3 contraction kernel");
-    if ((e = cudaEventRecord(evg1, stream))) return cuda_fail(e, "event");
     float2 *Hq = dMixH.as<float2>();
     float *Wq = (float *)(Hq + (size_t)nbrm * hs);
-    {
+    double *d_zdiag = zdiag ? (double *)(((uintptr_t)(Wq + nbrm) + 255) & ~(uintptr_t)255) : nullptr;
+    // The pass's device work: operand rows, the tcgen05 contraction (bracketed by the timing
+    // events), the FRF rows, the zone integration and its reductions.
+    auto launch_all = [&](bool captured) -> cudaError_t {
+        auto mark = [&](cudaEvent_t ev) {
+            return captured ? cudaEventRecordWithFlags(ev, stream, cudaEventRecordExternal) : cudaEventRecord(ev, stream);
+        };
+        k_prep_u_rows<<<dim3(nU, Kp / 32), 256, 0, stream>>>(nm, K, Kp, Mp, d_usrc, dA32.as<float>(), dQ.as<double>(),
+                                                             Uh, Ul);
+        k_prep_b_rows<<<dim3((unsigned)ncol, Kp / 64), 256, 0, stream>>>(nm, NMT, K, Kp, d_gsrc, dA32.as<float>(), Gh,
+                                                                         Gl);
+        k_prep_b_rows<<<dim3((unsigned)(2 * npts), Kp / 64), 256, 0, stream>>>(nm, NMT, K, Kp, d_ssrc, dA32.as<float>(),
+                                                                               Sh, Sl);
+        cudaError_t r = mark(evg0);
+        if (r) return r;
+        k_msh_mixed<<<grid, 192, smem, stream>>>(maps[0], maps[1], maps[2], maps[3], maps[4], maps[5], prm);
+        if ((r = mark(evg1))) return r;
         const long long nt = nbrm * 3 * nm;
-        k_msh_frf<<<(unsigned)((nt + 255) / 256), 256, 0, stream>>>(nm, (int)zm.size(), d_zones, (int)nbrm, frf(), Hq, Wq);
+        k_msh_frf<<<(unsigned)((nt + 255) / 256), 256, 0, stream>>>(nm, (int)zm.size(), d_zones, (int)nbrm, frf(), Hq,
+                                                                     Wq);
+        k_msh_moments<<<dim3(G, nchunks), 256, MomLayout::smem(), stream>>>(nm, nm3p, ML, d_zones, (int)zm.size(), T1,
+                                                                           T3, T2, Hq, part, derr);
+        k_msh_reduce<<<(nm3 + 127) / 128, 128, 0, stream>>>(nm, G, part, red, red + nm3);
+        if (zdiag)
+            k_msh_zone_diag<<<(unsigned)zm.size(), 256, 0, stream>>>(nm, (size_t)nm3p, d_zones, T1, T3, T2, Hq, Wq,
+                                                                      d_zdiag);
+        return cudaGetLastError();
+    };
+    // ... launched as one CUDA graph (one graph per zone pass: per refinement level of the
+    // adaptive Mesher), captured from the stream; where capture or instantiation is not
+    // available the same sequence is launched directly.
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    bool graphed = false;
+    if (msh_graphs && cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+        const cudaError_t le = launch_all(true);
+        const cudaError_t ce = cudaStreamEndCapture(stream, &graph);
+        graphed = le == cudaSuccess && ce == cudaSuccess && graph &&
+                  cudaGraphInstantiate(&gexec, graph, 0) == cudaSuccess && cudaGraphLaunch(gexec, stream) == cudaSuccess;
+        if (!graphed) {
+            cudaGetLastError();
+            if (gexec) cudaGraphExecDestroy(gexec);
+            if (graph) cudaGraphDestroy(graph);
+            gexec = nullptr;
+            graph = nullptr;
+        }
     }
-    if ((e = cudaFuncSetAttribute(k_msh_moments, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)MomLayout::smem())))
-        return cuda_fail(e, "kernel attribute");
-    k_msh_moments<<<dim3(G, nchunks), 256, MomLayout::smem(), stream>>>(nm, nm3p, ML, d_zones, (int)zm.size(), T1,
-                                                                       T3, T2, Hq, part, derr);
-    k_msh_reduce<<<(nm3 + 127) / 128, 128, 0, stream>>>(nm, G, part, red, red + nm3);
-    double *d_zdiag = nullptr;
-    if (zdiag) {
-        d_zdiag = (double *)(((uintptr_t)(Wq + nbrm) + 255) & ~(uintptr_t)255);
-        k_msh_zone_diag<<<(unsigned)zm.size(), 256, 0, stream>>>(nm, (size_t)nm3p, d_zones, T1, T3, T2, Hq, Wq, d_zdiag);
-        kernels += 1;
-    }
-    if ((e = cudaGetLastError())) return cuda_fail(e, "Mesher zone integration");
-    kernels += 4;
+    if (!graphed && (e = launch_all(false))) return cuda_fail(e, "Mesher BF16x3 pass");
+    kernels += 7 + (zdiag ? 1 : 0);
+    graph_launches += graphed ? 1 : 0;
     std::vector<double> h(2 * (size_t)nm3);
     int herr = 0;
     if ((e = cudaMemcpyAsync(h.data(), red, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, stream)) ||
@@ -999,6 +1024,8 @@ int Engine::msh_mixed_batch(const std::vector<ZoneDev> &zs, std::vector<double> 
                                        stream))) ||
         (e = cudaEventRecord(ev1, stream)) || (e = cudaStreamSynchronize(stream)))
         return cuda_fail(e, "Mesher BF16x3 evaluation");
+    if (gexec) cudaGraphExecDestroy(gexec);
+    if (graph) cudaGraphDestroy(graph);
     d2h += (double)sizeof(double) * h.size() + sizeof(int);
     if (herr) return fail(BSA_ERR_TIMEOUT, "Mesher BF16x3 kernel: a pipeline wait ran out of its budget (role %d)", herr);
     float ms = 0.f;
@@ -1049,11 +1076,12 @@ int Engine::run_zones_mixed(const std::vector<ZoneDev> &zones, double *m3mf, dou
         for (long long x = 0; x < nm3; ++x) { accF[x] += f[x]; accR[x] += r[x]; }
     }
     kernels = 0;
+    graph_launches = 0;
     h2d = d2h = 0;
     if (!axis.empty()) {
         // batches by device bytes: U blocks of the distinct line / column frequencies, column
         // and sum tables, term tensors and BRM-point FRF tables
-        const int NMT = ((nm + 7) / 8) * 8;
+        const int NMT = plan_msh_width(nm, K);
         const double Kp = (double)(((K + 63) / 64) * 64), Mp = (double)(((nm * nm + 127) / 128) * 128);
         const double per_u = Mp * Kp * 4.0, per_col = NMT * Kp * 4.0;
         const double per_pt = 2.0 * NMT * Kp * 4.0 + 3.0 * nm3 * 4.0, per_q = 3.0 * nm * 8.0 + 4.0;

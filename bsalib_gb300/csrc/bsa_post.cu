@@ -114,6 +114,7 @@ __global__ void k_recomb(int ndofs, int nme, int diag_only, const double *__rest
 // recombination kernel; skewness on the host as the reference writes it, m3 / m2^(3/2).
 int Engine::modal_recomb(const double *m2mr, const double *m3mr, const double *m2o2mr, double *const *outs) {
     kernels = 0;
+    graph_launches = 0;
     h2d = d2h = 0;
     int rc = validate();
     if (rc) return rc;
@@ -161,6 +162,7 @@ int Engine::modal_recomb(const double *m2mr, const double *m3mr, const double *m
 
 int Engine::br_decomp(const double *m2mf, double *bkg, double *res) {
     kernels = 0;
+    graph_launches = 0;
     h2d = d2h = 0;
     int rc = upload_problem();
     if (rc) return rc;

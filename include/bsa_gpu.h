@@ -380,6 +380,8 @@ typedef struct {
     double d2h_bytes;         /* device-to-host bytes copied by the last run          */
     int kernels;              /* kernels launched by the last run                     */
     int precision;            /* BSA_PREC_* used                                      */
+    int graphs;               /* CUDA graphs launched by the last run (kernels counts  */
+                              /* the kernels inside them too)                          */
 } bsa_gpu_stats;
 int bsa_gpu_getStats(bsa_gpu_stats *st);
 
@@ -391,6 +393,30 @@ int bsa_gpu_getStats(bsa_gpu_stats *st);
  * bsa_Finalise). */
 int bsa_gpu_setClassicForm(int form);
 
+/* Tile plans of the split-precision contractions (no counterpart in the reference): the shape
+ * choices the project's autotuner (python -m bsalib_gb300.autotune) searches per range of kept
+ * modes nm, of K (turbulence components x loaded nodes) and of Classic grid points per axis nf.
+ *   BSA_PLAN_CLS_FORM     1: the E form of the Classic contraction where it applies, 0: D1 / D3
+ *   BSA_PLAN_CLS_E_WIDTH  E form FRF-table width: 8, 16, 24, 32 (2 x 16) or 48 (2 x 24)
+ *   BSA_PLAN_CLS_D_WIDTH  D1 / D3 form width: 8, 16, 24, 32 or 64 (2 x 32)
+ *   BSA_PLAN_MSH_WIDTH    Mesher kernel mode width: a multiple of 8 from nm to 64 (nf ignored)
+ * The table is read on first use from data/tile_plans.txt beside the library (or the file the
+ * environment variable BSA_TILE_PLANS names): lines "family nm_lo nm_hi k_lo k_hi nf_lo nf_hi
+ * value" with family cls_form | cls_e_width | cls_d_width | msh_width.  The first matching plan
+ * wins; a value that does not fit the case (narrower than nm, not a built width) falls back to
+ * the default rule (narrowest width holding nm, E form wherever it applies).  The plans are
+ * process-wide and survive bsa_Finalise.  setTilePlan adds a plan ahead of the table,
+ * clearTilePlans empties it (defaults only), loadTilePlans(path) replaces it (NULL: the default
+ * file again), getTilePlan reports the value the library would use. */
+#define BSA_PLAN_CLS_FORM 1
+#define BSA_PLAN_CLS_E_WIDTH 2
+#define BSA_PLAN_CLS_D_WIDTH 3
+#define BSA_PLAN_MSH_WIDTH 4
+int bsa_gpu_setTilePlan(int family, int nm_lo, int nm_hi, int k_lo, int k_hi, int nf_lo, int nf_hi, int value);
+int bsa_gpu_clearTilePlans(void);
+int bsa_gpu_loadTilePlans(const char *path);
+int bsa_gpu_getTilePlan(int family, int nm, int K, int nf, int *value);
+
 /* Diagnostics, no counterpart in the reference: exercises the bounded device waits.  Every
  * mbarrier wait of the tensor-core kernels gives up after 2 s (or at once when another role of the
  * launch has already given up), lets its in-flight copies and MMAs land, frees its TMEM and
@@ -399,6 +425,12 @@ int bsa_gpu_setClassicForm(int form);
  * accumulator-ready signal of that CTA's accumulator tile, so the epilogue's wait runs out (no
  * fault, no copy left in flight); -1 switches it off.  Applies to one analysis. */
 int bsa_gpu_setWaitTest(int tile);
+
+/* No counterpart in the reference.  on != 0 (default): each split-precision Mesher zone pass
+ * (every refinement level of an adaptive refinement) runs its device work -- operand rows, the
+ * tcgen05 contraction, FRF rows, zone integration, reductions -- as one CUDA graph captured from
+ * the library's stream; 0 launches the same kernels one by one.  Same results either way. */
+int bsa_gpu_setMesherGraphs(int on);
 
 /* Device memory.  Blocks the library releases (bsa_Finalise, buffer growth) are kept for reuse
  * by the next analysis, up to a quarter of the device memory, so repeated bsa_Init ...
