@@ -396,7 +396,7 @@ class BsaSession:
         """bsa_enableVisualMode + bsa_setVisualIndexes: bsa_Run writes bsaexport_cls.brm (modal,
         Classic), bsaexport_msh.brm / .brn (Mesher) in the working directory."""
         idx = np.ascontiguousarray(indexes, dtype=np.int32)
-        self._keep.append(idx)
+        self._keep["visual_indexes"] = idx
         check(self.lib.bsa_enableVisualMode(), "bsa_enableVisualMode")
         check(self.lib.bsa_setVisualIndexes(_p(idx), int(bool(modal))), "bsa_setVisualIndexes")
 

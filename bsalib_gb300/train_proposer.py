@@ -1,11 +1,13 @@
 """Train the zone-refinement proposer on records of the plain refinement criterion and
 compare the learned form with the plain one on held-out structures.
 
-  python -m bsalib_gb300.train_proposer [--train 600] [--test 60] [--tol 1e-3]
+  python -m bsalib_gb300.train_proposer [--train 2000] [--test 200] [--tol 1e-3]
                                         [--thr-cap 0.02] [--out proposer.npz] [--json r.json]
 
-Structures are seeded random cantilevers (`problem.random_structure`, nodes 50-300, modes
-5-20, frequencies log-uniform 0.05-5 Hz, damping 0.3-3 %, U 15-50 m/s, I_u 0.08-0.2).
+Structures are seeded random cantilevers (`problem.random_structure`) drawn as the learned
+refinement configuration specifies: nodes uniform 50-800, modes 5-60, natural frequencies
+log-uniform 0.05-5 Hz, damping 0.3-3 %, U 15-50 m/s, I_u 0.08-0.2; training seeds 0 .. train-1,
+held-out seeds 100000 .. 100000 + test - 1.
 Training records come from the plain criterion on the training seeds; the held-out seeds
 are evaluated with both forms in the split precision, and the plain form's final zone set
 once more with the FP64 path, the reference for the errors.  Skewness uses the second
@@ -26,7 +28,7 @@ from .refine import Proposer, Refiner
 
 
 def structure(seed):
-    p = random_structure(seed, nodes=(50, 300), modes=(5, 20), nfreq_grid=(129, 129))
+    p = random_structure(seed, nodes=(50, 800), modes=(5, 60), nfreq_grid=(129, 129))
     p.settings.suban = 2
     return p
 
@@ -61,39 +63,81 @@ def records(seeds, tol, levels):
     return np.concatenate(X), np.concatenate(Y), np.concatenate(E)
 
 
-def compare(prop, thr, seeds, tol, levels):
+def brm_points(zones):
+    return int(sum(((z.ni - 1) * z.Fi + 1) * ((z.nj - 1) * z.Fj + 1) for z in zones))
+
+
+def compare(prop, thr, seeds, tol, levels, fp64_every=1):
+    """Plain and learned refinement of each held-out structure in the split precision (device
+    time and host wall time of each run), and, on every fp64_every-th structure, the plain
+    FP64 GPU path integrating the plain criterion's final mesh (the error reference)."""
     rows = []
     rel = lambda x, y: float(np.max(np.abs(x - y)) / np.max(np.abs(y)))
-    for seed in seeds:
+    for k, seed in enumerate(seeds):
         prob = structure(seed)
         s = api.BsaSession(prob, precision=api.PREC_BF16X3)
         try:
             nm = s.nmodes()
+            t0 = time.perf_counter()
             plain = Refiner(s, tol, levels).run()
+            t1 = time.perf_counter()
             learned = Refiner(s, tol, levels).run(proposer=prop, threshold=thr)
+            t2 = time.perf_counter()
         finally:
             s.close()
-        s64 = api.BsaSession(prob, precision=api.PREC_FP64)
-        try:
-            _, mr64, _ = s64.msh_zones(plain.final_zones)
-            ms64 = s64.stats().ms_total
-        finally:
-            s64.close()
-        m2 = second_moments(prob)
-        rows.append({"seed": seed, "modes": nm, "nodes": prob.nnl,
-                     "plain_points": plain.points, "learned_points": learned.points,
-                     "plain_ms": plain.ms, "learned_ms": learned.ms, "fp64_final_ms": ms64,
-                     "m3mr_rel_learned_vs_plain": rel(learned.m3mr, plain.m3mr),
-                     "m3mr_rel_learned_vs_fp64": rel(learned.m3mr, mr64),
-                     "skew_rel_learned_vs_fp64": rel(skew(nm, m2, learned.m3mr), skew(nm, m2, mr64)),
-                     "skew_rel_plain_vs_fp64": rel(skew(nm, m2, plain.m3mr), skew(nm, m2, mr64))})
+        row = {"seed": seed, "modes": nm, "nodes": prob.nnl,
+               "plain_points": plain.points, "learned_points": learned.points,
+               "plain_ms": plain.ms, "learned_ms": learned.ms,
+               "plain_wall_s": t1 - t0, "learned_wall_s": t2 - t1,
+               "final_brm_points": brm_points(learned.final_zones),
+               "m3mr_rel_learned_vs_plain": rel(learned.m3mr, plain.m3mr)}
+        if k % fp64_every == 0:
+            s64 = api.BsaSession(prob, precision=api.PREC_FP64)
+            try:
+                s64.use_driver_controls()
+                _, mr64, _ = s64.msh_zones(plain.final_zones)
+                ms64 = s64.stats().ms_total
+            finally:
+                s64.close()
+            m2 = second_moments(prob)
+            row.update({"fp64_final_ms": ms64, "plain_final_brm_points": brm_points(plain.final_zones),
+                        "m3mr_rel_learned_vs_fp64": rel(learned.m3mr, mr64),
+                        "skew_rel_learned_vs_fp64": rel(skew(nm, m2, learned.m3mr), skew(nm, m2, mr64)),
+                        "skew_rel_plain_vs_fp64": rel(skew(nm, m2, plain.m3mr), skew(nm, m2, mr64))})
+        rows.append(row)
     return rows
+
+
+def summary(rows):
+    """Medians of the per-structure ratios and the aggregate rates."""
+    f = [r for r in rows if "fp64_final_ms" in r]
+    out = {"points_ratio_learned_over_plain_median": float(np.median([r["learned_points"] / r["plain_points"]
+                                                                      for r in rows])),
+           "time_ratio_learned_over_plain_median": float(np.median([r["learned_ms"] / r["plain_ms"] for r in rows])),
+           "wall_ratio_learned_over_plain_median": float(np.median([r["learned_wall_s"] / r["plain_wall_s"]
+                                                                    for r in rows])),
+           "exact_match_fraction": float(np.mean([r["m3mr_rel_learned_vs_plain"] < 1e-10 for r in rows])),
+           "m3mr_rel_learned_vs_plain_max": float(max(r["m3mr_rel_learned_vs_plain"] for r in rows))}
+    if f:
+        pts = sum(r["plain_final_brm_points"] for r in f)
+        learned_rate = sum(r["final_brm_points"] for r in f) / (sum(r["learned_ms"] for r in f) * 1e-3)
+        fp64_rate = pts / (sum(r["fp64_final_ms"] for r in f) * 1e-3)
+        out.update({"fp64_structures": len(f),
+                    "skew_rel_learned_vs_fp64_max": float(max(r["skew_rel_learned_vs_fp64"] for r in f)),
+                    "skew_rel_plain_vs_fp64_max": float(max(r["skew_rel_plain_vs_fp64"] for r in f)),
+                    "learned_brm_pts_per_s": learned_rate, "fp64_brm_pts_per_s": fp64_rate,
+                    "pts_per_s_ratio_learned_over_fp64": learned_rate / fp64_rate,
+                    "wall_ratio_fp64_over_learned": sum(r["fp64_final_ms"] for r in f) /
+                    sum(r["learned_ms"] for r in f)})
+    return out
 
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--train", type=int, default=600)
-    ap.add_argument("--test", type=int, default=60)
+    ap.add_argument("--train", type=int, default=2000)
+    ap.add_argument("--test", type=int, default=200)
+    ap.add_argument("--fp64-every", type=int, default=1,
+                    help="the FP64 reference on every k-th held-out structure (1: all)")
     ap.add_argument("--tol", type=float, default=1e-3)
     ap.add_argument("--levels", type=int, default=2)
     ap.add_argument("--epochs", type=int, default=40)
@@ -119,18 +163,13 @@ def main():
     thr = float(min(0.5 * np.min(p[Y > 0.5]), a.thr_cap)) if np.any(Y > 0.5) else a.thr_cap
     recall = float(np.mean(p[Y > 0.5] > thr)) if np.any(Y > 0.5) else 1.0
     skipped = float(np.mean(p[Y < 0.5] <= thr)) if np.any(Y < 0.5) else 0.0
-    rows = compare(prop, thr, range(100000, 100000 + a.test), a.tol, a.levels)
+    t0 = time.perf_counter()
+    rows = compare(prop, thr, range(100000, 100000 + a.test), a.tol, a.levels, a.fp64_every)
+    t_cmp = time.perf_counter() - t0
     res = {"train_structures": a.train, "test_structures": a.test, "records": int(len(Y)),
-           "positive_fraction": float(Y.mean()), "record_s": t_rec, "fit_s": t_fit, "final_train_loss": loss,
-           "threshold": thr, "train_recall": recall, "train_skipped_negatives": skipped,
-           "points_ratio_learned_over_plain_median": float(np.median([r["learned_points"] / r["plain_points"]
-                                                                      for r in rows])),
-           "time_ratio_learned_over_plain_median": float(np.median([r["learned_ms"] / r["plain_ms"] for r in rows])),
-           "exact_match_fraction": float(np.mean([r["m3mr_rel_learned_vs_plain"] < 1e-10 for r in rows])),
-           "m3mr_rel_learned_vs_plain_max": float(max(r["m3mr_rel_learned_vs_plain"] for r in rows)),
-           "skew_rel_learned_vs_fp64_max": float(max(r["skew_rel_learned_vs_fp64"] for r in rows)),
-           "skew_rel_plain_vs_fp64_max": float(max(r["skew_rel_plain_vs_fp64"] for r in rows)),
-           "rows": rows}
+           "positive_fraction": float(Y.mean()), "record_s": t_rec, "fit_s": t_fit, "compare_s": t_cmp,
+           "final_train_loss": loss, "threshold": thr, "train_recall": recall, "train_skipped_negatives": skipped,
+           **summary(rows), "rows": rows}
     if a.out:
         prop.save(a.out, thr, a.tol)
     prop.close()
