@@ -35,8 +35,8 @@ DEFAULT_OUT = os.path.join(HERE, "data", "tile_plans.txt")
 
 NM_RANGES = [(1, 8), (9, 12), (13, 16), (17, 20), (21, 24), (25, 28), (29, 32), (33, 40), (41, 48), (49, 56),
              (57, 64)]
-K_RANGES = [(1, 1000, 300), (1001, 1 << 30, 2400)]          # (lo, hi, representative K)
-NF_RANGES = [(1, 300, 129), (301, 1 << 30, 513)]            # (lo, hi, representative grid points)
+K_RANGES = [(1, 500, 300), (501, 1500, 800), (1501, 1 << 30, 2400)]        # (lo, hi, representative K)
+NF_RANGES = [(1, 300, 129), (301, 700, 513), (701, 1 << 30, 1025)]        # (lo, hi, representative grid)
 E_WIDTHS = (8, 16, 24, 32, 48)
 D_WIDTHS = (8, 16, 24, 32, 64)
 FAMILY = {"cls_form": api.PLAN_CLS_FORM, "cls_e_width": api.PLAN_CLS_E_WIDTH, "cls_d_width": api.PLAN_CLS_D_WIDTH,

@@ -32,6 +32,8 @@ def main():
     ap.add_argument("--precision", default="bf16x3", choices=["bf16x3", "fp64"])
     ap.add_argument("--steps", type=int, default=2)
     ap.add_argument("--zones-only", action="store_true")
+    ap.add_argument("--synthetic", type=int, default=0,
+                    help="evaluate this many seeded synthetic zones (problem.synthetic_zones) instead of the layout")
     ap.add_argument("--controls", default="driver", choices=["driver", "library"],
                     help="Mesher controls: the standalone driver's (default) or the library's")
     a = ap.parse_args()
@@ -42,7 +44,11 @@ def main():
     try:
         if a.controls == "driver":
             s.use_driver_controls()
-        zs = s.generate_zones()
+        if a.synthetic:
+            from .problem import synthetic_zones
+            zs = synthetic_zones(prob, a.synthetic)
+        else:
+            zs = s.generate_zones()
         nbfm = sum(z.ni * z.nj for z in zs)
         nbrm = sum(((z.ni - 1) * z.Fi + 1) * ((z.nj - 1) * z.Fj + 1) for z in zs)
         print(f"{a.structure}: {prob.nnl} nodes, {s.nmodes()} modes, {len(zs)} zones, "
@@ -50,7 +56,10 @@ def main():
         if a.zones_only:
             return
         for _ in range(a.steps):
-            s.run()
+            if a.synthetic:
+                s.msh_zones(zs)
+            else:
+                s.run()
             st = s.stats()
             print(f"  {st.ms_total:.1f} ms total, {st.ms_gemm:.1f} ms contraction kernel, {st.kernels} kernels, "
                   f"{st.points / (st.ms_total * 1e-3):.4g} BRM pts/s", flush=True)

@@ -61,10 +61,18 @@ struct MParams {
     float *T1, *T3, *T2;  // [point][j'][a*nm + b], points nm3p (nm^3 rounded up to 4) apart
     int nm3p;
     int *err;
+    int *head;  // device work queue: the next unclaimed item (zero at launch)
 };
 
-// Work item w = (task, row tile, N tiles [nt0, nt1)), CTAs stride over work items; all three
-// roles walk the same (item, K chunk) sequence, one TMEM buffer per item.  The items of one
+constexpr int kQueue = 4;  // item slots between the producer and the two consumer roles
+
+// Work item w = (task, row tile, N tiles [nt0, nt1)).  The items sit in a device queue (the
+// zone list expanded into lines and columns, row tiles and N tiles); a CTA's TMA thread claims
+// the next one with an atomic on the queue head and publishes its index through a ring of
+// kQueue shared-memory slots (mbarriers qfull / qempty: the MMA thread and the four epilogue
+// warps read each slot once), so all three roles walk the same (item, K chunk) sequence, one
+// TMEM buffer per item, and a CTA whose items are short (small zones, lone N tiles) simply
+// claims more of them.  Each CTA ends on the first index past the queue.  The items of one
 // task are consecutive (row tile major), so the CTAs running at the same time share its U row
 // blocks and its B tiles through L2 instead of each streaming them from HBM.  Stage layout:
 // U hi, U lo, B0 hi, B1 hi, B0 lo, B1 lo, the unit's 256 B rows B0 | B1 in one N = 256 MMA:
@@ -82,7 +90,9 @@ __global__ void __launch_bounds__(192, 1)
     uint64_t *bars = (uint64_t *)(smem + kStages * kStageBytes);
     uint64_t *full = bars, *empty = bars + kStages, *tfull = bars + 2 * kStages, *tempty = bars + 2 * kStages + 2;
     uint64_t *done = bars + 2 * kStages + 4;
-    uint32_t *tmem_slot = (uint32_t *)(bars + 2 * kStages + 5);
+    uint64_t *qfull = bars + 2 * kStages + 5, *qempty = qfull + kQueue;
+    uint32_t *tmem_slot = (uint32_t *)(qempty + kQueue);
+    volatile int *ring = (volatile int *)(qempty + kQueue + 1);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     int *err = p.err;
     const int nwork = p.nitems;
@@ -104,6 +114,10 @@ __global__ void __launch_bounds__(192, 1)
             mbar_init(&tempty[b], 128);
         }
         mbar_init(done, 1);
+        for (int q = 0; q < kQueue; ++q) {
+            mbar_init(&qfull[q], 1);
+            mbar_init(&qempty[q], 1 + 4);  // the MMA thread and the four epilogue warps
+        }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     }
@@ -121,7 +135,14 @@ __global__ void __launch_bounds__(192, 1)
         if (lane == 0) {
             uint32_t it = 0;
             bool ok = true;
-            for (int w = blockIdx.x; w < nwork && ok; w += gridDim.x) {
+            for (int qi = 0; ok; ++qi) {
+                // claim the next item of the queue and publish it to the MMA and epilogue roles
+                const int slot = qi % kQueue;
+                if (!mbar_wait(&qempty[slot], ((qi / kQueue) & 1u) ^ 1u, err, 5)) { ok = false; break; }
+                const int w = atomicAdd(p.head, 1);
+                ring[slot] = w;
+                mbar_arrive(&qfull[slot]);
+                if (w >= nwork) break;
                 const int4 wi = p.items[w];
                 const Task tk = p.tasks[wi.x];
                 const int mt = wi.y;
@@ -172,7 +193,12 @@ __global__ void __launch_bounds__(192, 1)
         if (lane == 0) {
             uint32_t it = 0, tile = 0;
             bool ok = true;
-            for (int w = blockIdx.x; w < nwork && ok; w += gridDim.x) {
+            for (int qi = 0; ok; ++qi) {
+                const int slot = qi % kQueue;
+                if (!mbar_wait(&qfull[slot], (qi / kQueue) & 1u, err, 6)) { ok = false; break; }
+                const int w = ring[slot];
+                mbar_arrive(&qempty[slot]);
+                if (w >= nwork) break;
                 const int4 wi = p.items[w];
                 const Task tk = p.tasks[wi.x];
                 const bool wide = tk.kind == 0 || wi.w - wi.z == 2;
@@ -228,7 +254,14 @@ __global__ void __launch_bounds__(192, 1)
         const int nm = p.nm, nm2 = nm * nm;
         uint32_t tile = 0;
         bool ok = true;
-        for (int w = blockIdx.x; w < nwork && ok; w += gridDim.x) {
+        for (int qi = 0; ok; ++qi) {
+            const int slot = qi % kQueue;
+            // warp-uniform: every lane waits, reads the slot, then one arrive per warp
+            if (!__all_sync(0xffffffffu, mbar_wait(&qfull[slot], (qi / kQueue) & 1u, err, 7))) { ok = false; break; }
+            const int w = ring[slot];
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&qempty[slot]);
+            if (w >= nwork) break;
             const int4 wi = p.items[w];
             const Task tk = p.tasks[wi.x];
             const int mt = wi.y;
@@ -931,14 +964,14 @@ int Engine::msh_mixed_batch(const std::vector<ZoneDev> &zs, std::vector<double> 
     ZoneM *d_zones = (ZoneM *)(((uintptr_t)(d_tasks + tasks.size()) + 15) & ~(uintptr_t)15);
     int4 *d_items = (int4 *)(((uintptr_t)(d_zones + zm.size()) + 15) & ~(uintptr_t)15);
     double *part = dMixPart.as<double>(), *red = part + (size_t)G * 6 * nm3;
-    int *derr = (int *)(red + 2 * (size_t)nm3);
+    int *derr = (int *)(red + 2 * (size_t)nm3), *dhead = derr + 1;
     if ((e = cudaMemcpyAsync(d_usrc, usrc.data(), nU * sizeof(int), cudaMemcpyHostToDevice, stream)) ||
         (e = cudaMemcpyAsync(d_gsrc, gsrc.data(), ncol * sizeof(int), cudaMemcpyHostToDevice, stream)) ||
         (e = cudaMemcpyAsync(d_ssrc, ssrc.data(), 2 * npts * sizeof(int), cudaMemcpyHostToDevice, stream)) ||
         (e = cudaMemcpyAsync(d_tasks, tasks.data(), tasks.size() * sizeof(Task), cudaMemcpyHostToDevice, stream)) ||
         (e = cudaMemcpyAsync(d_zones, zm.data(), zm.size() * sizeof(ZoneM), cudaMemcpyHostToDevice, stream)) ||
         (e = cudaMemcpyAsync(d_items, witems.data(), witems.size() * sizeof(int4), cudaMemcpyHostToDevice, stream)) ||
-        (e = cudaMemsetAsync(derr, 0, sizeof(int), stream)))
+        (e = cudaMemsetAsync(derr, 0, 2 * sizeof(int), stream)))  // error flag and queue head
         return cuda_fail(e, "Mesher task upload");
     h2d += (double)(nidx * sizeof(int) + tasks.size() * sizeof(Task) + zm.size() * sizeof(ZoneM) +
                     witems.size() * sizeof(int4));
@@ -958,6 +991,7 @@ int Engine::msh_mixed_batch(const std::vector<ZoneDev> &zs, std::vector<double> 
     prm.T1 = T1; prm.T3 = T3; prm.T2 = T2;
     prm.nm3p = nm3p;
     prm.err = derr;
+    prm.head = dhead;
     const long long nwork = (long long)witems.size();
     const int grid = (int)std::min<long long>(nwork, nsm);
     const size_t smem = (size_t)kStages * kStageBytes + 1024 + 256;

@@ -423,3 +423,70 @@ def random_structure(seed: int, nodes=(30, 600), modes=(4, 40), nfreq_grid=(129,
     s = Settings(suban=1, nfreqs=(nf - 1) // 2 + 1, df=fmax / ((nf - 1) // 2), tc=(1,), test=1)
     return _assemble(z, U, Iu * U, 0.75 * Iu * U, 0.5 * Iu * U, 120.0, 80.0, 40.0, phi, natf, xsi,
                      lin, quad, (8.0, 8.0, 8.0), 5, s, rho=rho)
+
+
+def synthetic_zones(prob: Problem, nzones: int = 50000, seed: int = 0, brm_min: int = 8, brm_max: int = 256):
+    """A seeded zone list for the batched Mesher workload: about `nzones` axis-aligned zones of
+    uneven size tiling [-F, F]^2 (F = 1.25 max natural frequency of the kept modes), refined
+    around the resonance ridges f1 = +-f_m, f2 = +-f_m and f1 + f2 = +-f_m (bands of +-8 xi_m f_m)
+    and coarse in the background.  A quadtree: starting from 16 x 16 cells, the largest cell that
+    crosses a ridge band is split into four until the leaf count reaches `nzones`.  Each leaf is a
+    zone with a BFM lattice of 2-5 points per side (seeded) and a BRM lattice of brm_min ..
+    brm_max points per side in proportion to the cell's size (the smallest cells brm_min).
+    Returns bsalib_gb300.api.Zone records (spatial symmetry 1, policy 0)."""
+    import heapq
+
+    from .api import Zone
+    rng = np.random.default_rng(seed)
+    keep = np.nonzero(np.max(np.abs(prob.phi), axis=0) == 1.0)[0]
+    fm = np.asarray(prob.natf, dtype=float)[keep]
+    bw = 8.0 * np.asarray(prob.xsi, dtype=float)[keep] * fm
+    F = 1.25 * float(fm.max())
+
+    def crosses(x0, x1, y0, y1):
+        for c, b in zip(fm, bw):
+            for v in (c, -c):
+                if x0 <= v + b and x1 >= v - b:
+                    return True
+                if y0 <= v + b and y1 >= v - b:
+                    return True
+                if x0 + y0 <= v + b and x1 + y1 >= v - b:
+                    return True
+        return False
+
+    n0 = 16
+    h0 = 2.0 * F / n0
+    leaves = []   # (x0, y0, size)
+    heap = []     # (-size, x0, y0) of cells crossing a band
+    for i in range(n0):
+        for j in range(n0):
+            x0, y0 = -F + i * h0, -F + j * h0
+            if crosses(x0, x0 + h0, y0, y0 + h0):
+                heapq.heappush(heap, (-h0, x0, y0))
+            else:
+                leaves.append((x0, y0, h0))
+    while heap and len(leaves) + len(heap) < nzones:
+        nh, x0, y0 = heapq.heappop(heap)
+        h = -nh / 2.0
+        for dx in (0.0, h):
+            for dy in (0.0, h):
+                a, b = x0 + dx, y0 + dy
+                if crosses(a, a + h, b, b + h):
+                    heapq.heappush(heap, (-h, a, b))
+                else:
+                    leaves.append((a, b, h))
+    leaves += [(x0, y0, -nh) for nh, x0, y0 in heap]
+    hmin = min(h for _, _, h in leaves)
+    hmax = max(h for _, _, h in leaves)
+    span = max(np.log(hmax / hmin), 1e-12)
+    zones = []
+    for (x0, y0, h) in sorted(leaves):
+        ni, nj = int(rng.integers(2, 6)), int(rng.integers(2, 6))
+        # BRM points per side from brm_min (smallest cells) to brm_max (largest), geometric in size
+        side = brm_min * (brm_max / brm_min) ** (np.log(h / hmin) / span)
+        Fi = max(1, int(np.floor((side - 1) / (ni - 1))))
+        Fj = max(1, int(np.floor((side - 1) / (nj - 1))))
+        Fi = max(Fi, -(-(brm_min - 1) // (ni - 1)))
+        Fj = max(Fj, -(-(brm_min - 1) // (nj - 1)))
+        zones.append(Zone(x0, y0, h / (ni - 1), 0.0, 0.0, h / (nj - 1), ni, nj, Fi, Fj, 1.0, 0))
+    return zones

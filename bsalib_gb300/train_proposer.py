@@ -48,12 +48,24 @@ def skew(nm, m2, m3):
     return m3 / np.einsum("i,j,k->ijk", sig, sig, sig).reshape(-1, order="F")
 
 
-def records(seeds, tol, levels):
+def layout_refused(err):
+    """The reference's pre-mesh aborts on this structure as well (BsaMesherImpl.F90:809-810,
+    "Negative base."): its first quadrant zone would have no extent."""
+    return "negative base" in str(err)
+
+
+def records(seeds, tol, levels, skipped=None):
     X, Y, E = [], [], []
     for seed in seeds:
         s = api.BsaSession(structure(seed), precision=api.PREC_BF16X3)
         try:
             out = Refiner(s, tol, levels).run(keep_records=True)
+        except api.BsaError as e:
+            if not layout_refused(e):
+                raise
+            if skipped is not None:
+                skipped.append(seed)
+            continue
         finally:
             s.close()
         if out.records is not None:
@@ -83,6 +95,11 @@ def compare(prop, thr, seeds, tol, levels, fp64_every=1):
             t1 = time.perf_counter()
             learned = Refiner(s, tol, levels).run(proposer=prop, threshold=thr)
             t2 = time.perf_counter()
+        except api.BsaError as e:
+            if not layout_refused(e):
+                raise
+            rows.append({"seed": seed, "skipped": "the reference's pre-mesh refuses the layout (negative base)"})
+            continue
         finally:
             s.close()
         row = {"seed": seed, "modes": nm, "nodes": prob.nnl,
@@ -110,6 +127,8 @@ def compare(prop, thr, seeds, tol, levels, fp64_every=1):
 
 def summary(rows):
     """Medians of the per-structure ratios and the aggregate rates."""
+    skipped = [r["seed"] for r in rows if "skipped" in r]
+    rows = [r for r in rows if "skipped" not in r]
     f = [r for r in rows if "fp64_final_ms" in r]
     out = {"points_ratio_learned_over_plain_median": float(np.median([r["learned_points"] / r["plain_points"]
                                                                       for r in rows])),
@@ -117,7 +136,8 @@ def summary(rows):
            "wall_ratio_learned_over_plain_median": float(np.median([r["learned_wall_s"] / r["plain_wall_s"]
                                                                     for r in rows])),
            "exact_match_fraction": float(np.mean([r["m3mr_rel_learned_vs_plain"] < 1e-10 for r in rows])),
-           "m3mr_rel_learned_vs_plain_max": float(max(r["m3mr_rel_learned_vs_plain"] for r in rows))}
+           "m3mr_rel_learned_vs_plain_max": float(max(r["m3mr_rel_learned_vs_plain"] for r in rows)),
+           "evaluated_structures": len(rows), "skipped_structures": skipped}
     if f:
         pts = sum(r["plain_final_brm_points"] for r in f)
         learned_rate = sum(r["final_brm_points"] for r in f) / (sum(r["learned_ms"] for r in f) * 1e-3)
@@ -148,7 +168,8 @@ def main():
     a = ap.parse_args()
     build.build()
     t0 = time.perf_counter()
-    X, Y, E = records(range(a.train), a.tol, a.levels)
+    skipped_train = []
+    X, Y, E = records(range(a.train), a.tol, a.levels, skipped_train)
     t_rec = time.perf_counter() - t0
     if a.records:
         np.savez(a.records, X=X, Y=Y, E=E)
@@ -166,7 +187,8 @@ def main():
     t0 = time.perf_counter()
     rows = compare(prop, thr, range(100000, 100000 + a.test), a.tol, a.levels, a.fp64_every)
     t_cmp = time.perf_counter() - t0
-    res = {"train_structures": a.train, "test_structures": a.test, "records": int(len(Y)),
+    res = {"train_structures": a.train, "train_skipped": skipped_train, "test_structures": a.test,
+           "records": int(len(Y)),
            "positive_fraction": float(Y.mean()), "record_s": t_rec, "fit_s": t_fit, "compare_s": t_cmp,
            "final_train_loss": loss, "threshold": thr, "train_recall": recall, "train_skipped_negatives": skipped,
            **summary(rows), "rows": rows}
