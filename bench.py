@@ -16,7 +16,9 @@ e2e   : the same metric through the public call sequence a BsaLib user makes
 --impl reference times the reference's own algorithm (the oracle's restatement of
         BsaLib's OpenMP Classic scalar routine, run on the host cores) on a bounded sample.
 Multi-GPU (--gpus N under torchrun): every rank evaluates its own structure (independent
-wind cases, seed per rank): weak scaling, no collective on the data path.
+wind cases, seed per rank): weak scaling, no collective on the data path.  With --shard the
+ranks split one analysis of one structure instead (bsa_gpu_setClassicShard: interleaved product
+rows of the E form; the moments summed once over NCCL): strong scaling.
 """
 from __future__ import annotations
 
@@ -415,7 +417,8 @@ def run_ours(args):
     from bsalib_gb300.problem import tall_building
     bbuild.build()
     prec = api.PREC_BF16X3 if args.precision == "bf16x3" else api.PREC_FP64
-    prob = tall_building(seed=2024 + rank)
+    shard = args.shard and ws > 1
+    prob = tall_building(seed=2024 if shard else 2024 + rank)
     nf = prob.classic_nf()
     npts = nf * nf
 
@@ -426,6 +429,8 @@ def run_ours(args):
 
     # ---- value: problem resident on the device, device-timed steps ----
     s = api.BsaSession(prob, precision=prec)
+    if shard:
+        s.set_shard(rank, ws)
     for _ in range(args.warmup):
         s.run()
     ms, gemm_ms, launches = [], [], 0
@@ -445,9 +450,16 @@ def run_ours(args):
         t = torch.tensor([step_ms], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         step_ms = float(t.item())
-    value = ws * npts / (step_ms / 1e3)
+    value = (1 if shard else ws) * npts / (step_ms / 1e3)
+    if shard:
+        # the shards' moments summed once over the ranks (the path's only exchange)
+        from bsalib_gb300.dist import sum_moments
+        r = dict(r, **sum_moments({k: r[k] for k in ("m2mr_cls", "m3mr_cls", "m3mf_cls")}, torch.distributed,
+                                  device="cuda"))
     sk_mixed = s.skewness(r["m2mr_cls"], r["m3mr_cls"])
     # ---- the same analysis with the central symmetry of the grid (half the rows) ----
+    if shard:
+        s.set_shard(0, 1)
     s.set_symmetry(True)
     s.run()
     sym_ms = []
@@ -475,6 +487,8 @@ def run_ours(args):
     h2d = d2h = 0.0
     for _ in range(args.steps):
         s2 = api.BsaSession(prob, precision=prec)
+        if shard:
+            s2.set_shard(rank, ws)
         s2.run()
         st2 = s2.stats()
         h2d, d2h = st2.h2d_bytes, st2.d2h_bytes
@@ -485,7 +499,7 @@ def run_ours(args):
         t = torch.tensor([e2e_step], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         e2e_step = float(t.item())
-    e2e = ws * npts / e2e_step
+    e2e = (1 if shard else ws) * npts / e2e_step
     # bytes the caller hands over: the problem arrays borrowed by the setters
     h2d_in = sum(a.nbytes for a in (prob.phi, prob.wfc, prob.nod_corr, prob.u_node, prob.wz_node, prob.L,
                                     prob.sigma, prob.natf, prob.Mg, prob.Kg, prob.Cg, prob.xsi, prob.n_load))
@@ -517,7 +531,8 @@ def run_ours(args):
         swp = sweep_leg()
         out = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
+            "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True,
+            "scaling": "strong" if shard else "weak",
             "vs_baseline": None, "dtype": "bf16x3 contraction (fp32 accumulate), fp64 FRF/moments"
             if prec == api.PREC_BF16X3 else "f64", "data": "synthetic",
             "config": dict(CONFIG),
@@ -558,6 +573,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="bf16x3", choices=["bf16x3", "fp64"])
+    ap.add_argument("--shard", action="store_true",
+                    help="with --gpus N > 1: the ranks split one analysis (strong scaling) instead of running "
+                         "one structure each")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -101,7 +101,7 @@ def load(path: Optional[str] = None):
         "bsa_gpu_setPrecision": [i], "bsa_gpu_setClassicTruncation": [i], "bsa_gpu_setClassicRows": [i, i],
         "bsa_gpu_clsBispectra": [vp, i, vp, vp, vp], "bsa_gpu_mshBispectra": [vp, vp, i, vp, vp],
         "bsa_gpu_clsBispectraAt": [vp, vp, i, vp, vp], "bsa_gpu_setWaitTest": [i],
-        "bsa_gpu_setMesherGraphs": [i], "bsa_enableVisualMode": [], "bsa_setVisualIndexes": [vp, i], "bsa_setBRMExportDefaultMode": [i],
+        "bsa_gpu_setMesherGraphs": [i], "bsa_gpu_setClassicShard": [i, i], "bsa_enableVisualMode": [], "bsa_setVisualIndexes": [vp, i], "bsa_setBRMExportDefaultMode": [i],
         "bsa_gpu_setTilePlan": [i] * 8, "bsa_gpu_clearTilePlans": [], "bsa_gpu_loadTilePlans": [C.c_char_p],
         "bsa_gpu_getTilePlan": [i, i, i, i, vp],
         "bsa_gpu_mshMoments": [vp, vp, vp, i, vp, vp], "bsa_gpu_getStats": [vp], "bsa_gpu_releaseDeviceCache": [], "bsa_gpu_setClassicForm": [i],
@@ -235,6 +235,10 @@ class BsaSession:
     def set_classic_form(self, form: int):
         """1: the E form of the split contraction where it applies (default); 0: D1 / D3 form."""
         check(self.lib.bsa_gpu_setClassicForm(int(form)), "bsa_gpu_setClassicForm")
+
+    def set_shard(self, rank: int, nshards: int):
+        """bsa_gpu_setClassicShard: this session evaluates shard `rank` of `nshards`."""
+        check(self.lib.bsa_gpu_setClassicShard(int(rank), int(nshards)), "bsa_gpu_setClassicShard")
 
     def set_rows(self, r_begin: int, r_end: int = -1):
         """Evaluate only Classic grid rows [r_begin, r_end) (f1 index)."""

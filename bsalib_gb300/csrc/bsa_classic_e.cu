@@ -96,8 +96,10 @@ __global__ void __launch_bounds__(kThreads, 1)  // 14 warps: at most 128 registe
     const uint32_t tmem = *tmem_slot;
 
     const int mt = blockIdx.x % P.MT;
-    const int rstep = gridDim.x / P.MT;
-    const int r0 = blockIdx.x / P.MT;
+    // grid rows p of this CTA: every (grid / MT)-th row of the shard's rows p0 + pstep l
+    const int pstep = P.pstep_m1 + 1;
+    const int rstep = (gridDim.x / P.MT) * pstep;
+    const int r0 = P.p0 + (blockIdx.x / P.MT) * pstep;
     const uint32_t tx_bytes = 2u * kTileBytes + 4u * (uint32_t)(BROWS * 128);
 
     if (warp == 0) {
@@ -376,6 +378,10 @@ int Engine::contract_e(const PointSrc &ps, double *m3mf, double *m3mr, const ESa
     prm.err = derr;
     prm.test_skip_tile1 = wait_test_tile1;
     wait_test_tile1 = 0;  // one analysis only
+    if (cls_shards > 1 && !smp) {  // product rows p = rank + shards l (bsa_gpu_setClassicShard)
+        prm.p0 = cls_shard;
+        prm.pstep_m1 = cls_shards - 1;
+    }
     const long long nm3 = (long long)nm * nm * nm;
     if (smp) {
         prm.slot = smp->slot;

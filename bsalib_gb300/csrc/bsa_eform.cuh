@@ -59,6 +59,9 @@ struct EParams {
     // Diagnostics (bsa_gpu_setWaitTest): t + 1 makes CTA 0's MMA warp omit the accumulator-ready
     // signal of its tile t, so the epilogue's bounded wait runs out; 0 = off.
     int test_skip_tile1;
+    // Shard of the product rows (bsa_gpu_setClassicShard): rows p = p0 + (pstep_m1 + 1) l, l = 0, 1, ...
+    // (zero-initialised: every row).
+    int p0, pstep_m1;
 };
 
 // Shared-memory float2 load the compiler does not hoist (keeps the per-mode FRF values out

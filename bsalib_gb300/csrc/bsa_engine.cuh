@@ -91,6 +91,7 @@ struct Engine {
     int precision = 0;          // BSA_PREC_FP64
     bool classic_trunc = true;  // S(f1+f2) beyond the classic grid reads zero
     int shard_r0 = 0, shard_r1 = -1;  // classic grid rows evaluated (-1: to the end)
+    int cls_shard = 0, cls_shards = 1;  // bsa_gpu_setClassicShard: this shard of cls_shards
     // POD truncation requests (bsa_setPODTruncationThreshold / bsa_setPODNOfModesKept)
     std::vector<std::vector<int>> own_i;     // arrays read by bsa_loadInputFiles (owned here)
     std::vector<std::vector<double>> own_d;

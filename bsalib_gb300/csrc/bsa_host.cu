@@ -134,6 +134,8 @@ void Engine::reset_inputs() {
     classic_trunc = true;
     shard_r0 = 0;
     shard_r1 = -1;
+    cls_shard = 0;
+    cls_shards = 1;
     pod_trunc_lim = 0.0;
     pod_nmodes = 0;
     export_fn = nullptr;
@@ -447,9 +449,17 @@ int Engine::run_classic(double *m2mf, double *m2mr, double *m2o2mr, double *m3mf
     if (grid_out) *grid_out = f;
     const int nf = (int)f.size();
     if (nf < 2) return fail(BSA_ERR_ARG, "classic grid needs at least 2 frequencies");
-    // Row shard (f1 index): the moments of all shards sum to the full grid's.
-    const int r0 = std::min(std::max(shard_r0, 0), nf);
-    const int r1 = shard_r1 < 0 ? nf : std::min(shard_r1, nf);
+    // Row shard (f1 index): the moments of all shards sum to the full grid's.  With
+    // bsa_gpu_setClassicShard the rows are the shard's contiguous block (the second-order
+    // moments, and the bispectrum outside the E form); the E form shards its products instead.
+    int r0 = std::min(std::max(shard_r0, 0), nf);
+    int r1 = shard_r1 < 0 ? nf : std::min(shard_r1, nf);
+    if (cls_shards > 1) {
+        if (cls_shards > nf) return fail(BSA_ERR_ARG, "%d shards of a %d-row grid", cls_shards, nf);
+        const int base = nf / cls_shards, extra = nf % cls_shards;
+        r0 = cls_shard * base + std::min(cls_shard, extra);
+        r1 = r0 + base + (cls_shard < extra ? 1 : 0);
+    }
     if (r1 <= r0) return fail(BSA_ERR_ARG, "empty classic row shard [%d, %d)", r0, r1);
     if ((bf_host || br_host) && (r0 != 0 || r1 != nf))
         return fail(BSA_ERR_ARG, "materialised bispectra need the full grid");
@@ -524,7 +534,13 @@ int Engine::run_classic(double *m2mf, double *m2mr, double *m2o2mr, double *m3mf
         // The split path's E form (bsa_classic_e.cu) already forms each distinct product of the
         // whole grid once, which half the rows would not improve on: there the symmetry is not
         // applied.
-        const bool e_form = mixed && use_e_form && nme <= kEFormMaxModes && !analytic && (nf & 1) && r0 == 0 && r1 == nf;
+        bool e_form = mixed && use_e_form && nme <= kEFormMaxModes && !analytic && (nf & 1) &&
+                      plan_prefer_e(nme, K, nf) && ((r0 == 0 && r1 == nf) || cls_shards > 1);
+        if (e_form && cls_shards > 1) {
+            // the E form of a shard: every output point, the products of rows p = shard + shards l
+            ps.r0 = 0;
+            ps.nr = nf;
+        }
         const bool file_export = brm_file_wanted(true);
         const bool sym =
             classic_sym && set.defsc == 1 && !bf_host && !br_host && !export_fn && !file_export && !e_form;
@@ -1163,6 +1179,15 @@ int bsa_gpu_clsBispectra(double *f_out, int nf_cap, int *nf, double *bisp_f, dou
     E.precision = prec;
     if (rc) return rc;
     if (f_out) std::memcpy(f_out, grid.data(), sizeof(double) * grid.size());
+    return BSA_OK;
+}
+
+int bsa_gpu_setClassicShard(int rank, int nshards) {
+    GUARD();
+    if (nshards < 1 || rank < 0 || rank >= nshards)
+        return eng().fail(BSA_ERR_ARG, "shard %d of %d", rank, nshards);
+    eng().cls_shard = rank;
+    eng().cls_shards = nshards;
     return BSA_OK;
 }
 

@@ -38,9 +38,10 @@ def sum_moments(parts: Dict[str, np.ndarray], dist=None, device="cpu") -> Dict[s
 
 
 def run_classic_sharded(session, dist=None, device="cuda") -> Dict[str, np.ndarray]:
-    """One Classic analysis split over the ranks of the default process group."""
+    """One Classic analysis split over the ranks of the default process group
+    (bsa_gpu_setClassicShard: contiguous row blocks, interleaved product rows in the split
+    precision's E form), the moments summed over the ranks."""
     rank, world = (dist.get_rank(), dist.get_world_size()) if dist is not None and dist.is_initialized() else (0, 1)
-    r0, r1 = shard_rows(session.prob.classic_nf(), rank, world)
-    session.set_rows(r0, r1)
+    session.set_shard(rank, world)
     out = session.run()
     return sum_moments({k: out[k] for k in MOMENT_KEYS}, dist, device)

@@ -241,6 +241,15 @@ int bsa_gpu_setClassicTruncation(int on);
  * the rows sum to the full grid's (multi-GPU / multi-process sharding, one host sum). */
 int bsa_gpu_setClassicRows(int r_begin, int r_end);
 
+/* Shard rank of nshards of the Classic analysis (no counterpart in the reference; multi-GPU or
+ * multi-process runs, one host sum): the second-order moments take the shard's contiguous block
+ * of grid rows (f1 index, sizes differing by at most one); the bispectrum moments take the same
+ * block, except in the split precision's E form, which forms each product E(f_p, f_q), q >= p,
+ * once for the whole grid and so takes the product rows p = rank + nshards l (interleaved, for
+ * balance).  Either way the moments of the nshards shards sum to the full grid's.  Overrides
+ * bsa_gpu_setClassicRows; (0, 1) is the whole analysis.  Reset by bsa_Finalise. */
+int bsa_gpu_setClassicShard(int rank, int nshards);
+
 /* No counterpart in the reference.  on != 0: on the symmetric Classic grid f = -N..N
  * (circular-frequency scaling, the reference's default) every factor of the path is even in
  * f, so B(f1, f2) = B(-f1, -f2); bsa_Run then evaluates the rows f1 <= 0 only, the rows f1 < 0
