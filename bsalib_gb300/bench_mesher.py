@@ -8,6 +8,7 @@ Prints the zone and lattice-point counts and, per run, the library statistics an
 response-bispectrum (BRM lattice) points per second.
 """
 import argparse
+import time
 
 from . import api, build
 from .problem import bridge_deck, cantilever_tower, tall_building
@@ -56,13 +57,16 @@ def main():
         if a.zones_only:
             return
         for _ in range(a.steps):
+            t0 = time.perf_counter()
             if a.synthetic:
                 s.msh_zones(zs)
             else:
                 s.run()
+            wall = time.perf_counter() - t0
             st = s.stats()
-            print(f"  {st.ms_total:.1f} ms total, {st.ms_gemm:.1f} ms contraction kernel, {st.kernels} kernels, "
-                  f"{st.points / (st.ms_total * 1e-3):.4g} BRM pts/s", flush=True)
+            print(f"  {st.ms_total:.1f} ms total (device), {wall * 1e3:.1f} ms wall, {st.ms_gemm:.1f} ms contraction "
+                  f"kernel, {st.kernels} kernels, {st.graphs} graphs, {st.points / (st.ms_total * 1e-3):.4g} BRM pts/s",
+                  flush=True)
     finally:
         s.close()
 
