@@ -1126,6 +1126,39 @@ int Engine::run_zones_mixed(const std::vector<ZoneDev> &zones, double *m3mf, dou
         size_t fr = 0, tot = 0;
         if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) tot = 0;
         const double budget = std::max(4e9, 0.4 * (double)tot);
+        // A zone too large for a quarter of a pass is split into strips of consecutive lattice
+        // lines that share their boundary lines (the trapezoid's half weights of a shared BFM /
+        // BRM line from both strips add up to the unsplit zone's interior weight, and every cell
+        // is interpolated within one strip): the same integrals in passes that fit.
+        std::vector<int> parent;
+        {
+            std::vector<ZoneDev> split;
+            for (size_t k = 0; k < axis.size(); ++k) {
+                const ZoneDev &z = axis[k];
+                const double NJ = (double)((z.nj - 1) * z.Fj + 1);
+                const double line = per_u + per_pt * z.nj + per_q * z.Fi * NJ;  // bytes one more line adds
+                const double fixed = per_u * z.nj + per_col * z.nj + per_q * NJ;
+                const double whole = fixed + line * z.ni;
+                if (whole <= 0.25 * budget && (long long)z.ni * z.nj <= 1000000) {
+                    split.push_back(z);
+                    parent.push_back((int)k);
+                    continue;
+                }
+                const int L = (int)std::max(2.0, std::min(std::floor((0.25 * budget - fixed) / line),
+                                                          std::floor(1000000.0 / z.nj)));
+                for (int i0 = 0; i0 < z.ni - 1;) {
+                    const int i1 = std::min(i0 + L - 1, z.ni - 1);
+                    ZoneDev st = z;
+                    st.fi0 = z.fi0 + i0 * z.dIi;
+                    st.ni = i1 - i0 + 1;
+                    split.push_back(st);
+                    parent.push_back((int)k);
+                    i0 = i1;
+                }
+            }
+            axis.swap(split);
+        }
+        std::vector<double> zsplit(zdiag ? axis.size() * (size_t)nm : 0, 0.0);
         size_t b0 = 0;
         while (b0 < axis.size()) {
             std::vector<double> uf;
@@ -1151,9 +1184,14 @@ int Engine::run_zones_mixed(const std::vector<ZoneDev> &zones, double *m3mf, dou
                 ++b1;
             }
             std::vector<ZoneDev> batch(axis.begin() + b0, axis.begin() + b1);
-            if ((rc = msh_mixed_batch(batch, accF, accR, ms_gemm, ms_all, zdiag ? zdiag + b0 * nm : nullptr)))
+            if ((rc = msh_mixed_batch(batch, accF, accR, ms_gemm, ms_all, zdiag ? zsplit.data() + b0 * nm : nullptr)))
                 return rc;
             b0 = b1;
+        }
+        if (zdiag) {  // per-zone moments of the caller's zones: the sum over each zone's strips
+            for (size_t k = 0; k < zones.size() * (size_t)nm; ++k) zdiag[k] = 0.0;
+            for (size_t k = 0; k < axis.size(); ++k)
+                for (int m = 0; m < nm; ++m) zdiag[(size_t)parent[k] * nm + m] += zsplit[k * nm + m];
         }
     }
     if (m3mf) std::memcpy(m3mf, accF.data(), sizeof(double) * nm3);
