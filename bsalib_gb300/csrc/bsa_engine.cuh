@@ -99,6 +99,7 @@ struct Engine {
     bool use_e_form = true;     // bsa_gpu_setClassicForm: E form of the split contraction where it applies
     int wait_test_tile1 = 0;    // bsa_gpu_setWaitTest: tile + 1 whose ready signal CTA 0 omits (0 = off)
     bool msh_graphs = true;     // bsa_gpu_setMesherGraphs: each Mesher zone pass as one CUDA graph
+    bool msh_dev_expand = true; // bsa_gpu_setMesherExpansion: zone passes expanded on the device
     // Mesher controls (BsaLibData.F90:219-233, 273): delta validation, BFM multi-level
     // refinement, background peak restricted to the first direction, diagonal-crest scheme
     bool validate_deltas = true, bfm_mlr = true, bkg_restrict = false, premesh_diag_crest = false;
@@ -132,7 +133,7 @@ struct Engine {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr;
     DevBuf dL, dQ, dLogc, dPsdPar, dFrfM, dFrfK, dFrfC, dFreq, dS, dA, dPartF, dPartR, dOut, dPsdF, dWf, dPts,
         dPtsD, dBF, dBR, dMixA, dMixB, dMixH, dMixPart, dA32, dZones, dZidx, dWd3, dWd2, dMshT, dMshIdx, dLogc32, dL32,
-        dPod, dFlag, dSlot;
+        dPod, dFlag, dSlot, dHash;
 
     // stats
     double last_ms = 0, last_ms_contraction = 0, last_ms_gemm = 0, last_points = 0;
@@ -153,6 +154,8 @@ struct Engine {
     int build_atable(const std::vector<double> &freqs, bool fp32 = false, bool msh = false);
     int pod_atable(const std::vector<double> &freqs, bool fp32);
     int build_psd(const std::vector<double> &freqs);
+    int build_psd_dev(int nf);                 // the nf frequencies already in dFreq
+    int build_atable_dev(int nf, bool fp32);   // the same, A table (not the truncated POD form)
     // dimM_psd_ / dimM_bisp_ (src/bsa/BsaLibImpl.F90:313-355): nm / nm for the diagonal-only
     // spectra, nm^2 / nm^3 otherwise.
     long long dim_psd() const { return set.onlyd ? nme : (long long)nme * nme; }

@@ -157,7 +157,7 @@ void Engine::free_device() {
     if (stream) cudaStreamSynchronize(stream);  // the blocks go back to the cache for reuse
     for (DevBuf *b : {&dL, &dQ, &dLogc, &dPsdPar, &dFrfM, &dFrfK, &dFrfC, &dFreq, &dS, &dA, &dPartF, &dPartR,
                       &dOut, &dPsdF, &dWf, &dPts, &dPtsD, &dBF, &dBR, &dMixA, &dMixB, &dMixH, &dMixPart, &dA32,
-                      &dZones, &dZidx, &dWd3, &dWd2, &dMshT, &dMshIdx, &dLogc32, &dL32, &dPod, &dFlag, &dSlot})
+                      &dZones, &dZidx, &dWd3, &dWd2, &dMshT, &dMshIdx, &dLogc32, &dL32, &dPod, &dFlag, &dSlot, &dHash})
         b->release();
     if (stream) cudaStreamDestroy(stream);
     stream = nullptr;
@@ -347,10 +347,15 @@ FrfPar Engine::frf() const { return FrfPar{dFrfM.as<double>(), dFrfK.as<double>(
 
 // Nodal PSD table S[f][k] for a host list of frequencies (into dFreq, dS).
 int Engine::build_psd(const std::vector<double> &freqs) {
-    const int nf = (int)freqs.size();
-    const int ntc = (int)set.tc.size();
     cudaError_t e;
     if ((e = upload(dFreq, freqs, stream))) return cuda_fail(e, "uploading frequencies");
+    return build_psd_dev((int)freqs.size());
+}
+
+// Nodal PSD table S[f][k] for the nf frequencies already in dFreq.
+int Engine::build_psd_dev(int nf) {
+    const int ntc = (int)set.tc.size();
+    cudaError_t e;
     if ((e = dS.reserve(sizeof(double) * (size_t)nf * ntc * in.nnl))) return cuda_fail(e, "allocating S");
     if ((e = launch_nodal_psd(stream, nf, dFreq.as<double>(), ntc, set.tc.data(), in.nnl, dPsdPar.as<PsdNode>(),
                               in.psd_type, set.defsc, dS.as<double>())))
@@ -362,10 +367,16 @@ int Engine::build_psd(const std::vector<double> &freqs) {
 // Nodal PSD + A(f) for a host list of frequencies, into dA (FP64) or dA32 (FP32) rows.
 int Engine::build_atable(const std::vector<double> &freqs, bool fp32, bool msh) {
     if (msh && pod_truncates()) return pod_atable(freqs, fp32);  // bsa_pod.cu
-    const int nf = (int)freqs.size();
+    cudaError_t e;
+    if ((e = upload(dFreq, freqs, stream))) return cuda_fail(e, "uploading frequencies");
+    return build_atable_dev((int)freqs.size(), fp32);
+}
+
+// Nodal PSD + A(f) for the nf frequencies already in dFreq (not the truncated POD form).
+int Engine::build_atable_dev(int nf, bool fp32) {
     const int ntc = (int)set.tc.size();
     cudaError_t e;
-    int rc = build_psd(freqs);
+    int rc = build_psd_dev(nf);
     if (rc) return rc;
     if (fp32) {
         // FP32 table on the tensor cores (tf32 hi/lo split, FP32-level accuracy)
@@ -1233,6 +1244,12 @@ int bsa_gpu_getStats(bsa_gpu_stats *st) {
 int bsa_gpu_setMesherGraphs(int on) {
     GUARD();
     eng().msh_graphs = on != 0;
+    return BSA_OK;
+}
+
+int bsa_gpu_setMesherExpansion(int on_device) {
+    GUARD();
+    eng().msh_dev_expand = on_device != 0;
     return BSA_OK;
 }
 

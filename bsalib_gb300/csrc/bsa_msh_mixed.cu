@@ -814,6 +814,202 @@ __global__ void k_msh_reduce(int nm, int G, const double *__restrict__ part, dou
     m3mr[x] = 2.0 * sr;
 }
 
+// ------------------------------------------------------------------------------------
+// Device-side expansion of a zone pass: the zone list (one ZoneX per axis-aligned zone, with
+// its offsets) becomes, on the device, the distinct frequencies (A-table rows), the distinct
+// line / column frequencies (U blocks), the point and column index tables, the tasks and the
+// work queue.  Frequencies meet in open-addressing hash tables keyed by round(f 2^40) (values
+// equal to ~1e-12 Hz share a row); the occupied slots are then numbered in slot order.
+// ------------------------------------------------------------------------------------
+struct ZoneX {
+    double fi0, fj0, dI, dJ;  // f1 = fi0 + i dI (lines), f2 = fj0 + j dJ (columns)
+    int ni, nj;
+    long long pbase;  // first BFM point of the zone
+    int gbase;        // first column (G row block)
+    int tbase;        // first task: ni line tasks, then nj column tasks
+    long long ibase;  // first work item
+};
+
+constexpr unsigned long long kEmptyKey = 0x8080808080808080ull;  // memset pattern 0x80
+
+__device__ __forceinline__ long long fkey(double f) { return __double2ll_rn(f * 1099511627776.0); }  // 2^40
+
+__device__ __forceinline__ unsigned long long fhash(long long q, int bits) {
+    return ((unsigned long long)q * 0x9E3779B97F4A7C15ull) >> (64 - bits);
+}
+
+// Insert f's key; the table is at most half full.  A row's frequency is its key q 2^-40 (within
+// 4.6e-13 Hz of every frequency it serves), so the rows' values do not depend on which thread
+// inserted first.
+__device__ __forceinline__ void ht_insert(unsigned long long *keys, int bits, double f) {
+    const long long q = fkey(f);
+    const unsigned long long mask = (1ull << bits) - 1;
+    unsigned long long h = fhash(q, bits);
+    for (unsigned long long probe = 0; probe <= mask; ++probe, h = (h + 1) & mask) {
+        const unsigned long long prev = atomicCAS(&keys[h], kEmptyKey, (unsigned long long)q);
+        if (prev == kEmptyKey || prev == (unsigned long long)q) return;
+    }
+}
+
+// Row of f (its slot's number); -1 if absent (never for an inserted f).
+__device__ __forceinline__ int ht_find(const unsigned long long *keys, const int *ids, int bits, double f) {
+    const long long q = fkey(f);
+    const unsigned long long mask = (1ull << bits) - 1;
+    unsigned long long h = fhash(q, bits);
+    for (unsigned long long probe = 0; probe <= mask; ++probe, h = (h + 1) & mask) {
+        const unsigned long long k = keys[h];
+        if (k == (unsigned long long)q) return ids[h];
+        if (k == kEmptyKey) return -1;
+    }
+    return -1;
+}
+
+// Line, column and point frequencies of a zone, rounded as written (no contraction).
+__device__ __forceinline__ double zx_line(const ZoneX &z, int i) { return __dadd_rn(z.fi0, __dmul_rn((double)i, z.dI)); }
+__device__ __forceinline__ double zx_col(const ZoneX &z, int j) { return __dadd_rn(z.fj0, __dmul_rn((double)j, z.dJ)); }
+
+__global__ void k_fx_insert(int nz, const ZoneX *__restrict__ zx, unsigned long long *keysF, int bitsF,
+                            unsigned long long *keysU, int bitsU) {
+    const ZoneX z = zx[blockIdx.x];
+    const long long n = (long long)z.ni + z.nj + (long long)z.ni * z.nj;
+    for (long long x = threadIdx.x; x < n; x += blockDim.x) {
+        double f;
+        bool lc = true;
+        if (x < z.ni) {
+            f = zx_line(z, (int)x);
+        } else if (x < z.ni + z.nj) {
+            f = zx_col(z, (int)(x - z.ni));
+        } else {
+            const long long y = x - z.ni - z.nj;
+            const int i = (int)(y / z.nj), j = (int)(y - (long long)i * z.nj);
+            f = __dadd_rn(zx_line(z, i), zx_col(z, j));
+            lc = false;
+        }
+        ht_insert(keysF, bitsF, f);
+        if (lc) ht_insert(keysU, bitsU, f);
+    }
+}
+
+constexpr int kScanBlock = 1024;
+
+// Occupied slots per block of kScanBlock slots.
+__global__ void k_fx_count(int cap, const unsigned long long *__restrict__ keys, int *__restrict__ cnt) {
+    const int s = blockIdx.x * kScanBlock + threadIdx.x;
+    const int occ = s < cap && keys[s] != kEmptyKey;
+    const int c = __syncthreads_count(occ);
+    if (threadIdx.x == 0) cnt[blockIdx.x] = c;
+}
+
+// Exclusive scan of the block counts in place (one block); cnt[nb] receives the total.
+__global__ void k_fx_scan(int nb, int *__restrict__ cnt) {
+    __shared__ int carry;
+    __shared__ int ws[32];
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int b0 = 0; b0 < nb; b0 += blockDim.x) {
+        const int b = b0 + threadIdx.x;
+        const int v = b < nb ? cnt[b] : 0;
+        int x = v;  // inclusive warp scan
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, x, o);
+            if ((threadIdx.x & 31) >= o) x += y;
+        }
+        if ((threadIdx.x & 31) == 31) ws[threadIdx.x >> 5] = x;
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            int w = threadIdx.x < (int)(blockDim.x >> 5) ? ws[threadIdx.x] : 0;
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, w, o);
+                if (threadIdx.x >= o) w += y;
+            }
+            ws[threadIdx.x] = w;  // inclusive over warps
+        }
+        __syncthreads();
+        const int excl = carry + x - v + ((threadIdx.x >> 5) ? ws[(threadIdx.x >> 5) - 1] : 0);
+        if (b < nb) cnt[b] = excl;
+        __syncthreads();
+        if (threadIdx.x == blockDim.x - 1) carry = excl + v;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) cnt[nb] = carry;
+}
+
+// Number the occupied slots in slot order; the row's frequency is its key q 2^-40.
+__global__ void k_fx_ids(int cap, const unsigned long long *__restrict__ keys, const int *__restrict__ off,
+                         int *__restrict__ ids, double *__restrict__ freq) {
+    __shared__ int ws[kScanBlock / 32];
+    const int s = blockIdx.x * kScanBlock + threadIdx.x;
+    const int occ = s < cap && keys[s] != kEmptyKey;
+    const unsigned bal = __ballot_sync(0xffffffffu, occ);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) ws[warp] = __popc(bal);
+    __syncthreads();
+    int before = 0;
+    for (int w = 0; w < warp; ++w) before += ws[w];
+    if (occ) {
+        const int id = off[blockIdx.x] + before + __popc(bal & ((1u << lane) - 1u));
+        ids[s] = id;
+        freq[id] = __ll2double_rn((long long)keys[s]) * 9.094947017729282379150390625e-13;  // 2^-40
+    }
+}
+
+// The zone's tables: U block and A row of its lines and columns, its point (sum) rows in line
+// and in column order, its tasks and its work items, in the order the host would list them.
+__global__ void k_fx_expand(int nz, const ZoneX *__restrict__ zx, const unsigned long long *__restrict__ keysF,
+                            const int *__restrict__ idsF, int bitsF, const unsigned long long *__restrict__ keysU,
+                            const int *__restrict__ idsU, int bitsU, long long npts, int Mp, int NMT, int NC, int MT,
+                            int *__restrict__ usrc, int *__restrict__ gsrc, int *__restrict__ ssrc,
+                            Task *__restrict__ tasks, int4 *__restrict__ items, int *__restrict__ err) {
+    const ZoneX z = zx[blockIdx.x];
+    const int ntl_l = (z.nj + NC - 1) / NC, ntl_c = (z.ni + NC - 1) / NC, nic = (ntl_c + 1) / 2;
+    const long long line_items = (long long)z.ni * MT * ntl_l;
+    for (int x = threadIdx.x; x < z.ni + z.nj; x += blockDim.x) {
+        const bool line = x < z.ni;
+        const int i = line ? x : x - z.ni;
+        const double f = line ? zx_line(z, i) : zx_col(z, i);
+        int fid = ht_find(keysF, idsF, bitsF, f), uid = ht_find(keysU, idsU, bitsU, f);
+        if (fid < 0 || uid < 0) {  // never for an inserted frequency; row 0 keeps every index valid
+            atomicCAS(err, 0, 8);
+            fid = max(fid, 0);
+            uid = max(uid, 0);
+        }
+        usrc[uid] = fid;  // zones sharing the frequency write the same value
+        if (line) {
+            tasks[z.tbase + i] = Task{uid * Mp, z.gbase * NMT, (int)((z.pbase + (long long)i * z.nj) * NMT), z.nj,
+                                      (int)(z.pbase + (long long)i * z.nj), 1, 0};
+        } else {
+            gsrc[z.gbase + i] = fid;
+            tasks[z.tbase + z.ni + i] = Task{uid * Mp, -1, (int)((npts + z.pbase + (long long)i * z.ni) * NMT), z.ni,
+                                             (int)(z.pbase + i), z.nj, 1};
+        }
+    }
+    for (long long y = threadIdx.x; y < (long long)z.ni * z.nj; y += blockDim.x) {
+        const int i = (int)(y / z.nj), j = (int)(y - (long long)i * z.nj);
+        int fid = ht_find(keysF, idsF, bitsF, __dadd_rn(zx_line(z, i), zx_col(z, j)));
+        if (fid < 0) {
+            atomicCAS(err, 0, 8);
+            fid = 0;
+        }
+        ssrc[z.pbase + y] = fid;                                    // line order (line tasks)
+        ssrc[npts + z.pbase + (long long)j * z.ni + i] = fid;       // column order (column tasks)
+    }
+    const long long nit = line_items + (long long)z.nj * MT * nic;
+    for (long long y = threadIdx.x; y < nit; y += blockDim.x) {
+        int4 it;
+        if (y < line_items) {
+            const int i = (int)(y / ((long long)MT * ntl_l));
+            const int r = (int)(y - (long long)i * MT * ntl_l), mt = r / ntl_l, nt = r - mt * ntl_l;
+            it = make_int4(z.tbase + i, mt, nt, nt + 1);
+        } else {
+            const long long yc = y - line_items;
+            const int j = (int)(yc / ((long long)MT * nic));
+            const int r = (int)(yc - (long long)j * MT * nic), mt = r / nic, k = r - mt * nic;
+            it = make_int4(z.tbase + z.ni + j, mt, 2 * k, min(2 * k + 2, ntl_c));
+        }
+        items[z.ibase + y] = it;
+    }
+}
+
 }  // namespace mshmix
 
 // ------------------------------------------------------------------------------------
@@ -871,46 +1067,124 @@ int Engine::msh_mixed_batch(const std::vector<ZoneDev> &zs, std::vector<double> 
     const int nm = nme, nm2 = nm * nm, nm3 = nm2 * nm;
     const int NMT = plan_msh_width(nm, K), NC = kBN / NMT, BROWS = NC * NMT;
     const int Kp = ((K + kBK - 1) / kBK) * kBK, Mp = ((nm2 + kBM - 1) / kBM) * kBM, MT = Mp / kBM;
-    // frequencies of lines, columns and points
-    FreqIndex F, UF;
-    long long npts = 0, ncells = 0, ncol = 0, nbrm = 0;
+    // Per-zone records and offsets (O(zones) on the host): ZoneM for the zone integration, ZoneX
+    // for the expansion -- the first BFM point, column, task and work item of every zone.
+    long long npts = 0, ncells = 0, ncol = 0, nbrm = 0, ntasks = 0, nitems = 0;
+    std::vector<ZoneM> zm;
+    std::vector<ZoneX> zx;
+    zm.reserve(zs.size());
+    zx.reserve(zs.size());
     for (const ZoneDev &z : zs) {
-        for (int i = 0; i < z.ni; ++i) {
-            const double r = z.fi0 + i * z.dIi;
-            F.add(r);
-            UF.add(r);
-            for (int j = 0; j < z.nj; ++j) F.add(r + (z.fj0 + j * z.dJj));
-        }
-        for (int j = 0; j < z.nj; ++j) {
-            F.add(z.fj0 + j * z.dJj);
-            UF.add(z.fj0 + j * z.dJj);
-        }
+        zm.push_back(ZoneM{z.fi0, z.fj0, z.dIi, z.dJj, z.wI, z.wJ, z.sym, z.ni, z.nj, z.Fi, z.Fj, (int)npts, (int)ncells,
+                           (int)nbrm, (float)(z.sym * z.wI * z.wJ)});
+        zx.push_back(ZoneX{z.fi0, z.fj0, z.dIi, z.dJj, z.ni, z.nj, npts, (int)ncol, (int)ntasks, nitems});
+        const long long ntl_l = (z.nj + NC - 1) / NC, ntl_c = (z.ni + NC - 1) / NC;
+        nitems += (long long)z.ni * MT * ntl_l + (long long)z.nj * MT * ((ntl_c + 1) / 2);
         npts += (long long)z.ni * z.nj;
         ncells += (long long)(z.ni - 1) * (z.nj - 1);
         ncol += z.nj;
+        ntasks += z.ni + z.nj;
         nbrm += (long long)((z.ni - 1) * z.Fi + 1) * ((z.nj - 1) * z.Fj + 1);
     }
-    F.seal();
-    UF.seal();
-    const int nU = (int)UF.v.size();
-    std::vector<int> usrc(nU), gsrc((size_t)ncol), ssrc(2 * (size_t)npts);
-    for (int u = 0; u < nU; ++u) usrc[u] = F.at(UF.v[u]);
-    std::vector<Task> tasks;
-    std::vector<ZoneM> zm;
-    {
-        long long pb = 0, cb = 0, gb = 0, qb = 0;
+    if (2 * npts * NMT > 0x7fffffffLL || nitems > 0x7fffffffLL || nbrm > 0x7fffffffLL)
+        return fail(BSA_ERR_ARG, "Mesher zone pass too large");
+    cudaError_t e;
+    int rc;
+    if ((e = cudaEventRecord(ev2, stream))) return cuda_fail(e, "event");
+    // index tables, tasks, zone records and the work queue (U blocks: at most one per line /
+    // column frequency)
+    const size_t nlc = (size_t)ntasks;
+    const size_t nidx = nlc + ncol + 2 * (size_t)npts;
+    auto al16 = [](const void *q) { return (((uintptr_t)q) + 15) & ~(uintptr_t)15; };
+    if ((e = dMshIdx.reserve(nidx * sizeof(int) + ntasks * sizeof(Task) + zm.size() * sizeof(ZoneM) +
+                             nitems * sizeof(int4) + zx.size() * sizeof(ZoneX) + 128)))
+        return cuda_fail(e, "allocating Mesher tables");
+    char *ib = (char *)dMshIdx.p;
+    int *d_usrc = (int *)ib, *d_gsrc = d_usrc + nlc, *d_ssrc = d_gsrc + ncol;
+    Task *d_tasks = (Task *)al16(d_ssrc + 2 * npts);
+    ZoneM *d_zones = (ZoneM *)al16(d_tasks + ntasks);
+    int4 *d_items = (int4 *)al16(d_zones + zm.size());
+    ZoneX *d_zx = (ZoneX *)al16(d_items + nitems);
+    int nU = 0, *d_xerr = nullptr;
+    if ((e = cudaMemcpyAsync(d_zones, zm.data(), zm.size() * sizeof(ZoneM), cudaMemcpyHostToDevice, stream)))
+        return cuda_fail(e, "Mesher zone upload");
+    h2d += (double)(zm.size() * sizeof(ZoneM));
+    if (msh_dev_expand && !pod_truncates()) {
+        // The pass expanded on the device: distinct frequencies through hash tables, numbered in
+        // slot order (A rows into dFreq, U blocks), then every zone's tables and work items.
+        const long long nF_max = (long long)nlc + npts;
+        int bitsF = 4, bitsU = 4;
+        while ((1LL << bitsF) < 2 * nF_max) ++bitsF;
+        while ((1LL << bitsU) < 2 * (long long)nlc) ++bitsU;
+        const long long capF = 1LL << bitsF, capU = 1LL << bitsU;
+        if (capF > (1LL << 30)) return fail(BSA_ERR_ARG, "Mesher zone pass too large");
+        const int nbF = (int)((capF + kScanBlock - 1) / kScanBlock), nbU = (int)((capU + kScanBlock - 1) / kScanBlock);
+        const size_t hbytes = (size_t)(capF + capU) * (8 + 4) + (size_t)(nbF + nbU + 2) * 4 + 16 * 8 +
+                              (size_t)capU * 8;
+        if ((e = dHash.reserve(hbytes)) || (e = dFreq.reserve(sizeof(double) * (size_t)nF_max)))
+            return cuda_fail(e, "allocating Mesher frequency tables");
+        unsigned long long *keysF = dHash.as<unsigned long long>(), *keysU = keysF + capF;
+        double *ufreq = (double *)(keysU + capU);
+        int *idsF = (int *)(ufreq + capU), *idsU = idsF + capF, *cntF = idsU + capU, *cntU = cntF + nbF + 1;
+        d_xerr = cntU + nbU + 1;
+        if ((e = cudaMemsetAsync(keysF, 0x80, (size_t)(capF + capU) * 8, stream)) ||
+            (e = cudaMemsetAsync(d_xerr, 0, sizeof(int), stream)) ||
+            (e = cudaMemcpyAsync(d_zx, zx.data(), zx.size() * sizeof(ZoneX), cudaMemcpyHostToDevice, stream)))
+            return cuda_fail(e, "Mesher expansion set-up");
+        h2d += (double)(zx.size() * sizeof(ZoneX));
+        const int nz = (int)zx.size();
+        k_fx_insert<<<nz, 256, 0, stream>>>(nz, d_zx, keysF, bitsF, keysU, bitsU);
+        k_fx_count<<<nbF, kScanBlock, 0, stream>>>((int)capF, keysF, cntF);
+        k_fx_scan<<<1, 1024, 0, stream>>>(nbF, cntF);
+        k_fx_ids<<<nbF, kScanBlock, 0, stream>>>((int)capF, keysF, cntF, idsF, dFreq.as<double>());
+        k_fx_count<<<nbU, kScanBlock, 0, stream>>>((int)capU, keysU, cntU);
+        k_fx_scan<<<1, 1024, 0, stream>>>(nbU, cntU);
+        k_fx_ids<<<nbU, kScanBlock, 0, stream>>>((int)capU, keysU, cntU, idsU, ufreq);
+        int counts[2] = {0, 0};
+        if ((e = cudaGetLastError()) ||
+            (e = cudaMemcpyAsync(&counts[0], cntF + nbF, sizeof(int), cudaMemcpyDeviceToHost, stream)) ||
+            (e = cudaMemcpyAsync(&counts[1], cntU + nbU, sizeof(int), cudaMemcpyDeviceToHost, stream)) ||
+            (e = cudaStreamSynchronize(stream)))
+            return cuda_fail(e, "Mesher frequency tables");
+        nU = counts[1];
+        k_fx_expand<<<nz, 256, 0, stream>>>(nz, d_zx, keysF, idsF, bitsF, keysU, idsU, bitsU, npts, Mp, NMT, NC, MT,
+                                            d_usrc, d_gsrc, d_ssrc, d_tasks, d_items, d_xerr);
+        if ((e = cudaGetLastError())) return cuda_fail(e, "Mesher zone expansion");
+        kernels += 8;
+        if ((rc = build_atable_dev(counts[0], true))) return rc;
+    } else {
+        // The same tables built on the host (and the frequencies of the truncated POD form,
+        // whose A table is formed from host frequencies).
+        FreqIndex F, UF;
         for (const ZoneDev &z : zs) {
-            ZoneM m{z.fi0, z.fj0, z.dIi, z.dJj, z.wI, z.wJ, z.sym, z.ni, z.nj, z.Fi, z.Fj, (int)pb, (int)cb, (int)qb,
-                    (float)(z.sym * z.wI * z.wJ)};
-            qb += (long long)((z.ni - 1) * z.Fi + 1) * ((z.nj - 1) * z.Fj + 1);
-            zm.push_back(m);
+            for (int i = 0; i < z.ni; ++i) {
+                const double r = z.fi0 + i * z.dIi;
+                F.add(r);
+                UF.add(r);
+                for (int j = 0; j < z.nj; ++j) F.add(r + (z.fj0 + j * z.dJj));
+            }
+            for (int j = 0; j < z.nj; ++j) {
+                F.add(z.fj0 + j * z.dJj);
+                UF.add(z.fj0 + j * z.dJj);
+            }
+        }
+        F.seal();
+        UF.seal();
+        nU = (int)UF.v.size();
+        std::vector<int> usrc(nU), gsrc((size_t)ncol), ssrc(2 * (size_t)npts);
+        for (int u = 0; u < nU; ++u) usrc[u] = F.at(UF.v[u]);
+        std::vector<Task> tasks;
+        tasks.reserve(ntasks);
+        for (size_t k = 0; k < zs.size(); ++k) {
+            const ZoneDev &z = zs[k];
+            const long long pb = zx[k].pbase, gb = zx[k].gbase;
             for (int j = 0; j < z.nj; ++j) gsrc[gb + j] = F.at(z.fj0 + j * z.dJj);
             for (int i = 0; i < z.ni; ++i) {
                 const double r = z.fi0 + i * z.dIi;
                 for (int j = 0; j < z.nj; ++j) {
                     const int row = F.at(r + (z.fj0 + j * z.dJj));
-                    ssrc[pb + (size_t)i * z.nj + j] = row;                  // line order (kind 0)
-                    ssrc[npts + pb + (size_t)j * z.ni + i] = row;           // column order (kind 1)
+                    ssrc[pb + (size_t)i * z.nj + j] = row;         // line order (kind 0)
+                    ssrc[npts + pb + (size_t)j * z.ni + i] = row;  // column order (kind 1)
                 }
                 tasks.push_back(Task{UF.at(r) * Mp, (int)gb * NMT, (int)(pb + (long long)i * z.nj) * NMT, z.nj,
                                      (int)(pb + (long long)i * z.nj), 1, 0});
@@ -918,28 +1192,32 @@ int Engine::msh_mixed_batch(const std::vector<ZoneDev> &zs, std::vector<double> 
             for (int j = 0; j < z.nj; ++j)
                 tasks.push_back(Task{UF.at(z.fj0 + j * z.dJj) * Mp, -1, (int)(npts + pb + (long long)j * z.ni) * NMT,
                                      z.ni, (int)(pb + j), z.nj, 1});
-            pb += (long long)z.ni * z.nj;
-            cb += (long long)(z.ni - 1) * (z.nj - 1);
-            gb += z.nj;
         }
+        // work items: per task, its row tiles x N tiles (one, or two for column tasks), consecutive
+        std::vector<int4> witems;
+        witems.reserve(nitems);
+        for (size_t t = 0; t < tasks.size(); ++t) {
+            const int ntl = (tasks[t].ncols + NC - 1) / NC;
+            const int step = tasks[t].kind == 1 ? 2 : 1;  // column tasks: two N tiles per item
+            for (int mt = 0; mt < MT; ++mt)
+                for (int nt = 0; nt < ntl; nt += step)
+                    witems.push_back(make_int4((int)t, mt, nt, std::min(nt + step, ntl)));
+        }
+        if ((long long)witems.size() != nitems) return fail(BSA_ERR_STATE, "Mesher work-item count");
+        if ((e = cudaMemcpyAsync(d_usrc, usrc.data(), nU * sizeof(int), cudaMemcpyHostToDevice, stream)) ||
+            (e = cudaMemcpyAsync(d_gsrc, gsrc.data(), ncol * sizeof(int), cudaMemcpyHostToDevice, stream)) ||
+            (e = cudaMemcpyAsync(d_ssrc, ssrc.data(), 2 * npts * sizeof(int), cudaMemcpyHostToDevice, stream)) ||
+            (e = cudaMemcpyAsync(d_tasks, tasks.data(), tasks.size() * sizeof(Task), cudaMemcpyHostToDevice, stream)) ||
+            (e = cudaMemcpyAsync(d_items, witems.data(), witems.size() * sizeof(int4), cudaMemcpyHostToDevice,
+                                 stream)))
+            return cuda_fail(e, "Mesher task upload");
+        h2d += (double)((nU + ncol + 2 * npts) * sizeof(int) + tasks.size() * sizeof(Task) +
+                        witems.size() * sizeof(int4));
+        if ((rc = build_atable(F.v, true, true))) return rc;
     }
-    cudaError_t e;
-    int rc;
-    if ((e = cudaEventRecord(ev2, stream))) return cuda_fail(e, "event");
-    if ((rc = build_atable(F.v, true, true))) return rc;
     const size_t uel = (size_t)nU * Mp * Kp, gel = (size_t)ncol * NMT * Kp, sel = 2 * (size_t)npts * NMT * Kp;
     const int nm3p = (nm3 + 3) & ~3, hs = frf_row(nm);
     const size_t tel = (size_t)npts * nm3p;
-    const size_t nidx = (size_t)nU + ncol + 2 * (size_t)npts;
-    // work items: per task, its row tiles x N tiles (one, or two for column tasks), consecutive
-    std::vector<int4> witems;
-    for (size_t t = 0; t < tasks.size(); ++t) {
-        const int ntl = (tasks[t].ncols + NC - 1) / NC;
-        const int step = tasks[t].kind == 1 ? 2 : 1;  // column tasks: two N tiles per item
-        for (int mt = 0; mt < MT; ++mt)
-            for (int nt = 0; nt < ntl; nt += step) witems.push_back(make_int4((int)t, mt, nt, std::min(nt + step, ntl)));
-    }
-    if (witems.size() > (size_t)0x7fffffff) return fail(BSA_ERR_ARG, "too many Mesher work items");
     int dev = 0, nsm = 0;
     if ((e = cudaGetDevice(&dev)) || (e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev)))
         return cuda_fail(e, "device query");
@@ -949,8 +1227,6 @@ int Engine::msh_mixed_batch(const std::vector<ZoneDev> &zs, std::vector<double> 
     const int G = (int)std::max(1LL, std::min((long long)(2 * nsm) / nchunks, ncells));
     if ((e = dMixA.reserve(2 * uel * 2)) || (e = dMixB.reserve(2 * (gel + sel) * 2)) ||
         (e = dMshT.reserve(3 * tel * sizeof(float))) ||
-        (e = dMshIdx.reserve(nidx * sizeof(int) + tasks.size() * sizeof(Task) + zm.size() * sizeof(ZoneM) +
-                             witems.size() * sizeof(int4) + 64)) ||
         (e = dMixPart.reserve((size_t)G * 6 * nm3 * sizeof(double) + 2 * (size_t)nm3 * sizeof(double) + 256)) ||
         (e = dMixH.reserve((size_t)nbrm * hs * sizeof(float2) + (size_t)nbrm * sizeof(float) + 256 +
                            (zdiag ? zm.size() * nm * sizeof(double) : 0))))
@@ -958,23 +1234,10 @@ int Engine::msh_mixed_batch(const std::vector<ZoneDev> &zs, std::vector<double> 
     __nv_bfloat16 *Uh = dMixA.as<__nv_bfloat16>(), *Ul = Uh + uel;
     __nv_bfloat16 *Gh = dMixB.as<__nv_bfloat16>(), *Gl = Gh + gel, *Sh = Gl + gel, *Sl = Sh + sel;
     float *T1 = dMshT.as<float>(), *T3 = T1 + tel, *T2 = T3 + tel;
-    char *ib = (char *)dMshIdx.p;
-    int *d_usrc = (int *)ib, *d_gsrc = d_usrc + nU, *d_ssrc = d_gsrc + ncol;
-    Task *d_tasks = (Task *)(((uintptr_t)(d_ssrc + 2 * npts) + 15) & ~(uintptr_t)15);
-    ZoneM *d_zones = (ZoneM *)(((uintptr_t)(d_tasks + tasks.size()) + 15) & ~(uintptr_t)15);
-    int4 *d_items = (int4 *)(((uintptr_t)(d_zones + zm.size()) + 15) & ~(uintptr_t)15);
     double *part = dMixPart.as<double>(), *red = part + (size_t)G * 6 * nm3;
     int *derr = (int *)(red + 2 * (size_t)nm3), *dhead = derr + 1;
-    if ((e = cudaMemcpyAsync(d_usrc, usrc.data(), nU * sizeof(int), cudaMemcpyHostToDevice, stream)) ||
-        (e = cudaMemcpyAsync(d_gsrc, gsrc.data(), ncol * sizeof(int), cudaMemcpyHostToDevice, stream)) ||
-        (e = cudaMemcpyAsync(d_ssrc, ssrc.data(), 2 * npts * sizeof(int), cudaMemcpyHostToDevice, stream)) ||
-        (e = cudaMemcpyAsync(d_tasks, tasks.data(), tasks.size() * sizeof(Task), cudaMemcpyHostToDevice, stream)) ||
-        (e = cudaMemcpyAsync(d_zones, zm.data(), zm.size() * sizeof(ZoneM), cudaMemcpyHostToDevice, stream)) ||
-        (e = cudaMemcpyAsync(d_items, witems.data(), witems.size() * sizeof(int4), cudaMemcpyHostToDevice, stream)) ||
-        (e = cudaMemsetAsync(derr, 0, 2 * sizeof(int), stream)))  // error flag and queue head
+    if ((e = cudaMemsetAsync(derr, 0, 2 * sizeof(int), stream)))  // error flag and queue head
         return cuda_fail(e, "Mesher task upload");
-    h2d += (double)(nidx * sizeof(int) + tasks.size() * sizeof(Task) + zm.size() * sizeof(ZoneM) +
-                    witems.size() * sizeof(int4));
     CUtensorMap maps[6];
     if (!make_map(&maps[0], Uh, Kp, (uint64_t)nU * Mp, kBM) || !make_map(&maps[1], Ul, Kp, (uint64_t)nU * Mp, kBM) ||
         !make_map(&maps[2], Gh, Kp, (uint64_t)ncol * NMT, BROWS) || !make_map(&maps[3], Gl, Kp, (uint64_t)ncol * NMT, BROWS) ||
@@ -985,14 +1248,14 @@ int Engine::msh_mixed_batch(const std::vector<ZoneDev> &zs, std::vector<double> 
     prm.nm = nm; prm.NMT = NMT; prm.NC = NC; prm.BROWS = BROWS; prm.Mp = Mp; prm.MT = MT;
     prm.nk = Kp / kBK;
     prm.ks_last = (K - (prm.nk - 1) * kBK + 15) / 16;
-    prm.nitems = (int)witems.size();
+    prm.nitems = (int)nitems;
     prm.tasks = d_tasks;
     prm.items = d_items;
     prm.T1 = T1; prm.T3 = T3; prm.T2 = T2;
     prm.nm3p = nm3p;
     prm.err = derr;
     prm.head = dhead;
-    const long long nwork = (long long)witems.size();
+    const long long nwork = nitems;
     const int grid = (int)std::min<long long>(nwork, nsm);
     const size_t smem = (size_t)kStages * kStageBytes + 1024 + 256;
     if ((e = cudaFuncSetAttribute(k_msh_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) ||
@@ -1051,8 +1314,9 @@ int Engine::msh_mixed_batch(const std::vector<ZoneDev> &zs, std::vector<double> 
     kernels += 7 + (zdiag ? 1 : 0);
     graph_launches += graphed ? 1 : 0;
     std::vector<double> h(2 * (size_t)nm3);
-    int herr = 0;
-    if ((e = cudaMemcpyAsync(h.data(), red, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, stream)) ||
+    int herr = 0, xerr = 0;
+    if ((d_xerr && (e = cudaMemcpyAsync(&xerr, d_xerr, sizeof(int), cudaMemcpyDeviceToHost, stream))) ||
+        (e = cudaMemcpyAsync(h.data(), red, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, stream)) ||
         (e = cudaMemcpyAsync(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost, stream)) ||
         (zdiag && (e = cudaMemcpyAsync(zdiag, d_zdiag, sizeof(double) * zm.size() * nm, cudaMemcpyDeviceToHost,
                                        stream))) ||
@@ -1061,6 +1325,7 @@ int Engine::msh_mixed_batch(const std::vector<ZoneDev> &zs, std::vector<double> 
     if (gexec) cudaGraphExecDestroy(gexec);
     if (graph) cudaGraphDestroy(graph);
     d2h += (double)sizeof(double) * h.size() + sizeof(int);
+    if (xerr) return fail(BSA_ERR_STATE, "Mesher zone expansion: a frequency missing from its table");
     if (herr) return fail(BSA_ERR_TIMEOUT, "Mesher BF16x3 kernel: a pipeline wait ran out of its budget (role %d)", herr);
     float ms = 0.f;
     cudaEventElapsedTime(&ms, evg0, evg1);

@@ -441,6 +441,13 @@ int bsa_gpu_setWaitTest(int tile);
  * the library's stream; 0 launches the same kernels one by one.  Same results either way. */
 int bsa_gpu_setMesherGraphs(int on);
 
+/* No counterpart in the reference.  on_device != 0 (default): each split-precision Mesher zone
+ * pass is expanded on the device from its zone list -- distinct frequencies through hash tables
+ * (A-table rows, U blocks), the point and column index tables, the tasks and the work queue of
+ * the contraction; 0 builds the same tables on the host and uploads them.  The A rows' order
+ * differs (hash order), the moments agree to FP32 rounding. */
+int bsa_gpu_setMesherExpansion(int on_device);
+
 /* Device memory.  Blocks the library releases (bsa_Finalise, buffer growth) are kept for reuse
  * by the next analysis, up to a quarter of the device memory, so repeated bsa_Init ...
  * bsa_Finalise cycles do not pay cudaMalloc / cudaFree of the operand tables each time.  This
