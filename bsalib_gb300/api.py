@@ -58,6 +58,34 @@ class Zone(C.Structure):
                 ("Fi", C.c_int), ("Fj", C.c_int), ("sym", C.c_double), ("policy", C.c_int)]
 
 
+class Triangle(C.Structure):
+    """bsa_triangle: a triangular Mesher zone as the pre-mesh dumps it (include/bsa_gpu.h)."""
+    _fields_ = [("Ci", C.c_double), ("Cj", C.c_double), ("Ai", C.c_double), ("Aj", C.c_double),
+                ("Bi", C.c_double), ("Bj", C.c_double), ("rot", C.c_double), ("sym", C.c_double),
+                ("n", C.c_int), ("policy", C.c_int), ("bfm_i", C.c_int), ("bfm_j", C.c_int),
+                ("bfm_levels", C.c_int), ("brm_i", C.c_int), ("brm_j", C.c_int), ("seq", C.c_int)]
+
+
+def triangle_lattice(t: Triangle, visual=False):
+    """bsa_gpu_mshTriangLattice (host only): the post-mesh lattice of one triangle as a dict of
+    arrays (bfm [nb, 3], brm [nq, 3], qptr, qsrc, qc, exp [ne, 2], eq) and counts."""
+    lib = load()
+    cnt = np.zeros(6, dtype=np.int64)
+    oob = C.c_int(0)
+    check(lib.bsa_gpu_mshTriangLattice(C.byref(t), int(visual), _p(cnt), C.byref(oob), None, None, None, None,
+                                       None, None, None), "bsa_gpu_mshTriangLattice")
+    nb, nq, nnz, ne = (int(x) for x in cnt[:4])
+    out = dict(bfm=np.zeros((nb, 3)), brm=np.zeros((nq, 3)), qptr=np.zeros(nq + 1, dtype=np.int32),
+               qsrc=np.zeros(max(nnz, 1), dtype=np.int32), qc=np.zeros(max(nnz, 1)), exp=np.zeros((max(ne, 1), 2)),
+               eq=np.zeros(max(ne, 1), dtype=np.int32))
+    check(lib.bsa_gpu_mshTriangLattice(C.byref(t), int(visual), _p(cnt), C.byref(oob), _p(out["bfm"]),
+                                       _p(out["brm"]), _p(out["qptr"]), _p(out["qsrc"]), _p(out["qc"]),
+                                       _p(out["exp"]), _p(out["eq"])), "bsa_gpu_mshTriangLattice")
+    out["qsrc"], out["qc"], out["exp"], out["eq"] = out["qsrc"][:nnz], out["qc"][:nnz], out["exp"][:ne], out["eq"][:ne]
+    out["bfm_post"], out["brm_post"], out["oob"] = int(cnt[4]), int(cnt[5]), bool(oob.value)
+    return out
+
+
 class Stats(C.Structure):
     _fields_ = [("ms_total", C.c_double), ("ms_contraction", C.c_double), ("ms_gemm", C.c_double),
                 ("points", C.c_double), ("h2d_bytes", C.c_double), ("d2h_bytes", C.c_double),
@@ -118,6 +146,8 @@ def load(path: Optional[str] = None):
         "bsa_gpu_batchAdd": [vp], "bsa_gpu_batchCase": [i, vp, vp], "bsa_gpu_batchRun": [vp] * 5,
         "bsa_gpu_batchClear": [], "bsa_doValidateZoneDeltas": [i], "bsa_setBfmMLR": [i],
         "bsa_setMaxBkgPeakRestriction": [i], "bsa_setPremeshScheme": [i], "bsa_setPremeshMode": [i],
+        "bsa_gpu_mshGenerateTriangles": [vp, i, vp], "bsa_gpu_mshTriangles": [vp, i, vp, vp, vp],
+        "bsa_gpu_mshTriangLattice": [vp, i, vp, vp, vp, vp, vp, vp, vp, vp, vp],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)
@@ -330,6 +360,32 @@ class BsaSession:
         check(self.lib.bsa_gpu_mshGenerateZones(C.cast(arr, C.c_void_p), n.value, C.byref(n)),
               "bsa_gpu_mshGenerateZones")
         return list(arr)
+
+    def generate_triangles(self):
+        """The triangles of the Mesher layout (the diagonal-crest scheme lays them)."""
+        n = C.c_int(0)
+        check(self.lib.bsa_gpu_mshGenerateTriangles(None, 0, C.byref(n)), "bsa_gpu_mshGenerateTriangles")
+        arr = (Triangle * max(n.value, 1))()
+        check(self.lib.bsa_gpu_mshGenerateTriangles(C.cast(arr, C.c_void_p), n.value, C.byref(n)),
+              "bsa_gpu_mshGenerateTriangles")
+        return list(arr)[:n.value]
+
+    def msh_triangles(self, tris):
+        """Third moments (m3mf, m3mr) over a list of Triangle structures, and the BFM / BRM
+        point counts."""
+        arr = (Triangle * len(tris))(*tris)
+        nm3 = self.dims()[1]
+        mf, mr, cnt = np.zeros(nm3), np.zeros(nm3), np.zeros(2)
+        check(self.lib.bsa_gpu_mshTriangles(C.cast(arr, C.c_void_p), len(tris), _p(mf), _p(mr), _p(cnt)),
+              "bsa_gpu_mshTriangles")
+        return mf, mr, cnt
+
+    def set_premesh(self, diag_crest=False, mode_base=False):
+        """bsa_setPremeshScheme / bsa_setPremeshMode: each selects its non-default value only."""
+        if diag_crest:
+            check(self.lib.bsa_setPremeshScheme(1), "bsa_setPremeshScheme")
+        if mode_base:
+            check(self.lib.bsa_setPremeshMode(0), "bsa_setPremeshMode")
 
     def stats(self) -> Stats:
         st = Stats()

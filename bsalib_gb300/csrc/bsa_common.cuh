@@ -70,6 +70,11 @@ struct PointSrc {
     const double *f1, *f2;  // point frequencies (kPointsList)
     const ZoneDev *zones;   // optional (kPointsList): BRM neighbourhood of each point
     const int *zid, *zi, *zj; // zone and lattice coordinates of each point
+    // optional (kPointsList), listed BRM points: point p feeds entries [cptr[p], cptr[p + 1]) of
+    // cq, each (f1, f2, coefficient) of a BRM point, the coefficient its integration weight
+    // times the share of this BFM point in its interpolated BFM
+    const long long *cptr;
+    const double *cq;
 };
 
 struct FrfPar {

@@ -108,6 +108,22 @@ __global__ __launch_bounds__(256) void k_diag_fp64(const double *__restrict__ S,
             const double bfv = 2.0 * acc[u];
             const double M = frf.M[m], Kk = frf.K[m], C = frf.C[m];
             double F;
+            if (ps.cptr) {
+                // listed BRM points (triangular zones), each with its coefficient
+                F = 0.0;
+                const long long e1 = ps.cptr[p + 1];
+                for (long long e = ps.cptr[p]; e < e1; ++e) {
+                    const double v1 = ps.cq[3 * e] * kPi2, v2 = ps.cq[3 * e + 1] * kPi2;
+                    double h1r, h1i, h2r, h2i, h3r, h3i;
+                    frf_eval(M, Kk, C, v1, h1r, h1i);
+                    frf_eval(M, Kk, C, v2, h2r, h2i);
+                    frf_eval(M, Kk, C, v1 + v2, h3r, h3i);
+                    F = fma(ps.cq[3 * e + 2], (h1r * h2r - h1i * h2i) * h3r + (h1r * h2i + h1i * h2r) * h3i, F);
+                }
+                smf[u] = fma(w, bfv, smf[u]);
+                smr[u] = fma(F, bfv, smr[u]);
+                continue;
+            }
             if (z) {
                 // Mesher zone point: this BFM lattice point enters every BRM lattice point of
                 // its bilinear support with weight lambda (the full-tensor kernel's rule).

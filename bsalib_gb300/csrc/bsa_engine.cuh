@@ -73,6 +73,27 @@ struct Settings {
 };
 
 struct BatchCase;  // one case of the batched Classic sweep (bsa_batch.cu)
+
+// A dumped triangular zone (dumpTZ and DumpZone: corner C, A at the end of the J side, B,
+// rotation, refinements ni = nj = n, policy) with its policy's factors resolved (BFM
+// refinement levels disabled by bsa_setBfmMLR(false)) and the spatial-symmetry weight.
+struct TriDump {
+    double Ci, Cj, Ai, Aj, Bi, Bj, rot, sym;
+    int n, pol, bfi, bfj, bri, brj, nlevs;
+};
+
+// The post-mesh lattice of one triangle (bsa_triang.cu): BFM points (evaluation coordinates,
+// m3mf weights without the symmetry factor), BRM points (m3mr weights), per BRM point the BFM
+// points its interpolated BFM combines (CSR qptr / qsrc / qc), and the BRM export in the
+// routine's write order (written coordinates, BRM point or -1 for a slot never written).
+struct TriLattice {
+    std::vector<double> bf1, bf2, bw, q1, q2, qw, qc, e1, e2;
+    std::vector<int> qptr, qsrc, eq;
+    long long bfm_post = 0, brm_post = 0;  // the counts the reference adds to msh_*pts_post_
+    int nI = 0, nJ = 0;                    // the export header's nI_, nJ_
+    bool oob = false;                      // the walk used brm / work-array slots past their sizes
+};
+int triangle_lattice(const TriDump &t, bool visual, TriLattice &L, const char **err);
 struct BrmSink;    // an open response-bispectrum export file (bsa_brmfile.cu)
 
 // Sampled grid points of the E-form contraction: slot[i1 + nf i2] = row in sF / sR
@@ -102,7 +123,8 @@ struct Engine {
     bool msh_dev_expand = true; // bsa_gpu_setMesherExpansion: zone passes expanded on the device
     // Mesher controls (BsaLibData.F90:219-233, 273): delta validation, BFM multi-level
     // refinement, background peak restricted to the first direction, diagonal-crest scheme
-    bool validate_deltas = true, bfm_mlr = true, bkg_restrict = false, premesh_diag_crest = false;
+    bool validate_deltas = true, bfm_mlr = true, bkg_restrict = false, premesh_diag_crest = false,
+         premesh_mode_base = false;
     bsa_brm_export_fn export_fn = nullptr;  // bsa_setBispExportCallback
     void *export_user = nullptr;
     // bsa_enableVisualMode / bsa_setVisualIndexes / bsa_setBRMExportDefaultMode (bsa_brmfile.cu)
@@ -133,7 +155,7 @@ struct Engine {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr;
     DevBuf dL, dQ, dLogc, dPsdPar, dFrfM, dFrfK, dFrfC, dFreq, dS, dA, dPartF, dPartR, dOut, dPsdF, dWf, dPts,
         dPtsD, dBF, dBR, dMixA, dMixB, dMixH, dMixPart, dA32, dZones, dZidx, dWd3, dWd2, dMshT, dMshIdx, dLogc32, dL32,
-        dPod, dFlag, dSlot, dHash;
+        dPod, dFlag, dSlot, dHash, dCptr, dCq;
 
     // stats
     double last_ms = 0, last_ms_contraction = 0, last_ms_gemm = 0, last_points = 0;
@@ -174,16 +196,22 @@ struct Engine {
     int run_points(const double *fi, const double *fj, const double *w, double wuniform, long long npts,
                    double *m3mf, double *m3mr, double *bfm, double *brm,
                    const std::vector<ZoneDev> *zones = nullptr, const int *zid = nullptr, const int *zi = nullptr,
-                   const int *zj = nullptr);
+                   const int *zj = nullptr, const long long *cptr = nullptr, const double *cq = nullptr);
     int run_zones(const std::vector<ZoneDev> &zones, double *m3mf, double *m3mr, double *npts);
     int run_zones_fp64(const std::vector<ZoneDev> &zones, double *m3mf, double *m3mr, double *npts);
     int run_zones_mixed(const std::vector<ZoneDev> &zones, double *m3mf, double *m3mr, double *npts,
                         double *zdiag = nullptr);
     int msh_mixed_batch(const std::vector<ZoneDev> &zones, std::vector<double> &accF, std::vector<double> &accR,
                         float &ms_gemm, float &ms_all, double *zdiag);
-    int mesher_zones(std::vector<ZoneDev> &zones, std::vector<int> &policy);
+    // the pre-mesh layout: rectangles (zones, policy, whether the walk exchanges the start
+    // point's coordinates), triangles, and the dump order (k >= 0: rectangle k, k < 0:
+    // triangle -k - 1)
+    int mesher_zones(std::vector<ZoneDev> &zones, std::vector<int> &policy, std::vector<TriDump> *tris = nullptr,
+                     std::vector<int> *order = nullptr, std::vector<unsigned char> *swapped = nullptr);
     int run_mesher(double *m3mf, double *m3mr);
-    int zones_export(const std::vector<ZoneDev> &zones);
+    int run_triangles(const std::vector<TriDump> &tris, double *m3mf, double *m3mr, double *npts);
+    int zones_export(const std::vector<ZoneDev> &zones, const std::vector<TriDump> &tris, const std::vector<int> &order,
+                     const std::vector<unsigned char> &swapped);
     // response-bispectrum export files (bsa_brmfile.cu); emit_brm also feeds the callback
     bool brm_file_wanted(bool classic) const;
     int brm_file_open(bool classic, int nzones);

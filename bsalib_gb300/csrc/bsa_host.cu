@@ -151,6 +151,7 @@ void Engine::reset_inputs() {
     bfm_mlr = true;
     bkg_restrict = false;
     premesh_diag_crest = false;
+    premesh_mode_base = false;
 }
 
 void Engine::free_device() {
@@ -674,7 +675,7 @@ int Engine::contract(const PointSrc &ps, long long npts, double *m3mf, double *m
 // Point-set evaluation with analytic f1+f2 (Mesher functions and BsaCL semantics).
 int Engine::run_points(const double *fi, const double *fj, const double *w, double wuniform, long long npts,
                        double *m3mf, double *m3mr, double *bfm, double *brm, const std::vector<ZoneDev> *zones,
-                       const int *zid, const int *zi, const int *zj) {
+                       const int *zid, const int *zi, const int *zj, const long long *cptr, const double *cq) {
     kernels = 0;
     graph_launches = 0;
     h2d = d2h = 0;
@@ -743,6 +744,17 @@ int Engine::run_points(const double *fi, const double *fj, const double *w, doub
         ps.zid = dzid;
         ps.zi = dzi;
         ps.zj = dzj;
+    }
+    if (cptr) {
+        const size_t ne = (size_t)cptr[n];
+        if ((e = dCptr.reserve((n + 1) * sizeof(long long))) || (e = dCq.reserve((3 * ne + 1) * sizeof(double))))
+            return cuda_fail(e, "BRM point lists");
+        if ((e = cudaMemcpyAsync(dCptr.p, cptr, (n + 1) * sizeof(long long), cudaMemcpyHostToDevice, stream)) ||
+            (ne && (e = cudaMemcpyAsync(dCq.p, cq, 3 * ne * sizeof(double), cudaMemcpyHostToDevice, stream))))
+            return cuda_fail(e, "BRM point lists");
+        h2d += (double)(n + 1) * sizeof(long long) + 3.0 * ne * sizeof(double);
+        ps.cptr = dCptr.as<long long>();
+        ps.cq = dCq.as<double>();
     }
     // Mesher functions: the diagonal-only form is getFM_diag_tnm_scalar_msh_'s.
     rc = set.onlyd ? contract_diag(ps, npts, 1, m3mf, m3mr, bfm, brm) : contract(ps, npts, m3mf, m3mr, bfm, brm);
@@ -989,9 +1001,11 @@ int bsa_setPremeshScheme(int itype) {
     if (itype == 1) eng().premesh_diag_crest = true;
     return BSA_OK;
 }
+// bsa_setPremeshMode (BsaLibImpl.F90:813-826): 0 selects the base mode, any other value
+// leaves the mode as it is; the diagonal-crest scheme reads it (and refuses the base mode).
 int bsa_setPremeshMode(int imode) {
     GUARD();
-    (void)imode;  // read by the diagonal-crest scheme only
+    if (imode == 0) eng().premesh_mode_base = true;
     return BSA_OK;
 }
 int bsa_setWindDirections(const int *dirs, int ndirs) {

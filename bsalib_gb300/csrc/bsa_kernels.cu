@@ -331,6 +331,45 @@ __global__ __launch_bounds__(256) void k_bfm_fp64(const double *__restrict__ A,
             }
             __syncthreads();
         }
+        if (ps.cptr) {
+            // listed BRM points (triangular zones): G = sum_e c_e Re[H_m(w1_e) H_n(w2_e) conj H_o(w1_e + w2_e)]
+            double g[MT];
+#pragma unroll
+            for (int u = 0; u < MT; ++u) g[u] = 0.0;
+            const long long e1 = ps.cptr[p + 1];
+            for (long long e = ps.cptr[p]; e < e1; ++e) {
+                const double v1 = ps.cq[3 * e] * kPi2, v2 = ps.cq[3 * e + 1] * kPi2, ce = ps.cq[3 * e + 2];
+                if (t < nm) {
+                    frf_eval(frf.M[t], frf.K[t], frf.C[t], v1, Hs[2 * t], Hs[2 * t + 1]);
+                    frf_eval(frf.M[t], frf.K[t], frf.C[t], v2, Hs[2 * nm + 2 * t], Hs[2 * nm + 2 * t + 1]);
+                    frf_eval(frf.M[t], frf.K[t], frf.C[t], v1 + v2, Hs[4 * nm + 2 * t], Hs[4 * nm + 2 * t + 1]);
+                }
+                __syncthreads();
+                if (ok) {
+                    const double h2r = Hs[2 * nm + 2 * n], h2i = Hs[2 * nm + 2 * n + 1];
+                    const double h3r = Hs[4 * nm + 2 * o], h3i = Hs[4 * nm + 2 * o + 1];
+                    const double cr = h2r * h3r + h2i * h3i, ci = h2i * h3r - h2r * h3i;
+#pragma unroll
+                    for (int u = 0; u < MT; ++u) {
+                        const int m = mg + MG * u;
+                        if (m < nm) g[u] = fma(ce, Hs[2 * m] * cr - Hs[2 * m + 1] * ci, g[u]);
+                    }
+                }
+                __syncthreads();
+            }
+            if (ok) {
+#pragma unroll
+                for (int u = 0; u < MT; ++u) {
+                    const int m = mg + MG * u;
+                    if (m < nm) {
+                        const double bfv = 2.0 * acc[u];
+                        smf[u] = fma(w, bfv, smf[u]);
+                        smr[u] = fma(g[u], bfv, smr[u]);
+                    }
+                }
+            }
+            continue;
+        }
         if (ps.zones) {
             // Mesher zone point: the force bispectrum of this BFM lattice point enters every
             // BRM lattice point of its bilinear support with weight lambda; accumulate

@@ -1225,12 +1225,25 @@ int Engine::msh_mixed_batch(const std::vector<ZoneDev> &zs, std::vector<double> 
     const int nchunks = ML.groups(nm) * ML.nchj;
     // one wave of two resident blocks per SM where the element chunks allow it
     const int G = (int)std::max(1LL, std::min((long long)(2 * nsm) / nchunks, ncells));
-    if ((e = dMixA.reserve(2 * uel * 2)) || (e = dMixB.reserve(2 * (gel + sel) * 2)) ||
-        (e = dMshT.reserve(3 * tel * sizeof(float))) ||
-        (e = dMixPart.reserve((size_t)G * 6 * nm3 * sizeof(double) + 2 * (size_t)nm3 * sizeof(double) + 256)) ||
-        (e = dMixH.reserve((size_t)nbrm * hs * sizeof(float2) + (size_t)nbrm * sizeof(float) + 256 +
-                           (zdiag ? zm.size() * nm * sizeof(double) : 0))))
-        return cuda_fail(e, "allocating Mesher BF16x3 operands");
+    auto reserve_pass = [&]() -> cudaError_t {
+        cudaError_t r;
+        if ((r = dMixA.reserve(2 * uel * 2)) || (r = dMixB.reserve(2 * (gel + sel) * 2)) ||
+            (r = dMshT.reserve(3 * tel * sizeof(float))) ||
+            (r = dMixPart.reserve((size_t)G * 6 * nm3 * sizeof(double) + 2 * (size_t)nm3 * sizeof(double) + 256)) ||
+            (r = dMixH.reserve((size_t)nbrm * hs * sizeof(float2) + (size_t)nbrm * sizeof(float) + 256 +
+                               (zdiag ? zm.size() * nm * sizeof(double) : 0))))
+            return r;
+        return cudaSuccess;
+    };
+    if ((e = reserve_pass()) == cudaErrorMemoryAllocation) {
+        // each buffer keeps the largest size an earlier pass asked for, and passes that peak in
+        // different operands can hold more together than one pass needs: start over from empty
+        cudaGetLastError();
+        dMixA.release(); dMixB.release(); dMshT.release(); dMixPart.release(); dMixH.release();
+        release_device_cache();
+        e = reserve_pass();
+    }
+    if (e) return cuda_fail(e, "allocating Mesher BF16x3 operands");
     __nv_bfloat16 *Uh = dMixA.as<__nv_bfloat16>(), *Ul = Uh + uel;
     __nv_bfloat16 *Gh = dMixB.as<__nv_bfloat16>(), *Gl = Gh + gel, *Sh = Gl + gel, *Sl = Sh + sel;
     float *T1 = dMshT.as<float>(), *T3 = T1 + tel, *T2 = T3 + tel;

@@ -237,6 +237,22 @@ struct RZ {
         otherBase(pt, base_dir, coord_ty, coord);
         setDeltas(dfi, dfj);
     }
+    // defineFromEndPtCoordAndBase_norm(.., called): without called, the deltas follow from the
+    // refinements already set
+    void fromEndCoordAndBaseNorm(const Pt &Pi, double coord, char coord_ty, double base, char base_dir, bool called) {
+        I = Pi;
+        double ang;
+        if (base_dir == 'i') {
+            baseI = base;
+            ang = rot >= PIt3d2 ? rot - PIt3d2 : rot + PId2;
+        } else {
+            baseJ = base;
+            ang = rot;
+        }
+        const Pt pt = from_dist_rot(I, base, ang);
+        otherBase(pt, base_dir, coord_ty, coord);
+        if (!called) deduceDeltas();
+    }
     // defineFromDeltas_maxvalues(pt, 'i', dfi, dfj, maxF_i, maxF_j, force=.true.)
     void fromDeltasMax(const Pt &p, double dfi, double dfj, double mi, double mj) {
         if (!aligned()) throw Fail{"padding zone is not aligned with the frequency axes"};
@@ -269,28 +285,81 @@ struct RZ {
     Dumped dump() const { return Dumped{I, rot, baseI, baseJ, ni, nj, pol, id_im}; }
 };
 
-// MRectZone directions in the (f1, f2) plane of an axis-aligned zone: the I and J axes of
-// getUnaryDeltas with the frequency swap interpolateRZ_HTPC_v3 applies for rot in
-// [pi/2, pi) and [3 pi/2, 2 pi).
-void axes(double rot, double &Ii, double &Ij, double &Ji, double &Jj) {
+// MTriangZone_t (zones/MTriangZoneImpl.F90) with the state the pre-mesh reads and writes:
+// corner C, A at the end of the J side CA, B at the end of the I side CB.
+struct TZ {
+    Pt C, A, B;
+    double rot = 0.0;
+    int ni = 0, nj = 0, pol = kNull, id_im = 0;
+
+    void setRefinements(int n_i, int n_j, bool *sticky) {  // M2DPolygZone setRefinements, not forced
+        if (*sticky) {
+            ni = n_i;
+            nj = n_j;
+        } else {
+            ni = n_i % 2 == 0 ? n_i + 1 : n_i;
+            nj = n_j % 2 == 0 ? n_j + 1 : n_j;
+        }
+    }
+    // defineFromPts_norm (:275-346): which of P1, P2 is A, then deduceRotation (:157-198)
+    void define(const Pt &Cp, const Pt &P1, const Pt &P2) {
+        if (ni == 0 || nj == 0) throw Fail{"missing triangle refinement information"};
+        if (P1.fj > P2.fj || P1.fj < P2.fj) {
+            A = P1; B = P2;
+        } else if (P1.fj > Cp.fj) {
+            if (P1.fi < P2.fi) { A = P1; B = P2; }
+            else if (P2.fi < P1.fi) { A = P2; B = P1; }
+            else throw Fail{"triangle collapsed into a segment"};
+        } else if (P1.fj < Cp.fj) {
+            if (P1.fi > P2.fi) { A = P1; B = P2; }
+            else if (P2.fi > P1.fi) { A = P2; B = P1; }
+            else throw Fail{"triangle collapsed into a segment"};
+        } else {
+            throw Fail{"three triangle points on one line"};
+        }
+        C = Cp;
+        const double dx = A.fi - C.fi, dy = A.fj - C.fj;
+        double ang = std::atan(std::fabs(dx) / std::fabs(dy));
+        if (!(dx >= 0.0 && dy >= 0.0)) {
+            if (dy < 0.0)
+                ang = dx >= 0.0 ? PI - ang : PI + ang;
+            else
+                ang = ang > 1e-14 ? PIt2 - ang : 0.0;
+        }
+        rot = ang;
+    }
+    double baseI() const { return distance(C, B); }
+    double baseJ() const { return distance(C, A); }
+};
+
+// M2DPolygZone getUnaryDeltas (M2DPolygZone.F90:172-226): the unit steps along the zone's I
+// and J sides as the lattice walk adds them to (fi, fj).
+void unary_deltas(double rot, double &Ii, double &Ij, double &Ji, double &Jj) {
     if (rot < PId2) {
         const double c = std::cos(rot), s = std::sin(rot);
-        Ii = c; Ij = -s; Ji = s; Jj = c;
+        Ji = s; Jj = c; Ii = c; Ij = -s;
     } else if (rot < PI) {
         const double a = rot - PId2, c = std::cos(a), s = std::sin(a);
-        Ii = -s; Ij = -c; Ji = c; Jj = -s;
+        Ji = -s; Jj = c; Ii = -c; Ij = -s;
     } else if (rot < PIt3d2) {
         const double a = rot - PI, c = std::cos(a), s = std::sin(a);
-        Ii = -c; Ij = s; Ji = -s; Jj = -c;
+        Ji = -s; Jj = -c; Ii = -c; Ij = s;
     } else {
         const double a = rot - PIt3d2, c = std::cos(a), s = std::sin(a);
-        Ii = s; Ij = c; Ji = -c; Jj = s;
+        Ji = s; Jj = -c; Ii = c; Ij = s;
     }
 }
 
+// The lattice walks of compute_rz_ / compute_TZ_iso_ and of both interpolations start from the
+// zone's init point with its two coordinates exchanged when rot lies in [pi/2, pi) or
+// [3 pi/2, 2 pi) (_shared_poly2d.fi:196-212, 873-900), and write the exported BRM points with
+// the coordinates exchanged back (fi_ptr => fj).
+bool swaps_base(double rot) { return (rot >= PId2 && rot < PI) || (rot >= PIt3d2 && rot < PIt2); }
+
 }  // namespace premesh
 
-int Engine::mesher_zones(std::vector<ZoneDev> &zones, std::vector<int> &policy_out) {
+int Engine::mesher_zones(std::vector<ZoneDev> &zones, std::vector<int> &policy_out, std::vector<TriDump> *tris,
+                         std::vector<int> *order, std::vector<unsigned char> *swapped) {
     using namespace premesh;
     int rc = validate();
     if (rc) return rc;
@@ -300,8 +369,6 @@ int Engine::mesher_zones(std::vector<ZoneDev> &zones, std::vector<int> &policy_o
     const bool half = set.bispsym == 2;
     const double isym = set.bispsym == 0 ? 1.0 : (double)set.bispsym;
     bool sticky = false;  // setRefinements' saved force flag
-    if (premesh_diag_crest)
-        return fail(BSA_ERR_UNSUPPORTED, "the pre-mesh scheme with diagonal crests (triangular zones) is not on this path");
     if (!in.natf || !in.xsi) return fail(BSA_ERR_STATE, "natural frequencies / damping not set");
     if (!in.ubref) return fail(BSA_ERR_STATE, "zone mean wind speeds not set");
     // bkg_peak_width_(i, j) = 1 / max_z L(i, j, z) / U(z) (computeBKGPeakWidths,
@@ -395,12 +462,23 @@ int Engine::mesher_zones(std::vector<ZoneDev> &zones, std::vector<int> &policy_o
 
     // ---- pre-mesh ----
     std::vector<Dumped> dz;
+    std::vector<TZ> dt;
+    std::vector<int> seq;  // dump order: k >= 0 rectangle k, k < 0 triangle -k - 1
     // compute_rz_ (_shared_poly2d.fi:76-88, 433-449): a zone with a side of zero length is
     // skipped (not dumped); a zero delta aborts the reference
     auto emit = [&](const RZ &z) {
         if (z.baseI <= MACHINE_PRECISION || z.baseJ <= MACHINE_PRECISION) return;
         if (z.dI <= MACHINE_PRECISION || z.dJ <= MACHINE_PRECISION) throw Fail{"a zone delta is zero"};
+        seq.push_back((int)dz.size());
         dz.push_back(z.dump());
+    };
+    // MTriangZone compute (MTriangZoneImpl.F90:489-510, _shared_poly2d.fi:78-80): isosceles,
+    // equal refinements, or the reference aborts
+    auto emit_tri = [&](const TZ &t) {
+        if (!(std::fabs(t.baseJ() - t.baseI()) <= MACHINE_PRECISION)) throw Fail{"triangle must be isosceles"};
+        if (t.ni != t.nj) throw Fail{"different triangle side refinements not allowed"};
+        seq.push_back(-(int)dt.size() - 1);
+        dt.push_back(t);
     };
     RZ bkgz;
     const double base_j = base_i;
@@ -487,8 +565,92 @@ int Engine::mesher_zones(std::vector<ZoneDev> &zones, std::vector<int> &policy_o
                 emit(rz);
             }
             imz[NLimsP1] = id_im_last;
+            if (premesh_diag_crest) {
+                // diagonal-crest scheme (BsaMesherImpl.F90:924-1279): an internal padding
+                // rectangle over the NE (and SW) quadrant, and along the SE (and NW) diagonal
+                // crest a triangle at the background zone's corner, then per zone limit a
+                // rotated crest rectangle, two levelling triangles and two closing rectangles,
+                // and a closing triangle at the far corner
+                if (premesh_mode_base) throw Fail{"the BASE pre-mesh mode is not implemented by the reference"};
+                const int ndiag = half ? 1 : 2;
+                {
+                    const Policy P = premesh::policy(kPadIntern);
+                    for (int idir = 1; idir <= ndiag; ++idir) {
+                        RZ rz;  // a copy of the master's zone object, interest-mode pointer 0
+                        rz.setRotation(ROT[2 * idir]);
+                        rz.pol = kPadIntern;
+                        const double r = LSIGN[2 * idir] * maxF;
+                        rz.fromDeltasMax(basePts[2 * idir], df_I_ref * P.dfI, df_J_ref * P.dfJ, r, r);
+                        emit(rz);
+                    }
+                }
+                Pt bpd[5] = {Pt{}, basePts[3], basePts[1], basePts[3], basePts[4]};
+                const double trots[3] = {0.0, PId2 + PI / 4.0, PIt3d2 + PI / 4.0};
+                for (int idir = 1; idir <= ndiag; ++idir) {
+                    const int S = LSIGN[2 * idir];
+                    const double tdel = dS2_2 * S;
+                    TZ tz;
+                    const double limI = bpd[idir].fi, limJ = bpd[idir].fj;
+                    Pt ptI{limI + tdel, limJ}, ptA{limI, limJ - tdel};
+                    tz.id_im = 1;
+                    tz.setRefinements(bkgz.ni, bkgz.nj, &sticky);
+                    tz.pol = kPeak;
+                    tz.define(bpd[idir], ptI, ptA);
+                    emit_tri(tz);
+                    const double trot = trots[idir];
+                    int k0 = 1;  // limits the first triangle covers (one count per direction loop)
+                    while (std::fabs(ptI.fi) > lim[k0] && k0 <= NLims) ++k0;
+                    const bool warn = k0 == NLims + 1;
+                    const double rvals[2] = {trot - trots[1], trot + trots[1]};
+                    int idrot = 0;
+                    RZ rz;
+                    int iim = 1;
+                    for (int ilim = k0; ilim <= NLimsP1; ++ilim) {
+                        const double l = lim[ilim];
+                        rz.setRefinements(bkgz.ni, ref2[ilim], false, &sticky);
+                        rz.id_im = iim;
+                        rz.setRotation(trot);
+                        rz.pol = pol[ilim];
+                        rz.fromEndCoordAndBaseNorm(ptI, -l * S, 'j', base_ib, 'i', false);
+                        emit(rz);
+                        ptA = rz.getA();
+                        const Pt ptB = rz.getB(), ptE = rz.E;
+                        const int pl = pol[ilim] == kPeak ? kCrest : kBasin;
+                        tz.id_im = iim;
+                        const int nim = IM[iim];
+                        iim += nim < 0 ? 1 : nim + 1;
+                        ptI = Pt{l * S, rz.I.fj};
+                        tz.setRefinements(rz.nj, rz.nj, &sticky);
+                        tz.pol = pl;
+                        tz.define(ptI, ptA, rz.I);
+                        emit_tri(tz);
+                        const double rtmp = tz.baseI();
+                        const Policy dP = premesh::policy(pl);
+                        rz.setRotation(rvals[idrot++ % 2]);
+                        rz.pol = pl;
+                        rz.fromEndCoordAndBase(Pt(rz.I), limJ, 'j', rtmp, 'i', dlt2[ilim] * dP.dfI, dlt2[ilim] * dP.dfJ);
+                        emit(rz);
+                        ptI = Pt{ptB.fi, -l * S};
+                        tz.define(ptI, ptB, ptE);
+                        emit_tri(tz);
+                        rz.setRotation(rvals[idrot++ % 2]);
+                        rz.fromEndCoordAndBase(Pt(tz.C), limI, 'i', rtmp, 'i', dlt2[ilim] * dP.dfI, dlt2[ilim] * dP.dfJ);
+                        emit(rz);
+                        ptI = ptA;
+                    }
+                    if (!warn) {  // closing triangle
+                        const Policy dP = premesh::policy(kPeak);
+                        tz.id_im = id_im_last;
+                        tz.pol = kPeak;
+                        tz.setRefinements(set.bkgrfmt * dP.dfI, set.bkgrfmt * dP.dfJ, &sticky);
+                        const Pt c{maxF * S, -maxF * S};
+                        tz.define(c, Pt{c.fi - dS2_2 * S, c.fj}, Pt{c.fi, c.fj + dS2_2 * S});
+                        emit_tri(tz);
+                    }
+                }
+            }
             // quadrants (scheme without diagonal crests, BsaMesherImpl.F90:743-920)
-            {
+            if (!premesh_diag_crest) {
                 const Pt p1 = basePts[1];
                 basePts[1] = basePts[2]; basePts[2] = basePts[3]; basePts[3] = basePts[4]; basePts[4] = p1;
                 const double init_freq = basePts[1].fi;
@@ -554,6 +716,7 @@ int Engine::mesher_zones(std::vector<ZoneDev> &zones, std::vector<int> &policy_o
     // ---- post-mesh lattice of every zone (interpolateRZ_HTPC_v3, _shared_poly2d.fi:588-870) ----
     zones.clear();
     policy_out.clear();
+    if (swapped) swapped->clear();
     for (const Dumped &d : dz) {
         if (d.ni < 2 || d.nj < 2) return fail(BSA_ERR_ARG, "zone with fewer than 2 lattice points per side");
         const double dI0 = d.baseI / (d.ni - 1), dJ0 = d.baseJ / (d.nj - 1);  // setRefinements(.., force)
@@ -563,13 +726,14 @@ int Engine::mesher_zones(std::vector<ZoneDev> &zones, std::vector<int> &policy_o
             P.bfm_i = 1;
             P.bfm_j = 1;
         }
+        if (visual) P.nlevs = 0;  // the visual mode interpolates the BFM lattice as dumped
         int si = 1, sj = 1;
         for (int l = 0; l < P.nlevs; ++l) {
             si *= P.bfm_i;
             sj *= P.bfm_j;
         }
         double dIr = dI0 / si, dJr = dJ0 / sj;
-        if (validate_deltas) {
+        if (validate_deltas && !visual) {
             int idx = d.id_im == 0 ? 1 : d.id_im;
             int nim = IM.size() > (size_t)idx ? IM[idx] : 0;
             double dwI;
@@ -593,10 +757,11 @@ int Engine::mesher_zones(std::vector<ZoneDev> &zones, std::vector<int> &policy_o
             }
         }
         double Ii, Ij, Ji, Jj;
-        axes(d.rot, Ii, Ij, Ji, Jj);
+        unary_deltas(d.rot, Ii, Ij, Ji, Jj);
+        const bool sw = swaps_base(d.rot);
         ZoneDev z{};
-        z.fi0 = d.I.fi;
-        z.fj0 = d.I.fj;
+        z.fi0 = sw ? d.I.fj : d.I.fi;
+        z.fj0 = sw ? d.I.fi : d.I.fj;
         z.dIi = Ii * dIr; z.dIj = Ij * dIr;
         z.dJi = Ji * dJr; z.dJj = Jj * dJr;
         z.ni = (d.ni - 1) * si + 1;
@@ -608,7 +773,32 @@ int Engine::mesher_zones(std::vector<ZoneDev> &zones, std::vector<int> &policy_o
         z.sym = isym;  // m3 += intg * i_bisp_sym_ (_shared_poly2d.fi:2117-2119)
         zones.push_back(z);
         policy_out.push_back(d.pol);
+        if (swapped) swapped->push_back(sw ? 1 : 0);
     }
+    // triangles: the policy's factors for the post-mesh walk (interpolateTZ_HTPC_v3 has no
+    // delta validation); the walk itself is bsa_triang.cu's
+    if (tris) {
+        tris->clear();
+        for (const TZ &t : dt) {
+            Policy P = premesh::policy(t.pol);
+            if (!bfm_mlr) {
+                P.nlevs = 0;
+                P.bfm_i = 1;
+                P.bfm_j = 1;
+            }
+            TriDump d;
+            d.Ci = t.C.fi; d.Cj = t.C.fj; d.Ai = t.A.fi; d.Aj = t.A.fj; d.Bi = t.B.fi; d.Bj = t.B.fj;
+            d.rot = t.rot;
+            d.sym = isym;
+            d.n = t.ni;
+            d.pol = t.pol;
+            d.bfi = P.bfm_i; d.bfj = P.bfm_j; d.bri = P.brm_i; d.brj = P.brm_j; d.nlevs = P.nlevs;
+            tris->push_back(d);
+        }
+    } else if (!dt.empty()) {
+        return fail(BSA_ERR_UNSUPPORTED, "this entry takes rectangular zones only; the layout has triangles");
+    }
+    if (order) *order = seq;
     return BSA_OK;
 }
 

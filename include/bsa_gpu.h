@@ -374,10 +374,47 @@ int bsa_mlp_train(int h, const float *x, const float *y, const float *sw, int n,
 const char *bsa_mlp_lastError(void);
 
 /* The zone layout the Mesher analysis (bsa_Run with analysis type 2) evaluates: restates
- * prefetchZoneLimits_ (BsaMesherImpl.F90:1638-1859) and the background peak zone of
- * PreMesh (:266-420), and lays rectangular zones over those limits on both axes.  Writes
- * at most cap zones, *nz receives the full count. */
+ * prefetchZoneLimits_ (BsaMesherImpl.F90:1638-1859) and PreMesh (:266-1393) in the scheme
+ * bsa_setPremeshScheme selected, and returns its rectangular zones as the lattices the walk
+ * evaluates (for rotations in [pi/2, pi) and [3 pi/2, 2 pi) the walk starts from the init
+ * point with its coordinates exchanged, _shared_poly2d.fi:196-212, 873-900).  Writes at most
+ * cap zones, *nz receives the full count.  The diagonal-crest scheme also lays triangles:
+ * bsa_gpu_mshGenerateTriangles. */
 int bsa_gpu_mshGenerateZones(bsa_zone *zones, int cap, int *nz);
+
+/* A triangular Mesher zone (MTriangZone_t, src/bsa/meshing/zones/MTriangZoneImpl.F90) as
+ * dumpTZ / DumpZone record it: corner C, A at the end of the J side CA, B, rotation rot (of CA
+ * from the +f2 axis), refinements ni = nj = n; its policy's factors (BFM refinement i / j and
+ * levels, after bsa_setBfmMLR; BRM factors) and the spatial-symmetry weight; seq is its
+ * position in the layout's dump order (rectangles fill the other positions in order). */
+typedef struct {
+    double Ci, Cj, Ai, Aj, Bi, Bj;
+    double rot, sym;
+    int n, policy;
+    int bfm_i, bfm_j, bfm_levels, brm_i, brm_j;
+    int seq;
+} bsa_triangle;
+
+/* The triangles of the Mesher layout (the diagonal-crest scheme's only).  Writes at most cap
+ * triangles, *nt receives the full count. */
+int bsa_gpu_mshGenerateTriangles(bsa_triangle *tris, int cap, int *nt);
+
+/* Third moments over a list of triangles (interpolateTZ_HTPC_v3, _shared_poly2d.fi:470-2166):
+ * the BFM at every BFM point of each triangle's post-mesh lattice in one FP64 device pass, the
+ * BRM points each feeds, with their weights and interpolation shares, in its epilogue.  npts
+ * (optional, 2 doubles): BFM and BRM point counts. */
+int bsa_gpu_mshTriangles(const bsa_triangle *tris, int nt, double *m3mf, double *m3mr, double *npts);
+
+/* The post-mesh lattice of one triangle, host only (what bsa_gpu_mshTriangles evaluates):
+ * counts[6] = BFM points, BRM points, interpolation terms, export records, and the point
+ * counts the reference adds to msh_bfmpts_post_ / msh_brmpts_post_; *oob = 1 where the
+ * reference's walk indexes its work arrays past their sizes.  Arrays (each may be NULL):
+ * bfm[3 * nb] (f1, f2, m3mf weight without sym), brm[3 * nq] (f1, f2, m3mr weight), qptr[nq + 1],
+ * qsrc[nnz], qc[nnz] (BRM point r interpolates sum_k qc[k] BFM(qsrc[k]), k in
+ * [qptr[r], qptr[r + 1])), exp[2 * ne] (written f1, f2), eq[ne] (BRM point, -1 for zero);
+ * visual != 0: the lattice of the visual mode (no BFM refinement). */
+int bsa_gpu_mshTriangLattice(const bsa_triangle *t, int visual, long long *counts, int *oob, double *bfm,
+                             double *brm, int *qptr, int *qsrc, double *qc, double *exp, int *eq);
 
 /* Timing and counters of the last run. */
 typedef struct {

@@ -158,6 +158,27 @@ class Rect:
         self.other_base(new_point(self.I, base, ang), base_dir, coord_ty, coord)
         self.set_deltas_adapt(dfi, dfj)
 
+    def set_rotation(self, r):
+        """M2DPolygZone setRotation: r in [0, 2 pi)."""
+        if r >= PIt2:
+            r -= math.floor(r / PIt2) * PIt2
+        self.rot = r
+
+    def from_end_coord_base_norm(self, p, coord, coord_ty, base, base_dir, called):
+        """defineFromEndPtCoordAndBase_norm: with called false the deltas follow from the
+        refinements already set (deduceDeltas)."""
+        self.I = p
+        if base_dir == "i":
+            self.bI = base
+            ang = self.rot - PIt3d2 if self.rot >= PIt3d2 else self.rot + PId2
+        else:
+            self.bJ = base
+            ang = self.rot
+        self.other_base(new_point(self.I, base, ang), base_dir, coord_ty, coord)
+        if not called:
+            self.dI = self.bI / (self.ni - 1)
+            self.dJ = self.bJ / (self.nj - 1)
+
     def from_deltas_max(self, p, dfi, dfj, mi, mj):
         fi, fj = p
         r = self.rot
@@ -240,9 +261,13 @@ def zone_limits(modes, natf, xsi, peak_area_ext, bpw2):
 
 
 def layout(modes, natf, xsi, L, ubref, bkgrfmt, bkgaext, peak_area_ext, maxaext, fcov=1,
-           validate=True, mlr=True, restrict=False, bispsym=0):
-    """Zones of the Mesher analysis, as (fi0, fj0, dIi, dIj, dJi, dJj, ni, nj, Fi, Fj, policy).
-    L: turbulence length scales (3, 3, nz) column-major flattened; ubref: zone mean speeds."""
+           validate=True, mlr=True, restrict=False, bispsym=0, diag=False, mode_base=False, visual=False):
+    """Zones of the Mesher analysis in dump order: rectangles as (fi0, fj0, dIi, dIj, dJi, dJj,
+    ni, nj, Fi, Fj, policy, sym), the lattice the walk evaluates; with diag (the diagonal-crest
+    scheme) also triangles, as dicts (C, A, B, rot, n, pol, sym and the policy's BFM / BRM
+    factors).  L: turbulence length scales (3, 3, nz) column-major flattened; ubref: zone mean
+    speeds.  A condition the reference aborts on raises AssertionError or TriError."""
+    from .triang import Tri
     nz = len(ubref)
     bkgw = 0.0
     for j in range(1 if restrict else 3):
@@ -323,11 +348,97 @@ def layout(modes, natf, xsi, L, ubref, bkgrfmt, bkgaext, peak_area_ext, maxaext,
                 refm[P1], dlt[P1] = (rz.ni, rz.nj), (rz.dI, rz.dJ)
             emit(rz)
         izm[P1] = last
+        if diag:                                                # BsaMesherImpl.F90:924-1279
+            assert not mode_base, "BASE pre mesh mode not yet implemented"
+            dS2_2 = 2.0 * d2
+
+            def emit_tri(t):  # compute: isosceles, equal refinements
+                t.check_compute()
+                dumped.append(dict(tri=True, C=t.C, A=t.A, B=t.B, rot=t.rot, ni=t.ni, nj=t.nj, pol=t.pol,
+                                   im=t.im))
+
+            P = POLICY[PADI]
+            for d in range(1, 2 if half else 3):               # internal padding NE (, SW)
+                rz = Rect()
+                rz.im = 0
+                rz.set_rotation(ROT[2 * d])
+                rz.pol = PADI
+                r = SGN[2 * d] * maxF
+                rz.from_deltas_max(base_pts[2 * d], dfI0 * P[0], dfJ0 * P[1], r, r)
+                emit(rz)
+            bpd = list(base_pts)
+            bpd[2] = bpd[1]
+            bpd[1] = bpd[3]
+            trots = [None, PId2 + PI / 4.0, PIt3d2 + PI / 4.0]
+            for d in range(1, 2 if half else 3):               # diagonal crests SE (, NW)
+                S = SGN[2 * d]
+                tdel = dS2_2 * S
+                tz = Tri()
+                limI, limJ = bpd[d]
+                ptI = (limI + tdel, limJ)
+                ptA = (limI, limJ - tdel)
+                tz.im = 1
+                tz.set_refinements(bkg.ni, bkg.nj, False, sticky)
+                tz.pol = PEAK
+                tz.define(bpd[d], ptI, ptA)
+                emit_tri(tz)
+                trot = trots[d]
+                k0 = 1
+                while abs(ptI[0]) > lim[k0] and k0 <= NL:
+                    k0 += 1
+                warn = k0 == NL + 1
+                vals = [trot - trots[1], trot + trots[1]]
+                rots = [vals[i % 2] for i in range(2 * P1)]
+                idrot = 0
+                rz = Rect()
+                rz.im = 0
+                iim = 1
+                for k in range(k0, P1 + 1):
+                    lk = lim[k]
+                    rz.set_refinements(bkg.ni, refm[k][1], False, sticky)
+                    rz.im = iim
+                    rz.set_rotation(trot)
+                    rz.pol = pol[k]
+                    rz.from_end_coord_base_norm(ptI, -lk * S, "j", base_b, "i", False)
+                    emit(rz)
+                    ptA, ptB, ptE = rz.a_point(), rz.b_point(), rz.E
+                    pl = CREST if pol[k] == PEAK else BASIN
+                    tz.im = iim
+                    n = im[iim]
+                    iim += 1 if n < 0 else n + 1
+                    ptI = (lk * S, rz.I[1])
+                    tz.set_refinements(rz.nj, rz.nj, False, sticky)
+                    tz.pol = pl
+                    tz.define(ptI, ptA, rz.I)
+                    emit_tri(tz)
+                    rtmp = tz.base_i()
+                    rz.set_rotation(rots[idrot])
+                    idrot += 1
+                    rz.pol = pl
+                    dP = POLICY[pl]
+                    rz.from_end_coord_base(rz.I, limJ, "j", rtmp, "i", dlt[k][1] * dP[0], dlt[k][1] * dP[1])
+                    emit(rz)
+                    ptI = (ptB[0], -lk * S)
+                    tz.define(ptI, ptB, ptE)
+                    emit_tri(tz)
+                    rz.set_rotation(rots[idrot])
+                    idrot += 1
+                    rz.from_end_coord_base(tz.C, limI, "i", rtmp, "i", dlt[k][1] * dP[0], dlt[k][1] * dP[1])
+                    emit(rz)
+                    ptI = ptA
+                if not warn:                                    # closing triangle
+                    tz.im = last
+                    tz.pol = PEAK
+                    dP = POLICY[PEAK]
+                    tz.set_refinements(bkgrfmt * dP[0], bkgrfmt * dP[1], False, sticky)
+                    ptI = (maxF * S, -maxF * S)
+                    tz.define(ptI, (ptI[0] - dS2_2 * S, ptI[1]), (ptI[0], ptI[1] + dS2_2 * S))
+                    emit_tri(tz)
         bp = [None, base_pts[2], base_pts[3], base_pts[4], base_pts[1]]    # quadrants
         init = bp[1][0]
         mrefs = max(refm[1])
         bch = [None, "i", "j", "i", "j"]
-        for d in range(1, 3 if half else 5):                   # quadrants
+        for d in range(1, (3 if half else 5) if not diag else 1):  # quadrants
             rz = Rect()
             rz.rot = ROT[d + 1]
             rz.pol = pol[1]
@@ -366,13 +477,22 @@ def layout(modes, natf, xsi, L, ubref, bkgrfmt, bkgaext, peak_area_ext, maxaext,
                 emit(rz)
     out = []
     for z in dumped:                                            # post-mesh lattices
+        if z.get("tri"):                                        # interpolateTZ_HTPC_v3 (triang.py)
+            _, _, bi, bj, ri, rj, lv = POLICY[z["pol"]]
+            if not mlr:
+                lv, bi, bj = 0, 1, 1
+            out.append(dict(tri=True, C=z["C"], A=z["A"], B=z["B"], rot=z["rot"], ni=z["ni"], nj=z["nj"],
+                            pol=z["pol"], sym=isym, bfi=bi, bfj=bj, bri=ri, brj=rj, nlevs=lv))
+            continue
         dI0, dJ0 = z["bI"] / (z["ni"] - 1), z["bJ"] / (z["nj"] - 1)
         dfi, dfj, bi, bj, ri, rj, lv = POLICY[z["pol"]]
         if not mlr:
             lv, bi, bj = 0, 1, 1
+        if visual:
+            lv = 0
         si, sj = bi ** lv, bj ** lv
         dIr, dJr = dI0 / si, dJ0 / sj
-        if validate:
+        if validate and not visual:
             idx = z["im"] or 1
             n = im[idx] if im is not None else 0
             if n == PRE_OK:
@@ -381,7 +501,7 @@ def layout(modes, natf, xsi, L, ubref, bkgrfmt, bkgaext, peak_area_ext, maxaext,
                 if n < 0:
                     idx += 1
                     n = im[idx]
-                dw = min(peak_ext[m] for m in im[idx + 1: idx + n + 1])
+                dw = min((peak_ext[m] for m in im[idx + 1: idx + n + 1]), default=math.inf) if im else math.inf
             if dIr > dw / bi:
                 while dIr > dw / bi:
                     si += 1
@@ -398,6 +518,8 @@ def layout(modes, natf, xsi, L, ubref, bkgrfmt, bkgaext, peak_area_ext, maxaext,
                 while dJr < dw / bj and sj > 1:
                     sj -= 1
                     dJr = dJ0 / sj
+        # getUnaryDeltas (M2DPolygZone.F90:172-226) from the init point, its coordinates
+        # exchanged for rot in [pi/2, pi) and [3 pi/2, 2 pi) (_shared_poly2d.fi:873-900)
         r = z["rot"]
         if r < PId2:
             c, s = math.cos(r), math.sin(r)
@@ -405,7 +527,7 @@ def layout(modes, natf, xsi, L, ubref, bkgrfmt, bkgaext, peak_area_ext, maxaext,
         elif r < PI:
             a = r - PId2
             c, s = math.cos(a), math.sin(a)
-            ax = (-s, -c, c, -s)
+            ax = (-c, -s, -s, c)
         elif r < PIt3d2:
             a = r - PI
             c, s = math.cos(a), math.sin(a)
@@ -413,16 +535,29 @@ def layout(modes, natf, xsi, L, ubref, bkgrfmt, bkgaext, peak_area_ext, maxaext,
         else:
             a = r - PIt3d2
             c, s = math.cos(a), math.sin(a)
-            ax = (s, c, -c, s)
-        out.append((z["I"][0], z["I"][1], ax[0] * dIr, ax[1] * dIr, ax[2] * dJr, ax[3] * dJr,
+            ax = (c, s, s, -c)
+        f0 = (z["I"][1], z["I"][0]) if (PId2 <= r < PI or PIt3d2 <= r < PIt2) else z["I"]
+        out.append((f0[0], f0[1], ax[0] * dIr, ax[1] * dIr, ax[2] * dJr, ax[3] * dJr,
                     (z["ni"] - 1) * si + 1, (z["nj"] - 1) * sj + 1, ri, rj, z["pol"], isym))
     return out
 
 
-def layout_for(prob, modes, validate=True, mlr=True, restrict=False):  # spatial symmetry: prob.settings.bispsym
-    """layout() for a bsalib_gb300 Problem and its kept modes (1-based)."""
+def unmirror(z):
+    """The geometric zone of an evaluated rectangle (the walk of a zone with rot in [pi/2, pi)
+    or [3 pi/2, 2 pi) evaluates the mirror image of the zone through f1 = f2, whose lattice has
+    the opposite orientation)."""
+    fi0, fj0, dIi, dIj, dJi, dJj = z[:6]
+    if dIi * dJj - dIj * dJi < 0.0:
+        return (fj0, fi0, dIj, dIi, dJj, dJi) + tuple(z[6:])
+    return tuple(z)
+
+
+def layout_for(prob, modes, validate=True, mlr=True, restrict=False, diag=False, mode_base=False, visual=False):
+    """layout() for a bsalib_gb300 Problem and its kept modes (1-based); spatial symmetry from
+    prob.settings.bispsym."""
     import numpy as np
     s = prob.settings
     return layout([int(m) for m in modes], list(prob.natf), list(prob.xsi),
                   list(np.asarray(prob.L, dtype=float).reshape(-1, order="F")), list(prob.UBref), s.bkgrfmt,
-                  s.bkgaext, s.genpaext, s.maxaext, s.fcov, validate, mlr, restrict, s.bispsym)
+                  s.bkgaext, s.genpaext, s.maxaext, s.fcov, validate, mlr, restrict, s.bispsym, diag, mode_base,
+                  visual)

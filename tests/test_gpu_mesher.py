@@ -199,7 +199,8 @@ def test_mesher_export(bsalib, prec, tol):
     lattice point (i fastest, then j) with the bilinear interpolation of the zone's BFM lattice
     times the FRF product.  At the BFM lattice points it equals the point bispectra; summed
     with the zone integration weights it gives the analysis' m3mr (FP64 export; the analysis
-    in the selected precision)."""
+    in the selected precision).  A zone whose walk exchanges its start point's coordinates
+    (its evaluated lattice has negative orientation) is written with the exchange undone."""
     prob = cantilever_tower(nodes=5)
     prob.settings.suban = 2
     prob.settings.bkgrfmt = 6
@@ -220,6 +221,8 @@ def test_mesher_export(bsalib, prec, tol):
             qi, qj = np.meshgrid(np.arange(NI), np.arange(NJ))  # qi fastest
             qi, qj = qi.ravel(), qj.ravel()
             a, c = qi / z.Fi, qj / z.Fj
+            if z.dIi * z.dJj - z.dIj * z.dJi < 0.0:
+                f1, f2 = f2, f1                        # back to the evaluated coordinates
             np.testing.assert_allclose(f1, z.fi0 + a * z.dIi + c * z.dJi, rtol=0, atol=1e-12)
             np.testing.assert_allclose(f2, z.fj0 + a * z.dIj + c * z.dJj, rtol=0, atol=1e-12)
             ti = np.where((qi == 0) | (qi == NI - 1), 0.5, 1.0)

@@ -6,11 +6,11 @@ import pytest
 
 from bsalib_gb300.problem import bridge_deck, cantilever_tower, random_structure, tall_building
 from oracle.oracle import Oracle
-from oracle.premesh import layout_for, zone_limits
+from oracle.premesh import layout_for, unmirror, zone_limits
 
 
 def corners(z):
-    fi0, fj0, dIi, dIj, dJi, dJj, ni, nj = z[:8]
+    fi0, fj0, dIi, dIj, dJi, dJj, ni, nj = unmirror(z)[:8]
     a = np.array([fi0, fj0])
     u = np.array([dIi, dIj]) * (ni - 1)
     v = np.array([dJi, dJj]) * (nj - 1)
