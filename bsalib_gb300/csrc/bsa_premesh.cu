@@ -1,11 +1,13 @@
 // bsa_premesh.cu -- the Mesher's zone layout (pre-mesh) and each zone's post-mesh lattice,
 // restated from BsaLib so that the Mesher evaluates the reference's zones.
 //
-// Pre-mesh (PreMesh, src/bsa/meshing/BsaMesherImpl.F90:266-1393, the default scheme without
-// diagonal crests): the background peak zone centred at the origin, the four crest bands along
-// the axes (one zone per zone limit and a closing one), the four quadrants as nested L-shapes
-// (a diagonal square and two side strips per limit) and, with full coverage, four external
-// padding bands up to max(natf) * max_area_ext.  Zone limits, policies and interest modes come
+// Pre-mesh (PreMesh, src/bsa/meshing/BsaMesherImpl.F90:266-1393): the background peak zone
+// centred at the origin, the four crest bands along the axes (one zone per zone limit and a
+// closing one), then in the default scheme the four quadrants as nested L-shapes (a diagonal
+// square and two side strips per limit), in the diagonal-crest scheme (bsa_setPremeshScheme(1),
+// :924-1279) padding rectangles over the NE / SW quadrants and triangles and rotated rectangles
+// along the SE / NW diagonals (MTriangZone, zones/MTriangZoneImpl.F90), and, with full
+// coverage, four external padding bands up to max(natf) * max_area_ext.  Zone limits, policies and interest modes come
 // from prefetchZoneLimits_ (:1638-1859) over the peak extensions of
 // getActualPeakZoneExtensionLimits_ (:1864-1890).  The geometry follows MRectZone
 // (zones/MRectZoneImpl.F90), M2DPolygZone (zones/M2DPolygZone.F90) and MPoint
@@ -17,8 +19,11 @@
 // point, rotation, bases, refinements, policy, interest-mode pointer) gets its deltas back from
 // bases / (n - 1), its BFM lattice refined by the policy's BFM factors (multi-level
 // refinement, bsa_setBfmMLR) and, with bsa_doValidateZoneDeltas, re-refined until its step
-// resolves the narrowest peak of its interest modes; the BRM lattice refines the BFM one by the
-// policy's BRM factors.  The result is the device zone record the integration kernels read.
+// resolves the narrowest peak of its interest modes (neither in visual mode); the BRM lattice
+// refines the BFM one by the policy's BRM factors.  The result is the device zone record the
+// integration kernels read: the lattice the walk evaluates, from the init point with its
+// coordinates exchanged for rot in [pi/2, pi) and [3 pi/2, 2 pi).  Triangles leave as their
+// dump with the policy's factors; their walk is bsa_triang.cu's.
 //
 // Settings of the reference's standalone driver (app/bsa.F90:544-552) differ from the library
 // defaults used here: bsa_loadInputFiles applies the driver's (no delta validation, no BFM

@@ -5,16 +5,19 @@ library's (bsalib_gb300/csrc/bsa_premesh.cu) zone by zone:
 
 * limits, policies and interest modes: prefetchZoneLimits_ and
   getActualPeakZoneExtensionLimits_ (src/bsa/meshing/BsaMesherImpl.F90:1638-1890);
-* zones: PreMesh (:266-1393, scheme without diagonal crests): background peak zone, crest
-  bands (:450-730), quadrants (:743-920), external padding (:1286-1350);
+* zones: PreMesh (:266-1393): background peak zone, crest bands (:450-730), quadrants
+  (:743-920) or, in the diagonal-crest scheme, padding rectangles, triangles and rotated
+  rectangles along the diagonals (:924-1279; triangle geometry in triang.py), external padding
+  (:1286-1350);
 * rectangle geometry: MRectZone (zones/MRectZoneImpl.F90: define, setIEpts, getOtherBase,
   defineFromEndPtCoordAndBase, defineFromDeltas_maxvalues, setDeltas / deduceRefinements,
   deduceDeltas), M2DPolygZone (setRefinements, getUnaryDeltas), MPoint
   (getNewPointFromDistAndRot), MPolicy_fromID (policy/MPolicy.F90:130-168);
 * post-mesh refinement of every zone: interpolateRZ_HTPC_v3 (zones/_shared_poly2d.fi:588-870).
 
-Each zone comes out as (fi0, fj0, dIi, dIj, dJi, dJj, ni, nj, Fi, Fj, policy, sym), the lattice
-the integration evaluates and its weight (i_bisp_sym_: 1 without spatial symmetry, 2 for HALF,
+Each rectangle comes out as (fi0, fj0, dIi, dIj, dJi, dJj, ni, nj, Fi, Fj, policy, sym), the
+lattice the integration evaluates (walked from the init point with its coordinates exchanged
+for rot in [pi/2, pi) and [3 pi/2, 2 pi), _shared_poly2d.fi:873-900) and its weight (i_bisp_sym_: 1 without spatial symmetry, 2 for HALF,
 whose layout covers f1 >= 0, 4 for FOURTH, whose layout is the whole plane).
 """
 from __future__ import annotations
