@@ -18,8 +18,12 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libbsagpu.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xptxas", "-warn-spills",
-              "--expt-relaxed-constexpr"]
+# Host code without floating-point contraction: the zone layout's geometry compares rounded
+# values (floor of a base / delta ratio, a rotation against pi), so a fused a * b + c where the
+# reference rounds twice moves zones (gcc contracts by default where the target has FMA, as on
+# aarch64; an x86-64 build of the reference has none)
+NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+              "-Xptxas", "-warn-spills", "--expt-relaxed-constexpr"]
 
 
 def nvcc() -> str:

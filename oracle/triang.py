@@ -117,8 +117,10 @@ class Tri:
     def deduce_rotation(self):
         dx = self.A[0] - self.C[0]
         dy = self.A[1] - self.C[1]
-        with np.errstate(divide="ignore", invalid="ignore"):
-            ang = float(np.arctan(np.float64(abs(dx)) / np.float64(abs(dy))))
+        if dy == 0.0:
+            ang = math.atan(math.inf) if dx != 0.0 else math.nan
+        else:
+            ang = math.atan(abs(dx) / abs(dy))
         if not (dx >= 0.0 and dy >= 0.0):
             if dy < 0.0:
                 ang = PI - ang if dx >= 0.0 else PI + ang
