@@ -56,7 +56,10 @@ def layout_refused(err):
 
 def records(seeds, tol, levels, skipped=None):
     X, Y, E = [], [], []
-    for seed in seeds:
+    t0 = time.perf_counter()
+    for n, seed in enumerate(seeds):
+        if n and n % 100 == 0:
+            print(f"records: {n} structures, {time.perf_counter() - t0:.0f} s", flush=True)
         s = api.BsaSession(structure(seed), precision=api.PREC_BF16X3)
         try:
             out = Refiner(s, tol, levels).run(keep_records=True)
@@ -85,7 +88,10 @@ def compare(prop, thr, seeds, tol, levels, fp64_every=1):
     FP64 GPU path integrating the plain criterion's final mesh (the error reference)."""
     rows = []
     rel = lambda x, y: float(np.max(np.abs(x - y)) / np.max(np.abs(y)))
+    t0 = time.perf_counter()
     for k, seed in enumerate(seeds):
+        if k and k % 20 == 0:
+            print(f"compare: {k} structures, {time.perf_counter() - t0:.0f} s", flush=True)
         prob = structure(seed)
         s = api.BsaSession(prob, precision=api.PREC_BF16X3)
         try:
