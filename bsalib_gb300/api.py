@@ -33,7 +33,7 @@ EXPORT_FN = C.CFUNCTYPE(None, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_doub
                         C.c_void_p)
 
 
-PLAN_CLS_FORM, PLAN_CLS_E_WIDTH, PLAN_CLS_D_WIDTH, PLAN_MSH_WIDTH = 1, 2, 3, 4
+PLAN_CLS_FORM, PLAN_CLS_E_WIDTH, PLAN_CLS_D_WIDTH, PLAN_MSH_WIDTH, PLAN_CLS_E_SPLIT = 1, 2, 3, 4, 5
 
 
 def tile_plan(family: int, nm: int, K: int, nf: int = 0) -> int:

@@ -9,8 +9,9 @@ analysis, the best of `reps` runs after one warm-up run), and writes the fastest
 to the table libbsagpu.so loads at first use (data/tile_plans.txt beside the library).
 
   Classic (tall building, bsa_Run in BF16x3): every combination of the form (E form where it
-  applies, D1 / D3 form) and of that form's FRF-table width that holds the modes; the table
-  records the best form, the best E width and the best D1 / D3 width of each bucket.
+  applies, D1 / D3 form) and of that form's FRF-table width that holds the modes (E widths 16
+  and 24 in one pass or two); the table records the best form, the best E width and its pass
+  count, and the best D1 / D3 width of each bucket.
   Mesher (bridge deck, the standalone driver's Mesher controls, bsa_Run with analysis type 2 in
   BF16x3): the mode width NMT of the zone kernel, every multiple of 8 from nm up to nm + 16.
 
@@ -40,7 +41,7 @@ NF_RANGES = [(1, 300, 129), (301, 700, 513), (701, 1 << 30, 1025)]        # (lo,
 E_WIDTHS = (8, 16, 24, 32, 48)
 D_WIDTHS = (8, 16, 24, 32, 64)
 FAMILY = {"cls_form": api.PLAN_CLS_FORM, "cls_e_width": api.PLAN_CLS_E_WIDTH, "cls_d_width": api.PLAN_CLS_D_WIDTH,
-          "msh_width": api.PLAN_MSH_WIDTH}
+          "msh_width": api.PLAN_MSH_WIDTH, "cls_e_split": api.PLAN_CLS_E_SPLIT}
 
 
 def _set(lib, fam, val):
@@ -68,7 +69,10 @@ def _time(prob, reps, plans, mesher=False):
 def classic_candidates(nm):
     c = []
     if nm <= 48:
-        c += [{"cls_form": 1, "cls_e_width": w} for w in E_WIDTHS if nm <= w <= max(8, 2 * nm)]
+        for w in E_WIDTHS:
+            if nm <= w <= max(8, 2 * nm):
+                # 16 and 24 in one pass or in two of half the modes (32 and 48 are always two)
+                c += [{"cls_form": 1, "cls_e_width": w, "cls_e_split": sp} for sp in ((1, 2) if w in (16, 24) else (0,))]
     c += [{"cls_form": 0, "cls_d_width": w} for w in D_WIDTHS if nm <= w <= max(8, 2 * nm)]
     return c
 
@@ -90,6 +94,7 @@ def tune_classic(reps, quick):
                 best_d = min((r for r in res if r[1]["cls_form"] == 0), key=lambda r: r[0])
                 rows.append({"nm": (nlo, nhi), "K": (klo, khi), "nf": (flo, fhi), "rep": (nhi, K, nf),
                              "form": res[0][1]["cls_form"], "e_width": best_e[1]["cls_e_width"] if best_e else None,
+                             "e_split": best_e[1]["cls_e_split"] if best_e and best_e[1]["cls_e_split"] else None,
                              "d_width": best_d[1]["cls_d_width"],
                              "times_ms": [(round(t, 3), c) for t, c in res]})
                 print(json.dumps(rows[-1]), flush=True)
@@ -116,7 +121,8 @@ def write_table(path, cls_rows, msh_rows, note):
     lines = ["# Tile plans of the split-precision contractions, written by python -m bsalib_gb300.autotune",
              f"# {note}",
              "# family nm_lo nm_hi k_lo k_hi nf_lo nf_hi value   # measured ms of the candidates (value: ms)"]
-    for fam, key in (("cls_form", "form"), ("cls_e_width", "e_width"), ("cls_d_width", "d_width")):
+    for fam, key in (("cls_form", "form"), ("cls_e_width", "e_width"), ("cls_e_split", "e_split"),
+                     ("cls_d_width", "d_width")):
         for r in cls_rows:
             if r[key] is None:
                 continue

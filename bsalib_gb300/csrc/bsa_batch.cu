@@ -767,7 +767,14 @@ int Engine::batch_run(double *m3mf, double *m3mr, double *m2mr, double *case_ms,
     while (g0 < order.size()) {
         const int Wd = width(order[g0]);
         const bool eform = e_ok(order[g0]);
-        const int NMT = eform ? (Wd == 32 ? 16 : Wd == 48 ? 24 : Wd) : (Wd > 32 ? 32 : Wd), JH = Wd / NMT;
+        int NMT;
+        if (eform) {
+            const BatchCase &c0 = g_batch[order[g0]];
+            NMT = Wd / plan_e_split(Wd, c0.nme, c0.K, (int)c0.f.size());
+        } else {
+            NMT = Wd > 32 ? 32 : Wd;
+        }
+        const int JH = Wd / NMT;
         size_t g1 = g0;
         double rows = 0.0;
         while (g1 < order.size() && width(order[g1]) == Wd && e_ok(order[g1]) == eform) {
@@ -915,11 +922,13 @@ int Engine::batch_run(double *m3mf, double *m3mr, double *m2mr, double *case_ms,
             cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
             kern<<<grid, ecls::kThreads, sm, stream>>>(maps[0], maps[1], maps[2], maps[3], prm);
         };
-        if (eform) switch (Wd) {
-        case 8: launch_e(k_bfm_e_batch<8, 1>, sizeof(ecls::UTile<8, 1>)); break;
-        case 16: launch_e(k_bfm_e_batch<16, 1>, sizeof(ecls::UTile<16, 1>)); break;
-        case 24: launch_e(k_bfm_e_batch<24, 1>, sizeof(ecls::UTile<24, 1>)); break;
-        case 32: launch_e(k_bfm_e_batch<16, 2>, sizeof(ecls::UTile<16, 2>)); break;
+        if (eform) switch (NMT * 10 + JH) {
+        case 81: launch_e(k_bfm_e_batch<8, 1>, sizeof(ecls::UTile<8, 1>)); break;
+        case 82: launch_e(k_bfm_e_batch<8, 2>, sizeof(ecls::UTile<8, 2>)); break;
+        case 122: launch_e(k_bfm_e_batch<12, 2>, sizeof(ecls::UTile<12, 2>)); break;
+        case 161: launch_e(k_bfm_e_batch<16, 1>, sizeof(ecls::UTile<16, 1>)); break;
+        case 162: launch_e(k_bfm_e_batch<16, 2>, sizeof(ecls::UTile<16, 2>)); break;
+        case 241: launch_e(k_bfm_e_batch<24, 1>, sizeof(ecls::UTile<24, 1>)); break;
         default: launch_e(k_bfm_e_batch<24, 2>, sizeof(ecls::UTile<24, 2>)); break;
         }
         else switch (Wd) {

@@ -27,7 +27,9 @@
 // the row + column sums and at the column - row and row - column differences) are staged in
 // shared memory one unit ahead.  Used for whole-grid launches with the truncated sum, up to
 // 48 kept modes (above 24 the G rows hold one half of the modes, JH = 2, and each unit is
-// swept once per half) and no central symmetry; bsa_mixed.cu's form otherwise.
+// swept once per half; a width of 16 or 24 may also run as two halves of 8 or 12, which halves
+// the epilogue's accumulators at the same MMA work, the tile plan's choice) and no central
+// symmetry; bsa_mixed.cu's form otherwise.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -318,7 +320,7 @@ int Engine::contract_e(const PointSrc &ps, double *m3mf, double *m3mr, const ESa
     using namespace ecls;
     const int nf = ps.nf, nm = nme;
     const int W = plan_e_width(nm, K, nf);  // 8, 16, 24; 32 and 48 as two mode halves
-    const int JH = W <= 24 ? 1 : 2, NMT = W / JH;
+    const int JH = plan_e_split(W, nm, K, nf), NMT = W / JH;  // 16 and 24 in one or two passes
     const int NC = kBN / NMT;
     const int Kp = ((K + kBK - 1) / kBK) * kBK;
     const int Mp = ((nm * nm + kBM - 1) / kBM) * kBM;
@@ -392,22 +394,22 @@ int Engine::contract_e(const PointSrc &ps, double *m3mf, double *m3mr, const ESa
             return cuda_fail(e, "memset");
     }
     if ((e = cudaEventRecord(evg0, stream))) return cuda_fail(e, "event");
-    if (smp) {
-        switch (W) {
-        case 8: e = launch_k<8, 1, true>(stream, maps, prm, grid); break;
-        case 16: e = launch_k<16, 1, true>(stream, maps, prm, grid); break;
-        case 24: e = launch_k<24, 1, true>(stream, maps, prm, grid); break;
-        case 32: e = launch_k<16, 2, true>(stream, maps, prm, grid); break;
-        default: e = launch_k<24, 2, true>(stream, maps, prm, grid); break;
-        }
-    } else {
-        switch (W) {
-        case 8: e = launch_k<8, 1>(stream, maps, prm, grid); break;
-        case 16: e = launch_k<16, 1>(stream, maps, prm, grid); break;
-        case 24: e = launch_k<24, 1>(stream, maps, prm, grid); break;
-        case 32: e = launch_k<16, 2>(stream, maps, prm, grid); break;
-        default: e = launch_k<24, 2>(stream, maps, prm, grid); break;
-        }
+    switch ((smp ? 1000 : 0) + NMT * 10 + JH) {
+    case 81: e = launch_k<8, 1>(stream, maps, prm, grid); break;
+    case 82: e = launch_k<8, 2>(stream, maps, prm, grid); break;
+    case 122: e = launch_k<12, 2>(stream, maps, prm, grid); break;
+    case 161: e = launch_k<16, 1>(stream, maps, prm, grid); break;
+    case 162: e = launch_k<16, 2>(stream, maps, prm, grid); break;
+    case 241: e = launch_k<24, 1>(stream, maps, prm, grid); break;
+    case 242: e = launch_k<24, 2>(stream, maps, prm, grid); break;
+    case 1081: e = launch_k<8, 1, true>(stream, maps, prm, grid); break;
+    case 1082: e = launch_k<8, 2, true>(stream, maps, prm, grid); break;
+    case 1122: e = launch_k<12, 2, true>(stream, maps, prm, grid); break;
+    case 1161: e = launch_k<16, 1, true>(stream, maps, prm, grid); break;
+    case 1162: e = launch_k<16, 2, true>(stream, maps, prm, grid); break;
+    case 1241: e = launch_k<24, 1, true>(stream, maps, prm, grid); break;
+    case 1242: e = launch_k<24, 2, true>(stream, maps, prm, grid); break;
+    default: return fail(BSA_ERR_STATE, "no E-form kernel for %d modes in %d passes", NMT, JH);
     }
     if (e) return cuda_fail(e, "BF16x3 tcgen05 contraction kernel (E form)");
     if ((e = cudaEventRecord(evg1, stream))) return cuda_fail(e, "event");

@@ -21,6 +21,7 @@ constexpr int kEFormMaxModes = 48;
 int plan_e_width(int nm, int K, int nf);
 int plan_d_width(int nm, int K, int nf);
 bool plan_prefer_e(int nm, int K, int nf);
+int plan_e_split(int W, int nm, int K, int nf);  // E form passes over the modes of width W
 int plan_msh_width(int nm, int K);
 
 // Device buffer that only grows (kept across runs; freed by bsa_Finalise).

@@ -8,14 +8,16 @@
 //     a wider table pads more modes but changes the grid columns per N tile (128 / NMT) and the
 //     epilogue's registers;
 //   * the D1 / D3 form's width (8, 16, 24, 32, or 64 as two halves of 32);
-//   * the Mesher kernel's mode width NMT (a multiple of 8 from the kept modes to 64).
+//   * the Mesher kernel's mode width NMT (a multiple of 8 from the kept modes to 64);
+//   * the E form's mode passes: a width of 16 or 24 in one pass or in two of half the modes
+//     (half the epilogue's accumulators per pass, fewer register spills, the same MMAs).
 // A plan line names a family, a range of kept modes, of K (= components x loaded nodes) and of
 // grid points per axis, and the value; the first matching line wins, and a value that does not
 // fit the case (narrower than its modes, or not a built width) falls back to the default rule,
 // the narrowest width that holds the modes, E form wherever it applies.
 //
 // Table file: one plan per line, "family nm_lo nm_hi k_lo k_hi nf_lo nf_hi value" with family
-// cls_form | cls_e_width | cls_d_width | msh_width; '#' starts a comment.  Loaded on first use
+// cls_form | cls_e_width | cls_d_width | msh_width | cls_e_split; '#' starts a comment.  Loaded on first use
 // from data/tile_plans.txt beside libbsagpu.so (or the file BSA_TILE_PLANS names), or by
 // bsa_gpu_loadTilePlans.
 #include <cuda_runtime.h>
@@ -56,6 +58,7 @@ int family_id(const char *name) {
     if (!std::strcmp(name, "cls_e_width")) return BSA_PLAN_CLS_E_WIDTH;
     if (!std::strcmp(name, "cls_d_width")) return BSA_PLAN_CLS_D_WIDTH;
     if (!std::strcmp(name, "msh_width")) return BSA_PLAN_MSH_WIDTH;
+    if (!std::strcmp(name, "cls_e_split")) return BSA_PLAN_CLS_E_SPLIT;
     return 0;
 }
 
@@ -143,6 +146,16 @@ int plan_d_width(int nm, int K, int nf) {
 
 bool plan_prefer_e(int nm, int K, int nf) { return lookup(BSA_PLAN_CLS_FORM, nm, K, nf, 1) != 0; }
 
+int plan_e_split(int W, int nm, int K, int nf) {
+    if (W == 8) return 1;
+    if (W == 32 || W == 48) return 2;
+    // GB300 (24-mode building, 257^2 / 1025^2 grids): 24 as 2 x 12 is 2-8 % faster on both grids;
+    // 16 as 2 x 8 2.5 % faster on the 1025^2 grid, 7 % slower on the 257^2 one
+    const int d = W == 24 ? 2 : (nf > 700 ? 2 : 1);
+    const int v = lookup(BSA_PLAN_CLS_E_SPLIT, nm, K, nf, d);
+    return v == 1 || v == 2 ? v : d;
+}
+
 int plan_msh_width(int nm, int K) {
     const int d = ((nm + 7) / 8) * 8;
     const int w = lookup(BSA_PLAN_MSH_WIDTH, nm, K, 0, d);
@@ -154,7 +167,7 @@ int plan_msh_width(int nm, int K) {
 extern "C" {
 
 int bsa_gpu_setTilePlan(int family, int nm_lo, int nm_hi, int k_lo, int k_hi, int nf_lo, int nf_hi, int value) {
-    if (family < BSA_PLAN_CLS_FORM || family > BSA_PLAN_MSH_WIDTH || nm_lo > nm_hi || k_lo > k_hi || nf_lo > nf_hi)
+    if (family < BSA_PLAN_CLS_FORM || family > BSA_PLAN_CLS_E_SPLIT || nm_lo > nm_hi || k_lo > k_hi || nf_lo > nf_hi)
         return bsa::eng().fail(BSA_ERR_ARG, "invalid tile plan");
     bsa::PlanTable &t = bsa::table();
     std::lock_guard<std::mutex> lk(t.m);
@@ -198,6 +211,7 @@ int bsa_gpu_getTilePlan(int family, int nm, int K, int nf, int *value) {
     case BSA_PLAN_CLS_E_WIDTH: *value = bsa::plan_e_width(nm, K, nf); break;
     case BSA_PLAN_CLS_D_WIDTH: *value = bsa::plan_d_width(nm, K, nf); break;
     case BSA_PLAN_MSH_WIDTH: *value = bsa::plan_msh_width(nm, K); break;
+    case BSA_PLAN_CLS_E_SPLIT: *value = bsa::plan_e_split(bsa::plan_e_width(nm, K, nf), nm, K, nf); break;
     default: return bsa::eng().fail(BSA_ERR_ARG, "unknown plan family %d", family);
     }
     return BSA_OK;

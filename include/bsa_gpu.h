@@ -446,9 +446,12 @@ int bsa_gpu_setClassicForm(int form);
  *   BSA_PLAN_CLS_E_WIDTH  E form FRF-table width: 8, 16, 24, 32 (2 x 16) or 48 (2 x 24)
  *   BSA_PLAN_CLS_D_WIDTH  D1 / D3 form width: 8, 16, 24, 32 or 64 (2 x 32)
  *   BSA_PLAN_MSH_WIDTH    Mesher kernel mode width: a multiple of 8 from nm to 64 (nf ignored)
+ *   BSA_PLAN_CLS_E_SPLIT  E form mode passes per unit: 1, or 2 (width 16 as 2 x 8 modes, 24 as
+ *                         2 x 12: half the epilogue's accumulators per pass); widths 32 and 48 are
+ *                         always 2 passes, width 8 one
  * The table is read on first use from data/tile_plans.txt beside the library (or the file the
  * environment variable BSA_TILE_PLANS names): lines "family nm_lo nm_hi k_lo k_hi nf_lo nf_hi
- * value" with family cls_form | cls_e_width | cls_d_width | msh_width.  The first matching plan
+ * value" with family cls_form | cls_e_width | cls_d_width | msh_width | cls_e_split.  The first matching plan
  * wins; a value that does not fit the case (narrower than nm, not a built width) falls back to
  * the default rule (narrowest width holding nm, E form wherever it applies).  The plans are
  * process-wide and survive bsa_Finalise.  setTilePlan adds a plan ahead of the table,
@@ -458,6 +461,7 @@ int bsa_gpu_setClassicForm(int form);
 #define BSA_PLAN_CLS_E_WIDTH 2
 #define BSA_PLAN_CLS_D_WIDTH 3
 #define BSA_PLAN_MSH_WIDTH 4
+#define BSA_PLAN_CLS_E_SPLIT 5
 int bsa_gpu_setTilePlan(int family, int nm_lo, int nm_hi, int k_lo, int k_hi, int nf_lo, int nf_hi, int value);
 int bsa_gpu_clearTilePlans(void);
 int bsa_gpu_loadTilePlans(const char *path);

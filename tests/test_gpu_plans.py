@@ -37,6 +37,7 @@ def test_classic_plans_agree(bsalib, modes):
     prob = tall_building(nodes=60, modes=modes, nfreqs=33, df=0.125, seed=9)
     ref = run(prob, [])
     cands = [[(api.PLAN_CLS_E_WIDTH, w)] for w in (16, 24, 32, 48) if w >= modes]
+    cands += [[(api.PLAN_CLS_E_WIDTH, w), (api.PLAN_CLS_E_SPLIT, sp)] for w in (16, 24) if w >= modes for sp in (1, 2)]
     cands += [[(api.PLAN_CLS_FORM, 0), (api.PLAN_CLS_D_WIDTH, w)] for w in (16, 24, 32, 64) if w >= modes]
     for c in cands:
         mr, mf = run(prob, c)
