@@ -54,10 +54,14 @@ def layout_refused(err):
     return "negative base" in str(err)
 
 
-def records(seeds, tol, levels, skipped=None):
+def records(seeds, tol, levels, skipped=None, budget_s=None, done=None):
     X, Y, E = [], [], []
     t0 = time.perf_counter()
     for n, seed in enumerate(seeds):
+        if budget_s is not None and time.perf_counter() - t0 > budget_s:
+            break
+        if done is not None:
+            done.append(seed)
         if n and n % 100 == 0:
             print(f"records: {n} structures, {time.perf_counter() - t0:.0f} s", flush=True)
         s = api.BsaSession(structure(seed), precision=api.PREC_BF16X3)
@@ -82,7 +86,7 @@ def brm_points(zones):
     return int(sum(((z.ni - 1) * z.Fi + 1) * ((z.nj - 1) * z.Fj + 1) for z in zones))
 
 
-def compare(prop, thr, seeds, tol, levels, fp64_every=1):
+def compare(prop, thr, seeds, tol, levels, fp64_every=1, budget_s=None):
     """Plain and learned refinement of each held-out structure in the split precision (device
     time and host wall time of each run), and, on every fp64_every-th structure, the plain
     FP64 GPU path integrating the plain criterion's final mesh (the error reference)."""
@@ -90,6 +94,8 @@ def compare(prop, thr, seeds, tol, levels, fp64_every=1):
     rel = lambda x, y: float(np.max(np.abs(x - y)) / np.max(np.abs(y)))
     t0 = time.perf_counter()
     for k, seed in enumerate(seeds):
+        if budget_s is not None and time.perf_counter() - t0 > budget_s:
+            break
         if k and k % 20 == 0:
             print(f"compare: {k} structures, {time.perf_counter() - t0:.0f} s", flush=True)
         prob = structure(seed)
@@ -171,11 +177,15 @@ def main():
     ap.add_argument("--out", default="")
     ap.add_argument("--json", default="")
     ap.add_argument("--records", default="", help="write the training records (features, label, change)")
+    ap.add_argument("--record-budget-s", type=float, default=None,
+                    help="stop drawing training structures after this many seconds (the count used is reported)")
+    ap.add_argument("--compare-budget-s", type=float, default=None,
+                    help="stop the held-out comparison after this many seconds (the count used is reported)")
     a = ap.parse_args()
     build.build()
     t0 = time.perf_counter()
-    skipped_train = []
-    X, Y, E = records(range(a.train), a.tol, a.levels, skipped_train)
+    skipped_train, used_train = [], []
+    X, Y, E = records(range(a.train), a.tol, a.levels, skipped_train, a.record_budget_s, used_train)
     t_rec = time.perf_counter() - t0
     if a.records:
         np.savez(a.records, X=X, Y=Y, E=E)
@@ -191,9 +201,10 @@ def main():
     recall = float(np.mean(p[Y > 0.5] > thr)) if np.any(Y > 0.5) else 1.0
     skipped = float(np.mean(p[Y < 0.5] <= thr)) if np.any(Y < 0.5) else 0.0
     t0 = time.perf_counter()
-    rows = compare(prop, thr, range(100000, 100000 + a.test), a.tol, a.levels, a.fp64_every)
+    rows = compare(prop, thr, range(100000, 100000 + a.test), a.tol, a.levels, a.fp64_every, a.compare_budget_s)
     t_cmp = time.perf_counter() - t0
-    res = {"train_structures": a.train, "train_skipped": skipped_train, "test_structures": a.test,
+    res = {"train_structures": len(used_train), "train_requested": a.train, "train_skipped": skipped_train,
+           "test_structures": len(rows), "test_requested": a.test,
            "records": int(len(Y)),
            "positive_fraction": float(Y.mean()), "record_s": t_rec, "fit_s": t_fit, "compare_s": t_cmp,
            "final_train_loss": loss, "threshold": thr, "train_recall": recall, "train_skipped_negatives": skipped,
