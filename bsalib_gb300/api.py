@@ -129,7 +129,7 @@ def load(path: Optional[str] = None):
         "bsa_gpu_setPrecision": [i], "bsa_gpu_setClassicTruncation": [i], "bsa_gpu_setClassicRows": [i, i],
         "bsa_gpu_clsBispectra": [vp, i, vp, vp, vp], "bsa_gpu_mshBispectra": [vp, vp, i, vp, vp],
         "bsa_gpu_clsBispectraAt": [vp, vp, i, vp, vp], "bsa_gpu_setWaitTest": [i],
-        "bsa_gpu_setMesherGraphs": [i], "bsa_gpu_setMesherExpansion": [i], "bsa_gpu_setClassicShard": [i, i], "bsa_enableVisualMode": [], "bsa_setVisualIndexes": [vp, i], "bsa_setBRMExportDefaultMode": [i],
+        "bsa_gpu_setMesherGraphs": [i], "bsa_gpu_setMesherExpansion": [i], "bsa_gpu_setMesherPassBytes": [d], "bsa_gpu_setClassicShard": [i, i], "bsa_enableVisualMode": [], "bsa_setVisualIndexes": [vp, i], "bsa_setBRMExportDefaultMode": [i],
         "bsa_gpu_setTilePlan": [i] * 8, "bsa_gpu_clearTilePlans": [], "bsa_gpu_loadTilePlans": [C.c_char_p],
         "bsa_gpu_getTilePlan": [i, i, i, i, vp],
         "bsa_gpu_mshMoments": [vp, vp, vp, i, vp, vp], "bsa_gpu_getStats": [vp], "bsa_gpu_releaseDeviceCache": [], "bsa_gpu_setClassicForm": [i],

@@ -122,6 +122,7 @@ struct Engine {
     int wait_test_tile1 = 0;    // bsa_gpu_setWaitTest: tile + 1 whose ready signal CTA 0 omits (0 = off)
     bool msh_graphs = true;     // bsa_gpu_setMesherGraphs: each Mesher zone pass as one CUDA graph
     bool msh_dev_expand = true; // bsa_gpu_setMesherExpansion: zone passes expanded on the device
+    double msh_pass_bytes = 0.0; // bsa_gpu_setMesherPassBytes: device bytes of one zone pass (0: default)
     // Mesher controls (BsaLibData.F90:219-233, 273): delta validation, BFM multi-level
     // refinement, background peak restricted to the first direction, diagonal-crest scheme
     bool validate_deltas = true, bfm_mlr = true, bkg_restrict = false, premesh_diag_crest = false,

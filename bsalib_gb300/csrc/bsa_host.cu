@@ -1267,6 +1267,12 @@ int bsa_gpu_setMesherExpansion(int on_device) {
     return BSA_OK;
 }
 
+int bsa_gpu_setMesherPassBytes(double bytes) {
+    GUARD();
+    eng().msh_pass_bytes = bytes > 0.0 ? bytes : 0.0;
+    return BSA_OK;
+}
+
 int bsa_gpu_setClassicForm(int form) {
     if (form != 0 && form != 1) return BSA_ERR_ARG;
     eng().use_e_form = form == 1;

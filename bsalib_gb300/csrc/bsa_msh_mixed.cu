@@ -1392,35 +1392,38 @@ int Engine::run_zones_mixed(const std::vector<ZoneDev> &zones, double *m3mf, dou
     h2d = d2h = 0;
     if (!axis.empty()) {
         // batches by device bytes: U blocks of the distinct line / column frequencies, column
-        // and sum tables, term tensors and BRM-point FRF tables
+        // and sum tables, term tensors and BRM-point FRF tables, and the FP32 A row and nodal
+        // spectra of each distinct frequency (a point may bring a sum frequency of its own)
         const int NMT = plan_msh_width(nm, K);
         const double Kp = (double)(((K + 63) / 64) * 64), Mp = (double)(((nm * nm + 127) / 128) * 128);
-        const double per_u = Mp * Kp * 4.0, per_col = NMT * Kp * 4.0;
-        const double per_pt = 2.0 * NMT * Kp * 4.0 + 3.0 * nm3 * 4.0, per_q = 3.0 * nm * 8.0 + 4.0;
+        const double per_f = (double)K * nm * 4.0 + (double)K * 8.0;
+        const double per_u = Mp * Kp * 4.0 + per_f, per_col = NMT * Kp * 4.0 + per_f;
+        const double per_pt = 2.0 * NMT * Kp * 4.0 + 3.0 * nm3 * 4.0 + per_f, per_q = 3.0 * nm * 8.0 + 4.0;
         // as much of the zone list per pass as 40 % of the device memory holds (one pass for the
         // reference layouts of the bench's structures on a GB300: the 60-mode bridge needs about
         // 88 GB), at least 4 GB; from the total, not the free memory, so the batching of a zone
         // list does not depend on what earlier analyses left allocated
         size_t fr = 0, tot = 0;
         if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) tot = 0;
-        const double budget = std::max(4e9, 0.4 * (double)tot);
+        const double budget = msh_pass_bytes > 0.0 ? msh_pass_bytes : std::max(4e9, 0.4 * (double)tot);
         // A zone too large for a quarter of a pass is split into strips of consecutive lattice
         // lines that share their boundary lines (the trapezoid's half weights of a shared BFM /
         // BRM line from both strips add up to the unsplit zone's interior weight, and every cell
-        // is interpolated within one strip): the same integrals in passes that fit.
+        // is interpolated within one strip): the same integrals in passes that fit.  A zone with
+        // so many columns that their U blocks alone crowd a pass is first cut the same way into
+        // blocks of columns that share their boundary columns.
         std::vector<int> parent;
         {
             std::vector<ZoneDev> split;
-            for (size_t k = 0; k < axis.size(); ++k) {
-                const ZoneDev &z = axis[k];
+            auto by_lines = [&](const ZoneDev &z, int k) {
                 const double NJ = (double)((z.nj - 1) * z.Fj + 1);
                 const double line = per_u + per_pt * z.nj + per_q * z.Fi * NJ;  // bytes one more line adds
                 const double fixed = per_u * z.nj + per_col * z.nj + per_q * NJ;
                 const double whole = fixed + line * z.ni;
                 if (whole <= 0.25 * budget && (long long)z.ni * z.nj <= 1000000) {
                     split.push_back(z);
-                    parent.push_back((int)k);
-                    continue;
+                    parent.push_back(k);
+                    return;
                 }
                 const int L = (int)std::max(2.0, std::min(std::floor((0.25 * budget - fixed) / line),
                                                           std::floor(1000000.0 / z.nj)));
@@ -1430,8 +1433,27 @@ int Engine::run_zones_mixed(const std::vector<ZoneDev> &zones, double *m3mf, dou
                     st.fi0 = z.fi0 + i0 * z.dIi;
                     st.ni = i1 - i0 + 1;
                     split.push_back(st);
-                    parent.push_back((int)k);
+                    parent.push_back(k);
                     i0 = i1;
+                }
+            };
+            for (size_t k = 0; k < axis.size(); ++k) {
+                const ZoneDev &z = axis[k];
+                // bytes a column adds to a two-line strip: its U block, column row, two points and
+                // their BRM cells
+                const double col = per_u + per_col + 2.0 * per_pt + per_q * z.Fj * (2.0 * z.Fi + 1.0);
+                const int Jc = (int)std::max(2.0, std::floor(0.125 * budget / col));
+                if (z.nj <= Jc) {
+                    by_lines(z, (int)k);
+                    continue;
+                }
+                for (int j0 = 0; j0 < z.nj - 1;) {
+                    const int j1 = std::min(j0 + Jc - 1, z.nj - 1);
+                    ZoneDev cb = z;
+                    cb.fj0 = z.fj0 + j0 * z.dJj;
+                    cb.nj = j1 - j0 + 1;
+                    by_lines(cb, (int)k);
+                    j0 = j1;
                 }
             }
             axis.swap(split);

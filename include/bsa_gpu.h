@@ -489,6 +489,13 @@ int bsa_gpu_setMesherGraphs(int on);
  * differs (hash order), the moments agree to FP32 rounding. */
 int bsa_gpu_setMesherExpansion(int on_device);
 
+/* No counterpart in the reference.  Device bytes one split-precision Mesher zone pass may use
+ * (operand blocks, term tensors, FRF rows, A rows); bytes <= 0 (default): 40 % of the device
+ * memory, at least 4 GB.  Zones too large for a quarter of a pass run as blocks of columns and
+ * strips of lines that share their boundary lattice lines (the same integrals).  A host sharing
+ * the device with other allocations sets a smaller figure. */
+int bsa_gpu_setMesherPassBytes(double bytes);
+
 /* Device memory.  Blocks the library releases (bsa_Finalise, buffer growth) are kept for reuse
  * by the next analysis, up to a quarter of the device memory, so repeated bsa_Init ...
  * bsa_Finalise cycles do not pay cudaMalloc / cudaFree of the operand tables each time.  This

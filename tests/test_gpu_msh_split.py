@@ -40,3 +40,31 @@ def test_oversized_zone_in_strips(bsalib):
     assert rel(mf, mf64) < 1e-4 and rel(mr, mr64) < 1e-4
     assert rel(mr_d, mr) < 1e-5
     assert rel(zd[0], zd2.sum(axis=0)) < 1e-5
+
+
+def test_small_pass_budget_blocks_and_strips(bsalib):
+    """With a small pass budget (bsa_gpu_setMesherPassBytes) a zone runs as blocks of columns and
+    strips of lines sharing their boundary lattice lines: the same integrals as the FP64 zone
+    path, zones of both lattice orientations, and the per-zone moments the sum over the pieces."""
+    prob = tall_building(nodes=20, modes=4, nfreqs=9, df=0.3, seed=6)
+    prob.settings.suban = 2
+    zs = [api.Zone(0.05, -0.6, 0.9 / 120, 0.0, 0.0, 0.9 / 300, 121, 301, 2, 1, 1.0, 0),
+          api.Zone(-0.7, 0.1, 0.0, 0.6 / 200, 0.8 / 90, 0.0, 201, 91, 1, 2, 2.0, 0)]
+    s = api.BsaSession(prob, precision=api.PREC_FP64)
+    try:
+        mf64, mr64, cnt = s.msh_zones(zs)
+    finally:
+        s.close()
+    s = api.BsaSession(prob, precision=api.PREC_BF16X3)
+    try:
+        _, mr_whole, zd_whole = s.msh_zones_diag(zs)
+        api.check(s.lib.bsa_gpu_setMesherPassBytes(8e6), "bsa_gpu_setMesherPassBytes")
+        mf, mr, cnt2 = s.msh_zones(zs)
+        _, mr_d, zd = s.msh_zones_diag(zs)
+    finally:
+        s.lib.bsa_gpu_setMesherPassBytes(0.0)
+        s.close()
+    assert cnt[0] == cnt2[0] and cnt[1] == cnt2[1]
+    assert rel(mf, mf64) < 1e-4 and rel(mr, mr64) < 1e-4
+    assert rel(mr_d, mr_whole) < 1e-5
+    assert rel(zd, zd_whole) < 1e-5
