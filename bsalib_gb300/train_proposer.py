@@ -50,8 +50,9 @@ def skew(nm, m2, m3):
 
 def layout_refused(err):
     """The reference's pre-mesh aborts on this structure as well (BsaMesherImpl.F90:809-810,
-    "Negative base."): its first quadrant zone would have no extent."""
-    return "negative base" in str(err)
+    "Negative base."): its first quadrant zone would have no extent.  A refinement level whose
+    zone pass does not fit the device memory is skipped the same way (and reported)."""
+    return "negative base" in str(err) or "out of memory" in str(err)
 
 
 def records(seeds, tol, levels, skipped=None, budget_s=None, done=None):
@@ -110,7 +111,8 @@ def compare(prop, thr, seeds, tol, levels, fp64_every=1, budget_s=None):
         except api.BsaError as e:
             if not layout_refused(e):
                 raise
-            rows.append({"seed": seed, "skipped": "the reference's pre-mesh refuses the layout (negative base)"})
+            rows.append({"seed": seed, "skipped": "out of device memory" if "out of memory" in str(e) else
+                         "the reference's pre-mesh refuses the layout (negative base)"})
             continue
         finally:
             s.close()
