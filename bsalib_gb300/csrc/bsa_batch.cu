@@ -384,14 +384,15 @@ __global__ void k_batch_reduce(const CaseP *__restrict__ cases, const long long 
 // columns q >= p, once per mode half) of bsa_classic_e.cu's pipeline, whose three epilogue
 // warpgroups add the six contributions of each E(f_p, f_q) element into the case's
 // accumulators [9 kinds][W][Mp].  Only the U and G tables are read (no S table).
-template <int NMT, int JH>
-__global__ void __launch_bounds__(ecls::kThreads, 1)  // 14 warps: at most 128 registers a thread
+template <int NMT, int JH, bool RS = ecls::use_regsplit(NMT, JH)>
+__global__ void __launch_bounds__(ecls::ELayout<RS>::threads, 1)  // 128 registers a thread at launch
     k_bfm_e_batch(const __grid_constant__ CUtensorMap tmUh, const __grid_constant__ CUtensorMap tmUl,
                   const __grid_constant__ CUtensorMap tmGh, const __grid_constant__ CUtensorMap tmGl, const BParams p) {
     using namespace ecls;
     constexpr int NC = kBN / NMT;
     constexpr int BROWS = NC * NMT;
     constexpr int W = NMT * JH;
+    using L = ELayout<RS>;
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint64_t *bars = (uint64_t *)(smem + ecls::kStages * ecls::kStageBytes);
@@ -422,7 +423,7 @@ __global__ void __launch_bounds__(ecls::kThreads, 1)  // 14 warps: at most 128 r
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     }
-    if (warp == 1) {
+    if (warp == L::warp_mma) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(su32(tmem_slot)) : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
@@ -432,7 +433,9 @@ __global__ void __launch_bounds__(ecls::kThreads, 1)  // 14 warps: at most 128 r
     const uint32_t tmem = *tmem_slot;
     const uint32_t tx_bytes = 2u * kTileBytes + 4u * (uint32_t)(BROWS * 128);
 
-    if (warp == 0) {
+    if (RS ? warp >= L::warp_tma : warp < L::epi_warp0) {
+      if constexpr (RS) regs_producer();  // the whole producer warpgroup, before its warps part
+      if (warp == L::warp_tma) {
         // ---------------- TMA producer ----------------
         if (lane == 0) {
             uint32_t it = 0;
@@ -471,7 +474,7 @@ __global__ void __launch_bounds__(ecls::kThreads, 1)  // 14 warps: at most 128 r
             }
         }
         __syncwarp();
-    } else if (warp == 1) {
+      } else if (warp == L::warp_mma) {
         // ---------------- MMA issuer ----------------
         if (lane == 0) {
             uint32_t it = 0, tile = 0;
@@ -514,13 +517,15 @@ __global__ void __launch_bounds__(ecls::kThreads, 1)  // 14 warps: at most 128 r
             }
         }
         __syncwarp();
+      }
     } else {
+        if constexpr (RS) regs_epilogue();
         // ---------------- three epilogue warpgroups ----------------
         // After a failed wait a warp walks the unit sequence without work, so every warp
         // reaches every epi_sync384.
-        const int wg = (warp - 2) >> 2;
+        const int wg = (warp - L::epi_warp0) >> 2;
         const int quarter = warp & 3;
-        const int et = threadIdx.x - 64;
+        const int et = threadIdx.x - 32 * L::epi_warp0;
         const int row = quarter * 32 + lane;
         const uint32_t lane_base = tmem + ((uint32_t)(quarter * 32) << 16);
         using UT = UTile<NMT, JH>;
@@ -613,7 +618,7 @@ __global__ void __launch_bounds__(ecls::kThreads, 1)  // 14 warps: at most 128 r
     fence_before();
     __syncthreads();
     fence_after();
-    if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem) : "memory");
+    if (warp == L::warp_mma) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem) : "memory");
 }
 
 // m3 of case c from the E-form accumulators (kinds: 0 K_i, 1 K_iv, 2 F14, 3 K_iii, 4 K_v,
@@ -917,20 +922,27 @@ int Engine::batch_run(double *m3mf, double *m3mr, double *m2mr, double *case_ms,
             cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             kern<<<grid, 192, smem, stream>>>(maps[0], maps[1], maps[2], maps[3], maps[4], maps[5], prm);
         };
-        auto launch_e = [&](auto kern, size_t ut) {  // UTile bytes ut: fits with the stages (static_assert in bsa_classic_e.cu)
+        bool launched = true;
+        auto launch_e = [&](auto kern, size_t ut, bool rs) {  // UTile bytes ut: fits with the stages (static_assert in bsa_classic_e.cu)
             const size_t sm = (size_t)ecls::kStages * ecls::kStageBytes + 1024 + ecls::kBarBytes + 2 * ut;
             cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-            kern<<<grid, ecls::kThreads, sm, stream>>>(maps[0], maps[1], maps[2], maps[3], prm);
+            if (rs && ecls::regsplit_check(kern) != cudaSuccess) {
+                launched = false;
+                return;
+            }
+            kern<<<grid, rs ? ecls::ELayout<true>::threads : ecls::ELayout<false>::threads, sm, stream>>>(
+                maps[0], maps[1], maps[2], maps[3], prm);
         };
         if (eform) switch (NMT * 10 + JH) {
-        case 81: launch_e(k_bfm_e_batch<8, 1>, sizeof(ecls::UTile<8, 1>)); break;
-        case 82: launch_e(k_bfm_e_batch<8, 2>, sizeof(ecls::UTile<8, 2>)); break;
-        case 122: launch_e(k_bfm_e_batch<12, 2>, sizeof(ecls::UTile<12, 2>)); break;
-        case 161: launch_e(k_bfm_e_batch<16, 1>, sizeof(ecls::UTile<16, 1>)); break;
-        case 162: launch_e(k_bfm_e_batch<16, 2>, sizeof(ecls::UTile<16, 2>)); break;
-        case 241: launch_e(k_bfm_e_batch<24, 1>, sizeof(ecls::UTile<24, 1>)); break;
-        default: launch_e(k_bfm_e_batch<24, 2>, sizeof(ecls::UTile<24, 2>)); break;
+        case 81: launch_e(k_bfm_e_batch<8, 1>, sizeof(ecls::UTile<8, 1>), ecls::use_regsplit(8, 1)); break;
+        case 82: launch_e(k_bfm_e_batch<8, 2>, sizeof(ecls::UTile<8, 2>), ecls::use_regsplit(8, 2)); break;
+        case 122: launch_e(k_bfm_e_batch<12, 2>, sizeof(ecls::UTile<12, 2>), ecls::use_regsplit(12, 2)); break;
+        case 161: launch_e(k_bfm_e_batch<16, 1>, sizeof(ecls::UTile<16, 1>), ecls::use_regsplit(16, 1)); break;
+        case 162: launch_e(k_bfm_e_batch<16, 2>, sizeof(ecls::UTile<16, 2>), ecls::use_regsplit(16, 2)); break;
+        case 241: launch_e(k_bfm_e_batch<24, 1>, sizeof(ecls::UTile<24, 1>), ecls::use_regsplit(24, 1)); break;
+        default: launch_e(k_bfm_e_batch<24, 2>, sizeof(ecls::UTile<24, 2>), ecls::use_regsplit(24, 2)); break;
         }
+        if (!launched) return fail(BSA_ERR_STATE, "register split of the batched E-form kernel: launch registers");
         else switch (Wd) {
         case 8: launch(k_bfm_batch<8, 1, true>); break;
         case 16: launch(k_bfm_batch<16, 1, true>); break;

@@ -53,13 +53,14 @@ using namespace tc;
 // SAMPLE = true is the diagnostic instantiation: the same products, with the epilogue writing
 // the unweighted per-point bispectra of the grid points P.slot lists (unit_half_sample) instead
 // of the weighted moment partials.
-template <int NMT, int JH, bool SAMPLE>
-__global__ void __launch_bounds__(kThreads, 1)  // 14 warps: at most 128 registers a thread
+template <int NMT, int JH, bool SAMPLE, bool RS = use_regsplit(NMT, JH)>
+__global__ void __launch_bounds__(ELayout<RS>::threads, 1)  // 128 registers a thread at launch
     k_bfm_e(const __grid_constant__ CUtensorMap tmUh, const __grid_constant__ CUtensorMap tmUl,
             const __grid_constant__ CUtensorMap tmGh, const __grid_constant__ CUtensorMap tmGl, const EParams P) {
     constexpr int NC = kBN / NMT;
     constexpr int BROWS = NC * NMT;
     constexpr int W = NMT * JH;
+    using L = ELayout<RS>;
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint64_t *bars = (uint64_t *)(smem + kStages * kStageBytes);
@@ -88,7 +89,7 @@ __global__ void __launch_bounds__(kThreads, 1)  // 14 warps: at most 128 registe
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     }
-    if (warp == 1) {
+    if (warp == L::warp_mma) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(su32(tmem_slot)) : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
@@ -104,7 +105,9 @@ __global__ void __launch_bounds__(kThreads, 1)  // 14 warps: at most 128 registe
     const int r0 = P.p0 + (blockIdx.x / P.MT) * pstep;
     const uint32_t tx_bytes = 2u * kTileBytes + 4u * (uint32_t)(BROWS * 128);
 
-    if (warp == 0) {
+    if (RS ? warp >= L::warp_tma : warp < L::epi_warp0) {
+      if constexpr (RS) regs_producer();  // the whole producer warpgroup, before its warps part
+      if (warp == L::warp_tma) {
         // ---------------- TMA producer ----------------
         if (lane == 0) {
             uint32_t it = 0;
@@ -142,7 +145,7 @@ __global__ void __launch_bounds__(kThreads, 1)  // 14 warps: at most 128 registe
             }
         }
         __syncwarp();
-    } else if (warp == 1) {
+      } else if (warp == L::warp_mma) {
         // ---------------- MMA issuer ----------------
         if (lane == 0) {
             uint32_t it = 0, tile = 0;
@@ -185,11 +188,13 @@ __global__ void __launch_bounds__(kThreads, 1)  // 14 warps: at most 128 registe
             }
         }
         __syncwarp();
+      }
     } else {
+        if constexpr (RS) regs_epilogue();
         // ---------------- three epilogue warpgroups ----------------
-        const int wg = (warp - 2) >> 2;        // 0: warps 2-5, 1: warps 6-9, 2: warps 10-13
-        const int quarter = warp & 3;          // TMEM lane quarter of this warp
-        const int et = threadIdx.x - 64;       // 0 .. 383
+        const int wg = (warp - L::epi_warp0) >> 2;
+        const int quarter = warp & 3;               // TMEM lane quarter of this warp
+        const int et = threadIdx.x - 32 * L::epi_warp0;  // 0 .. 383
         const int row = quarter * 32 + lane;
         const int grow = mt * kBM + row;
         const bool vrow = grow < P.nm * P.nm;
@@ -267,7 +272,7 @@ __global__ void __launch_bounds__(kThreads, 1)  // 14 warps: at most 128 registe
     fence_before();
     __syncthreads();
     fence_after();
-    if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem) : "memory");
+    if (warp == L::warp_mma) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem) : "memory");
 }
 
 }  // namespace ecls
@@ -306,7 +311,9 @@ static cudaError_t launch_k(cudaStream_t st, const CUtensorMap *maps, const EPar
     cudaError_t e =
         cudaFuncSetAttribute(k_bfm_e<NMT, JH, SAMPLE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    k_bfm_e<NMT, JH, SAMPLE><<<grid, kThreads, smem, st>>>(maps[0], maps[1], maps[2], maps[3], p);
+    constexpr bool RS = use_regsplit(NMT, JH);
+    if (RS && (e = regsplit_check(k_bfm_e<NMT, JH, SAMPLE>)) != cudaSuccess) return e;
+    k_bfm_e<NMT, JH, SAMPLE><<<grid, ELayout<RS>::threads, smem, st>>>(maps[0], maps[1], maps[2], maps[3], p);
     return cudaGetLastError();
 }
 

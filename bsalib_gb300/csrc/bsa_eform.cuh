@@ -27,8 +27,39 @@ constexpr int kKindsWG = 3;  // per epilogue warpgroup: two response kinds and o
 constexpr int kKinds = 3 * kKindsWG;  // 0 K_i, 1 K_iv, 2 F14, 3 K_iii, 4 K_v, 5 F35, 6 K_ii, 7 K_vi, 8 F26
 constexpr int kFlushTiles = 64;
 constexpr int kBarBytes = 256;
-constexpr int kThreads = 448;  // TMA warp, MMA warp, 3 x 4 epilogue warps
-constexpr int kEpi = 384;
+constexpr int kEpi = 384;  // three epilogue warpgroups
+
+// Warp layouts of the E-form kernels.  Plain: 14 warps, the TMA warp 0, the MMA warp 1, the
+// epilogue warps 2-13, at most 128 registers a thread.  Register split: 16 warps, the epilogue
+// warpgroups first (warps 0-11), then a producer warpgroup of the TMA warp 12, the MMA warp 13
+// and two idle warps; launched at 128 registers a thread, the producer warpgroup keeps 40 and
+// the epilogue warpgroups take 152 (setmaxnreg): 384 x 152 + 128 x 40 = 63 488 of the launch's
+// 65 536.  The split pays where the epilogue's accumulators spill most (the 32- and 48-mode
+// widths, two passes of 16 or 24 modes); below that the plain layout is faster.
+template <bool RS>
+struct ELayout {
+    static constexpr int threads = RS ? 512 : 448;
+    static constexpr int warp_tma = RS ? 12 : 0, warp_mma = RS ? 13 : 1, epi_warp0 = RS ? 0 : 2;
+};
+constexpr int kRegsEpi = 152, kRegsProd = 40;
+static_assert(kEpi * kRegsEpi + (ELayout<true>::threads - kEpi) * kRegsProd <= ELayout<true>::threads * 128,
+              "register split above the registers the block is launched with");
+constexpr bool use_regsplit(int NMT, int JH) { return JH == 2 && NMT >= 16; }
+
+__device__ __forceinline__ void regs_producer() { asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;" ::"n"(kRegsProd)); }
+__device__ __forceinline__ void regs_epilogue() { asm volatile("setmaxnreg.inc.sync.aligned.u32 %0;" ::"n"(kRegsEpi)); }
+
+// A register-split kernel needs its 128 registers a thread at launch: a setmaxnreg.inc the
+// block cannot satisfy would wait for ever, so the host checks before every launch.
+template <class K>
+inline cudaError_t regsplit_check(K kern) {
+    cudaFuncAttributes fa;
+    cudaError_t e = cudaFuncGetAttributes(&fa, kern);
+    if (e != cudaSuccess) return e;
+    return fa.numRegs * ELayout<true>::threads >= kEpi * kRegsEpi + (ELayout<true>::threads - kEpi) * kRegsProd
+               ? cudaSuccess
+               : cudaErrorInvalidConfiguration;
+}
 
 // FRF values of one unit (row p, columns q0 .. q0 + 2 NC - 1): H_j at the row, and per
 // column H_j(v), H_j(u + v), H_j(v - u), H_j(u - v), all W = NMT x JH modes (above 24 kept
