@@ -20,12 +20,13 @@
 // each with its point's integration weight; (iii)-(vi) exist where q - p <= h.  A diagonal
 // element (q = p) feeds all six at half weight (its transpose is in the same tile).
 //
-// The kernel is bsa_mixed.cu's pipeline (warp 0 TMA, warp 1 tcgen05 MMA, BF16x3, FP32 TMEM
+// The kernel is bsa_mixed.cu's pipeline (a TMA warp, a tcgen05 MMA warp, BF16x3, FP32 TMEM
 // accumulators, 2 stages of 96 KB, N = 256 MMAs over two N tiles of grid columns) with three
-// epilogue warpgroups on the same TMEM buffer, one per weight: warps 2-5 accumulate (i), (iv)
-// and their force moment, warps 6-9 (iii), (v) and theirs, warps 10-13 (ii), (vi) and theirs.  The FRF values a unit reads (H at the row, at the unit's columns, at
-// the row + column sums and at the column - row and row - column differences) are staged in
-// shared memory one unit ahead.  Used for whole-grid launches with the truncated sum, up to
+// epilogue warpgroups on the same TMEM buffer, one per weight: the first accumulates (i), (iv)
+// and their force moment, the second (iii), (v) and theirs, the third (ii), (vi) and theirs
+// (warp layouts, plain or register split: ELayout in bsa_eform.cuh).  The FRF values a unit
+// reads (H at the row, at the unit's columns, at the row + column sums and at the column - row
+// and row - column differences) are staged in shared memory one unit ahead.  Used for whole-grid launches with the truncated sum, up to
 // 48 kept modes (above 24 the G rows hold one half of the modes, JH = 2, and each unit is
 // swept once per half; a width of 16 or 24 may also run as two halves of 8 or 12, which halves
 // the epilogue's accumulators at the same MMA work, the tile plan's choice) and no central
