@@ -922,33 +922,30 @@ int Engine::batch_run(double *m3mf, double *m3mr, double *m2mr, double *case_ms,
             cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             kern<<<grid, 192, smem, stream>>>(maps[0], maps[1], maps[2], maps[3], maps[4], maps[5], prm);
         };
-        bool launched = true;
-        auto launch_e = [&](auto kern, size_t ut, bool rs) {  // UTile bytes ut: fits with the stages (static_assert in bsa_classic_e.cu)
+        // the batched E-form kernel runs in the plain warp layout (ecls::ELayout<false>)
+        auto launch_e = [&](auto kern, size_t ut) {  // UTile bytes ut: fits with the stages (static_assert in bsa_classic_e.cu)
             const size_t sm = (size_t)ecls::kStages * ecls::kStageBytes + 1024 + ecls::kBarBytes + 2 * ut;
             cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-            if (rs && ecls::regsplit_check(kern) != cudaSuccess) {
-                launched = false;
-                return;
-            }
-            kern<<<grid, rs ? ecls::ELayout<true>::threads : ecls::ELayout<false>::threads, sm, stream>>>(
-                maps[0], maps[1], maps[2], maps[3], prm);
+            kern<<<grid, ecls::ELayout<false>::threads, sm, stream>>>(maps[0], maps[1], maps[2], maps[3], prm);
         };
-        if (eform) switch (NMT * 10 + JH) {
-        case 81: launch_e(k_bfm_e_batch<8, 1>, sizeof(ecls::UTile<8, 1>), false); break;
-        case 82: launch_e(k_bfm_e_batch<8, 2>, sizeof(ecls::UTile<8, 2>), false); break;
-        case 122: launch_e(k_bfm_e_batch<12, 2>, sizeof(ecls::UTile<12, 2>), false); break;
-        case 161: launch_e(k_bfm_e_batch<16, 1>, sizeof(ecls::UTile<16, 1>), false); break;
-        case 162: launch_e(k_bfm_e_batch<16, 2>, sizeof(ecls::UTile<16, 2>), false); break;
-        case 241: launch_e(k_bfm_e_batch<24, 1>, sizeof(ecls::UTile<24, 1>), false); break;
-        default: launch_e(k_bfm_e_batch<24, 2>, sizeof(ecls::UTile<24, 2>), false); break;
-        }
-        if (!launched) return fail(BSA_ERR_STATE, "register split of the batched E-form kernel: launch registers");
-        else switch (Wd) {
-        case 8: launch(k_bfm_batch<8, 1, true>); break;
-        case 16: launch(k_bfm_batch<16, 1, true>); break;
-        case 24: launch(k_bfm_batch<24, 1, true>); break;
-        case 32: launch(k_bfm_batch<32, 1, false>); break;
-        default: launch(k_bfm_batch<32, 2, false>); break;
+        if (eform) {
+            switch (NMT * 10 + JH) {
+            case 81: launch_e(k_bfm_e_batch<8, 1>, sizeof(ecls::UTile<8, 1>)); break;
+            case 82: launch_e(k_bfm_e_batch<8, 2>, sizeof(ecls::UTile<8, 2>)); break;
+            case 122: launch_e(k_bfm_e_batch<12, 2>, sizeof(ecls::UTile<12, 2>)); break;
+            case 161: launch_e(k_bfm_e_batch<16, 1>, sizeof(ecls::UTile<16, 1>)); break;
+            case 162: launch_e(k_bfm_e_batch<16, 2>, sizeof(ecls::UTile<16, 2>)); break;
+            case 241: launch_e(k_bfm_e_batch<24, 1>, sizeof(ecls::UTile<24, 1>)); break;
+            default: launch_e(k_bfm_e_batch<24, 2>, sizeof(ecls::UTile<24, 2>)); break;
+            }
+        } else {
+            switch (Wd) {
+            case 8: launch(k_bfm_batch<8, 1, true>); break;
+            case 16: launch(k_bfm_batch<16, 1, true>); break;
+            case 24: launch(k_bfm_batch<24, 1, true>); break;
+            case 32: launch(k_bfm_batch<32, 1, false>); break;
+            default: launch(k_bfm_batch<32, 2, false>); break;
+            }
         }
         if ((e = cudaGetLastError())) return cuda_fail(e, "batched tcgen05 contraction kernel");
         if ((e = cudaEventRecord(evg1, stream))) return cuda_fail(e, "event");

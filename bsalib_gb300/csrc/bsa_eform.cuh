@@ -35,9 +35,8 @@ constexpr int kEpi = 384;  // three epilogue warpgroups
 // and two idle warps; launched at 128 registers a thread, the producer warpgroup keeps 40 and
 // the epilogue warpgroups take 152 (setmaxnreg): 384 x 152 + 128 x 40 = 63 488 of the launch's
 // 65 536.  Measured 17 % faster for the 48-mode width (two passes of 24 modes) of the
-// single-analysis kernel and slower below it; the batched kernel in the same layout raised an
-// illegal-instruction fault on the GPU whose cause was not found, so no kernel is built with
-// it (use_regsplit is false).
+// single-analysis kernel and slower below it, so only that kernel uses it; the batched kernel
+// keeps the plain layout.
 template <bool RS>
 struct ELayout {
     static constexpr int threads = RS ? 512 : 448;
@@ -46,7 +45,7 @@ struct ELayout {
 constexpr int kRegsEpi = 152, kRegsProd = 40;
 static_assert(kEpi * kRegsEpi + (ELayout<true>::threads - kEpi) * kRegsProd <= ELayout<true>::threads * 128,
               "register split above the registers the block is launched with");
-constexpr bool use_regsplit(int /*NMT*/, int /*JH*/) { return false; }
+constexpr bool use_regsplit(int NMT, int JH) { return JH == 2 && NMT == 24; }
 
 __device__ __forceinline__ void regs_producer() { asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;" ::"n"(kRegsProd)); }
 __device__ __forceinline__ void regs_epilogue() { asm volatile("setmaxnreg.inc.sync.aligned.u32 %0;" ::"n"(kRegsEpi)); }
