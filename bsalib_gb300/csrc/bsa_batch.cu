@@ -384,7 +384,7 @@ __global__ void k_batch_reduce(const CaseP *__restrict__ cases, const long long 
 // columns q >= p, once per mode half) of bsa_classic_e.cu's pipeline, whose three epilogue
 // warpgroups add the six contributions of each E(f_p, f_q) element into the case's
 // accumulators [9 kinds][W][Mp].  Only the U and G tables are read (no S table).
-template <int NMT, int JH, bool RS = false>
+template <int NMT, int JH, bool RS = ecls::use_regsplit(NMT, JH)>
 __global__ void __launch_bounds__(ecls::ELayout<RS>::threads, 1)  // 128 registers a thread at launch
     k_bfm_e_batch(const __grid_constant__ CUtensorMap tmUh, const __grid_constant__ CUtensorMap tmUl,
                   const __grid_constant__ CUtensorMap tmGh, const __grid_constant__ CUtensorMap tmGl, const BParams p) {
@@ -922,22 +922,28 @@ int Engine::batch_run(double *m3mf, double *m3mr, double *m2mr, double *case_ms,
             cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             kern<<<grid, 192, smem, stream>>>(maps[0], maps[1], maps[2], maps[3], maps[4], maps[5], prm);
         };
-        // the batched E-form kernel runs in the plain warp layout (ecls::ELayout<false>)
-        auto launch_e = [&](auto kern, size_t ut) {  // UTile bytes ut: fits with the stages (static_assert in bsa_classic_e.cu)
+        // the warp layout of each instantiation (register split for the 48-mode width) is its
+        // template default; a split kernel is launched only at its full launch registers
+        auto launch_e = [&](auto kern, size_t ut, bool rs) -> bool {  // UTile bytes ut: fits with the stages (static_assert in bsa_classic_e.cu)
             const size_t sm = (size_t)ecls::kStages * ecls::kStageBytes + 1024 + ecls::kBarBytes + 2 * ut;
             cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-            kern<<<grid, ecls::ELayout<false>::threads, sm, stream>>>(maps[0], maps[1], maps[2], maps[3], prm);
+            if (rs && ecls::regsplit_check(kern) != cudaSuccess) return false;
+            kern<<<grid, rs ? ecls::ELayout<true>::threads : ecls::ELayout<false>::threads, sm, stream>>>(
+                maps[0], maps[1], maps[2], maps[3], prm);
+            return true;
         };
+        bool launched = true;
         if (eform) {
             switch (NMT * 10 + JH) {
-            case 81: launch_e(k_bfm_e_batch<8, 1>, sizeof(ecls::UTile<8, 1>)); break;
-            case 82: launch_e(k_bfm_e_batch<8, 2>, sizeof(ecls::UTile<8, 2>)); break;
-            case 122: launch_e(k_bfm_e_batch<12, 2>, sizeof(ecls::UTile<12, 2>)); break;
-            case 161: launch_e(k_bfm_e_batch<16, 1>, sizeof(ecls::UTile<16, 1>)); break;
-            case 162: launch_e(k_bfm_e_batch<16, 2>, sizeof(ecls::UTile<16, 2>)); break;
-            case 241: launch_e(k_bfm_e_batch<24, 1>, sizeof(ecls::UTile<24, 1>)); break;
-            default: launch_e(k_bfm_e_batch<24, 2>, sizeof(ecls::UTile<24, 2>)); break;
+            case 81: launched = launch_e(k_bfm_e_batch<8, 1>, sizeof(ecls::UTile<8, 1>), ecls::use_regsplit(8, 1)); break;
+            case 82: launched = launch_e(k_bfm_e_batch<8, 2>, sizeof(ecls::UTile<8, 2>), ecls::use_regsplit(8, 2)); break;
+            case 122: launched = launch_e(k_bfm_e_batch<12, 2>, sizeof(ecls::UTile<12, 2>), ecls::use_regsplit(12, 2)); break;
+            case 161: launched = launch_e(k_bfm_e_batch<16, 1>, sizeof(ecls::UTile<16, 1>), ecls::use_regsplit(16, 1)); break;
+            case 162: launched = launch_e(k_bfm_e_batch<16, 2>, sizeof(ecls::UTile<16, 2>), ecls::use_regsplit(16, 2)); break;
+            case 241: launched = launch_e(k_bfm_e_batch<24, 1>, sizeof(ecls::UTile<24, 1>), ecls::use_regsplit(24, 1)); break;
+            default: launched = launch_e(k_bfm_e_batch<24, 2>, sizeof(ecls::UTile<24, 2>), ecls::use_regsplit(24, 2)); break;
             }
+            if (!launched) return fail(BSA_ERR_STATE, "batched E-form kernel: launch registers below its register split");
         } else {
             switch (Wd) {
             case 8: launch(k_bfm_batch<8, 1, true>); break;

@@ -35,8 +35,8 @@ constexpr int kEpi = 384;  // three epilogue warpgroups
 // and two idle warps; launched at 128 registers a thread, the producer warpgroup keeps 40 and
 // the epilogue warpgroups take 152 (setmaxnreg): 384 x 152 + 128 x 40 = 63 488 of the launch's
 // 65 536.  Measured 17 % faster for the 48-mode width (two passes of 24 modes) of the
-// single-analysis kernel and slower below it, so only that kernel uses it; the batched kernel
-// keeps the plain layout.
+// single-analysis kernel and slower below it, so the 48-mode kernels (single analysis and
+// batched) use it and the others keep the plain layout.
 template <bool RS>
 struct ELayout {
     static constexpr int threads = RS ? 512 : 448;
