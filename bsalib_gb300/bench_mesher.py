@@ -3,6 +3,7 @@ times (also the command the committed ncu summaries under profiles/ were taken w
 
   python -m bsalib_gb300.bench_mesher [--structure bridge|building|tower] [--nodes N]
                                         [--modes M] [--precision bf16x3|fp64] [--steps 2]
+                                        [--max-zones N] [--synthetic N]
 
 Prints the zone and lattice-point counts and, per run, the library statistics and the
 response-bispectrum (BRM lattice) points per second.
@@ -35,6 +36,8 @@ def main():
     ap.add_argument("--zones-only", action="store_true")
     ap.add_argument("--synthetic", type=int, default=0,
                     help="evaluate this many seeded synthetic zones (problem.synthetic_zones) instead of the layout")
+    ap.add_argument("--max-zones", type=int, default=0,
+                    help="evaluate only the first N zones of the layout (a small case of the same zones)")
     ap.add_argument("--controls", default="driver", choices=["driver", "library"],
                     help="Mesher controls: the standalone driver's (default) or the library's")
     a = ap.parse_args()
@@ -50,6 +53,8 @@ def main():
             zs = synthetic_zones(prob, a.synthetic)
         else:
             zs = s.generate_zones()
+            if a.max_zones:
+                zs = zs[:a.max_zones]
         nbfm = sum(z.ni * z.nj for z in zs)
         nbrm = sum(((z.ni - 1) * z.Fi + 1) * ((z.nj - 1) * z.Fj + 1) for z in zs)
         print(f"{a.structure}: {prob.nnl} nodes, {s.nmodes()} modes, {len(zs)} zones, "
@@ -58,7 +63,7 @@ def main():
             return
         for _ in range(a.steps):
             t0 = time.perf_counter()
-            if a.synthetic:
+            if a.synthetic or a.max_zones:
                 s.msh_zones(zs)
             else:
                 s.run()

@@ -424,12 +424,29 @@ constexpr int kVY = 64;      // staged (j', mode) pairs per point
 constexpr int kWin = 776;    // corner window (floats): 3 x 256 elements + alignment slack
 constexpr int kHrow = 194;   // FRF row capacity (float2): frf_row(64)
 
-// s + c += x, compensated (Neumaier): the zone sums are added in FP32 with their rounding
-// errors carried, so no FP64 arithmetic (slow on GB300) runs in the moment pass.
-__device__ __forceinline__ void csum(float &s, float &c, float x) {
-    const float t = s + x;
-    c += fabsf(s) >= fabsf(x) ? (s - t) + x : (x - t) + s;
-    s = t;
+// Two FP32 lanes in one 64-bit register.  The paired FP32 instructions of sm_100 and later
+// (fma.rn.f32x2, mul.rn.f32x2) run both lanes from one issue slot, each lane rounded as the
+// scalar fma.rn / mul.rn would round it.
+using f2x = unsigned long long;
+__device__ __forceinline__ f2x pk2(float lo, float hi) {
+    f2x r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ float2 up2(f2x v) {
+    float2 r;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(v));
+    return r;
+}
+__device__ __forceinline__ f2x fma2(f2x a, f2x b, f2x c) {
+    f2x d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+__device__ __forceinline__ f2x mul2(f2x a, f2x b) {
+    f2x d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
 }
 
 // Bulk copy global -> shared (16-byte aligned, size a multiple of 16), completing on bar.
@@ -471,6 +488,10 @@ struct MomLayout {
 struct MomItem {
     int z, loc, q0, nb, nq, nqj, qi0, qj0, rowq, nj;  // rowq: BRM points per zone lattice row
     int valid, zend;                                  // zend: the zone's last item of this block
+    // corner staging: the cell's left corner column (i0, j0), (i0 + 1, j0) is in slot cl of
+    // the corner windows, its right column in slot 1 - cl; reuse: the left column is the
+    // previous cell's right column, still staged (the next cell of a zone row)
+    int cl, reuse;
     long long qbase, P00;
     float wp[4];  // BFM lattice trapezoid weights of the corners the cell owns
     float rFi, rFj;
@@ -496,6 +517,8 @@ __device__ __forceinline__ void mom_fill(const ZoneM *__restrict__ zones, int z,
     it.nj = nj;
     it.valid = 1;
     it.zend = 0;
+    it.cl = 0;
+    it.reuse = 0;
     it.qbase = Z.qbase;
     it.P00 = (long long)Z.pbase + (long long)i0 * nj + j0;
     const int ci[4] = {i0, i0, i0 + 1, i0 + 1}, cj[4] = {j0, j0 + 1, j0, j0 + 1};
@@ -541,8 +564,9 @@ __device__ __forceinline__ void mom_seek(const ZoneM *__restrict__ zones, int nz
 // (mom_first).  Each BRM point belongs to the cell (min(qi/Fi, ni-2), min(qj/Fj, nj-2)) and
 // each BFM point to the cell (min(i, ni-2), min(j, nj-2)), so every lattice point is counted
 // once.  part[g][6][nm^3]: m3mf of T1, T3, T2, then m3mr of T1, T3, T2.  A zone's cells are
-// summed in FP32 and the zone sums added with compensation, so each zone's share depends on that
-// zone alone and the result is the same, to ~1e-13, for any zone order.
+// summed in FP32 registers and each zone sum added in FP64 to the thread's own elements of
+// part (a read-modify-write in global memory once per zone, no atomics), so each zone's share
+// depends on that zone alone and the result is the same, to ~1e-13, for any zone order.
 //
 // The FRF products factor through per-point vectors staged in shared memory: with w the
 // point's weight, V_j'(a) = w H1(a) conj H3(j'), Y_j'(b) = w H1(j') H2(b),
@@ -551,12 +575,19 @@ __device__ __forceinline__ void mom_seek(const ZoneM *__restrict__ zones, int nz
 //   T2: Re[H1(j') H2(a) conj H3(b)] w = Re[Y_j'(a) conj H3(b)]
 // and the bilinear interpolation of each term over the cell is c0 + ti (c2 - c0) + tj (c1 - c0)
 // + ti tj (c0 - c1 - c2 + c3), its coefficients formed once per cell.  The b-indexed values are
-// read once per point for the thread's EPT elements.
+// read once per point for the thread's EPT elements.  The arithmetic runs on FP32 pairs: T1
+// and T2 of one element share every step (V, Y staged as {Vr, Yr, Vi, Yi}, H2, H3 as {H2r,
+// H3r, -H2i, H3i}, so {T1, T2} = {H2r, H3r} (.) {Vr, Yr} + {-H2i, H3i} (.) {Vi, Yi}), and T3
+// runs on pairs of elements; 32 instead of 54 FP32 instructions per point for 3 elements.
 //
-// Pipeline: thread 0 builds the work items and issues bulk copies (one mbarrier phase per
-// item): the FRF rows of the next item's points (one copy per lattice-row segment) and, at a
-// cell's first item, the block's element window of the 4 corners x 3 terms.  They land while
-// the current item computes.  The waits are bounded (err code 5 on timeout).
+// Pipeline: thread 32 builds the work items and thread 0 issues bulk copies (one mbarrier
+// phase per item): the FRF rows of the next item's points (one copy per lattice-row segment)
+// and, at a cell's first item, the block's element window of the corners x 3 terms.  The
+// windows sit in two column slots: the next cell of a zone row finds its left corner column
+// staged as the previous cell's right one and copies only its right column, so each BFM
+// point's window is copied about twice (once per cell row it bounds) instead of four times.
+// The copies land while the current item computes.  The waits are bounded (err code 5 on
+// timeout).
 __global__ __launch_bounds__(256, 2) void k_msh_moments(int nm, int nm3p, MomLayout L, const ZoneM *__restrict__ zones,
                                                         int nz, const float *__restrict__ T1,
                                                         const float *__restrict__ T3, const float *__restrict__ T2,
@@ -564,13 +595,16 @@ __global__ __launch_bounds__(256, 2) void k_msh_moments(int nm, int nm3p, MomLay
                                                         int *__restrict__ err) {
     constexpr int EPT = kMomEPT;
     extern __shared__ __align__(16) unsigned char msm[];
-    float4(*VY)[kVY] = reinterpret_cast<float4(*)[kVY]>(msm);                            // {V_j'(m), Y_j'(m)}
-    float4(*H23)[64] = reinterpret_cast<float4(*)[64]>(msm + kQB * kVY * 16);            // {H2(m), H3(m)}
+    float4(*VY)[kVY] = reinterpret_cast<float4(*)[kVY]>(msm);                            // {Vr, Yr, Vi, Yi}
+    float4(*H23)[64] = reinterpret_cast<float4(*)[64]>(msm + kQB * kVY * 16);            // {H2r, H3r, -H2i, H3i}
     float2 *Hraw = reinterpret_cast<float2 *>(msm + kQB * kVY * 16 + kQB * 64 * 16);     // [kQB][hs]
-    float *Cs = reinterpret_cast<float *>(Hraw + kQB * kHrow);                           // [12][kWin]
+    float *Cs = reinterpret_cast<float *>(Hraw + kQB * kHrow);                           // [2][2][3][kWin]
     uint64_t *bar = reinterpret_cast<uint64_t *>(Cs + 12 * kWin);
-    __shared__ float2 tq[kQB];  // (ti, tj)
-    __shared__ MomItem sit[2];  // the current and the next item
+    const ulonglong2(*VYp)[kVY] = reinterpret_cast<const ulonglong2(*)[kVY]>(msm);      // the same, as pairs
+    const ulonglong2(*H23p)[64] = reinterpret_cast<const ulonglong2(*)[64]>(msm + kQB * kVY * 16);
+    __shared__ ulonglong2 tq[kQB];  // {ti, ti}, {tj, tj}
+    __shared__ f2x tq2[kQB];        // {ti tj, ti tj}
+    __shared__ MomItem sit[3];      // the current item and the two after it
     const int nm2 = nm * nm, nm3 = nm2 * nm, tid = threadIdx.x, hs = frf_row(nm);
     const int grp = blockIdx.y / L.nchj, chunk = blockIdx.y % L.nchj;
     const int jg0 = grp * L.JB, njb = min(L.JB, nm - jg0), per_j = L.AR * nm;
@@ -608,73 +642,124 @@ __global__ __launch_bounds__(256, 2) void k_msh_moments(int nm, int nm3p, MomLay
     const bool svy = sjl < njb;
     const float *Ts[3] = {T1, T3, T2};
 
-    // thread 0: the copies of item it (one mbarrier phase)
-    auto issue = [&](const MomItem &it) {
-        uint32_t bytes = 0;
-        {
-            int qq = it.q0;
-            const int qe = it.q0 + it.nb;
-            while (qq < qe) {
-                const int qr = qq / it.nqj, qc = qq - qr * it.nqj, n = min(it.nqj - qc, qe - qq);
-                bytes += (uint32_t)n * hs * 8;
-                qq += n;
+    // corner window of slot s (column), row r (0: i0, 1: i0 + 1), term t
+    auto cwin = [&](int s, int r, int t) { return Cs + ((s * 2 + r) * 3 + t) * kWin; };
+    // warp 0: the copies of item it (one mbarrier phase) spread over its lanes: lane l < 16 the
+    // FRF rows of the item's points on BRM lattice row r0 + l of the cell (at most 16 rows),
+    // lanes 20-31 at a cell's first item the corner window (column, row, term) = lane - 20;
+    // corner (r, c) of the cell is BFM point P00 + r nj + c
+    auto issue = [&](const MomItem &it, int lane) {
+        if (lane == 0) {
+            uint32_t bytes = (uint32_t)it.nb * hs * 8;
+            if (it.q0 == 0) bytes += (it.reuse ? 6u : 12u) * (uint32_t)wlen * 4;
+            mbar_expect_tx(bar, bytes);
+        }
+        __syncwarp();
+        if (lane < kQB) {
+            const int r0 = it.q0 / it.nqj, qr = r0 + lane;
+            const int qs = max(it.q0, qr * it.nqj), qn = min((qr + 1) * it.nqj, it.q0 + it.nb);
+            if (qs < qn) {
+                const size_t gq = (size_t)it.qbase + (size_t)(it.qi0 + qr) * it.rowq + (it.qj0 + qs - qr * it.nqj);
+                bulk_g2s(Hraw + (qs - it.q0) * hs, Hq + gq * hs, (uint32_t)(qn - qs) * hs * 8, bar);
             }
-        }
-        if (it.q0 == 0) bytes += 12u * (uint32_t)wlen * 4;
-        mbar_expect_tx(bar, bytes);
-        int qq = it.q0;
-        const int qe = it.q0 + it.nb;
-        while (qq < qe) {
-            const int qr = qq / it.nqj, qc = qq - qr * it.nqj, n = min(it.nqj - qc, qe - qq);
-            const size_t gq = (size_t)it.qbase + (size_t)(it.qi0 + qr) * it.rowq + (it.qj0 + qc);
-            bulk_g2s(Hraw + (qq - it.q0) * hs, Hq + gq * hs, (uint32_t)n * hs * 8, bar);
-            qq += n;
-        }
-        if (it.q0 == 0) {
-            const size_t P0 = (size_t)it.P00;
-            const size_t Pc[4] = {P0, P0 + 1, P0 + it.nj, P0 + it.nj + 1};
-            for (int t = 0; t < 3; ++t)
-                for (int k = 0; k < 4; ++k)
-                    bulk_g2s(Cs + (t * 4 + k) * kWin, Ts[t] + Pc[k] * nm3p + win0, (uint32_t)wlen * 4, bar);
+        } else if (lane >= 20 && it.q0 == 0) {
+            const int w = lane - 20, t = w >> 2, col = (w >> 1) & 1, r = w & 1;
+            if (col >= it.reuse)
+                bulk_g2s(cwin(col == 0 ? it.cl : 1 - it.cl, r, t),
+                         Ts[t] + (size_t)(it.P00 + (long long)r * it.nj + col) * nm3p + win0, (uint32_t)wlen * 4, bar);
         }
     };
+    // thread 32: nx = the item after p; p's zone ends with p when nx is in another zone
+    auto build = [&](MomItem &p, MomItem &nx) {
+        if (!p.valid) {
+            nx.valid = 0;
+            nx.z = nz;
+            return;
+        }
+        if (p.q0 + kQB < p.nq) {
+            mom_fill(zones, p.z, p.loc, p.q0 + kQB, nx);
+            nx.cl = p.cl;
+        } else {
+            mom_seek(zones, nz, gridDim.x, blockIdx.x, p.z, p.loc + gridDim.x, false, nx);
+            // the next cell of the zone row keeps this cell's right corner column
+            nx.reuse = nx.valid && nx.z == p.z && nx.loc == p.loc + 1 && nx.loc % (p.nj - 1) != 0;
+            nx.cl = nx.reuse ? 1 - p.cl : 0;
+        }
+        p.zend = nx.z != p.z;
+    };
 
-    float mf[EPT][3], mfe[EPT][3], mr[EPT][3], mre[EPT][3];  // compensated sums over zones
-    float cA[EPT][3], cB[EPT][3], cC[EPT][3], cD[EPT][3];    // the cell's bilinear coefficients
-    float zf[EPT][3], zr[EPT][3];                             // the zone's FP32 sums
+    static_assert(EPT == 2 || EPT == 3, "T3 runs on the element pair (0, 1), element 2 alone");
+    float zf[EPT][3];  // the zone's FP32 m3mf sums
+    // the cell's bilinear coefficients {A, B, C, D} and the zone's m3mr sums: {T1, T2} of each
+    // element as pairs, T3 of elements 0 and 1 as a pair, T3 of element 2 alone
+    f2x c12[EPT][4], z12[EPT], c3p[4], z3p;
+    float c3s[4], z3s;
+#pragma unroll
+    for (int u = 0; u < EPT; ++u) {
+        z12[u] = 0ull;
+#pragma unroll
+        for (int t = 0; t < 3; ++t) zf[u][t] = 0.f;
+    }
+    z3p = 0ull;
+    z3s = 0.f;
+    // the sums over zones: this thread's elements of the block column's partial
+    double *pg = part + (size_t)blockIdx.x * 6 * nm3 + ev0;
 #pragma unroll
     for (int u = 0; u < EPT; ++u)
+        if (u < nval)
 #pragma unroll
-        for (int t = 0; t < 3; ++t) mf[u][t] = mfe[u][t] = mr[u][t] = mre[u][t] = zf[u][t] = zr[u][t] = 0.f;
+            for (int t = 0; t < 6; ++t) pg[(size_t)t * nm3 + u * nm] = 0.0;
 
     if (tid == 0) {
         mbar_init(bar, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (tid == 32) {
         mom_seek(zones, nz, gridDim.x, blockIdx.x, 0, 0, true, sit[0]);
-        if (sit[0].valid) issue(sit[0]);
+        build(sit[0], sit[1]);
     }
     __syncthreads();
-    MomItem cur = sit[0];
+    if (tid < 32 && sit[0].valid) issue(sit[0], tid);
     bool ok = true;
-    for (int k = 0; cur.valid; ++k) {
+    // Item k sits in slot k % 3: built by thread 32 during item k - 2, its copies issued by
+    // warp 0 during item k - 1, its zone-end flag set when item k + 1 is built.
+    for (int k = 0; sit[k % 3].valid; ++k) {
+        const MomItem &cur = sit[k % 3];
         if (!mbar_wait(bar, (uint32_t)(k & 1), err, 5)) ok = false;
-        __syncthreads();  // every thread done with the previous item's VY, H23, tq and items
+        __syncthreads();  // every thread done with the previous item's VY, H23 and tq
+        const int nb = cur.nb;
+        const bool zend = cur.zend;
         if (cur.q0 == 0) {
+            // corner values c0..c3 of element u, term t -> {c0, c2 - c0, c1 - c0, c0 - c1 - c2 + c3}
+            const float *csl = cwin(cur.cl, 0, 0), *csr = cwin(1 - cur.cl, 0, 0);
+            auto coef = [&](int u, int t, float (&c)[4]) {
+                const int o = t * kWin + (u < nval ? wofs + u * nm : wofs);
+                const float c0 = csl[o], c1 = csr[o], c2 = csl[o + 3 * kWin], c3 = csr[o + 3 * kWin];
+                zf[u][t] += fmaf(cur.wp[3], c3, fmaf(cur.wp[2], c2, fmaf(cur.wp[1], c1, cur.wp[0] * c0)));
+                c[0] = c0;
+                c[1] = c2 - c0;
+                c[2] = c1 - c0;
+                c[3] = (c0 - c1) - (c2 - c3);
+            };
 #pragma unroll
-            for (int u = 0; u < EPT; ++u)
+            for (int u = 0; u < EPT; ++u) {
+                float a[4], b[4];
+                coef(u, 0, a);
+                coef(u, 2, b);
 #pragma unroll
-                for (int t = 0; t < 3; ++t) {
-                    const float *cs = Cs + (t * 4) * kWin + (u < nval ? wofs + u * nm : wofs);
-                    const float c0 = cs[0], c1 = cs[kWin], c2 = cs[2 * kWin], c3 = cs[3 * kWin];
-                    cA[u][t] = c0;
-                    cB[u][t] = c2 - c0;
-                    cC[u][t] = c1 - c0;
-                    cD[u][t] = (c0 - c1) - (c2 - c3);
-                    zf[u][t] += fmaf(cur.wp[3], c3, fmaf(cur.wp[2], c2, fmaf(cur.wp[1], c1, cur.wp[0] * c0)));
-                }
+                for (int c = 0; c < 4; ++c) c12[u][c] = pk2(a[c], b[c]);
+            }
+            {
+                float a[4], b[4];
+                coef(0, 1, a);
+                coef(1, 1, b);
+                if constexpr (EPT == 3) coef(2, 1, c3s);
+#pragma unroll
+                for (int c = 0; c < 4; ++c) c3p[c] = pk2(a[c], b[c]);
+            }
         }
         // FRF rows -> V, Y, H2, H3 of the item's points; (ti, tj)
-        for (int ql = sq0; ql < cur.nb; ql += 256 / kVY) {
+        for (int ql = sq0; ql < nb; ql += 256 / kVY) {
             const float2 *h = Hraw + ql * hs;
             if (svy) {
                 const float w = h[3 * nm].x;
@@ -682,73 +767,70 @@ __global__ __launch_bounds__(256, 2) void k_msh_moments(int nm, int nm3p, MomLay
                 const float2 h1 = h[sm], h2 = h[nm + sm];
                 const float2 h1j = h[jg], h3j = h[2 * nm + jg];
                 // V = w H1(m) conj H3(j'),  Y = w H1(j') H2(m)
-                VY[ql][st] = make_float4(w * (h1.x * h3j.x + h1.y * h3j.y), w * (h1.y * h3j.x - h1.x * h3j.y),
-                                         w * (h1j.x * h2.x - h1j.y * h2.y), w * (h1j.x * h2.y + h1j.y * h2.x));
+                VY[ql][st] = make_float4(w * (h1.x * h3j.x + h1.y * h3j.y), w * (h1j.x * h2.x - h1j.y * h2.y),
+                                         w * (h1.y * h3j.x - h1.x * h3j.y), w * (h1j.x * h2.y + h1j.y * h2.x));
             }
             if (st < nm) {
                 const float2 h2 = h[nm + st], h3 = h[2 * nm + st];
-                H23[ql][st] = make_float4(h2.x, h2.y, h3.x, h3.y);
+                H23[ql][st] = make_float4(h2.x, h3.x, -h2.y, h3.y);
             }
         }
-        if (tid < cur.nb) {
+        if (tid < nb) {
             const int qq = cur.q0 + tid, qr = qq / cur.nqj, qc = qq - qr * cur.nqj;
-            tq[tid] = make_float2((float)qr * cur.rFi, (float)qc * cur.rFj);
+            const float ti = (float)qr * cur.rFi, tj = (float)qc * cur.rFj;
+            tq[tid] = make_ulonglong2(pk2(ti, ti), pk2(tj, tj));
+            tq2[tid] = pk2(ti * tj, ti * tj);
         }
-        MomItem &nx = sit[(k + 1) & 1];
-        if (tid == 32) {
-            // the next item; cur's zone ends with it when nx is in another zone
-            if (cur.q0 + kQB < cur.nq)
-                mom_fill(zones, cur.z, cur.loc, cur.q0 + kQB, nx);
-            else
-                mom_seek(zones, nz, gridDim.x, blockIdx.x, cur.z, cur.loc + gridDim.x, false, nx);
-            sit[k & 1].zend = nx.z != cur.z;
-        }
-        // VY, H23, tq and the next item ready; FRF rows and corners consumed
+        // VY, H23 and tq ready; FRF rows and corners consumed, the item's fields read
         if (__syncthreads_or(!ok)) break;  // a copy did not arrive: leave with the error code set
-        const bool zend = sit[k & 1].zend;
-        const MomItem nxt = nx;
-        // the next item's copies run under this item's arithmetic
-        if (tid == 0 && nxt.valid) issue(nxt);
-        for (int ql = 0; ql < cur.nb; ++ql) {
-            const float2 tt = tq[ql];
-            const float ti = tt.x, tj = tt.y, tij = ti * tj;
-            const float4 hb = H23[ql][bb];                                         // H2(b), H3(b)
-            const float2 ybv = reinterpret_cast<const float2 *>(&VY[ql][yb])[1];  // Y_j'(b)
+        // the next item's copies and the item after it run under this item's arithmetic
+        MomItem &nxt = sit[(k + 1) % 3];
+        if (tid < 32 && nxt.valid) issue(nxt, tid);
+        if (tid == 32) build(nxt, sit[(k + 2) % 3]);
+        for (int ql = 0; ql < nb; ++ql) {
+            const ulonglong2 tt = tq[ql];
+            const f2x ti2 = tt.x, tj2 = tt.y, tij2 = tq2[ql];
+            const ulonglong2 hb = H23p[ql][bb];  // {H2r(b), H3r(b)}, {-H2i(b), H3i(b)}
+            const float4 ybv = VY[ql][yb];       // .y, .w: Y_j'(b)
+            float f3[EPT];
 #pragma unroll
             for (int u = 0; u < EPT; ++u) {
-                const float4 va = VY[ql][ia0 + u];                                          // V_j'(a), Y_j'(a)
-                const float2 h3a = reinterpret_cast<const float2 *>(&H23[ql][ih0 + u])[1];  // H3(a)
-                const float f1 = hb.x * va.x - hb.y * va.y;
-                const float f3 = ybv.x * h3a.x + ybv.y * h3a.y;
-                const float f2 = va.z * hb.z + va.w * hb.w;
-                const float fs[3] = {f1, f3, f2};
-#pragma unroll
-                for (int t = 0; t < 3; ++t) {
-                    const float v = fmaf(tij, cD[u][t], fmaf(tj, cC[u][t], fmaf(ti, cB[u][t], cA[u][t])));
-                    zr[u][t] = fmaf(fs[t], v, zr[u][t]);
+                const ulonglong2 va = VYp[ql][ia0 + u];  // {Vr(a), Yr(a)}, {Vi(a), Yi(a)}
+                const float4 h3a = H23[ql][ih0 + u];     // .y, .w: H3(a)
+                // {T1, T2} = {Re[H2(b) V_j'(a)], Re[Y_j'(a) conj H3(b)]}
+                const f2x f12 = fma2(hb.y, va.y, mul2(hb.x, va.x));
+                f3[u] = fmaf(ybv.w, h3a.w, ybv.y * h3a.y);  // T3 = Re[Y_j'(b) conj H3(a)]
+                const f2x v = fma2(tij2, c12[u][3], fma2(tj2, c12[u][2], fma2(ti2, c12[u][1], c12[u][0])));
+                z12[u] = fma2(f12, v, z12[u]);
+            }
+            {
+                const f2x v = fma2(tij2, c3p[3], fma2(tj2, c3p[2], fma2(ti2, c3p[1], c3p[0])));
+                z3p = fma2(pk2(f3[0], f3[1]), v, z3p);
+                if constexpr (EPT == 3) {
+                    const float ti = up2(ti2).x, tj = up2(tj2).x, tij = up2(tij2).x;
+                    const float vs = fmaf(tij, c3s[3], fmaf(tj, c3s[2], fmaf(ti, c3s[1], c3s[0])));
+                    z3s = fmaf(f3[EPT - 1], vs, z3s);
                 }
             }
         }
         if (zend) {
+            const float2 p3 = up2(z3p);
 #pragma unroll
-            for (int u = 0; u < EPT; ++u)
+            for (int u = 0; u < EPT; ++u) {
+                const float2 p12 = up2(z12[u]);
+                const float zr[3] = {p12.x, u == 0 ? p3.x : u == 1 ? p3.y : z3s, p12.y};
 #pragma unroll
                 for (int t = 0; t < 3; ++t) {
-                    csum(mf[u][t], mfe[u][t], zf[u][t]);
-                    csum(mr[u][t], mre[u][t], zr[u][t]);
-                    zf[u][t] = zr[u][t] = 0.f;
+                    if (u < nval) {
+                        pg[(size_t)t * nm3 + u * nm] += (double)zf[u][t];
+                        pg[(size_t)(3 + t) * nm3 + u * nm] += (double)zr[t];
+                    }
+                    zf[u][t] = 0.f;
                 }
-        }
-        cur = nxt;
-    }
-    double *pg = part + (size_t)blockIdx.x * 6 * nm3;
-#pragma unroll
-    for (int u = 0; u < EPT; ++u) {
-        if (u >= nval) continue;
-#pragma unroll
-        for (int t = 0; t < 3; ++t) {
-            pg[(size_t)t * nm3 + ev0 + u * nm] = (double)mf[u][t] + (double)mfe[u][t];
-            pg[(size_t)(3 + t) * nm3 + ev0 + u * nm] = (double)mr[u][t] + (double)mre[u][t];
+                z12[u] = 0ull;
+            }
+            z3p = 0ull;
+            z3s = 0.f;
         }
     }
 }
