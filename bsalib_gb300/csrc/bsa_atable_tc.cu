@@ -34,11 +34,12 @@ struct Layout {
     static constexpr int kBars = 2 * kStage;  // offset of the barrier block
 };
 
-__device__ __forceinline__ uint32_t tf32_rna(float x) {
-    uint32_t r;
-    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
-    return r;
-}
+// x rounded to tf32 (10 explicit mantissa bits), to nearest with ties away from zero, for
+// finite x: half the weight of the last kept bit is added to the sign-magnitude bit pattern
+// and the 13 dropped bits are cleared (a carry into the exponent is the correct rounding up).
+// Two integer ALU instructions in place of a conversion instruction, beside the ex2 of the
+// same element on the special-function pipe.
+__device__ __forceinline__ uint32_t tf32_rna(float x) { return (__float_as_uint(x) + 0x1000u) & 0xFFFFE000u; }
 
 // 128-byte swizzle: 16-byte chunk c of row r sits at chunk c ^ (r mod 8) of its 128-byte row.
 __device__ __forceinline__ uint32_t swz(int r, int c) { return (uint32_t)(r * 128 + ((c ^ (r & 7)) << 4)); }
@@ -85,7 +86,7 @@ __device__ __forceinline__ void cp_async16(uint32_t dst, const void *src) {
 // B tile: copied from the B tables (cp.async, one chunk ahead).  256 threads generate and copy,
 // thread 0 issues the MMAs, all eight warps drain TMEM.
 template <int N>
-__global__ void __launch_bounds__(kThreads) k_atable_tc(int ntc, int n, int nm, int MT, const double *__restrict__ f,
+__global__ void __launch_bounds__(kThreads, 2) k_atable_tc(int ntc, int n, int nm, int MT, const double *__restrict__ f,
                                                         const float *__restrict__ logc, const double *__restrict__ S,
                                                         const uint32_t *__restrict__ Bth,
                                                         const uint32_t *__restrict__ Btl, float *__restrict__ A,
@@ -169,13 +170,11 @@ __global__ void __launch_bounds__(kThreads) k_atable_tc(int ntc, int n, int nm, 
     load_chunk(0);
     copy_b(0, 0);
     bool ok = true;
+    // Chunk kc: its A tile is generated into stage s = kc & 1 (whose chunk kc - 2 MMAs were
+    // waited for one chunk ago) while the MMAs of chunk kc - 1 run; then, those MMAs done, the
+    // B tile of chunk kc + 1 is copied into stage s ^ 1 and chunk kc's MMAs are issued.
     for (int kc = 0; kc < nk; ++kc) {
         const int s = kc & 1;
-        // stage s^1 was read by the MMAs of chunk kc - 1: free before the next chunk's B copy
-        if (kc >= 1 && ok) ok = mbar_wait(&freeb[s ^ 1], (uint32_t)((kc - 1) >> 1) & 1u, err, 11);
-        ok = __syncthreads_and(ok);
-        if (!ok) break;
-        if (kc + 1 < nk) copy_b(kc + 1, s ^ 1);
         uint8_t *Ah = smem + s * LY::kStage, *Al = Ah + kATile;
         const int j0 = kc * kKc;
 #pragma unroll
@@ -197,13 +196,17 @@ __global__ void __launch_bounds__(kThreads) k_atable_tc(int ntc, int n, int nm, 
             *(uint4 *)(Al + swz(r, c)) = make_uint4(l[0], l[1], l[2], l[3]);
         }
         if (kc + 1 < nk) load_chunk(j0 + kKc);
-        // this chunk's B copy (issued one chunk ago, or above for chunk 0) has landed
-        if (kc + 1 < nk)
+        // stage s ^ 1 was read by the MMAs of chunk kc - 1: free before the next chunk's B copy
+        if (kc >= 1 && ok) ok = mbar_wait(&freeb[s ^ 1], (uint32_t)((kc - 1) >> 1) & 1u, err, 11);
+        if (kc + 1 < nk && ok) copy_b(kc + 1, s ^ 1);
+        // this chunk's B copy (issued one chunk ago, or before the loop for chunk 0) has landed
+        if (kc + 1 < nk && ok)
             asm volatile("cp.async.wait_group 1;" ::: "memory");
         else
             asm volatile("cp.async.wait_group 0;" ::: "memory");
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // generic and cp.async writes -> MMA reads
-        __syncthreads();
+        ok = __syncthreads_and(ok);
+        if (!ok) break;
         if (tid == 0) {
             fence_after();
             uint8_t *Bh = Al + kATile, *Bl = Bh + LY::kBTile;
