@@ -7,10 +7,11 @@
 // 32-wide j chunk straight into shared memory (128-byte swizzled, K-major, the layout the MMA
 // descriptors name) split as tf32 hi + lo (hi = the value rounded to tf32, lo = the rounded
 // remainder), the B tile (L, split the same way once per call, f-independent) arrives by
-// cp.async one chunk ahead, and one thread issues hi*hi + hi*lo + lo*hi tcgen05 MMAs into an
-// FP32 TMEM accumulator (two stages, mbarrier-ordered).  The split keeps ~21 bits of each
-// product; c^|f| comes from ex2.approx (relative error ~2^-22).  The epilogue scales row i by
-// s_i.  Every mbarrier wait is bounded (error flag).
+// cp.async one chunk ahead, and one thread issues per K step hi x [B hi | B lo] (one MMA of
+// twice the mode width) and lo x B hi into FP32 TMEM accumulators (two stages, mbarrier-
+// ordered); the epilogue adds the hi x lo columns and scales row i by s_i.  The split keeps
+// ~21 bits of each product; c^|f| comes from ex2.approx (relative error ~2^-22).  Every
+// mbarrier wait is bounded (error flag).
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -116,7 +117,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_atable_tc(int ntc, int n, int n
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(su32(tmem_slot)), "r"(N)
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(su32(tmem_slot)), "r"(2 * N)
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
@@ -211,12 +212,14 @@ __global__ void __launch_bounds__(kThreads, 2) k_atable_tc(int ntc, int n, int n
             fence_after();
             uint8_t *Bh = Al + kATile, *Bl = Bh + LY::kBTile;
             const uint32_t ah = su32(Ah), al = su32(Al), bh = su32(Bh), bl = su32(Bl);
+            // hi x [B hi | B lo] (the lo tile follows the hi tile: one B operand of 2N rows) into
+            // columns [0, 2N), then lo x B hi into [0, N): A hi is read once per K step
+            (void)bl;
 #pragma unroll
             for (int ks = 0; ks < kKc / 8; ++ks) {  // K = 8 per tf32 MMA: 32 bytes of each row
                 const uint32_t off = ks * 32;
                 const uint32_t acc = (kc > 0 || ks > 0) ? 1u : 0u;
-                mma_tf32<N>(tmem, sdesc(ah + off), sdesc(bh + off), acc);
-                mma_tf32<N>(tmem, sdesc(ah + off), sdesc(bl + off), 1u);
+                mma_tf32<2 * N>(tmem, sdesc(ah + off), sdesc(bh + off), acc);
                 mma_tf32<N>(tmem, sdesc(al + off), sdesc(bh + off), 1u);
             }
             mma_commit(&freeb[s]);
@@ -230,8 +233,9 @@ __global__ void __launch_bounds__(kThreads, 2) k_atable_tc(int ntc, int n, int n
         // warps w and w + 4 read TMEM lanes 32 (w mod 4) .., columns 32 (w div 4) ..
         const int r = (warp & 3) * 32 + lane, gi = i0 + r, q = warp >> 2;
         const uint32_t taddr = tmem + ((uint32_t)((warp & 3) * 32) << 16) + q * 32;
-        uint32_t v[32];
-        tmem_ld32(taddr, v);
+        uint32_t v[32], w[32];
+        tmem_ld32(taddr, v);      // hi x hi + lo x hi
+        tmem_ld32(taddr + N, w);  // hi x lo
         tmem_wait_ld();
         if (gi < n) {
             float *out = A + (((size_t)fi * ntc + itc) * n + gi) * nm;
@@ -239,14 +243,14 @@ __global__ void __launch_bounds__(kThreads, 2) k_atable_tc(int ntc, int n, int n
 #pragma unroll
             for (int e = 0; e < 32; ++e) {
                 const int m = q * 32 + e;
-                if (m < nm) out[m] = si * __uint_as_float(v[e]);
+                if (m < nm) out[m] = si * (__uint_as_float(v[e]) + __uint_as_float(w[e]));
             }
         }
     }
     fence_before();
     __syncthreads();
     fence_after();
-    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(N) : "memory");
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * N) : "memory");
 }
 
 template <int N>
