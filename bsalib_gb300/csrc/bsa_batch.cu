@@ -531,11 +531,11 @@ __global__ void __launch_bounds__(ecls::ELayout<RS>::threads, 1)  // 128 registe
         using UT = UTile<NMT, JH>;
         UT *hbs = (UT *)(smem + ecls::kStages * ecls::kStageBytes + ecls::kBarBytes);
         const int k0 = wg * kKindsWG;
-        float acc[kKindsWG][NMT];
+        f2x acc[kKindsWG][NMT / 2];  // modes j, j + 1 as FP32 lane pairs
 #pragma unroll
         for (int k = 0; k < kKindsWG; ++k)
 #pragma unroll
-            for (int j = 0; j < NMT; ++j) acc[k][j] = 0.f;
+            for (int j = 0; j < NMT / 2; ++j) acc[k][j] = 0ull;
         // FRF staging of unit u of item im
         auto stage = [&](UT *dst, const BItem &im, int u) {
             const CaseP c = p.cases[im.c];
@@ -596,10 +596,12 @@ __global__ void __launch_bounds__(ecls::ELayout<RS>::threads, 1)  // 128 registe
 #pragma unroll
                     for (int k = 0; k < kKindsWG; ++k)
 #pragma unroll
-                        for (int j = 0; j < NMT; ++j) {
-                            if (vrow && acc[k][j] != 0.f)
-                                atomicAdd(part + (size_t)((k0 + k) * W + jh * NMT + j) * Mp, (double)acc[k][j]);
-                            acc[k][j] = 0.f;
+                        for (int j = 0; j < NMT / 2; ++j) {
+                            const float2 s2 = up2(acc[k][j]);
+                            double *pk = part + (size_t)((k0 + k) * W + jh * NMT + 2 * j) * Mp;
+                            if (vrow && s2.x != 0.f) atomicAdd(pk, (double)s2.x);
+                            if (vrow && s2.y != 0.f) atomicAdd(pk + Mp, (double)s2.y);
+                            acc[k][j] = 0ull;
                         }
                     since = 0;
                 }
@@ -874,7 +876,7 @@ int Engine::batch_run(double *m3mf, double *m3mr, double *m2mr, double *case_ms,
             const float *A = dA32.as<float>();
             if ((e = mixed::prep_u(stream, nf, c.nme, c.K, Kp, q.Mp, A, dQ.as<double>(), Uh + (size_t)q.u_row0 * Kp,
                                    Ul + (size_t)q.u_row0 * Kp)) ||
-                (e = mixed::prep_h(stream, nf, c.nme, Wd, dFreq.as<double>(), frf(), Hg + q.hg0, Hs + q.hs0)))
+                (e = mixed::prep_h(stream, nf, c.nme, Wd, dFreq.as<double>(), frf(), Hg + q.hg0, Hs + q.hs0, eform)))
                 return cuda_fail(e, "batch operand preparation");
             for (int jh = 0; jh < JH; ++jh) {
                 const size_t og = ((size_t)q.g_row0 + (size_t)jh * nf * NMT) * Kp;

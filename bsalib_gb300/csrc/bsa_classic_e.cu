@@ -208,11 +208,11 @@ __global__ void __launch_bounds__(ELayout<RS>::threads, 1)  // 128 registers a t
         double *part = P.part + (size_t)blockIdx.x * kKinds * W * 128 + row;
         const int k0 = wg * kKindsWG;
         for (int k = 0; k < kKindsWG * W; ++k) part[(size_t)(k0 * W + k) * 128] = 0.0;
-        float acc[kKindsWG][NMT];
+        f2x acc[kKindsWG][NMT / 2];  // modes j, j + 1 as FP32 lane pairs
 #pragma unroll
         for (int k = 0; k < kKindsWG; ++k)
 #pragma unroll
-            for (int j = 0; j < NMT; ++j) acc[k][j] = 0.f;
+            for (int j = 0; j < NMT / 2; ++j) acc[k][j] = 0ull;
         uint32_t tile = 0;
         bool ok = true;
         int since = 0;
@@ -256,11 +256,12 @@ __global__ void __launch_bounds__(ELayout<RS>::threads, 1)  // 128 registers a t
 #pragma unroll
                             for (int k = 0; k < kKindsWG; ++k)
 #pragma unroll
-                                for (int j = 0; j < NMT; ++j) {
-                                    if (acc[k][j] != 0.f)
-                                        atomicAdd(part + (size_t)((k0 + k) * W + jh * NMT + j) * 128,
-                                                  (double)acc[k][j]);
-                                    acc[k][j] = 0.f;
+                                for (int j = 0; j < NMT / 2; ++j) {
+                                    const float2 s2 = up2(acc[k][j]);
+                                    double *pk = part + (size_t)((k0 + k) * W + jh * NMT + 2 * j) * 128;
+                                    if (s2.x != 0.f) atomicAdd(pk, (double)s2.x);
+                                    if (s2.y != 0.f) atomicAdd(pk + 128, (double)s2.y);
+                                    acc[k][j] = 0ull;
                                 }
                             since = 0;
                         }
@@ -356,7 +357,7 @@ int Engine::contract_e(const PointSrc &ps, double *m3mf, double *m3mr, const ESa
     {
         const float *A = dA32.as<float>();
         if ((e = mixed::prep_u(stream, nf, nm, K, Kp, Mp, A, dQ.as<double>(), Uh, Ul)) ||
-            (e = mixed::prep_h(stream, nf, nm, W, ps.fgrid, frf(), Hg, Hs)))
+            (e = mixed::prep_h(stream, nf, nm, W, ps.fgrid, frf(), Hg, Hs, true)))
             return cuda_fail(e, "BF16x3 operand preparation");
         for (int jh = 0; jh < JH; ++jh) {  // G rows of mode half jh at jh nf NMT
             const size_t og = (size_t)jh * nf * NMT * Kp;

@@ -104,6 +104,20 @@ __device__ __forceinline__ float2 lds2(const float2 *p) {
     return r;
 }
 
+// The FRF rows of the E form are in the mode-pair layout (prep_h with pairs): the 16 bytes of
+// modes 2i, 2i + 1 hold {Re H_2i, Re H_2i+1, Im H_2i, Im H_2i+1}.  ldc: mode m as a complex
+// value; lds_pair: modes m, m + 1 (m even) as the lane pairs {Re, Re} and {Im, Im}, one 16-byte
+// shared load the compiler does not hoist.
+__device__ __forceinline__ float2 ldc(const float2 *row, int m) {
+    const float *r = reinterpret_cast<const float *>(row) + 4 * (m >> 1) + (m & 1);
+    return make_float2(r[0], r[2]);
+}
+__device__ __forceinline__ ulonglong2 lds_pair(const float2 *row, int m) {
+    ulonglong2 r;
+    asm volatile("ld.shared.v2.u64 {%0, %1}, [%2];" : "=l"(r.x), "=l"(r.y) : "r"(su32(row + m)));
+    return r;
+}
+
 __device__ __forceinline__ void epi_sync384() { asm volatile("bar.sync 1, 384;" ::: "memory"); }
 
 // Units of grid row p: pairs of N tiles from the one holding column p (columns q < p masked).
@@ -169,19 +183,20 @@ __device__ __forceinline__ void stage_unit(UTile<NMT, JH> *dst, const EParams &P
 template <int NMT, int JH = 1>
 __device__ __forceinline__ void unit_half(const UTile<NMT, JH> &hb, uint32_t taddr, int wg, int a, int b, int p,
                                           int q0, int slot0, const EParams &P, bool vect, float wv,
-                                          float (&acc)[kKindsWG][NMT], int jo = 0) {
+                                          f2x (&acc)[kKindsWG][NMT / 2], int jo = 0) {
+    static_assert(NMT % 2 == 0, "modes in lane pairs");
     constexpr int NC = kBN / NMT, W = NMT * JH;
-    const float2 hra = hb.hr[a];
+    const float2 hra = ldc(hb.hr, a);
 #pragma unroll
     for (int qc = 0; qc < kBN / 16; ++qc) {
         uint32_t v[16];
         tmem_ld16(taddr + qc * 16, v);
         tmem_wait_ld();
-        float2 P1 = make_float2(0.f, 0.f), P2 = P1;
-        float wk = 0.f;
+        // the column's factors as lane pairs: {Re P, Re P}, {-Im P, -Im P}, {w, w}
+        f2x p1r = 0ull, p1i = 0ull, p2r = 0ull, p2i = 0ull, wk2 = 0ull;
         const float2 *X = hb.hr, *Y = hb.hr;  // per-mode factors of the two response kinds
 #pragma unroll
-        for (int e = 0; e < 16; ++e) {
+        for (int e = 0; e < 16; e += 2) {  // two modes j, j + 1 of one column (NMT and 16 even)
             const int col = qc * 16 + e;
             const int ci = col / NMT, j = col % NMT;
             if (ci >= NC) continue;
@@ -191,37 +206,42 @@ __device__ __forceinline__ void unit_half(const UTile<NMT, JH> &hb, uint32_t tad
                 const bool valid = q >= p && q < P.nf;
                 const bool vd = valid && q - p <= P.h;
                 const float dl = q == p ? 0.5f : 1.f;
-                const float2 Hbv = hb.hg[sl + b], Hav = hb.hg[sl + a];
+                const float2 Hbv = ldc(hb.hg + sl, b), Hav = ldc(hb.hg + sl, a);
                 float2 t1, t2;
+                float wk;
                 if (wg == 0) {
                     wk = valid ? dl * wpt(p, q, P.nf, vect, wv) : 0.f;
                     t1 = conjf2(cmul(hra, Hbv));               // conj: pairs with conj H_j(u+v)
-                    t2 = cmul(Hav, conjf2(hb.hs[sl + b]));
+                    t2 = cmul(Hav, conjf2(ldc(hb.hs + sl, b)));
                     X = hb.hs + sl;
                     Y = hb.hr;
                 } else if (wg == 1) {
                     wk = vd ? dl * wpt(p, q - p + P.h, P.nf, vect, wv) : 0.f;
-                    t1 = cmul(hb.hdp[sl + b], conjf2(Hav));
+                    t1 = cmul(ldc(hb.hdp + sl, b), conjf2(Hav));
                     t2 = cmul(hra, conjf2(Hbv));
                     X = hb.hr;
                     Y = hb.hdp + sl;
                 } else {
                     wk = vd ? dl * wpt(p - q + P.h, q, P.nf, vect, wv) : 0.f;
-                    t1 = conjf2(cmul(hb.hdm[sl + b], Hav));    // conj: pairs with conj H_j(u)
+                    t1 = conjf2(cmul(ldc(hb.hdm + sl, b), Hav));    // conj: pairs with conj H_j(u)
                     t2 = cmul(Hbv, conjf2(hra));
                     X = hb.hr;
                     Y = hb.hdm + sl;
                 }
-                X += jo;  // this pass's half of the modes j
+                X += jo;  // this pass's half of the modes j (jo even)
                 Y += jo;
-                P1 = make_float2(wk * t1.x, wk * t1.y);
-                P2 = make_float2(wk * t2.x, wk * t2.y);
+                p1r = pk2(wk * t1.x, wk * t1.x);
+                p1i = pk2(-wk * t1.y, -wk * t1.y);
+                p2r = pk2(wk * t2.x, wk * t2.x);
+                p2i = pk2(-wk * t2.y, -wk * t2.y);
+                wk2 = pk2(wk, wk);
             }
-            const float x = __uint_as_float(v[e]);
-            const float2 xj = lds2(X + j), yj = lds2(Y + j);
-            acc[0][j] = fmaf(P1.x * xj.x - P1.y * xj.y, x, acc[0][j]);  // Re[P1 X_j]
-            acc[1][j] = fmaf(P2.x * yj.x - P2.y * yj.y, x, acc[1][j]);  // Re[P2 Y_j]
-            acc[2][j] = fmaf(wk, x, acc[2][j]);
+            const f2x x2 = pk2(__uint_as_float(v[e]), __uint_as_float(v[e + 1]));
+            const ulonglong2 xq = lds_pair(X, j), yq = lds_pair(Y, j);
+            // Re[P1 X_j] x and Re[P2 Y_j] x for modes j, j + 1
+            acc[0][j >> 1] = fma2(fma2(p1i, xq.y, mul2(p1r, xq.x)), x2, acc[0][j >> 1]);
+            acc[1][j >> 1] = fma2(fma2(p2i, yq.y, mul2(p2r, yq.x)), x2, acc[1][j >> 1]);
+            acc[2][j >> 1] = fma2(wk2, x2, acc[2][j >> 1]);
         }
     }
 }
@@ -240,7 +260,7 @@ __device__ __forceinline__ void unit_half_sample(const UTile<NMT, JH> &hb, uint3
     constexpr int NC = kBN / NMT, W = NMT * JH;
     const int nm = P.nm, nm2 = nm * nm;
     const size_t nm3 = (size_t)nm2 * nm;
-    const float2 hra = hb.hr[a];
+    const float2 hra = ldc(hb.hr, a);
 #pragma unroll 1
     for (int qc = 0; qc < kBN / 16; ++qc) {
         uint32_t v[16];
@@ -256,32 +276,32 @@ __device__ __forceinline__ void unit_half_sample(const UTile<NMT, JH> &hb, uint3
             const bool valid = q >= p && q < P.nf;
             if (!(wg == 0 ? valid : (valid && q - p <= P.h))) continue;
             const int sl = (slot0 + ci) * W;
-            const float2 Hbv = hb.hg[sl + b], Hav = hb.hg[sl + a];
+            const float2 Hbv = ldc(hb.hg + sl, b), Hav = ldc(hb.hg + sl, a);
             int i1a, i2a, i1b, i2b, ia, ib;
             float2 t1, t2, xj, yj;
             if (wg == 0) {
                 i1a = p, i2a = q, ia = a + nm * b + nm2 * jg;
                 i1b = q, i2b = p, ib = a + nm * jg + nm2 * b;
                 t1 = conjf2(cmul(hra, Hbv));
-                t2 = cmul(Hav, conjf2(hb.hs[sl + b]));
-                xj = hb.hs[sl + jg];
-                yj = hb.hr[jg];
+                t2 = cmul(Hav, conjf2(ldc(hb.hs + sl, b)));
+                xj = ldc(hb.hs + sl, jg);
+                yj = ldc(hb.hr, jg);
             } else if (wg == 1) {
                 const int c = q - p + P.h;
                 i1a = p, i2a = c, ia = jg + nm * b + nm2 * a;
                 i1b = c, i2b = p, ib = jg + nm * a + nm2 * b;
-                t1 = cmul(hb.hdp[sl + b], conjf2(Hav));
+                t1 = cmul(ldc(hb.hdp + sl, b), conjf2(Hav));
                 t2 = cmul(hra, conjf2(Hbv));
-                xj = hb.hr[jg];
-                yj = hb.hdp[sl + jg];
+                xj = ldc(hb.hr, jg);
+                yj = ldc(hb.hdp + sl, jg);
             } else {
                 const int d = p - q + P.h;
                 i1a = d, i2a = q, ia = b + nm * a + nm2 * jg;
                 i1b = q, i2b = d, ib = b + nm * jg + nm2 * a;
-                t1 = conjf2(cmul(hb.hdm[sl + b], Hav));
+                t1 = conjf2(cmul(ldc(hb.hdm + sl, b), Hav));
                 t2 = cmul(Hbv, conjf2(hra));
-                xj = hb.hr[jg];
-                yj = hb.hdm[sl + jg];
+                xj = ldc(hb.hr, jg);
+                yj = ldc(hb.hdm + sl, jg);
             }
             const float x = __uint_as_float(v[e]);
             const double f = (q == p ? 1.0 : 2.0) * (double)x;  // 2 x, half weight on the diagonal

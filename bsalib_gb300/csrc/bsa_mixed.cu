@@ -430,21 +430,29 @@ __global__ void k_prep_b(int nm, int NMT, int j0, int K, int Kp, int nf, int n_p
 }
 
 // FRF tables in FP64, rounded once to FP32: Hg[c][j] = H_j(w_c), Hs[s][j] = H_j(w_r + w_c).
+// Complex values in mode order, or with pairs (even NMT) in mode pairs: the 16 bytes of modes
+// 2i, 2i + 1 hold {Re H_2i, Re H_2i+1, Im H_2i, Im H_2i+1}, so one 16-byte load gives two
+// modes' real parts and imaginary parts as FP32 lane pairs.
 __global__ void k_prep_h(int nf, int nm, int NMT, const double *__restrict__ f, FrfPar frf, float2 *__restrict__ Hg,
-                         float2 *__restrict__ Hs) {
+                         float2 *__restrict__ Hs, int pairs) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int ng = nf * NMT, ns = (2 * nf - 1) * NMT;
-    if (t < ng) {
-        const int c = t / NMT, j = t % NMT;
-        double hr = 0, hi = 0;
-        if (j < nm) frf_eval(frf.M[j], frf.K[j], frf.C[j], f[c] * kPi2, hr, hi);
-        Hg[t] = make_float2((float)hr, (float)hi);
-    } else if (t < ng + ns) {
-        const int u = t - ng, s = u / NMT, j = u % NMT;
-        const int r = s / 2, c = s - r;
-        double hr = 0, hi = 0;
-        if (j < nm) frf_eval(frf.M[j], frf.K[j], frf.C[j], f[r] * kPi2 + f[c] * kPi2, hr, hi);
-        Hs[u] = make_float2((float)hr, (float)hi);
+    if (t >= ng + ns) return;
+    const bool g = t < ng;
+    const int u = g ? t : t - ng, row = u / NMT, j = u % NMT;
+    double hr = 0, hi = 0;
+    if (j < nm) {
+        const int r = row / 2, c = row - r;
+        const double w = g ? f[row] * kPi2 : f[r] * kPi2 + f[c] * kPi2;
+        frf_eval(frf.M[j], frf.K[j], frf.C[j], w, hr, hi);
+    }
+    float2 *tab = g ? Hg : Hs;
+    if (pairs) {
+        float *rf = reinterpret_cast<float *>(tab + (size_t)row * NMT) + 4 * (j >> 1) + (j & 1);
+        rf[0] = (float)hr;
+        rf[2] = (float)hi;
+    } else {
+        tab[u] = make_float2((float)hr, (float)hi);
     }
 }
 
@@ -484,9 +492,10 @@ cudaError_t prep_b(cudaStream_t st, int rows, int nm, int NMT, int j0, int K, in
     return cudaGetLastError();
 }
 
-cudaError_t prep_h(cudaStream_t st, int nf, int nm, int NMT, const double *f, FrfPar frf, float2 *Hg, float2 *Hs) {
+cudaError_t prep_h(cudaStream_t st, int nf, int nm, int NMT, const double *f, FrfPar frf, float2 *Hg, float2 *Hs,
+                   bool pairs) {
     const int nh = (nf + 2 * nf - 1) * NMT;
-    k_prep_h<<<(nh + 255) / 256, 256, 0, st>>>(nf, nm, NMT, f, frf, Hg, Hs);
+    k_prep_h<<<(nh + 255) / 256, 256, 0, st>>>(nf, nm, NMT, f, frf, Hg, Hs, pairs ? 1 : 0);
     return cudaGetLastError();
 }
 
@@ -560,7 +569,7 @@ int Engine::contract_mixed(const PointSrc &ps, long long npts, double *m3mf, dou
                                              Sh + os, Sl + os);
         }
         const int nh = (nf + ns) * W;
-        k_prep_h<<<(nh + 255) / 256, 256, 0, stream>>>(nf, nm, W, ps.fgrid, frf(), Hg, Hs);
+        k_prep_h<<<(nh + 255) / 256, 256, 0, stream>>>(nf, nm, W, ps.fgrid, frf(), Hg, Hs, 0);
         if ((e = cudaGetLastError())) return cuda_fail(e, "BF16x3 operand preparation");
         kernels += 2 + 2 * JH;
     }

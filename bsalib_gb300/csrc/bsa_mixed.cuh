@@ -16,8 +16,10 @@ cudaError_t prep_u(cudaStream_t st, int nf, int nm, int K, int Kp, int Mp, const
 // NMT <= 32
 cudaError_t prep_b(cudaStream_t st, int rows, int nm, int NMT, int j0, int K, int Kp, int nf, int n_pad, int trunc,
                    int sum_base, int is_sum, const float *A, __nv_bfloat16 *Th, __nv_bfloat16 *Tl);
-// FRF tables Hg[c][j] = H_j(w_c), Hs[s][j] = H_j(w_r + w_c), s = r + c < 2 nf - 1
-cudaError_t prep_h(cudaStream_t st, int nf, int nm, int NMT, const double *f, FrfPar frf, float2 *Hg, float2 *Hs);
+// FRF tables Hg[c][j] = H_j(w_c), Hs[s][j] = H_j(w_r + w_c), s = r + c < 2 nf - 1; pairs:
+// each 16 bytes hold modes 2i, 2i + 1 as {Re, Re, Im, Im} (the E form's layout, even NMT)
+cudaError_t prep_h(cudaStream_t st, int nf, int nm, int NMT, const double *f, FrfPar frf, float2 *Hg, float2 *Hs,
+                   bool pairs = false);
 
 }  // namespace mixed
 }  // namespace bsa

@@ -424,31 +424,6 @@ constexpr int kVY = 64;      // staged (j', mode) pairs per point
 constexpr int kWin = 776;    // corner window (floats): 3 x 256 elements + alignment slack
 constexpr int kHrow = 194;   // FRF row capacity (float2): frf_row(64)
 
-// Two FP32 lanes in one 64-bit register.  The paired FP32 instructions of sm_100 and later
-// (fma.rn.f32x2, mul.rn.f32x2) run both lanes from one issue slot, each lane rounded as the
-// scalar fma.rn / mul.rn would round it.
-using f2x = unsigned long long;
-__device__ __forceinline__ f2x pk2(float lo, float hi) {
-    f2x r;
-    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
-    return r;
-}
-__device__ __forceinline__ float2 up2(f2x v) {
-    float2 r;
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(v));
-    return r;
-}
-__device__ __forceinline__ f2x fma2(f2x a, f2x b, f2x c) {
-    f2x d;
-    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
-    return d;
-}
-__device__ __forceinline__ f2x mul2(f2x a, f2x b) {
-    f2x d;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-    return d;
-}
-
 // Bulk copy global -> shared (16-byte aligned, size a multiple of 16), completing on bar.
 __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
     asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
