@@ -210,11 +210,9 @@ __global__ void __launch_bounds__(kThreads, 2) k_atable_tc(int ntc, int n, int n
         if (!ok) break;
         if (tid == 0) {
             fence_after();
-            uint8_t *Bh = Al + kATile, *Bl = Bh + LY::kBTile;
-            const uint32_t ah = su32(Ah), al = su32(Al), bh = su32(Bh), bl = su32(Bl);
+            const uint32_t ah = su32(Ah), al = su32(Al), bh = su32(Al + kATile);
             // hi x [B hi | B lo] (the lo tile follows the hi tile: one B operand of 2N rows) into
             // columns [0, 2N), then lo x B hi into [0, N): A hi is read once per K step
-            (void)bl;
 #pragma unroll
             for (int ks = 0; ks < kKc / 8; ++ks) {  // K = 8 per tf32 MMA: 32 bytes of each row
                 const uint32_t off = ks * 32;
