@@ -178,7 +178,7 @@ struct Engine {
     int build_atable(const std::vector<double> &freqs, bool fp32 = false, bool msh = false);
     int pod_atable(const std::vector<double> &freqs, bool fp32);
     int build_psd(const std::vector<double> &freqs);
-    int build_psd_dev(int nf);                 // the nf frequencies already in dFreq
+    int build_psd_dev(int nf, bool fp32 = false);  // the nf frequencies already in dFreq
     int build_atable_dev(int nf, bool fp32);   // the same, A table (not the truncated POD form)
     // dimM_psd_ / dimM_bisp_ (src/bsa/BsaLibImpl.F90:313-355): nm / nm for the diagonal-only
     // spectra, nm^2 / nm^3 otherwise.

@@ -353,13 +353,14 @@ int Engine::build_psd(const std::vector<double> &freqs) {
     return build_psd_dev((int)freqs.size());
 }
 
-// Nodal PSD table S[f][k] for the nf frequencies already in dFreq.
-int Engine::build_psd_dev(int nf) {
+// Nodal PSD table S[f][k] for the nf frequencies already in dFreq (fp32: the formulas
+// evaluated in FP32, for the split-precision A tables).
+int Engine::build_psd_dev(int nf, bool fp32) {
     const int ntc = (int)set.tc.size();
     cudaError_t e;
     if ((e = dS.reserve(sizeof(double) * (size_t)nf * ntc * in.nnl))) return cuda_fail(e, "allocating S");
     if ((e = launch_nodal_psd(stream, nf, dFreq.as<double>(), ntc, set.tc.data(), in.nnl, dPsdPar.as<PsdNode>(),
-                              in.psd_type, set.defsc, dS.as<double>())))
+                              in.psd_type, set.defsc, dS.as<double>(), fp32)))
         return cuda_fail(e, "nodal PSD kernel");
     kernels += 1;
     return BSA_OK;
@@ -377,7 +378,7 @@ int Engine::build_atable(const std::vector<double> &freqs, bool fp32, bool msh) 
 int Engine::build_atable_dev(int nf, bool fp32) {
     const int ntc = (int)set.tc.size();
     cudaError_t e;
-    int rc = build_psd_dev(nf);
+    int rc = build_psd_dev(nf, fp32);
     if (rc) return rc;
     if (fp32) {
         // FP32 table on the tensor cores (tf32 hi/lo split, FP32-level accuracy)

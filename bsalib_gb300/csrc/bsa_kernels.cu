@@ -12,8 +12,11 @@ namespace bsa {
 // stores are coalesced.  Model formulas: vonKarmanPSD_ (WindPSDImpl.F90:149-226, u form
 // for tc == 1, v/w form otherwise), kaimalPSD_ (:231-243, identically zero),
 // davenportPSD_Greisch_ (:249-277), davenportPSD_Uliege_ (:283-316); divided by 4 pi
-// under the circular-frequency convention (:142-143).
+// under the circular-frequency convention (:142-143).  R = double for the FP64 paths; the
+// split-precision paths, whose A(f) tables take sqrt(S) in FP32, evaluate the same formulas
+// in FP32 (R = float: relative error ~1e-7, where FP64's pow costs ~100 FP64 instructions).
 // ------------------------------------------------------------------------------------
+template <typename R>
 __global__ void k_nodal_psd(int nf, const double *__restrict__ f, int ntc, int4 tcs, int nnl,
                             const PsdNode *__restrict__ par, int psd_type, int scaling,
                             double *__restrict__ S) {
@@ -26,54 +29,57 @@ __global__ void k_nodal_psd(int nf, const double *__restrict__ f, int ntc, int4 
     const int fi = (int)(r / ntc);
     const int tc = itc == 0 ? tcs.x : (itc == 1 ? tcs.y : tcs.z);
     const PsdNode p = par[itc * nnl + i];
-    const double fr = f[fi];
-    const double sig2 = p.sigma * p.sigma;
-    double v = 0.0;
+    const R fr = (R)f[fi], Ls = (R)p.Ls, U = (R)p.U, Uref = (R)p.Uref, sg = (R)p.sigma;
+    const R sig2 = sg * sg;
+    R v = 0;
     switch (psd_type) {
     case 1:
         if (tc == 1) {
-            const double rt = p.Ls / p.U;
-            double x = fabs(fr) * rt;
+            const R rt = Ls / U;
+            R x = fabs(fr) * rt;
             x = x * x;
-            x = pow(1.0 + 70.7 * x, 5.0 / 6.0);
-            v = 4.0 * (rt * sig2) / x;
+            x = pow(R(1) + R(70.7) * x, R(5.0 / 6.0));
+            v = R(4) * (rt * sig2) / x;
         } else {
-            double d = 2.0 * (fr * (p.Ls / p.U));
+            R d = R(2) * (fr * (Ls / U));
             d = d * d;
-            const double r2 = pow(1.0 + 70.7 * d, 11.0 / 6.0) * p.U;
-            const double r3 = p.Ls * (1.0 + 188.4 * d) / r2 * sig2;
-            const double a = r3 + r3;
+            const R r2 = pow(R(1) + R(70.7) * d, R(11.0 / 6.0)) * U;
+            const R r3 = Ls * (R(1) + R(188.4) * d) / r2 * sig2;
+            const R a = r3 + r3;
             v = a + a;
         }
         break;
     case 2:
-        v = 0.0;
+        v = 0;
         break;
     case 3: {
-        const double cst1 = 0.65 * 1200.0;
-        const double x = cst1 * fr / p.Uref;
-        v = cst1 * sig2 / p.Uref / pow(1.0 + x * x, 5.0 / 6.0);
+        const R cst1 = R(0.65 * 1200.0);
+        const R x = cst1 * fr / Uref;
+        v = cst1 * sig2 / Uref / pow(R(1) + x * x, R(5.0 / 6.0));
     } break;
     case 5: {
-        const double clu = p.Ls / p.U;
-        const double cf = fabs(fr) * clu;
-        v = ((2.0 / 3.0) * cf * clu * sig2) / pow(1.0 + cf * cf, 4.0 / 3.0);
+        const R clu = Ls / U;
+        const R cf = fabs(fr) * clu;
+        v = ((R(2.0 / 3.0)) * cf * clu * sig2) / pow(R(1) + cf * cf, R(4.0 / 3.0));
     } break;
     default:
-        v = 0.0;
+        v = 0;
     }
-    if (scaling == 1) v = v / kPi4;
-    S[t] = v;
+    if (scaling == 1) v = v / R(kPi4);
+    S[t] = (double)v;
 }
 
 cudaError_t launch_nodal_psd(cudaStream_t st, int nf, const double *f, int ntc, const int *tcs_host,
-                             int nnl, const PsdNode *par, int psd_type, int scaling, double *S) {
+                             int nnl, const PsdNode *par, int psd_type, int scaling, double *S, bool fp32) {
     const long long tot = (long long)nf * ntc * nnl;
     if (tot == 0) return cudaSuccess;
     int4 tcs = make_int4(tcs_host[0], ntc > 1 ? tcs_host[1] : 0, ntc > 2 ? tcs_host[2] : 0, 0);
     const int blk = 256;
-    k_nodal_psd<<<(unsigned)((tot + blk - 1) / blk), blk, 0, st>>>(nf, f, ntc, tcs, nnl, par, psd_type,
-                                                                    scaling, S);
+    const unsigned grid = (unsigned)((tot + blk - 1) / blk);
+    if (fp32)
+        k_nodal_psd<float><<<grid, blk, 0, st>>>(nf, f, ntc, tcs, nnl, par, psd_type, scaling, S);
+    else
+        k_nodal_psd<double><<<grid, blk, 0, st>>>(nf, f, ntc, tcs, nnl, par, psd_type, scaling, S);
     return cudaGetLastError();
 }
 

@@ -7,7 +7,7 @@ namespace bsa {
 // Nodal PSD S[f][itc][i] for nf frequencies (evalPSD_ and the model functions,
 // src/wind/WindPSDImpl.F90:123-316).  tcs: turbulent component ids (1..3) per itc.
 cudaError_t launch_nodal_psd(cudaStream_t st, int nf, const double *f, int ntc, const int *tcs_host,
-                             int nnl, const PsdNode *par, int psd_type, int scaling, double *S);
+                             int nnl, const PsdNode *par, int psd_type, int scaling, double *S, bool fp32 = false);
 
 // A[f][k][m] = sqrt(S_i(f)) sum_j c_ij^|f| sqrt(S_j(f)) L[(itc,j)][m]  (FP64).
 // lc[x] = log(lc[x]) in place (FP64) and lc32[x] = (float)lc[x]: the coherence table log c.
