@@ -555,9 +555,11 @@ __device__ __forceinline__ void mom_seek(const ZoneM *__restrict__ zones, int nz
 // H3r, -H2i, H3i}, so {T1, T2} = {H2r, H3r} (.) {Vr, Yr} + {-H2i, H3i} (.) {Vi, Yi}), and T3
 // runs on pairs of elements; 32 instead of 54 FP32 instructions per point for 3 elements.
 //
-// Pipeline: thread 32 builds the work items and thread 0 issues bulk copies (one mbarrier
-// phase per item): the FRF rows of the next item's points (one copy per lattice-row segment)
-// and, at a cell's first item, the block's element window of the corners x 3 terms.  The
+// Pipeline: thread 32 builds each work item two items ahead and warp 0 issues its bulk copies
+// one item ahead (one mbarrier phase per item, the copies spread over the warp's lanes): the
+// FRF rows of the item's points (one copy per lattice-row segment) and, at a cell's first
+// item, the block's element window of the corners x 3 terms.  Both run after the item's
+// second block barrier, beside the other warps' arithmetic.  The
 // windows sit in two column slots: the next cell of a zone row finds its left corner column
 // staged as the previous cell's right one and copies only its right column, so each BFM
 // point's window is copied about twice (once per cell row it bounds) instead of four times.
