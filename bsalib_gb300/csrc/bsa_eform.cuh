@@ -187,20 +187,21 @@ __device__ __forceinline__ void unit_half(const UTile<NMT, JH> &hb, uint32_t tad
     static_assert(NMT % 2 == 0, "modes in lane pairs");
     constexpr int NC = kBN / NMT, W = NMT * JH;
     const float2 hra = ldc(hb.hr, a);
+    // the current column's factors as lane pairs: {Re P, Re P}, {-Im P, -Im P}, {w, w}; a
+    // column that runs on into the next 16-column TMEM load keeps them (the loops unroll)
+    f2x p1r = 0ull, p1i = 0ull, p2r = 0ull, p2i = 0ull, wk2 = 0ull;
+    const float2 *X = hb.hr, *Y = hb.hr;  // per-mode factors of the two response kinds
 #pragma unroll
     for (int qc = 0; qc < kBN / 16; ++qc) {
         uint32_t v[16];
         tmem_ld16(taddr + qc * 16, v);
         tmem_wait_ld();
-        // the column's factors as lane pairs: {Re P, Re P}, {-Im P, -Im P}, {w, w}
-        f2x p1r = 0ull, p1i = 0ull, p2r = 0ull, p2i = 0ull, wk2 = 0ull;
-        const float2 *X = hb.hr, *Y = hb.hr;  // per-mode factors of the two response kinds
 #pragma unroll
         for (int e = 0; e < 16; e += 2) {  // two modes j, j + 1 of one column (NMT and 16 even)
             const int col = qc * 16 + e;
             const int ci = col / NMT, j = col % NMT;
             if (ci >= NC) continue;
-            if (j == 0 || e == 0) {
+            if (j == 0) {
                 const int sl = (slot0 + ci) * W;
                 const int q = q0 + slot0 + ci;
                 const bool valid = q >= p && q < P.nf;
