@@ -544,6 +544,8 @@ __global__ void __launch_bounds__(ecls::ELayout<RS>::threads, 1)  // 128 registe
             ep.h = (c.nf - 1) / 2;
             ep.Hg = p.Hg + c.hg0;
             ep.Hs = p.Hs + c.hs0;
+            ep.wmode = c.wmode;
+            ep.wval = c.wval;
             stage_unit<NMT, JH>(dst, ep, im.r, im.r / NC + 2 * u, et, kEpi);
         };
         uint32_t tile = 0;
@@ -557,12 +559,7 @@ __global__ void __launch_bounds__(ecls::ELayout<RS>::threads, 1)  // 128 registe
             const int nm = csp->nm;
             const bool vrow = grow < nm * nm;
             const int a = vrow ? grow / nm : 0, b = vrow ? grow % nm : 0;
-            const float wv = (float)csp->wval;
-            const bool vect = csp->wmode == kWeightClassicVect;
-            EParams ep{};
-            ep.nf = csp->nf;
-            ep.h = (ep.nf - 1) / 2;
-            const int nu = n_units(r, csp->n_ntiles, NC), nt0 = r / NC;
+            const int nu = n_units(r, csp->n_ntiles, NC);
             int since = 0;
             for (int jh = 0; jh < JH; ++jh)
             for (int u = 0; u < nu; ++u, ++tile) {
@@ -581,10 +578,8 @@ __global__ void __launch_bounds__(ecls::ELayout<RS>::threads, 1)  // 128 registe
                 if (!ok) continue;
                 fence_after();
                 const UT &hb = hbs[buf];
-                const int q0 = (nt0 + 2 * u) * NC;
                 for (int h2 = 0; h2 < 2; ++h2)
-                    unit_half<NMT, JH>(hb, lane_base + buf * 256 + h2 * 128, wg, a, b, r, q0, h2 * NC, ep, vect, wv, acc,
-                                       jh * NMT);
+                    unit_half<NMT, JH>(hb, lane_base + buf * 256 + h2 * 128, wg, a, b, h2 * NC, acc, jh * NMT);
                 fence_before();
                 mbar_arrive(&tempty[buf]);
                 since += 2;

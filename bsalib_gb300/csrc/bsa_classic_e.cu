@@ -201,8 +201,6 @@ __global__ void __launch_bounds__(ELayout<RS>::threads, 1)  // 128 registers a t
         const bool vrow = grow < P.nm * P.nm;
         const int a = vrow ? grow / P.nm : 0, b = vrow ? grow % P.nm : 0;
         const uint32_t lane_base = tmem + ((uint32_t)(quarter * 32) << 16);
-        const float wv = (float)P.wval;
-        const bool vect = P.wmode == kWeightClassicVect;
         using UT = UTile<NMT, JH>;
         UT *hbs = (UT *)(smem + kStages * kStageBytes + kBarBytes);
         double *part = P.part + (size_t)blockIdx.x * kKinds * W * 128 + row;
@@ -243,8 +241,8 @@ __global__ void __launch_bounds__(ELayout<RS>::threads, 1)  // 128 registers a t
                                 unit_half_sample<NMT, JH>(hb, lane_base + buf * 256 + h2 * 128, wg, a, b, p, q0,
                                                           h2 * NC, P, jh * NMT, vrow);
                             else
-                                unit_half<NMT, JH>(hb, lane_base + buf * 256 + h2 * 128, wg, a, b, p, q0, h2 * NC, P,
-                                                   vect, wv, acc, jh * NMT);
+                                unit_half<NMT, JH>(hb, lane_base + buf * 256 + h2 * 128, wg, a, b, h2 * NC, acc,
+                                                   jh * NMT);
                         }
                         fence_before();
                         mbar_arrive(&tempty[buf]);

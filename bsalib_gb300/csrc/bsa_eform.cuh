@@ -66,15 +66,20 @@ inline cudaError_t regsplit_check(K kern) {
 // column H_j(v), H_j(u + v), H_j(v - u), H_j(u - v), all W = NMT x JH modes (above 24 kept
 // modes the G rows hold one half of NMT modes at a time, JH = 2, and every unit is swept
 // once per half; the row modes a, b of a TMEM lane range over all W).
+// Two of these sit back to back in shared memory and both take 16-byte copies and loads, so the
+// size is a multiple of 16 bytes (the weights alone are not, for 24 modes a pass).
 template <int NMT, int JH = 1>
-struct UTile {
+struct alignas(16) UTile {
     static constexpr int NC2 = 2 * (kBN / NMT), W = NMT * JH;
     float2 hr[W];
     float2 hg[NC2 * W];
     float2 hs[NC2 * W];
     float2 hdp[NC2 * W];
     float2 hdm[NC2 * W];
+    float wk[3][NC2];  // per warpgroup the integration weight of each column's target point
 };
+static_assert(sizeof(UTile<24, 2>) % 16 == 0 && sizeof(UTile<24, 1>) % 16 == 0 && sizeof(UTile<12, 2>) % 16 == 0,
+              "staging tiles 16-byte multiples");
 
 struct EParams {
     int nf, h, nm, Mp, MT, nk, ks_last, n_ntiles;
@@ -169,11 +174,27 @@ __device__ __forceinline__ void stage_unit(UTile<NMT, JH> *dst, const EParams &P
         epi::cp_async16(d + cc * W + 2 * k, v ? (const void *)(tab + (size_t)row * W + 2 * k) : (const void *)tab,
                         v);
     }
+    // the weights (zero where a contribution does not exist), the same for every TMEM lane:
+    //   wg 0: w(p, q);  wg 1: w(p, c), f_c = f_q - f_p;  wg 2: w(d, q), f_d = f_p - f_q;  half on q = p
+    if (t < 3 * NC2) {
+        const int wg = t / NC2, cc = t - wg * NC2, q = q0 + cc;
+        const bool vect = P.wmode == kWeightClassicVect, valid = q >= p && q < P.nf, vd = valid && q - p <= P.h;
+        const float wv = (float)P.wval, dl = q == p ? 0.5f : 1.f;
+        float w;
+        if (wg == 0)
+            w = valid ? dl * wpt(p, q, P.nf, vect, wv) : 0.f;
+        else if (wg == 1)
+            w = vd ? dl * wpt(p, q - p + P.h, P.nf, vect, wv) : 0.f;
+        else
+            w = vd ? dl * wpt(p - q + P.h, q, P.nf, vect, wv) : 0.f;
+        dst->wk[wg][cc] = w;
+    }
     epi::cp_async_commit();
 }
 
-// One N tile of a unit (TMEM columns taddr .. taddr + 127): grid columns q = q0 + slot0 + ci,
-// staged at column slot slot0 + ci.  Warpgroup wg accumulates kinds 3 wg .. 3 wg + 2:
+// One N tile of a unit (TMEM columns taddr .. taddr + 127): the unit's grid columns staged at
+// column slots slot0 + ci, with their weights (stage_unit).  Warpgroup wg accumulates kinds
+// 3 wg .. 3 wg + 2:
 //   wg 0: (i)   Re[w_pq H_a(u) H_b(v) conj H_j(u+v)],   (iv) Re[w_pq H_a(v) conj H_b(u+v) H_j(u)],   w_pq
 //   wg 1: (iii) Re[w_pc H_b(v-u) conj H_a(v) H_j(u)],   (v)  Re[w_pc H_a(u) conj H_b(v) H_j(v-u)],   w_pc
 //   wg 2: (ii)  Re[w_dq H_b(u-v) H_a(v) conj H_j(u)],   (vi) Re[w_dq H_b(v) conj H_a(u) H_j(u-v)],   w_dq
@@ -181,9 +202,8 @@ __device__ __forceinline__ void stage_unit(UTile<NMT, JH> *dst, const EParams &P
 // staged rows; a conj on H_j is folded into the factor), so the three warpgroups share one
 // instruction stream.
 template <int NMT, int JH = 1>
-__device__ __forceinline__ void unit_half(const UTile<NMT, JH> &hb, uint32_t taddr, int wg, int a, int b, int p,
-                                          int q0, int slot0, const EParams &P, bool vect, float wv,
-                                          f2x (&acc)[kKindsWG][NMT / 2], int jo = 0) {
+__device__ __forceinline__ void unit_half(const UTile<NMT, JH> &hb, uint32_t taddr, int wg, int a, int b,
+                                          int slot0, f2x (&acc)[kKindsWG][NMT / 2], int jo = 0) {
     static_assert(NMT % 2 == 0, "modes in lane pairs");
     constexpr int NC = kBN / NMT, W = NMT * JH;
     const float2 hra = ldc(hb.hr, a);
@@ -203,27 +223,20 @@ __device__ __forceinline__ void unit_half(const UTile<NMT, JH> &hb, uint32_t tad
             if (ci >= NC) continue;
             if (j == 0) {
                 const int sl = (slot0 + ci) * W;
-                const int q = q0 + slot0 + ci;
-                const bool valid = q >= p && q < P.nf;
-                const bool vd = valid && q - p <= P.h;
-                const float dl = q == p ? 0.5f : 1.f;
+                const float wk = hb.wk[wg][slot0 + ci];
                 const float2 Hbv = ldc(hb.hg + sl, b), Hav = ldc(hb.hg + sl, a);
                 float2 t1, t2;
-                float wk;
                 if (wg == 0) {
-                    wk = valid ? dl * wpt(p, q, P.nf, vect, wv) : 0.f;
                     t1 = conjf2(cmul(hra, Hbv));               // conj: pairs with conj H_j(u+v)
                     t2 = cmul(Hav, conjf2(ldc(hb.hs + sl, b)));
                     X = hb.hs + sl;
                     Y = hb.hr;
                 } else if (wg == 1) {
-                    wk = vd ? dl * wpt(p, q - p + P.h, P.nf, vect, wv) : 0.f;
                     t1 = cmul(ldc(hb.hdp + sl, b), conjf2(Hav));
                     t2 = cmul(hra, conjf2(Hbv));
                     X = hb.hr;
                     Y = hb.hdp + sl;
                 } else {
-                    wk = vd ? dl * wpt(p - q + P.h, q, P.nf, vect, wv) : 0.f;
                     t1 = conjf2(cmul(ldc(hb.hdm + sl, b), Hav));    // conj: pairs with conj H_j(u)
                     t2 = cmul(Hbv, conjf2(hra));
                     X = hb.hr;
